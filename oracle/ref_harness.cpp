@@ -1,0 +1,343 @@
+// Test-only harness around the reference's own solver classes (EFIE, CFIE,
+// MLFMA of xiangwei0909/EMFA).  It is compiled together with the reference
+// sources by oracle/build_ref.sh and dumps what those classes compute, in
+// binary, so tests can pin the oracle restatement and the GPU path to the
+// reference itself.  Nothing in the product links or runs this file.
+//
+//   emfa_ref_<f32|f64> rwg   <config> <outdir>
+//   emfa_ref_<f32|f64> efie  <config> <outdir> <gmres_tol>
+//   emfa_ref_<f32|f64> cfie  <config> <outdir> <bicgstab_tol>
+//   emfa_ref_<f32|f64> mlfma <config> <outdir> <seed>
+//   emfa_ref_<f32|f64> time  <config> <efie|cfie> <rows> <solve:0|1>
+//
+// The harness calls the same member functions EFIE::solve (EFIE.cpp:54-99),
+// CFIE::solve (CFIE.cpp:53-88) and MLFMA::solve (MLFMA.cpp:67-106) call, in
+// the same order, and reads the members they fill.
+#include "Custom.h"
+#include <thread>
+#include <mutex>
+#include <condition_variable>
+#include <functional>
+#include <queue>
+#include <atomic>
+#include <chrono>
+#include <list>
+#include <unordered_map>
+#include <random>
+#include <cstdio>
+#include <cstring>
+#include <experimental/filesystem>
+#include "Mathdef.h"
+#include "Quadrature.h"
+#include "VectorC3.h"
+#define private public
+#define protected public
+#include "ConfigLoader.h"
+#include "Mesh.h"
+#include "CommonEdge.h"
+#include "Result.h"
+#include "EFIE.h"
+#include "CFIE.h"
+#include "MLFMA.h"
+#include "iml.h"
+#undef private
+#undef protected
+
+using namespace component;
+using namespace mom;
+
+static std::string g_out;
+
+template <typename T>
+static void dump(const char* name, const T* data, size_t n)
+{
+    std::string p = g_out + "/" + name;
+    FILE* f = std::fopen(p.c_str(), "wb");
+    if (!f) { std::perror(p.c_str()); std::exit(2); }
+    std::fwrite(data, sizeof(T), n, f);
+    std::fclose(f);
+}
+
+template <typename S>
+static void dump_geometry(S& s)
+{
+    auto& mesh = *s.mesh_ptr_;
+    auto& ce = *s.ce_ptr_;
+    int nv = mesh.getNodeNum(), nt = mesh.getTriangleNum(), n = ce.getCommonEdgeNum();
+    std::vector<value_t> verts(3 * nv), normals(3 * nt), len(n);
+    std::vector<int> tris(3 * nt), rwg(6 * n);
+    for (int i = 0; i < nv; ++i) {
+        auto& v = mesh.getVertex(i);
+        verts[3 * i] = v.x; verts[3 * i + 1] = v.y; verts[3 * i + 2] = v.z;
+    }
+    for (int t = 0; t < nt; ++t) {
+        auto& tr = mesh.getTriangleRef(t);
+        tr.getVertex(tris[3 * t], tris[3 * t + 1], tris[3 * t + 2]);
+        auto& nm = tr.getNormal();
+        normals[3 * t] = nm.x; normals[3 * t + 1] = nm.y; normals[3 * t + 2] = nm.z;
+    }
+    for (int u = 0; u < n; ++u) {
+        int v1, v2, vp, vm, fp, fm;
+        value_t l;
+        ce.getCommonEdge(u, v1, v2);
+        ce.getCommonEdge(u, vp, vm, fp, fm, l);
+        int* r = &rwg[6 * u];
+        r[0] = v1; r[1] = v2; r[2] = vp; r[3] = vm; r[4] = fp; r[5] = fm;
+        len[u] = l;
+    }
+    dump("verts.bin", verts.data(), verts.size());
+    dump("tris.bin", tris.data(), tris.size());
+    dump("normals.bin", normals.data(), normals.size());
+    dump("rwg.bin", rwg.data(), rwg.size());
+    dump("rwg_len.bin", len.data(), len.size());
+    int meta[3] = {nv, nt, n};
+    dump("meta.bin", meta, 3);
+}
+
+// Directions of Result::getBistaticRCS (Result.h:59-98): one phi cut over
+// theta_from..theta_to, then the theta = 90 ring phi = 0..359.
+static std::vector<VectorR3> rcs_directions(const Scattering& sca)
+{
+    std::vector<VectorR3> dirs;
+    value_t phi = sca.phi_from * DegreesToRadians;
+    value_t cosp = cos(phi), sinp = sin(phi);
+    for (value_t td = sca.theta_from; td <= sca.theta_to; td += sca.theta_delta) {
+        value_t th = td * DegreesToRadians;
+        dirs.emplace_back(sin(th) * cosp, sin(th) * sinp, cos(th));
+    }
+    for (value_t pd = 0; pd < 360; pd += 1) {
+        value_t p = pd * DegreesToRadians;
+        dirs.emplace_back(cos(p), sin(p), 0);
+    }
+    return dirs;
+}
+
+template <typename S>
+static void dump_rcs(S& s)
+{
+    auto dirs = rcs_directions(s.scattering_);
+    std::vector<value_t> out(dirs.size()), kd(3 * dirs.size());
+    for (size_t i = 0; i < dirs.size(); ++i) {
+        out[i] = s.getBiRCS(dirs[i]);
+        kd[3 * i] = dirs[i].x; kd[3 * i + 1] = dirs[i].y; kd[3 * i + 2] = dirs[i].z;
+    }
+    dump("rcs.bin", out.data(), out.size());
+    dump("rcs_dirs.bin", kd.data(), kd.size());
+}
+
+static void dump_inc(const EM& s, value_t k)
+{
+    value_t v[10] = {s.inc_k_.x, s.inc_k_.y, s.inc_k_.z, s.inc_e_.x, s.inc_e_.y, s.inc_e_.z,
+                     s.inc_h_.x, s.inc_h_.y, s.inc_h_.z, k};
+    dump("inc.bin", v, 10);
+}
+
+static int run_efie(ConfigLoader& loader, double tol)
+{
+    EFIE s;
+    s.init(&loader);
+    dump_geometry(s);
+    dump_inc(s, s.k_);
+    int n = s.unknowns_;
+    s.Z.zeros(n, n);
+    s.Z_eigen.setZero(n, n);
+    s.fillZ();
+    std::vector<Complex> zb((size_t)n * n), ze((size_t)n * n);
+    for (int f = 0; f < n; ++f)
+        for (int c = 0; c < n; ++c) {
+            zb[(size_t)f * n + c] = s.Z(f, c);
+            ze[(size_t)f * n + c] = s.Z_eigen(f, c);
+        }
+    dump("Z_arma.bin", zb.data(), zb.size());
+    dump("Z.bin", ze.data(), ze.size());
+    s.I.zeros(n); s.V.zeros(n);
+    s.I_eigen.setZero(n); s.V_eigen.setZero(n);
+    s.fillV();
+    dump("V.bin", s.V_eigen.data(), n);
+    if (tol > 0) {
+        iml::GMRES(s.Z_eigen, s.V_eigen, s.I_eigen, (value_t)tol, 30, 5);
+        dump("I.bin", s.I_eigen.data(), n);
+        dump_rcs(s);
+        Result result;
+        result.getBistaticRCS(&s, &EFIE::getBiRCS);
+    }
+    return 0;
+}
+
+static int run_cfie(ConfigLoader& loader, double tol)
+{
+    CFIE s;
+    s.init(&loader);
+    dump_geometry(s);
+    dump_inc(s, s.k_);
+    int n = s.unknowns_;
+    s.fillZ();
+    std::vector<Complex> zb((size_t)n * n);
+    for (int f = 0; f < n; ++f)
+        for (int c = 0; c < n; ++c) zb[(size_t)f * n + c] = s.Z(f, c);
+    dump("Z.bin", zb.data(), zb.size());
+    s.fillV();
+    dump("V.bin", s.V.memptr(), n);
+    if (tol > 0) {
+        int iters = 0;
+        iml::BICGSTAB(s.Z, s.V, s.I, (value_t)tol, 500, iters);
+        dump("I.bin", s.I.memptr(), n);
+        int it[1] = {iters};
+        dump("iters.bin", it, 1);
+        dump_rcs(s);
+        Result result;
+        result.getBistaticRCS(&s, &CFIE::getBiRCS);
+    }
+    return 0;
+}
+
+static int run_mlfma(ConfigLoader& loader, unsigned seed)
+{
+    MLFMA s;
+    s.init(&loader);
+    dump_geometry(s);
+    dump_inc(s, s.k_);
+    int n = s.unknowns_;
+    int L = s.level_;
+    // box order of the unknowns and the finest-level tree
+    std::vector<int> perm;
+    for (auto& b : s.level_box_.back())
+        for (int u : b.unknown) perm.push_back(u);
+    dump("perm.bin", perm.data(), perm.size());
+    std::vector<int> lvl_boxes;
+    for (int l = 0; l <= L; ++l) lvl_boxes.push_back((int)s.level_box_[l].size());
+    dump("level_boxes.bin", lvl_boxes.data(), lvl_boxes.size());
+    std::vector<value_t> blen(s.box_len_.begin(), s.box_len_.end());
+    dump("box_len.bin", blen.data(), blen.size());
+    // per level box table: offset, count, parent index, center, #near, #far
+    for (int l = 2; l <= L; ++l) {
+        std::vector<double> tab;
+        for (auto& b : s.level_box_[l]) {
+            tab.push_back((double)b.offset);
+            tab.push_back((double)b.unknown.size());
+            tab.push_back(l > 2 ? (double)b.parent->index : -1.0);
+            tab.push_back(b.center.x); tab.push_back(b.center.y); tab.push_back(b.center.z);
+            tab.push_back((double)b.near.size()); tab.push_back((double)b.far.size());
+        }
+        char nm[64];
+        std::snprintf(nm, sizeof nm, "boxes_l%d.bin", l);
+        dump(nm, tab.data(), tab.size());
+    }
+    s.levelRootsAndWeights();
+    s.calculateInterpolationMtr();
+    s.calculateLevelK();
+    std::vector<int> poles;
+    for (auto& t : s.glxt_) poles.push_back((int)t.n_elem);
+    dump("poles.bin", poles.data(), poles.size());
+    s.calculateLevelTrans();
+    s.calculateRadAndRecv();
+    s.calculateNearZ();
+    s.fillVbyBox();
+    dump("V.bin", s.V_.memptr(), n);
+    {   // near matrix as (row, col, value) triplets in box order
+        std::vector<int> rc;
+        std::vector<Complex> val;
+        for (auto it = s.nearZ_.begin(); it != s.nearZ_.end(); ++it) {
+            rc.push_back((int)it.row());
+            rc.push_back((int)it.col());
+            val.push_back(*it);
+        }
+        dump("near_rc.bin", rc.data(), rc.size());
+        dump("near_val.bin", val.data(), val.size());
+    }
+    s.allocateForSolve();
+    s.calculateCoeff();
+    std::mt19937 gen(seed);
+    std::uniform_real_distribution<double> U(-1.0, 1.0);
+    Qcx_vec x(n);
+    for (int i = 0; i < n; ++i) x(i) = Complex((value_t)U(gen), (value_t)U(gen));
+    dump("mv_x.bin", x.memptr(), n);
+    Qcx_vec y = s.matrixVectorMultiply(x);
+    dump("mv_y.bin", y.memptr(), n);
+    Qcx_vec yn = s.nearZ_ * x;
+    dump("mv_near.bin", yn.memptr(), n);
+    int iters = s.iterativeSolve();
+    int it[1] = {iters};
+    dump("iters.bin", it, 1);
+    dump("I.bin", s.I_.memptr(), n);
+    dump_rcs(s);
+    return 0;
+}
+
+// Wall time of the reference fill on its leading rows x rows block: the
+// outer and inner loops of EFIE::fillZ / CFIE::fillZ both run to unknowns_,
+// so lowering unknowns_ bounds the sample; every entry costs the same work
+// as in the full fill (all kernels, singular terms where they fall).  With
+// solve=1 the full-size fill, RHS and Krylov solve run as the reference runs
+// them (BiCGStab 1e-2 for CFIE, GMRES 1e-3 for EFIE).
+static int run_time(ConfigLoader& loader, const std::string& kind, int rows, int solve)
+{
+    using clk = std::chrono::steady_clock;
+    double fill_s = 0, solve_s = 0, full_fill_s = 0;
+    int n = 0;
+    if (kind == "cfie") {
+        CFIE s;
+        s.init(&loader);
+        n = s.unknowns_;
+        s.unknowns_ = rows < n ? rows : n;
+        auto t0 = clk::now();
+        s.fillZ();
+        fill_s = std::chrono::duration<double>(clk::now() - t0).count();
+        s.unknowns_ = n;
+        if (solve) {
+            auto t1 = clk::now();
+            s.fillZ();
+            full_fill_s = std::chrono::duration<double>(clk::now() - t1).count();
+            s.fillV();
+            auto t2 = clk::now();
+            int iters = 0;
+            iml::BICGSTAB(s.Z, s.V, s.I, 0.01f, 500, iters);
+            solve_s = std::chrono::duration<double>(clk::now() - t2).count();
+        }
+    } else {
+        EFIE s;
+        s.init(&loader);
+        n = s.unknowns_;
+        s.unknowns_ = rows < n ? rows : n;
+        s.Z.zeros(s.unknowns_, s.unknowns_);
+        s.Z_eigen.setZero(s.unknowns_, s.unknowns_);
+        auto t0 = clk::now();
+        s.fillZ();
+        fill_s = std::chrono::duration<double>(clk::now() - t0).count();
+        s.unknowns_ = n;
+    }
+    std::printf("{\"n\": %d, \"rows\": %d, \"fill_s\": %.6f, \"full_fill_s\": %.6f, \"solve_s\": %.6f}\n",
+                n, rows < n ? rows : n, fill_s, full_fill_s, solve_s);
+    return 0;
+}
+
+int main(int argc, char** argv)
+{
+    if (argc < 4) {
+        std::fprintf(stderr, "usage: %s rwg|efie|cfie|mlfma|time <config> <outdir|kind> [arg]\n", argv[0]);
+        return 1;
+    }
+    std::string mode = argv[1];
+    ConfigLoader loader;
+    try {
+        loader.load(argv[2]);
+        if (mode == "time")
+            return run_time(loader, argv[3], argc > 4 ? std::atoi(argv[4]) : 64, argc > 5 ? std::atoi(argv[5]) : 0);
+        g_out = argv[3];
+        std::experimental::filesystem::create_directories(g_out);
+        if (mode == "rwg") {
+            EFIE s;
+            s.init(&loader);
+            dump_geometry(s);
+            return 0;
+        }
+        if (mode == "efie") return run_efie(loader, argc > 4 ? std::atof(argv[4]) : 1e-3);
+        if (mode == "cfie") return run_cfie(loader, argc > 4 ? std::atof(argv[4]) : 1e-2);
+        if (mode == "mlfma") return run_mlfma(loader, argc > 4 ? (unsigned)std::atoi(argv[4]) : 1u);
+    } catch (const std::exception& e) {
+        std::fprintf(stderr, "reference error: %s\n", e.what());
+        return 3;
+    }
+    std::fprintf(stderr, "unknown mode %s\n", mode.c_str());
+    return 1;
+}
