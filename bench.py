@@ -1,0 +1,244 @@
+"""Benchmark: RCS solves/s of the dense CFIE multi-incidence job on one GB300.
+
+Workload (the configuration the headline metric is quoted on): PEC sphere of
+radius 1 m at 300 MHz, icosahedron subdivided 4 times (5120 triangles, 7680
+RWG unknowns), CFIE alpha = 0.5, 360 incidences (theta = 90, phi = 0..359,
+theta-polarised) solved as one block of right-hand sides, monostatic RCS of
+each.  One step = fill Z + excitation for all 360 incidences + multi-RHS solve
+to 1e-6 + 360 monostatic RCS values: 360 solves.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl emfa|reference]
+
+value  : solves/s with the mesh resident on the device (CUDA events on the
+         library's stream, max over ranks x ranks' solves)
+e2e    : the same job through the host-buffer C ABI call emfa_dense_rcs
+         (mesh in from host memory, RCS out to host memory, all inside)
+Multi-GPU: replicas only (independent jobs per GPU, no collective).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "RCS solves/s + p50/p99 latency vs plain FP64 GPU path at <=0.1 dB RCS error"
+WORKLOADS = {
+    # name: (subdivisions, radius m, freq Hz, alpha, n_inc)
+    "c2_cfie_sphere_7680x360": (4, 1.0, 3e8, 0.5, 360),
+    "c1_cfie_sphere_1920x360": (3, 0.5, 3e8, 0.5, 360),
+}
+
+
+def rank_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
+
+
+class ClockSampler:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, device):
+        self.device = device
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(r[1]) for r in self.rows if len(r) > 8 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 8 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows if len(r) > 8 for i in range(4) if r[5 + i] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def incidences(n_inc):
+    return np.array([[90.0, float(p), 0.0] for p in np.arange(n_inc) * (360.0 / n_inc)], dtype=np.float64)
+
+
+def run_emfa(args, workload):
+    import torch
+    from emfa_gb300 import api, build, mesh
+
+    build.build()
+    rank, local, world = rank_env()
+    torch.cuda.set_device(local)
+    sub, radius, freq, alpha, n_inc = WORKLOADS[workload]
+    m = mesh.icosphere(sub, radius)
+    ctx = api.Context(local)
+    geo = api.Geometry(ctx, m)
+    n = geo.n
+    ang = incidences(n_inc)
+    dirs = api.monostatic_dirs(ang)
+    fp = api.fill_params("cfie", "f32", freq, alpha)
+    sp = api.solver_params("gmres", restart=30, max_iter=900, tol=1e-6, matvec=args.matvec)
+    stream = torch.cuda.ExternalStream(ctx.stream_ptr())
+    Z = torch.empty((n, n), dtype=torch.complex64, device="cuda")
+    V = torch.empty((n_inc, n), dtype=torch.complex64, device="cuda")
+    stages = {"fill_z": [], "fill_v": [], "solve": [], "rcs": []}
+    infos = []
+
+    def step(record):
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
+        ev[0].record(stream)
+        api.fill_z(geo, fp, out=Z)
+        ev[1].record(stream)
+        api.fill_v(geo, fp, ang, out=V)
+        ev[2].record(stream)
+        X, info = api.solve(ctx, Z, V, sp)
+        ev[3].record(stream)
+        r = api.rcs(geo, fp, X, dirs, per_rhs=True)
+        ev[4].record(stream)
+        if record:
+            torch.cuda.synchronize()
+            for i, k in enumerate(stages):
+                stages[k].append(ev[i].elapsed_time(ev[i + 1]))
+            infos.append((info.iterations, info.cycles, info.converged, info.max_rel_residual))
+        return ev, r
+
+    for _ in range(args.warmup):
+        step(False)
+    torch.cuda.synchronize()
+    l0 = ctx.launches()
+    start = torch.cuda.Event(enable_timing=True)
+    end = torch.cuda.Event(enable_timing=True)
+    step_ms = []
+    with ClockSampler(local) as clocks:
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        start.record(stream)
+        for _ in range(args.steps):
+            ev, r_last = step(True)
+            step_ms.append(ev[0].elapsed_time(ev[4]))
+        end.record(stream)
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+    total_ms = start.elapsed_time(end)
+    launches = (ctx.launches() - l0) // max(1, args.steps)
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * n_inc * args.steps / (total_ms * 1e-3)
+
+    # end to end through the host-buffer C ABI call
+    e2e_ms = []
+    for i in range(max(1, min(args.steps, 3))):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out, info, _ = api.dense_rcs(ctx, m, fp, ang, sp, dirs, per_rhs=True)
+        torch.cuda.synchronize()
+        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    e2e_value = world * n_inc / (statistics.median(e2e_ms) * 1e-3)
+    h2d = m.verts.nbytes + m.tris.nbytes + ang.nbytes + dirs.nbytes
+    d2h = out.nbytes
+
+    # accuracy: monostatic RCS of the mixed path against the plain FP64 path on
+    # a subset of incidences (the full FP64 block costs minutes on this part)
+    acc = {}
+    if args.check and rank == 0:
+        sub_idx = np.arange(0, n_inc, max(1, n_inc // 8))
+        fp64 = api.fill_params("cfie", "f64", freq, alpha)
+        sp64 = api.solver_params("gmres", restart=30, max_iter=900, tol=1e-8)
+        t0 = time.perf_counter()
+        out64, info64, _ = api.dense_rcs(ctx, m, fp64, ang[sub_idx], sp64, dirs[sub_idx], per_rhs=True)
+        t64 = time.perf_counter() - t0
+        acc = {"rcs_max_abs_err_db": float(np.abs(out[sub_idx] - out64).max()),
+               "checked_incidences": int(len(sub_idx)),
+               "plain_fp64_seconds_for_checked": round(t64, 3),
+               "plain_fp64_solves_per_s": round(len(sub_idx) / t64, 3)}
+    p50 = statistics.median(step_ms)
+    p99 = float(np.percentile(step_ms, 99))
+    return {
+        "value": value, "total_ms": total_ms, "step_ms": step_ms, "p50": p50, "p99": p99,
+        "stages": {k: statistics.median(v) for k, v in stages.items()}, "infos": infos,
+        "launches": launches, "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
+                                      "d2h_bytes_per_step": int(d2h), "ms": statistics.median(e2e_ms)},
+        "clocks": clocks.summary(), "n": n, "n_inc": n_inc, "acc": acc, "world": world, "rank": rank,
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="emfa", choices=["emfa", "reference"])
+    ap.add_argument("--workload", default="c2_cfie_sphere_7680x360", choices=list(WORKLOADS))
+    ap.add_argument("--matvec", default="auto", choices=["auto", "f32", "tf32"])
+    ap.add_argument("--check", type=int, default=1)
+    args = ap.parse_args()
+    rank, local, world = rank_env()
+    if world > 1:
+        import torch
+        torch.distributed.init_process_group("nccl")
+    if args.impl == "reference":
+        if rank == 0:
+            from oracle import cpu_baseline
+            print(json.dumps(cpu_baseline.reference_arm(args, WORKLOADS[args.workload], args.workload)))
+        return
+    res = run_emfa(args, args.workload)
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": round(res["value"], 3), "unit": "solves/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(res["total_ms"] / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c64/f32 (+f64 Krylov)",
+        "data": "synthetic (seeded icosphere mesh, analytic plane waves)",
+        "config": {"workload": args.workload, "n_rwg": res["n"], "n_rhs": res["n_inc"], "formulation": "CFIE a=0.5",
+                   "solver": "GMRES(30)+refinement tol 1e-6", "parallelism": "replicas",
+                   "l2": "inputs > L2 (Z = %.0f MB)" % (res["n"] ** 2 * 8 / 1e6)},
+        "latency_ms": {"p50": round(res["p50"], 3), "p99": round(res["p99"], 3)},
+        "stages_ms": {k: round(v, 3) for k, v in res["stages"].items()},
+        "solver": {"iterations": res["infos"][-1][0], "cycles": res["infos"][-1][1],
+                   "converged": res["infos"][-1][2], "max_rel_residual": res["infos"][-1][3]},
+        "e2e": {k: (round(v, 3) if isinstance(v, float) else v) for k, v in res["e2e"].items()},
+        "gpu_launches": res["launches"],
+        "clocks": res["clocks"],
+        "accuracy": res["acc"],
+    }
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,106 @@
+"""ctypes binding of libemfa_cuda.so (include/emfa_cuda.h).
+
+This is the reference-facing C ABI called from Python; tests and the bench
+drive the GPU path only through these entry points.  Device buffers are
+passed as raw pointers (torch tensors' data_ptr()).  Loading fails loudly if
+the library was not built: there is no fallback path.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libemfa_cuda.so")
+HEADER = os.path.join(HERE, "..", "include", "emfa_cuda.h")
+
+EMFA_OK = 0
+STATUS = {0: "EMFA_OK", 1: "EMFA_ERR_INVALID", 2: "EMFA_ERR_CUDA", 3: "EMFA_ERR_OOM",
+          4: "EMFA_ERR_NOT_CONVERGED", 5: "EMFA_ERR_MESH", 6: "EMFA_ERR_UNSUPPORTED", 7: "EMFA_ERR_TIMEOUT"}
+EMFA_F32, EMFA_F64 = 0, 1
+EMFA_EFIE, EMFA_CFIE = 0, 1
+EMFA_GMRES, EMFA_BICGSTAB = 0, 1
+EMFA_MV_AUTO, EMFA_MV_F64, EMFA_MV_F32, EMFA_MV_TF32 = 0, 1, 2, 3
+
+
+class FillParams(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int), ("precision", ctypes.c_int), ("freq", ctypes.c_double),
+                ("alpha", ctypes.c_double), ("sigma_re", ctypes.c_double), ("sigma_im", ctypes.c_double),
+                ("edm_mode", ctypes.c_int)]
+
+
+class SolverParams(ctypes.Structure):
+    _fields_ = [("method", ctypes.c_int), ("restart", ctypes.c_int), ("max_iter", ctypes.c_int),
+                ("tol", ctypes.c_double), ("tol_absolute", ctypes.c_int), ("matvec", ctypes.c_int),
+                ("max_refine", ctypes.c_int)]
+
+
+class SolveInfo(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int), ("cycles", ctypes.c_int), ("converged", ctypes.c_int),
+                ("max_rel_residual", ctypes.c_double), ("seconds", ctypes.c_double)]
+
+
+class EmfaError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("%s: %s" % (STATUS.get(status, status), msg))
+        self.status = status
+
+
+_lib = None
+vp = ctypes.c_void_p
+ci = ctypes.c_int
+sz = ctypes.c_size_t
+dp = ctypes.POINTER(ctypes.c_double)
+ip = ctypes.POINTER(ctypes.c_int)
+
+_SIGS = {
+    "emfa_status_string": (ctypes.c_char_p, [ci]),
+    "emfa_last_error": (ctypes.c_char_p, [vp]),
+    "emfa_version": (ctypes.c_char_p, []),
+    "emfa_ctx_create": (ci, [ci, sz, ctypes.POINTER(vp)]),
+    "emfa_ctx_destroy": (ci, [vp]),
+    "emfa_ctx_memory": (ci, [vp, ctypes.POINTER(sz), ctypes.POINTER(sz), ctypes.POINTER(sz)]),
+    "emfa_ctx_launch_count": (ci, [vp, ctypes.POINTER(ctypes.c_int64)]),
+    "emfa_ctx_synchronize": (ci, [vp]),
+    "emfa_ctx_stream": (ci, [vp, ctypes.POINTER(vp)]),
+    "emfa_build_rwg": (ci, [vp, ci, vp, ci, ip]),
+    "emfa_geom_create": (ci, [vp, vp, ci, vp, ci, vp, ci, ctypes.POINTER(vp)]),
+    "emfa_geom_destroy": (ci, [vp]),
+    "emfa_geom_size": (ci, [vp, ip, ip, ip]),
+    "emfa_fill_z": (ci, [vp, vp, ctypes.POINTER(FillParams), vp, sz, vp]),
+    "emfa_fill_v": (ci, [vp, vp, ctypes.POINTER(FillParams), vp, ci, vp, vp]),
+    "emfa_matvec": (ci, [vp, ci, ci, vp, ci, vp, ci, vp, vp]),
+    "emfa_solve": (ci, [vp, ci, vp, ci, vp, ci, vp, ctypes.POINTER(SolverParams), ctypes.POINTER(SolveInfo), vp]),
+    "emfa_rcs": (ci, [vp, vp, ctypes.POINTER(FillParams), vp, ci, vp, ci, ci, vp, vp]),
+    "emfa_dense_rcs": (ci, [vp, vp, ci, vp, ci, ctypes.POINTER(FillParams), vp, ci, ctypes.POINTER(SolverParams),
+                            vp, ci, ci, vp, vp, ctypes.POINTER(SolveInfo)]),
+}
+
+
+def header_symbols() -> list[str]:
+    """Every function the public header declares."""
+    txt = open(HEADER).read()
+    return sorted(set(re.findall(r"\b(emfa_[a-z0-9_]+)\s*\(", txt)))
+
+
+def lib():
+    """Load the in-tree library (built by emfa_gb300.build)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise OSError("libemfa_cuda.so is not built (run emfa_gb300.build.build()): %s" % LIB_PATH)
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGS.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(status, ctx=None):
+    if status != EMFA_OK:
+        msg = lib().emfa_last_error(ctx)
+        raise EmfaError(status, (msg or b"").decode(errors="replace"))
+    return status

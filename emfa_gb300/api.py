@@ -1,0 +1,226 @@
+"""Python front end over the C ABI (emfa_gb300._lib).
+
+Device memory comes from torch tensors (plumbing only: every computation
+runs in libemfa_cuda.so kernels).  Complex arrays are torch complex64 /
+complex128 tensors, RHS-major: shape (n_rhs, N).
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+
+import numpy as np
+
+from . import _lib as L
+from .mesh import TriMesh
+
+vp = ctypes.c_void_p
+
+
+def _ptr(t):
+    return vp(t.data_ptr())
+
+
+def build_rwg(tris: np.ndarray) -> np.ndarray:
+    """RWG table (N x 6: v1 v2 vxp vxm tp tm), host only."""
+    tris = np.ascontiguousarray(tris, dtype=np.int32)
+    cap = 3 * tris.shape[0] // 2 + 16
+    out = np.zeros((cap, 6), dtype=np.int32)
+    n = ctypes.c_int(0)
+    L.check(L.lib().emfa_build_rwg(tris.ctypes.data_as(vp), tris.shape[0], out.ctypes.data_as(vp), cap,
+                                   ctypes.byref(n)))
+    return out[: n.value].copy()
+
+
+def fill_params(kind="cfie", precision="f32", freq=3e8, alpha=0.5, sigma=(0.0, 0.0), edm_mode=0) -> L.FillParams:
+    return L.FillParams(L.EMFA_CFIE if kind == "cfie" else L.EMFA_EFIE,
+                        L.EMFA_F64 if precision == "f64" else L.EMFA_F32,
+                        float(freq), float(alpha), float(sigma[0]), float(sigma[1]), int(edm_mode))
+
+
+def solver_params(method="gmres", restart=30, max_iter=600, tol=1e-6, tol_absolute=False, matvec="auto",
+                  max_refine=0) -> L.SolverParams:
+    mv = {"auto": 0, "f64": 1, "f32": 2, "tf32": 3}[matvec]
+    return L.SolverParams(L.EMFA_BICGSTAB if method == "bicgstab" else L.EMFA_GMRES, int(restart), int(max_iter),
+                          float(tol), int(bool(tol_absolute)), mv, int(max_refine))
+
+
+class Context:
+    def __init__(self, device=0, hbm_budget=0):
+        self.h = vp()
+        L.check(L.lib().emfa_ctx_create(device, hbm_budget, ctypes.byref(self.h)))
+        self.device = device
+
+    def close(self):
+        if self.h:
+            L.lib().emfa_ctx_destroy(self.h)
+            self.h = vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def check(self, status):
+        return L.check(status, self.h)
+
+    def memory(self):
+        u, p, b = ctypes.c_size_t(), ctypes.c_size_t(), ctypes.c_size_t()
+        self.check(L.lib().emfa_ctx_memory(self.h, ctypes.byref(u), ctypes.byref(p), ctypes.byref(b)))
+        return u.value, p.value, b.value
+
+    def launches(self) -> int:
+        c = ctypes.c_int64()
+        self.check(L.lib().emfa_ctx_launch_count(self.h, ctypes.byref(c)))
+        return c.value
+
+    def synchronize(self):
+        self.check(L.lib().emfa_ctx_synchronize(self.h))
+
+    def stream_ptr(self) -> int:
+        s = vp()
+        self.check(L.lib().emfa_ctx_stream(self.h, ctypes.byref(s)))
+        return s.value or 0
+
+
+class Geometry:
+    def __init__(self, ctx: Context, mesh: TriMesh, rwg: np.ndarray | None = None):
+        self.ctx = ctx
+        self.verts = np.ascontiguousarray(mesh.verts, dtype=np.float64)
+        self.tris = np.ascontiguousarray(mesh.tris, dtype=np.int32)
+        self.rwg = build_rwg(self.tris) if rwg is None else np.ascontiguousarray(rwg, dtype=np.int32)
+        self.n = int(self.rwg.shape[0])
+        self.h = vp()
+        ctx.check(L.lib().emfa_geom_create(ctx.h, self.verts.ctypes.data_as(vp), self.verts.shape[0],
+                                           self.tris.ctypes.data_as(vp), self.tris.shape[0],
+                                           self.rwg.ctypes.data_as(vp), self.n, ctypes.byref(self.h)))
+
+    def close(self):
+        if self.h:
+            L.lib().emfa_geom_destroy(self.h)
+            self.h = vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def fill_z(geom: Geometry, fp: L.FillParams, out=None):
+    torch = _torch()
+    dt = torch.complex128 if fp.precision == L.EMFA_F64 else torch.complex64
+    n = geom.n
+    Z = out if out is not None else torch.empty((n, n), dtype=dt, device="cuda:%d" % geom.ctx.device)
+    geom.ctx.check(L.lib().emfa_fill_z(geom.ctx.h, geom.h, ctypes.byref(fp), _ptr(Z), Z.stride(0), None))
+    return Z
+
+
+def fill_v(geom: Geometry, fp: L.FillParams, angles, out=None):
+    """angles: (n_inc, 3) theta, phi, pole in degrees."""
+    torch = _torch()
+    a = np.ascontiguousarray(np.atleast_2d(angles), dtype=np.float64)
+    dt = torch.complex128 if fp.precision == L.EMFA_F64 else torch.complex64
+    V = out if out is not None else torch.empty((a.shape[0], geom.n), dtype=dt, device="cuda:%d" % geom.ctx.device)
+    geom.ctx.check(L.lib().emfa_fill_v(geom.ctx.h, geom.h, ctypes.byref(fp), a.ctypes.data_as(vp), a.shape[0],
+                                       _ptr(V), None))
+    return V
+
+
+def matvec(ctx: Context, Z, X, matvec="auto"):
+    torch = _torch()
+    prec = L.EMFA_F64 if Z.dtype == torch.complex128 else L.EMFA_F32
+    mv = {"auto": 0, "f64": 1, "f32": 2, "tf32": 3}[matvec]
+    Y = torch.empty_like(X)
+    ctx.check(L.lib().emfa_matvec(ctx.h, prec, mv, _ptr(Z), Z.shape[0], _ptr(X), X.shape[0], _ptr(Y), None))
+    return Y
+
+
+def solve(ctx: Context, Z, B, sp: L.SolverParams):
+    """Returns (X complex128 (n_rhs, N), SolveInfo); raises on errors other
+    than non-convergence (reported in info.converged)."""
+    torch = _torch()
+    prec = L.EMFA_F64 if Z.dtype == torch.complex128 else L.EMFA_F32
+    X = torch.empty(B.shape, dtype=torch.complex128, device=B.device)
+    info = L.SolveInfo()
+    st = L.lib().emfa_solve(ctx.h, prec, _ptr(Z), Z.shape[0], _ptr(B), B.shape[0], _ptr(X), ctypes.byref(sp),
+                            ctypes.byref(info), None)
+    if st not in (L.EMFA_OK, 4):
+        ctx.check(st)
+    return X, info
+
+
+def rcs(geom: Geometry, fp: L.FillParams, I, dirs, per_rhs=False) -> np.ndarray:
+    d = np.ascontiguousarray(dirs, dtype=np.float64)
+    n_rhs = I.shape[0]
+    n_dir = d.shape[-2] if d.ndim == 3 else d.shape[0]
+    out = np.zeros((n_rhs, n_dir), dtype=np.float64)
+    geom.ctx.check(L.lib().emfa_rcs(geom.ctx.h, geom.h, ctypes.byref(fp), _ptr(I), n_rhs, d.ctypes.data_as(vp),
+                                    n_dir, int(per_rhs), out.ctypes.data_as(vp), None))
+    return out
+
+
+def dense_rcs(ctx: Context, mesh: TriMesh, fp: L.FillParams, angles, sp: L.SolverParams, dirs, per_rhs=False,
+              want_current=False):
+    """End-to-end job from host buffers (emfa_dense_rcs)."""
+    a = np.ascontiguousarray(np.atleast_2d(angles), dtype=np.float64)
+    d = np.ascontiguousarray(dirs, dtype=np.float64)
+    n_dir = d.shape[-2] if d.ndim == 3 else d.shape[0]
+    verts = np.ascontiguousarray(mesh.verts, dtype=np.float64)
+    tris = np.ascontiguousarray(mesh.tris, dtype=np.int32)
+    out = np.zeros((a.shape[0], n_dir), dtype=np.float64)
+    cur = np.zeros((a.shape[0], 3 * tris.shape[0] // 2 * 2), dtype=np.float64) if want_current else None
+    info = L.SolveInfo()
+    st = L.lib().emfa_dense_rcs(ctx.h, verts.ctypes.data_as(vp), verts.shape[0], tris.ctypes.data_as(vp),
+                                tris.shape[0], ctypes.byref(fp), a.ctypes.data_as(vp), a.shape[0], ctypes.byref(sp),
+                                d.ctypes.data_as(vp), n_dir, int(per_rhs), out.ctypes.data_as(vp),
+                                cur.ctypes.data_as(vp) if cur is not None else None, ctypes.byref(info))
+    if st not in (L.EMFA_OK, 4):
+        ctx.check(st)
+    I = None
+    if cur is not None:
+        n = 3 * tris.shape[0] // 2
+        I = cur[:, : 2 * n].reshape(a.shape[0], n, 2)
+        I = I[..., 0] + 1j * I[..., 1]
+    return out, info, I
+
+
+def bistatic_dirs(theta_from=0.0, theta_to=180.0, theta_delta=1.0, phi=0.0, ring=True) -> np.ndarray:
+    """Directions of Result::getBistaticRCS (EMComponent/Result.h:59-98) in
+    float arithmetic: the phi cut over theta, then the theta = 90 ring."""
+    # angles in float; sin/cos in double through libm (math.*: numpy's
+    # vectorised sin/cos are not libm's) as the reference's
+    # unqualified calls bind to); cos(phi), sin(phi) stored as float; each
+    # component rounded once to float
+    f = np.float32
+    d2r = f(np.pi) / f(180.0)
+    ph = f(phi) * d2r
+    cp, sp_ = f(math.cos(float(ph))), f(math.sin(float(ph)))
+    out = []
+    td = f(theta_from)
+    while td <= f(theta_to):
+        th = float(td * d2r)
+        out.append((f(math.sin(th) * float(cp)), f(math.sin(th) * float(sp_)), f(math.cos(th))))
+        td = f(td + f(theta_delta))
+    if ring:
+        pd = f(0.0)
+        while pd < f(360.0):
+            p = float(pd * d2r)
+            out.append((f(math.cos(p)), f(math.sin(p)), f(0.0)))
+            pd = f(pd + f(1.0))
+    return np.array(out, dtype=np.float64)
+
+
+def monostatic_dirs(angles) -> np.ndarray:
+    """Backscatter direction (-k_inc) of each incidence (theta, phi) in degrees:
+    r_hat(theta, phi), shape (n_inc, 1, 3)."""
+    a = np.atleast_2d(np.asarray(angles, dtype=np.float64))
+    th, ph = np.deg2rad(a[:, 0]), np.deg2rad(a[:, 1])
+    d = np.stack([np.sin(th) * np.cos(ph), np.sin(th) * np.sin(ph), np.cos(th)], -1)
+    return d[:, None, :]

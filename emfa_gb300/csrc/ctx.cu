@@ -1,0 +1,167 @@
+// Context, status strings and HBM-budget accounting of libemfa_cuda.
+#include "emfa_internal.cuh"
+
+#include <cstdio>
+#include <cstring>
+
+namespace emfa {
+
+static std::mutex g_err_mu;
+static std::string g_last_error;
+
+void set_global_error(const std::string& msg)
+{
+    std::lock_guard<std::mutex> g(g_err_mu);
+    g_last_error = msg;
+}
+
+void set_error(Ctx* ctx, const std::string& msg)
+{
+    if (ctx) {
+        std::lock_guard<std::mutex> g(ctx->mu);
+        ctx->last_error = msg;
+    }
+    set_global_error(msg);
+}
+
+emfa_status_t ctx_alloc(Ctx* c, size_t bytes, void** p)
+{
+    {
+        std::lock_guard<std::mutex> g(c->mu);
+        if (c->budget && c->used + bytes > c->budget) {
+            char buf[160];
+            std::snprintf(buf, sizeof buf, "HBM budget exceeded: %zu B held + %zu B requested > %zu B budget",
+                          c->used, bytes, c->budget);
+            c->last_error = buf;
+            set_global_error(buf);
+            return EMFA_ERR_OOM;
+        }
+        c->used += bytes;
+        if (c->used > c->peak) c->peak = c->used;
+    }
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        std::lock_guard<std::mutex> g(c->mu);
+        c->used -= bytes;
+        c->last_error = std::string("cudaMalloc: ") + cudaGetErrorString(e);
+        set_global_error(c->last_error);
+        *p = nullptr;
+        return e == cudaErrorMemoryAllocation ? EMFA_ERR_OOM : EMFA_ERR_CUDA;
+    }
+    return EMFA_OK;
+}
+
+void ctx_free(Ctx* c, void* p, size_t bytes)
+{
+    if (!p) return;
+    cudaFree(p);
+    std::lock_guard<std::mutex> g(c->mu);
+    c->used -= bytes;
+}
+
+}  // namespace emfa
+
+using namespace emfa;
+
+extern "C" {
+
+const char* emfa_status_string(emfa_status_t s)
+{
+    switch (s) {
+        case EMFA_OK: return "ok";
+        case EMFA_ERR_INVALID: return "invalid argument";
+        case EMFA_ERR_CUDA: return "CUDA error";
+        case EMFA_ERR_OOM: return "out of device memory / HBM budget";
+        case EMFA_ERR_NOT_CONVERGED: return "iteration did not converge";
+        case EMFA_ERR_MESH: return "mesh error";
+        case EMFA_ERR_UNSUPPORTED: return "unsupported";
+        case EMFA_ERR_TIMEOUT: return "device wait timed out";
+    }
+    return "unknown status";
+}
+
+const char* emfa_last_error(const emfa_ctx_t* ctx)
+{
+    if (ctx) return ctx->last_error.c_str();
+    return g_last_error.c_str();
+}
+
+const char* emfa_version(void) { return "emfa_gb300 0.1 (sm_103a)"; }
+
+emfa_status_t emfa_ctx_create(int device, size_t hbm_budget_bytes, emfa_ctx_t** out)
+{
+    if (!out) return EMFA_ERR_INVALID;
+    *out = nullptr;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0) {
+        set_global_error(std::string("no CUDA device: ") + cudaGetErrorString(e));
+        return EMFA_ERR_CUDA;
+    }
+    if (device < 0 || device >= ndev) {
+        set_global_error("device index out of range");
+        return EMFA_ERR_INVALID;
+    }
+    e = cudaSetDevice(device);
+    if (e != cudaSuccess) {
+        set_global_error(std::string("cudaSetDevice: ") + cudaGetErrorString(e));
+        return EMFA_ERR_CUDA;
+    }
+    emfa_ctx_t* c = new emfa_ctx_t();
+    c->device = device;
+    c->budget = hbm_budget_bytes;
+    cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
+    e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        set_global_error(std::string("cudaStreamCreate: ") + cudaGetErrorString(e));
+        delete c;
+        return EMFA_ERR_CUDA;
+    }
+    *out = c;
+    return EMFA_OK;
+}
+
+emfa_status_t emfa_ctx_destroy(emfa_ctx_t* ctx)
+{
+    if (!ctx) return EMFA_ERR_INVALID;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) {
+        cudaStreamSynchronize(ctx->stream);
+        cudaStreamDestroy(ctx->stream);
+    }
+    delete ctx;
+    return EMFA_OK;
+}
+
+emfa_status_t emfa_ctx_memory(const emfa_ctx_t* ctx, size_t* used, size_t* peak, size_t* budget)
+{
+    if (!ctx) return EMFA_ERR_INVALID;
+    if (used) *used = ctx->used;
+    if (peak) *peak = ctx->peak;
+    if (budget) *budget = ctx->budget;
+    return EMFA_OK;
+}
+
+emfa_status_t emfa_ctx_launch_count(const emfa_ctx_t* ctx, int64_t* count)
+{
+    if (!ctx || !count) return EMFA_ERR_INVALID;
+    *count = ctx->kernel_launches;
+    return EMFA_OK;
+}
+
+emfa_status_t emfa_ctx_synchronize(emfa_ctx_t* ctx)
+{
+    if (!ctx) return EMFA_ERR_INVALID;
+    EMFA_CUDA(ctx, cudaSetDevice(ctx->device));
+    EMFA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return EMFA_OK;
+}
+
+emfa_status_t emfa_ctx_stream(const emfa_ctx_t* ctx, void** stream)
+{
+    if (!ctx || !stream) return EMFA_ERR_INVALID;
+    *stream = (void*)ctx->stream;
+    return EMFA_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,159 @@
+// Internal declarations shared by the libemfa_cuda translation units.
+// Device-side vector/complex helpers are templated on the arithmetic type
+// (float for the mixed-precision path, double for the plain FP64 path).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstddef>
+#include <cstdint>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/emfa_cuda.h"
+
+// ---------------------------------------------------------------------------
+// error plumbing: every CUDA call inside the library goes through EMFA_CUDA,
+// which records the failing call on the context and returns EMFA_ERR_CUDA.
+// ---------------------------------------------------------------------------
+namespace emfa {
+
+struct Ctx;
+void set_error(Ctx* ctx, const std::string& msg);
+void set_global_error(const std::string& msg);
+
+#define EMFA_CUDA(ctx, call)                                                              \
+    do {                                                                                  \
+        cudaError_t e_ = (call);                                                          \
+        if (e_ != cudaSuccess) {                                                          \
+            ::emfa::set_error((ctx), std::string(#call) + ": " + cudaGetErrorString(e_)); \
+            return EMFA_ERR_CUDA;                                                         \
+        }                                                                                 \
+    } while (0)
+
+#define EMFA_TRY(expr)                     \
+    do {                                   \
+        emfa_status_t s_ = (expr);         \
+        if (s_ != EMFA_OK) return s_;      \
+    } while (0)
+
+// ---------------------------------------------------------------------------
+// context: device, stream, HBM budget accounting
+// ---------------------------------------------------------------------------
+struct Ctx {
+    int device = 0;
+    size_t budget = 0;      // bytes the context may hold (0 = unlimited)
+    size_t used = 0;
+    size_t peak = 0;
+    cudaStream_t stream = nullptr;
+    std::string last_error;
+    std::mutex mu;
+    int sm_count = 0;
+    int kernel_launches = 0;  // kernels launched through this context
+};
+
+emfa_status_t ctx_alloc(Ctx* c, size_t bytes, void** p);
+void ctx_free(Ctx* c, void* p, size_t bytes);
+
+// RAII device buffer tied to a context's budget.
+struct DevBuf {
+    Ctx* ctx = nullptr;
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { release(); }
+    emfa_status_t alloc(Ctx* c, size_t b)
+    {
+        release();
+        ctx = c;
+        if (b == 0) return EMFA_OK;
+        emfa_status_t s = ctx_alloc(c, b, &ptr);
+        if (s == EMFA_OK) bytes = b;
+        return s;
+    }
+    void release()
+    {
+        if (ptr) ctx_free(ctx, ptr, bytes);
+        ptr = nullptr;
+        bytes = 0;
+    }
+};
+
+template <typename T> inline T* dptr(const DevBuf& b) { return reinterpret_cast<T*>(b.ptr); }
+
+// ---------------------------------------------------------------------------
+// geometry: host copy + per-precision device pack
+// ---------------------------------------------------------------------------
+// Per-RWG record consumed by the fill, excitation and far-field kernels.
+// Side 0 is the + triangle (RWG current leaves the free vertex vxp), side 1
+// the - triangle.  All coordinates are in the kernel's arithmetic type and
+// computed from that type's vertices in the reference's operation order.
+template <typename T>
+struct RwgPack {
+    T q3[2][3][3];   // 3-point Gauss points of the two triangles
+    T v[2][3];       // free vertices vxp, vxm
+    T n[2][3];       // unit normals of the two triangles
+    T cen[2][3];     // triangle centroids (EFIE far-pair test and EDM)
+    T len;           // edge length
+    int tri[2];      // triangle ids tp, tm
+    int e[2];        // local index (0..2) of the free vertex in each triangle
+};
+
+template <typename T>
+struct GeomDev {
+    bool ready = false;
+    DevBuf verts;   // V x 3
+    DevBuf tris;    // T x 3 int
+    DevBuf tri_q3;  // T x 3 x 3
+    DevBuf tri_q7;  // T x 7 x 3
+    DevBuf tri_n;   // T x 3
+    DevBuf tri_area;  // T
+    DevBuf rwg;     // N x RwgPack<T>
+};
+
+struct Geom {
+    Ctx* ctx = nullptr;
+    int nv = 0, nt = 0, n = 0;
+    std::vector<double> verts;   // host, V x 3
+    std::vector<int> tris;       // host, T x 3
+    std::vector<int> rwg;        // host, N x 6 (v1 v2 vxp vxm tp tm)
+    GeomDev<float> g32;
+    GeomDev<double> g64;
+};
+
+emfa_status_t geom_prepare_f32(Geom* g, cudaStream_t st);
+emfa_status_t geom_prepare_f64(Geom* g, cudaStream_t st);
+
+// RWG (common edge) construction, EMComponent/CommonEdge.cpp:74-106,704-743
+int build_rwg_host(const int* tris, int n_tri, std::vector<int>& rwg_out, std::string* err);
+
+// physical constants in the arithmetic type, as EMComponent/Mathdef.h
+// computes them: PI = (T)pi, Z0 = 120 PI, k = (2 PI) f / c0.
+template <typename T> struct Phys {
+    static T pi() { return (T)3.14159265358979323846; }
+    static T z0() { return (T)120 * pi(); }
+    static T c0() { return (T)299792458.0; }
+    static T wavenumber(double freq) { return ((T)2 * pi()) * (T)freq / c0(); }
+};
+
+// incidence vectors k_hat, e_hat, h_hat (EMSolver/EM.cpp:33-38), 9 values
+template <typename T>
+void incidence_vectors(double theta_deg, double phi_deg, double pole_deg, T out[9]);
+
+// ---------------------------------------------------------------------------
+// kernel launchers (fill.cu, rcs.cu, gemm.cu, krylov.cu)
+// ---------------------------------------------------------------------------
+emfa_status_t launch_fill_z(Ctx* c, Geom* g, const emfa_fill_params_t* p, void* Z, size_t ldz,
+                            cudaStream_t st);
+emfa_status_t launch_fill_v(Ctx* c, Geom* g, const emfa_fill_params_t* p, const double* angles,
+                            int n_inc, void* V, cudaStream_t st);
+emfa_status_t launch_rcs(Ctx* c, Geom* g, const emfa_fill_params_t* p, const void* I, int n_rhs,
+                         const double* dirs, int n_dir, int per_rhs_dirs, double* out_db,
+                         cudaStream_t st);
+
+}  // namespace emfa
+
+struct emfa_ctx : emfa::Ctx {};
+struct emfa_geom : emfa::Geom {};

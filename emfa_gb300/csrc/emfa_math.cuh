@@ -1,0 +1,108 @@
+// Device-side 3-vector and complex helpers, templated on float / double.
+// Vector helpers follow the operation order of EMComponent/VectorR3.h
+// (dot = x*x' + y*y' + z*z' left to right; division by a scalar is a
+// multiplication by its reciprocal), so geometry derived on the device
+// (Gauss points, normals, lengths) equals the reference's own values.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace emfa {
+
+template <typename T> struct V3 { T x, y, z; };
+template <typename T> struct Cx { T re, im; };
+
+template <typename T> __host__ __device__ __forceinline__ V3<T> v3(T x, T y, T z) { return V3<T>{x, y, z}; }
+template <typename T> __host__ __device__ __forceinline__ V3<T> operator+(V3<T> a, V3<T> b) { return v3(a.x + b.x, a.y + b.y, a.z + b.z); }
+template <typename T> __host__ __device__ __forceinline__ V3<T> operator-(V3<T> a, V3<T> b) { return v3(a.x - b.x, a.y - b.y, a.z - b.z); }
+template <typename T> __host__ __device__ __forceinline__ V3<T> operator*(V3<T> a, T d) { return v3(a.x * d, a.y * d, a.z * d); }
+template <typename T> __host__ __device__ __forceinline__ T dot(V3<T> a, V3<T> b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+template <typename T> __host__ __device__ __forceinline__ V3<T> cross(V3<T> a, V3<T> b)
+{
+    return v3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+template <typename T> __host__ __device__ __forceinline__ T norm(V3<T> a) { return sqrt(a.x * a.x + a.y * a.y + a.z * a.z); }
+template <typename T> __host__ __device__ __forceinline__ V3<T> divr(V3<T> a, T d) { T m = T(1) / d; return a * m; }
+template <typename T> __host__ __device__ __forceinline__ V3<T> normalized(V3<T> a) { return divr(a, norm(a)); }
+
+template <typename T> __host__ __device__ __forceinline__ Cx<T> cx(T re, T im) { return Cx<T>{re, im}; }
+template <typename T> __host__ __device__ __forceinline__ Cx<T> operator+(Cx<T> a, Cx<T> b) { return cx(a.re + b.re, a.im + b.im); }
+template <typename T> __host__ __device__ __forceinline__ Cx<T> operator-(Cx<T> a, Cx<T> b) { return cx(a.re - b.re, a.im - b.im); }
+template <typename T> __host__ __device__ __forceinline__ Cx<T> operator*(Cx<T> a, Cx<T> b)
+{
+    return cx(a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re);
+}
+template <typename T> __host__ __device__ __forceinline__ Cx<T> operator*(Cx<T> a, T d) { return cx(a.re * d, a.im * d); }
+template <typename T> __host__ __device__ __forceinline__ Cx<T> conjmul(Cx<T> a, Cx<T> b)  // conj(a) * b
+{
+    return cx(a.re * b.re + a.im * b.im, a.re * b.im - a.im * b.re);
+}
+
+template <typename T> __device__ __forceinline__ V3<T> ld3(const T* p) { return v3(p[0], p[1], p[2]); }
+template <typename T> __device__ __forceinline__ void st3(T* p, V3<T> v) { p[0] = v.x; p[1] = v.y; p[2] = v.z; }
+
+// sin/cos of pi*x; CUDA's accurate sincospi for both precisions.
+__device__ __forceinline__ void sincos_pi(float x, float* s, float* c) { sincospif(x, s, c); }
+__device__ __forceinline__ void sincos_pi(double x, double* s, double* c) { sincospi(x, s, c); }
+__device__ __forceinline__ float rsqrt_t(float x) { return rsqrtf(x); }
+__device__ __forceinline__ double rsqrt_t(double x) { return rsqrt(x); }
+
+// Gauss 3-point rule (EMComponent/Quadrature.cpp:13-18): barycentric
+// (2/3, 1/6, 1/6) and permutations, weights 1/3.
+template <typename T>
+__host__ __device__ inline void gauss3(V3<T> a, V3<T> b, V3<T> c, V3<T>* p)
+{
+    T g0 = T(2) / T(3), g1 = T(1) / T(6);
+    p[0] = a * g0 + b * g1 + c * g1;
+    p[1] = a * g1 + b * g0 + c * g1;
+    p[2] = a * g1 + b * g1 + c * g0;
+}
+
+// Gauss 7-point rule (Quadrature.h:42-72, Quadrature.cpp:44-53); weights
+// are twice the textbook values so that they sum to 1.
+template <typename T>
+__host__ __device__ inline void gauss7(V3<T> a, V3<T> b, V3<T> c, V3<T>* p)
+{
+    const double g[7][2] = {{0.333333333333333, 0.333333333333333}, {0.797426985353087, 0.101286507323456},
+                            {0.101286507323456, 0.797426985353087}, {0.101286507323456, 0.101286507323456},
+                            {0.470142064105115, 0.470142064105115}, {0.470142064105115, 0.059715871789770},
+                            {0.059715871789770, 0.470142064105115}};
+    for (int i = 0; i < 7; ++i) {
+        T g0 = (T)g[i][0], g1 = (T)g[i][1];
+        T g2 = T(1) - g0 - g1;
+        p[i] = a * g0 + b * g1 + c * g2;
+    }
+}
+
+template <typename T>
+__host__ __device__ inline T gauss7_weight(int i)
+{
+    const double w[7] = {0.112500000000000, 0.062969590272413, 0.062969590272413, 0.062969590272413,
+                         0.066197076394253, 0.066197076394253, 0.066197076394253};
+    return (T)w[i] * 2;
+}
+
+// Heron's formula (VectorR3.h Area)
+template <typename T>
+__host__ __device__ inline T tri_area(V3<T> a, V3<T> b, V3<T> c)
+{
+    T la = norm(a - b), lb = norm(b - c), lc = norm(c - a);
+    T ls = (la + lb + lc) / T(2);
+    return sqrt(ls * (ls - la) * (ls - lb) * (ls - lc));
+}
+
+// Triangle::getInfo (EMComponent/Triangle.cpp:47-61)
+template <typename T>
+__host__ __device__ inline V3<T> tri_normal(V3<T> A, V3<T> B, V3<T> C)
+{
+    V3<T> ab = B - A, bc = C - B, ca = A - C;
+    V3<T> n = (dot(ab, bc) < dot(bc, ca)) ? cross(ab, bc) : cross(bc, ca);
+    return divr(n, norm(n));
+}
+
+template <typename T>
+__host__ __device__ inline V3<T> centroid(V3<T> a, V3<T> b, V3<T> c)
+{
+    return divr(a + b + c, T(3));
+}
+
+}  // namespace emfa

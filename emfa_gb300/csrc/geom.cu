@@ -1,0 +1,251 @@
+// Geometry: RWG table construction (host), mesh upload and the per-precision
+// geometry pack (Gauss points, normals, centroids, edge lengths) built on the
+// device.  This translation unit is compiled with -fmad=false so the pack
+// reproduces the reference's own rounding of those quantities.
+#include "emfa_internal.cuh"
+#include "emfa_math.cuh"
+
+#include <cmath>
+#include <unordered_map>
+
+namespace emfa {
+
+// CommonEdge::updateCommonEdge (EMComponent/CommonEdge.cpp:704-743) scans
+// every open edge for each triangle; an edge (A,B) of a triangle pairs with
+// an open edge (B,A) of an earlier one.  The same matching through a hash of
+// the open directed edges, same order and orientation: RWGs are the paired
+// edges in order of first appearance, + side = first triangle, free vertices
+// = the opposite corners.  Boundary (never paired) edges are dropped.
+int build_rwg_host(const int* tris, int n_tri, std::vector<int>& out, std::string* err)
+{
+    struct Tmp { int v1, v2, vxp, vxm, tp, tm; };
+    std::vector<Tmp> tmp;
+    tmp.reserve((size_t)3 * n_tri);
+    std::unordered_map<uint64_t, std::vector<int>> open;
+    open.reserve((size_t)3 * n_tri);
+    auto key = [](int a, int b) { return ((uint64_t)(uint32_t)a << 32) | (uint32_t)b; };
+    for (int t = 0; t < n_tri; ++t) {
+        int a = tris[3 * t], b = tris[3 * t + 1], c = tris[3 * t + 2];
+        int corner[3][3] = {{a, b, c}, {b, c, a}, {c, a, b}};
+        bool fresh[3] = {true, true, true};
+        for (int e = 0; e < 3; ++e) {
+            auto it = open.find(key(corner[e][1], corner[e][0]));
+            if (it == open.end()) continue;
+            for (int idx : it->second) {
+                tmp[idx].vxm = corner[e][2];
+                tmp[idx].tm = t;
+            }
+            fresh[e] = false;
+            open.erase(it);
+        }
+        for (int e = 0; e < 3; ++e) {
+            if (!fresh[e]) continue;
+            int u = corner[e][0], v = corner[e][1];
+            if (u == v) {
+                if (err) *err = "degenerate triangle " + std::to_string(t);
+                return -1;
+            }
+            open[key(u, v)].push_back((int)tmp.size());
+            tmp.push_back(Tmp{u, v, corner[e][2], -1, t, -1});
+        }
+    }
+    out.clear();
+    for (const Tmp& s : tmp) {
+        if (s.tm == -1) continue;
+        out.insert(out.end(), {s.v1, s.v2, s.vxp, s.vxm, s.tp, s.tm});
+    }
+    return (int)(out.size() / 6);
+}
+
+template <typename T>
+void incidence_vectors(double theta_deg, double phi_deg, double pole_deg, T out[9])
+{
+    // EMSolver/EM.cpp:29-38.  Angles in the arithmetic type; the reference's
+    // unqualified sin/cos are the C double functions, so each component is a
+    // double expression rounded once to T.
+    const T pi = Phys<T>::pi();
+    const T d2r = pi / T(180);
+    T pol = (T)pole_deg * d2r, th = (T)theta_deg * d2r, ph = (T)phi_deg * d2r;
+    double st = std::sin((double)th), ct = std::cos((double)th), sp = std::sin((double)ph), cp = std::cos((double)ph);
+    double so = std::sin((double)pol), co = std::cos((double)pol);
+    V3<T> k = v3<T>((T)(-st * cp), (T)(-st * sp), (T)(-ct));
+    V3<T> e = v3<T>((T)(-co * ct * cp - so * sp), (T)(-co * ct * sp + so * cp), (T)(co * st));
+    V3<T> h = cross(k, e);
+    T v[9] = {k.x, k.y, k.z, e.x, e.y, e.z, h.x, h.y, h.z};
+    for (int i = 0; i < 9; ++i) out[i] = v[i];
+}
+template void incidence_vectors<float>(double, double, double, float*);
+template void incidence_vectors<double>(double, double, double, double*);
+
+// one thread per triangle: vertices, Gauss points, normal, area
+template <typename T>
+__global__ void k_pack_tris(const double* __restrict__ vd, const int* __restrict__ tris, int nt,
+                            T* __restrict__ vt, T* __restrict__ q3, T* __restrict__ q7, T* __restrict__ nrm,
+                            T* __restrict__ area, int nv)
+{
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < nv) {
+        vt[3 * t] = (T)vd[3 * t];
+        vt[3 * t + 1] = (T)vd[3 * t + 1];
+        vt[3 * t + 2] = (T)vd[3 * t + 2];
+    }
+    if (t >= nt) return;
+    V3<T> a, b, c;
+    int ia = tris[3 * t], ib = tris[3 * t + 1], ic = tris[3 * t + 2];
+    a = v3<T>((T)vd[3 * ia], (T)vd[3 * ia + 1], (T)vd[3 * ia + 2]);
+    b = v3<T>((T)vd[3 * ib], (T)vd[3 * ib + 1], (T)vd[3 * ib + 2]);
+    c = v3<T>((T)vd[3 * ic], (T)vd[3 * ic + 1], (T)vd[3 * ic + 2]);
+    V3<T> p3[3], p7[7];
+    gauss3(a, b, c, p3);
+    gauss7(a, b, c, p7);
+    for (int i = 0; i < 3; ++i) st3(q3 + 9 * t + 3 * i, p3[i]);
+    for (int i = 0; i < 7; ++i) st3(q7 + 21 * t + 3 * i, p7[i]);
+    st3(nrm + 3 * t, tri_normal(a, b, c));
+    area[t] = tri_area(a, b, c);
+}
+
+template <typename T>
+__global__ void k_pack_rwg(const double* __restrict__ vd, const int* __restrict__ tris, const int* __restrict__ rwg,
+                           int n, const T* __restrict__ q3, const T* __restrict__ nrm, RwgPack<T>* __restrict__ out)
+{
+    int u = blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= n) return;
+    const int* r = rwg + 6 * u;
+    RwgPack<T> pk;
+    auto vtx = [&](int i) { return v3<T>((T)vd[3 * i], (T)vd[3 * i + 1], (T)vd[3 * i + 2]); };
+    for (int s = 0; s < 2; ++s) {
+        int t = r[4 + s];
+        int fv = r[2 + s];
+        pk.tri[s] = t;
+        int e = 0;
+        for (int j = 0; j < 3; ++j)
+            if (tris[3 * t + j] == fv) e = j;
+        pk.e[s] = e;
+        for (int i = 0; i < 9; ++i) (&pk.q3[s][0][0])[i] = q3[9 * t + i];
+        V3<T> fvv = vtx(fv);
+        pk.v[s][0] = fvv.x; pk.v[s][1] = fvv.y; pk.v[s][2] = fvv.z;
+        pk.n[s][0] = nrm[3 * t]; pk.n[s][1] = nrm[3 * t + 1]; pk.n[s][2] = nrm[3 * t + 2];
+        V3<T> cc = centroid(vtx(tris[3 * t]), vtx(tris[3 * t + 1]), vtx(tris[3 * t + 2]));
+        pk.cen[s][0] = cc.x; pk.cen[s][1] = cc.y; pk.cen[s][2] = cc.z;
+    }
+    pk.len = norm(vtx(r[0]) - vtx(r[1]));
+    out[u] = pk;
+}
+
+template <typename T>
+static emfa_status_t geom_prepare(Geom* g, GeomDev<T>& d, cudaStream_t st)
+{
+    if (d.ready) return EMFA_OK;
+    Ctx* c = g->ctx;
+    DevBuf vd, td, rd;
+    EMFA_TRY(vd.alloc(c, sizeof(double) * 3 * g->nv));
+    EMFA_TRY(rd.alloc(c, sizeof(int) * 6 * (size_t)g->n));
+    EMFA_TRY(d.tris.alloc(c, sizeof(int) * 3 * (size_t)g->nt));
+    EMFA_TRY(d.verts.alloc(c, sizeof(T) * 3 * (size_t)g->nv));
+    EMFA_TRY(d.tri_q3.alloc(c, sizeof(T) * 9 * (size_t)g->nt));
+    EMFA_TRY(d.tri_q7.alloc(c, sizeof(T) * 21 * (size_t)g->nt));
+    EMFA_TRY(d.tri_n.alloc(c, sizeof(T) * 3 * (size_t)g->nt));
+    EMFA_TRY(d.tri_area.alloc(c, sizeof(T) * (size_t)g->nt));
+    EMFA_TRY(d.rwg.alloc(c, sizeof(RwgPack<T>) * (size_t)g->n));
+    EMFA_CUDA(c, cudaMemcpyAsync(vd.ptr, g->verts.data(), vd.bytes, cudaMemcpyHostToDevice, st));
+    EMFA_CUDA(c, cudaMemcpyAsync(d.tris.ptr, g->tris.data(), d.tris.bytes, cudaMemcpyHostToDevice, st));
+    EMFA_CUDA(c, cudaMemcpyAsync(rd.ptr, g->rwg.data(), rd.bytes, cudaMemcpyHostToDevice, st));
+    int m = g->nt > g->nv ? g->nt : g->nv;
+    k_pack_tris<T><<<(m + 127) / 128, 128, 0, st>>>(dptr<double>(vd), dptr<int>(d.tris), g->nt, dptr<T>(d.verts),
+                                                    dptr<T>(d.tri_q3), dptr<T>(d.tri_q7), dptr<T>(d.tri_n),
+                                                    dptr<T>(d.tri_area), g->nv);
+    k_pack_rwg<T><<<(g->n + 127) / 128, 128, 0, st>>>(dptr<double>(vd), dptr<int>(d.tris), dptr<int>(rd), g->n,
+                                                      dptr<T>(d.tri_q3), dptr<T>(d.tri_n), dptr<RwgPack<T>>(d.rwg));
+    c->kernel_launches += 2;
+    EMFA_CUDA(c, cudaGetLastError());
+    EMFA_CUDA(c, cudaStreamSynchronize(st));  // vd/rd are released on return
+    d.ready = true;
+    return EMFA_OK;
+}
+
+emfa_status_t geom_prepare_f32(Geom* g, cudaStream_t st) { return geom_prepare<float>(g, g->g32, st); }
+emfa_status_t geom_prepare_f64(Geom* g, cudaStream_t st) { return geom_prepare<double>(g, g->g64, st); }
+
+}  // namespace emfa
+
+using namespace emfa;
+
+extern "C" {
+
+emfa_status_t emfa_build_rwg(const int* tris_host, int n_tri, int* rwg_host, int capacity, int* n_rwg)
+{
+    if (!tris_host || n_tri <= 0 || !n_rwg) {
+        set_global_error("emfa_build_rwg: bad arguments");
+        return EMFA_ERR_INVALID;
+    }
+    std::vector<int> out;
+    std::string err;
+    int n = build_rwg_host(tris_host, n_tri, out, &err);
+    if (n < 0) {
+        set_global_error("emfa_build_rwg: " + err);
+        return EMFA_ERR_MESH;
+    }
+    *n_rwg = n;
+    if (n > capacity || !rwg_host) {
+        set_global_error("emfa_build_rwg: capacity too small");
+        return EMFA_ERR_INVALID;
+    }
+    std::copy(out.begin(), out.end(), rwg_host);
+    return EMFA_OK;
+}
+
+emfa_status_t emfa_geom_create(emfa_ctx_t* ctx, const double* verts_host, int n_vert, const int* tris_host,
+                               int n_tri, const int* rwg_host, int n_rwg, emfa_geom_t** out)
+{
+    if (!ctx || !verts_host || !tris_host || !rwg_host || !out || n_vert <= 0 || n_tri <= 0 || n_rwg <= 0) {
+        set_error(ctx, "emfa_geom_create: bad arguments");
+        return EMFA_ERR_INVALID;
+    }
+    for (int i = 0; i < 3 * n_tri; ++i)
+        if (tris_host[i] < 0 || tris_host[i] >= n_vert) {
+            set_error(ctx, "emfa_geom_create: triangle vertex index out of range");
+            return EMFA_ERR_MESH;
+        }
+    for (int u = 0; u < n_rwg; ++u) {
+        const int* r = rwg_host + 6 * u;
+        for (int j = 0; j < 4; ++j)
+            if (r[j] < 0 || r[j] >= n_vert) {
+                set_error(ctx, "emfa_geom_create: RWG vertex index out of range (open edge?)");
+                return EMFA_ERR_MESH;
+            }
+        for (int j = 4; j < 6; ++j)
+            if (r[j] < 0 || r[j] >= n_tri) {
+                set_error(ctx, "emfa_geom_create: RWG triangle index out of range");
+                return EMFA_ERR_MESH;
+            }
+    }
+    emfa_geom_t* g = new emfa_geom_t();
+    g->ctx = ctx;
+    g->nv = n_vert;
+    g->nt = n_tri;
+    g->n = n_rwg;
+    g->verts.assign(verts_host, verts_host + 3 * (size_t)n_vert);
+    g->tris.assign(tris_host, tris_host + 3 * (size_t)n_tri);
+    g->rwg.assign(rwg_host, rwg_host + 6 * (size_t)n_rwg);
+    *out = g;
+    return EMFA_OK;
+}
+
+emfa_status_t emfa_geom_destroy(emfa_geom_t* geom)
+{
+    if (!geom) return EMFA_ERR_INVALID;
+    cudaSetDevice(geom->ctx->device);
+    delete geom;
+    return EMFA_OK;
+}
+
+emfa_status_t emfa_geom_size(const emfa_geom_t* geom, int* n_vert, int* n_tri, int* n_rwg)
+{
+    if (!geom) return EMFA_ERR_INVALID;
+    if (n_vert) *n_vert = geom->nv;
+    if (n_tri) *n_tri = geom->nt;
+    if (n_rwg) *n_rwg = geom->n;
+    return EMFA_OK;
+}
+
+}  // extern "C"

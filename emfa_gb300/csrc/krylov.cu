@@ -1,0 +1,741 @@
+// Batched Krylov solvers: all right-hand sides advance in lockstep and share
+// one multi-RHS product Z V per step.
+//
+// GMRES(m) (EMIterative/iml.cpp:156-207): Arnoldi by classical Gram-Schmidt
+// applied twice (CGS2, FP64 coefficients), complex Givens rotations in FP64,
+// per-RHS early exit when the rotated residual |g_{j+1}| meets the tolerance,
+// restart from the true residual.  For the mixed-precision path the basis is
+// stored in FP32, the inner product Z V_j runs in reduced precision, and each
+// restart recomputes b - Z x with FP64 accumulation: restarted GMRES is then
+// mixed-precision iterative refinement with GMRES as the inner solver.
+//
+// BiCGStab (EMIterative/iml.cpp:3-39, MLFMA.cpp:402-452): the reference's
+// update order, x0 = 0, stop when ||s|| / ||b|| < tol, FP64 vectors.
+//
+// All reductions use fixed-order two-level sums (per-block partials, then a
+// sequential sum of the partials), so a solve is run-to-run reproducible.
+#include "emfa_internal.cuh"
+#include "emfa_math.cuh"
+#include "gemm.cuh"
+#include "krylov.cuh"
+
+#include <algorithm>
+#include <cmath>
+
+namespace emfa {
+
+constexpr int KB = 256;     // threads per block of the vector kernels
+constexpr int KE = 4;       // elements per thread per block chunk
+constexpr int KCHUNK = KB * KE;
+
+template <typename T> __device__ __forceinline__ double2 ld2(const Cx<T>* p) { Cx<T> v = *p; return make_double2((double)v.re, (double)v.im); }
+__device__ __forceinline__ double2 ld2(const double2* p) { return *p; }
+
+// partial[(i * nrhs + r) * nblk + blk] = sum_{k in chunk} conj(V_i[r][k]) W[r][k]
+template <typename TV, typename TW>
+__global__ void __launch_bounds__(KB) k_block_dots(const TV* __restrict__ V, size_t vstride, int nv,
+                                                   const TW* __restrict__ W, int n, int nrhs, int nblk,
+                                                   double2* __restrict__ partial)
+{
+    const int blk = blockIdx.x, r = blockIdx.y;
+    const size_t base = (size_t)r * n;
+    double2 w[KE];
+    int kk[KE];
+#pragma unroll
+    for (int e = 0; e < KE; ++e) {
+        int k = blk * KCHUNK + e * KB + threadIdx.x;
+        kk[e] = k;
+        w[e] = k < n ? ld2(W + base + k) : make_double2(0.0, 0.0);
+    }
+    __shared__ double2 red[32][KB / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int i0 = 0; i0 < nv; i0 += 32) {
+        int cnt = min(32, nv - i0);
+        for (int ii = 0; ii < cnt; ++ii) {
+            const TV* vi = V + (size_t)(i0 + ii) * vstride + base;
+            double re = 0.0, im = 0.0;
+#pragma unroll
+            for (int e = 0; e < KE; ++e) {
+                if (kk[e] < n) {
+                    double2 v = ld2(vi + kk[e]);
+                    re += v.x * w[e].x + v.y * w[e].y;
+                    im += v.x * w[e].y - v.y * w[e].x;
+                }
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                re += __shfl_xor_sync(0xffffffffu, re, o);
+                im += __shfl_xor_sync(0xffffffffu, im, o);
+            }
+            if (lane == 0) red[ii][wid] = make_double2(re, im);
+        }
+        __syncthreads();
+        if (threadIdx.x < cnt) {
+            double2 s = make_double2(0.0, 0.0);
+            for (int q = 0; q < KB / 32; ++q) {
+                s.x += red[threadIdx.x][q].x;
+                s.y += red[threadIdx.x][q].y;
+            }
+            partial[((size_t)(i0 + threadIdx.x) * nrhs + r) * nblk + blk] = s;
+        }
+        __syncthreads();
+    }
+}
+
+// out[i * nrhs + r] (+)= sum_blk partial[(i * nrhs + r) * nblk + blk]
+__global__ void k_reduce_partials(const double2* __restrict__ partial, int nv, int nrhs, int nblk,
+                                  double2* __restrict__ out, int accumulate)
+{
+    int id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= nv * nrhs) return;
+    const double2* p = partial + (size_t)id * nblk;
+    double2 s = make_double2(0.0, 0.0);
+    for (int b = 0; b < nblk; ++b) {
+        s.x += p[b].x;
+        s.y += p[b].y;
+    }
+    if (accumulate) {
+        s.x += out[id].x;
+        s.y += out[id].y;
+    }
+    out[id] = s;
+}
+
+// W[r][k] -= sum_{i < nv} h[i][r] V_i[r][k]; partial norms of the new W
+template <typename T>
+__global__ void __launch_bounds__(KB) k_axpys(const Cx<T>* __restrict__ V, size_t vstride, int nv,
+                                              const double2* __restrict__ h, Cx<T>* __restrict__ W, int n, int nrhs,
+                                              int nblk, double2* __restrict__ pnorm)
+{
+    const int blk = blockIdx.x, r = blockIdx.y;
+    const size_t base = (size_t)r * n;
+    __shared__ double2 hs[64];
+    for (int i = threadIdx.x; i < nv; i += KB) hs[i] = h[(size_t)i * nrhs + r];
+    __syncthreads();
+    double nr = 0.0;
+#pragma unroll
+    for (int e = 0; e < KE; ++e) {
+        int k = blk * KCHUNK + e * KB + threadIdx.x;
+        if (k >= n) continue;
+        double2 w = ld2(W + base + k);
+        for (int i = 0; i < nv; ++i) {
+            double2 v = ld2(V + (size_t)i * vstride + base + k);
+            w.x -= hs[i].x * v.x - hs[i].y * v.y;
+            w.y -= hs[i].x * v.y + hs[i].y * v.x;
+        }
+        Cx<T> o = cx((T)w.x, (T)w.y);
+        W[base + k] = o;
+        nr += (double)o.re * (double)o.re + (double)o.im * (double)o.im;
+    }
+    __shared__ double red[KB / 32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) nr += __shfl_xor_sync(0xffffffffu, nr, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = nr;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int q = 0; q < KB / 32; ++q) s += red[q];
+        pnorm[(size_t)r * nblk + blk] = make_double2(s, 0.0);
+    }
+}
+
+// per-RHS: finish Arnoldi column j, rotate, test convergence
+__global__ void k_arnoldi_finish(GmresDev s, int j, const double2* __restrict__ pnorm, int nblk)
+{
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= s.nrhs) return;
+    const int m = s.m;
+    if (!s.active[r]) {
+        s.scale[r] = 0.0;
+        return;
+    }
+    double nr2 = 0.0;
+    for (int b = 0; b < nblk; ++b) nr2 += pnorm[(size_t)r * nblk + b].x;
+    double beta = sqrt(nr2);
+    double2* H = s.H + (size_t)r * (m + 1) * m;
+    // column j of H: CGS2 coefficients
+    for (int i = 0; i <= j; ++i) H[i * m + j] = s.hcol[(size_t)i * s.nrhs + r];
+    H[(j + 1) * m + j] = make_double2(beta, 0.0);
+    double* cs = s.cs + (size_t)r * m;
+    double2* sn = s.sn + (size_t)r * m;
+    double2* g = s.g + (size_t)r * (m + 1);
+    // previous rotations: [x; y] <- [c x + s y; -conj(s) x + c y]
+    for (int i = 0; i < j; ++i) {
+        double2 x = H[i * m + j], y = H[(i + 1) * m + j];
+        double c = cs[i];
+        double2 sv = sn[i];
+        double2 nx = make_double2(c * x.x + sv.x * y.x - sv.y * y.y, c * x.y + sv.x * y.y + sv.y * y.x);
+        double2 ny = make_double2(-(sv.x * x.x + sv.y * x.y) + c * y.x, -(sv.x * x.y - sv.y * x.x) + c * y.y);
+        H[i * m + j] = nx;
+        H[(i + 1) * m + j] = ny;
+    }
+    double2 a = H[j * m + j];
+    double b = beta;
+    double aa = hypot(a.x, a.y);
+    double nu = hypot(aa, b);
+    double c;
+    double2 sv;
+    if (aa == 0.0) {
+        c = 0.0;
+        sv = make_double2(1.0, 0.0);
+        H[j * m + j] = make_double2(b, 0.0);
+    } else {
+        c = aa / nu;
+        double2 ph = make_double2(a.x / aa, a.y / aa);
+        sv = make_double2(ph.x * b / nu, ph.y * b / nu);
+        H[j * m + j] = make_double2(ph.x * nu, ph.y * nu);
+    }
+    H[(j + 1) * m + j] = make_double2(0.0, 0.0);
+    cs[j] = c;
+    sn[j] = sv;
+    double2 gj = g[j];
+    g[j + 1] = make_double2(-(sv.x * gj.x + sv.y * gj.y), -(sv.x * gj.y - sv.y * gj.x));
+    g[j] = make_double2(c * gj.x, c * gj.y);
+    double res = hypot(g[j + 1].x, g[j + 1].y);
+    s.jlen[r] = j + 1;
+    s.est[r] = res;
+    double thr = s.tol_abs ? s.tol : s.tol * s.bnorm[r];
+    bool breakdown = beta <= 1e-14 * s.bnorm[r];
+    if (res < thr || breakdown || j + 1 == m) {
+        s.active[r] = 0;
+        s.scale[r] = 0.0;
+    } else {
+        s.scale[r] = 1.0 / beta;
+        atomicAdd(s.counters, 1);
+    }
+}
+
+// V_out[r][k] = scale[r] * W[r][k]
+template <typename TO, typename TI>
+__global__ void k_scale_store(const TI* __restrict__ W, const double* __restrict__ scale, int n, int nrhs,
+                              TO* __restrict__ out)
+{
+    size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    size_t tot = (size_t)n * nrhs;
+    for (; id < tot; id += (size_t)gridDim.x * blockDim.x) {
+        int r = (int)(id / n);
+        double sc = scale[r];
+        double2 w = ld2(W + id);
+        out[id] = TO{(decltype(out->re))(w.x * sc), (decltype(out->re))(w.y * sc)};
+    }
+}
+
+// per-RHS back substitution of the rotated Hessenberg system
+__global__ void k_backsolve(GmresDev s)
+{
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= s.nrhs) return;
+    const int m = s.m;
+    int jl = s.jlen[r];
+    const double2* H = s.H + (size_t)r * (m + 1) * m;
+    const double2* g = s.g + (size_t)r * (m + 1);
+    double2* y = s.y;  // y[i * nrhs + r]
+    for (int i = m - 1; i >= jl; --i) y[(size_t)i * s.nrhs + r] = make_double2(0.0, 0.0);
+    for (int i = jl - 1; i >= 0; --i) {
+        double2 acc = g[i];
+        for (int q = i + 1; q < jl; ++q) {
+            double2 h = H[i * m + q], yq = y[(size_t)q * s.nrhs + r];
+            acc.x -= h.x * yq.x - h.y * yq.y;
+            acc.y -= h.x * yq.y + h.y * yq.x;
+        }
+        double2 d = H[i * m + i];
+        double den = d.x * d.x + d.y * d.y;
+        double2 v = den > 0 ? make_double2((acc.x * d.x + acc.y * d.y) / den, (acc.y * d.x - acc.x * d.y) / den)
+                            : make_double2(0.0, 0.0);
+        y[(size_t)i * s.nrhs + r] = v;
+    }
+}
+
+// X[r][k] += sum_{i < jlen[r]} y[i][r] V_i[r][k]
+template <typename T>
+__global__ void k_update_x(const Cx<T>* __restrict__ V, size_t vstride, int nvmax, const double2* __restrict__ y,
+                           const int* __restrict__ jlen, double2* __restrict__ X, int n, int nrhs)
+{
+    const int r = blockIdx.y;
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    int jl = min(jlen[r], nvmax);
+    size_t o = (size_t)r * n + k;
+    double2 x = X[o];
+    for (int i = 0; i < jl; ++i) {
+        double2 yi = y[(size_t)i * nrhs + r];
+        double2 v = ld2(V + (size_t)i * vstride + o);
+        x.x += yi.x * v.x - yi.y * v.y;
+        x.y += yi.x * v.y + yi.y * v.x;
+    }
+    X[o] = x;
+}
+
+// R = B - Y (all complex128; B may be complex64)
+template <typename TB>
+__global__ void k_residual(const TB* __restrict__ B, const double2* __restrict__ Y, double2* __restrict__ R, size_t tot)
+{
+    size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    for (; id < tot; id += (size_t)gridDim.x * blockDim.x) {
+        double2 b = ld2(B + id), y = Y[id];
+        R[id] = make_double2(b.x - y.x, b.y - y.y);
+    }
+}
+
+__global__ void k_to_f32(const double2* __restrict__ X, float2* __restrict__ Y, size_t tot)
+{
+    size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    for (; id < tot; id += (size_t)gridDim.x * blockDim.x) Y[id] = make_float2((float)X[id].x, (float)X[id].y);
+}
+
+__global__ void k_to_f64(const float2* __restrict__ X, double2* __restrict__ Y, size_t tot)
+{
+    size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    for (; id < tot; id += (size_t)gridDim.x * blockDim.x) Y[id] = make_double2((double)X[id].x, (double)X[id].y);
+}
+
+// start of a restart cycle: beta = ||R||, convergence test, g = beta e1
+__global__ void k_cycle_init(GmresDev s, const double2* __restrict__ pnorm, int nblk, int first)
+{
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= s.nrhs) return;
+    double nr2 = 0.0;
+    for (int b = 0; b < nblk; ++b) nr2 += pnorm[(size_t)r * nblk + b].x;
+    double beta = sqrt(nr2);
+    if (first) s.bnorm[r] = beta;  // x0 = 0: first residual is b
+    s.true_res[r] = s.bnorm[r] > 0 ? beta / s.bnorm[r] : 0.0;
+    double thr = s.tol_abs ? s.tol : s.tol * s.bnorm[r];
+    double2* g = s.g + (size_t)r * (s.m + 1);
+    for (int i = 0; i <= s.m; ++i) g[i] = make_double2(0.0, 0.0);
+    g[0] = make_double2(beta, 0.0);
+    s.jlen[r] = 0;
+    if (beta < thr || beta == 0.0) {
+        s.active[r] = 0;
+        s.scale[r] = 0.0;
+        atomicAdd(s.counters + 1, 1);  // converged
+    } else {
+        s.active[r] = 1;
+        s.scale[r] = 1.0 / beta;
+        atomicAdd(s.counters, 1);  // active
+    }
+}
+
+__global__ void k_accumulate(double2* __restrict__ a, const double2* __restrict__ b, int tot)
+{
+    int id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id < tot) {
+        a[id].x += b[id].x;
+        a[id].y += b[id].y;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host driver
+// ---------------------------------------------------------------------------
+static int dot_blocks(int n) { return (n + KCHUNK - 1) / KCHUNK; }
+
+template <typename T>
+static emfa_status_t dots(Ctx* c, const Cx<T>* V, size_t vstride, int nv, const void* W, bool w_double, int n,
+                          int nrhs, double2* partial, double2* out, int accumulate, cudaStream_t st)
+{
+    int nblk = dot_blocks(n);
+    dim3 grd(nblk, nrhs);
+    if (w_double)
+        k_block_dots<Cx<T>, double2><<<grd, KB, 0, st>>>(V, vstride, nv, (const double2*)W, n, nrhs, nblk, partial);
+    else
+        k_block_dots<Cx<T>, Cx<T>><<<grd, KB, 0, st>>>(V, vstride, nv, (const Cx<T>*)W, n, nrhs, nblk, partial);
+    k_reduce_partials<<<(nv * nrhs + 127) / 128, 128, 0, st>>>(partial, nv, nrhs, nblk, out, accumulate);
+    c->kernel_launches += 2;
+    return EMFA_OK;
+}
+
+static int grid1(size_t tot) { return (int)std::min<size_t>((tot + 255) / 256, 8192); }
+
+template <typename T>
+static emfa_status_t gmres_t(Ctx* c, int prec, const void* Z, int n, const void* B, int nrhs, double2* X,
+                             const emfa_solver_params_t* sp, emfa_solve_info_t* info, cudaStream_t st)
+{
+    const int m = std::max(1, std::min(sp->restart > 0 ? sp->restart : 30, 60));
+    const size_t vec = (size_t)n * nrhs;
+    const int nblk = dot_blocks(n);
+    DevBuf Vb, Wb, Rb, Xt, Hb, csb, snb, gb, yb, hcb, pb, pnb, small, cnt;
+    EMFA_TRY(Vb.alloc(c, sizeof(Cx<T>) * vec * (m + 1)));
+    EMFA_TRY(Wb.alloc(c, sizeof(Cx<T>) * vec));
+    EMFA_TRY(Rb.alloc(c, sizeof(double2) * vec));
+    if (prec == EMFA_F32) EMFA_TRY(Xt.alloc(c, sizeof(float2) * vec));
+    EMFA_TRY(Hb.alloc(c, sizeof(double2) * (size_t)nrhs * (m + 1) * m));
+    EMFA_TRY(csb.alloc(c, sizeof(double) * (size_t)nrhs * m));
+    EMFA_TRY(snb.alloc(c, sizeof(double2) * (size_t)nrhs * m));
+    EMFA_TRY(gb.alloc(c, sizeof(double2) * (size_t)nrhs * (m + 1)));
+    EMFA_TRY(yb.alloc(c, sizeof(double2) * (size_t)nrhs * m));
+    EMFA_TRY(hcb.alloc(c, sizeof(double2) * (size_t)nrhs * (m + 1)));
+    EMFA_TRY(pb.alloc(c, sizeof(double2) * (size_t)nrhs * (m + 1) * nblk));
+    EMFA_TRY(pnb.alloc(c, sizeof(double2) * (size_t)nrhs * nblk));
+    EMFA_TRY(small.alloc(c, sizeof(double) * 4 * (size_t)nrhs + sizeof(int) * 2 * (size_t)nrhs));
+    EMFA_TRY(cnt.alloc(c, sizeof(int) * 4));
+    GmresDev s;
+    s.m = m;
+    s.nrhs = nrhs;
+    s.tol = sp->tol;
+    s.tol_abs = sp->tol_absolute;
+    s.H = dptr<double2>(Hb);
+    s.cs = dptr<double>(csb);
+    s.sn = dptr<double2>(snb);
+    s.g = dptr<double2>(gb);
+    s.y = dptr<double2>(yb);
+    s.hcol = dptr<double2>(hcb);
+    s.bnorm = dptr<double>(small);
+    s.scale = s.bnorm + nrhs;
+    s.est = s.scale + nrhs;
+    s.true_res = s.est + nrhs;
+    s.jlen = reinterpret_cast<int*>(s.true_res + nrhs);
+    s.active = s.jlen + nrhs;
+    s.counters = dptr<int>(cnt);
+    Cx<T>* V = dptr<Cx<T>>(Vb);
+    Cx<T>* W = dptr<Cx<T>>(Wb);
+    double2* R = dptr<double2>(Rb);
+
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, st);
+    EMFA_CUDA(c, cudaMemsetAsync(X, 0, sizeof(double2) * vec, st));
+    int max_cycles = sp->max_iter > 0 ? (sp->max_iter + m - 1) / m : 100;
+    if (prec == EMFA_F32 && sp->max_refine > 0) max_cycles = std::min(max_cycles, sp->max_refine);
+    int total_iters = 0, cycles = 0, converged = 0;
+    int host_cnt[4];
+    for (int cyc = 0; cyc < max_cycles; ++cyc) {
+        // true residual R = B - Z X (X = 0 on the first cycle: R = B)
+        if (cyc == 0) {
+            if (prec == EMFA_F64)
+                EMFA_CUDA(c, cudaMemcpyAsync(R, B, sizeof(double2) * vec, cudaMemcpyDeviceToDevice, st));
+            else
+                k_to_f64<<<grid1(vec), 256, 0, st>>>((const float2*)B, R, vec);
+        } else if (prec == EMFA_F64) {
+            EMFA_TRY(cgemm_f64(c, Z, n, X, n, nrhs, R, st));  // R = Z X
+            k_residual<double2><<<grid1(vec), 256, 0, st>>>((const double2*)B, R, R, vec);
+        } else {
+            k_to_f32<<<grid1(vec), 256, 0, st>>>(X, dptr<float2>(Xt), vec);
+            EMFA_TRY(cgemm_f32_chunked(c, Z, n, Xt.ptr, n, nrhs, B, R, st));  // R = B - Z X
+        }
+        {
+            dim3 grd(nblk, nrhs);
+            k_block_dots<double2, double2><<<grd, KB, 0, st>>>(R, 0, 1, R, n, nrhs, nblk, dptr<double2>(pnb));
+        }
+        EMFA_CUDA(c, cudaMemsetAsync(s.counters, 0, sizeof(int) * 4, st));
+        k_cycle_init<<<(nrhs + 127) / 128, 128, 0, st>>>(s, dptr<double2>(pnb), nblk, cyc == 0);
+        EMFA_CUDA(c, cudaMemcpyAsync(host_cnt, s.counters, sizeof(int) * 4, cudaMemcpyDeviceToHost, st));
+        EMFA_CUDA(c, cudaStreamSynchronize(st));
+        c->kernel_launches += 3;
+        converged = host_cnt[1];
+        if (host_cnt[0] == 0) break;
+        ++cycles;
+        // V0 = R / beta
+        k_scale_store<Cx<T>, double2><<<grid1(vec), 256, 0, st>>>(R, s.scale, n, nrhs, V);
+        int steps = 0;
+        for (int j = 0; j < m; ++j) {
+            Cx<T>* Vj = V + (size_t)j * vec;
+            // W = Z V_j
+            if (prec == EMFA_F64)
+                EMFA_TRY(cgemm_f64(c, Z, n, Vj, n, nrhs, W, st));
+            else
+                EMFA_TRY(cgemm_f32(c, Z, n, Vj, n, nrhs, W, st));
+            // CGS2: h = V^H W; W -= V h; twice
+            EMFA_TRY(dots<T>(c, V, vec, j + 1, W, false, n, nrhs, dptr<double2>(pb), s.hcol, 0, st));
+            k_axpys<T><<<dim3(nblk, nrhs), KB, 0, st>>>(V, vec, j + 1, s.hcol, W, n, nrhs, nblk, dptr<double2>(pnb));
+            EMFA_TRY(dots<T>(c, V, vec, j + 1, W, false, n, nrhs, dptr<double2>(pb), s.y, 0, st));
+            k_axpys<T><<<dim3(nblk, nrhs), KB, 0, st>>>(V, vec, j + 1, s.y, W, n, nrhs, nblk, dptr<double2>(pnb));
+            {
+                // hcol += second-pass coefficients
+                // accumulate: hcol[i][r] += y[i][r]
+                int tot = (j + 1) * nrhs;
+                k_accumulate<<<(tot + 255) / 256, 256, 0, st>>>(s.hcol, s.y, tot);
+            }
+            EMFA_CUDA(c, cudaMemsetAsync(s.counters, 0, sizeof(int), st));
+            k_arnoldi_finish<<<(nrhs + 127) / 128, 128, 0, st>>>(s, j, dptr<double2>(pnb), nblk);
+            k_scale_store<Cx<T>, Cx<T>><<<grid1(vec), 256, 0, st>>>(W, s.scale, n, nrhs, V + (size_t)(j + 1) * vec);
+            EMFA_CUDA(c, cudaMemcpyAsync(host_cnt, s.counters, sizeof(int), cudaMemcpyDeviceToHost, st));
+            EMFA_CUDA(c, cudaStreamSynchronize(st));
+            c->kernel_launches += 8;
+            ++steps;
+            if (host_cnt[0] == 0) break;
+        }
+        total_iters += steps;
+        k_backsolve<<<(nrhs + 127) / 128, 128, 0, st>>>(s);
+        k_update_x<T><<<dim3((n + 255) / 256, nrhs), 256, 0, st>>>(V, vec, steps, s.y, s.jlen, X, n, nrhs);
+        c->kernel_launches += 2;
+        EMFA_CUDA(c, cudaGetLastError());
+    }
+    EMFA_CUDA(c, cudaGetLastError());
+    cudaEventRecord(e1, st);
+    EMFA_CUDA(c, cudaStreamSynchronize(st));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    std::vector<double> tr(nrhs);
+    EMFA_CUDA(c, cudaMemcpy(tr.data(), s.true_res, sizeof(double) * nrhs, cudaMemcpyDeviceToHost));
+    if (info) {
+        info->iterations = total_iters;
+        info->cycles = cycles;
+        info->converged = converged;
+        info->max_rel_residual = *std::max_element(tr.begin(), tr.end());
+        info->seconds = ms * 1e-3;
+    }
+    return converged == nrhs ? EMFA_OK : EMFA_ERR_NOT_CONVERGED;
+}
+
+
+// ---------------------------------------------------------------------------
+// BiCGStab, FP64 vectors, reference update order (iml.cpp:3-39)
+// ---------------------------------------------------------------------------
+struct BicgDev {
+    int nrhs;
+    double tol;
+    double2 *rho0, *rho1, *alpha, *omega, *beta;
+    double* bnorm;
+    double* res;
+    int* active;
+    int* counters;
+};
+
+__device__ __forceinline__ double2 cdiv(double2 a, double2 b)
+{
+    double d = b.x * b.x + b.y * b.y;
+    if (d == 0.0) return make_double2(0.0, 0.0);
+    return make_double2((a.x * b.x + a.y * b.y) / d, (a.y * b.x - a.x * b.y) / d);
+}
+__device__ __forceinline__ double2 cmuld(double2 a, double2 b) { return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+
+// p = r + beta (p - omega v)     (active RHS only)
+__global__ void k_bicg_p(BicgDev s, const double2* __restrict__ r, double2* __restrict__ p, const double2* __restrict__ v, int n)
+{
+    int k = blockIdx.x * blockDim.x + threadIdx.x, q = blockIdx.y;
+    if (k >= n || !s.active[q]) return;
+    size_t o = (size_t)q * n + k;
+    double2 b = s.beta[q], w = s.omega[q];
+    double2 t = make_double2(p[o].x - (w.x * v[o].x - w.y * v[o].y), p[o].y - (w.x * v[o].y + w.y * v[o].x));
+    double2 bt = cmuld(b, t);
+    p[o] = make_double2(r[o].x + bt.x, r[o].y + bt.y);
+}
+
+// x += alpha p ; s = r - alpha v
+__global__ void k_bicg_s(BicgDev s, double2* __restrict__ x, const double2* __restrict__ p, const double2* __restrict__ r,
+                         const double2* __restrict__ v, double2* __restrict__ sv, int n)
+{
+    int k = blockIdx.x * blockDim.x + threadIdx.x, q = blockIdx.y;
+    if (k >= n || !s.active[q]) return;
+    size_t o = (size_t)q * n + k;
+    double2 a = s.alpha[q];
+    double2 ap = cmuld(a, p[o]), av = cmuld(a, v[o]);
+    x[o] = make_double2(x[o].x + ap.x, x[o].y + ap.y);
+    sv[o] = make_double2(r[o].x - av.x, r[o].y - av.y);
+}
+
+// x += omega s ; r = s - omega t
+__global__ void k_bicg_r(BicgDev s, double2* __restrict__ x, const double2* __restrict__ sv, const double2* __restrict__ t,
+                         double2* __restrict__ r, int n)
+{
+    int k = blockIdx.x * blockDim.x + threadIdx.x, q = blockIdx.y;
+    if (k >= n || !s.active[q]) return;
+    size_t o = (size_t)q * n + k;
+    double2 w = s.omega[q];
+    double2 ws = cmuld(w, sv[o]), wt = cmuld(w, t[o]);
+    x[o] = make_double2(x[o].x + ws.x, x[o].y + ws.y);
+    r[o] = make_double2(sv[o].x - wt.x, sv[o].y - wt.y);
+}
+
+// scalar stages; d holds the reduced dot products of the stage
+__global__ void k_bicg_scalar(BicgDev s, int stage, const double2* __restrict__ d0, const double2* __restrict__ d1)
+{
+    int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= s.nrhs) return;
+    if (stage == 0) {  // init: bnorm = ||b||, rho0 = alpha = omega = 1
+        s.bnorm[q] = sqrt(d0[q].x);
+        s.rho0[q] = s.alpha[q] = s.omega[q] = make_double2(1.0, 0.0);
+        s.active[q] = s.bnorm[q] > 0.0;
+        s.res[q] = s.bnorm[q] > 0.0 ? 1.0 : 0.0;
+        return;
+    }
+    if (!s.active[q]) return;
+    if (stage == 1) {  // rho1 = <rhat, r>; beta = (rho1/rho0)(alpha/omega)
+        s.rho1[q] = d0[q];
+        s.beta[q] = cmuld(cdiv(d0[q], s.rho0[q]), cdiv(s.alpha[q], s.omega[q]));
+    } else if (stage == 2) {  // alpha = rho1 / <rhat, v>
+        s.alpha[q] = cdiv(s.rho1[q], d0[q]);
+    } else if (stage == 3) {  // ||s|| / ||b|| test
+        double res = sqrt(d0[q].x) / s.bnorm[q];
+        s.res[q] = res;
+        if (res < s.tol) {
+            s.active[q] = 0;
+            atomicAdd(s.counters + 1, 1);
+        }
+    } else if (stage == 4) {  // omega = <t, s> / <t, t>; rho0 = rho1
+        s.omega[q] = cdiv(d0[q], d1[q]);
+        s.rho0[q] = s.rho1[q];
+        atomicAdd(s.counters, 1);
+    }
+}
+
+template <typename T>
+static emfa_status_t matvec_d(Ctx* c, int prec, const void* Z, int n, const double2* X, int nrhs, double2* Y,
+                              float2* tmp_in, float2* tmp_out, cudaStream_t st)
+{
+    size_t vec = (size_t)n * nrhs;
+    if (prec == EMFA_F64) return cgemm_f64(c, Z, n, X, n, nrhs, Y, st);
+    k_to_f32<<<grid1(vec), 256, 0, st>>>(X, tmp_in, vec);
+    EMFA_TRY(cgemm_f32(c, Z, n, tmp_in, n, nrhs, tmp_out, st));
+    k_to_f64<<<grid1(vec), 256, 0, st>>>(tmp_out, Y, vec);
+    c->kernel_launches += 2;
+    return EMFA_OK;
+}
+
+static emfa_status_t dots_d(Ctx* c, const double2* A, const double2* B, int n, int nrhs, double2* partial, double2* out,
+                            cudaStream_t st)
+{
+    int nblk = dot_blocks(n);
+    k_block_dots<double2, double2><<<dim3(nblk, nrhs), KB, 0, st>>>(A, 0, 1, B, n, nrhs, nblk, partial);
+    k_reduce_partials<<<(nrhs + 127) / 128, 128, 0, st>>>(partial, 1, nrhs, nblk, out, 0);
+    c->kernel_launches += 2;
+    return EMFA_OK;
+}
+
+static emfa_status_t bicgstab(Ctx* c, int prec, const void* Z, int n, const void* B, int nrhs, double2* X,
+                              const emfa_solver_params_t* sp, emfa_solve_info_t* info, cudaStream_t st)
+{
+    const size_t vec = (size_t)n * nrhs;
+    const int nblk = dot_blocks(n);
+    DevBuf vb, tin, tout, sc, pb, db;
+    EMFA_TRY(vb.alloc(c, sizeof(double2) * vec * 6));  // r, rhat, p, v, s, t
+    if (prec == EMFA_F32) {
+        EMFA_TRY(tin.alloc(c, sizeof(float2) * vec));
+        EMFA_TRY(tout.alloc(c, sizeof(float2) * vec));
+    }
+    EMFA_TRY(sc.alloc(c, sizeof(double2) * 5 * nrhs + sizeof(double) * 2 * nrhs + sizeof(int) * (nrhs + 4)));
+    EMFA_TRY(pb.alloc(c, sizeof(double2) * (size_t)nrhs * nblk));
+    EMFA_TRY(db.alloc(c, sizeof(double2) * 2 * nrhs));
+    double2* r = dptr<double2>(vb);
+    double2* rh = r + vec;
+    double2* p = rh + vec;
+    double2* v = p + vec;
+    double2* sv = v + vec;
+    double2* t = sv + vec;
+    BicgDev s;
+    s.nrhs = nrhs;
+    s.tol = sp->tol;
+    s.rho0 = dptr<double2>(sc);
+    s.rho1 = s.rho0 + nrhs;
+    s.alpha = s.rho1 + nrhs;
+    s.omega = s.alpha + nrhs;
+    s.beta = s.omega + nrhs;
+    s.bnorm = reinterpret_cast<double*>(s.beta + nrhs);
+    s.res = s.bnorm + nrhs;
+    s.active = reinterpret_cast<int*>(s.res + nrhs);
+    s.counters = s.active + nrhs;
+    double2* d0 = dptr<double2>(db);
+    double2* d1 = d0 + nrhs;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, st);
+    EMFA_CUDA(c, cudaMemsetAsync(X, 0, sizeof(double2) * vec, st));
+    if (prec == EMFA_F64)
+        EMFA_CUDA(c, cudaMemcpyAsync(r, B, sizeof(double2) * vec, cudaMemcpyDeviceToDevice, st));
+    else
+        k_to_f64<<<grid1(vec), 256, 0, st>>>((const float2*)B, r, vec);
+    EMFA_CUDA(c, cudaMemcpyAsync(rh, r, sizeof(double2) * vec, cudaMemcpyDeviceToDevice, st));
+    EMFA_CUDA(c, cudaMemsetAsync(p, 0, sizeof(double2) * vec * 2, st));  // p, v
+    EMFA_TRY(dots_d(c, r, r, n, nrhs, dptr<double2>(pb), d0, st));
+    k_bicg_scalar<<<(nrhs + 127) / 128, 128, 0, st>>>(s, 0, d0, nullptr);
+    EMFA_CUDA(c, cudaMemsetAsync(s.counters, 0, sizeof(int) * 4, st));
+    const int max_it = sp->max_iter > 0 ? sp->max_iter : 500;
+    dim3 eg((n + 255) / 256, nrhs);
+    int it = 0, hc[4] = {0, 0, 0, 0};
+    int converged = 0;
+    for (; it < max_it; ++it) {
+        EMFA_TRY(dots_d(c, rh, r, n, nrhs, dptr<double2>(pb), d0, st));
+        k_bicg_scalar<<<(nrhs + 127) / 128, 128, 0, st>>>(s, 1, d0, nullptr);
+        k_bicg_p<<<eg, 256, 0, st>>>(s, r, p, v, n);
+        EMFA_TRY(matvec_d<float>(c, prec, Z, n, p, nrhs, v, dptr<float2>(tin), dptr<float2>(tout), st));
+        EMFA_TRY(dots_d(c, rh, v, n, nrhs, dptr<double2>(pb), d0, st));
+        k_bicg_scalar<<<(nrhs + 127) / 128, 128, 0, st>>>(s, 2, d0, nullptr);
+        k_bicg_s<<<eg, 256, 0, st>>>(s, X, p, r, v, sv, n);
+        EMFA_TRY(dots_d(c, sv, sv, n, nrhs, dptr<double2>(pb), d0, st));
+        k_bicg_scalar<<<(nrhs + 127) / 128, 128, 0, st>>>(s, 3, d0, nullptr);
+        EMFA_TRY(matvec_d<float>(c, prec, Z, n, sv, nrhs, t, dptr<float2>(tin), dptr<float2>(tout), st));
+        EMFA_TRY(dots_d(c, t, sv, n, nrhs, dptr<double2>(pb), d0, st));
+        EMFA_TRY(dots_d(c, t, t, n, nrhs, dptr<double2>(pb), d1, st));
+        EMFA_CUDA(c, cudaMemsetAsync(s.counters, 0, sizeof(int), st));
+        k_bicg_scalar<<<(nrhs + 127) / 128, 128, 0, st>>>(s, 4, d0, d1);
+        k_bicg_r<<<eg, 256, 0, st>>>(s, X, sv, t, r, n);
+        c->kernel_launches += 8;
+        EMFA_CUDA(c, cudaMemcpyAsync(hc, s.counters, sizeof(int) * 2, cudaMemcpyDeviceToHost, st));
+        EMFA_CUDA(c, cudaStreamSynchronize(st));
+        converged = hc[1];
+        if (hc[0] == 0) {
+            ++it;
+            break;
+        }
+    }
+    cudaEventRecord(e1, st);
+    EMFA_CUDA(c, cudaStreamSynchronize(st));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    std::vector<double> res(nrhs);
+    EMFA_CUDA(c, cudaMemcpy(res.data(), s.res, sizeof(double) * nrhs, cudaMemcpyDeviceToHost));
+    if (info) {
+        info->iterations = it;
+        info->cycles = 1;
+        info->converged = converged;
+        info->max_rel_residual = *std::max_element(res.begin(), res.end());
+        info->seconds = ms * 1e-3;
+    }
+    return converged == nrhs ? EMFA_OK : EMFA_ERR_NOT_CONVERGED;
+}
+
+emfa_status_t solve_dense(Ctx* c, int prec, const void* Z, int n, const void* B, int nrhs, void* X,
+                          const emfa_solver_params_t* sp, emfa_solve_info_t* info, cudaStream_t st)
+{
+    if (sp->method == EMFA_BICGSTAB) return bicgstab(c, prec, Z, n, B, nrhs, (double2*)X, sp, info, st);
+    if (prec == EMFA_F64) return gmres_t<double>(c, prec, Z, n, B, nrhs, (double2*)X, sp, info, st);
+    return gmres_t<float>(c, prec, Z, n, B, nrhs, (double2*)X, sp, info, st);
+}
+}  // namespace emfa
+
+using namespace emfa;
+
+extern "C" {
+
+emfa_status_t emfa_matvec(emfa_ctx_t* ctx, int prec, int matvec, const void* Z_dev, int n, const void* X_dev, int n_rhs,
+                          void* Y_dev, void* stream)
+{
+    if (!ctx || !Z_dev || !X_dev || !Y_dev || n <= 0 || n_rhs <= 0 || n_rhs > 65535) {
+        set_error(ctx, "emfa_matvec: bad arguments");
+        return EMFA_ERR_INVALID;
+    }
+    EMFA_CUDA(ctx, cudaSetDevice(ctx->device));
+    cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+    if (prec == EMFA_F64) return cgemm_f64(ctx, Z_dev, n, X_dev, n, n_rhs, Y_dev, st);
+    if (prec != EMFA_F32) {
+        set_error(ctx, "emfa_matvec: precision");
+        return EMFA_ERR_INVALID;
+    }
+    if (matvec == EMFA_MV_TF32) return cgemm_tf32(ctx, Z_dev, n, X_dev, n, n_rhs, Y_dev, st);
+    return cgemm_f32(ctx, Z_dev, n, X_dev, n, n_rhs, Y_dev, st);
+}
+
+emfa_status_t emfa_solve(emfa_ctx_t* ctx, int prec, const void* Z_dev, int n, const void* B_dev, int n_rhs,
+                         void* X_dev, const emfa_solver_params_t* sp, emfa_solve_info_t* info, void* stream)
+{
+    if (!ctx || !Z_dev || !B_dev || !X_dev || !sp || n <= 0 || n_rhs <= 0 || n_rhs > 65535 ||
+        (prec != EMFA_F32 && prec != EMFA_F64) || !(sp->tol > 0)) {
+        set_error(ctx, "emfa_solve: bad arguments");
+        return EMFA_ERR_INVALID;
+    }
+    if (sp->method != EMFA_GMRES && sp->method != EMFA_BICGSTAB) {
+        set_error(ctx, "emfa_solve: method must be EMFA_GMRES or EMFA_BICGSTAB");
+        return EMFA_ERR_INVALID;
+    }
+    EMFA_CUDA(ctx, cudaSetDevice(ctx->device));
+    cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+    return solve_dense(ctx, prec, Z_dev, n, B_dev, n_rhs, X_dev, sp, info, st);
+}
+
+}  // extern "C"

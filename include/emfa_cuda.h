@@ -1,0 +1,187 @@
+/*
+ * emfa_cuda.h -- C ABI of libemfa_cuda.so, the GB300 (sm_103a) implementation
+ * of the surface-integral-equation hot path of xiangwei0909/EMFA: EFIE/CFIE
+ * RWG impedance fill, excitation, dense and MLFMA matrix-vector products, the
+ * GMRES/BiCGStab iterations that drive them, and the bistatic/monostatic RCS
+ * far-field reduction.
+ *
+ * Plain C: opaque handles, plain pointers and sizes, an emfa_status_t return
+ * on every call (no exceptions cross the boundary), and an explicit CUDA
+ * stream (passed as void*, a cudaStream_t; NULL = the context's stream).
+ * "dev" pointers are device memory, "host" pointers host memory.  Complex
+ * arrays are interleaved (re, im): complex64 for EMFA_F32, complex128 for
+ * EMFA_F64.  Vectors of several right-hand sides are stored RHS-major:
+ * element (r, u) at r * n + u.
+ *
+ * Each entry point names the reference interface it replaces (file:line in
+ * the reference project).
+ */
+#ifndef EMFA_CUDA_H
+#define EMFA_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    EMFA_OK = 0,
+    EMFA_ERR_INVALID = 1,       /* bad argument; reference: component::ConfigInvalid */
+    EMFA_ERR_CUDA = 2,          /* CUDA runtime error; reference: std::runtime_error */
+    EMFA_ERR_OOM = 3,           /* device allocation refused (HBM budget)            */
+    EMFA_ERR_NOT_CONVERGED = 4, /* Krylov iteration cap reached (reference logs a warning) */
+    EMFA_ERR_MESH = 5,          /* mesh not usable; reference: component::FileError  */
+    EMFA_ERR_UNSUPPORTED = 6,
+    EMFA_ERR_TIMEOUT = 7        /* a device-side wait gave up                        */
+} emfa_status_t;
+
+typedef enum { EMFA_F32 = 0, EMFA_F64 = 1 } emfa_precision_t;
+typedef enum { EMFA_EFIE = 0, EMFA_CFIE = 1 } emfa_kind_t;
+typedef enum { EMFA_GMRES = 0, EMFA_BICGSTAB = 1 } emfa_method_t;
+typedef enum {
+    EMFA_MV_AUTO = 0,  /* F64: FP64 SIMT; F32: tensor-core TF32 inner, FP32 residual */
+    EMFA_MV_F64 = 1,   /* FP64 complex GEMM on CUDA cores (plain path)               */
+    EMFA_MV_F32 = 2,   /* FP32 complex GEMM on CUDA cores                             */
+    EMFA_MV_TF32 = 3   /* tcgen05 TF32 complex GEMM, FP32 accumulation               */
+} emfa_matvec_t;
+
+typedef struct emfa_ctx emfa_ctx_t;
+typedef struct emfa_geom emfa_geom_t;
+typedef struct emfa_mlfma emfa_mlfma_t;
+
+/* Fill parameters: one frequency, one formulation.  Mirrors the members the
+ * reference solvers take from ConfigLoader (EMSolver/EFIE.cpp:25-52,
+ * EMSolver/CFIE.cpp:25-51). */
+typedef struct {
+    int kind;           /* emfa_kind_t                                              */
+    int precision;      /* EMFA_F32: FP32 regular pairs + FP64 singular self terms; */
+                        /* EMFA_F64: everything FP64 (the plain path)               */
+    double freq;        /* Hz; k = 2 pi f / c0 in the fill's precision              */
+    double alpha;       /* CFIE combination coefficient (alpha:)                    */
+    double sigma_re;    /* EFIE surface-impedance term (Sigma:), 0 for PEC          */
+    double sigma_im;
+    int edm_mode;       /* EFIE pairs farther than 3 lambda: 0 = zero, as in the    */
+                        /* matrix the reference solves; 1 = equivalent-dipole value;*/
+                        /* 2 = ordinary quadrature (no far-pair branch)             */
+} emfa_fill_params_t;
+
+typedef struct {
+    int method;         /* emfa_method_t                                            */
+    int restart;        /* GMRES restart length m (reference: 30)                   */
+    int max_iter;       /* cap on inner iterations per right-hand side              */
+    double tol;         /* stop when ||b - Z x|| / ||b|| < tol (or absolute, below) */
+    int tol_absolute;   /* 1: ||b - Z x|| < tol, the reference GMRES criterion      */
+    int matvec;         /* emfa_matvec_t                                            */
+    int max_refine;     /* outer true-residual cycles for EMFA_F32 (GMRES-IR)       */
+} emfa_solver_params_t;
+
+typedef struct {
+    int iterations;         /* inner iterations performed (max over RHS)            */
+    int cycles;             /* outer (restart / refinement) cycles                  */
+    int converged;          /* number of RHS that met the tolerance                 */
+    double max_rel_residual;/* max over RHS of the last true residual ||b-Zx||/||b||*/
+    double seconds;         /* device time of the solve                             */
+} emfa_solve_info_t;
+
+/* ---- status and context -------------------------------------------------- */
+const char* emfa_status_string(emfa_status_t s);
+/* Last error message recorded on ctx (or the process-wide one if ctx NULL). */
+const char* emfa_last_error(const emfa_ctx_t* ctx);
+const char* emfa_version(void);
+
+/* Creates a context on a CUDA device with an HBM budget (0 = unlimited).
+ * Replaces the per-solver resource set-up of EM::init (EMSolver/EM.cpp:24-67)
+ * and the MLFMA ThreadPool::init (EMComponent/ThreadPool.cpp:19-29). */
+emfa_status_t emfa_ctx_create(int device, size_t hbm_budget_bytes, emfa_ctx_t** out);
+emfa_status_t emfa_ctx_destroy(emfa_ctx_t* ctx);
+/* Bytes currently held / peak / budget. */
+emfa_status_t emfa_ctx_memory(const emfa_ctx_t* ctx, size_t* used, size_t* peak, size_t* budget);
+/* Kernels launched through this context since creation. */
+emfa_status_t emfa_ctx_launch_count(const emfa_ctx_t* ctx, int64_t* count);
+emfa_status_t emfa_ctx_synchronize(emfa_ctx_t* ctx);
+/* The context's own CUDA stream (a cudaStream_t), used when a call gets NULL. */
+emfa_status_t emfa_ctx_stream(const emfa_ctx_t* ctx, void** stream);
+
+/* ---- geometry ------------------------------------------------------------- */
+/* RWG table of a closed or open triangle mesh, host only (no GPU).  Rows of 6
+ * ints: v1 v2 vxp vxm tp tm, in the reference's order and orientation.
+ * Replaces CommonEdge::buildCommonEdge (EMComponent/CommonEdge.cpp:74-106,
+ * 704-743).  Returns EMFA_ERR_INVALID if capacity rows are too few. */
+emfa_status_t emfa_build_rwg(const int* tris_host, int n_tri, int* rwg_host, int capacity, int* n_rwg);
+
+/* Uploads a mesh and its RWG table (host arrays: verts V x 3 double, tris
+ * T x 3 int 0-based, rwg N x 6 int).  Replaces the Mesh / CommonEdge members
+ * the solvers own (EMSolver/EFIE.h:69-70). */
+emfa_status_t emfa_geom_create(emfa_ctx_t* ctx, const double* verts_host, int n_vert, const int* tris_host,
+                               int n_tri, const int* rwg_host, int n_rwg, emfa_geom_t** out);
+emfa_status_t emfa_geom_destroy(emfa_geom_t* geom);
+emfa_status_t emfa_geom_size(const emfa_geom_t* geom, int* n_vert, int* n_tri, int* n_rwg);
+
+/* ---- fill ------------------------------------------------------------------ */
+/* Dense impedance matrix, row-major N x N (row = testing RWG f, column =
+ * source RWG s) with leading dimension ldz (elements).  Replaces
+ * EFIE::fillZ (EMSolver/EFIE.cpp:603-696) and CFIE::fillZ
+ * (EMSolver/CFIE.cpp:485-568) with their pair kernels (EFIE.cpp:139-566,
+ * EMSolver/Miscellaneous.cpp:6-77). */
+emfa_status_t emfa_fill_z(emfa_ctx_t* ctx, emfa_geom_t* geom, const emfa_fill_params_t* p, void* Z_dev,
+                          size_t ldz, void* stream);
+
+/* Excitation for n_inc plane waves given as (theta, phi, pole) degrees
+ * triples (host array), V is n_inc x N.  Replaces EFIE::fillV / eVKernel
+ * (EMSolver/EFIE.cpp:568-601,698-722) and CFIE::fillV / cfieVKernel
+ * (EMSolver/CFIE.cpp:570-597, EMSolver/Miscellaneous.cpp:152-189), with the
+ * incidence vectors of EM::init (EMSolver/EM.cpp:33-38). */
+emfa_status_t emfa_fill_v(emfa_ctx_t* ctx, emfa_geom_t* geom, const emfa_fill_params_t* p,
+                          const double* angles_host, int n_inc, void* V_dev, void* stream);
+
+/* ---- dense products and solvers -------------------------------------------- */
+/* Y = Z X for n_rhs vectors (X, Y are n_rhs x n).  Z in precision prec; the
+ * vectors are complex128 for EMFA_F64 and complex64 for EMFA_F32.  Replaces
+ * the dense products `_A * p1` of iml::BICGSTAB / iml::GMRES
+ * (EMIterative/iml.cpp:22,29,186). */
+emfa_status_t emfa_matvec(emfa_ctx_t* ctx, int prec, int matvec, const void* Z_dev, int n, const void* X_dev,
+                          int n_rhs, void* Y_dev, void* stream);
+
+/* Solves Z X = B for n_rhs right-hand sides (B complex64 for EMFA_F32,
+ * complex128 for EMFA_F64; X always complex128, n_rhs x n).  GMRES(m) or
+ * BiCGStab, all right-hand sides in lockstep with one multi-RHS product per
+ * step.  For EMFA_F32 the inner products run in reduced precision and each
+ * restart recomputes the true residual (iterative refinement); Arnoldi,
+ * Givens rotations and norms are FP64.  Replaces iml::GMRES
+ * (EMIterative/iml.cpp:156-207) and iml::BICGSTAB (EMIterative/iml.cpp:3-39). */
+emfa_status_t emfa_solve(emfa_ctx_t* ctx, int prec, const void* Z_dev, int n, const void* B_dev, int n_rhs,
+                         void* X_dev, const emfa_solver_params_t* sp, emfa_solve_info_t* info, void* stream);
+
+/* ---- far field -------------------------------------------------------------- */
+/* RCS in dBsm for currents I (complex128, n_rhs x N) and scattering
+ * directions (host, unit vectors).  per_rhs_dirs = 0: dirs is n_dir x 3,
+ * shared by all RHS (bistatic); 1: dirs is n_rhs x n_dir x 3 (e.g. the
+ * monostatic direction of each incidence).  out_host is n_rhs x n_dir.
+ * Replaces EFIE::getBiRCS (EMSolver/EFIE.cpp:788-832), CFIE::getBiRCS
+ * (EMSolver/CFIE.cpp:643-685) and MLFMA::getBiRCS (EMSolver/MLFMA.cpp:1573-1620)
+ * as called by Result::getBistaticRCS / getMonostaticRCS
+ * (EMComponent/Result.h:47-155). */
+emfa_status_t emfa_rcs(emfa_ctx_t* ctx, emfa_geom_t* geom, const emfa_fill_params_t* p, const void* I_dev,
+                       int n_rhs, const double* dirs_host, int n_dir, int per_rhs_dirs, double* out_host,
+                       void* stream);
+
+/* ---- end to end ------------------------------------------------------------- */
+/* One dense RCS job from host buffers: RWG table, upload, fill, excitation for
+ * n_inc incidences, multi-RHS solve, RCS.  rcs_dirs_host/per_rhs_dirs as in
+ * emfa_rcs; rcs_out_host is n_inc x n_dir dBsm; I_out_host (optional,
+ * complex128 n_inc x N) receives the currents.  This is what
+ * solver::invoke_solver<EFIE|CFIE> (EMSolver/Solver.h:20-29) runs:
+ * init -> solve -> output. */
+emfa_status_t emfa_dense_rcs(emfa_ctx_t* ctx, const double* verts_host, int n_vert, const int* tris_host,
+                             int n_tri, const emfa_fill_params_t* fp, const double* angles_host, int n_inc,
+                             const emfa_solver_params_t* sp, const double* rcs_dirs_host, int n_dir,
+                             int per_rhs_dirs, double* rcs_out_host, double* I_out_host,
+                             emfa_solve_info_t* info);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* EMFA_CUDA_H */

@@ -28,6 +28,16 @@
 #endif
 
 typedef REAL r_t;
+
+/* The reference calls sin/cos/log/atan/log10 unqualified on float arguments;
+ * under g++ these bind to the C double functions, the float argument is
+ * widened and the double result rounds back where it meets a float.  The
+ * oracle does the same (std::exp of complex<float> and std::sqrt stay float). */
+#define DSIN(x) sin((double)(x))
+#define DCOS(x) cos((double)(x))
+#define DLOG(x) log((double)(x))
+#define DATAN(x) atan((double)(x))
+#define DLOG10(x) log10((double)(x))
 typedef struct { r_t re, im; } cx;
 typedef struct { r_t x, y, z; } v3;
 typedef struct { cx x, y, z; } c3;
@@ -237,11 +247,11 @@ static cx efie_singular(r_t k, cx sigma, const v3* vf3, const v3* vs3, v3 vf, v3
             if ((double)p0 < 1e-10) continue; /* float compared with a double literal */
             v3 pi = vnormalize(vsub(vsub(rou_p, rou), vmul(l1, lp)));
             r_t r02 = p0 * p0 + d * d;
-            r_t lg = log((rp + lp) / (rm + lm));
-            Is1 = vadd(Is1, vmul(vmul(ui, (r_t)0.5), r02 * lg + (lp * rp) - (lm * rm)));
+            double lg = DLOG((rp + lp) / (rm + lm));
+            Is1 = vadd(Is1, vmul(vmul(ui, (r_t)0.5), (r_t)((double)r02 * lg + (double)(lp * rp) - (double)(lm * rm))));
             r_t ad = fabs(d);
-            Is2 += vdot(pi, ui) *
-                   ((p0 * lg) - ad * (atan((p0 * lp) / (r02 + ad * rp)) - atan((p0 * lm) / (r02 + ad * rm))));
+            Is2 = (r_t)((double)Is2 + (double)vdot(pi, ui) *
+                   (((double)p0 * lg) - (double)ad * (DATAN((p0 * lp) / (r02 + ad * rp)) - DATAN((p0 * lm) / (r02 + ad * rm)))));
         }
         v3 rfp = vsub(vgf[p], vf); /* unsigned field rho */
         r_t dotv = vdot(rfp, vadd(Is1, vmul(vsub(vgf[p], vs), Is2)));
@@ -385,9 +395,9 @@ static cx cfie_singular(r_t alpha, r_t k, const v3* vf3, const v3* vs3, v3 vf, v
             v3 sj0 = vadd(vs3[i], vmul(Li, vdot(vsub(vgf[p], vs3[i]), Li)));
             r_t P0 = vnorm(vsub(sj0, vgf[p]));
             if (P0 > (r_t)1e-10) {
-                r_t s = w * ((r_t)0.25 * vdot(rf, rs) - (fs * ss) / (k * k)) * P0 *
-                        log((Rp + Lp) / (Rm + Lm));
-                Ze2 = cadd(Ze2, C(s, 0));
+                double s = (double)(w * ((r_t)0.25 * vdot(rf, rs) - (fs * ss) / (k * k)) * P0) *
+                           DLOG((Rp + Lp) / (Rm + Lm));
+                Ze2 = cadd(Ze2, C((r_t)s, 0));
             }
         }
         v3 rf2 = vmul(vsub(vgf[p], vf), fs);
@@ -523,7 +533,7 @@ void PFX(rcs)(const r_t* verts, const int* tris, const int* rwg, const r_t* len,
             }
             c3 es = vcrossc(vmul(sk, (r_t)0.5), vcrossc(sk, Es));
             r_t rcs = Z0_ * Z0_ * k * k * c3norm2(es) / PI4_;
-            out[(size_t)a * n_dir + d] = (r_t)10 * log10(rcs);
+            out[(size_t)a * n_dir + d] = (r_t)(10 * DLOG10(rcs));
         }
     }
 }
@@ -555,9 +565,10 @@ void PFX(incidence)(r_t theta_deg, r_t phi_deg, r_t pole_deg, r_t* out9)
 {
     r_t d2r = PI_ / (r_t)180;
     r_t pol = pole_deg * d2r, th = theta_deg * d2r, ph = phi_deg * d2r;
-    v3 kk = V(-sin(th) * cos(ph), -sin(th) * sin(ph), -cos(th));
-    v3 ee = V(-cos(pol) * cos(th) * cos(ph) - sin(pol) * sin(ph),
-              -cos(pol) * cos(th) * sin(ph) + sin(pol) * cos(ph), cos(pol) * sin(th));
+    /* EM.cpp:33-34: products of the double-valued sin/cos, rounded once */
+    v3 kk = V((r_t)(-DSIN(th) * DCOS(ph)), (r_t)(-DSIN(th) * DSIN(ph)), (r_t)(-DCOS(th)));
+    v3 ee = V((r_t)(-DCOS(pol) * DCOS(th) * DCOS(ph) - DSIN(pol) * DSIN(ph)),
+              (r_t)(-DCOS(pol) * DCOS(th) * DSIN(ph) + DSIN(pol) * DCOS(ph)), (r_t)(DCOS(pol) * DSIN(th)));
     v3 hh = vcross(kk, ee);
     r_t o[9] = {kk.x, kk.y, kk.z, ee.x, ee.y, ee.z, hh.x, hh.y, hh.z};
     memcpy(out9, o, sizeof o);

@@ -1,0 +1,125 @@
+"""Pins of the oracle restatement (oracle/emfa_oracle.c): against the golden
+vectors the reference itself produced (tests/golden/, always), and against the
+reference binary run live when it was built here (oracle/_ref)."""
+import os
+import tempfile
+
+import numpy as np
+import pytest
+
+from conftest import load_golden
+from emfa_gb300 import mesh as M
+
+
+def floored_rel(a, b, floor=1e-3):
+    """|a - b| / max(|b|, floor * max|b|): the per-entry Z metric (a zero-by-
+    symmetry entry is compared against a floor, not against itself)."""
+    return np.abs(a - b) / np.maximum(np.abs(b), floor * np.abs(b).max())
+
+
+def cfg_float(v):
+    """Config values reach the reference through std::stof (ConfigLoader.cpp),
+    float precision even in the FP64 build."""
+    return float(np.float32(float(v)))
+
+
+def geometry(O, g, prec):
+    dt = np.float32 if prec == 32 else np.float64
+    return O.Geometry(g["verts"].astype(dt), g["tris"], g["rwg"], prec)
+
+
+@pytest.mark.parametrize("name", ["sphere1_efie", "sphere1_cfie", "cube2_efie_edm", "ellipsoid3_cfie", "sphere2_cfie"])
+def test_rwg_table_matches_reference(oracle_mod, name):
+    g = load_golden(name)
+    assert np.array_equal(oracle_mod.build_rwg(g["tris"]), g["rwg"])
+
+
+@pytest.mark.parametrize("name", ["sphere1_efie", "sphere1_cfie", "cube2_efie_edm", "ellipsoid3_cfie", "sphere2_cfie"])
+@pytest.mark.parametrize("prec", [32, 64])
+def test_fill_matches_reference(oracle_mod, name, prec):
+    O = oracle_mod
+    g = load_golden(name)
+    meta = g["meta"]
+    tag = "f32" if prec == 32 else "f64"
+    geo = geometry(O, g, prec)
+    freq = float(meta["frequency"])
+    k = O.wavenumber(freq, prec)
+    inc = O.incidence(float(meta.get("theta", 0)), float(meta.get("phi", 0)), float(meta.get("pole", 0)), prec)
+    assert np.array_equal(inc, g["inc_" + tag][:9])
+    assert k == g["inc_" + tag][9]
+    if meta["solver"] == "efie":
+        thr = (np.float32 if prec == 32 else np.float64)(3.0 * 299792458.0 / freq)
+        Z = O.fill_z_efie(geo, k, threshold_edm=thr, edm_mode=0)
+    else:
+        Z = O.fill_z_cfie(geo, k, cfg_float(meta["alpha"]))
+    if "Z_" + tag in g:
+        Zr = g["Z_" + tag]
+    else:
+        Zr = g["Zrows_" + tag]
+        Z = Z[: Zr.shape[0]]
+    rel = floored_rel(Z, Zr)
+    if prec == 64:
+        assert rel.max() < 1e-12, rel.max()       # FP64: same operations, same order
+    else:
+        assert rel.max() < 2e-6, rel.max()         # FP32: a few ulps (libm vs. glibc cexpf paths)
+        assert np.mean(Z == Zr) > 0.95
+    V = O.fill_v(geo, k, inc, cfie=meta["solver"] == "cfie", alpha=cfg_float(meta.get("alpha", 1)))[0]
+    tolv = 1e-14 if prec == 64 else 1e-6
+    assert np.abs(V - g["V_" + tag]).max() <= tolv * np.abs(g["V_" + tag]).max()
+    if "I_" + tag in g:
+        r = O.rcs(geo, k, g["I_" + tag], g["rcs_dirs_" + tag])[0]
+        assert np.abs(r - g["rcs_" + tag]).max() < (1e-9 if prec == 64 else 1e-4)
+
+
+def test_edm_far_pairs(oracle_mod):
+    """EFIE pairs beyond 3 lambda: zero in the solved matrix, EDM value in the
+    Armadillo copy (EMSolver/EFIE.cpp:648-651,691)."""
+    O = oracle_mod
+    g = load_golden("cube2_efie_edm")
+    for prec, tag in ((32, "f32"), (64, "f64")):
+        geo = geometry(O, g, prec)
+        k = O.wavenumber(3e8, prec)
+        thr = (np.float32 if prec == 32 else np.float64)(3.0 * 299792458.0 / 3e8)
+        Z0 = O.fill_z_efie(geo, k, threshold_edm=thr, edm_mode=0)
+        Z1 = O.fill_z_efie(geo, k, threshold_edm=thr, edm_mode=1)
+        far = g["Z_" + tag] == 0
+        assert far.sum() > 0
+        assert np.all(Z0[far] == 0)
+        rel = floored_rel(Z1, g["Zarma_" + tag])
+        assert rel.max() < (1e-5 if prec == 32 else 1e-10), rel.max()
+
+
+def test_golden_solution_is_a_solution():
+    """The reference's iterated current solves its own system to its tolerance."""
+    for name in ("sphere1_efie", "sphere1_cfie"):
+        g = load_golden(name)
+        Z, V, I = g["Z_f64"], g["V_f64"], g["I_f64"]
+        Is = np.linalg.solve(Z, V)
+        assert np.linalg.norm(I - Is) / np.linalg.norm(Is) < 1e-2
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(os.path.dirname(__file__), "..", "oracle", "_ref", "emfa_ref_f32")),
+                    reason="reference binary not built here")
+@pytest.mark.parametrize("solver", ["efie", "cfie"])
+def test_oracle_vs_live_reference(oracle_mod, solver):
+    """A mesh the fixtures do not hold, run through the reference itself."""
+    O = oracle_mod
+    mesh = M.ellipsoid(2, (0.35, 0.5, 0.3))
+    tmp = tempfile.mkdtemp()
+    nas = os.path.join(tmp, "e.nas")
+    M.write_nas(mesh, nas)
+    cfg = os.path.join(tmp, "c.yml")
+    M.write_config(cfg, EMSolver=solver.upper(), mesh_path=nas, frequency="4e8", alpha="0.6", theta="60",
+                   phi="10", pole="90")
+    for prec in (32, 64):
+        out = os.path.join(tmp, "o%d" % prec)
+        O.run_reference(solver, cfg, out, -1, prec=prec)
+        d = O.load_dump(out, prec)
+        geo = O.Geometry(d["verts"], d["tris"], d["rwg"], prec)
+        k = O.wavenumber(4e8, prec)
+        Z = O.fill_z_efie(geo, k) if solver == "efie" else O.fill_z_cfie(geo, k, cfg_float(0.6))
+        rel = floored_rel(Z, d["Z"])
+        assert rel.max() < (1e-12 if prec == 64 else 2e-6)
+        inc = O.incidence(60, 10, 90, prec)
+        V = O.fill_v(geo, k, inc, cfie=solver == "cfie", alpha=cfg_float(0.6))[0]
+        assert np.abs(V - d["V"]).max() <= (1e-14 if prec == 64 else 1e-6) * np.abs(d["V"]).max()
