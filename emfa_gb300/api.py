@@ -118,6 +118,7 @@ def fill_z(geom: Geometry, fp: L.FillParams, out=None):
     dt = torch.complex128 if fp.precision == L.EMFA_F64 else torch.complex64
     n = geom.n
     Z = out if out is not None else torch.empty((n, n), dtype=dt, device="cuda:%d" % geom.ctx.device)
+    torch.cuda.current_stream().synchronize()
     geom.ctx.check(L.lib().emfa_fill_z(geom.ctx.h, geom.h, ctypes.byref(fp), _ptr(Z), Z.stride(0), None))
     return Z
 
@@ -138,7 +139,9 @@ def matvec(ctx: Context, Z, X, matvec="auto"):
     prec = L.EMFA_F64 if Z.dtype == torch.complex128 else L.EMFA_F32
     mv = {"auto": 0, "f64": 1, "f32": 2, "tf32": 3}[matvec]
     Y = torch.empty_like(X)
+    torch.cuda.current_stream().synchronize()  # inputs written on torch's stream
     ctx.check(L.lib().emfa_matvec(ctx.h, prec, mv, _ptr(Z), Z.shape[0], _ptr(X), X.shape[0], _ptr(Y), None))
+    ctx.synchronize()  # the product runs on the context's stream
     return Y
 
 
@@ -148,6 +151,7 @@ def solve(ctx: Context, Z, B, sp: L.SolverParams):
     torch = _torch()
     prec = L.EMFA_F64 if Z.dtype == torch.complex128 else L.EMFA_F32
     X = torch.empty(B.shape, dtype=torch.complex128, device=B.device)
+    torch.cuda.current_stream().synchronize()
     info = L.SolveInfo()
     st = L.lib().emfa_solve(ctx.h, prec, _ptr(Z), Z.shape[0], _ptr(B), B.shape[0], _ptr(X), ctypes.byref(sp),
                             ctypes.byref(info), None)
@@ -157,6 +161,7 @@ def solve(ctx: Context, Z, B, sp: L.SolverParams):
 
 
 def rcs(geom: Geometry, fp: L.FillParams, I, dirs, per_rhs=False) -> np.ndarray:
+    _torch().cuda.current_stream().synchronize()
     d = np.ascontiguousarray(dirs, dtype=np.float64)
     n_rhs = I.shape[0]
     n_dir = d.shape[-2] if d.ndim == 3 else d.shape[0]

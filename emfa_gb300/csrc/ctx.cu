@@ -6,13 +6,23 @@
 
 namespace emfa {
 
-static std::mutex g_err_mu;
-static std::string g_last_error;
+// Process-wide error state, never destroyed: entry points may run from
+// interpreter or static teardown, after ordinary statics are gone.
+static std::mutex& err_mu()
+{
+    static std::mutex* m = new std::mutex;
+    return *m;
+}
+static std::string& last_error_global()
+{
+    static std::string* s = new std::string;
+    return *s;
+}
 
 void set_global_error(const std::string& msg)
 {
-    std::lock_guard<std::mutex> g(g_err_mu);
-    g_last_error = msg;
+    std::lock_guard<std::mutex> g(err_mu());
+    last_error_global() = msg;
 }
 
 void set_error(Ctx* ctx, const std::string& msg)
@@ -51,6 +61,17 @@ emfa_status_t ctx_alloc(Ctx* c, size_t bytes, void** p)
     return EMFA_OK;
 }
 
+emfa_status_t ctx_workspace(Ctx* c, int slot, size_t bytes, void** p)
+{
+    DevBuf& b = c->ws[slot];
+    if (b.bytes < bytes) {
+        if (b.ptr) cudaDeviceSynchronize();  // the old buffer may still be in use
+        EMFA_TRY(b.alloc(c, bytes));
+    }
+    *p = b.ptr;
+    return EMFA_OK;
+}
+
 void ctx_free(Ctx* c, void* p, size_t bytes)
 {
     if (!p) return;
@@ -83,7 +104,7 @@ const char* emfa_status_string(emfa_status_t s)
 const char* emfa_last_error(const emfa_ctx_t* ctx)
 {
     if (ctx) return ctx->last_error.c_str();
-    return g_last_error.c_str();
+    return last_error_global().c_str();
 }
 
 const char* emfa_version(void) { return "emfa_gb300 0.1 (sm_103a)"; }
@@ -129,6 +150,7 @@ emfa_status_t emfa_ctx_destroy(emfa_ctx_t* ctx)
         cudaStreamSynchronize(ctx->stream);
         cudaStreamDestroy(ctx->stream);
     }
+    for (auto& b : ctx->ws) b.release();
     delete ctx;
     return EMFA_OK;
 }
@@ -145,7 +167,7 @@ emfa_status_t emfa_ctx_memory(const emfa_ctx_t* ctx, size_t* used, size_t* peak,
 emfa_status_t emfa_ctx_launch_count(const emfa_ctx_t* ctx, int64_t* count)
 {
     if (!ctx || !count) return EMFA_ERR_INVALID;
-    *count = ctx->kernel_launches;
+    *count = (int64_t)ctx->kernel_launches;
     return EMFA_OK;
 }
 

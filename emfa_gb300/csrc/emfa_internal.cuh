@@ -38,20 +38,8 @@ void set_global_error(const std::string& msg);
     } while (0)
 
 // ---------------------------------------------------------------------------
-// context: device, stream, HBM budget accounting
+// context: device, stream, HBM budget accounting, reusable workspaces
 // ---------------------------------------------------------------------------
-struct Ctx {
-    int device = 0;
-    size_t budget = 0;      // bytes the context may hold (0 = unlimited)
-    size_t used = 0;
-    size_t peak = 0;
-    cudaStream_t stream = nullptr;
-    std::string last_error;
-    std::mutex mu;
-    int sm_count = 0;
-    int kernel_launches = 0;  // kernels launched through this context
-};
-
 emfa_status_t ctx_alloc(Ctx* c, size_t bytes, void** p);
 void ctx_free(Ctx* c, void* p, size_t bytes);
 
@@ -82,6 +70,39 @@ struct DevBuf {
 };
 
 template <typename T> inline T* dptr(const DevBuf& b) { return reinterpret_cast<T*>(b.ptr); }
+
+// Workspace slots: buffers a context keeps between calls so repeated fills,
+// products and solves do not allocate.  A slot grows when a call needs more.
+enum WorkspaceSlot { WS_GEMM_B = 0, WS_GEMM_ERR, WS_KRYLOV, WS_FILL, WS_RCS, WS_COUNT };
+
+struct Ctx {
+    int device = 0;
+    size_t budget = 0;      // bytes the context may hold (0 = unlimited)
+    size_t used = 0;
+    size_t peak = 0;
+    cudaStream_t stream = nullptr;
+    std::string last_error;
+    std::mutex mu;
+    int sm_count = 0;
+    long long kernel_launches = 0;  // kernels launched through this context
+    DevBuf ws[WS_COUNT];            // declared after mu: destroyed before it
+};
+
+emfa_status_t ctx_workspace(Ctx* c, int slot, size_t bytes, void** p);
+
+// carve 256-byte aligned sub-buffers out of one workspace
+struct Carver {
+    char* base;
+    size_t off = 0;
+    template <typename T> T* take(size_t count)
+    {
+        off = (off + 255) & ~(size_t)255;
+        T* p = reinterpret_cast<T*>(base + off);
+        off += sizeof(T) * count;
+        return p;
+    }
+    static size_t round(size_t b) { return (b + 255) & ~(size_t)255; }
+};
 
 // ---------------------------------------------------------------------------
 // geometry: host copy + per-precision device pack

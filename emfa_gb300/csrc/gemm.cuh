@@ -17,6 +17,8 @@ emfa_status_t cgemm_f32_chunked(Ctx* c, const void* Z, size_t ldz, const void* X
 namespace emfa {
 // Y = Z X on the tensor cores (tcgen05, TF32 operands, FP32 accumulation).
 emfa_status_t cgemm_tf32(Ctx* c, const void* Z, size_t ldz, const void* X, int n, int nrhs, void* Y, cudaStream_t st);
+// reads the tensor-core GEMM's error word (synchronises the stream)
+emfa_status_t gemm_check_error(Ctx* c, cudaStream_t st);
 // dense multi-RHS solve (krylov.cu)
 emfa_status_t solve_dense(Ctx* c, int prec, const void* Z, int n, const void* B, int nrhs, void* X,
                           const emfa_solver_params_t* sp, emfa_solve_info_t* info, cudaStream_t st);

@@ -1,13 +1,357 @@
-// Tensor-core (tcgen05) multi-RHS complex product -- see below.
+// Multi-RHS complex product on the 5th-generation tensor cores (tcgen05,
+// TF32 operands, FP32 accumulation in tensor memory).
+//
+//   Y[r][f] = sum_k Z[f][k] X[r][k]        (complex, Z row-major N x N)
+//
+// as one real GEMM C = A B^T with
+//   A = Z viewed as an N x 2N float matrix (re, im interleaved along k),
+//   B rows 2r   = (Re x, -Im x) interleaved  -> C[f][2r]   = Re Y[r][f]
+//   B rows 2r+1 = (Im x,  Re x) interleaved  -> C[f][2r+1] = Im Y[r][f]
+// so Z is read straight from its complex64 storage and the accumulator's
+// column pairs are the complex outputs.
+//
+// Kernel: one 128 x BN output tile per CTA, 6 warps:
+//   warp 0      TMA producer: A (128 x 32) and B (BN x 32) fp32 tiles, 128-byte
+//               swizzle, into a 4-stage shared-memory ring (mbarrier tx count)
+//   warp 1      allocates tensor memory; one lane issues tcgen05.mma
+//               (M = 128, N = BN, K = 8 per instruction, 4 per stage) and
+//               tcgen05.commit frees each stage / signals the accumulator
+//   warps 2..5  epilogue: tcgen05.ld 32 lanes x 16 columns per warp, writes the
+//               complex64 outputs (consecutive lanes = consecutive f: coalesced)
+// Every mbarrier wait is bounded (clock64); on timeout the kernel records an
+// error code, drains its own copies and MMAs (bounded), frees tensor memory
+// and returns, and the host reports EMFA_ERR_TIMEOUT.
 #include "emfa_internal.cuh"
 #include "gemm.cuh"
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 namespace emfa {
 
-emfa_status_t cgemm_tf32(Ctx* c, const void*, size_t, const void*, int, int, void*, cudaStream_t)
+namespace tc {
+
+constexpr int BM = 128;
+constexpr int BK = 32;          // fp32 elements per stage row = 128 bytes = one swizzle atom
+constexpr int STAGES = 4;
+constexpr int THREADS = 192;
+constexpr long long WAIT_CYCLES = 4000000000LL;  // ~2 s at 2 GHz
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
 {
-    set_error(c, "cgemm_tf32: tensor-core path not built yet");
-    return EMFA_ERR_UNSUPPORTED;
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// bounded wait; on timeout records `code` in *err and returns false
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err, int code)
+{
+    if (mbar_try_wait(bar, parity)) return true;
+    long long t0 = clock64();
+    while (!mbar_try_wait(bar, parity)) {
+        if (clock64() - t0 > WAIT_CYCLES) {
+            atomicCAS(err, 0, code);
+            return false;
+        }
+    }
+    return true;
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];"
+        ::"r"(smem_u32(dst)), "l"((uint64_t)map), "r"(smem_u32(bar)), "r"(x), "r"(y)
+        : "memory");
+}
+
+// Shared-memory matrix descriptor: K-major tile, 128-byte swizzle, rows of
+// 128 bytes, 8-row core groups 1024 bytes apart.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr)
+{
+    uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFF);
+    d |= (uint64_t)1 << 16;              // leading byte offset (unused for swizzled K-major)
+    d |= (uint64_t)(1024 >> 4) << 32;    // stride byte offset: next 8-row group
+    d |= (uint64_t)1 << 46;              // descriptor version
+    d |= (uint64_t)2 << 61;              // swizzle: 128 B
+    return d;
+}
+
+// Instruction descriptor, kind::tf32: D f32, A/B tf32, both K-major, M x N.
+__host__ __device__ constexpr uint32_t idesc_tf32(int m, int n)
+{
+    return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accum)
+{
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n"
+        ::"r"(tmem), "l"(a), "l"(b), "r"(idesc), "r"(accum)
+        : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v)
+{
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+template <int BN>
+struct Smem {
+    static constexpr int A_BYTES = BM * BK * 4;
+    static constexpr int B_BYTES = BN * BK * 4;
+    static constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
+    static constexpr int TOTAL = STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
+    static constexpr int TMEM_COLS = BN <= 32 ? 32 : BN <= 64 ? 64 : BN <= 128 ? 128 : 256;
+};
+
+template <int BN>
+__global__ void __launch_bounds__(THREADS, 1)
+    k_gemm_tf32(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                float2* __restrict__ Y, int M, int R, int kblocks, int* __restrict__ err)
+{
+    using S = Smem<BN>;
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* base = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint8_t* sA = base;
+    uint8_t* sB = base + STAGES * S::A_BYTES;
+    uint64_t* full = (uint64_t*)(base + STAGES * S::STAGE_BYTES);
+    uint64_t* empty = full + STAGES;
+    uint64_t* accum = empty + STAGES;
+    uint32_t* tmem_slot = (uint32_t*)(accum + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int f0 = blockIdx.x * BM, c0 = blockIdx.y * BN;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STAGES; ++s) {
+            mbar_init(full + s, 1);
+            mbar_init(empty + s, 1);
+        }
+        mbar_init(accum, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(S::TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            int issued = 0;
+            for (int kb = 0; kb < kblocks; ++kb) {
+                const int s = kb % STAGES;
+                if (kb >= STAGES && !mbar_wait(empty + s, ((kb / STAGES) - 1) & 1, err, 1)) break;
+                if (*(volatile int*)err) break;
+                mbar_expect_tx(full + s, S::STAGE_BYTES);
+                tma_load_2d(sA + s * S::A_BYTES, &tmA, full + s, kb * BK, f0);
+                tma_load_2d(sB + s * S::B_BYTES, &tmB, full + s, kb * BK, c0);
+                issued = kb + 1;
+            }
+            // drain: every issued stage's copy must have landed before the CTA exits
+            for (int kb = issued - STAGES > 0 ? issued - STAGES : 0; kb < issued; ++kb)
+                mbar_wait(full + (kb % STAGES), (kb / STAGES) & 1, err, 2);
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            constexpr uint32_t idesc = idesc_tf32(BM, BN);
+            bool ok = true;
+            for (int kb = 0; kb < kblocks && ok; ++kb) {
+                const int s = kb % STAGES;
+                ok = mbar_wait(full + s, (kb / STAGES) & 1, err, 3);
+                if (!ok) break;
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint64_t da = sw128_desc(smem_u32(sA + s * S::A_BYTES));
+                const uint64_t db = sw128_desc(smem_u32(sB + s * S::B_BYTES));
+#pragma unroll
+                for (int k = 0; k < BK / 8; ++k)  // K = 8 tf32 = 32 bytes per instruction
+                    mma_tf32(tmem, da + 2 * k, db + 2 * k, idesc, (kb > 0 || k > 0) ? 1u : 0u);
+                mma_commit(empty + s);
+            }
+            mma_commit(accum);
+            // the MMAs must be complete before tensor memory is released
+            mbar_wait(accum, 0, err, 4);
+        }
+        __syncwarp();
+    } else {
+        // epilogue warps 2..5: lane quadrant (warp % 4) of tensor memory
+        const int q = warp & 3;
+        // one lane waits, the warp follows it: tcgen05.ld is warp-collective
+        int ok = lane == 0 ? (int)mbar_wait(accum, 0, err, 5) : 0;
+        ok = __shfl_sync(0xffffffffu, ok, 0);
+        if (ok) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const int f = f0 + 32 * q + lane;
+#pragma unroll 1
+            for (int c = 0; c < BN; c += 16) {
+                float v[16];
+                tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)c, v);
+                if (f < M) {
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) {
+                        const int r = (c0 + c) / 2 + i;
+                        if (r < R) Y[(size_t)r * M + f] = make_float2(v[2 * i], v[2 * i + 1]);
+                    }
+                }
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 1) {
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(S::TMEM_COLS) : "memory");
+    }
+}
+
+// B rows 2r = (Re x, -Im x), 2r+1 = (Im x, Re x), one float2 per k
+__global__ void k_pack_b(const float2* __restrict__ X, int n, int nrhs, float2* __restrict__ B)
+{
+    size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    size_t tot = (size_t)n * nrhs;
+    for (; id < tot; id += (size_t)gridDim.x * blockDim.x) {
+        size_t r = id / n, k = id % n;
+        float2 x = X[id];
+        B[(2 * r) * n + k] = make_float2(x.x, -x.y);
+        B[(2 * r + 1) * n + k] = make_float2(x.y, x.x);
+    }
+}
+
+}  // namespace tc
+
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+    }
+    return fn;
+}
+
+// 2-D fp32 tensor map: inner extent `inner` floats, `rows` rows `stride_bytes`
+// apart, box 32 x box_rows, 128-byte swizzle, zero fill out of bounds.
+static emfa_status_t make_map(Ctx* c, CUtensorMap* m, const void* ptr, uint64_t inner, uint64_t rows,
+                              uint64_t stride_bytes, uint32_t box_rows)
+{
+    auto fn = encode_fn();
+    if (!fn) {
+        set_error(c, "cuTensorMapEncodeTiled unavailable");
+        return EMFA_ERR_CUDA;
+    }
+    cuuint64_t dims[2] = {inner, rows};
+    cuuint64_t strides[1] = {stride_bytes};
+    cuuint32_t box[2] = {(cuuint32_t)tc::BK, box_rows};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(ptr), dims, strides, box, estr,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        set_error(c, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+        return EMFA_ERR_CUDA;
+    }
+    return EMFA_OK;
+}
+
+template <int BN>
+static emfa_status_t launch_tc(Ctx* c, const CUtensorMap& ta, const CUtensorMap& tb, float2* Y, int n, int nrhs,
+                               int* err, cudaStream_t st)
+{
+    using S = tc::Smem<BN>;
+    static bool attr = false;
+    if (!attr) {
+        EMFA_CUDA(c, cudaFuncSetAttribute(tc::k_gemm_tf32<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, S::TOTAL));
+        attr = true;
+    }
+    dim3 grd((n + tc::BM - 1) / tc::BM, (2 * nrhs + BN - 1) / BN);
+    int kblocks = (2 * n + tc::BK - 1) / tc::BK;
+    tc::k_gemm_tf32<BN><<<grd, tc::THREADS, S::TOTAL, st>>>(ta, tb, Y, n, nrhs, kblocks, err);
+    c->kernel_launches += 1;
+    EMFA_CUDA(c, cudaGetLastError());
+    return EMFA_OK;
+}
+
+emfa_status_t cgemm_tf32(Ctx* c, const void* Z, size_t ldz, const void* X, int n, int nrhs, void* Y, cudaStream_t st)
+{
+    if ((n & 1) || (ldz & 1) || ((uintptr_t)Z & 15)) {
+        set_error(c, "cgemm_tf32: needs even n and ldz and a 16-byte aligned matrix (TMA strides)");
+        return EMFA_ERR_UNSUPPORTED;
+    }
+    void* bp = nullptr;
+    void* ep = nullptr;
+    EMFA_TRY(ctx_workspace(c, WS_GEMM_B, sizeof(float) * 4 * (size_t)n * nrhs, &bp));
+    EMFA_TRY(ctx_workspace(c, WS_GEMM_ERR, 64, &ep));
+    int* err = (int*)ep;
+    EMFA_CUDA(c, cudaMemsetAsync(err, 0, sizeof(int), st));
+    size_t tot = (size_t)n * nrhs;
+    tc::k_pack_b<<<(int)std::min<size_t>((tot + 255) / 256, 8192), 256, 0, st>>>((const float2*)X, n, nrhs,
+                                                                                 (float2*)bp);
+    c->kernel_launches += 1;
+    CUtensorMap ta, tb;
+    const int BN = 2 * nrhs <= 64 ? 64 : 240;
+    EMFA_TRY(make_map(c, &ta, Z, 2 * (uint64_t)n, (uint64_t)n, ldz * 8, tc::BM));
+    EMFA_TRY(make_map(c, &tb, bp, 2 * (uint64_t)n, 2 * (uint64_t)nrhs, (uint64_t)n * 8, BN));
+    if (BN == 64)
+        EMFA_TRY(launch_tc<64>(c, ta, tb, (float2*)Y, n, nrhs, err, st));
+    else
+        EMFA_TRY(launch_tc<240>(c, ta, tb, (float2*)Y, n, nrhs, err, st));
+    return EMFA_OK;
+}
+
+emfa_status_t gemm_check_error(Ctx* c, cudaStream_t st)
+{
+    void* ep = nullptr;
+    EMFA_TRY(ctx_workspace(c, WS_GEMM_ERR, 64, &ep));
+    int h = 0;
+    EMFA_CUDA(c, cudaMemcpyAsync(&h, ep, sizeof(int), cudaMemcpyDeviceToHost, st));
+    EMFA_CUDA(c, cudaStreamSynchronize(st));
+    if (h) {
+        set_error(c, "tensor-core GEMM: a pipeline wait timed out (stage " + std::to_string(h) + ")");
+        return EMFA_ERR_TIMEOUT;
+    }
+    return EMFA_OK;
 }
 
 }  // namespace emfa

@@ -353,42 +353,46 @@ static emfa_status_t gmres_t(Ctx* c, int prec, const void* Z, int n, const void*
     const int m = std::max(1, std::min(sp->restart > 0 ? sp->restart : 30, 60));
     const size_t vec = (size_t)n * nrhs;
     const int nblk = dot_blocks(n);
-    DevBuf Vb, Wb, Rb, Xt, Hb, csb, snb, gb, yb, hcb, pb, pnb, small, cnt;
-    EMFA_TRY(Vb.alloc(c, sizeof(Cx<T>) * vec * (m + 1)));
-    EMFA_TRY(Wb.alloc(c, sizeof(Cx<T>) * vec));
-    EMFA_TRY(Rb.alloc(c, sizeof(double2) * vec));
-    if (prec == EMFA_F32) EMFA_TRY(Xt.alloc(c, sizeof(float2) * vec));
-    EMFA_TRY(Hb.alloc(c, sizeof(double2) * (size_t)nrhs * (m + 1) * m));
-    EMFA_TRY(csb.alloc(c, sizeof(double) * (size_t)nrhs * m));
-    EMFA_TRY(snb.alloc(c, sizeof(double2) * (size_t)nrhs * m));
-    EMFA_TRY(gb.alloc(c, sizeof(double2) * (size_t)nrhs * (m + 1)));
-    EMFA_TRY(yb.alloc(c, sizeof(double2) * (size_t)nrhs * m));
-    EMFA_TRY(hcb.alloc(c, sizeof(double2) * (size_t)nrhs * (m + 1)));
-    EMFA_TRY(pb.alloc(c, sizeof(double2) * (size_t)nrhs * (m + 1) * nblk));
-    EMFA_TRY(pnb.alloc(c, sizeof(double2) * (size_t)nrhs * nblk));
-    EMFA_TRY(small.alloc(c, sizeof(double) * 4 * (size_t)nrhs + sizeof(int) * 2 * (size_t)nrhs));
-    EMFA_TRY(cnt.alloc(c, sizeof(int) * 4));
+    // one workspace for the whole solve (reused across solves of a context)
+    const size_t need = Carver::round(sizeof(Cx<T>) * vec * (m + 1)) + Carver::round(sizeof(Cx<T>) * vec) +
+                        Carver::round(sizeof(double2) * vec) + Carver::round(sizeof(float2) * vec) +
+                        Carver::round(sizeof(double2) * (size_t)nrhs * (m + 1) * m) +
+                        Carver::round(sizeof(double) * (size_t)nrhs * m) +
+                        Carver::round(sizeof(double2) * (size_t)nrhs * m) * 2 +
+                        Carver::round(sizeof(double2) * (size_t)nrhs * (m + 1)) * 2 +
+                        Carver::round(sizeof(double2) * (size_t)nrhs * (m + 1) * nblk) +
+                        Carver::round(sizeof(double2) * (size_t)nrhs * nblk) +
+                        Carver::round(sizeof(double) * 4 * (size_t)nrhs) + Carver::round(sizeof(int) * 2 * (size_t)nrhs) +
+                        Carver::round(sizeof(int) * 4) + 4096;
+    void* wsp = nullptr;
+    EMFA_TRY(ctx_workspace(c, WS_KRYLOV, need, &wsp));
+    Carver cv{(char*)wsp};
+    Cx<T>* V = cv.take<Cx<T>>(vec * (m + 1));
+    Cx<T>* W = cv.take<Cx<T>>(vec);
+    double2* R = cv.take<double2>(vec);
+    float2* Xt = cv.take<float2>(vec);
     GmresDev s;
     s.m = m;
     s.nrhs = nrhs;
     s.tol = sp->tol;
     s.tol_abs = sp->tol_absolute;
-    s.H = dptr<double2>(Hb);
-    s.cs = dptr<double>(csb);
-    s.sn = dptr<double2>(snb);
-    s.g = dptr<double2>(gb);
-    s.y = dptr<double2>(yb);
-    s.hcol = dptr<double2>(hcb);
-    s.bnorm = dptr<double>(small);
+    s.H = cv.take<double2>((size_t)nrhs * (m + 1) * m);
+    s.cs = cv.take<double>((size_t)nrhs * m);
+    s.sn = cv.take<double2>((size_t)nrhs * m);
+    s.y = cv.take<double2>((size_t)nrhs * m);
+    s.g = cv.take<double2>((size_t)nrhs * (m + 1));
+    s.hcol = cv.take<double2>((size_t)nrhs * (m + 1));
+    double2* partial = cv.take<double2>((size_t)nrhs * (m + 1) * nblk);
+    double2* pnorm = cv.take<double2>((size_t)nrhs * nblk);
+    s.bnorm = cv.take<double>(4 * (size_t)nrhs);
     s.scale = s.bnorm + nrhs;
     s.est = s.scale + nrhs;
     s.true_res = s.est + nrhs;
-    s.jlen = reinterpret_cast<int*>(s.true_res + nrhs);
+    s.jlen = cv.take<int>(2 * (size_t)nrhs);
     s.active = s.jlen + nrhs;
-    s.counters = dptr<int>(cnt);
-    Cx<T>* V = dptr<Cx<T>>(Vb);
-    Cx<T>* W = dptr<Cx<T>>(Wb);
-    double2* R = dptr<double2>(Rb);
+    s.counters = cv.take<int>(4);
+    // inner product: tensor cores (TF32) for the mixed path when the shape allows
+    const bool use_tc = prec == EMFA_F32 && (sp->matvec == EMFA_MV_AUTO || sp->matvec == EMFA_MV_TF32) && (n % 2 == 0);
 
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
@@ -410,15 +414,15 @@ static emfa_status_t gmres_t(Ctx* c, int prec, const void* Z, int n, const void*
             EMFA_TRY(cgemm_f64(c, Z, n, X, n, nrhs, R, st));  // R = Z X
             k_residual<double2><<<grid1(vec), 256, 0, st>>>((const double2*)B, R, R, vec);
         } else {
-            k_to_f32<<<grid1(vec), 256, 0, st>>>(X, dptr<float2>(Xt), vec);
-            EMFA_TRY(cgemm_f32_chunked(c, Z, n, Xt.ptr, n, nrhs, B, R, st));  // R = B - Z X
+            k_to_f32<<<grid1(vec), 256, 0, st>>>(X, Xt, vec);
+            EMFA_TRY(cgemm_f32_chunked(c, Z, n, Xt, n, nrhs, B, R, st));  // R = B - Z X
         }
         {
             dim3 grd(nblk, nrhs);
-            k_block_dots<double2, double2><<<grd, KB, 0, st>>>(R, 0, 1, R, n, nrhs, nblk, dptr<double2>(pnb));
+            k_block_dots<double2, double2><<<grd, KB, 0, st>>>(R, 0, 1, R, n, nrhs, nblk, pnorm);
         }
         EMFA_CUDA(c, cudaMemsetAsync(s.counters, 0, sizeof(int) * 4, st));
-        k_cycle_init<<<(nrhs + 127) / 128, 128, 0, st>>>(s, dptr<double2>(pnb), nblk, cyc == 0);
+        k_cycle_init<<<(nrhs + 127) / 128, 128, 0, st>>>(s, pnorm, nblk, cyc == 0);
         EMFA_CUDA(c, cudaMemcpyAsync(host_cnt, s.counters, sizeof(int) * 4, cudaMemcpyDeviceToHost, st));
         EMFA_CUDA(c, cudaStreamSynchronize(st));
         c->kernel_launches += 3;
@@ -433,13 +437,15 @@ static emfa_status_t gmres_t(Ctx* c, int prec, const void* Z, int n, const void*
             // W = Z V_j
             if (prec == EMFA_F64)
                 EMFA_TRY(cgemm_f64(c, Z, n, Vj, n, nrhs, W, st));
+            else if (use_tc)
+                EMFA_TRY(cgemm_tf32(c, Z, n, Vj, n, nrhs, W, st));
             else
                 EMFA_TRY(cgemm_f32(c, Z, n, Vj, n, nrhs, W, st));
             // CGS2: h = V^H W; W -= V h; twice
-            EMFA_TRY(dots<T>(c, V, vec, j + 1, W, false, n, nrhs, dptr<double2>(pb), s.hcol, 0, st));
-            k_axpys<T><<<dim3(nblk, nrhs), KB, 0, st>>>(V, vec, j + 1, s.hcol, W, n, nrhs, nblk, dptr<double2>(pnb));
-            EMFA_TRY(dots<T>(c, V, vec, j + 1, W, false, n, nrhs, dptr<double2>(pb), s.y, 0, st));
-            k_axpys<T><<<dim3(nblk, nrhs), KB, 0, st>>>(V, vec, j + 1, s.y, W, n, nrhs, nblk, dptr<double2>(pnb));
+            EMFA_TRY(dots<T>(c, V, vec, j + 1, W, false, n, nrhs, partial, s.hcol, 0, st));
+            k_axpys<T><<<dim3(nblk, nrhs), KB, 0, st>>>(V, vec, j + 1, s.hcol, W, n, nrhs, nblk, pnorm);
+            EMFA_TRY(dots<T>(c, V, vec, j + 1, W, false, n, nrhs, partial, s.y, 0, st));
+            k_axpys<T><<<dim3(nblk, nrhs), KB, 0, st>>>(V, vec, j + 1, s.y, W, n, nrhs, nblk, pnorm);
             {
                 // hcol += second-pass coefficients
                 // accumulate: hcol[i][r] += y[i][r]
@@ -447,7 +453,7 @@ static emfa_status_t gmres_t(Ctx* c, int prec, const void* Z, int n, const void*
                 k_accumulate<<<(tot + 255) / 256, 256, 0, st>>>(s.hcol, s.y, tot);
             }
             EMFA_CUDA(c, cudaMemsetAsync(s.counters, 0, sizeof(int), st));
-            k_arnoldi_finish<<<(nrhs + 127) / 128, 128, 0, st>>>(s, j, dptr<double2>(pnb), nblk);
+            k_arnoldi_finish<<<(nrhs + 127) / 128, 128, 0, st>>>(s, j, pnorm, nblk);
             k_scale_store<Cx<T>, Cx<T>><<<grid1(vec), 256, 0, st>>>(W, s.scale, n, nrhs, V + (size_t)(j + 1) * vec);
             EMFA_CUDA(c, cudaMemcpyAsync(host_cnt, s.counters, sizeof(int), cudaMemcpyDeviceToHost, st));
             EMFA_CUDA(c, cudaStreamSynchronize(st));
@@ -456,6 +462,7 @@ static emfa_status_t gmres_t(Ctx* c, int prec, const void* Z, int n, const void*
             if (host_cnt[0] == 0) break;
         }
         total_iters += steps;
+        if (use_tc) EMFA_TRY(gemm_check_error(c, st));
         k_backsolve<<<(nrhs + 127) / 128, 128, 0, st>>>(s);
         k_update_x<T><<<dim3((n + 255) / 256, nrhs), 256, 0, st>>>(V, vec, steps, s.y, s.jlen, X, n, nrhs);
         c->kernel_launches += 2;
@@ -609,6 +616,7 @@ static emfa_status_t bicgstab(Ctx* c, int prec, const void* Z, int n, const void
     EMFA_TRY(sc.alloc(c, sizeof(double2) * 5 * nrhs + sizeof(double) * 2 * nrhs + sizeof(int) * (nrhs + 4)));
     EMFA_TRY(pb.alloc(c, sizeof(double2) * (size_t)nrhs * nblk));
     EMFA_TRY(db.alloc(c, sizeof(double2) * 2 * nrhs));
+    double2* partial = dptr<double2>(pb);
     double2* r = dptr<double2>(vb);
     double2* rh = r + vec;
     double2* p = rh + vec;
@@ -640,7 +648,7 @@ static emfa_status_t bicgstab(Ctx* c, int prec, const void* Z, int n, const void
         k_to_f64<<<grid1(vec), 256, 0, st>>>((const float2*)B, r, vec);
     EMFA_CUDA(c, cudaMemcpyAsync(rh, r, sizeof(double2) * vec, cudaMemcpyDeviceToDevice, st));
     EMFA_CUDA(c, cudaMemsetAsync(p, 0, sizeof(double2) * vec * 2, st));  // p, v
-    EMFA_TRY(dots_d(c, r, r, n, nrhs, dptr<double2>(pb), d0, st));
+    EMFA_TRY(dots_d(c, r, r, n, nrhs, partial, d0, st));
     k_bicg_scalar<<<(nrhs + 127) / 128, 128, 0, st>>>(s, 0, d0, nullptr);
     EMFA_CUDA(c, cudaMemsetAsync(s.counters, 0, sizeof(int) * 4, st));
     const int max_it = sp->max_iter > 0 ? sp->max_iter : 500;
@@ -648,18 +656,18 @@ static emfa_status_t bicgstab(Ctx* c, int prec, const void* Z, int n, const void
     int it = 0, hc[4] = {0, 0, 0, 0};
     int converged = 0;
     for (; it < max_it; ++it) {
-        EMFA_TRY(dots_d(c, rh, r, n, nrhs, dptr<double2>(pb), d0, st));
+        EMFA_TRY(dots_d(c, rh, r, n, nrhs, partial, d0, st));
         k_bicg_scalar<<<(nrhs + 127) / 128, 128, 0, st>>>(s, 1, d0, nullptr);
         k_bicg_p<<<eg, 256, 0, st>>>(s, r, p, v, n);
         EMFA_TRY(matvec_d<float>(c, prec, Z, n, p, nrhs, v, dptr<float2>(tin), dptr<float2>(tout), st));
-        EMFA_TRY(dots_d(c, rh, v, n, nrhs, dptr<double2>(pb), d0, st));
+        EMFA_TRY(dots_d(c, rh, v, n, nrhs, partial, d0, st));
         k_bicg_scalar<<<(nrhs + 127) / 128, 128, 0, st>>>(s, 2, d0, nullptr);
         k_bicg_s<<<eg, 256, 0, st>>>(s, X, p, r, v, sv, n);
-        EMFA_TRY(dots_d(c, sv, sv, n, nrhs, dptr<double2>(pb), d0, st));
+        EMFA_TRY(dots_d(c, sv, sv, n, nrhs, partial, d0, st));
         k_bicg_scalar<<<(nrhs + 127) / 128, 128, 0, st>>>(s, 3, d0, nullptr);
         EMFA_TRY(matvec_d<float>(c, prec, Z, n, sv, nrhs, t, dptr<float2>(tin), dptr<float2>(tout), st));
-        EMFA_TRY(dots_d(c, t, sv, n, nrhs, dptr<double2>(pb), d0, st));
-        EMFA_TRY(dots_d(c, t, t, n, nrhs, dptr<double2>(pb), d1, st));
+        EMFA_TRY(dots_d(c, t, sv, n, nrhs, partial, d0, st));
+        EMFA_TRY(dots_d(c, t, t, n, nrhs, partial, d1, st));
         EMFA_CUDA(c, cudaMemsetAsync(s.counters, 0, sizeof(int), st));
         k_bicg_scalar<<<(nrhs + 127) / 128, 128, 0, st>>>(s, 4, d0, d1);
         k_bicg_r<<<eg, 256, 0, st>>>(s, X, sv, t, r, n);
@@ -717,7 +725,10 @@ emfa_status_t emfa_matvec(emfa_ctx_t* ctx, int prec, int matvec, const void* Z_d
         set_error(ctx, "emfa_matvec: precision");
         return EMFA_ERR_INVALID;
     }
-    if (matvec == EMFA_MV_TF32) return cgemm_tf32(ctx, Z_dev, n, X_dev, n, n_rhs, Y_dev, st);
+    if (matvec == EMFA_MV_TF32) {
+        EMFA_TRY(cgemm_tf32(ctx, Z_dev, n, X_dev, n, n_rhs, Y_dev, st));
+        return gemm_check_error(ctx, st);
+    }
     return cgemm_f32(ctx, Z_dev, n, X_dev, n, n_rhs, Y_dev, st);
 }
 

@@ -4,7 +4,9 @@ reference's golden vectors and the oracle restatement.
 
 Tolerances (written here, per entry unless stated):
   FP64 fill vs FP64 reference      floored rel 1e-11, normwise 1e-12
-  FP32 fill vs FP32 reference      floored rel 1e-5  (floor 1e-3 max|Z|)
+  FP32 fill vs FP64 reference      normwise 1e-5; per entry (floored, floor
+                                   1e-3 max|Z|) no worse than the reference's
+                                   own FP32 fill vs its FP64 fill
   current vs I* = Z64^-1 V64       rel L2 1e-4
   RCS                               0.1 dB (0.01 dB where both sides solve tightly)
 """
@@ -59,14 +61,23 @@ def test_fill_z_fp64_matches_reference(ctx, name):
 
 @pytest.mark.parametrize("name", CASES)
 def test_fill_z_fp32_matches_reference(ctx, name):
+    """FP32 fill: the reference's own FP32 fill already deviates from its
+    FP64 fill by up to ~6e-5 per entry (cancellation among the four triangle
+    pairs of far RWG pairs), so two FP32 implementations cannot agree to 1e-5
+    per entry.  The bar: normwise within 1e-5 of the FP64 reference, and per
+    entry (floored) no worse than the reference's own FP32 error."""
     from emfa_gb300 import api
     g = load_golden(name)
     geo = golden_geometry(ctx, g)
     Z = api.fill_z(geo, params(g, "f32")).cpu().numpy()
-    for tag in ("f32", "f64"):
-        Zr = g["Z_" + tag] if "Z_" + tag in g else g["Zrows_" + tag]
-        rel = floored_rel(Z[: Zr.shape[0]], Zr)
-        assert rel.max() < 1e-5, (tag, rel.max())
+    r32 = g["Z_f32"] if "Z_f32" in g else g["Zrows_f32"]
+    r64 = g["Z_f64"] if "Z_f64" in g else g["Zrows_f64"]
+    Z = Z[: r64.shape[0]]
+    own = floored_rel(r32, r64).max()
+    ours = floored_rel(Z, r64).max()
+    assert ours <= max(1e-5, 1.5 * own), (ours, own)
+    assert np.linalg.norm(Z - r64) / np.linalg.norm(r64) < 1e-5
+    assert floored_rel(Z, r32).max() < 2.5 * max(own, 1e-5)
 
 
 def test_fill_z_edm_modes(ctx):
@@ -193,3 +204,22 @@ def test_dense_rcs_end_to_end_vs_reference(ctx):
         assert np.abs(out[0] - g["rcs_" + prec]).max() < 0.1
         Istar = np.linalg.solve(g["Z_f64"], g["V_f64"])
         assert np.linalg.norm(I[0] - Istar) / np.linalg.norm(Istar) < 1e-4
+
+
+@pytest.mark.parametrize("n,r", [(128, 4), (256, 32), (998, 37), (1920, 360)])
+def test_matvec_tf32_tensor_cores(ctx, n, r):
+    """tcgen05 TF32 product against an FP64 product of the same inputs.
+    TF32 keeps 10 mantissa bits: normwise error ~1e-3 of |Z||X|."""
+    import torch
+    from emfa_gb300 import api
+    rng = np.random.default_rng(n + r)
+    Z = torch.tensor(rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)), dtype=torch.complex64,
+                     device="cuda")
+    X = torch.tensor(rng.standard_normal((r, n)) + 1j * rng.standard_normal((r, n)), dtype=torch.complex64,
+                     device="cuda")
+    Y = api.matvec(ctx, Z, X, "tf32").cpu().numpy()
+    ref = (Z.cpu().numpy().astype(np.complex128) @ X.cpu().numpy().astype(np.complex128).T).T
+    err = np.linalg.norm(Y - ref) / np.linalg.norm(ref)
+    assert err < 3e-3, err
+    # every column must be populated (no tile or RHS skipped)
+    assert np.all(np.abs(Y).max(axis=1) > 0)
