@@ -198,6 +198,30 @@ def run_emfa(args, workload):
     }
 
 
+def run_gemm_only(args):
+    """Micro-benchmark of the multi-RHS product alone (the inner product of the
+    solver): Z (N x N complex64, random) times 360 vectors.  Used to profile
+    the tensor-core kernel in isolation."""
+    import torch
+    from emfa_gb300 import api, build
+    build.build()
+    n, r = args.gemm_n, args.gemm_r
+    ctx = api.Context(0)
+    g = torch.Generator(device="cuda").manual_seed(1)
+    Z = torch.randn((n, n), dtype=torch.complex64, device="cuda", generator=g)
+    X = torch.randn((r, n), dtype=torch.complex64, device="cuda", generator=g)
+    for _ in range(args.warmup):
+        api.matvec(ctx, Z, X, args.matvec if args.matvec != "auto" else "tf32")
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        api.matvec(ctx, Z, X, args.matvec if args.matvec != "auto" else "tf32")
+    torch.cuda.synchronize()
+    dt = (time.perf_counter() - t0) / max(1, args.steps)
+    flops = 8.0 * n * n * r
+    print(json.dumps({"mode": "gemm", "n": n, "r": r, "ms": dt * 1e3, "tflops": flops / dt / 1e12}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -207,7 +231,13 @@ def main():
     ap.add_argument("--workload", default="c2_cfie_sphere_7680x360", choices=list(WORKLOADS))
     ap.add_argument("--matvec", default="auto", choices=["auto", "f32", "tf32"])
     ap.add_argument("--check", type=int, default=1)
+    ap.add_argument("--mode", default="job", choices=["job", "gemm"])
+    ap.add_argument("--gemm-n", type=int, default=7680)
+    ap.add_argument("--gemm-r", type=int, default=360)
     args = ap.parse_args()
+    if args.mode == "gemm":
+        run_gemm_only(args)
+        return
     rank, local, world = rank_env()
     if world > 1:
         import torch

@@ -64,6 +64,9 @@ _SIGS = {
     "emfa_ctx_launch_count": (ci, [vp, ctypes.POINTER(ctypes.c_int64)]),
     "emfa_ctx_synchronize": (ci, [vp]),
     "emfa_ctx_stream": (ci, [vp, ctypes.POINTER(vp)]),
+    "emfa_device_alloc": (ci, [vp, sz, ctypes.POINTER(vp)]),
+    "emfa_device_free": (ci, [vp, vp]),
+    "emfa_memcpy": (ci, [vp, vp, vp, sz, ci]),
     "emfa_build_rwg": (ci, [vp, ci, vp, ci, ip]),
     "emfa_geom_create": (ci, [vp, vp, ci, vp, ci, vp, ci, ctypes.POINTER(vp)]),
     "emfa_geom_destroy": (ci, [vp]),

@@ -17,6 +17,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libemfa_cuda.so")
+LAUNCHER = os.path.join(BUILD, "emfa_launcher")
+HOST = os.path.join(CSRC, "host")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # host code: no FP contraction so host-side geometry/incidence math rounds
 # like the reference's (x86 has no FMA in its baseline ISA; aarch64 does)
@@ -47,11 +49,23 @@ def _compile(src: str, verbose: bool) -> str:
 
 
 def _stale(objs) -> bool:
-    if not os.path.exists(LIB):
+    if not os.path.exists(LIB) or not os.path.exists(LAUNCHER):
         return True
-    t = os.path.getmtime(LIB)
-    deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [os.path.join(HERE, "..", "include", "emfa_cuda.h")]
+    t = min(os.path.getmtime(LIB), os.path.getmtime(LAUNCHER))
+    deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [os.path.join(HOST, f) for f in os.listdir(HOST)]
+    deps.append(os.path.join(HERE, "..", "include", "emfa_cuda.h"))
     return any(os.path.getmtime(d) > t for d in deps)
+
+
+def _build_launcher() -> None:
+    """C++ host front end (solver classes + launcher) linked against the library."""
+    srcs = [os.path.join(HOST, f) for f in sorted(os.listdir(HOST)) if f.endswith(".cpp")]
+    cxx = shutil.which("g++") or "c++"
+    cmd = [cxx, "-O2", "-std=c++17", "-ffp-contract=off", *srcs, "-o", LAUNCHER, "-L" + BUILD, "-lemfa_cuda",
+           "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("host front end build failed:\n" + r.stderr)
 
 
 def build(force: bool = False, verbose: bool = False) -> str:
@@ -65,6 +79,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n" + r.stderr)
+    _build_launcher()
     return LIB
 
 

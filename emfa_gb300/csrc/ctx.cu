@@ -151,6 +151,7 @@ emfa_status_t emfa_ctx_destroy(emfa_ctx_t* ctx)
         cudaStreamDestroy(ctx->stream);
     }
     for (auto& b : ctx->ws) b.release();
+    for (auto& kv : ctx->user_bufs) cudaFree(kv.first);
     delete ctx;
     return EMFA_OK;
 }
@@ -175,6 +176,46 @@ emfa_status_t emfa_ctx_synchronize(emfa_ctx_t* ctx)
 {
     if (!ctx) return EMFA_ERR_INVALID;
     EMFA_CUDA(ctx, cudaSetDevice(ctx->device));
+    EMFA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return EMFA_OK;
+}
+
+emfa_status_t emfa_device_alloc(emfa_ctx_t* ctx, size_t bytes, void** dev)
+{
+    if (!ctx || !dev || bytes == 0) return EMFA_ERR_INVALID;
+    EMFA_CUDA(ctx, cudaSetDevice(ctx->device));
+    EMFA_TRY(ctx_alloc(ctx, bytes, dev));
+    std::lock_guard<std::mutex> g(ctx->mu);
+    ctx->user_bufs[*dev] = bytes;
+    return EMFA_OK;
+}
+
+emfa_status_t emfa_device_free(emfa_ctx_t* ctx, void* dev)
+{
+    if (!ctx || !dev) return EMFA_ERR_INVALID;
+    size_t bytes = 0;
+    {
+        std::lock_guard<std::mutex> g(ctx->mu);
+        auto it = ctx->user_bufs.find(dev);
+        if (it == ctx->user_bufs.end()) {
+            ctx->last_error = "emfa_device_free: pointer not allocated by this context";
+            return EMFA_ERR_INVALID;
+        }
+        bytes = it->second;
+        ctx->user_bufs.erase(it);
+    }
+    EMFA_CUDA(ctx, cudaSetDevice(ctx->device));
+    EMFA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    ctx_free(ctx, dev, bytes);
+    return EMFA_OK;
+}
+
+emfa_status_t emfa_memcpy(emfa_ctx_t* ctx, void* dst, const void* src, size_t bytes, int kind)
+{
+    if (!ctx || !dst || !src || kind < 0 || kind > 2) return EMFA_ERR_INVALID;
+    cudaMemcpyKind k = kind == 0 ? cudaMemcpyHostToDevice : kind == 1 ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+    EMFA_CUDA(ctx, cudaSetDevice(ctx->device));
+    EMFA_CUDA(ctx, cudaMemcpyAsync(dst, src, bytes, k, ctx->stream));
     EMFA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return EMFA_OK;
 }

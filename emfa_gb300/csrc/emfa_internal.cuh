@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 #include <cstddef>
 #include <cstdint>
+#include <map>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -86,6 +87,7 @@ struct Ctx {
     int sm_count = 0;
     long long kernel_launches = 0;  // kernels launched through this context
     DevBuf ws[WS_COUNT];            // declared after mu: destroyed before it
+    std::map<void*, size_t> user_bufs;  // emfa_device_alloc'ed buffers
 };
 
 emfa_status_t ctx_workspace(Ctx* c, int slot, size_t bytes, void** p);

@@ -199,9 +199,10 @@ __device__ __forceinline__ void regular_pair(const T (&P)[3][3], const T (&Q)[3]
 #pragma unroll
         for (int q = 0; q < 3; ++q) {
             V3<T> d = v3(pp.x - Q[q][0], pp.y - Q[q][1], pp.z - Q[q][2]);
-            T r2 = dot(d, d);
-            T rinv = rsqrt_t(r2);
-            T r = r2 * rinv;
+            // IEEE sqrt and reciprocal: the four triangle-pair terms of a far
+            // RWG pair nearly cancel, so G needs every bit it can keep
+            T r = sqrt(dot(d, d));
+            T rinv = T(1) / r;
             T sn, cs;
             sincos_pi(r * c.kpi, &sn, &cs);
             T gr = cs * rinv, gi = -sn * rinv;

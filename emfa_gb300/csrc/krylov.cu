@@ -139,6 +139,153 @@ __global__ void __launch_bounds__(KB) k_axpys(const Cx<T>* __restrict__ V, size_
     }
 }
 
+// ---------------------------------------------------------------------------
+// Gram-Schmidt passes over the whole basis.  Each thread keeps one
+// accumulator per basis vector in registers (all loads of an element
+// independent), sums its elements in the storage precision (FP32 for the
+// mixed path: GB300's FP64 pipe is ~1/64 of FP32), and the per-thread sums
+// meet in FP64 across the block and across blocks.
+// ---------------------------------------------------------------------------
+constexpr int MAXV = 32;  // basis vectors per pass (GMRES restart <= 31)
+
+template <typename T> struct Acc { using type = float; };
+template <> struct Acc<double> { using type = double; };
+
+template <typename A>
+__device__ __forceinline__ void block_reduce_write(A (&ar)[MAXV], A (&ai)[MAXV], int nv, double2* out, size_t ostride)
+{
+    __shared__ double2 red[MAXV][KB / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int i = 0; i < MAXV; ++i) {
+        if (i < nv) {
+            double re = (double)ar[i], im = (double)ai[i];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                re += __shfl_xor_sync(0xffffffffu, re, o);
+                im += __shfl_xor_sync(0xffffffffu, im, o);
+            }
+            if (lane == 0) red[i][wid] = make_double2(re, im);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < nv) {
+        double2 t = make_double2(0.0, 0.0);
+        for (int q = 0; q < KB / 32; ++q) {
+            t.x += red[threadIdx.x][q].x;
+            t.y += red[threadIdx.x][q].y;
+        }
+        out[(size_t)threadIdx.x * ostride] = t;
+    }
+}
+
+// partial[(i * nrhs + r) * nblk + blk] = sum over the block's chunk of conj(V_i) W
+template <typename T>
+__global__ void __launch_bounds__(KB) k_multidot(const Cx<T>* __restrict__ V, size_t vstride, int nv,
+                                                 const Cx<T>* __restrict__ W, int n, int nrhs, int nblk, int chunk,
+                                                 double2* __restrict__ partial)
+{
+    using A = typename Acc<T>::type;
+    const int blk = blockIdx.x, r = blockIdx.y;
+    const size_t base = (size_t)r * n;
+    const int k1 = min(n, (blk + 1) * chunk);
+    A ar[MAXV], ai[MAXV];
+#pragma unroll
+    for (int i = 0; i < MAXV; ++i) ar[i] = ai[i] = A(0);
+    for (int k = blk * chunk + threadIdx.x; k < k1; k += KB) {
+        const Cx<T> w = W[base + k];
+#pragma unroll
+        for (int i = 0; i < MAXV; ++i) {
+            if (i < nv) {
+                const Cx<T> v = V[(size_t)i * vstride + base + k];
+                ar[i] += (A)v.re * (A)w.re + (A)v.im * (A)w.im;
+                ai[i] += (A)v.re * (A)w.im - (A)v.im * (A)w.re;
+            }
+        }
+    }
+    block_reduce_write<A>(ar, ai, nv, partial + ((size_t)r * nblk + blk), (size_t)nrhs * nblk);
+}
+
+// W -= sum_i h_i V_i over the chunk; then either the dot products of the new
+// W with every V_i (second Gram-Schmidt pass) or the squared norm of W.
+template <typename T, bool DOTS>
+__global__ void __launch_bounds__(KB) k_cgs_update(const Cx<T>* __restrict__ V, size_t vstride, int nv,
+                                                   const double2* __restrict__ h, Cx<T>* __restrict__ W, int n,
+                                                   int nrhs, int nblk, int chunk, double2* __restrict__ partial)
+{
+    using A = typename Acc<T>::type;
+    const int blk = blockIdx.x, r = blockIdx.y;
+    const size_t base = (size_t)r * n;
+    const int k1 = min(n, (blk + 1) * chunk);
+    __shared__ double2 hs[MAXV];
+    if (threadIdx.x < nv) hs[threadIdx.x] = h[(size_t)threadIdx.x * nrhs + r];
+    __syncthreads();
+    __shared__ A hsa[2][MAXV];
+    if (threadIdx.x < MAXV) {
+        hsa[0][threadIdx.x] = threadIdx.x < nv ? (A)hs[threadIdx.x].x : A(0);
+        hsa[1][threadIdx.x] = threadIdx.x < nv ? (A)hs[threadIdx.x].y : A(0);
+    }
+    __syncthreads();
+    A ar[MAXV], ai[MAXV];
+#pragma unroll
+    for (int i = 0; i < MAXV; ++i) ar[i] = ai[i] = A(0);
+    A nr = A(0);
+    for (int k = blk * chunk + threadIdx.x; k < k1; k += KB) {
+        Cx<T> w = W[base + k];
+        A sr = A(0), si = A(0);
+#pragma unroll
+        for (int i = 0; i < MAXV; ++i) {
+            if (i < nv) {
+                const Cx<T> v = V[(size_t)i * vstride + base + k];
+                const A hr = hsa[0][i], hi = hsa[1][i];
+                sr += hr * (A)v.re - hi * (A)v.im;
+                si += hr * (A)v.im + hi * (A)v.re;
+            }
+        }
+        w.re = (T)((A)w.re - sr);
+        w.im = (T)((A)w.im - si);
+        W[base + k] = w;
+        if (DOTS) {
+            // second read of V_i[k]: the line was just fetched, served by L1
+#pragma unroll
+            for (int i = 0; i < MAXV; ++i) {
+                if (i < nv) {
+                    const Cx<T> v = V[(size_t)i * vstride + base + k];
+                    ar[i] += (A)v.re * (A)w.re + (A)v.im * (A)w.im;
+                    ai[i] += (A)v.re * (A)w.im - (A)v.im * (A)w.re;
+                }
+            }
+        } else {
+            nr += (A)w.re * (A)w.re + (A)w.im * (A)w.im;
+        }
+    }
+    if (DOTS) {
+        block_reduce_write<A>(ar, ai, nv, partial + ((size_t)r * nblk + blk), (size_t)nrhs * nblk);
+    } else {
+        A a1[MAXV], a2[MAXV];
+        a1[0] = nr;
+        a2[0] = A(0);
+        block_reduce_write<A>(a1, a2, 1, partial + ((size_t)r * nblk + blk), (size_t)nrhs * nblk);
+    }
+}
+
+// squared norms of complex128 vectors: partial[r * nblk + blk]
+__global__ void __launch_bounds__(KB) k_norm2(const double2* __restrict__ X, int n, int nblk, int chunk,
+                                              double2* __restrict__ partial)
+{
+    const int blk = blockIdx.x, r = blockIdx.y;
+    const size_t base = (size_t)r * n;
+    const int k1 = min(n, (blk + 1) * chunk);
+    double a1[MAXV], a2[MAXV];
+    a1[0] = 0.0;
+    a2[0] = 0.0;
+    for (int k = blk * chunk + threadIdx.x; k < k1; k += KB) {
+        double2 x = X[base + k];
+        a1[0] += x.x * x.x + x.y * x.y;
+    }
+    block_reduce_write<double>(a1, a2, 1, partial + ((size_t)r * nblk + blk), 1);
+}
+
 // per-RHS: finish Arnoldi column j, rotate, test convergence
 __global__ void k_arnoldi_finish(GmresDev s, int j, const double2* __restrict__ pnorm, int nblk)
 {
@@ -154,7 +301,10 @@ __global__ void k_arnoldi_finish(GmresDev s, int j, const double2* __restrict__ 
     double beta = sqrt(nr2);
     double2* H = s.H + (size_t)r * (m + 1) * m;
     // column j of H: CGS2 coefficients
-    for (int i = 0; i <= j; ++i) H[i * m + j] = s.hcol[(size_t)i * s.nrhs + r];
+    for (int i = 0; i <= j; ++i) {
+        double2 a = s.hcol[(size_t)i * s.nrhs + r], b = s.y[(size_t)i * s.nrhs + r];
+        H[i * m + j] = make_double2(a.x + b.x, a.y + b.y);
+    }
     H[(j + 1) * m + j] = make_double2(beta, 0.0);
     double* cs = s.cs + (size_t)r * m;
     double2* sn = s.sn + (size_t)r * m;
@@ -350,9 +500,12 @@ template <typename T>
 static emfa_status_t gmres_t(Ctx* c, int prec, const void* Z, int n, const void* B, int nrhs, double2* X,
                              const emfa_solver_params_t* sp, emfa_solve_info_t* info, cudaStream_t st)
 {
-    const int m = std::max(1, std::min(sp->restart > 0 ? sp->restart : 30, 60));
+    const int m = std::max(1, std::min(sp->restart > 0 ? sp->restart : 30, MAXV - 1));
     const size_t vec = (size_t)n * nrhs;
-    const int nblk = dot_blocks(n);
+    // vector-pass grid: ~2 CTAs per SM over (chunks of N) x (right-hand sides)
+    const int sms = c->sm_count > 0 ? c->sm_count : 148;
+    const int nblk = std::max(1, std::min((2 * sms + nrhs - 1) / nrhs, (n + 4 * KB - 1) / (4 * KB)));
+    const int chunk = (n + nblk - 1) / nblk;
     // one workspace for the whole solve (reused across solves of a context)
     const size_t need = Carver::round(sizeof(Cx<T>) * vec * (m + 1)) + Carver::round(sizeof(Cx<T>) * vec) +
                         Carver::round(sizeof(double2) * vec) + Carver::round(sizeof(float2) * vec) +
@@ -417,10 +570,7 @@ static emfa_status_t gmres_t(Ctx* c, int prec, const void* Z, int n, const void*
             k_to_f32<<<grid1(vec), 256, 0, st>>>(X, Xt, vec);
             EMFA_TRY(cgemm_f32_chunked(c, Z, n, Xt, n, nrhs, B, R, st));  // R = B - Z X
         }
-        {
-            dim3 grd(nblk, nrhs);
-            k_block_dots<double2, double2><<<grd, KB, 0, st>>>(R, 0, 1, R, n, nrhs, nblk, pnorm);
-        }
+        k_norm2<<<dim3(nblk, nrhs), KB, 0, st>>>(R, n, nblk, chunk, pnorm);
         EMFA_CUDA(c, cudaMemsetAsync(s.counters, 0, sizeof(int) * 4, st));
         k_cycle_init<<<(nrhs + 127) / 128, 128, 0, st>>>(s, pnorm, nblk, cyc == 0);
         EMFA_CUDA(c, cudaMemcpyAsync(host_cnt, s.counters, sizeof(int) * 4, cudaMemcpyDeviceToHost, st));
@@ -441,17 +591,15 @@ static emfa_status_t gmres_t(Ctx* c, int prec, const void* Z, int n, const void*
                 EMFA_TRY(cgemm_tf32(c, Z, n, Vj, n, nrhs, W, st));
             else
                 EMFA_TRY(cgemm_f32(c, Z, n, Vj, n, nrhs, W, st));
-            // CGS2: h = V^H W; W -= V h; twice
-            EMFA_TRY(dots<T>(c, V, vec, j + 1, W, false, n, nrhs, partial, s.hcol, 0, st));
-            k_axpys<T><<<dim3(nblk, nrhs), KB, 0, st>>>(V, vec, j + 1, s.hcol, W, n, nrhs, nblk, pnorm);
-            EMFA_TRY(dots<T>(c, V, vec, j + 1, W, false, n, nrhs, partial, s.y, 0, st));
-            k_axpys<T><<<dim3(nblk, nrhs), KB, 0, st>>>(V, vec, j + 1, s.y, W, n, nrhs, nblk, pnorm);
-            {
-                // hcol += second-pass coefficients
-                // accumulate: hcol[i][r] += y[i][r]
-                int tot = (j + 1) * nrhs;
-                k_accumulate<<<(tot + 255) / 256, 256, 0, st>>>(s.hcol, s.y, tot);
-            }
+            // CGS2 in three passes: h1 = V^H W; W -= V h1 and h2 = V^H W; W -= V h2 and |W|^2
+            const dim3 vg(nblk, nrhs);
+            const int nv = j + 1;
+            const int rg = (nv * nrhs + 127) / 128;
+            k_multidot<T><<<vg, KB, 0, st>>>(V, vec, nv, W, n, nrhs, nblk, chunk, partial);
+            k_reduce_partials<<<rg, 128, 0, st>>>(partial, nv, nrhs, nblk, s.hcol, 0);
+            k_cgs_update<T, true><<<vg, KB, 0, st>>>(V, vec, nv, s.hcol, W, n, nrhs, nblk, chunk, partial);
+            k_reduce_partials<<<rg, 128, 0, st>>>(partial, nv, nrhs, nblk, s.y, 0);
+            k_cgs_update<T, false><<<vg, KB, 0, st>>>(V, vec, nv, s.y, W, n, nrhs, nblk, chunk, pnorm);
             EMFA_CUDA(c, cudaMemsetAsync(s.counters, 0, sizeof(int), st));
             k_arnoldi_finish<<<(nrhs + 127) / 128, 128, 0, st>>>(s, j, pnorm, nblk);
             k_scale_store<Cx<T>, Cx<T>><<<grid1(vec), 256, 0, st>>>(W, s.scale, n, nrhs, V + (size_t)(j + 1) * vec);

@@ -104,6 +104,13 @@ emfa_status_t emfa_ctx_synchronize(emfa_ctx_t* ctx);
 /* The context's own CUDA stream (a cudaStream_t), used when a call gets NULL. */
 emfa_status_t emfa_ctx_stream(const emfa_ctx_t* ctx, void** stream);
 
+/* Device buffers charged to the context's HBM budget, for callers without
+ * CUDA runtime bindings of their own (the C++ front end, FFI users).
+ * kind: 0 host->device, 1 device->host, 2 device->device; synchronous. */
+emfa_status_t emfa_device_alloc(emfa_ctx_t* ctx, size_t bytes, void** dev);
+emfa_status_t emfa_device_free(emfa_ctx_t* ctx, void* dev);
+emfa_status_t emfa_memcpy(emfa_ctx_t* ctx, void* dst, const void* src, size_t bytes, int kind);
+
 /* ---- geometry ------------------------------------------------------------- */
 /* RWG table of a closed or open triangle mesh, host only (no GPU).  Rows of 6
  * ints: v1 v2 vxp vxm tp tm, in the reference's order and orientation.

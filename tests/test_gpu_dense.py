@@ -147,7 +147,9 @@ def test_solve_current_vs_direct(ctx, name, prec, method):
     fp = params(g, prec)
     Z = api.fill_z(geo, fp)
     V = api.fill_v(geo, fp, angles(g))
-    sp = api.solver_params(method, tol=1e-7 if method == "gmres" else 1e-7, max_iter=2000)
+    # FP32 matrices: the true residual is resolved to ~1e-7, so 1e-6 (the
+    # BASELINE tolerance) for them; FP64 matrices go to 1e-9
+    sp = api.solver_params(method, tol=1e-6 if prec == "f32" else 1e-9, max_iter=2000)
     X, info = api.solve(ctx, Z, V, sp)
     assert info.converged == 1, (info.iterations, info.max_rel_residual)
     I = X.cpu().numpy()[0]
@@ -168,7 +170,7 @@ def test_batched_solve_equals_single(ctx):
     Z = api.fill_z(geo, fp)
     ang = np.array([[90.0, p, 0.0] for p in range(0, 360, 12)])
     V = api.fill_v(geo, fp, ang)
-    sp = api.solver_params("gmres", tol=1e-7, max_iter=2000)
+    sp = api.solver_params("gmres", tol=1e-6, max_iter=2000)
     X, info = api.solve(ctx, Z, V, sp)
     assert info.converged == len(ang)
     for i in (0, 7, 29):
