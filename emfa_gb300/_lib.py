@@ -36,6 +36,10 @@ class SolverParams(ctypes.Structure):
                 ("max_refine", ctypes.c_int)]
 
 
+class MlfmaParams(ctypes.Structure):
+    _fields_ = [("freq", ctypes.c_double), ("alpha", ctypes.c_double), ("box_threshold", ctypes.c_double)]
+
+
 class SolveInfo(ctypes.Structure):
     _fields_ = [("iterations", ctypes.c_int), ("cycles", ctypes.c_int), ("converged", ctypes.c_int),
                 ("max_rel_residual", ctypes.c_double), ("seconds", ctypes.c_double)]
@@ -76,6 +80,15 @@ _SIGS = {
     "emfa_matvec": (ci, [vp, ci, ci, vp, ci, vp, ci, vp, vp]),
     "emfa_solve": (ci, [vp, ci, vp, ci, vp, ci, vp, ctypes.POINTER(SolverParams), ctypes.POINTER(SolveInfo), vp]),
     "emfa_rcs": (ci, [vp, vp, ctypes.POINTER(FillParams), vp, ci, vp, ci, ci, vp, vp]),
+    "emfa_mlfma_plan": (ci, [vp, ci, vp, ci, ctypes.POINTER(MlfmaParams), ip, vp, ci, vp, vp]),
+    "emfa_mlfma_create": (ci, [vp, vp, ctypes.POINTER(MlfmaParams), ctypes.POINTER(vp)]),
+    "emfa_mlfma_destroy": (ci, [vp]),
+    "emfa_mlfma_info": (ci, [vp, ip, vp, vp, ctypes.POINTER(sz), vp]),
+    "emfa_mlfma_apply": (ci, [vp, vp, vp, ci, vp]),
+    "emfa_mlfma_apply_part": (ci, [vp, vp, vp, ci, vp]),
+    "emfa_mlfma_fill_v": (ci, [vp, vp, ci, vp, vp]),
+    "emfa_mlfma_solve": (ci, [vp, vp, ci, vp, ctypes.POINTER(SolverParams), ctypes.POINTER(SolveInfo), vp]),
+    "emfa_mlfma_unpermute": (ci, [vp, vp, ci, vp, vp]),
     "emfa_dense_rcs": (ci, [vp, vp, ci, vp, ci, ctypes.POINTER(FillParams), vp, ci, ctypes.POINTER(SolverParams),
                             vp, ci, ci, vp, vp, ctypes.POINTER(SolveInfo)]),
 }

@@ -229,3 +229,99 @@ def monostatic_dirs(angles) -> np.ndarray:
     th, ph = np.deg2rad(a[:, 0]), np.deg2rad(a[:, 1])
     d = np.stack([np.sin(th) * np.cos(ph), np.sin(th) * np.sin(ph), np.cos(th)], -1)
     return d[:, None, :]
+
+
+# ---------------------------------------------------------------------------
+# MLFMA
+# ---------------------------------------------------------------------------
+def mlfma_params(freq=3e8, alpha=0.5, box_threshold=0.25) -> L.MlfmaParams:
+    return L.MlfmaParams(float(freq), float(alpha), float(box_threshold))
+
+
+def mlfma_plan(mesh: TriMesh, rwg: np.ndarray, mp: L.MlfmaParams):
+    """Host-only octree plan: (levels, boxes per level, poles per level, perm)."""
+    verts = np.ascontiguousarray(mesh.verts, dtype=np.float64)
+    rwg = np.ascontiguousarray(rwg, dtype=np.int32)
+    lev = ctypes.c_int()
+    lb = np.zeros(64, dtype=np.int32)
+    poles = np.zeros(64, dtype=np.int32)
+    perm = np.zeros(rwg.shape[0], dtype=np.int32)
+    L.check(L.lib().emfa_mlfma_plan(verts.ctypes.data_as(vp), verts.shape[0], rwg.ctypes.data_as(vp), rwg.shape[0],
+                                    ctypes.byref(mp), ctypes.byref(lev), lb.ctypes.data_as(vp), 64,
+                                    poles.ctypes.data_as(vp), perm.ctypes.data_as(vp)))
+    return lev.value, lb[: lev.value + 1].copy(), poles[: lev.value - 1].copy(), perm
+
+
+class Mlfma:
+    def __init__(self, geom: Geometry, mp: L.MlfmaParams):
+        self.geom = geom
+        self.ctx = geom.ctx
+        self.h = vp()
+        self.ctx.check(L.lib().emfa_mlfma_create(self.ctx.h, geom.h, ctypes.byref(mp), ctypes.byref(self.h)))
+        lev = ctypes.c_int()
+        nnz = ctypes.c_size_t()
+        self.perm = np.zeros(geom.n, dtype=np.int32)
+        lb = np.zeros(64, dtype=np.int32)
+        poles = np.zeros(64, dtype=np.int32)
+        self.ctx.check(L.lib().emfa_mlfma_info(self.h, ctypes.byref(lev), lb.ctypes.data_as(vp),
+                                               poles.ctypes.data_as(vp), ctypes.byref(nnz),
+                                               self.perm.ctypes.data_as(vp)))
+        self.levels = lev.value
+        self.level_boxes = lb[: lev.value + 1].copy()
+        self.poles = poles[: lev.value - 1].copy()
+        self.nnz = nnz.value
+
+    def close(self):
+        if self.h:
+            L.lib().emfa_mlfma_destroy(self.h)
+            self.h = vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def apply(self, X):
+        torch = _torch()
+        X = X.reshape(-1, self.geom.n).contiguous()
+        Y = torch.empty_like(X)
+        torch.cuda.current_stream().synchronize()
+        self.ctx.check(L.lib().emfa_mlfma_apply(self.h, _ptr(X), _ptr(Y), X.shape[0], None))
+        self.ctx.synchronize()
+        return Y
+
+    def apply_part(self, x, part):
+        """part 0: near + far, 1: near only, 2: far only (one vector)."""
+        torch = _torch()
+        x = x.reshape(self.geom.n).contiguous()
+        y = torch.empty_like(x)
+        torch.cuda.current_stream().synchronize()
+        self.ctx.check(L.lib().emfa_mlfma_apply_part(self.h, _ptr(x), _ptr(y), int(part), None))
+        self.ctx.synchronize()
+        return y
+
+    def fill_v(self, angles):
+        torch = _torch()
+        a = np.ascontiguousarray(np.atleast_2d(angles), dtype=np.float64)
+        V = torch.empty((a.shape[0], self.geom.n), dtype=torch.complex64, device="cuda:%d" % self.ctx.device)
+        torch.cuda.current_stream().synchronize()
+        self.ctx.check(L.lib().emfa_mlfma_fill_v(self.h, a.ctypes.data_as(vp), a.shape[0], _ptr(V), None))
+        return V
+
+    def solve(self, B, sp: L.SolverParams):
+        torch = _torch()
+        X = torch.empty(B.shape, dtype=torch.complex128, device=B.device)
+        info = L.SolveInfo()
+        torch.cuda.current_stream().synchronize()
+        st = L.lib().emfa_mlfma_solve(self.h, _ptr(B), B.shape[0], _ptr(X), ctypes.byref(sp), ctypes.byref(info),
+                                      None)
+        if st not in (L.EMFA_OK, 4):
+            self.ctx.check(st)
+        return X, info
+
+    def unpermute(self, Xbox):
+        torch = _torch()
+        X = torch.empty_like(Xbox)
+        self.ctx.check(L.lib().emfa_mlfma_unpermute(self.h, _ptr(Xbox), Xbox.shape[0], _ptr(X), None))
+        return X

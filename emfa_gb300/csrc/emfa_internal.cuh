@@ -52,6 +52,11 @@ struct DevBuf {
     DevBuf() = default;
     DevBuf(const DevBuf&) = delete;
     DevBuf& operator=(const DevBuf&) = delete;
+    DevBuf(DevBuf&& o) noexcept : ctx(o.ctx), ptr(o.ptr), bytes(o.bytes)
+    {
+        o.ptr = nullptr;
+        o.bytes = 0;
+    }
     ~DevBuf() { release(); }
     emfa_status_t alloc(Ctx* c, size_t b)
     {

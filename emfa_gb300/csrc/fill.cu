@@ -12,6 +12,7 @@
 // pairs run in the fill precision (FP32 for the mixed path, FP64 plain).
 #include "emfa_internal.cuh"
 #include "emfa_math.cuh"
+#include "fill_entry.cuh"
 
 namespace emfa {
 
@@ -167,99 +168,6 @@ __global__ void k_singular_table(const double* __restrict__ vd, const int* __res
 // ---------------------------------------------------------------------------
 // entry kernel: one thread per Z(f, s); a warp runs 32 consecutive s of one f
 // ---------------------------------------------------------------------------
-template <typename T>
-struct FillConst {
-    T k, kpi, inv_k2;      // k, k / pi, 1 / k^2
-    T ce, cm;              // regular-pair scale: EFIE ce = w^2; CFIE ce = alpha k Z0 w^2 / 4pi, cm = (1-alpha) Z0 w^2 / 16pi
-    double coef_efie;      // EFIE: k Z0 / 4pi (the j is applied in the epilogue)
-    T thr_edm;             // 3 lambda
-    int edm_mode;
-    T z0, pi;
-};
-
-// regular pair, unsigned: ze = sum_pq (rf.rs/4 - 1/k^2) G,
-// zm = sum_pq [rf . (n x (d x rs))] (1 + j kR) G / R^2  (d = P_p - Q_q)
-template <typename T, bool MFIE>
-__device__ __forceinline__ void regular_pair(const T (&P)[3][3], const T (&Q)[3][3], const T (&vf)[3],
-                                             const T (&vs)[3], const T (&nf)[3], const FillConst<T>& c,
-                                             Cx<T>& ze, Cx<T>& zm)
-{
-    V3<T> n = v3(nf[0], nf[1], nf[2]);
-    V3<T> rs[3];
-    T nrs[3];
-#pragma unroll
-    for (int q = 0; q < 3; ++q) {
-        rs[q] = v3(Q[q][0] - vs[0], Q[q][1] - vs[1], Q[q][2] - vs[2]);
-        nrs[q] = dot(n, rs[q]);
-    }
-#pragma unroll
-    for (int p = 0; p < 3; ++p) {
-        V3<T> pp = v3(P[p][0], P[p][1], P[p][2]);
-        V3<T> rf = v3(P[p][0] - vf[0], P[p][1] - vf[1], P[p][2] - vf[2]);
-#pragma unroll
-        for (int q = 0; q < 3; ++q) {
-            V3<T> d = v3(pp.x - Q[q][0], pp.y - Q[q][1], pp.z - Q[q][2]);
-            // IEEE sqrt and reciprocal: the four triangle-pair terms of a far
-            // RWG pair nearly cancel, so G needs every bit it can keep
-            T r = sqrt(dot(d, d));
-            T rinv = T(1) / r;
-            T sn, cs;
-            sincos_pi(r * c.kpi, &sn, &cs);
-            T gr = cs * rinv, gi = -sn * rinv;
-            T rfrs = dot(rf, rs[q]);
-            T e = T(0.25) * rfrs - c.inv_k2;
-            ze.re += e * gr;
-            ze.im += e * gi;
-            if (MFIE) {
-                T m = dot(rf, d) * nrs[q] - rfrs * dot(n, d);
-                T t = m * (rinv * rinv);
-                T kr = r * c.k;
-                T hr = gr - kr * gi, hi = gi + kr * gr;
-                zm.re += t * hr;
-                zm.im += t * hi;
-            }
-        }
-    }
-}
-
-template <typename T>
-__device__ __forceinline__ void load_side(const RwgPack<T>& pk, int s, T (&q)[3][3], T (&v)[3], T (&n)[3])
-{
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-        for (int j = 0; j < 3; ++j) q[i][j] = pk.q3[s][i][j];
-#pragma unroll
-    for (int j = 0; j < 3; ++j) {
-        v[j] = pk.v[s][j];
-        n[j] = pk.n[s][j];
-    }
-}
-
-// EFIE::EDMKernel (EFIE.cpp:544-566)
-template <typename T>
-__device__ Cx<T> edm_value(const RwgPack<T>& F, const RwgPack<T>& S, const FillConst<T>& c)
-{
-    V3<T> fcp = v3(F.cen[0][0], F.cen[0][1], F.cen[0][2]), fcm = v3(F.cen[1][0], F.cen[1][1], F.cen[1][2]);
-    V3<T> scp = v3(S.cen[0][0], S.cen[0][1], S.cen[0][2]), scm = v3(S.cen[1][0], S.cen[1][1], S.cen[1][2]);
-    V3<T> R = divr(fcp + fcm, T(2)) - divr(scp + scm, T(2));
-    T Rn = norm(R);
-    V3<T> ms = (scm - scp) * S.len;
-    T ir2 = T(1) / (Rn * Rn);
-    Cx<T> C = cx(ir2, -ir2 / (c.k * Rn));
-    V3<T> Ms = divr(R * dot(R, ms), Rn * Rn);
-    Cx<T> f1 = cx(C.re, c.k / Rn + C.im);
-    T sn, cs;
-    sincos_pi(Rn * c.kpi, &sn, &cs);
-    Cx<T> ph = cx(cs, -sn) * (c.z0 / (T(4) * c.pi));
-    V3<T> a = Ms - ms, b = Ms * T(2);
-    V3<T> dl = fcm - fcp;
-    // E . dl with E = (a f1 + b C) ph
-    Cx<T> e = f1 * dot(a, dl) + C * dot(b, dl);
-    e = e * ph;
-    return e * (-F.len);
-}
-
 template <typename T, bool CFIE>
 __global__ void __launch_bounds__(256) k_fill_z(const RwgPack<T>* __restrict__ rw, int n, FillConst<T> c,
                                                 const double2* __restrict__ sing, Cx<T>* __restrict__ Z, size_t ldz)
@@ -267,64 +175,7 @@ __global__ void __launch_bounds__(256) k_fill_z(const RwgPack<T>* __restrict__ r
     int s = blockIdx.x * 32 + threadIdx.x;
     int f = blockIdx.y * blockDim.y + threadIdx.y;
     if (s >= n || f >= n) return;
-    const RwgPack<T>& F = rw[f];
-    const RwgPack<T>& S = rw[s];
-    Cx<T>* out = Z + (size_t)f * ldz + s;
-    if (!CFIE && c.edm_mode != 2) {
-        V3<T> fc = divr(v3(F.cen[0][0], F.cen[0][1], F.cen[0][2]) + v3(F.cen[1][0], F.cen[1][1], F.cen[1][2]), T(2));
-        V3<T> sc = divr(v3(S.cen[0][0], S.cen[0][1], S.cen[0][2]) + v3(S.cen[1][0], S.cen[1][1], S.cen[1][2]), T(2));
-        if (norm(fc - sc) > c.thr_edm) {
-            *out = c.edm_mode == 1 ? edm_value(F, S, c) : cx(T(0), T(0));
-            return;
-        }
-    }
-    Cx<T> ze = cx(T(0), T(0)), zm = cx(T(0), T(0));
-    double sr = 0.0, si = 0.0;
-#pragma unroll 1
-    for (int a = 0; a < 2; ++a) {
-        T P[3][3], vf[3], nf[3];
-        load_side(F, a, P, vf, nf);
-#pragma unroll 1
-        for (int b = 0; b < 2; ++b) {
-            T sgn = (a == b) ? T(1) : T(-1);
-            if (F.tri[a] == S.tri[b]) {
-                int id = 9 * F.tri[a] + 3 * F.e[a] + S.e[b];
-                if (CFIE) {
-                    double2 v = sing[id];
-                    sr += (double)sgn * v.x;
-                    si += (double)sgn * v.y;
-                } else {
-                    double2 v = sing[3 * id + ((a == 0 && b == 0) ? 0 : 1)];
-                    double2 g = sing[3 * id + 2];
-                    sr += (double)sgn * v.x + g.x;
-                    si += (double)sgn * v.y + g.y;
-                }
-                continue;
-            }
-            T Q[3][3], vs[3], ns[3];
-            load_side(S, b, Q, vs, ns);
-            Cx<T> e = cx(T(0), T(0)), m = cx(T(0), T(0));
-            regular_pair<T, CFIE>(P, Q, vf, vs, nf, c, e, m);
-            ze.re += sgn * e.re;
-            ze.im += sgn * e.im;
-            if (CFIE) {
-                zm.re += sgn * m.re;
-                zm.im += sgn * m.im;
-            }
-        }
-    }
-    T l = F.len * S.len;
-    if (CFIE) {
-        // lf ls [ j ce ze + cm zm + singular ]
-        T re = -c.ce * ze.im + c.cm * zm.re + (T)sr;
-        T im = c.ce * ze.re + c.cm * zm.im + (T)si;
-        *out = cx(re * l, im * l);
-    } else {
-        // j (k Z0 / 4pi) lf ls (w^2 ze + singular)
-        T kz = (T)c.coef_efie * l;
-        T re = c.ce * ze.re + (T)sr, im = c.ce * ze.im + (T)si;
-        *out = cx(-kz * im, kz * re);
-    }
+    Z[(size_t)f * ldz + s] = z_entry<T, CFIE>(rw[f], rw[s], c, sing);
 }
 
 // ---------------------------------------------------------------------------
@@ -388,15 +239,37 @@ static emfa_status_t fill_z_t(Ctx* c, Geom* g, GeomDev<T>& d, const emfa_fill_pa
 {
     const bool cfie = p->kind == EMFA_CFIE;
     // singular table (FP64), 9 (CFIE) or 27 (EFIE) double2 per triangle
-    DevBuf tab, vd;
-    EMFA_TRY(tab.alloc(c, sizeof(double2) * (size_t)g->nt * (cfie ? 9 : 27)));
+    void* tab = nullptr;
+    EMFA_TRY(ctx_workspace(c, WS_FILL, sizeof(double2) * (size_t)g->nt * (cfie ? 9 : 27), &tab));
+    EMFA_TRY(build_singular_table(c, g, p, (double2*)tab, st));
+    FillConst<T> fc = make_fill_const<T>(p);
+    dim3 blk(32, 8);
+    dim3 grd((g->n + 31) / 32, (g->n + 7) / 8);
+    if (cfie)
+        k_fill_z<T, true><<<grd, blk, 0, st>>>(dptr<RwgPack<T>>(d.rwg), g->n, fc, (const double2*)tab,
+                                               reinterpret_cast<Cx<T>*>(Z), ldz);
+    else
+        k_fill_z<T, false><<<grd, blk, 0, st>>>(dptr<RwgPack<T>>(d.rwg), g->n, fc, (const double2*)tab,
+                                                reinterpret_cast<Cx<T>*>(Z), ldz);
+    c->kernel_launches += 1;
+    EMFA_CUDA(c, cudaGetLastError());
+    EMFA_CUDA(c, cudaStreamSynchronize(st));
+    return EMFA_OK;
+}
+
+emfa_status_t build_singular_table(Ctx* c, Geom* g, const emfa_fill_params_t* p, double2* tab, cudaStream_t st)
+{
+    const bool cfie = p->kind == EMFA_CFIE;
+    if (p->precision == EMFA_F64)
+        EMFA_TRY(geom_prepare_f64(g, st));
+    else
+        EMFA_TRY(geom_prepare_f32(g, st));
+    // the table's vertices and k: the fill precision's k, in FP64 arithmetic
+    DevBuf vd;
     EMFA_TRY(vd.alloc(c, sizeof(double) * 3 * (size_t)g->nv));
     EMFA_CUDA(c, cudaMemcpyAsync(vd.ptr, g->verts.data(), vd.bytes, cudaMemcpyHostToDevice, st));
     SingConst sc;
-    // constants of the self terms in FP64 from the fill-precision k, so both
-    // parts of the matrix see the same wavenumber
-    T kt = Phys<T>::wavenumber(p->freq);
-    sc.k = (double)kt;
+    sc.k = p->precision == EMFA_F64 ? Phys<double>::wavenumber(p->freq) : (double)Phys<float>::wavenumber(p->freq);
     sc.inv_k2 = 1.0 / (sc.k * sc.k);
     sc.w = 1.0 / 3.0;
     sc.alpha = p->alpha;
@@ -405,39 +278,11 @@ static emfa_status_t fill_z_t(Ctx* c, Geom* g, GeomDev<T>& d, const emfa_fill_pa
     sc.sig_re = p->sigma_re;
     sc.sig_im = p->sigma_im;
     sc.cfie = cfie;
-    k_singular_table<<<(9 * g->nt + 127) / 128, 128, 0, st>>>(dptr<double>(vd), dptr<int>(d.tris), g->nt, sc,
-                                                              dptr<double2>(tab));
-    FillConst<T> fc;
-    const T pi = Phys<T>::pi(), z0 = Phys<T>::z0();
-    T w = T(1) / T(3);
-    T w2 = w * w;
-    fc.k = kt;
-    fc.kpi = kt / pi;
-    fc.inv_k2 = T(1) / (kt * kt);
-    fc.pi = pi;
-    fc.z0 = z0;
-    if (cfie) {
-        fc.ce = (T)p->alpha * (kt * z0 / (T(4) * pi)) * w2;
-        fc.cm = (T(1) - (T)p->alpha) * (z0 / (T(16) * pi)) * w2;
-    } else {
-        fc.ce = w2;
-        fc.cm = 0;
-    }
-    fc.coef_efie = (double)(kt * z0 / (T(4) * pi));
-    fc.thr_edm = T(3) * Phys<T>::c0() / (T)p->freq;
-    fc.edm_mode = p->edm_mode;
-    dim3 blk(32, 8);
-    dim3 grd((g->n + 31) / 32, (g->n + 7) / 8);
-    if (cfie)
-        k_fill_z<T, true><<<grd, blk, 0, st>>>(dptr<RwgPack<T>>(d.rwg), g->n, fc, dptr<double2>(tab),
-                                               reinterpret_cast<Cx<T>*>(Z), ldz);
-    else
-        k_fill_z<T, false><<<grd, blk, 0, st>>>(dptr<RwgPack<T>>(d.rwg), g->n, fc, dptr<double2>(tab),
-                                                reinterpret_cast<Cx<T>*>(Z), ldz);
-    c->kernel_launches += 2;
+    const int* tris = p->precision == EMFA_F64 ? dptr<int>(g->g64.tris) : dptr<int>(g->g32.tris);
+    k_singular_table<<<(9 * g->nt + 127) / 128, 128, 0, st>>>(dptr<double>(vd), tris, g->nt, sc, tab);
+    c->kernel_launches += 1;
     EMFA_CUDA(c, cudaGetLastError());
-    // the table and vertex buffers are freed on return: wait for the kernels
-    EMFA_CUDA(c, cudaStreamSynchronize(st));
+    EMFA_CUDA(c, cudaStreamSynchronize(st));  // vd is released on return
     return EMFA_OK;
 }
 

@@ -19,6 +19,24 @@ namespace emfa {
 emfa_status_t cgemm_tf32(Ctx* c, const void* Z, size_t ldz, const void* X, int n, int nrhs, void* Y, cudaStream_t st);
 // reads the tensor-core GEMM's error word (synchronises the stream)
 emfa_status_t gemm_check_error(Ctx* c, cudaStream_t st);
+// Linear operator driven by the batched Krylov solvers (krylov.cu): the
+// dense impedance matrix or the MLFMA operator.
+struct LinOp {
+    int n = 0;
+    int prec = EMFA_F32;  // EMFA_F32: iteration vectors complex64; EMFA_F64: complex128
+    virtual ~LinOp() {}
+    // Y = A X in the iteration precision (nrhs vectors, RHS-major)
+    virtual emfa_status_t apply(Ctx* c, const void* X, void* Y, int nrhs, cudaStream_t st) = 0;
+    // R = B - A X, accurate: X and R complex128, B in the iteration precision;
+    // xt: complex64 scratch of nrhs * n
+    virtual emfa_status_t residual(Ctx* c, const double2* X, const void* B, double2* R, int nrhs, float2* xt,
+                                   cudaStream_t st) = 0;
+    // error word of asynchronous device-side checks (synchronises)
+    virtual emfa_status_t check(Ctx*, cudaStream_t) { return EMFA_OK; }
+};
+
+emfa_status_t solve_op(Ctx* c, LinOp& A, const void* B, int nrhs, void* X, const emfa_solver_params_t* sp,
+                       emfa_solve_info_t* info, cudaStream_t st);
 // dense multi-RHS solve (krylov.cu)
 emfa_status_t solve_dense(Ctx* c, int prec, const void* Z, int n, const void* B, int nrhs, void* X,
                           const emfa_solver_params_t* sp, emfa_solve_info_t* info, cudaStream_t st);

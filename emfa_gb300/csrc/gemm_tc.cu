@@ -33,7 +33,7 @@ namespace tc {
 
 constexpr int BM = 128;
 constexpr int BK = 32;          // fp32 elements per stage row = 128 bytes = one swizzle atom
-constexpr int STAGES = 4;
+constexpr int STAGES = 6;
 constexpr int THREADS = 192;
 constexpr long long WAIT_CYCLES = 4000000000LL;  // ~2 s at 2 GHz
 
@@ -153,7 +153,9 @@ __global__ void __launch_bounds__(THREADS, 1)
     uint32_t* tmem_slot = (uint32_t*)(accum + 1);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int f0 = blockIdx.x * BM, c0 = blockIdx.y * BN;
+    // grid x = column tiles, y = row tiles: the CTAs sharing a row block of Z
+    // run back to back, so the block is read from DRAM once and reused in L2
+    const int f0 = blockIdx.y * BM, c0 = blockIdx.x * BN;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; ++s) {
@@ -305,7 +307,7 @@ static emfa_status_t launch_tc(Ctx* c, const CUtensorMap& ta, const CUtensorMap&
         EMFA_CUDA(c, cudaFuncSetAttribute(tc::k_gemm_tf32<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, S::TOTAL));
         attr = true;
     }
-    dim3 grd((n + tc::BM - 1) / tc::BM, (2 * nrhs + BN - 1) / BN);
+    dim3 grd((2 * nrhs + BN - 1) / BN, (n + tc::BM - 1) / tc::BM);
     int kblocks = (2 * n + tc::BK - 1) / tc::BK;
     tc::k_gemm_tf32<BN><<<grd, tc::THREADS, S::TOTAL, st>>>(ta, tb, Y, n, nrhs, kblocks, err);
     c->kernel_launches += 1;
@@ -330,13 +332,14 @@ emfa_status_t cgemm_tf32(Ctx* c, const void* Z, size_t ldz, const void* X, int n
                                                                                  (float2*)bp);
     c->kernel_launches += 1;
     CUtensorMap ta, tb;
-    const int BN = 2 * nrhs <= 64 ? 64 : 240;
+    // 144 columns: 720 outputs (360 RHS) = 5 tiles, 300 CTAs = 1.97 waves on 152 SMs
+    const int BN = 2 * nrhs <= 64 ? 64 : 144;
     EMFA_TRY(make_map(c, &ta, Z, 2 * (uint64_t)n, (uint64_t)n, ldz * 8, tc::BM));
     EMFA_TRY(make_map(c, &tb, bp, 2 * (uint64_t)n, 2 * (uint64_t)nrhs, (uint64_t)n * 8, BN));
     if (BN == 64)
         EMFA_TRY(launch_tc<64>(c, ta, tb, (float2*)Y, n, nrhs, err, st));
     else
-        EMFA_TRY(launch_tc<240>(c, ta, tb, (float2*)Y, n, nrhs, err, st));
+        EMFA_TRY(launch_tc<144>(c, ta, tb, (float2*)Y, n, nrhs, err, st));
     return EMFA_OK;
 }
 

@@ -286,6 +286,140 @@ __global__ void __launch_bounds__(KB) k_norm2(const double2* __restrict__ X, int
     block_reduce_write<double>(a1, a2, 1, partial + ((size_t)r * nblk + blk), 1);
 }
 
+// ---------------------------------------------------------------------------
+// Gram-Schmidt passes, second form (low register pressure, many loads in
+// flight).  k_vdots: CTA per (chunk of N, RHS); warp w takes basis vectors
+// w, w+8, ...; lanes stride the chunk with 4 independent loads in flight; the
+// W chunk stays in L1 across the warp's vectors.  k_vupdate: thread per
+// element, W -= sum_i h_i V_i with 8 vectors in flight, optional |W|^2.
+// Sums within a warp are in the storage precision, across warps and blocks
+// in FP64.
+// ---------------------------------------------------------------------------
+constexpr int VCHUNK = 1024;
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_vdots(const Cx<T>* __restrict__ V, size_t vstride, int nv,
+                                               const Cx<T>* __restrict__ W, int n, int nrhs, int nblk,
+                                               double2* __restrict__ partial)
+{
+    using A = typename Acc<T>::type;
+    const int blk = blockIdx.x, r = blockIdx.y;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const size_t base = (size_t)r * n;
+    const int k0 = blk * VCHUNK, k1 = min(n, k0 + VCHUNK);
+    for (int i = warp; i < nv; i += 8) {
+        const Cx<T>* vi = V + (size_t)i * vstride + base;
+        A re = 0, im = 0;
+        for (int k = k0 + lane; k < k1; k += 128) {
+            Cx<T> v[4], w[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int kk = k + 32 * u;
+                v[u] = kk < k1 ? vi[kk] : Cx<T>{T(0), T(0)};
+                w[u] = kk < k1 ? W[base + kk] : Cx<T>{T(0), T(0)};
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                re += (A)v[u].re * (A)w[u].re + (A)v[u].im * (A)w[u].im;
+                im += (A)v[u].re * (A)w[u].im - (A)v[u].im * (A)w[u].re;
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            re += __shfl_xor_sync(0xffffffffu, re, o);
+            im += __shfl_xor_sync(0xffffffffu, im, o);
+        }
+        if (lane == 0) partial[((size_t)i * nrhs + r) * nblk + blk] = make_double2((double)re, (double)im);
+    }
+}
+
+template <typename T, bool NORM>
+__global__ void __launch_bounds__(256) k_vupdate(const Cx<T>* __restrict__ V, size_t vstride, int nv,
+                                                 const double2* __restrict__ h, Cx<T>* __restrict__ W, int n,
+                                                 int nrhs, int nblk, double2* __restrict__ pnorm)
+{
+    using A = typename Acc<T>::type;
+    const int blk = blockIdx.x, r = blockIdx.y;
+    const size_t base = (size_t)r * n;
+    __shared__ A hs[2][64];
+    __shared__ double red[8];
+    for (int i = threadIdx.x; i < nv; i += blockDim.x) {
+        double2 t = h[(size_t)i * nrhs + r];
+        hs[0][i] = (A)t.x;
+        hs[1][i] = (A)t.y;
+    }
+    __syncthreads();
+    A nr = 0;
+    const int k0 = blk * VCHUNK, k1 = min(n, k0 + VCHUNK);
+    for (int k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
+        const Cx<T>* vk = V + base + k;
+        A sr = 0, si = 0;
+        int i = 0;
+        for (; i + 8 <= nv; i += 8) {
+            Cx<T> v[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) v[u] = vk[(size_t)(i + u) * vstride];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const A hr = hs[0][i + u], hi = hs[1][i + u];
+                sr += hr * (A)v[u].re - hi * (A)v[u].im;
+                si += hr * (A)v[u].im + hi * (A)v[u].re;
+            }
+        }
+        for (; i < nv; ++i) {
+            const Cx<T> v = vk[(size_t)i * vstride];
+            const A hr = hs[0][i], hi = hs[1][i];
+            sr += hr * (A)v.re - hi * (A)v.im;
+            si += hr * (A)v.im + hi * (A)v.re;
+        }
+        Cx<T> w = W[base + k];
+        w.re = (T)((A)w.re - sr);
+        w.im = (T)((A)w.im - si);
+        W[base + k] = w;
+        if (NORM) nr += (A)w.re * (A)w.re + (A)w.im * (A)w.im;
+    }
+    if (NORM) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) nr += __shfl_xor_sync(0xffffffffu, nr, o);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = (double)nr;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double t = 0;
+            for (int q = 0; q < (int)(blockDim.x >> 5); ++q) t += red[q];
+            pnorm[(size_t)r * nblk + blk] = make_double2(t, 0.0);
+        }
+    }
+}
+
+// X[r][k] += sum_i y_i V_i[r][k]; the sum in the basis precision, added to
+// the FP64 iterate once
+template <typename T>
+__global__ void k_update_x2(const Cx<T>* __restrict__ V, size_t vstride, int nvmax, const double2* __restrict__ y,
+                            const int* __restrict__ jlen, double2* __restrict__ X, int n, int nrhs)
+{
+    using A = typename Acc<T>::type;
+    const int r = blockIdx.y;
+    __shared__ A ys[2][64];
+    const int jl = min(jlen[r], nvmax);
+    for (int i = threadIdx.x; i < jl; i += blockDim.x) {
+        double2 t = y[(size_t)i * nrhs + r];
+        ys[0][i] = (A)t.x;
+        ys[1][i] = (A)t.y;
+    }
+    __syncthreads();
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    size_t o = (size_t)r * n + k;
+    A sr = 0, si = 0;
+    for (int i = 0; i < jl; ++i) {
+        const Cx<T> v = V[(size_t)i * vstride + o];
+        sr += ys[0][i] * (A)v.re - ys[1][i] * (A)v.im;
+        si += ys[0][i] * (A)v.im + ys[1][i] * (A)v.re;
+    }
+    double2 x = X[o];
+    X[o] = make_double2(x.x + (double)sr, x.y + (double)si);
+}
+
 // per-RHS: finish Arnoldi column j, rotate, test convergence
 __global__ void k_arnoldi_finish(GmresDev s, int j, const double2* __restrict__ pnorm, int nblk)
 {
@@ -497,15 +631,17 @@ static emfa_status_t dots(Ctx* c, const Cx<T>* V, size_t vstride, int nv, const 
 static int grid1(size_t tot) { return (int)std::min<size_t>((tot + 255) / 256, 8192); }
 
 template <typename T>
-static emfa_status_t gmres_t(Ctx* c, int prec, const void* Z, int n, const void* B, int nrhs, double2* X,
-                             const emfa_solver_params_t* sp, emfa_solve_info_t* info, cudaStream_t st)
+static emfa_status_t gmres_t(Ctx* c, LinOp& A, const void* B, int nrhs, double2* X, const emfa_solver_params_t* sp,
+                             emfa_solve_info_t* info, cudaStream_t st)
 {
+    const int n = A.n, prec = A.prec;
     const int m = std::max(1, std::min(sp->restart > 0 ? sp->restart : 30, MAXV - 1));
     const size_t vec = (size_t)n * nrhs;
     // vector-pass grid: ~2 CTAs per SM over (chunks of N) x (right-hand sides)
     const int sms = c->sm_count > 0 ? c->sm_count : 148;
     const int nblk = std::max(1, std::min((2 * sms + nrhs - 1) / nrhs, (n + 4 * KB - 1) / (4 * KB)));
     const int chunk = (n + nblk - 1) / nblk;
+    const int vblk = (n + VCHUNK - 1) / VCHUNK;  // chunks of the Gram-Schmidt passes
     // one workspace for the whole solve (reused across solves of a context)
     const size_t need = Carver::round(sizeof(Cx<T>) * vec * (m + 1)) + Carver::round(sizeof(Cx<T>) * vec) +
                         Carver::round(sizeof(double2) * vec) + Carver::round(sizeof(float2) * vec) +
@@ -513,8 +649,8 @@ static emfa_status_t gmres_t(Ctx* c, int prec, const void* Z, int n, const void*
                         Carver::round(sizeof(double) * (size_t)nrhs * m) +
                         Carver::round(sizeof(double2) * (size_t)nrhs * m) * 2 +
                         Carver::round(sizeof(double2) * (size_t)nrhs * (m + 1)) * 2 +
-                        Carver::round(sizeof(double2) * (size_t)nrhs * (m + 1) * nblk) +
-                        Carver::round(sizeof(double2) * (size_t)nrhs * nblk) +
+                        Carver::round(sizeof(double2) * (size_t)nrhs * (m + 1) * std::max(nblk, (n + VCHUNK - 1) / VCHUNK)) +
+                        Carver::round(sizeof(double2) * (size_t)nrhs * std::max(nblk, (n + VCHUNK - 1) / VCHUNK)) +
                         Carver::round(sizeof(double) * 4 * (size_t)nrhs) + Carver::round(sizeof(int) * 2 * (size_t)nrhs) +
                         Carver::round(sizeof(int) * 4) + 4096;
     void* wsp = nullptr;
@@ -535,8 +671,9 @@ static emfa_status_t gmres_t(Ctx* c, int prec, const void* Z, int n, const void*
     s.y = cv.take<double2>((size_t)nrhs * m);
     s.g = cv.take<double2>((size_t)nrhs * (m + 1));
     s.hcol = cv.take<double2>((size_t)nrhs * (m + 1));
-    double2* partial = cv.take<double2>((size_t)nrhs * (m + 1) * nblk);
-    double2* pnorm = cv.take<double2>((size_t)nrhs * nblk);
+    const int pb = std::max(nblk, (n + VCHUNK - 1) / VCHUNK);
+    double2* partial = cv.take<double2>((size_t)nrhs * (m + 1) * pb);
+    double2* pnorm = cv.take<double2>((size_t)nrhs * pb);
     s.bnorm = cv.take<double>(4 * (size_t)nrhs);
     s.scale = s.bnorm + nrhs;
     s.est = s.scale + nrhs;
@@ -544,8 +681,6 @@ static emfa_status_t gmres_t(Ctx* c, int prec, const void* Z, int n, const void*
     s.jlen = cv.take<int>(2 * (size_t)nrhs);
     s.active = s.jlen + nrhs;
     s.counters = cv.take<int>(4);
-    // inner product: tensor cores (TF32) for the mixed path when the shape allows
-    const bool use_tc = prec == EMFA_F32 && (sp->matvec == EMFA_MV_AUTO || sp->matvec == EMFA_MV_TF32) && (n % 2 == 0);
 
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
@@ -563,12 +698,8 @@ static emfa_status_t gmres_t(Ctx* c, int prec, const void* Z, int n, const void*
                 EMFA_CUDA(c, cudaMemcpyAsync(R, B, sizeof(double2) * vec, cudaMemcpyDeviceToDevice, st));
             else
                 k_to_f64<<<grid1(vec), 256, 0, st>>>((const float2*)B, R, vec);
-        } else if (prec == EMFA_F64) {
-            EMFA_TRY(cgemm_f64(c, Z, n, X, n, nrhs, R, st));  // R = Z X
-            k_residual<double2><<<grid1(vec), 256, 0, st>>>((const double2*)B, R, R, vec);
         } else {
-            k_to_f32<<<grid1(vec), 256, 0, st>>>(X, Xt, vec);
-            EMFA_TRY(cgemm_f32_chunked(c, Z, n, Xt, n, nrhs, B, R, st));  // R = B - Z X
+            EMFA_TRY(A.residual(c, X, B, R, nrhs, Xt, st));
         }
         k_norm2<<<dim3(nblk, nrhs), KB, 0, st>>>(R, n, nblk, chunk, pnorm);
         EMFA_CUDA(c, cudaMemsetAsync(s.counters, 0, sizeof(int) * 4, st));
@@ -584,24 +715,20 @@ static emfa_status_t gmres_t(Ctx* c, int prec, const void* Z, int n, const void*
         int steps = 0;
         for (int j = 0; j < m; ++j) {
             Cx<T>* Vj = V + (size_t)j * vec;
-            // W = Z V_j
-            if (prec == EMFA_F64)
-                EMFA_TRY(cgemm_f64(c, Z, n, Vj, n, nrhs, W, st));
-            else if (use_tc)
-                EMFA_TRY(cgemm_tf32(c, Z, n, Vj, n, nrhs, W, st));
-            else
-                EMFA_TRY(cgemm_f32(c, Z, n, Vj, n, nrhs, W, st));
-            // CGS2 in three passes: h1 = V^H W; W -= V h1 and h2 = V^H W; W -= V h2 and |W|^2
-            const dim3 vg(nblk, nrhs);
+            // W = A V_j
+            EMFA_TRY(A.apply(c, Vj, W, nrhs, st));
+            // CGS2: h1 = V^H W; W -= V h1; h2 = V^H W; W -= V h2 with |W|^2
+            const dim3 vg(vblk, nrhs);
             const int nv = j + 1;
             const int rg = (nv * nrhs + 127) / 128;
-            k_multidot<T><<<vg, KB, 0, st>>>(V, vec, nv, W, n, nrhs, nblk, chunk, partial);
-            k_reduce_partials<<<rg, 128, 0, st>>>(partial, nv, nrhs, nblk, s.hcol, 0);
-            k_cgs_update<T, true><<<vg, KB, 0, st>>>(V, vec, nv, s.hcol, W, n, nrhs, nblk, chunk, partial);
-            k_reduce_partials<<<rg, 128, 0, st>>>(partial, nv, nrhs, nblk, s.y, 0);
-            k_cgs_update<T, false><<<vg, KB, 0, st>>>(V, vec, nv, s.y, W, n, nrhs, nblk, chunk, pnorm);
+            k_vdots<T><<<vg, 256, 0, st>>>(V, vec, nv, W, n, nrhs, vblk, partial);
+            k_reduce_partials<<<rg, 128, 0, st>>>(partial, nv, nrhs, vblk, s.hcol, 0);
+            k_vupdate<T, false><<<vg, 256, 0, st>>>(V, vec, nv, s.hcol, W, n, nrhs, vblk, pnorm);
+            k_vdots<T><<<vg, 256, 0, st>>>(V, vec, nv, W, n, nrhs, vblk, partial);
+            k_reduce_partials<<<rg, 128, 0, st>>>(partial, nv, nrhs, vblk, s.y, 0);
+            k_vupdate<T, true><<<vg, 256, 0, st>>>(V, vec, nv, s.y, W, n, nrhs, vblk, pnorm);
             EMFA_CUDA(c, cudaMemsetAsync(s.counters, 0, sizeof(int), st));
-            k_arnoldi_finish<<<(nrhs + 127) / 128, 128, 0, st>>>(s, j, pnorm, nblk);
+            k_arnoldi_finish<<<(nrhs + 127) / 128, 128, 0, st>>>(s, j, pnorm, vblk);
             k_scale_store<Cx<T>, Cx<T>><<<grid1(vec), 256, 0, st>>>(W, s.scale, n, nrhs, V + (size_t)(j + 1) * vec);
             EMFA_CUDA(c, cudaMemcpyAsync(host_cnt, s.counters, sizeof(int), cudaMemcpyDeviceToHost, st));
             EMFA_CUDA(c, cudaStreamSynchronize(st));
@@ -610,9 +737,9 @@ static emfa_status_t gmres_t(Ctx* c, int prec, const void* Z, int n, const void*
             if (host_cnt[0] == 0) break;
         }
         total_iters += steps;
-        if (use_tc) EMFA_TRY(gemm_check_error(c, st));
+        EMFA_TRY(A.check(c, st));
         k_backsolve<<<(nrhs + 127) / 128, 128, 0, st>>>(s);
-        k_update_x<T><<<dim3((n + 255) / 256, nrhs), 256, 0, st>>>(V, vec, steps, s.y, s.jlen, X, n, nrhs);
+        k_update_x2<T><<<dim3((n + 255) / 256, nrhs), 256, 0, st>>>(V, vec, steps, s.y, s.jlen, X, n, nrhs);
         c->kernel_launches += 2;
         EMFA_CUDA(c, cudaGetLastError());
     }
@@ -727,14 +854,13 @@ __global__ void k_bicg_scalar(BicgDev s, int stage, const double2* __restrict__ 
     }
 }
 
-template <typename T>
-static emfa_status_t matvec_d(Ctx* c, int prec, const void* Z, int n, const double2* X, int nrhs, double2* Y,
-                              float2* tmp_in, float2* tmp_out, cudaStream_t st)
+static emfa_status_t matvec_d(Ctx* c, LinOp& A, const double2* X, int nrhs, double2* Y, float2* tmp_in,
+                              float2* tmp_out, cudaStream_t st)
 {
-    size_t vec = (size_t)n * nrhs;
-    if (prec == EMFA_F64) return cgemm_f64(c, Z, n, X, n, nrhs, Y, st);
+    size_t vec = (size_t)A.n * nrhs;
+    if (A.prec == EMFA_F64) return A.apply(c, X, Y, nrhs, st);
     k_to_f32<<<grid1(vec), 256, 0, st>>>(X, tmp_in, vec);
-    EMFA_TRY(cgemm_f32(c, Z, n, tmp_in, n, nrhs, tmp_out, st));
+    EMFA_TRY(A.apply(c, tmp_in, tmp_out, nrhs, st));
     k_to_f64<<<grid1(vec), 256, 0, st>>>(tmp_out, Y, vec);
     c->kernel_launches += 2;
     return EMFA_OK;
@@ -750,9 +876,10 @@ static emfa_status_t dots_d(Ctx* c, const double2* A, const double2* B, int n, i
     return EMFA_OK;
 }
 
-static emfa_status_t bicgstab(Ctx* c, int prec, const void* Z, int n, const void* B, int nrhs, double2* X,
-                              const emfa_solver_params_t* sp, emfa_solve_info_t* info, cudaStream_t st)
+static emfa_status_t bicgstab(Ctx* c, LinOp& A, const void* B, int nrhs, double2* X, const emfa_solver_params_t* sp,
+                              emfa_solve_info_t* info, cudaStream_t st)
 {
+    const int n = A.n, prec = A.prec;
     const size_t vec = (size_t)n * nrhs;
     const int nblk = dot_blocks(n);
     DevBuf vb, tin, tout, sc, pb, db;
@@ -807,13 +934,13 @@ static emfa_status_t bicgstab(Ctx* c, int prec, const void* Z, int n, const void
         EMFA_TRY(dots_d(c, rh, r, n, nrhs, partial, d0, st));
         k_bicg_scalar<<<(nrhs + 127) / 128, 128, 0, st>>>(s, 1, d0, nullptr);
         k_bicg_p<<<eg, 256, 0, st>>>(s, r, p, v, n);
-        EMFA_TRY(matvec_d<float>(c, prec, Z, n, p, nrhs, v, dptr<float2>(tin), dptr<float2>(tout), st));
+        EMFA_TRY(matvec_d(c, A, p, nrhs, v, dptr<float2>(tin), dptr<float2>(tout), st));
         EMFA_TRY(dots_d(c, rh, v, n, nrhs, partial, d0, st));
         k_bicg_scalar<<<(nrhs + 127) / 128, 128, 0, st>>>(s, 2, d0, nullptr);
         k_bicg_s<<<eg, 256, 0, st>>>(s, X, p, r, v, sv, n);
         EMFA_TRY(dots_d(c, sv, sv, n, nrhs, partial, d0, st));
         k_bicg_scalar<<<(nrhs + 127) / 128, 128, 0, st>>>(s, 3, d0, nullptr);
-        EMFA_TRY(matvec_d<float>(c, prec, Z, n, sv, nrhs, t, dptr<float2>(tin), dptr<float2>(tout), st));
+        EMFA_TRY(matvec_d(c, A, sv, nrhs, t, dptr<float2>(tin), dptr<float2>(tout), st));
         EMFA_TRY(dots_d(c, t, sv, n, nrhs, partial, d0, st));
         EMFA_TRY(dots_d(c, t, t, n, nrhs, partial, d1, st));
         EMFA_CUDA(c, cudaMemsetAsync(s.counters, 0, sizeof(int), st));
@@ -846,12 +973,53 @@ static emfa_status_t bicgstab(Ctx* c, int prec, const void* Z, int n, const void
     return converged == nrhs ? EMFA_OK : EMFA_ERR_NOT_CONVERGED;
 }
 
+emfa_status_t solve_op(Ctx* c, LinOp& A, const void* B, int nrhs, void* X, const emfa_solver_params_t* sp,
+                       emfa_solve_info_t* info, cudaStream_t st)
+{
+    if (sp->method == EMFA_BICGSTAB) return bicgstab(c, A, B, nrhs, (double2*)X, sp, info, st);
+    if (A.prec == EMFA_F64) return gmres_t<double>(c, A, B, nrhs, (double2*)X, sp, info, st);
+    return gmres_t<float>(c, A, B, nrhs, (double2*)X, sp, info, st);
+}
+
+// Dense impedance matrix as a Krylov operator.  Mixed path: inner products
+// on the tensor cores (TF32) or FP32 CUDA cores, refinement residual with
+// FP32 products and FP64 chunk sums.  Plain path: FP64 throughout.
+struct DenseOp : LinOp {
+    const void* Z = nullptr;
+    bool use_tc = false;
+    emfa_status_t apply(Ctx* c, const void* X, void* Y, int nrhs, cudaStream_t st) override
+    {
+        if (prec == EMFA_F64) return cgemm_f64(c, Z, n, X, n, nrhs, Y, st);
+        if (use_tc) return cgemm_tf32(c, Z, n, X, n, nrhs, Y, st);
+        return cgemm_f32(c, Z, n, X, n, nrhs, Y, st);
+    }
+    emfa_status_t residual(Ctx* c, const double2* X, const void* B, double2* R, int nrhs, float2* xt,
+                           cudaStream_t st) override
+    {
+        const size_t vec = (size_t)n * nrhs;
+        if (prec == EMFA_F64) {
+            EMFA_TRY(cgemm_f64(c, Z, n, X, n, nrhs, R, st));  // R = Z X
+            k_residual<double2><<<grid1(vec), 256, 0, st>>>((const double2*)B, R, R, vec);
+            c->kernel_launches += 1;
+            return EMFA_OK;
+        }
+        k_to_f32<<<grid1(vec), 256, 0, st>>>(X, xt, vec);
+        c->kernel_launches += 1;
+        return cgemm_f32_chunked(c, Z, n, xt, n, nrhs, B, R, st);  // R = B - Z X
+    }
+    emfa_status_t check(Ctx* c, cudaStream_t st) override { return use_tc ? gemm_check_error(c, st) : EMFA_OK; }
+};
+
 emfa_status_t solve_dense(Ctx* c, int prec, const void* Z, int n, const void* B, int nrhs, void* X,
                           const emfa_solver_params_t* sp, emfa_solve_info_t* info, cudaStream_t st)
 {
-    if (sp->method == EMFA_BICGSTAB) return bicgstab(c, prec, Z, n, B, nrhs, (double2*)X, sp, info, st);
-    if (prec == EMFA_F64) return gmres_t<double>(c, prec, Z, n, B, nrhs, (double2*)X, sp, info, st);
-    return gmres_t<float>(c, prec, Z, n, B, nrhs, (double2*)X, sp, info, st);
+    DenseOp A;
+    A.n = n;
+    A.prec = prec;
+    A.Z = Z;
+    A.use_tc = prec == EMFA_F32 && (sp->matvec == EMFA_MV_AUTO || sp->matvec == EMFA_MV_TF32) && (n % 2 == 0) &&
+               (((uintptr_t)Z & 15) == 0);
+    return solve_op(c, A, B, nrhs, X, sp, info, st);
 }
 }  // namespace emfa
 

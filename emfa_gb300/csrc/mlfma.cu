@@ -1,0 +1,1027 @@
+// Multilevel fast multipole CFIE operator (EMSolver/MLFMA.cpp).
+//
+// Host (float arithmetic, the reference's own rules, so box order, multipole
+// counts, sample points and stencils are the reference's):
+//   bounding cube and level count   MLFMA_Boundary::init (MLFMA_Boundary.cpp:15-35)
+//   octree, box order of unknowns   buildBox / buildFirstLevel / buildCurLevel (MLFMA.cpp:688-805)
+//   near / far lists                setBoxParameter (MLFMA.cpp:807-866)
+//   multipoles, Gauss-Legendre      getMultipoleNumber / levelRootsAndWeights (MLFMA.cpp:877-915)
+//   3x3 Lagrange stencils           calculateInterpolationMtr / lagrangeIPWeights (MLFMA.cpp:917-1002)
+//   translation operators           parallelLevelTrans (MLFMA.cpp:1191-1222), tabulated once per
+//                                   distinct box offset (at most 7^3 per level) instead of per box pair
+// Device (FP32 patterns, 3 Cartesian components as in the reference):
+//   k_radrec     radiation / receive patterns (MLFMA.cpp:1244-1292,1393-1422)
+//   k_near_fill  near-field CFIE blocks per (field box, near box) (MLFMA.cpp:1004-1131)
+//   per mat-vec (MLFMA.cpp:454-686):
+//     k_agg_finest    finest-level aggregation
+//     k_upward        interpolation + shift, child -> parent (gather over children)
+//     k_downward      translation from far boxes + anterpolation from the parent (gather)
+//     k_disagg_near   disaggregation at the finest level fused with the near-field product
+#include "emfa_internal.cuh"
+#include "emfa_math.cuh"
+#include "fill_entry.cuh"
+#include "gemm.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+
+namespace emfa {
+
+struct C3f {
+    float2 x, y, z;
+};
+
+__device__ __forceinline__ float2 cmulf(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+__device__ __forceinline__ float2 caddf(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 cscalef(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+__device__ __forceinline__ C3f c3zero() { return C3f{make_float2(0, 0), make_float2(0, 0), make_float2(0, 0)}; }
+__device__ __forceinline__ void c3fma(C3f& acc, float2 s, const C3f& v)
+{
+    acc.x = caddf(acc.x, cmulf(s, v.x));
+    acc.y = caddf(acc.y, cmulf(s, v.y));
+    acc.z = caddf(acc.z, cmulf(s, v.z));
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+namespace mh {
+
+const float PI = 3.14159265358979323846f;
+
+struct Box {
+    float c[3];
+    int parent = -1;
+    int oct = 0;      // child index (x*2+y)*2+z within the parent
+    int offset = 0;   // first unknown (box order)
+    std::vector<int> unk;
+    std::vector<int> child, near, far;
+};
+
+// Legendre value / derivative recurrence of GaussLegendre::Evaluation
+static void gl_eval(float x, int n, float& v, float& d)
+{
+    float vsub1 = x, vsub2 = 1;
+    float f = 1 / (x * x - 1);
+    v = 1;
+    d = 0;
+    for (int i = 2; i <= n; ++i) {
+        v = ((2 * i - 1) * x * vsub1 - (i - 1) * vsub2) / i;
+        d = i * f * (x * v - vsub1);
+        vsub2 = vsub1;
+        vsub1 = v;
+    }
+}
+
+// GaussLegendre::set (EMComponent/Quadrature.cpp:93-112): Newton from the
+// Chebyshev-like guess, float arithmetic, roots ascending
+static void gauss_legendre(int n, std::vector<float>& r, std::vector<float>& w)
+{
+    r.assign(n, 0);
+    w.assign(n, 0);
+    for (int i = 0; i < n; ++i) {
+        float x = (float)std::cos((double)(PI * (i + 0.75f) / (n + 0.5f)));
+        float v, d, dr;
+        gl_eval(x, n, v, d);
+        int guard = 0;
+        do {
+            dr = v / d;
+            x = x - dr;
+            gl_eval(x, n, v, d);
+        } while (std::fabs((double)dr) > 2e-7f && ++guard < 1000);
+        r[n - 1 - i] = x;
+        w[n - 1 - i] = 2 / ((1 - x * x) * d * d);
+    }
+}
+
+// lagrangeIPWeights (MLFMA.cpp:962-1002): 3-point stencils of the samples
+// `cur` (parent level) in the samples `nxt` (child level), clamped at the ends
+static void lagrange(const std::vector<float>& nxt, const std::vector<float>& cur, std::vector<int>& loc,
+                     std::vector<float>& el)
+{
+    size_t cols = cur.size();
+    loc.assign(3 * cols, 0);
+    el.assign(3 * cols, 0);
+    size_t nlast = nxt.size() - 1;
+    size_t nid = 2;
+    float low = nxt[1], high = nxt[nlast - 1];
+    for (size_t cid = 0; cid < cols; ++cid) {
+        const float xx = cur[cid];
+        size_t p1, p2, p3;
+        if (xx < low) {
+            p1 = 0; p2 = 1; p3 = 2;
+        } else if (xx > high) {
+            p1 = nlast - 2; p2 = nlast - 1; p3 = nlast;
+        } else {
+            nid += nxt[nid] < xx ? 1 : 0;
+            size_t off = (nxt[nid] - xx < xx - nxt[nid - 1]) ? 1 : 0;
+            p1 = nid + off - 2; p2 = nid + off - 1; p3 = nid + off;
+        }
+        loc[3 * cid] = (int)p1; loc[3 * cid + 1] = (int)p2; loc[3 * cid + 2] = (int)p3;
+        const float x0 = nxt[p1], x1 = nxt[p2], x2 = nxt[p3];
+        el[3 * cid] = (xx - x1) * (xx - x2) / ((x0 - x1) * (x0 - x2));
+        el[3 * cid + 1] = (xx - x0) * (xx - x2) / ((x1 - x0) * (x1 - x2));
+        el[3 * cid + 2] = (xx - x0) * (xx - x1) / ((x2 - x0) * (x2 - x1));
+    }
+}
+
+static float fnorm3(const float* a, const float* b)
+{
+    float x = a[0] - b[0], y = a[1] - b[1], z = a[2] - b[2];
+    return std::sqrt(x * x + y * y + z * z);
+}
+
+}  // namespace mh
+
+// per-level device data
+struct MLevel {
+    int nbox = 0, L = 0, K = 0;
+    float len = 0;
+    DevBuf parent, oct;                 // int per box
+    DevBuf child_ptr, child_idx;        // CSR children (int)
+    DevBuf far_ptr, far_box, far_off;   // CSR far lists (int)
+    DevBuf trans;                       // float2 [343][K]
+    DevBuf up, down;                    // C3f [nbox][K]
+    DevBuf ip_col, ip_w;                // interpolation to this level from the level below: [K][9]
+    DevBuf an_ptr, an_kp, an_w;         // anterpolation from the level above, transposed stencil
+    DevBuf up_phase;                    // float2 [8][K]: exp(-j k k.(parent - child)) for the level below
+    std::vector<float> w_host;          // quadrature weights (host)
+};
+
+}  // namespace emfa
+
+struct emfa_mlfma {
+    emfa::Ctx* ctx = nullptr;
+    emfa::Geom* geom = nullptr;
+    emfa_mlfma_params_t p{};
+    int levels = 0;   // finest level number L (levels 2..L carry patterns)
+    int n = 0;
+    float k = 0;
+    std::vector<int> perm;         // box order -> RWG index
+    std::vector<int> level_boxes;  // boxes per level 0..L
+    std::vector<int> poles;        // multipoles per level 2..L
+    std::vector<emfa::MLevel> lv;  // index level - 2
+    emfa::DevBuf perm_d, box_of;   // int [n]
+    emfa::DevBuf rad, rec;         // C3f [n][Kf]
+    emfa::DevBuf coeff;            // float [Kf]
+    emfa::DevBuf box_off, box_cnt; // finest boxes: first unknown, count
+    emfa::DevBuf near_ptr, near_box, near_col, row_cols;  // CSR near lists, column base per slot, C_b per box
+    emfa::DevBuf row_base;         // size_t per finest box: first value of the box's rows
+    emfa::DevBuf near_val;         // float2 [nnz]
+    size_t nnz = 0;
+    emfa::DevBuf tmp_in, tmp_out;  // complex64 scratch for residuals
+};
+
+namespace emfa {
+
+// ---------------------------------------------------------------------------
+// device kernels
+// ---------------------------------------------------------------------------
+// radiation / receive patterns of every unknown (box order) at every finest sample
+__global__ void k_radrec(const RwgPack<float>* __restrict__ rw, const int* __restrict__ perm,
+                         const int* __restrict__ box_of, const float* __restrict__ centers,
+                         const float* __restrict__ kdir, int n, int K, float k, float alpha, C3f* __restrict__ rad,
+                         C3f* __restrict__ rec)
+{
+    size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= (size_t)n * K) return;
+    const int u = (int)(id / K), kk = (int)(id % K);
+    const RwgPack<float>& R = rw[perm[u]];
+    const float* c = centers + 3 * box_of[u];
+    const V3<float> kh = v3(kdir[3 * kk], kdir[3 * kk + 1], kdir[3 * kk + 2]);
+    const V3<float> cen = v3(c[0], c[1], c[2]);
+    const float w3 = 1.0f / 3.0f;
+    float2 ra[3] = {{0, 0}, {0, 0}, {0, 0}}, rh[3] = {{0, 0}, {0, 0}, {0, 0}};
+    for (int s = 0; s < 2; ++s) {
+        const float sg = s == 0 ? 1.0f : -1.0f;
+        const V3<float> fv = v3(R.v[s][0], R.v[s][1], R.v[s][2]);
+        const V3<float> nn = v3(R.n[s][0], R.n[s][1], R.n[s][2]);
+        for (int q = 0; q < 3; ++q) {
+            const V3<float> g = v3(R.q3[s][q][0], R.q3[s][q][1], R.q3[s][q][2]);
+            const V3<float> rho = (g - fv) * (sg * w3);
+            const V3<float> nr = cross(nn, rho);
+            float sn, cs;
+            sincos_pi(k * dot(kh, g - cen) / mh::PI, &sn, &cs);
+            // rad: rho e^{+j phase}; half receive: (n x rho) e^{-j phase}
+            ra[0] = caddf(ra[0], make_float2(rho.x * cs, rho.x * sn));
+            ra[1] = caddf(ra[1], make_float2(rho.y * cs, rho.y * sn));
+            ra[2] = caddf(ra[2], make_float2(rho.z * cs, rho.z * sn));
+            rh[0] = caddf(rh[0], make_float2(nr.x * cs, -nr.x * sn));
+            rh[1] = caddf(rh[1], make_float2(nr.y * cs, -nr.y * sn));
+            rh[2] = caddf(rh[2], make_float2(nr.z * cs, -nr.z * sn));
+        }
+    }
+    // rad - (k . rad) k
+    float2 kd = make_float2(kh.x * ra[0].x + kh.y * ra[1].x + kh.z * ra[2].x, kh.x * ra[0].y + kh.y * ra[1].y + kh.z * ra[2].y);
+    ra[0] = make_float2(ra[0].x - kd.x * kh.x, ra[0].y - kd.y * kh.x);
+    ra[1] = make_float2(ra[1].x - kd.x * kh.y, ra[1].y - kd.y * kh.y);
+    ra[2] = make_float2(ra[2].x - kd.x * kh.z, ra[2].y - kd.y * kh.z);
+    // k x half-receive
+    float2 hx = make_float2(kh.y * rh[2].x - kh.z * rh[1].x, kh.y * rh[2].y - kh.z * rh[1].y);
+    float2 hy = make_float2(kh.z * rh[0].x - kh.x * rh[2].x, kh.z * rh[0].y - kh.x * rh[2].y);
+    float2 hz = make_float2(kh.x * rh[1].x - kh.y * rh[0].x, kh.x * rh[1].y - kh.y * rh[0].y);
+    const float h = R.len / 2;
+    C3f o;
+    o.x = cscalef(ra[0], h);
+    o.y = cscalef(ra[1], h);
+    o.z = cscalef(ra[2], h);
+    rad[id] = o;
+    const float b = 1.0f - alpha;
+    o.x = make_float2(h * (alpha * ra[0].x + b * hx.x), h * (-alpha * ra[0].y + b * hx.y));
+    o.y = make_float2(h * (alpha * ra[1].x + b * hy.x), h * (-alpha * ra[1].y + b * hy.y));
+    o.z = make_float2(h * (alpha * ra[2].x + b * hz.x), h * (-alpha * ra[2].y + b * hz.y));
+    rec[id] = o;
+}
+
+// near-field blocks: thread per (field unknown, near-slot); values row-major
+// per field box over the concatenated near-box columns
+__global__ void k_near_fill(const RwgPack<float>* __restrict__ rw, const int* __restrict__ perm,
+                            const int* __restrict__ box_of, const int* __restrict__ box_off,
+                            const int* __restrict__ box_cnt, const int* __restrict__ near_ptr,
+                            const int* __restrict__ near_box, const int* __restrict__ near_col,
+                            const int* __restrict__ row_cols, const size_t* __restrict__ row_base, int n,
+                            int max_near, FillConst<float> fc, const double2* __restrict__ sing,
+                            float2* __restrict__ val)
+{
+    size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= (size_t)n * max_near) return;
+    const int u = (int)(id / max_near), j = (int)(id % max_near);
+    const int b = box_of[u];
+    const int slot = near_ptr[b] + j;
+    if (slot >= near_ptr[b + 1]) return;
+    const int nb = near_box[slot];
+    const int s0 = box_off[nb], ns = box_cnt[nb];
+    const RwgPack<float> F = rw[perm[u]];
+    float2* out = val + row_base[b] + (size_t)(u - box_off[b]) * row_cols[b] + near_col[slot];
+    for (int q = 0; q < ns; ++q) {
+        Cx<float> z = z_entry<float, true>(F, rw[perm[s0 + q]], fc, sing);
+        out[q] = make_float2(z.re, z.im);
+    }
+}
+
+// finest aggregation: CTA per finest box, threads over samples
+__global__ void k_agg_finest(const float2* __restrict__ x, const C3f* __restrict__ rad,
+                             const int* __restrict__ box_off, const int* __restrict__ box_cnt, int K,
+                             C3f* __restrict__ out)
+{
+    const int b = blockIdx.x;
+    const int o = box_off[b], cnt = box_cnt[b];
+    for (int kk = threadIdx.x; kk < K; kk += blockDim.x) {
+        C3f acc = c3zero();
+        for (int u = 0; u < cnt; ++u) c3fma(acc, x[o + u], rad[(size_t)(o + u) * K + kk]);
+        out[(size_t)b * K + kk] = acc;
+    }
+}
+
+// interpolation + phase shift: parent (b, k) gathers its children's patterns
+__global__ void k_upward(const C3f* __restrict__ child, int Kc, const int* __restrict__ child_ptr,
+                         const int* __restrict__ child_idx, const int* __restrict__ child_oct,
+                         const int* __restrict__ ip_col, const float* __restrict__ ip_w,
+                         const float2* __restrict__ phase, int nbox, int K, C3f* __restrict__ out)
+{
+    size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= (size_t)nbox * K) return;
+    const int b = (int)(id / K), kp = (int)(id % K);
+    C3f acc = c3zero();
+    for (int ci = child_ptr[b]; ci < child_ptr[b + 1]; ++ci) {
+        const int c = child_idx[ci];
+        const C3f* src = child + (size_t)c * Kc;
+        C3f v = c3zero();
+#pragma unroll
+        for (int t = 0; t < 9; ++t) {
+            const float w = ip_w[kp * 9 + t];
+            const C3f& s = src[ip_col[kp * 9 + t]];
+            v.x = caddf(v.x, cscalef(s.x, w));
+            v.y = caddf(v.y, cscalef(s.y, w));
+            v.z = caddf(v.z, cscalef(s.z, w));
+        }
+        c3fma(acc, phase[child_oct[c] * K + kp], v);
+    }
+    out[id] = acc;
+}
+
+// translation from far boxes (+ anterpolation from the parent level)
+__global__ void k_downward(const C3f* __restrict__ up, const int* __restrict__ far_ptr,
+                           const int* __restrict__ far_box, const int* __restrict__ far_off,
+                           const float2* __restrict__ trans, int nbox, int K, const C3f* __restrict__ pdown, int Kp,
+                           const int* __restrict__ parent, const int* __restrict__ oct,
+                           const int* __restrict__ an_ptr, const int* __restrict__ an_kp,
+                           const float* __restrict__ an_w, const float2* __restrict__ pphase, C3f* __restrict__ out)
+{
+    size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= (size_t)nbox * K) return;
+    const int b = (int)(id / K), kk = (int)(id % K);
+    C3f acc = c3zero();
+    for (int f = far_ptr[b]; f < far_ptr[b + 1]; ++f)
+        c3fma(acc, trans[(size_t)far_off[f] * K + kk], up[(size_t)far_box[f] * K + kk]);
+    if (pdown) {
+        const C3f* src = pdown + (size_t)parent[b] * Kp;
+        const int o = oct[b];
+        for (int a = an_ptr[kk]; a < an_ptr[kk + 1]; ++a) {
+            const int kp = an_kp[a];
+            float2 ph = pphase[o * Kp + kp];
+            ph = make_float2(ph.x * an_w[a], -ph.y * an_w[a]);  // conj: exp(+j k k.(parent - child))
+            c3fma(acc, ph, src[kp]);
+        }
+    }
+    out[id] = acc;
+}
+
+// disaggregation + near field: warp per unknown (box order)
+__global__ void k_disagg_near(const float2* __restrict__ x, const C3f* __restrict__ rec,
+                              const C3f* __restrict__ down, const float* __restrict__ coeff, int K,
+                              const int* __restrict__ box_of, const int* __restrict__ box_off,
+                              const int* __restrict__ box_cnt, const int* __restrict__ near_ptr,
+                              const int* __restrict__ near_box, const int* __restrict__ near_col,
+                              const int* __restrict__ row_cols, const size_t* __restrict__ row_base,
+                              const float2* __restrict__ val, int n, int skip_near, float2* __restrict__ y)
+{
+    const int warp = (int)(((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (warp >= n) return;
+    const int u = warp, b = box_of[u];
+    float2 acc = make_float2(0, 0);
+    const C3f* rr = rec + (size_t)u * K;
+    const C3f* dd = down + (size_t)b * K;
+    for (int kk = lane; kk < K; kk += 32) {
+        const C3f r = rr[kk], d = dd[kk];
+        float2 t = caddf(caddf(cmulf(r.x, d.x), cmulf(r.y, d.y)), cmulf(r.z, d.z));
+        acc = caddf(acc, cscalef(t, coeff[kk]));
+    }
+    const float2* vrow = val + row_base[b] + (size_t)(u - box_off[b]) * row_cols[b];
+    for (int sl = skip_near ? near_ptr[b + 1] : near_ptr[b]; sl < near_ptr[b + 1]; ++sl) {
+        const int nb = near_box[sl];
+        const int s0 = box_off[nb], ns = box_cnt[nb];
+        const float2* vr = vrow + near_col[sl];
+        for (int q = lane; q < ns; q += 32) acc = caddf(acc, cmulf(vr[q], x[s0 + q]));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
+        acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
+    }
+    if (lane == 0) y[u] = acc;
+}
+
+__global__ void k_gather_c64(const float2* __restrict__ src, const int* __restrict__ idx, int n, int nrhs,
+                             float2* __restrict__ dst)
+{
+    size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= (size_t)n * nrhs) return;
+    size_t r = id / n, u = id % n;
+    dst[id] = src[r * n + idx[u]];
+}
+
+__global__ void k_scatter_c128(const double2* __restrict__ src, const int* __restrict__ idx, int n, int nrhs,
+                               double2* __restrict__ dst)
+{
+    size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= (size_t)n * nrhs) return;
+    size_t r = id / n, u = id % n;
+    dst[r * n + idx[u]] = src[id];
+}
+
+__global__ void k_resid_c64(const float2* __restrict__ B, const float2* __restrict__ Y, double2* __restrict__ R, size_t tot)
+{
+    size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id < tot) R[id] = make_double2((double)B[id].x - (double)Y[id].x, (double)B[id].y - (double)Y[id].y);
+}
+
+__global__ void k_f64_to_f32(const double2* __restrict__ X, float2* __restrict__ Y, size_t tot)
+{
+    size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id < tot) Y[id] = make_float2((float)X[id].x, (float)X[id].y);
+}
+
+// ---------------------------------------------------------------------------
+// host build
+// ---------------------------------------------------------------------------
+template <typename T>
+static emfa_status_t upload(Ctx* c, DevBuf& b, const std::vector<T>& v, cudaStream_t st)
+{
+    EMFA_TRY(b.alloc(c, sizeof(T) * std::max<size_t>(v.size(), 1)));
+    if (!v.empty()) EMFA_CUDA(c, cudaMemcpyAsync(b.ptr, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, st));
+    return EMFA_OK;
+}
+
+// Host plan: everything the reference computes before its operators, in its
+// float arithmetic (tree, box order, near/far lists, multipoles, samples).
+struct Plan {
+    int L = 0;
+    float k = 0;
+    std::vector<float> blen;
+    std::vector<std::vector<mh::Box>> lb;
+    std::vector<int> poles;
+    std::vector<std::vector<float>> gt, gp, gw, kd;
+    std::vector<int> perm, box_of, off, cnt;
+    std::vector<float> cen;
+};
+
+static bool build_plan(const std::vector<double>& verts, int nv, const std::vector<int>& rwg, int n,
+                       const emfa_mlfma_params_t& prm, Plan& P, std::string& err)
+{
+    const float freq = (float)prm.freq;
+    const float cc = 299792458.0f;
+    const float k = ((2.0f * mh::PI) * freq) / cc;  // PI2 * f / cc
+    P.k = k;
+    const float lambda = cc / freq;
+    // float vertices, as the reference holds them
+    std::vector<float> vf(verts.size());
+    for (size_t i = 0; i < vf.size(); ++i) vf[i] = (float)verts[i];
+    // MLFMA_Boundary::init
+    float mn[3] = {3.4e38f, 3.4e38f, 3.4e38f}, mx[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
+    for (int i = 0; i < nv; ++i)
+        for (int d = 0; d < 3; ++d) {
+            mn[d] = std::min(mn[d], vf[3 * i + d]);
+            mx[d] = std::max(mx[d], vf[3 * i + d]);
+        }
+    float cen[3], half;
+    for (int d = 0; d < 3; ++d) cen[d] = (mn[d] + mx[d]) * 0.5f;
+    float maxlen = std::max(std::max(mx[0] - mn[0], mx[1] - mn[1]), mx[2] - mn[2]) + 0.1f * lambda;
+    half = maxlen / 2;
+    float bmin[3], bmax[3];
+    for (int d = 0; d < 3; ++d) {
+        bmin[d] = cen[d] - half;
+        bmax[d] = cen[d] + half;
+    }
+    const float delta = (float)prm.box_threshold * lambda;
+    int L = 0;
+    for (float ml = maxlen; ml > delta; ++L) ml /= 2;
+    if (L < 2) {
+        err = "level number of MLFMA is too small (MLFMA box threshold is too large)";
+        return false;
+    }
+    P.L = L;
+    const float big = bmax[0] - bmin[0];
+    float root[3];
+    for (int d = 0; d < 3; ++d) root[d] = (bmin[d] + bmax[d]) * 0.5f;
+    // RWG centres: (v1 + v2) / 2
+    std::vector<float> cp(3 * (size_t)n);
+    for (int u = 0; u < n; ++u)
+        for (int d = 0; d < 3; ++d) cp[3 * u + d] = (vf[3 * rwg[6 * u] + d] + vf[3 * rwg[6 * u + 1] + d]) * 0.5f;
+    // octree (buildBox)
+    auto& lb = P.lb;
+    auto& blen = P.blen;
+    lb.assign(L + 1, {});
+    blen.assign(L + 1, 0.f);
+    mh::Box rb;
+    std::copy(root, root + 3, rb.c);
+    for (int u = 0; u < n; ++u) rb.unk.push_back(u);
+    lb[0].push_back(rb);
+    float cur = big / 2;
+    blen[1] = cur;
+    for (int l = 1; l <= L; ++l) {
+        if (l > 1) {
+            cur /= 2;
+            blen[l] = cur;
+        }
+        for (size_t pi = 0; pi < lb[l - 1].size(); ++pi) {
+            mh::Box& pb = lb[l - 1][pi];
+            mh::Box ch[8];
+            for (int x = 0; x < 2; ++x)
+                for (int y = 0; y < 2; ++y)
+                    for (int z = 0; z < 2; ++z) {
+                        int idx = (x * 2 + y) * 2 + z;
+                        ch[idx].c[0] = pb.c[0] + (x - 0.5f) * cur;
+                        ch[idx].c[1] = pb.c[1] + (y - 0.5f) * cur;
+                        ch[idx].c[2] = pb.c[2] + (z - 0.5f) * cur;
+                        ch[idx].parent = (int)pi;
+                        ch[idx].oct = idx;
+                    }
+            for (int u : pb.unk) {
+                int xf = cp[3 * u] < pb.c[0] ? 0 : 1, yf = cp[3 * u + 1] < pb.c[1] ? 0 : 1,
+                    zf = cp[3 * u + 2] < pb.c[2] ? 0 : 1;
+                ch[(xf * 2 + yf) * 2 + zf].unk.push_back(u);
+            }
+            int pos = pb.offset;
+            for (int ci = 0; ci < 8; ++ci) {
+                if (ch[ci].unk.empty()) continue;
+                ch[ci].offset = pos;
+                pos += (int)ch[ci].unk.size();
+                pb.child.push_back((int)lb[l].size());
+                lb[l].push_back(std::move(ch[ci]));
+            }
+        }
+    }
+    // setBoxParameter: level 1 all near; level >= 2 near if centre distance < 1.75 box
+    for (size_t f = 0; f < lb[1].size(); ++f)
+        for (size_t s2 = 0; s2 < lb[1].size(); ++s2) lb[1][f].near.push_back((int)s2);
+    float clen = big / 4;
+    for (int l = 2; l <= L; ++l, clen /= 2) {
+        float lim = 1.75f * clen;
+        for (auto& b : lb[l]) {
+            for (int pn : lb[l - 1][b.parent].near)
+                for (int cidx : lb[l - 1][pn].child) {
+                    float dist = mh::fnorm3(lb[l][cidx].c, b.c);
+                    (dist < lim ? b.near : b.far).push_back(cidx);
+                }
+        }
+    }
+    // box order of the unknowns
+    const auto& fin = lb[L];
+    P.perm.clear();
+    P.box_of.assign(n, 0);
+    for (size_t b = 0; b < fin.size(); ++b) {
+        P.off.push_back(fin[b].offset);
+        P.cnt.push_back((int)fin[b].unk.size());
+        for (int u : fin[b].unk) {
+            P.box_of[P.perm.size()] = (int)b;
+            P.perm.push_back(u);
+        }
+        P.cen.insert(P.cen.end(), fin[b].c, fin[b].c + 3);
+    }
+    // multipoles, samples, weights, directions
+    const int nl = L - 1;
+    P.poles.assign(nl, 0);
+    auto& gt = P.gt;
+    auto& gp = P.gp;
+    auto& gw = P.gw;
+    auto& kd = P.kd;
+    gt.assign(nl, {});
+    gp.assign(nl, {});
+    gw.assign(nl, {});
+    kd.assign(nl, {});
+    for (int l = 2; l <= L; ++l) {
+        int i = l - 2;
+        float kdl = 1.732051f * k * blen[l];
+        int Pm = (int)(kdl + 6 * cbrtf(kdl));
+        P.poles[i] = Pm;
+        std::vector<float> rt, wt, rp, wp;
+        mh::gauss_legendre(Pm, rt, wt);
+        mh::gauss_legendre(2 * Pm, rp, wp);
+        gt[i] = rt;
+        gp[i] = rp;
+        gw[i].resize(2 * (size_t)Pm * Pm);
+        kd[i].resize(3 * 2 * (size_t)Pm * Pm);
+        size_t q = 0;
+        for (int pp = 0; pp < 2 * Pm; ++pp)
+            for (int t = 0; t < Pm; ++t, ++q) gw[i][q] = wp[pp] * wt[t];
+        const float PIh = 0.5f * mh::PI;
+        for (int pp = 0; pp < 2 * Pm; ++pp) {
+            float phi = mh::PI * (rp[pp] + 1);
+            float ps = (float)std::sin((double)phi), pc = (float)std::cos((double)phi);
+            for (int t = 0; t < Pm; ++t) {
+                float th = PIh * (rt[t] + 1);
+                float ts = (float)std::sin((double)th), tc = (float)std::cos((double)th);
+                size_t kk = (size_t)pp * Pm + t;
+                kd[i][3 * kk] = ts * pc;
+                kd[i][3 * kk + 1] = ts * ps;
+                kd[i][3 * kk + 2] = tc;
+            }
+        }
+    }
+    return true;
+}
+
+static emfa_status_t mlfma_build(emfa_mlfma* M, cudaStream_t st)
+{
+    Ctx* c = M->ctx;
+    Geom* g = M->geom;
+    const int n = g->n;
+    M->n = n;
+    Plan P;
+    std::string err;
+    if (!build_plan(g->verts, g->nv, g->rwg, n, M->p, P, err)) {
+        set_error(c, err);
+        return EMFA_ERR_INVALID;
+    }
+    const int L = P.L;
+    const float k = P.k;
+    M->k = k;
+    M->levels = L;
+    auto& lb = P.lb;
+    auto& gt = P.gt;
+    auto& gp = P.gp;
+    auto& gw = P.gw;
+    auto& kd = P.kd;
+    const auto& fin = lb[L];
+    M->level_boxes.clear();
+    for (int l = 0; l <= L; ++l) M->level_boxes.push_back((int)lb[l].size());
+    M->perm = P.perm;
+    M->poles = P.poles;
+    std::vector<int>& box_of_h = P.box_of;
+    std::vector<int>& off_h = P.off;
+    std::vector<int>& cnt_h = P.cnt;
+    std::vector<float>& cen_h = P.cen;
+    const int nl = L - 1;
+    M->lv.clear();
+    M->lv.resize(nl);
+    for (int l = 2; l <= L; ++l) {
+        const int i = l - 2;
+        MLevel& ml = M->lv[i];
+        ml.nbox = (int)lb[l].size();
+        ml.L = P.poles[i];
+        ml.K = 2 * ml.L * ml.L;
+        ml.len = P.blen[l];
+        ml.w_host = gw[i];
+    }
+    // per-level device tables
+    for (int l = 2; l <= L; ++l) {
+        const int i = l - 2;
+        MLevel& ml = M->lv[i];
+        const int K = ml.K;
+        std::vector<int> par, oc, cptr{0}, cidx, fptr{0}, fbox, foff;
+        for (auto& b : lb[l]) {
+            par.push_back(b.parent);
+            oc.push_back(b.oct);
+            for (int f : b.far) {
+                const float* a = b.c;
+                const float* o = lb[l][f].c;
+                int dx = (int)std::lround((a[0] - o[0]) / ml.len), dy = (int)std::lround((a[1] - o[1]) / ml.len),
+                    dz = (int)std::lround((a[2] - o[2]) / ml.len);
+                fbox.push_back(f);
+                foff.push_back(((dx + 3) * 7 + (dy + 3)) * 7 + (dz + 3));
+            }
+            fptr.push_back((int)fbox.size());
+        }
+        if (l < L)
+            for (auto& b : lb[l]) {
+                for (int ch : b.child) cidx.push_back(ch);
+                cptr.push_back((int)cidx.size());
+            }
+        EMFA_TRY(upload(c, ml.parent, par, st));
+        EMFA_TRY(upload(c, ml.oct, oc, st));
+        EMFA_TRY(upload(c, ml.far_ptr, fptr, st));
+        EMFA_TRY(upload(c, ml.far_box, fbox, st));
+        EMFA_TRY(upload(c, ml.far_off, foff, st));
+        EMFA_TRY(upload(c, ml.child_ptr, cptr, st));
+        EMFA_TRY(upload(c, ml.child_idx, cidx, st));
+        // translation operators per offset: sum_l (2l+1)(-j)^l h_l^(2)(kD) P_l(k.D/|D|),
+        // l <= min(poles, floor(kD)) (MLFMA.cpp:1203-1219), evaluated in FP64
+        std::vector<float2> tr((size_t)343 * K, make_float2(0, 0));
+        for (int dx = -3; dx <= 3; ++dx)
+            for (int dy = -3; dy <= 3; ++dy)
+                for (int dz = -3; dz <= 3; ++dz) {
+                    if (std::abs(dx) <= 1 && std::abs(dy) <= 1 && std::abs(dz) <= 1) continue;
+                    const int off = ((dx + 3) * 7 + (dy + 3)) * 7 + (dz + 3);
+                    double D[3] = {dx * (double)ml.len, dy * (double)ml.len, dz * (double)ml.len};
+                    double Dn = std::sqrt(D[0] * D[0] + D[1] * D[1] + D[2] * D[2]);
+                    double x = (double)k * Dn;
+                    int minL = (int)std::min((float)ml.L, (float)(k * (float)Dn));
+                    std::vector<std::complex<double>> hl(minL + 1);
+                    hl[0] = std::complex<double>(std::sin(x), std::cos(x)) / x;
+                    if (minL >= 1) hl[1] = std::complex<double>(std::sin(x) / x - std::cos(x), std::cos(x) / x + std::sin(x)) / x;
+                    for (int q = 2; q <= minL; ++q) hl[q] = ((2.0 * q - 1) / x) * hl[q - 1] - hl[q - 2];
+                    for (int kk = 0; kk < K; ++kk) {
+                        double ct = (kd[i][3 * kk] * D[0] + kd[i][3 * kk + 1] * D[1] + kd[i][3 * kk + 2] * D[2]) / Dn;
+                        std::complex<double> val(0, 0);
+                        double p0 = 1, p1 = ct;
+                        const std::complex<double> jl[4] = {{1, 0}, {0, -1}, {-1, 0}, {0, 1}};
+                        for (int q = 0; q <= minL; ++q) {
+                            double Pq = q == 0 ? 1 : q == 1 ? ct : 0;
+                            if (q >= 2) {
+                                Pq = ((2 * q - 1) * ct * p1 - (q - 1) * p0) / q;
+                                p0 = p1;
+                                p1 = Pq;
+                            }
+                            val += (2.0 * q + 1) * jl[q % 4] * hl[q] * Pq;
+                        }
+                        tr[(size_t)off * K + kk] = make_float2((float)val.real(), (float)val.imag());
+                    }
+                }
+        EMFA_TRY(upload(c, ml.trans, tr, st));
+        EMFA_TRY(ml.up.alloc(c, sizeof(C3f) * (size_t)ml.nbox * K));
+        EMFA_TRY(ml.down.alloc(c, sizeof(C3f) * (size_t)ml.nbox * K));
+    }
+    // interpolation level i+1 (child, fewer samples) -> level i (parent), i = 0..nl-2
+    for (int i = 0; i + 1 < nl; ++i) {
+        MLevel& pm = M->lv[i];
+        MLevel& cm = M->lv[i + 1];
+        std::vector<int> tloc, ploc;
+        std::vector<float> tel, pel;
+        mh::lagrange(gt[i + 1], gt[i], tloc, tel);
+        mh::lagrange(gp[i + 1], gp[i], ploc, pel);
+        const int Kp = pm.K, Lc = cm.L;
+        std::vector<int> col((size_t)Kp * 9);
+        std::vector<float> w((size_t)Kp * 9);
+        size_t row = 0;
+        for (int pp = 0; pp < 2 * pm.L; ++pp)
+            for (int t = 0; t < pm.L; ++t, ++row) {
+                int q = 0;
+                for (int ip = 0; ip < 3; ++ip) {
+                    int base = ploc[3 * pp + ip] * Lc;
+                    for (int it = 0; it < 3; ++it, ++q) {
+                        col[row * 9 + q] = base + tloc[3 * t + it];
+                        w[row * 9 + q] = pel[3 * pp + ip] * tel[3 * t + it];
+                    }
+                }
+            }
+        EMFA_TRY(upload(c, pm.ip_col, col, st));
+        EMFA_TRY(upload(c, pm.ip_w, w, st));
+        // phases for the children of level i: exp(-j k kp . (parent - child)), per octant
+        std::vector<float2> ph((size_t)8 * Kp);
+        for (int o = 0; o < 8; ++o) {
+            int x = o >> 2, y = (o >> 1) & 1, z = o & 1;
+            float rv[3] = {-(x - 0.5f) * cm.len, -(y - 0.5f) * cm.len, -(z - 0.5f) * cm.len};
+            for (int kk = 0; kk < Kp; ++kk) {
+                double a = (double)k * ((double)kd[i][3 * kk] * rv[0] + (double)kd[i][3 * kk + 1] * rv[1] +
+                                         (double)kd[i][3 * kk + 2] * rv[2]);
+                ph[(size_t)o * Kp + kk] = make_float2((float)std::cos(a), (float)-std::sin(a));
+            }
+        }
+        EMFA_TRY(upload(c, pm.up_phase, ph, st));
+        // anterpolation into level i+1: transpose of the stencil, weight * w_parent / w_child
+        const int Kc = cm.K;
+        std::vector<std::vector<std::pair<int, float>>> tpos(Kc);
+        for (int kp = 0; kp < Kp; ++kp)
+            for (int q = 0; q < 9; ++q) {
+                int kc = col[(size_t)kp * 9 + q];
+                tpos[kc].push_back({kp, w[(size_t)kp * 9 + q] * gw[i][kp] / gw[i + 1][kc]});
+            }
+        std::vector<int> aptr{0}, akp;
+        std::vector<float> aw;
+        for (int kc = 0; kc < Kc; ++kc) {
+            for (auto& e : tpos[kc]) {
+                akp.push_back(e.first);
+                aw.push_back(e.second);
+            }
+            aptr.push_back((int)akp.size());
+        }
+        EMFA_TRY(upload(c, cm.an_ptr, aptr, st));
+        EMFA_TRY(upload(c, cm.an_kp, akp, st));
+        EMFA_TRY(upload(c, cm.an_w, aw, st));
+    }
+    // finest-level data
+    MLevel& fl = M->lv[nl - 1];
+    const int Kf = fl.K;
+    std::vector<float> coeff(Kf);
+    {
+        const float PIh = 0.5f * mh::PI;
+        size_t q = 0;
+        const int P = fl.L;
+        for (int pp = 0; pp < 2 * P; ++pp)
+            for (int t = 0; t < P; ++t, ++q) coeff[q] = (float)(gw[nl - 1][q] * std::sin((double)(PIh * (gt[nl - 1][t] + 1))));
+        const float z0 = 120.0f * mh::PI;
+        const float cn = k * k * z0 / 32;
+        for (auto& v : coeff) v = cn * v;
+    }
+    EMFA_TRY(upload(c, M->coeff, coeff, st));
+    EMFA_TRY(upload(c, M->perm_d, M->perm, st));
+    EMFA_TRY(upload(c, M->box_of, box_of_h, st));
+    EMFA_TRY(upload(c, M->box_off, off_h, st));
+    EMFA_TRY(upload(c, M->box_cnt, cnt_h, st));
+    DevBuf cen_d, kdir_d;
+    EMFA_TRY(upload(c, cen_d, cen_h, st));
+    EMFA_TRY(upload(c, kdir_d, kd[nl - 1], st));
+    EMFA_TRY(geom_prepare_f32(g, st));
+    EMFA_TRY(M->rad.alloc(c, sizeof(C3f) * (size_t)n * Kf));
+    EMFA_TRY(M->rec.alloc(c, sizeof(C3f) * (size_t)n * Kf));
+    {
+        size_t tot = (size_t)n * Kf;
+        k_radrec<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(dptr<RwgPack<float>>(g->g32.rwg), dptr<int>(M->perm_d),
+                                                               dptr<int>(M->box_of), dptr<float>(cen_d),
+                                                               dptr<float>(kdir_d), n, Kf, k, (float)M->p.alpha,
+                                                               dptr<C3f>(M->rad), dptr<C3f>(M->rec));
+        c->kernel_launches += 1;
+    }
+    // near field: CSR of near boxes, column bases, row bases
+    std::vector<int> nptr{0}, nbox, ncol, rcols;
+    std::vector<size_t> rbase;
+    size_t nnz = 0;
+    int max_near = 0;
+    for (size_t b = 0; b < fin.size(); ++b) {
+        int cols = 0;
+        for (int nb : fin[b].near) {
+            nbox.push_back(nb);
+            ncol.push_back(cols);
+            cols += (int)fin[nb].unk.size();
+        }
+        nptr.push_back((int)nbox.size());
+        max_near = std::max(max_near, (int)fin[b].near.size());
+        rcols.push_back(cols);
+        rbase.push_back(nnz);
+        nnz += (size_t)cols * fin[b].unk.size();
+    }
+    M->nnz = nnz;
+    EMFA_TRY(upload(c, M->near_ptr, nptr, st));
+    EMFA_TRY(upload(c, M->near_box, nbox, st));
+    EMFA_TRY(upload(c, M->near_col, ncol, st));
+    EMFA_TRY(upload(c, M->row_cols, rcols, st));
+    EMFA_TRY(upload(c, M->row_base, rbase, st));
+    EMFA_TRY(M->near_val.alloc(c, sizeof(float2) * std::max<size_t>(nnz, 1)));
+    {
+        emfa_fill_params_t fp{EMFA_CFIE, EMFA_F32, M->p.freq, M->p.alpha, 0, 0, 0};
+        DevBuf tab;
+        EMFA_TRY(tab.alloc(c, sizeof(double2) * (size_t)g->nt * 9));
+        EMFA_TRY(build_singular_table(c, g, &fp, dptr<double2>(tab), st));
+        FillConst<float> fc = make_fill_const<float>(&fp);
+        size_t tot = (size_t)n * max_near;
+        k_near_fill<<<(unsigned)((tot + 127) / 128), 128, 0, st>>>(
+            dptr<RwgPack<float>>(g->g32.rwg), dptr<int>(M->perm_d), dptr<int>(M->box_of), dptr<int>(M->box_off),
+            dptr<int>(M->box_cnt), dptr<int>(M->near_ptr), dptr<int>(M->near_box), dptr<int>(M->near_col),
+            dptr<int>(M->row_cols), dptr<size_t>(M->row_base), n, max_near, fc, dptr<double2>(tab),
+            dptr<float2>(M->near_val));
+        c->kernel_launches += 1;
+        EMFA_CUDA(c, cudaGetLastError());
+        EMFA_CUDA(c, cudaStreamSynchronize(st));
+    }
+    EMFA_CUDA(c, cudaGetLastError());
+    EMFA_CUDA(c, cudaStreamSynchronize(st));
+    return EMFA_OK;
+}
+
+// y = Z x for one vector (box order, complex64); parts: 0 near + far, 1 near, 2 far
+static emfa_status_t mlfma_apply1(emfa_mlfma* M, const float2* x, float2* y, cudaStream_t st, int parts = 0)
+{
+    Ctx* c = M->ctx;
+    const int nl = M->levels - 1;
+    MLevel& fl = M->lv[nl - 1];
+    const int Kf = fl.K;
+    k_agg_finest<<<fl.nbox, 128, 0, st>>>(x, dptr<C3f>(M->rad), dptr<int>(M->box_off), dptr<int>(M->box_cnt), Kf,
+                                          dptr<C3f>(fl.up));
+    for (int i = nl - 2; i >= 0; --i) {
+        MLevel& pm = M->lv[i];
+        MLevel& cm = M->lv[i + 1];
+        size_t tot = (size_t)pm.nbox * pm.K;
+        k_upward<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(dptr<C3f>(cm.up), cm.K, dptr<int>(pm.child_ptr),
+                                                               dptr<int>(pm.child_idx), dptr<int>(cm.oct),
+                                                               dptr<int>(pm.ip_col), dptr<float>(pm.ip_w),
+                                                               dptr<float2>(pm.up_phase), pm.nbox, pm.K,
+                                                               dptr<C3f>(pm.up));
+    }
+    for (int i = 0; i < nl; ++i) {
+        MLevel& ml = M->lv[i];
+        size_t tot = (size_t)ml.nbox * ml.K;
+        const bool top = i == 0;
+        MLevel& pm = M->lv[top ? 0 : i - 1];
+        k_downward<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(
+            dptr<C3f>(ml.up), dptr<int>(ml.far_ptr), dptr<int>(ml.far_box), dptr<int>(ml.far_off),
+            dptr<float2>(ml.trans), ml.nbox, ml.K, top ? nullptr : dptr<C3f>(pm.down), pm.K, dptr<int>(ml.parent),
+            dptr<int>(ml.oct), dptr<int>(ml.an_ptr), dptr<int>(ml.an_kp), dptr<float>(ml.an_w),
+            dptr<float2>(pm.up_phase), dptr<C3f>(ml.down));
+    }
+    const int n = M->n;
+    k_disagg_near<<<(unsigned)(((size_t)n * 32 + 255) / 256), 256, 0, st>>>(
+        x, dptr<C3f>(M->rec), dptr<C3f>(fl.down), dptr<float>(M->coeff), parts == 1 ? 0 : Kf, dptr<int>(M->box_of),
+        dptr<int>(M->box_off), dptr<int>(M->box_cnt), dptr<int>(M->near_ptr), dptr<int>(M->near_box),
+        dptr<int>(M->near_col), dptr<int>(M->row_cols), dptr<size_t>(M->row_base), dptr<float2>(M->near_val), n,
+        parts == 2 ? 1 : 0, y);
+    c->kernel_launches += 2 * nl + 1;
+    EMFA_CUDA(c, cudaGetLastError());
+    return EMFA_OK;
+}
+
+// MLFMA as a Krylov operator (iteration vectors complex64, box order)
+struct MlfmaOp : LinOp {
+    emfa_mlfma* M = nullptr;
+    emfa_status_t apply(Ctx*, const void* X, void* Y, int nrhs, cudaStream_t st) override
+    {
+        for (int r = 0; r < nrhs; ++r)
+            EMFA_TRY(mlfma_apply1(M, (const float2*)X + (size_t)r * n, (float2*)Y + (size_t)r * n, st));
+        return EMFA_OK;
+    }
+    emfa_status_t residual(Ctx* c, const double2* X, const void* B, double2* R, int nrhs, float2* xt,
+                           cudaStream_t st) override
+    {
+        const size_t tot = (size_t)n * nrhs;
+        EMFA_TRY(M->tmp_out.bytes >= sizeof(float2) * tot ? EMFA_OK : M->tmp_out.alloc(c, sizeof(float2) * tot));
+        k_f64_to_f32<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(X, xt, tot);
+        EMFA_TRY(apply(c, xt, M->tmp_out.ptr, nrhs, st));
+        k_resid_c64<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>((const float2*)B, dptr<float2>(M->tmp_out), R, tot);
+        c->kernel_launches += 2;
+        return EMFA_OK;
+    }
+};
+
+}  // namespace emfa
+
+using namespace emfa;
+
+extern "C" {
+
+emfa_status_t emfa_mlfma_create(emfa_ctx_t* ctx, emfa_geom_t* geom, const emfa_mlfma_params_t* p, emfa_mlfma_t** out)
+{
+    if (!ctx || !geom || !p || !out || !(p->freq > 0) || !(p->box_threshold > 0)) {
+        set_error(ctx, "emfa_mlfma_create: bad arguments");
+        return EMFA_ERR_INVALID;
+    }
+    EMFA_CUDA(ctx, cudaSetDevice(ctx->device));
+    emfa_mlfma_t* M = new emfa_mlfma_t();
+    M->ctx = ctx;
+    M->geom = geom;
+    M->p = *p;
+    emfa_status_t s = mlfma_build(M, ctx->stream);
+    if (s != EMFA_OK) {
+        delete M;
+        return s;
+    }
+    *out = M;
+    return EMFA_OK;
+}
+
+emfa_status_t emfa_mlfma_plan(const double* verts_host, int n_vert, const int* rwg_host, int n_rwg,
+                              const emfa_mlfma_params_t* p, int* levels, int* level_boxes, int level_cap, int* poles,
+                              int* perm)
+{
+    if (!verts_host || !rwg_host || !p || n_vert <= 0 || n_rwg <= 0 || !levels) return EMFA_ERR_INVALID;
+    std::vector<double> v(verts_host, verts_host + 3 * (size_t)n_vert);
+    std::vector<int> r(rwg_host, rwg_host + 6 * (size_t)n_rwg);
+    Plan P;
+    std::string err;
+    if (!build_plan(v, n_vert, r, n_rwg, *p, P, err)) {
+        set_global_error("emfa_mlfma_plan: " + err);
+        return EMFA_ERR_INVALID;
+    }
+    *levels = P.L;
+    if (level_boxes) {
+        if (level_cap < P.L + 1) return EMFA_ERR_INVALID;
+        for (int l = 0; l <= P.L; ++l) level_boxes[l] = (int)P.lb[l].size();
+    }
+    if (poles)
+        for (size_t i = 0; i < P.poles.size(); ++i) poles[i] = P.poles[i];
+    if (perm) std::copy(P.perm.begin(), P.perm.end(), perm);
+    return EMFA_OK;
+}
+
+emfa_status_t emfa_mlfma_destroy(emfa_mlfma_t* M)
+{
+    if (!M) return EMFA_ERR_INVALID;
+    cudaSetDevice(M->ctx->device);
+    cudaStreamSynchronize(M->ctx->stream);
+    delete M;
+    return EMFA_OK;
+}
+
+emfa_status_t emfa_mlfma_info(const emfa_mlfma_t* M, int* levels, int* level_boxes, int* poles, size_t* near_nnz,
+                              int* perm)
+{
+    if (!M) return EMFA_ERR_INVALID;
+    if (levels) *levels = M->levels;
+    if (level_boxes) std::copy(M->level_boxes.begin(), M->level_boxes.end(), level_boxes);
+    if (poles) std::copy(M->poles.begin(), M->poles.end(), poles);
+    if (near_nnz) *near_nnz = M->nnz;
+    if (perm) std::copy(M->perm.begin(), M->perm.end(), perm);
+    return EMFA_OK;
+}
+
+emfa_status_t emfa_mlfma_apply_part(emfa_mlfma_t* M, const void* x_dev, void* y_dev, int part, void* stream)
+{
+    if (!M || !x_dev || !y_dev || part < 0 || part > 2) return EMFA_ERR_INVALID;
+    Ctx* c = M->ctx;
+    EMFA_CUDA(c, cudaSetDevice(c->device));
+    cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+    return mlfma_apply1(M, (const float2*)x_dev, (float2*)y_dev, st, part);
+}
+
+emfa_status_t emfa_mlfma_apply(emfa_mlfma_t* M, const void* x_dev, void* y_dev, int n_rhs, void* stream)
+{
+    if (!M || !x_dev || !y_dev || n_rhs <= 0) return EMFA_ERR_INVALID;
+    Ctx* c = M->ctx;
+    EMFA_CUDA(c, cudaSetDevice(c->device));
+    cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+    MlfmaOp A;
+    A.M = M;
+    A.n = M->n;
+    A.prec = EMFA_F32;
+    return A.apply(c, x_dev, y_dev, n_rhs, st);
+}
+
+emfa_status_t emfa_mlfma_fill_v(emfa_mlfma_t* M, const double* angles_host, int n_inc, void* V_dev, void* stream)
+{
+    if (!M || !angles_host || n_inc <= 0 || !V_dev) return EMFA_ERR_INVALID;
+    Ctx* c = M->ctx;
+    EMFA_CUDA(c, cudaSetDevice(c->device));
+    cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+    emfa_fill_params_t fp{EMFA_CFIE, EMFA_F32, M->p.freq, M->p.alpha, 0, 0, 0};
+    DevBuf tmp;
+    EMFA_TRY(tmp.alloc(c, sizeof(float2) * (size_t)M->n * n_inc));
+    EMFA_TRY(launch_fill_v(c, M->geom, &fp, angles_host, n_inc, tmp.ptr, st));
+    size_t tot = (size_t)M->n * n_inc;
+    k_gather_c64<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(dptr<float2>(tmp), dptr<int>(M->perm_d), M->n, n_inc,
+                                                                (float2*)V_dev);
+    c->kernel_launches += 1;
+    EMFA_CUDA(c, cudaGetLastError());
+    EMFA_CUDA(c, cudaStreamSynchronize(st));
+    return EMFA_OK;
+}
+
+emfa_status_t emfa_mlfma_solve(emfa_mlfma_t* M, const void* B_dev, int n_rhs, void* X_dev,
+                               const emfa_solver_params_t* sp, emfa_solve_info_t* info, void* stream)
+{
+    if (!M || !B_dev || !X_dev || !sp || n_rhs <= 0 || !(sp->tol > 0)) return EMFA_ERR_INVALID;
+    Ctx* c = M->ctx;
+    EMFA_CUDA(c, cudaSetDevice(c->device));
+    cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+    MlfmaOp A;
+    A.M = M;
+    A.n = M->n;
+    A.prec = EMFA_F32;
+    return solve_op(c, A, B_dev, n_rhs, X_dev, sp, info, st);
+}
+
+emfa_status_t emfa_mlfma_unpermute(emfa_mlfma_t* M, const void* X_box_dev, int n_rhs, void* X_rwg_dev, void* stream)
+{
+    if (!M || !X_box_dev || !X_rwg_dev || n_rhs <= 0) return EMFA_ERR_INVALID;
+    Ctx* c = M->ctx;
+    EMFA_CUDA(c, cudaSetDevice(c->device));
+    cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+    size_t tot = (size_t)M->n * n_rhs;
+    k_scatter_c128<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>((const double2*)X_box_dev, dptr<int>(M->perm_d),
+                                                                  M->n, n_rhs, (double2*)X_rwg_dev);
+    c->kernel_launches += 1;
+    EMFA_CUDA(c, cudaGetLastError());
+    EMFA_CUDA(c, cudaStreamSynchronize(st));
+    return EMFA_OK;
+}
+
+}  // extern "C"

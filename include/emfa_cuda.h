@@ -174,6 +174,51 @@ emfa_status_t emfa_rcs(emfa_ctx_t* ctx, emfa_geom_t* geom, const emfa_fill_param
                        int n_rhs, const double* dirs_host, int n_dir, int per_rhs_dirs, double* out_host,
                        void* stream);
 
+/* ---- MLFMA ------------------------------------------------------------------- */
+/* Multilevel fast multipole CFIE operator.  Replaces MLFMA::init / solve
+ * (EMSolver/MLFMA.cpp:23-106): octree and box order (MLFMA.cpp:688-875,
+ * MLFMA_Boundary.cpp:15-35), multipoles and interpolation (MLFMA.cpp:877-1002),
+ * translation / radiation / receive operators (MLFMA.cpp:1133-1292), near
+ * field (MLFMA.cpp:1004-1131) and the mat-vec (MLFMA.cpp:454-686).  Vectors
+ * of emfa_mlfma_apply / _fill_v / _solve are in box order (the reference's
+ * own unknown order); emfa_mlfma_unpermute maps currents back to RWG order. */
+typedef struct {
+    double freq;           /* Hz                                                     */
+    double alpha;          /* CFIE combination (alpha:)                              */
+    double box_threshold;  /* finest box side in wavelengths (mlfma_box_threshold:)  */
+} emfa_mlfma_params_t;
+
+/* Host only (no GPU): the octree plan the operator is built on -- finest
+ * level number, boxes per level (level_cap >= levels + 1), multipoles per
+ * level 2..L and the box-order permutation (N ints).  MLFMA::init and
+ * levelRootsAndWeights (EMSolver/MLFMA.cpp:23-65,688-915). */
+emfa_status_t emfa_mlfma_plan(const double* verts_host, int n_vert, const int* rwg_host, int n_rwg,
+                              const emfa_mlfma_params_t* p, int* levels, int* level_boxes, int level_cap, int* poles,
+                              int* perm);
+emfa_status_t emfa_mlfma_create(emfa_ctx_t* ctx, emfa_geom_t* geom, const emfa_mlfma_params_t* p,
+                                emfa_mlfma_t** out);
+emfa_status_t emfa_mlfma_destroy(emfa_mlfma_t* mlfma);
+/* levels = finest level number L (levels 0..L); level_boxes (L+1 ints), poles
+ * (L-1 ints, levels 2..L) and perm (N ints: box position -> RWG index) are
+ * optional outputs. */
+emfa_status_t emfa_mlfma_info(const emfa_mlfma_t* mlfma, int* levels, int* level_boxes, int* poles,
+                              size_t* near_nnz, int* perm);
+/* y = Z x, complex64, n_rhs vectors of N in box order (MLFMA::matrixVectorMultiply). */
+emfa_status_t emfa_mlfma_apply(emfa_mlfma_t* mlfma, const void* x_dev, void* y_dev, int n_rhs, void* stream);
+/* One vector, one part of the operator: part 1 = near field only (nearZ_ * x),
+ * 2 = far field only (the multipole stages), 0 = both.  For diagnostics. */
+emfa_status_t emfa_mlfma_apply_part(emfa_mlfma_t* mlfma, const void* x_dev, void* y_dev, int part, void* stream);
+/* CFIE excitation in box order, complex64 (MLFMA::fillVbyBox, MLFMA.cpp:1536-1571). */
+emfa_status_t emfa_mlfma_fill_v(emfa_mlfma_t* mlfma, const double* angles_host, int n_inc, void* V_dev,
+                                void* stream);
+/* GMRES or BiCGStab on the MLFMA operator (MLFMA::iterativeSolve, MLFMA.cpp:402-452);
+ * B complex64, X complex128, box order. */
+emfa_status_t emfa_mlfma_solve(emfa_mlfma_t* mlfma, const void* B_dev, int n_rhs, void* X_dev,
+                               const emfa_solver_params_t* sp, emfa_solve_info_t* info, void* stream);
+/* X_rwg[r][perm[u]] = X_box[r][u], complex128. */
+emfa_status_t emfa_mlfma_unpermute(emfa_mlfma_t* mlfma, const void* X_box_dev, int n_rhs, void* X_rwg_dev,
+                                   void* stream);
+
 /* ---- end to end ------------------------------------------------------------- */
 /* One dense RCS job from host buffers: RWG table, upload, fill, excitation for
  * n_inc incidences, multi-RHS solve, RCS.  rcs_dirs_host/per_rhs_dirs as in

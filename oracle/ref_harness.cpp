@@ -261,6 +261,7 @@ static int run_mlfma(ConfigLoader& loader, unsigned seed)
     dump("iters.bin", it, 1);
     dump("I.bin", s.I_.memptr(), n);
     dump_rcs(s);
+    s.clear();  // joins the ThreadPool, as solver::invoke_solver does
     return 0;
 }
 

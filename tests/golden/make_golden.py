@@ -38,6 +38,37 @@ CASES = {
 }
 
 
+def run_mlfma_case(name, factory, over, seed=7):
+    """The reference's MLFMA: octree plan, V, one mat-vec of a seeded vector
+    (near part and total), BiCGStab current and RCS (box order)."""
+    mesh = factory()
+    tmp = tempfile.mkdtemp(prefix="golden_")
+    nas = os.path.join(tmp, name + ".nas")
+    M.write_nas(mesh, nas)
+    cfg = os.path.join(tmp, "CONFIG.yml")
+    M.write_config(cfg, **{"EMSolver": "MLFMA", "mesh_path": nas, **over})
+    out = os.path.join(tmp, "out")
+    O.run_reference("mlfma", cfg, out, seed, prec=32)
+    d = O.load_dump(out, 32)
+    rec = {"verts": mesh.verts, "tris": mesh.tris, "rwg": d["rwg"], "perm": d["perm"],
+           "level_boxes": d["level_boxes"], "poles": d["poles"], "V": d["V"], "mv_x": d["mv_x"],
+           "mv_y": d["mv_y"], "mv_near": d["mv_near"], "I": d["I"], "iters": d["iters"], "rcs": d["rcs"],
+           "rcs_dirs": d["rcs_dirs"], "near_nnz": np.array(len(d["near_val"]))}
+    rec["meta"] = np.array(repr(dict(solver="mlfma", **{k: str(v) for k, v in over.items()})))
+    np.savez_compressed(os.path.join(OUT, name + ".npz"), **rec)
+    print(name, mesh.n_tri, "tri", d["rwg"].shape[0], "rwg", "levels", d["level_boxes"])
+
+
+MLFMA_CASES = {
+    "sphere3_mlfma": (lambda: M.icosphere(3, 1.0), {"frequency": "3e8", "alpha": "0.5", "mlfma_box_threshold": "0.25",
+                                                    "iteration_threshold": "1e-3", "max_iteration_number": "200"}),
+    "ellipsoid8_mlfma": (lambda: M.ellipsoid(8, (1.2, 0.8, 0.6)),
+                         {"frequency": "4e8", "alpha": "0.3", "mlfma_box_threshold": "0.3", "theta": "40",
+                          "phi": "20", "pole": "45", "phi_from": "20", "phi_to": "20",
+                          "iteration_threshold": "1e-3", "max_iteration_number": "200"}),
+}
+
+
 def run_case(name, factory, solver, over, tol, full_z, rows):
     mesh = factory()
     tmp = tempfile.mkdtemp(prefix="golden_")
@@ -82,3 +113,7 @@ if __name__ == "__main__":
         if only and name not in only:
             continue
         run_case(name, *args)
+    for name, (factory, over) in MLFMA_CASES.items():
+        if only and name not in only:
+            continue
+        run_mlfma_case(name, factory, over)

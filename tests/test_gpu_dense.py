@@ -200,7 +200,8 @@ def test_dense_rcs_end_to_end_vs_reference(ctx):
     mesh = M.TriMesh(g["verts"], g["tris"])
     dirs = api.bistatic_dirs()
     for prec in ("f32", "f64"):
-        out, info, I = api.dense_rcs(ctx, mesh, params(g, prec), angles(g), api.solver_params("gmres", tol=1e-7),
+        tol = 1e-6 if prec == "f32" else 1e-9
+        out, info, I = api.dense_rcs(ctx, mesh, params(g, prec), angles(g), api.solver_params("gmres", tol=tol),
                                      dirs, want_current=True)
         assert info.converged == 1
         assert np.abs(out[0] - g["rcs_" + prec]).max() < 0.1
