@@ -222,6 +222,46 @@ def run_gemm_only(args):
     print(json.dumps({"mode": "gemm", "n": n, "r": r, "ms": dt * 1e3, "tflops": flops / dt / 1e12}))
 
 
+def run_mlfma(args):
+    """MLFMA CFIE on the 5-lambda sphere (81920 triangles, 122880 RWG), finest
+    box 0.25 lambda, one plane wave: operator set-up, GMRES(30) to 1e-3 and the
+    mat-vec alone (time and HBM bytes)."""
+    import torch
+    from emfa_gb300 import api, build, mesh
+    build.build()
+    lam = 299792458.0 / 3e8
+    m = mesh.icosphere(args.mlfma_subdiv, 5.0 * lam)
+    ctx = api.Context(0)
+    t0 = time.perf_counter()
+    geo = api.Geometry(ctx, m)
+    ml = api.Mlfma(geo, api.mlfma_params(3e8, 0.5, 0.25))
+    torch.cuda.synchronize()
+    t_setup = time.perf_counter() - t0
+    V = ml.fill_v(np.array([[0.0, 0.0, 0.0]]))
+    x = V.clone()
+    for _ in range(args.warmup):
+        ml.apply(x)
+    torch.cuda.synchronize()
+    stream = torch.cuda.ExternalStream(ctx.stream_ptr())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = max(1, args.steps)
+    e0.record(stream)
+    for _ in range(reps):
+        ml.apply(x)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    mv_ms = e0.elapsed_time(e1) / reps
+    sp = api.solver_params("gmres", restart=30, max_iter=300, tol=1e-3)
+    t0 = time.perf_counter()
+    X, info = ml.solve(V, sp)
+    torch.cuda.synchronize()
+    t_solve = time.perf_counter() - t0
+    print(json.dumps({"mode": "mlfma", "n_rwg": geo.n, "levels": ml.levels, "level_boxes": ml.level_boxes.tolist(),
+                      "poles": ml.poles.tolist(), "near_nnz": ml.nnz, "setup_s": round(t_setup, 3),
+                      "matvec_ms": round(mv_ms, 4), "solve_s": round(t_solve, 4), "iterations": info.iterations,
+                      "converged": info.converged, "rel_residual": info.max_rel_residual}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -231,12 +271,16 @@ def main():
     ap.add_argument("--workload", default="c2_cfie_sphere_7680x360", choices=list(WORKLOADS))
     ap.add_argument("--matvec", default="auto", choices=["auto", "f32", "tf32"])
     ap.add_argument("--check", type=int, default=1)
-    ap.add_argument("--mode", default="job", choices=["job", "gemm"])
+    ap.add_argument("--mode", default="job", choices=["job", "gemm", "mlfma"])
+    ap.add_argument("--mlfma-subdiv", type=int, default=6)
     ap.add_argument("--gemm-n", type=int, default=7680)
     ap.add_argument("--gemm-r", type=int, default=360)
     args = ap.parse_args()
     if args.mode == "gemm":
         run_gemm_only(args)
+        return
+    if args.mode == "mlfma":
+        run_mlfma(args)
         return
     rank, local, world = rank_env()
     if world > 1:

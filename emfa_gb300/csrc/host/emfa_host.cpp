@@ -509,6 +509,75 @@ void CFIE::clear()
     EM::clear();
 }
 
+void MLFMA::init(ConfigLoader* ploader)
+{
+    EM::init(ploader);
+    alpha_ = ploader->getAlpha();
+    dir_ = make_folder(dir_, folder_name_ + "_MLFMA_CFIE_" + std::to_string(alpha_).substr(0, 3));
+    logger_.open(dir_ + "/sca_parallel_runtime.log");
+    tol_ = ploader->getIterationThreshold();
+    max_iter_ = ploader->getMaxIterationNum();
+    precond_ = ploader->getPreconditioningSwitch();
+    ploader->getRowThreshold();
+    ploader->getColThreshold();
+    threshold_ = ploader->getMLFMABoxThreshold();
+    ploader->getThreadNumber();
+    ploader->getTaskFactor();
+    if (precond_)
+        logger_ << "    WARNING: preconditioning (SAI) is not available in this build; solving unpreconditioned\n";
+    emfa_mlfma_params_t mp{(double)incidence_.freq, (double)alpha_, (double)threshold_};
+    check(emfa_mlfma_create(ctx_, geom_, &mp, &ml_), ctx_, "MLFMA init");
+    check(emfa_mlfma_info(ml_, &levels_, nullptr, nullptr, nullptr, nullptr), ctx_, "MLFMA info");
+    logger_ << ploader->getReport();
+    reportInfo(logger_);
+    timeLog("init");
+}
+
+void MLFMA::reportInfo(std::ostream& strm) const
+{
+    EM::reportInfo(strm);
+    strm << "MLFMA Level Information\n    Number of level: " << levels_ + 1 << '\n';
+}
+
+void MLFMA::solve()
+{
+    const size_t n = unknowns_;
+    check(emfa_device_alloc(ctx_, 8 * n, &V_), ctx_, "alloc V");
+    check(emfa_device_alloc(ctx_, 16 * n, &Ibox_), ctx_, "alloc I");
+    check(emfa_device_alloc(ctx_, 16 * n, &I_), ctx_, "alloc I");
+    double ang[3] = {incidence_.theta, incidence_.phi, incidence_.pole};
+    check(emfa_mlfma_fill_v(ml_, ang, 1, V_, nullptr), ctx_, "fillVbyBox");
+    timeLog("fillVbyBox");
+    emfa_solver_params_t sp{EMFA_BICGSTAB, 30, max_iter_, tol_, 0, EMFA_MV_AUTO, 0};
+    emfa_solve_info_t info{};
+    emfa_status_t s = emfa_mlfma_solve(ml_, V_, 1, Ibox_, &sp, &info, nullptr);
+    if (s == EMFA_ERR_NOT_CONVERGED)
+        logger_ << "    WARNING: Iteration cannot converge\n";
+    else
+        check(s, ctx_, "iterativeSolve");
+    logger_ << "    Iterative number: " << info.iterations << '\n';
+    std::cout << "    Iterative number: " << info.iterations << std::endl;
+    check(emfa_mlfma_unpermute(ml_, Ibox_, 1, I_, nullptr), ctx_, "unpermute");
+    timeLog("iterativeSolve");
+}
+
+void MLFMA::output()
+{
+    emfa_fill_params_t fp{EMFA_CFIE, EMFA_F32, (double)incidence_.freq, (double)alpha_, 0, 0, 0};
+    writeBistatic(fp, I_);
+    timeLog("getBistaticRCS");
+}
+
+void MLFMA::clear()
+{
+    for (void* p : {V_, Ibox_, I_})
+        if (p) emfa_device_free(ctx_, p);
+    V_ = Ibox_ = I_ = nullptr;
+    if (ml_) emfa_mlfma_destroy(ml_);
+    ml_ = nullptr;
+    EM::clear();
+}
+
 }  // namespace mom
 
 namespace solver {
@@ -533,6 +602,8 @@ void loadSolver(const std::string& conf_file)
         invoke_solver<mom::EFIE>(&loader);
     else if (type == "CFIE")
         invoke_solver<mom::CFIE>(&loader);
+    else if (type == "MLFMA")
+        invoke_solver<mom::MLFMA>(&loader);
     else
         throw component::ConfigInvalid("undefined EM solver type (" + type + ')');
 }

@@ -154,6 +154,31 @@ private:
     int iterations_ = 0;
 };
 
+// MLFMA (EMSolver/MLFMA.cpp:23-131): CFIE operator with the multilevel fast
+// multipole far field, BiCGStab to iteration_threshold (box order).
+class MLFMA : public EM {
+public:
+    ~MLFMA() override
+    {
+        if (ml_) emfa_mlfma_destroy(ml_);
+    }
+    void init(component::ConfigLoader* ploader) override;
+    void solve() override;
+    void output() override;
+    void clear() override;
+    void reportInfo(std::ostream& strm) const override;
+
+private:
+    float alpha_ = 1.0f, threshold_ = 0.25f, tol_ = 1e-3f;
+    int max_iter_ = 500;
+    bool precond_ = false;
+    emfa_mlfma_t* ml_ = nullptr;
+    void* V_ = nullptr;
+    void* Ibox_ = nullptr;
+    void* I_ = nullptr;
+    int levels_ = 0;
+};
+
 }  // namespace mom
 
 namespace solver {

@@ -73,3 +73,22 @@ def test_launcher_end_to_end_vs_reference(emfa_lib, solver):
         ref = g["rcs_f32"][sl]
         assert len(vals) == len(ref)
         assert np.abs(vals - ref).max() < 0.1, np.abs(vals - ref).max()
+
+
+@pytest.mark.gpu
+def test_launcher_mlfma_vs_reference(emfa_lib):
+    """MLFMA through CONFIG.yml: bistatic RCS within 0.1 dB of the reference's
+    own MLFMA run on the same mesh."""
+    g = load_golden("sphere3_mlfma")
+    d = tempfile.mkdtemp()
+    nas = os.path.join(d, "sph.nas")
+    M.write_nas(M.TriMesh(g["verts"], g["tris"]), nas)
+    cfg = os.path.join(d, "CONFIG.yml")
+    M.write_config(cfg, EMSolver="MLFMA", mesh_path=nas, frequency="3e8", alpha="0.5", mlfma_box_threshold="0.25",
+                   iteration_threshold="1e-3", max_iteration_number="200")
+    r = run([cfg], cwd=d)
+    assert "Exit State: OK" in r.stdout, r.stdout[-2000:] + r.stderr[-2000:]
+    out = os.path.join(d, "sph_MLFMA_CFIE_0.5")
+    lines = open(os.path.join(out, "bistatic_rcs_phi_0.dat")).read().splitlines()
+    vals = np.array([float(l.split()[1]) for l in lines[1:]])
+    assert np.abs(vals - g["rcs"][:181]).max() < 0.1
