@@ -271,6 +271,7 @@ def main():
     ap.add_argument("--workload", default="c2_cfie_sphere_7680x360", choices=list(WORKLOADS))
     ap.add_argument("--matvec", default="auto", choices=["auto", "f32", "tf32"])
     ap.add_argument("--check", type=int, default=1)
+    ap.add_argument("--cpu-baseline", type=int, default=1)
     ap.add_argument("--mode", default="job", choices=["job", "gemm", "mlfma"])
     ap.add_argument("--mlfma-subdiv", type=int, default=6)
     ap.add_argument("--gemm-n", type=int, default=7680)
@@ -311,6 +312,12 @@ def main():
         "clocks": res["clocks"],
         "accuracy": res["acc"],
     }
+    if world == 1 and args.cpu_baseline:
+        # the reference's own CPU path on this host's cores, bounded sample (oracle/cpu_baseline.py)
+        from oracle import cpu_baseline
+        vals, det = cpu_baseline.measure(WORKLOADS[args.workload], args.workload, rows=1024, steps=1)
+        line["cpu_baseline"] = {"value": round(vals[0], 6), "unit": "solves/s", "cores": det["cores"],
+                                "kind": det["kind"], "sample": det["sample"]}
     print(json.dumps(line))
 
 

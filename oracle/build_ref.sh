@@ -14,16 +14,35 @@
 # The f64 variant additionally sets value_t = double and strips the 'f'
 # suffix of float literals, giving the FP64-promoted reference.
 #
+# The patched sources and the header libraries they include (Armadillo, Eigen,
+# vendored by the reference) are staged under oracle/_ref/ (git-ignored), so
+# `oracle/build_ref.sh --staged` rebuilds the binaries on a machine without the
+# reference tree (the GPU host is another architecture).
+#
 # Usage: oracle/build_ref.sh [reference_root]   (default /root/reference)
+#        oracle/build_ref.sh --staged
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
-REF="${1:-${EMFA_REFERENCE:-/root/reference}}"
 OUT="$HERE/_ref"
-if [ ! -d "$REF/EMSolver" ]; then
-  echo "build_ref: reference sources not found at $REF; skipping" >&2
-  exit 0
+STAGED=0
+if [ "${1:-}" = "--staged" ]; then
+  STAGED=1
+  if [ ! -d "$OUT/src_f32" ] || [ ! -d "$OUT/include" ]; then
+    echo "build_ref: no staged reference under $OUT; skipping" >&2
+    exit 0
+  fi
+  INC="$OUT/include"
+else
+  REF="${1:-${EMFA_REFERENCE:-/root/reference}}"
+  if [ ! -d "$REF/EMSolver" ]; then
+    echo "build_ref: reference sources not found at $REF; skipping" >&2
+    exit 0
+  fi
+  mkdir -p "$OUT/include/Eigen"
+  cp -r "$REF/include/armadillo" "$REF/include/armadillo_bits" "$OUT/include/"
+  cp -r "$REF/include/Eigen/Eigen" "$REF/include/Eigen/unsupported" "$OUT/include/Eigen/"
+  INC="$OUT/include"
 fi
-mkdir -p "$OUT"
 
 COMP_SRC="Mesh Triangle Tetrahedron CommonEdge ConfigLoader Quadrature Result ThreadPool tools MLFMA_Boundary"
 SOLV_SRC="EM EFIE CFIE MLFMA Miscellaneous"
@@ -31,6 +50,7 @@ SOLV_SRC="EM EFIE CFIE MLFMA Miscellaneous"
 build_variant() {
   local v="$1"
   local S="$OUT/src_$v"
+  if [ "$STAGED" = "0" ]; then
   rm -rf "$S"
   mkdir -p "$S"
   cp "$REF"/EMComponent/*.h "$S/"
@@ -53,17 +73,20 @@ build_variant() {
     sed -i -E 's/([0-9]\.[0-9]*([eE][-+]?[0-9]+)?|\.[0-9]+([eE][-+]?[0-9]+)?|[0-9][eE][-+]?[0-9]+)[fF]\b/\1/g' \
         "$S"/*.cpp "$S"/*.h
   fi
+  fi
   grep -q "typedef arma::umat Qumat" "$S/Custom.h" || { echo "P3 failed" >&2; exit 1; }
   local objs=()
   for f in "$S"/*.cpp "$HERE/ref_harness.cpp"; do
     local o="$S/$(basename "${f%.cpp}").o"
     objs+=("$o")
     g++ -std=c++14 -O2 -w -fpermissive -DARMA_DONT_USE_LAPACK -DARMA_DONT_USE_BLAS \
-        -DARMA_DONT_USE_WRAPPER -I"$S" -I"$REF/include" -I"$REF/include/Eigen" \
+        -DARMA_DONT_USE_WRAPPER -I"$S" -I"$INC" -I"$INC/Eigen" \
         -c "$f" -o "$o" &
   done
   wait
-  g++ -o "$OUT/emfa_ref_$v" "${objs[@]}" -lstdc++fs -lpthread
+  g++ -o "$OUT/emfa_ref_$v.tmp" "${objs[@]}" -lstdc++fs -lpthread
+  mv -f "$OUT/emfa_ref_$v.tmp" "$OUT/emfa_ref_$v"
+  rm -f "${objs[@]}"
   echo "build_ref: built $OUT/emfa_ref_$v"
 }
 

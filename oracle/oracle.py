@@ -176,7 +176,7 @@ def time_reference(config_path, kind, rows, solve=0, prec=32, timeout=3600):
                        cwd=cwd, stdin=subprocess.DEVNULL, capture_output=True, text=True, timeout=timeout)
     if r.returncode != 0:
         raise RuntimeError("reference timing failed: %s" % r.stderr[-2000:])
-    line = [l for l in r.stdout.splitlines() if l.startswith("{")][-1]
+    line = [l[l.index('{"n"'):] for l in r.stdout.splitlines() if '{"n"' in l][-1]
     return json.loads(line)
 
 

@@ -9,6 +9,7 @@
 //   emfa_ref_<f32|f64> cfie  <config> <outdir> <bicgstab_tol>
 //   emfa_ref_<f32|f64> mlfma <config> <outdir> <seed>
 //   emfa_ref_<f32|f64> time  <config> <efie|cfie> <rows> <solve:0|1>
+//   emfa_ref_<f32|f64> stages <config> <rows> <gemv_reps>
 //
 // The harness calls the same member functions EFIE::solve (EFIE.cpp:54-99),
 // CFIE::solve (CFIE.cpp:53-88) and MLFMA::solve (MLFMA.cpp:67-106) call, in
@@ -312,6 +313,50 @@ static int run_time(ConfigLoader& loader, const std::string& kind, int rows, int
     return 0;
 }
 
+// Per-stage wall times of the reference's CFIE path on a bounded sample:
+// mesh + RWG init, the leading rows x rows block of the fill, fillV, one
+// Armadillo complex GEMV of the full order (the product iml::BICGSTAB runs
+// twice per iteration, EMIterative/iml.cpp:22,29) and getBiRCS for one
+// direction.  The caller scales these to the full job.
+static int run_stages(ConfigLoader& loader, int rows, int reps)
+{
+    using clk = std::chrono::steady_clock;
+    auto sec = [](clk::time_point a) { return std::chrono::duration<double>(clk::now() - a).count(); };
+    auto t0 = clk::now();
+    CFIE s;
+    s.init(&loader);
+    double t_init = sec(t0);
+    int n = s.unknowns_;
+    s.unknowns_ = rows < n ? rows : n;
+    t0 = clk::now();
+    s.fillZ();
+    double t_block = sec(t0);
+    s.unknowns_ = n;
+    t0 = clk::now();
+    s.fillV();
+    double t_fillv = sec(t0);
+    Qcx_mat Z(n, n);
+    std::mt19937 gen(3);
+    std::uniform_real_distribution<float> U(-1.0f, 1.0f);
+    for (size_t i = 0; i < Z.n_elem; ++i) Z(i) = Complex(U(gen), U(gen));
+    Qcx_vec x(n), y(n);
+    for (int i = 0; i < n; ++i) x(i) = Complex(U(gen), U(gen));
+    y = Z * x;  // warm
+    t0 = clk::now();
+    for (int r = 0; r < reps; ++r) y = Z * x;
+    double t_gemv = sec(t0) / reps;
+    s.I = x;
+    t0 = clk::now();
+    volatile value_t v = s.getBiRCS(VectorR3(1, 0, 0));
+    (void)v;
+    double t_rcs = sec(t0);
+    std::printf("{\"n\": %d, \"rows\": %d, \"init_s\": %.6f, \"block_fill_s\": %.6f, \"fillv_s\": %.6f, "
+                "\"gemv_s\": %.6f, \"rcs_dir_s\": %.6f}\n",
+                n, rows < n ? rows : n, t_init, t_block, t_fillv, t_gemv, t_rcs);
+    s.clear();
+    return 0;
+}
+
 int main(int argc, char** argv)
 {
     if (argc < 4) {
@@ -324,6 +369,8 @@ int main(int argc, char** argv)
         loader.load(argv[2]);
         if (mode == "time")
             return run_time(loader, argv[3], argc > 4 ? std::atoi(argv[4]) : 64, argc > 5 ? std::atoi(argv[5]) : 0);
+        if (mode == "stages")
+            return run_stages(loader, std::atoi(argv[3]), argc > 4 ? std::atoi(argv[4]) : 3);
         g_out = argv[3];
         std::experimental::filesystem::create_directories(g_out);
         if (mode == "rwg") {
