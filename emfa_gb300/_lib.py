@@ -78,6 +78,7 @@ _SIGS = {
     "emfa_fill_z": (ci, [vp, vp, ctypes.POINTER(FillParams), vp, sz, vp]),
     "emfa_fill_v": (ci, [vp, vp, ctypes.POINTER(FillParams), vp, ci, vp, vp]),
     "emfa_matvec": (ci, [vp, ci, ci, vp, ci, vp, ci, vp, vp]),
+    "emfa_matvec_tf32_noalloc": (ci, [vp, ci, vp, ci, vp, vp]),
     "emfa_solve": (ci, [vp, ci, vp, ci, vp, ci, vp, ctypes.POINTER(SolverParams), ctypes.POINTER(SolveInfo), vp]),
     "emfa_rcs": (ci, [vp, vp, ctypes.POINTER(FillParams), vp, ci, vp, ci, ci, vp, vp]),
     "emfa_mlfma_plan": (ci, [vp, ci, vp, ci, ctypes.POINTER(MlfmaParams), ip, vp, ci, vp, vp]),

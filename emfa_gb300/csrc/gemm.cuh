@@ -19,6 +19,12 @@ namespace emfa {
 emfa_status_t cgemm_tf32(Ctx* c, const void* Z, size_t ldz, const void* X, int n, int nrhs, void* Y, cudaStream_t st);
 // reads the tensor-core GEMM's error word (synchronises the stream)
 emfa_status_t gemm_check_error(Ctx* c, cudaStream_t st);
+// The same product on caller-owned scratch and without a context: bpack holds
+// 16 * n * nrhs bytes (16-byte aligned), err is an int the caller has zeroed.
+// cgemm_tf32_prepare sets the kernels' shared-memory limit on the current device.
+emfa_status_t cgemm_tf32_prepare();
+emfa_status_t cgemm_tf32_scratch(const void* Z, size_t ldz, const void* X, int n, int nrhs, void* Y, void* bpack,
+                                 int* err, cudaStream_t st);
 // Linear operator driven by the batched Krylov solvers (krylov.cu): the
 // dense impedance matrix or the MLFMA operator.
 struct LinOp {

@@ -357,4 +357,39 @@ emfa_status_t gemm_check_error(Ctx* c, cudaStream_t st)
     return EMFA_OK;
 }
 
+emfa_status_t cgemm_tf32_prepare()
+{
+    EMFA_CUDA(nullptr, cudaFuncSetAttribute(tc::k_gemm_tf32<64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            tc::Smem<64>::TOTAL));
+    EMFA_CUDA(nullptr, cudaFuncSetAttribute(tc::k_gemm_tf32<144>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            tc::Smem<144>::TOTAL));
+    return EMFA_OK;
+}
+
+emfa_status_t cgemm_tf32_scratch(const void* Z, size_t ldz, const void* X, int n, int nrhs, void* Y, void* bpack,
+                                 int* err, cudaStream_t st)
+{
+    if ((n & 1) || (ldz & 1) || ((uintptr_t)Z & 15) || ((uintptr_t)bpack & 15)) {
+        set_error(nullptr, "cgemm_tf32: needs even n and ldz and 16-byte aligned operands (TMA strides)");
+        return EMFA_ERR_UNSUPPORTED;
+    }
+    size_t tot = (size_t)n * nrhs;
+    tc::k_pack_b<<<(int)std::min<size_t>((tot + 255) / 256, 8192), 256, 0, st>>>((const float2*)X, n, nrhs,
+                                                                                 (float2*)bpack);
+    EMFA_CUDA(nullptr, cudaGetLastError());
+    CUtensorMap ta, tb;
+    const int BN = 2 * nrhs <= 64 ? 64 : 144;
+    EMFA_TRY(make_map(nullptr, &ta, Z, 2 * (uint64_t)n, (uint64_t)n, ldz * 8, tc::BM));
+    EMFA_TRY(make_map(nullptr, &tb, bpack, 2 * (uint64_t)n, 2 * (uint64_t)nrhs, (uint64_t)n * 8, BN));
+    dim3 grd((2 * nrhs + BN - 1) / BN, (n + tc::BM - 1) / tc::BM);
+    int kblocks = (2 * n + tc::BK - 1) / tc::BK;
+    if (BN == 64)
+        tc::k_gemm_tf32<64><<<grd, tc::THREADS, tc::Smem<64>::TOTAL, st>>>(ta, tb, (float2*)Y, n, nrhs, kblocks, err);
+    else
+        tc::k_gemm_tf32<144><<<grd, tc::THREADS, tc::Smem<144>::TOTAL, st>>>(ta, tb, (float2*)Y, n, nrhs, kblocks,
+                                                                             err);
+    EMFA_CUDA(nullptr, cudaGetLastError());
+    return EMFA_OK;
+}
+
 }  // namespace emfa

@@ -151,6 +151,34 @@ emfa_status_t emfa_fill_v(emfa_ctx_t* ctx, emfa_geom_t* geom, const emfa_fill_pa
 emfa_status_t emfa_matvec(emfa_ctx_t* ctx, int prec, int matvec, const void* Z_dev, int n, const void* X_dev,
                           int n_rhs, void* Y_dev, void* stream);
 
+/* Largest n * n_rhs accepted by emfa_matvec_tf32_noalloc (16 MiB of scratch). */
+#define EMFA_NOALLOC_MAX_ELEMS 1048576u
+
+/* Y = Z X exactly as emfa_matvec(ctx, EMFA_F32, EMFA_MV_TF32, ...) computes it
+ * (complex64 Z row-major n x n, X and Y n_rhs x n, device pointers, Z 16-byte
+ * aligned, n even), but the call allocates no device memory: no cudaMalloc,
+ * no cudaFree, no allocating library routine.  No counterpart in the
+ * reference, which has no device code.
+ *
+ * Who needs it: a caller whose device memory is all handed out by its own
+ * pool (so a library allocation would fail or evict), or a serving loop that
+ * shares the GPU with other streams, where cudaFree would synchronise the whole
+ * device and stall them.  It needs no context either.
+ *
+ * Scratch: one fixed static device array per device, sized for
+ * n * n_rhs <= EMFA_NOALLOC_MAX_ELEMS; larger products return
+ * EMFA_ERR_INVALID with a message saying so (use emfa_matvec for them).
+ * The first call on a device, made with that device current, looks the array
+ * up (loading this part of the library's device code there) and sets the
+ * kernels' shared-memory limit; make that first call before any stream
+ * capture.  Calls on one device share the array, so two calls that overlap in
+ * time (different streams, or different host threads) race and corrupt each
+ * other's result: order them.  stream NULL is the default stream; the call
+ * synchronises `stream` before it returns, to read the kernel's error word.
+ * Errors are reported through emfa_last_error(NULL). */
+emfa_status_t emfa_matvec_tf32_noalloc(const void* Z_dev, int n, const void* X_dev, int n_rhs, void* Y_dev,
+                                       void* stream);
+
 /* Solves Z X = B for n_rhs right-hand sides (B complex64 for EMFA_F32,
  * complex128 for EMFA_F64; X always complex128, n_rhs x n).  GMRES(m) or
  * BiCGStab, all right-hand sides in lockstep with one multi-RHS product per
