@@ -138,6 +138,7 @@ def run_emfa(args, workload):
         step(False)
     torch.cuda.synchronize()
     l0 = ctx.launches()
+    ctx.kernel_timing(True)  # event pairs around the fill, the TF32 product and the residual
     start = torch.cuda.Event(enable_timing=True)
     end = torch.cuda.Event(enable_timing=True)
     step_ms = []
@@ -155,6 +156,8 @@ def run_emfa(args, workload):
             torch.distributed.barrier()
     total_ms = start.elapsed_time(end)
     launches = (ctx.launches() - l0) // max(1, args.steps)
+    kernels = {k: ctx.kernel_time(k) for k in ctx.KERNEL_TIMERS}
+    ctx.kernel_timing(False)
     if world > 1:
         t = torch.tensor([total_ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -195,7 +198,49 @@ def run_emfa(args, workload):
         "launches": launches, "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
                                       "d2h_bytes_per_step": int(d2h), "ms": statistics.median(e2e_ms)},
         "clocks": clocks.summary(), "n": n, "n_inc": n_inc, "acc": acc, "world": world, "rank": rank,
+        "kernels": kernels,
     }
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except (OSError, ValueError):
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+# DRAM bytes (read + write) per launch of the TF32 product on the 7680 x 360
+# job, from one ncu capture (profiles/k_gemm_tf32_c2_7680x360.md).
+GEMM_TRAFFIC_BYTES = None
+
+
+def roofline(res):
+    """Roofline of the dominant kernel of the step (the tensor-core product
+    of the Krylov iterations), from the event-timed launches of the timed
+    region.  TF32 runs at half the bf16 tensor rate on this part, so the
+    fraction of the measured bf16 peak is at most ~0.5 for a TF32 kernel."""
+    peaks, src = measured_peaks()
+    n_l, ms, flops = res["kernels"]["gemm_tf32"]
+    if not n_l:
+        return None
+    achieved = flops / (ms * 1e-3) / 1e12
+    peak = peaks["bf16_tflops_sustained"]
+    return {"kernel": "tc::k_gemm_tf32", "bound": "tensor", "achieved": round(achieved, 2), "peak": peak,
+            "unit": "TFLOP/s", "frac": round(achieved / peak, 4), "traffic": GEMM_TRAFFIC_BYTES,
+            "peak_source": "%s bf16 dense, sustained (kernel timed inside a long step)" % src,
+            "operand": "tf32 (nominal tf32 dense rate = 1/2 bf16)", "launches": n_l,
+            "avg_launch_ms": round(ms / n_l, 5), "flops_per_launch": flops / n_l}
+
+
+def kernel_table(res):
+    out = {}
+    for k, (n_l, ms, work) in res["kernels"].items():
+        if n_l:
+            unit = "Gentries/s" if k == "fill_z" else "TFLOP/s"
+            rate = work / (ms * 1e-3) / (1e9 if k == "fill_z" else 1e12)
+            out[k] = {"launches": n_l, "avg_ms": round(ms / n_l, 4), "rate": round(rate, 2), "unit": unit}
+    return out
 
 
 def run_gemm_only(args):
@@ -311,6 +356,8 @@ def main():
         "gpu_launches": res["launches"],
         "clocks": res["clocks"],
         "accuracy": res["acc"],
+        "roofline": roofline(res),
+        "kernels": kernel_table(res),
     }
     if world == 1 and args.cpu_baseline:
         # the reference's own CPU path on this host's cores, bounded sample (oracle/cpu_baseline.py)

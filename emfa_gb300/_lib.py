@@ -79,6 +79,9 @@ _SIGS = {
     "emfa_fill_v": (ci, [vp, vp, ctypes.POINTER(FillParams), vp, ci, vp, vp]),
     "emfa_matvec": (ci, [vp, ci, ci, vp, ci, vp, ci, vp, vp]),
     "emfa_matvec_tf32_noalloc": (ci, [vp, ci, vp, ci, vp, vp]),
+    "emfa_ctx_set_kernel_timing": (ci, [vp, ci]),
+    "emfa_ctx_kernel_time": (ci, [vp, ci, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_double),
+                                  ctypes.POINTER(ctypes.c_double)]),
     "emfa_solve": (ci, [vp, ci, vp, ci, vp, ci, vp, ctypes.POINTER(SolverParams), ctypes.POINTER(SolveInfo), vp]),
     "emfa_rcs": (ci, [vp, vp, ctypes.POINTER(FillParams), vp, ci, vp, ci, ci, vp, vp]),
     "emfa_mlfma_plan": (ci, [vp, ci, vp, ci, ctypes.POINTER(MlfmaParams), ip, vp, ci, vp, vp]),

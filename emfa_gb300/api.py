@@ -83,6 +83,21 @@ class Context:
         self.check(L.lib().emfa_ctx_stream(self.h, ctypes.byref(s)))
         return s.value or 0
 
+    KERNEL_TIMERS = {"fill_z": 0, "gemm_tf32": 1, "residual": 2}
+
+    def kernel_timing(self, on: bool):
+        """Turns per-kernel event timing on or off (and clears its records)."""
+        self.check(L.lib().emfa_ctx_set_kernel_timing(self.h, 1 if on else 0))
+
+    def kernel_time(self, kernel: str):
+        """(launches, summed device ms, summed algorithmic work) of one timed
+        kernel since timing was turned on; work is FLOPs for the products and
+        Z entries for the fill."""
+        n, ms, w = ctypes.c_int64(), ctypes.c_double(), ctypes.c_double()
+        self.check(L.lib().emfa_ctx_kernel_time(self.h, self.KERNEL_TIMERS[kernel], ctypes.byref(n), ctypes.byref(ms),
+                                                ctypes.byref(w)))
+        return n.value, ms.value, w.value
+
 
 class Geometry:
     def __init__(self, ctx: Context, mesh: TriMesh, rwg: np.ndarray | None = None):

@@ -61,6 +61,32 @@ emfa_status_t ctx_alloc(Ctx* c, size_t bytes, void** p)
     return EMFA_OK;
 }
 
+TimedLaunch::TimedLaunch(Ctx* c, int id, cudaStream_t st, double work) : c_(c), st_(st)
+{
+    if (!c || !c->time_kernels) return;
+    std::lock_guard<std::mutex> g(c->mu);
+    KernelTimer& t = c->timers[id];
+    if (t.used == t.start.size()) {
+        cudaEvent_t a = nullptr, b = nullptr;
+        if (cudaEventCreate(&a) != cudaSuccess) return;
+        if (cudaEventCreate(&b) != cudaSuccess) {
+            cudaEventDestroy(a);
+            return;
+        }
+        t.start.push_back(a);
+        t.stop.push_back(b);
+    }
+    if (cudaEventRecord(t.start[t.used], st) != cudaSuccess) return;
+    stop_ = t.stop[t.used];
+    t.used += 1;
+    t.work += work;
+}
+
+TimedLaunch::~TimedLaunch()
+{
+    if (stop_) cudaEventRecord(stop_, st_);
+}
+
 emfa_status_t ctx_workspace(Ctx* c, int slot, size_t bytes, void** p)
 {
     DevBuf& b = c->ws[slot];
@@ -152,6 +178,10 @@ emfa_status_t emfa_ctx_destroy(emfa_ctx_t* ctx)
     }
     for (auto& b : ctx->ws) b.release();
     for (auto& kv : ctx->user_bufs) cudaFree(kv.first);
+    for (auto& t : ctx->timers) {
+        for (auto e : t.start) cudaEventDestroy(e);
+        for (auto e : t.stop) cudaEventDestroy(e);
+    }
     delete ctx;
     return EMFA_OK;
 }
@@ -169,6 +199,37 @@ emfa_status_t emfa_ctx_launch_count(const emfa_ctx_t* ctx, int64_t* count)
 {
     if (!ctx || !count) return EMFA_ERR_INVALID;
     *count = (int64_t)ctx->kernel_launches;
+    return EMFA_OK;
+}
+
+emfa_status_t emfa_ctx_set_kernel_timing(emfa_ctx_t* ctx, int on)
+{
+    if (!ctx) return EMFA_ERR_INVALID;
+    std::lock_guard<std::mutex> g(ctx->mu);
+    ctx->time_kernels = on != 0;
+    for (auto& t : ctx->timers) {
+        t.used = 0;
+        t.work = 0.0;
+    }
+    return EMFA_OK;
+}
+
+emfa_status_t emfa_ctx_kernel_time(emfa_ctx_t* ctx, int kernel, int64_t* launches, double* total_ms, double* work)
+{
+    if (!ctx || kernel < 0 || kernel >= KT_COUNT || !launches || !total_ms) return EMFA_ERR_INVALID;
+    EMFA_CUDA(ctx, cudaSetDevice(ctx->device));
+    std::lock_guard<std::mutex> g(ctx->mu);
+    const KernelTimer& t = ctx->timers[kernel];
+    double sum = 0.0;
+    for (size_t i = 0; i < t.used; ++i) {
+        EMFA_CUDA(ctx, cudaEventSynchronize(t.stop[i]));
+        float ms = 0.f;
+        EMFA_CUDA(ctx, cudaEventElapsedTime(&ms, t.start[i], t.stop[i]));
+        sum += ms;
+    }
+    *launches = (int64_t)t.used;
+    *total_ms = sum;
+    if (work) *work = t.work;
     return EMFA_OK;
 }
 

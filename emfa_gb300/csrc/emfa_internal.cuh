@@ -81,6 +81,15 @@ template <typename T> inline T* dptr(const DevBuf& b) { return reinterpret_cast<
 // products and solves do not allocate.  A slot grows when a call needs more.
 enum WorkspaceSlot { WS_GEMM_B = 0, WS_GEMM_ERR, WS_KRYLOV, WS_FILL, WS_RCS, WS_COUNT };
 
+// Kernels the context can time with CUDA events (emfa_ctx_set_kernel_timing).
+enum KernelTimerId { KT_FILL_Z = 0, KT_GEMM_TF32, KT_RESIDUAL, KT_COUNT };
+
+struct KernelTimer {
+    std::vector<cudaEvent_t> start, stop;  // one pair per timed launch
+    size_t used = 0;
+    double work = 0.0;  // algorithmic FLOPs (products) or entries (fill) of the recorded launches
+};
+
 struct Ctx {
     int device = 0;
     size_t budget = 0;      // bytes the context may hold (0 = unlimited)
@@ -91,11 +100,26 @@ struct Ctx {
     std::mutex mu;
     int sm_count = 0;
     long long kernel_launches = 0;  // kernels launched through this context
+    bool time_kernels = false;
+    KernelTimer timers[KT_COUNT];
     DevBuf ws[WS_COUNT];            // declared after mu: destroyed before it
     std::map<void*, size_t> user_bufs;  // emfa_device_alloc'ed buffers
 };
 
 emfa_status_t ctx_workspace(Ctx* c, int slot, size_t bytes, void** p);
+
+// Brackets one kernel launch with events on its stream when the context's
+// kernel timing is on; does nothing otherwise.
+class TimedLaunch {
+public:
+    TimedLaunch(Ctx* c, int id, cudaStream_t st, double work);
+    ~TimedLaunch();
+
+private:
+    Ctx* c_;
+    cudaStream_t st_;
+    cudaEvent_t stop_ = nullptr;
+};
 
 // carve 256-byte aligned sub-buffers out of one workspace
 struct Carver {

@@ -245,12 +245,15 @@ static emfa_status_t fill_z_t(Ctx* c, Geom* g, GeomDev<T>& d, const emfa_fill_pa
     FillConst<T> fc = make_fill_const<T>(p);
     dim3 blk(32, 8);
     dim3 grd((g->n + 31) / 32, (g->n + 7) / 8);
-    if (cfie)
-        k_fill_z<T, true><<<grd, blk, 0, st>>>(dptr<RwgPack<T>>(d.rwg), g->n, fc, (const double2*)tab,
-                                               reinterpret_cast<Cx<T>*>(Z), ldz);
-    else
-        k_fill_z<T, false><<<grd, blk, 0, st>>>(dptr<RwgPack<T>>(d.rwg), g->n, fc, (const double2*)tab,
-                                                reinterpret_cast<Cx<T>*>(Z), ldz);
+    {
+        TimedLaunch tl(c, KT_FILL_Z, st, (double)g->n * g->n);
+        if (cfie)
+            k_fill_z<T, true><<<grd, blk, 0, st>>>(dptr<RwgPack<T>>(d.rwg), g->n, fc, (const double2*)tab,
+                                                   reinterpret_cast<Cx<T>*>(Z), ldz);
+        else
+            k_fill_z<T, false><<<grd, blk, 0, st>>>(dptr<RwgPack<T>>(d.rwg), g->n, fc, (const double2*)tab,
+                                                    reinterpret_cast<Cx<T>*>(Z), ldz);
+    }
     c->kernel_launches += 1;
     EMFA_CUDA(c, cudaGetLastError());
     EMFA_CUDA(c, cudaStreamSynchronize(st));

@@ -124,8 +124,11 @@ emfa_status_t cgemm_f32_chunked(Ctx* c, const void* Z, size_t ldz, const void* X
                                 void* Yd, cudaStream_t st)
 {
     dim3 grd((n + 63) / 64, (nrhs + 63) / 64);
-    k_cgemm<float, true><<<grd, 256, 0, st>>>((const Cx<float>*)Z, ldz, (const Cx<float>*)X, n, nrhs, nullptr,
-                                              (const Cx<float>*)Bsub, (Cx<double>*)Yd);
+    {
+        TimedLaunch tl(c, KT_RESIDUAL, st, 8.0 * n * (double)n * nrhs);
+        k_cgemm<float, true><<<grd, 256, 0, st>>>((const Cx<float>*)Z, ldz, (const Cx<float>*)X, n, nrhs, nullptr,
+                                                  (const Cx<float>*)Bsub, (Cx<double>*)Yd);
+    }
     c->kernel_launches += 1;
     EMFA_CUDA(c, cudaGetLastError());
     return EMFA_OK;

@@ -309,7 +309,10 @@ static emfa_status_t launch_tc(Ctx* c, const CUtensorMap& ta, const CUtensorMap&
     }
     dim3 grd((2 * nrhs + BN - 1) / BN, (n + tc::BM - 1) / tc::BM);
     int kblocks = (2 * n + tc::BK - 1) / tc::BK;
-    tc::k_gemm_tf32<BN><<<grd, tc::THREADS, S::TOTAL, st>>>(ta, tb, Y, n, nrhs, kblocks, err);
+    {
+        TimedLaunch tl(c, KT_GEMM_TF32, st, 8.0 * n * (double)n * nrhs);
+        tc::k_gemm_tf32<BN><<<grd, tc::THREADS, S::TOTAL, st>>>(ta, tb, Y, n, nrhs, kblocks, err);
+    }
     c->kernel_launches += 1;
     EMFA_CUDA(c, cudaGetLastError());
     return EMFA_OK;

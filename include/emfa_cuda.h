@@ -104,6 +104,22 @@ emfa_status_t emfa_ctx_synchronize(emfa_ctx_t* ctx);
 /* The context's own CUDA stream (a cudaStream_t), used when a call gets NULL. */
 emfa_status_t emfa_ctx_stream(const emfa_ctx_t* ctx, void** stream);
 
+/* Per-kernel timing (the time log of EM::reportTimeInfo, EMSolver/EM.cpp:85-89,
+ * at kernel granularity).  While on, every launch of the kernels below is
+ * bracketed by a pair of CUDA events on its own stream; turning it on or off
+ * clears the records.  emfa_ctx_kernel_time waits for the recorded launches
+ * and returns their count, summed device time and summed algorithmic work
+ * (work may be NULL): FLOPs for the products (8 n^2 per right-hand side of a
+ * complex product), Z entries for the fill. */
+typedef enum {
+    EMFA_KT_FILL_Z = 0,    /* impedance fill (EFIE/CFIE)                       */
+    EMFA_KT_GEMM_TF32 = 1, /* tensor-core multi-RHS product of the solvers     */
+    EMFA_KT_RESIDUAL = 2   /* accurate refinement residual b - Z x             */
+} emfa_kernel_timer_t;
+emfa_status_t emfa_ctx_set_kernel_timing(emfa_ctx_t* ctx, int on);
+emfa_status_t emfa_ctx_kernel_time(emfa_ctx_t* ctx, int kernel, int64_t* launches, double* total_ms,
+                                   double* work);
+
 /* Device buffers charged to the context's HBM budget, for callers without
  * CUDA runtime bindings of their own (the C++ front end, FFI users).
  * kind: 0 host->device, 1 device->host, 2 device->device; synchronous. */
