@@ -215,21 +215,29 @@ def measured_peaks():
 GEMM_TRAFFIC_BYTES = None
 
 
+_ARGS = {}
+
+
+def args_matvec():
+    return _ARGS.get("matvec", "auto")
+
+
 def roofline(res):
-    """Roofline of the dominant kernel of the step (the tensor-core product
-    of the Krylov iterations), from the event-timed launches of the timed
-    region.  TF32 runs at half the bf16 tensor rate on this part, so the
-    fraction of the measured bf16 peak is at most ~0.5 for a TF32 kernel."""
+    """Roofline of the dominant kernel of the step (the tensor-core inner
+    product of the Krylov iterations: split-FP16 kind::f16, the bf16 rate),
+    from the event-timed launches of the timed region."""
     peaks, src = measured_peaks()
-    n_l, ms, flops = res["kernels"]["gemm_tf32"]
+    n_l, ms, flops = res["kernels"]["gemm"]
     if not n_l:
         return None
     achieved = flops / (ms * 1e-3) / 1e12
     peak = peaks["bf16_tflops_sustained"]
-    return {"kernel": "tc::k_gemm_tf32", "bound": "tensor", "achieved": round(achieved, 2), "peak": peak,
+    return {"kernel": "th::k_hgemm<144,1>" if args_matvec() in ("auto", "f16x") else "tc::k_gemm_tf32",
+            "bound": "tensor", "achieved": round(achieved, 2), "peak": peak,
             "unit": "TFLOP/s", "frac": round(achieved / peak, 4), "traffic": GEMM_TRAFFIC_BYTES,
             "peak_source": "%s bf16 dense, sustained (kernel timed inside a long step)" % src,
-            "operand": "tf32 (nominal tf32 dense rate = 1/2 bf16)", "launches": n_l,
+            "operand": "fp16 (hi plane of Z) x fp16, fp32 accumulate" if args_matvec() in ("auto", "f16x")
+            else "tf32 (nominal tf32 dense rate = 1/2 bf16)", "launches": n_l,
             "avg_launch_ms": round(ms / n_l, 5), "flops_per_launch": flops / n_l}
 
 
@@ -314,7 +322,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="emfa", choices=["emfa", "reference"])
     ap.add_argument("--workload", default="c2_cfie_sphere_7680x360", choices=list(WORKLOADS))
-    ap.add_argument("--matvec", default="auto", choices=["auto", "f32", "tf32"])
+    ap.add_argument("--matvec", default="auto", choices=["auto", "f32", "tf32", "f16x"])
     ap.add_argument("--check", type=int, default=1)
     ap.add_argument("--cpu-baseline", type=int, default=1)
     ap.add_argument("--mode", default="job", choices=["job", "gemm", "mlfma"])
@@ -337,6 +345,7 @@ def main():
             from oracle import cpu_baseline
             print(json.dumps(cpu_baseline.reference_arm(args, WORKLOADS[args.workload], args.workload)))
         return
+    _ARGS["matvec"] = args.matvec
     res = run_emfa(args, args.workload)
     if rank != 0:
         return

@@ -21,7 +21,7 @@ STATUS = {0: "EMFA_OK", 1: "EMFA_ERR_INVALID", 2: "EMFA_ERR_CUDA", 3: "EMFA_ERR_
 EMFA_F32, EMFA_F64 = 0, 1
 EMFA_EFIE, EMFA_CFIE = 0, 1
 EMFA_GMRES, EMFA_BICGSTAB = 0, 1
-EMFA_MV_AUTO, EMFA_MV_F64, EMFA_MV_F32, EMFA_MV_TF32 = 0, 1, 2, 3
+EMFA_MV_AUTO, EMFA_MV_F64, EMFA_MV_F32, EMFA_MV_TF32, EMFA_MV_F16X = 0, 1, 2, 3, 4
 
 
 class FillParams(ctypes.Structure):
@@ -80,6 +80,7 @@ _SIGS = {
     "emfa_matvec": (ci, [vp, ci, ci, vp, ci, vp, ci, vp, vp]),
     "emfa_matvec_tf32_noalloc": (ci, [vp, ci, vp, ci, vp, vp]),
     "emfa_ctx_set_kernel_timing": (ci, [vp, ci]),
+    "emfa_residual": (ci, [vp, ci, ci, vp, ci, vp, vp, ci, vp, vp]),
     "emfa_ctx_kernel_time": (ci, [vp, ci, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_double),
                                   ctypes.POINTER(ctypes.c_double)]),
     "emfa_solve": (ci, [vp, ci, vp, ci, vp, ci, vp, ctypes.POINTER(SolverParams), ctypes.POINTER(SolveInfo), vp]),

@@ -18,6 +18,9 @@ vp = ctypes.c_void_p
 
 
 def _ptr(t):
+    """Device pointer of a tensor the C ABI reads as a dense row-major array."""
+    if not t.is_contiguous():
+        raise ValueError("emfa: tensor arguments must be contiguous (got strides %s)" % (tuple(t.stride()),))
     return vp(t.data_ptr())
 
 
@@ -40,7 +43,7 @@ def fill_params(kind="cfie", precision="f32", freq=3e8, alpha=0.5, sigma=(0.0, 0
 
 def solver_params(method="gmres", restart=30, max_iter=600, tol=1e-6, tol_absolute=False, matvec="auto",
                   max_refine=0) -> L.SolverParams:
-    mv = {"auto": 0, "f64": 1, "f32": 2, "tf32": 3}[matvec]
+    mv = {"auto": 0, "f64": 1, "f32": 2, "tf32": 3, "f16x": 4}[matvec]
     return L.SolverParams(L.EMFA_BICGSTAB if method == "bicgstab" else L.EMFA_GMRES, int(restart), int(max_iter),
                           float(tol), int(bool(tol_absolute)), mv, int(max_refine))
 
@@ -83,7 +86,7 @@ class Context:
         self.check(L.lib().emfa_ctx_stream(self.h, ctypes.byref(s)))
         return s.value or 0
 
-    KERNEL_TIMERS = {"fill_z": 0, "gemm_tf32": 1, "residual": 2}
+    KERNEL_TIMERS = {"fill_z": 0, "gemm": 1, "residual": 2}
 
     def kernel_timing(self, on: bool):
         """Turns per-kernel event timing on or off (and clears its records)."""
@@ -152,12 +155,25 @@ def fill_v(geom: Geometry, fp: L.FillParams, angles, out=None):
 def matvec(ctx: Context, Z, X, matvec="auto"):
     torch = _torch()
     prec = L.EMFA_F64 if Z.dtype == torch.complex128 else L.EMFA_F32
-    mv = {"auto": 0, "f64": 1, "f32": 2, "tf32": 3}[matvec]
+    mv = {"auto": 0, "f64": 1, "f32": 2, "tf32": 3, "f16x": 4}[matvec]
     Y = torch.empty_like(X)
     torch.cuda.current_stream().synchronize()  # inputs written on torch's stream
     ctx.check(L.lib().emfa_matvec(ctx.h, prec, mv, _ptr(Z), Z.shape[0], _ptr(X), X.shape[0], _ptr(Y), None))
     ctx.synchronize()  # the product runs on the context's stream
     return Y
+
+
+def residual(ctx: Context, Z, X, B, matvec="auto"):
+    """R = B - Z X (complex128) with the refinement residual of a matvec mode;
+    X complex128, B in Z's precision."""
+    torch = _torch()
+    prec = L.EMFA_F64 if Z.dtype == torch.complex128 else L.EMFA_F32
+    mv = {"auto": 0, "f64": 1, "f32": 2, "tf32": 3, "f16x": 4}[matvec]
+    R = torch.empty(X.shape, dtype=torch.complex128, device=X.device)
+    torch.cuda.current_stream().synchronize()
+    ctx.check(L.lib().emfa_residual(ctx.h, prec, mv, _ptr(Z), Z.shape[0], _ptr(X), _ptr(B), X.shape[0], _ptr(R), None))
+    ctx.synchronize()
+    return R
 
 
 def solve(ctx: Context, Z, B, sp: L.SolverParams):

@@ -79,10 +79,10 @@ template <typename T> inline T* dptr(const DevBuf& b) { return reinterpret_cast<
 
 // Workspace slots: buffers a context keeps between calls so repeated fills,
 // products and solves do not allocate.  A slot grows when a call needs more.
-enum WorkspaceSlot { WS_GEMM_B = 0, WS_GEMM_ERR, WS_KRYLOV, WS_FILL, WS_RCS, WS_COUNT };
+enum WorkspaceSlot { WS_GEMM_B = 0, WS_GEMM_ERR, WS_KRYLOV, WS_FILL, WS_RCS, WS_ZPLANES, WS_HGEMM, WS_COUNT };
 
 // Kernels the context can time with CUDA events (emfa_ctx_set_kernel_timing).
-enum KernelTimerId { KT_FILL_Z = 0, KT_GEMM_TF32, KT_RESIDUAL, KT_COUNT };
+enum KernelTimerId { KT_FILL_Z = 0, KT_GEMM, KT_RESIDUAL, KT_COUNT };
 
 struct KernelTimer {
     std::vector<cudaEvent_t> start, stop;  // one pair per timed launch

@@ -14,7 +14,13 @@ emfa_status_t cgemm_f32_chunked(Ctx* c, const void* Z, size_t ldz, const void* X
 
 }  // namespace emfa
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_fp16.h>
+
 namespace emfa {
+// driver entry point of cuTensorMapEncodeTiled (null if unavailable)
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder();
 // Y = Z X on the tensor cores (tcgen05, TF32 operands, FP32 accumulation).
 emfa_status_t cgemm_tf32(Ctx* c, const void* Z, size_t ldz, const void* X, int n, int nrhs, void* Y, cudaStream_t st);
 // reads the tensor-core GEMM's error word (synchronises the stream)
@@ -25,6 +31,27 @@ emfa_status_t gemm_check_error(Ctx* c, cudaStream_t st);
 emfa_status_t cgemm_tf32_prepare();
 emfa_status_t cgemm_tf32_scratch(const void* Z, size_t ldz, const void* X, int n, int nrhs, void* Y, void* bpack,
                                  int* err, cudaStream_t st);
+// Split-FP16 planes of a complex64 matrix Z (gemm_h.cu): Zh = fp16(s Z),
+// Zl = fp16(s Z - Zh) with s a power of two (max |s Z| < 2^15), each an
+// n x 2n real matrix (re, im interleaved) with rows ldh halves apart.
+struct HPlanes {
+    const __half* zh = nullptr;
+    const __half* zl = nullptr;
+    const float* inv_s = nullptr;  // device: 1 / s
+    int n = 0;
+    size_t ldh = 0;
+};
+// splits Z into the context's plane workspace (two passes over Z)
+emfa_status_t hsplit_prepare(Ctx* c, const void* Z, size_t ldz, int n, HPlanes* out, cudaStream_t st);
+// Y (complex64) = Z X (complex64): Zh times an FP16 copy of X scaled per
+// right-hand side; accuracy of a TF32 product at the FP16 tensor rate
+emfa_status_t hgemm_apply(Ctx* c, const HPlanes& h, const void* X, void* Y, int nrhs, cudaStream_t st);
+// R (complex128) = B - Z X for X complex128 and B complex64 (f32b) or complex128:
+// Zh Xh + Zh Xl + Zl Xh on the tensor cores, FP32 chunk sums reduced in FP64
+emfa_status_t hgemm_residual(Ctx* c, const HPlanes& h, const double2* X, const void* B, bool b_is_f32, double2* R,
+                             int nrhs, cudaStream_t st);
+emfa_status_t hgemm_check_error(Ctx* c, cudaStream_t st);
+
 // Linear operator driven by the batched Krylov solvers (krylov.cu): the
 // dense impedance matrix or the MLFMA operator.
 struct LinOp {

@@ -1,0 +1,699 @@
+// Split-FP16 complex products on the 5th-generation tensor cores
+// (tcgen05.mma kind::f16, FP32 accumulation in tensor memory) for the
+// mixed-precision dense solver.
+//
+// Z (complex64) is split once per solve into two FP16 planes after scaling
+// by a power of two s (max |s Z| < 2^15, so every value is in FP16 range):
+//     Zh = fp16(s Z),   Zl = fp16(s Z - Zh)        Zh + Zl = s Z to ~2^-22
+// each an n x 2n real matrix (re, im interleaved along k).  A right-hand side
+// x_r gets its own power-of-two scale t_r (max |t_r x_r| < 2^14) and is packed
+// as B rows 2r = (Re, -Im), 2r+1 = (Im, Re), so C = A B^T has the complex
+// outputs in its column pairs (the layout of the TF32 kernel, gemm_tc.cu).
+//
+//   inner product of the Krylov iterations:  Z X  ~  Zh Xh / (s t)
+//       11-bit significands on both sides: the accuracy of a TF32 product
+//       at the FP16 tensor rate, reading half the bytes of Z
+//   refinement residual:  B - Z X  with  Z X ~ (Zh Xh + Zh Xl + Zl Xh) / (s t)
+//       k_hresid: a fresh accumulator per k-block, drained into compensated
+//       FP32 sums in registers (see the kernel's comment)
+//
+// Kernel k_hgemm<BN, NP>: one 128 x BN output tile per CTA, 6 warps:
+//   warp 0      TMA producer: NP planes of A (128 x 64 halves) and of B
+//               (BN x 64 halves), 128-byte swizzle, multi-stage ring
+//   warp 1      allocates tensor memory (two accumulators); one lane issues
+//               tcgen05.mma (M = 128, N = BN, K = 16): 4 per stage and plane
+//               pair, commits each stage free and each chunk's accumulator full
+//   warps 2..5  epilogue: tcgen05.ld 32 lanes x 16 columns, scaled complex64
+//               stores (consecutive lanes = consecutive rows: coalesced)
+// Every wait is bounded (clock64): on timeout the kernel records a code in
+// the error word, waits (bounded) for its own copies and MMAs, frees tensor
+// memory and returns; the host reports EMFA_ERR_TIMEOUT.
+#include "emfa_internal.cuh"
+#include "gemm.cuh"
+#include "tcgen05.cuh"
+
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <atomic>
+
+namespace emfa {
+
+namespace th {
+
+constexpr int BM = 128;
+constexpr int BKH = 64;  // halves per stage row = 128 bytes = one swizzle atom
+constexpr int THREADS = 192;
+constexpr int SMEM_BUDGET = 216 * 1024;
+
+template <int BN, int NP>
+struct Smem {
+    static constexpr int A_BYTES = BM * 128;
+    static constexpr int B_BYTES = BN * 128;
+    static constexpr int STAGE_BYTES = NP * (A_BYTES + B_BYTES);
+    static constexpr int STAGES = SMEM_BUDGET / STAGE_BYTES > 8 ? 8 : SMEM_BUDGET / STAGE_BYTES;
+    static constexpr int ACC = BN <= 32 ? 32 : BN <= 64 ? 64 : BN <= 128 ? 128 : 256;  // columns per accumulator
+    static constexpr int TMEM_COLS = 2 * ACC;
+    static constexpr int TOTAL = STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
+};
+
+template <int BN, int NP>
+__global__ void __launch_bounds__(THREADS, 1)
+    k_hgemm(const __grid_constant__ CUtensorMap tmA0, const __grid_constant__ CUtensorMap tmA1,
+            const __grid_constant__ CUtensorMap tmB0, const __grid_constant__ CUtensorMap tmB1,
+            float2* __restrict__ Y, size_t pstride, int M, int R, int kblocks, int kc,
+            const float* __restrict__ inv_s, const float* __restrict__ inv_t, int* __restrict__ err)
+{
+    using S = Smem<BN, NP>;
+    using namespace tc;
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* base = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint8_t* sA = base;                                // [stage][plane]
+    uint8_t* sB = base + S::STAGES * NP * S::A_BYTES;  // [stage][plane]
+    uint64_t* full = (uint64_t*)(base + S::STAGES * S::STAGE_BYTES);
+    uint64_t* empty = full + S::STAGES;
+    uint64_t* acc_full = empty + S::STAGES;
+    uint64_t* acc_empty = acc_full + 2;
+    uint64_t* done = acc_empty + 2;
+    uint32_t* tmem_slot = (uint32_t*)(done + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    // grid x = column tiles, y = row tiles: CTAs sharing a row block of the
+    // planes run back to back and reuse it from L2
+    const int f0 = blockIdx.y * BM, c0 = blockIdx.x * BN;
+    const int nchunks = (kblocks + kc - 1) / kc;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < S::STAGES; ++s) {
+            mbar_init(full + s, 1);
+            mbar_init(empty + s, 1);
+        }
+        for (int a = 0; a < 2; ++a) {
+            mbar_init(acc_full + a, 1);
+            mbar_init(acc_empty + a, 4);  // one arrival per epilogue warp
+        }
+        mbar_init(done, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(S::TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            int issued = 0;
+            for (int kb = 0; kb < kblocks; ++kb) {
+                const int s = kb % S::STAGES;
+                if (kb >= S::STAGES && !mbar_wait(empty + s, ((kb / S::STAGES) - 1) & 1, err, 1)) break;
+                if (*(volatile int*)err) break;
+                mbar_expect_tx(full + s, S::STAGE_BYTES);
+                tma_load_2d(sA + (s * NP) * S::A_BYTES, &tmA0, full + s, kb * BKH, f0);
+                tma_load_2d(sB + (s * NP) * S::B_BYTES, &tmB0, full + s, kb * BKH, c0);
+                if (NP == 2) {
+                    tma_load_2d(sA + (s * NP + 1) * S::A_BYTES, &tmA1, full + s, kb * BKH, f0);
+                    tma_load_2d(sB + (s * NP + 1) * S::B_BYTES, &tmB1, full + s, kb * BKH, c0);
+                }
+                issued = kb + 1;
+            }
+            // every issued stage's copy must have landed before the CTA exits
+            for (int kb = issued - S::STAGES > 0 ? issued - S::STAGES : 0; kb < issued; ++kb)
+                mbar_wait(full + (kb % S::STAGES), (kb / S::STAGES) & 1, err, 2);
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            constexpr uint32_t idesc = idesc_f16(BM, BN);
+            for (int kb = 0; kb < kblocks; ++kb) {
+                const int s = kb % S::STAGES;
+                const int ch = kb / kc, kin = kb - ch * kc;
+                const uint32_t acc = tmem + (uint32_t)((ch & 1) * S::ACC);
+                // the accumulator is free once the epilogue drained chunk ch - 2
+                if (kin == 0 && ch >= 2) {
+                    if (!mbar_wait(acc_empty + (ch & 1), ((ch >> 1) - 1) & 1, err, 6)) break;
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                }
+                if (!mbar_wait(full + s, (kb / S::STAGES) & 1, err, 3)) break;
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint64_t da0 = sw128_desc(smem_u32(sA + (s * NP) * S::A_BYTES));
+                const uint64_t db0 = sw128_desc(smem_u32(sB + (s * NP) * S::B_BYTES));
+                const uint64_t da1 = NP == 2 ? sw128_desc(smem_u32(sA + (s * NP + 1) * S::A_BYTES)) : 0;
+                const uint64_t db1 = NP == 2 ? sw128_desc(smem_u32(sB + (s * NP + 1) * S::B_BYTES)) : 0;
+#pragma unroll
+                for (int k = 0; k < BKH / 16; ++k) {  // K = 16 halves = 32 bytes per instruction
+                    mma_f16(acc, da0 + 2 * k, db0 + 2 * k, idesc, (kin > 0 || k > 0) ? 1u : 0u);
+                    if (NP == 2) {
+                        mma_f16(acc, da0 + 2 * k, db1 + 2 * k, idesc, 1u);
+                        mma_f16(acc, da1 + 2 * k, db0 + 2 * k, idesc, 1u);
+                    }
+                }
+                mma_commit(empty + s);
+                if (kin == kc - 1 || kb == kblocks - 1) mma_commit(acc_full + (ch & 1));
+            }
+            // every MMA issued must be complete before tensor memory is released
+            mma_commit(done);
+            mbar_wait(done, 0, err, 4);
+        }
+        __syncwarp();
+    } else {
+        // epilogue warps 2..5: lane quadrant (warp % 4) of tensor memory
+        const int q = warp & 3;
+        const int f = f0 + 32 * q + lane;
+        const float is = *inv_s;
+#pragma unroll 1
+        for (int ch = 0; ch < nchunks; ++ch) {
+            const int a = ch & 1;
+            // one lane waits, the warp follows it: tcgen05.ld is warp-collective
+            int ok = lane == 0 ? (int)mbar_wait(acc_full + a, (ch >> 1) & 1, err, 5) : 0;
+            ok = __shfl_sync(0xffffffffu, ok, 0);
+            if (!ok) break;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            float2* out = Y + (size_t)ch * pstride;
+#pragma unroll 1
+            for (int c = 0; c < BN; c += 16) {
+                float v[16];
+                tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(a * S::ACC + c), v);
+                if (f < M) {
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) {
+                        const int r = (c0 + c) / 2 + i;
+                        if (r < R) {
+                            const float sc = is * inv_t[r];
+                            out[(size_t)r * M + f] = make_float2(v[2 * i] * sc, v[2 * i + 1] * sc);
+                        }
+                    }
+                }
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(acc_empty + a);
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 1) {
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(S::TMEM_COLS) : "memory");
+    }
+}
+
+// ---------------------------------------------------------------------------
+// operand preparation
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float block_max(float m, float* red)
+{
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) red[w] = m;
+    __syncthreads();
+    if (w == 0) {
+        m = l < (int)(blockDim.x >> 5) ? red[l] : 0.f;
+        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (l == 0) red[0] = m;
+    }
+    __syncthreads();
+    return red[0];
+}
+
+// max |Re|, |Im| over Z: non-negative floats order like their bit patterns
+__global__ void k_zmax(const float2* __restrict__ Z, size_t ldz, int n, unsigned int* __restrict__ amax)
+{
+    __shared__ float red[32];
+    float m = 0.f;
+    const size_t tot = (size_t)n * n;
+    for (size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x; id < tot; id += (size_t)gridDim.x * blockDim.x) {
+        const size_t i = id / n, j = id % n;
+        const float2 z = Z[i * ldz + j];
+        m = fmaxf(m, fmaxf(fabsf(z.x), fabsf(z.y)));
+    }
+    m = block_max(m, red);
+    if (threadIdx.x == 0) atomicMax(amax, __float_as_uint(m));
+}
+
+// Zh = fp16(s Z), Zl = fp16(s Z - Zh) with s = 2^(15 - e), max|Z| = m 2^e, m in [0.5, 1)
+__global__ void k_zsplit(const float2* __restrict__ Z, size_t ldz, int n, size_t ldh,
+                         const unsigned int* __restrict__ amax, __half* __restrict__ Zh, __half* __restrict__ Zl,
+                         float* __restrict__ inv_s)
+{
+    int e = 0;
+    frexpf(__uint_as_float(*amax), &e);
+    const float s = ldexpf(1.f, 15 - e);
+    if (blockIdx.x == 0 && threadIdx.x == 0) *inv_s = ldexpf(1.f, e - 15);
+    const size_t tot = (size_t)n * n;
+    for (size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x; id < tot; id += (size_t)gridDim.x * blockDim.x) {
+        const size_t i = id / n, j = id % n;
+        const float2 z = Z[i * ldz + j];
+        const float a = s * z.x, b = s * z.y;  // exact: power-of-two scaling
+        const __half ha = __float2half_rn(a), hb = __float2half_rn(b);
+        const __half la = __float2half_rn(a - __half2float(ha)), lb = __float2half_rn(b - __half2float(hb));
+        reinterpret_cast<__half2*>(Zh + i * ldh)[j] = __halves2half2(ha, hb);
+        reinterpret_cast<__half2*>(Zl + i * ldh)[j] = __halves2half2(la, lb);
+    }
+}
+
+// One CTA per right-hand side r: scale t_r = 2^(14 - e), max|x_r| = m 2^e,
+// then B rows 2r = (Re, -Im), 2r+1 = (Im, Re) of t_r x_r as FP16 pairs; the
+// lo plane (NP = 2) holds fp16(t_r x_r - hi).
+__global__ void __launch_bounds__(256) k_hpack_f32(const float2* __restrict__ X, int n, size_t ldh,
+                                                   __half* __restrict__ Bh, float* __restrict__ inv_t)
+{
+    __shared__ float red[32];
+    const int r = blockIdx.x;
+    const float2* x = X + (size_t)r * n;
+    float m = 0.f;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) m = fmaxf(m, fmaxf(fabsf(x[k].x), fabsf(x[k].y)));
+    m = block_max(m, red);
+    int e = 0;
+    frexpf(m, &e);
+    const float t = ldexpf(1.f, 14 - e);
+    if (threadIdx.x == 0) inv_t[r] = ldexpf(1.f, e - 14);
+    __half2* h0 = reinterpret_cast<__half2*>(Bh + (size_t)(2 * r) * ldh);
+    __half2* h1 = reinterpret_cast<__half2*>(Bh + (size_t)(2 * r + 1) * ldh);
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const __half hre = __float2half_rn(t * x[k].x), him = __float2half_rn(t * x[k].y);
+        h0[k] = __halves2half2(hre, __hneg(him));
+        h1[k] = __halves2half2(him, hre);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_hpack_f64(const double2* __restrict__ X, int n, size_t ldh,
+                                                   __half* __restrict__ Bh, __half* __restrict__ Bl,
+                                                   float* __restrict__ inv_t)
+{
+    __shared__ float red[32];
+    const int r = blockIdx.x;
+    const double2* x = X + (size_t)r * n;
+    float m = 0.f;
+    for (int k = threadIdx.x; k < n; k += blockDim.x)
+        m = fmaxf(m, (float)fmax(fabs(x[k].x), fabs(x[k].y)));
+    m = block_max(m, red);
+    // the float max can round up to the next power of two: scale from it
+    // keeps max |t x| < 2^14 either way
+    int e = 0;
+    frexpf(m, &e);
+    const double t = ldexp(1.0, 14 - e);
+    if (threadIdx.x == 0) inv_t[r] = ldexpf(1.f, e - 14);
+    __half2* h0 = reinterpret_cast<__half2*>(Bh + (size_t)(2 * r) * ldh);
+    __half2* h1 = reinterpret_cast<__half2*>(Bh + (size_t)(2 * r + 1) * ldh);
+    __half2* l0 = reinterpret_cast<__half2*>(Bl + (size_t)(2 * r) * ldh);
+    __half2* l1 = reinterpret_cast<__half2*>(Bl + (size_t)(2 * r + 1) * ldh);
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const double a = t * x[k].x, b = t * x[k].y;
+        const __half hre = __double2half(a), him = __double2half(b);
+        const __half lre = __double2half(a - (double)__half2float(hre));
+        const __half lim = __double2half(b - (double)__half2float(him));
+        h0[k] = __halves2half2(hre, __hneg(him));
+        h1[k] = __halves2half2(him, hre);
+        l0[k] = __halves2half2(lre, __hneg(lim));
+        l1[k] = __halves2half2(lim, lre);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// refinement residual R = B - Z X, Z X ~ (Zh Xh + Zh Xl + Zl Xh) / (s t)
+//
+// The tensor cores add into their FP32 accumulator with truncation, so the
+// error of a long accumulation grows with its length (measured on the
+// 7680-unknown CFIE matrix: 4e-6 of ||B|| for partial sums over 1024
+// columns, 5e-6 over the whole row).  Here every k-block (64 real columns)
+// starts a fresh accumulator, the two correction products go first (their
+// partial sums are 2^-11 smaller, so truncating them costs little) and the
+// hi x hi products last; eight epilogue warps drain each k-block into
+// Kahan-compensated FP32 sums in registers (56 columns each) while the next
+// k-block accumulates in the second buffer, and the last step forms
+// B - sum / (s t) in FP64.
+// ---------------------------------------------------------------------------
+constexpr int RBN = 112;  // 56 columns per epilogue warp: the sums fit the 168 registers of a 10-warp block
+constexpr int RTHREADS = 320;  // producer, MMA, 8 epilogue warps
+
+struct RSmem {
+    static constexpr int A_BYTES = BM * 128;
+    static constexpr int B_BYTES = RBN * 128;
+    static constexpr int STAGE_BYTES = 2 * (A_BYTES + B_BYTES);
+    static constexpr int STAGES = SMEM_BUDGET / STAGE_BYTES;
+    static constexpr int ACC = 128;
+    static constexpr int TMEM_COLS = 256;
+    static constexpr int TOTAL = STAGES * STAGE_BYTES + 1024 + 256;
+};
+
+__global__ void __launch_bounds__(RTHREADS, 1)
+    k_hresid(const __grid_constant__ CUtensorMap tmA0, const __grid_constant__ CUtensorMap tmA1,
+             const __grid_constant__ CUtensorMap tmB0, const __grid_constant__ CUtensorMap tmB1,
+             const void* __restrict__ Bv, int b_f64, double2* __restrict__ Rout, int M, int R, int kblocks,
+             const float* __restrict__ inv_s, const float* __restrict__ inv_t, int* __restrict__ err)
+{
+    using S = RSmem;
+    using namespace tc;
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* base = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint8_t* sA = base;                               // [stage][plane]
+    uint8_t* sB = base + S::STAGES * 2 * S::A_BYTES;  // [stage][plane]
+    uint64_t* full = (uint64_t*)(base + S::STAGES * S::STAGE_BYTES);
+    uint64_t* empty = full + S::STAGES;
+    uint64_t* acc_full = empty + S::STAGES;
+    uint64_t* acc_empty = acc_full + 2;
+    uint64_t* done = acc_empty + 2;
+    uint32_t* tmem_slot = (uint32_t*)(done + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int f0 = blockIdx.y * BM, c0 = blockIdx.x * RBN;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < S::STAGES; ++s) {
+            mbar_init(full + s, 1);
+            mbar_init(empty + s, 1);
+        }
+        for (int a = 0; a < 2; ++a) {
+            mbar_init(acc_full + a, 1);
+            mbar_init(acc_empty + a, 8);  // one arrival per epilogue warp
+        }
+        mbar_init(done, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(S::TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            int issued = 0;
+            for (int kb = 0; kb < kblocks; ++kb) {
+                const int s = kb % S::STAGES;
+                if (kb >= S::STAGES && !mbar_wait(empty + s, ((kb / S::STAGES) - 1) & 1, err, 11)) break;
+                if (*(volatile int*)err) break;
+                mbar_expect_tx(full + s, S::STAGE_BYTES);
+                tma_load_2d(sA + (2 * s) * S::A_BYTES, &tmA0, full + s, kb * BKH, f0);
+                tma_load_2d(sA + (2 * s + 1) * S::A_BYTES, &tmA1, full + s, kb * BKH, f0);
+                tma_load_2d(sB + (2 * s) * S::B_BYTES, &tmB0, full + s, kb * BKH, c0);
+                tma_load_2d(sB + (2 * s + 1) * S::B_BYTES, &tmB1, full + s, kb * BKH, c0);
+                issued = kb + 1;
+            }
+            for (int kb = issued - S::STAGES > 0 ? issued - S::STAGES : 0; kb < issued; ++kb)
+                mbar_wait(full + (kb % S::STAGES), (kb / S::STAGES) & 1, err, 12);
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            constexpr uint32_t idesc = idesc_f16(BM, RBN);
+            for (int kb = 0; kb < kblocks; ++kb) {
+                const int s = kb % S::STAGES;
+                const uint32_t acc = tmem + (uint32_t)((kb & 1) * S::ACC);
+                if (kb >= 2) {
+                    if (!mbar_wait(acc_empty + (kb & 1), ((kb >> 1) - 1) & 1, err, 16)) break;
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                }
+                if (!mbar_wait(full + s, (kb / S::STAGES) & 1, err, 13)) break;
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint64_t dah = sw128_desc(smem_u32(sA + (2 * s) * S::A_BYTES));
+                const uint64_t dal = sw128_desc(smem_u32(sA + (2 * s + 1) * S::A_BYTES));
+                const uint64_t dbh = sw128_desc(smem_u32(sB + (2 * s) * S::B_BYTES));
+                const uint64_t dbl = sw128_desc(smem_u32(sB + (2 * s + 1) * S::B_BYTES));
+#pragma unroll
+                for (int k = 0; k < BKH / 16; ++k) {  // corrections: Zh Xl + Zl Xh
+                    mma_f16(acc, dah + 2 * k, dbl + 2 * k, idesc, k > 0 ? 1u : 0u);
+                    mma_f16(acc, dal + 2 * k, dbh + 2 * k, idesc, 1u);
+                }
+#pragma unroll
+                for (int k = 0; k < BKH / 16; ++k) mma_f16(acc, dah + 2 * k, dbh + 2 * k, idesc, 1u);
+                mma_commit(empty + s);
+                mma_commit(acc_full + (kb & 1));
+            }
+            mma_commit(done);
+            mbar_wait(done, 0, err, 14);
+        }
+        __syncwarp();
+    } else {
+        // epilogue warps 2..9: lane quadrant warp % 4, column half (warp - 2) / 4
+        const int q = warp & 3, h = (warp - 2) >> 2;
+        const int f = f0 + 32 * q + lane;
+        const int col0 = 56 * h;
+        // Kahan sums: sum - cmp is the running total.  cmp stays below half an
+        // ulp of sum, so bf16 holds it to 2^-32 of the total (84 registers for
+        // 56 columns instead of 112)
+        float sum[56];
+        __nv_bfloat162 cmp[28];
+#pragma unroll
+        for (int i = 0; i < 56; ++i) sum[i] = 0.f;
+#pragma unroll
+        for (int i = 0; i < 28; ++i) cmp[i] = __floats2bfloat162_rn(0.f, 0.f);
+        bool ok = true;
+#pragma unroll 1
+        for (int kb = 0; kb < kblocks; ++kb) {
+            const int a = kb & 1;
+            int w = lane == 0 ? (int)mbar_wait(acc_full + a, (kb >> 1) & 1, err, 15) : 0;
+            w = __shfl_sync(0xffffffffu, w, 0);
+            if (!w) {
+                ok = false;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+            for (int g = 0; g < 7; ++g) {
+                float v[8];
+                tmem_ld8(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(a * S::ACC + col0 + 8 * g), v);
+#pragma unroll
+                for (int i = 0; i < 8; i += 2) {
+                    const int j = 8 * g + i;
+                    const float2 c = __bfloat1622float2(cmp[j / 2]);
+                    const float y0 = __fsub_rn(v[i], c.x), y1 = __fsub_rn(v[i + 1], c.y);
+                    const float t0 = __fadd_rn(sum[j], y0), t1 = __fadd_rn(sum[j + 1], y1);
+                    cmp[j / 2] = __floats2bfloat162_rn(__fsub_rn(__fsub_rn(t0, sum[j]), y0),
+                                                       __fsub_rn(__fsub_rn(t1, sum[j + 1]), y1));
+                    sum[j] = t0;
+                    sum[j + 1] = t1;
+                }
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(acc_empty + a);
+        }
+        if (ok) {
+            // the stage ring is idle once the last accumulator was drained: park
+            // the sums there and form the outputs one at a time
+            float* park = reinterpret_cast<float*>(base) + (size_t)((warp - 2) * 32 + lane) * 112;
+#pragma unroll
+            for (int i = 0; i < 28; ++i) {
+                const float2 cf = __bfloat1622float2(cmp[i]);
+                park[4 * i] = sum[2 * i];
+                park[4 * i + 1] = cf.x;
+                park[4 * i + 2] = sum[2 * i + 1];
+                park[4 * i + 3] = cf.y;
+            }
+            if (f < M) {
+                const double is = (double)*inv_s;
+#pragma unroll 1
+                for (int i = 0; i < 28; ++i) {
+                    const int r = (c0 + col0) / 2 + i;
+                    if (r >= R) break;
+                    const double sc = is * (double)inv_t[r];
+                    const double re = ((double)park[4 * i] - (double)park[4 * i + 1]) * sc;
+                    const double im = ((double)park[4 * i + 2] - (double)park[4 * i + 3]) * sc;
+                    const size_t o = (size_t)r * M + f;
+                    double2 b;
+                    if (b_f64) {
+                        b = reinterpret_cast<const double2*>(Bv)[o];
+                    } else {
+                        const float2 bf = reinterpret_cast<const float2*>(Bv)[o];
+                        b = make_double2(bf.x, bf.y);
+                    }
+                    Rout[o] = make_double2(b.x - re, b.y - im);
+                }
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 1) {
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(S::TMEM_COLS) : "memory");
+    }
+}
+
+}  // namespace th
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+static size_t ld_halves(int n) { return ((size_t)2 * n + 7) & ~(size_t)7; }  // 16-byte rows
+
+static int grid_stride_blocks(Ctx* c, size_t tot)
+{
+    const int sms = c->sm_count > 0 ? c->sm_count : 148;
+    return (int)std::max<size_t>(1, std::min<size_t>((tot + 255) / 256, (size_t)sms * 8));
+}
+
+// FP16 2-D tensor map: inner extent `inner` halves, `rows` rows `ld` halves
+// apart, box 64 x box_rows, 128-byte swizzle, zero fill out of bounds.
+static emfa_status_t make_map_h(Ctx* c, CUtensorMap* m, const void* ptr, uint64_t inner, uint64_t rows, size_t ld,
+                                uint32_t box_rows)
+{
+    auto fn = tensor_map_encoder();
+    if (!fn) {
+        set_error(c, "cuTensorMapEncodeTiled unavailable");
+        return EMFA_ERR_CUDA;
+    }
+    cuuint64_t dims[2] = {inner, rows};
+    cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
+    cuuint32_t box[2] = {(cuuint32_t)th::BKH, box_rows};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, const_cast<void*>(ptr), dims, strides, box, estr,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        set_error(c, "cuTensorMapEncodeTiled (fp16) failed (" + std::to_string((int)r) + ")");
+        return EMFA_ERR_CUDA;
+    }
+    return EMFA_OK;
+}
+
+template <int BN, int NP>
+static emfa_status_t launch_h(Ctx* c, const CUtensorMap& a0, const CUtensorMap& a1, const CUtensorMap& b0,
+                              const CUtensorMap& b1, float2* Y, size_t pstride, int n, int nrhs, int kc,
+                              const float* inv_s, const float* inv_t, int* err, cudaStream_t st, int timer)
+{
+    using S = th::Smem<BN, NP>;
+    static std::atomic<unsigned long long> attr_set{0};  // one bit per device
+    const unsigned long long bit = 1ull << (c->device & 63);
+    if (!(attr_set.load() & bit)) {
+        EMFA_CUDA(c, cudaFuncSetAttribute(th::k_hgemm<BN, NP>, cudaFuncAttributeMaxDynamicSharedMemorySize, S::TOTAL));
+        attr_set.fetch_or(bit);
+    }
+    dim3 grd((2 * nrhs + BN - 1) / BN, (n + th::BM - 1) / th::BM);
+    const int kblocks = (2 * n + th::BKH - 1) / th::BKH;
+    {
+        TimedLaunch tl(c, timer, st, 8.0 * n * (double)n * nrhs);
+        th::k_hgemm<BN, NP><<<grd, th::THREADS, S::TOTAL, st>>>(a0, a1, b0, b1, Y, pstride, n, nrhs, kblocks, kc,
+                                                               inv_s, inv_t, err);
+    }
+    c->kernel_launches += 1;
+    EMFA_CUDA(c, cudaGetLastError());
+    return EMFA_OK;
+}
+
+// error word of the split kernels: int 4 of the context's GEMM error slot
+static emfa_status_t herr(Ctx* c, int** err)
+{
+    void* ep = nullptr;
+    EMFA_TRY(ctx_workspace(c, WS_GEMM_ERR, 64, &ep));
+    *err = (int*)ep + 4;
+    return EMFA_OK;
+}
+
+emfa_status_t hsplit_prepare(Ctx* c, const void* Z, size_t ldz, int n, HPlanes* out, cudaStream_t st)
+{
+    const size_t ldh = ld_halves(n);
+    const size_t plane = Carver::round(sizeof(__half) * ldh * (size_t)n);
+    void* wp = nullptr;
+    EMFA_TRY(ctx_workspace(c, WS_ZPLANES, 2 * plane + 256, &wp));
+    Carver cv{(char*)wp};
+    __half* zh = cv.take<__half>(ldh * (size_t)n);
+    __half* zl = cv.take<__half>(ldh * (size_t)n);
+    unsigned int* amax = cv.take<unsigned int>(1);
+    float* inv_s = cv.take<float>(1);
+    int* err = nullptr;
+    EMFA_TRY(herr(c, &err));
+    EMFA_CUDA(c, cudaMemsetAsync(err, 0, sizeof(int), st));
+    EMFA_CUDA(c, cudaMemsetAsync(amax, 0, sizeof(unsigned int), st));
+    const int g = grid_stride_blocks(c, (size_t)n * n);
+    th::k_zmax<<<g, 256, 0, st>>>((const float2*)Z, ldz, n, amax);
+    th::k_zsplit<<<g, 256, 0, st>>>((const float2*)Z, ldz, n, ldh, amax, zh, zl, inv_s);
+    c->kernel_launches += 2;
+    EMFA_CUDA(c, cudaGetLastError());
+    out->zh = zh;
+    out->zl = zl;
+    out->inv_s = inv_s;
+    out->n = n;
+    out->ldh = ldh;
+    return EMFA_OK;
+}
+
+emfa_status_t hgemm_apply(Ctx* c, const HPlanes& h, const void* X, void* Y, int nrhs, cudaStream_t st)
+{
+    const int n = h.n;
+    const size_t ldh = h.ldh;
+    void* wp = nullptr;
+    const size_t bplane = Carver::round(sizeof(__half) * ldh * 2 * (size_t)nrhs);
+    EMFA_TRY(ctx_workspace(c, WS_HGEMM, bplane + Carver::round(sizeof(float) * nrhs) + 256, &wp));
+    Carver cv{(char*)wp};
+    __half* bh = cv.take<__half>(ldh * 2 * (size_t)nrhs);
+    float* inv_t = cv.take<float>(nrhs);
+    int* err = nullptr;
+    EMFA_TRY(herr(c, &err));
+    th::k_hpack_f32<<<nrhs, 256, 0, st>>>((const float2*)X, n, ldh, bh, inv_t);
+    c->kernel_launches += 1;
+    const int BN = 2 * nrhs <= 64 ? 64 : 144;
+    CUtensorMap ta, tb;
+    EMFA_TRY(make_map_h(c, &ta, h.zh, 2 * (uint64_t)n, (uint64_t)n, ldh, th::BM));
+    EMFA_TRY(make_map_h(c, &tb, bh, 2 * (uint64_t)n, 2 * (uint64_t)nrhs, ldh, BN));
+    const int kc = 1 << 30;  // one chunk: the whole K in one accumulator
+    if (BN == 64)
+        return launch_h<64, 1>(c, ta, ta, tb, tb, (float2*)Y, 0, n, nrhs, kc, h.inv_s, inv_t, err, st, KT_GEMM);
+    return launch_h<144, 1>(c, ta, ta, tb, tb, (float2*)Y, 0, n, nrhs, kc, h.inv_s, inv_t, err, st, KT_GEMM);
+}
+
+emfa_status_t hgemm_residual(Ctx* c, const HPlanes& h, const double2* X, const void* B, bool b_is_f32, double2* R,
+                             int nrhs, cudaStream_t st)
+{
+    using S = th::RSmem;
+    const int n = h.n;
+    const size_t ldh = h.ldh;
+    const size_t bplane = Carver::round(sizeof(__half) * ldh * 2 * (size_t)nrhs);
+    void* wp = nullptr;
+    EMFA_TRY(ctx_workspace(c, WS_HGEMM, 2 * bplane + Carver::round(sizeof(float) * nrhs) + 256, &wp));
+    Carver cv{(char*)wp};
+    __half* bh = cv.take<__half>(ldh * 2 * (size_t)nrhs);
+    __half* bl = cv.take<__half>(ldh * 2 * (size_t)nrhs);
+    float* inv_t = cv.take<float>(nrhs);
+    int* err = nullptr;
+    EMFA_TRY(herr(c, &err));
+    th::k_hpack_f64<<<nrhs, 256, 0, st>>>(X, n, ldh, bh, bl, inv_t);
+    c->kernel_launches += 1;
+    CUtensorMap a0, a1, b0, b1;
+    EMFA_TRY(make_map_h(c, &a0, h.zh, 2 * (uint64_t)n, (uint64_t)n, ldh, th::BM));
+    EMFA_TRY(make_map_h(c, &a1, h.zl, 2 * (uint64_t)n, (uint64_t)n, ldh, th::BM));
+    EMFA_TRY(make_map_h(c, &b0, bh, 2 * (uint64_t)n, 2 * (uint64_t)nrhs, ldh, th::RBN));
+    EMFA_TRY(make_map_h(c, &b1, bl, 2 * (uint64_t)n, 2 * (uint64_t)nrhs, ldh, th::RBN));
+    static std::atomic<unsigned long long> attr_set{0};
+    const unsigned long long bit = 1ull << (c->device & 63);
+    if (!(attr_set.load() & bit)) {
+        EMFA_CUDA(c, cudaFuncSetAttribute(th::k_hresid, cudaFuncAttributeMaxDynamicSharedMemorySize, S::TOTAL));
+        attr_set.fetch_or(bit);
+    }
+    dim3 grd((2 * nrhs + th::RBN - 1) / th::RBN, (n + th::BM - 1) / th::BM);
+    const int kblocks = (2 * n + th::BKH - 1) / th::BKH;
+    {
+        TimedLaunch tl(c, KT_RESIDUAL, st, 8.0 * n * (double)n * nrhs);
+        th::k_hresid<<<grd, th::RTHREADS, S::TOTAL, st>>>(a0, a1, b0, b1, B, b_is_f32 ? 0 : 1, R, n, nrhs, kblocks,
+                                                          h.inv_s, inv_t, err);
+    }
+    c->kernel_launches += 1;
+    EMFA_CUDA(c, cudaGetLastError());
+    return EMFA_OK;
+}
+
+emfa_status_t hgemm_check_error(Ctx* c, cudaStream_t st)
+{
+    int* err = nullptr;
+    EMFA_TRY(herr(c, &err));
+    int h = 0;
+    EMFA_CUDA(c, cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    EMFA_CUDA(c, cudaStreamSynchronize(st));
+    if (h) {
+        set_error(c, "split-FP16 tensor-core product: a pipeline wait timed out (stage " + std::to_string(h) + ")");
+        return EMFA_ERR_TIMEOUT;
+    }
+    return EMFA_OK;
+}
+
+}  // namespace emfa

@@ -23,6 +23,7 @@
 // and returns, and the host reports EMFA_ERR_TIMEOUT.
 #include "emfa_internal.cuh"
 #include "gemm.cuh"
+#include "tcgen05.cuh"
 
 #include <cuda.h>
 #include <cudaTypedefs.h>
@@ -35,99 +36,6 @@ constexpr int BM = 128;
 constexpr int BK = 32;          // fp32 elements per stage row = 128 bytes = one swizzle atom
 constexpr int STAGES = 6;
 constexpr int THREADS = 192;
-constexpr long long WAIT_CYCLES = 4000000000LL;  // ~2 s at 2 GHz
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
-{
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes)
-{
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
-{
-    uint32_t ok;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-
-// bounded wait; on timeout records `code` in *err and returns false
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err, int code)
-{
-    if (mbar_try_wait(bar, parity)) return true;
-    long long t0 = clock64();
-    while (!mbar_try_wait(bar, parity)) {
-        if (clock64() - t0 > WAIT_CYCLES) {
-            atomicCAS(err, 0, code);
-            return false;
-        }
-    }
-    return true;
-}
-
-__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y)
-{
-    asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];"
-        ::"r"(smem_u32(dst)), "l"((uint64_t)map), "r"(smem_u32(bar)), "r"(x), "r"(y)
-        : "memory");
-}
-
-// Shared-memory matrix descriptor: K-major tile, 128-byte swizzle, rows of
-// 128 bytes, 8-row core groups 1024 bytes apart.
-__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr)
-{
-    uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFF);
-    d |= (uint64_t)1 << 16;              // leading byte offset (unused for swizzled K-major)
-    d |= (uint64_t)(1024 >> 4) << 32;    // stride byte offset: next 8-row group
-    d |= (uint64_t)1 << 46;              // descriptor version
-    d |= (uint64_t)2 << 61;              // swizzle: 128 B
-    return d;
-}
-
-// Instruction descriptor, kind::tf32: D f32, A/B tf32, both K-major, M x N.
-__host__ __device__ constexpr uint32_t idesc_tf32(int m, int n)
-{
-    return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
-}
-
-__device__ __forceinline__ void mma_tf32(uint32_t tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accum)
-{
-    asm volatile(
-        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-        " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n"
-        ::"r"(tmem), "l"(a), "l"(b), "r"(idesc), "r"(accum)
-        : "memory");
-}
-
-__device__ __forceinline__ void mma_commit(uint64_t* bar)
-{
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
-                 : "memory");
-}
-
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v)
-{
-    uint32_t r[16];
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-        : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
-}
-
 template <int BN>
 struct Smem {
     static constexpr int A_BYTES = BM * BK * 4;
@@ -259,7 +167,7 @@ __global__ void k_pack_b(const float2* __restrict__ X, int n, int nrhs, float2* 
 
 }  // namespace tc
 
-static PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
 {
     static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
     if (!fn) {
@@ -278,7 +186,7 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
 static emfa_status_t make_map(Ctx* c, CUtensorMap* m, const void* ptr, uint64_t inner, uint64_t rows,
                               uint64_t stride_bytes, uint32_t box_rows)
 {
-    auto fn = encode_fn();
+    auto fn = tensor_map_encoder();
     if (!fn) {
         set_error(c, "cuTensorMapEncodeTiled unavailable");
         return EMFA_ERR_CUDA;
@@ -310,7 +218,7 @@ static emfa_status_t launch_tc(Ctx* c, const CUtensorMap& ta, const CUtensorMap&
     dim3 grd((2 * nrhs + BN - 1) / BN, (n + tc::BM - 1) / tc::BM);
     int kblocks = (2 * n + tc::BK - 1) / tc::BK;
     {
-        TimedLaunch tl(c, KT_GEMM_TF32, st, 8.0 * n * (double)n * nrhs);
+        TimedLaunch tl(c, KT_GEMM, st, 8.0 * n * (double)n * nrhs);
         tc::k_gemm_tf32<BN><<<grd, tc::THREADS, S::TOTAL, st>>>(ta, tb, Y, n, nrhs, kblocks, err);
     }
     c->kernel_launches += 1;

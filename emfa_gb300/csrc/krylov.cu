@@ -1069,21 +1069,30 @@ emfa_status_t solve_op(Ctx* c, LinOp& A, const void* B, int nrhs, void* X, const
 }
 
 // Dense impedance matrix as a Krylov operator.  Mixed path: inner products
-// on the tensor cores (TF32) or FP32 CUDA cores, refinement residual with
-// FP32 products and FP64 chunk sums.  Plain path: FP64 throughout.
+// on the tensor cores (split FP16 or TF32) or FP32 CUDA cores; refinement
+// residual from the three-term split-FP16 product (F16X) or FP32 products
+// with FP64 chunk sums.  Plain path: FP64 throughout.
 struct DenseOp : LinOp {
+    enum Mode { SIMT = 0, TF32 = 1, F16X = 2 };
     const void* Z = nullptr;
-    bool use_tc = false;
+    int mode = SIMT;
+    HPlanes hp;  // F16X: planes of Z, split by prepare()
+    emfa_status_t prepare(Ctx* c, cudaStream_t st)
+    {
+        return mode == F16X ? hsplit_prepare(c, Z, n, n, &hp, st) : EMFA_OK;
+    }
     emfa_status_t apply(Ctx* c, const void* X, void* Y, int nrhs, cudaStream_t st) override
     {
         if (prec == EMFA_F64) return cgemm_f64(c, Z, n, X, n, nrhs, Y, st);
-        if (use_tc) return cgemm_tf32(c, Z, n, X, n, nrhs, Y, st);
+        if (mode == F16X) return hgemm_apply(c, hp, X, Y, nrhs, st);
+        if (mode == TF32) return cgemm_tf32(c, Z, n, X, n, nrhs, Y, st);
         return cgemm_f32(c, Z, n, X, n, nrhs, Y, st);
     }
     emfa_status_t residual(Ctx* c, const double2* X, const void* B, double2* R, int nrhs, float2* xt,
                            cudaStream_t st) override
     {
         const size_t vec = (size_t)n * nrhs;
+        if (prec == EMFA_F32 && mode == F16X) return hgemm_residual(c, hp, X, B, true, R, nrhs, st);
         if (prec == EMFA_F64) {
             EMFA_TRY(cgemm_f64(c, Z, n, X, n, nrhs, R, st));  // R = Z X
             k_residual<double2><<<grid1(vec), 256, 0, st>>>((const double2*)B, R, R, vec);
@@ -1094,8 +1103,21 @@ struct DenseOp : LinOp {
         c->kernel_launches += 1;
         return cgemm_f32_chunked(c, Z, n, xt, n, nrhs, B, R, st);  // R = B - Z X
     }
-    emfa_status_t check(Ctx* c, cudaStream_t st) override { return use_tc ? gemm_check_error(c, st) : EMFA_OK; }
+    emfa_status_t check(Ctx* c, cudaStream_t st) override
+    {
+        if (mode == F16X) return hgemm_check_error(c, st);
+        return mode == TF32 ? gemm_check_error(c, st) : EMFA_OK;
+    }
 };
+
+// matvec mode of the dense operator; TF32 needs even n and a 16-byte aligned Z
+static int dense_mode(int prec, int matvec, const void* Z, int n)
+{
+    if (prec != EMFA_F32) return DenseOp::SIMT;
+    if (matvec == EMFA_MV_AUTO || matvec == EMFA_MV_F16X) return DenseOp::F16X;
+    if (matvec == EMFA_MV_TF32 && n % 2 == 0 && ((uintptr_t)Z & 15) == 0) return DenseOp::TF32;
+    return DenseOp::SIMT;
+}
 
 emfa_status_t solve_dense(Ctx* c, int prec, const void* Z, int n, const void* B, int nrhs, void* X,
                           const emfa_solver_params_t* sp, emfa_solve_info_t* info, cudaStream_t st)
@@ -1104,8 +1126,8 @@ emfa_status_t solve_dense(Ctx* c, int prec, const void* Z, int n, const void* B,
     A.n = n;
     A.prec = prec;
     A.Z = Z;
-    A.use_tc = prec == EMFA_F32 && (sp->matvec == EMFA_MV_AUTO || sp->matvec == EMFA_MV_TF32) && (n % 2 == 0) &&
-               (((uintptr_t)Z & 15) == 0);
+    A.mode = dense_mode(prec, sp->matvec, Z, n);
+    EMFA_TRY(A.prepare(c, st));
     return solve_op(c, A, B, nrhs, X, sp, info, st);
 }
 }  // namespace emfa
@@ -1132,7 +1154,37 @@ emfa_status_t emfa_matvec(emfa_ctx_t* ctx, int prec, int matvec, const void* Z_d
         EMFA_TRY(cgemm_tf32(ctx, Z_dev, n, X_dev, n, n_rhs, Y_dev, st));
         return gemm_check_error(ctx, st);
     }
+    if (matvec == EMFA_MV_F16X) {
+        HPlanes hp;
+        EMFA_TRY(hsplit_prepare(ctx, Z_dev, n, n, &hp, st));
+        EMFA_TRY(hgemm_apply(ctx, hp, X_dev, Y_dev, n_rhs, st));
+        return hgemm_check_error(ctx, st);
+    }
     return cgemm_f32(ctx, Z_dev, n, X_dev, n, n_rhs, Y_dev, st);
+}
+
+emfa_status_t emfa_residual(emfa_ctx_t* ctx, int prec, int matvec, const void* Z_dev, int n, const void* X_dev,
+                            const void* B_dev, int n_rhs, void* R_dev, void* stream)
+{
+    if (!ctx || !Z_dev || !X_dev || !B_dev || !R_dev || n <= 0 || n_rhs <= 0 || n_rhs > 65535 ||
+        (prec != EMFA_F32 && prec != EMFA_F64) || matvec < EMFA_MV_AUTO || matvec > EMFA_MV_F16X) {
+        set_error(ctx, "emfa_residual: bad arguments");
+        return EMFA_ERR_INVALID;
+    }
+    EMFA_CUDA(ctx, cudaSetDevice(ctx->device));
+    cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+    DenseOp A;
+    A.n = n;
+    A.prec = prec;
+    A.Z = Z_dev;
+    A.mode = dense_mode(prec, matvec, Z_dev, n);
+    EMFA_TRY(A.prepare(ctx, st));
+    DevBuf xt;
+    if (A.mode != DenseOp::F16X) EMFA_TRY(xt.alloc(ctx, sizeof(float2) * (size_t)n * n_rhs));
+    EMFA_TRY(A.residual(ctx, (const double2*)X_dev, B_dev, (double2*)R_dev, n_rhs, dptr<float2>(xt), st));
+    EMFA_TRY(A.check(ctx, st));
+    EMFA_CUDA(ctx, cudaStreamSynchronize(st));
+    return EMFA_OK;
 }
 
 emfa_status_t emfa_solve(emfa_ctx_t* ctx, int prec, const void* Z_dev, int n, const void* B_dev, int n_rhs,

@@ -41,10 +41,16 @@ typedef enum { EMFA_F32 = 0, EMFA_F64 = 1 } emfa_precision_t;
 typedef enum { EMFA_EFIE = 0, EMFA_CFIE = 1 } emfa_kind_t;
 typedef enum { EMFA_GMRES = 0, EMFA_BICGSTAB = 1 } emfa_method_t;
 typedef enum {
-    EMFA_MV_AUTO = 0,  /* F64: FP64 SIMT; F32: tensor-core TF32 inner, FP32 residual */
+    EMFA_MV_AUTO = 0,  /* F64: FP64 SIMT; F32: EMFA_MV_F16X                          */
     EMFA_MV_F64 = 1,   /* FP64 complex GEMM on CUDA cores (plain path)               */
-    EMFA_MV_F32 = 2,   /* FP32 complex GEMM on CUDA cores                             */
-    EMFA_MV_TF32 = 3   /* tcgen05 TF32 complex GEMM, FP32 accumulation               */
+    EMFA_MV_F32 = 2,   /* FP32 complex GEMM on CUDA cores; residual FP32 products    */
+                       /* with FP64 chunk sums                                       */
+    EMFA_MV_TF32 = 3,  /* tcgen05 TF32 complex GEMM, FP32 accumulation; residual as  */
+                       /* EMFA_MV_F32                                                */
+    EMFA_MV_F16X = 4   /* tcgen05 split FP16: Z = (Zh + Zl)/s once per solve; inner  */
+                       /* product Zh x at the FP16 rate (TF32 accuracy); residual    */
+                       /* Zh xh + Zh xl + Zl xh per 64-column block, compensated     */
+                       /* FP32 sums across blocks, B - Z x formed in FP64            */
 } emfa_matvec_t;
 
 typedef struct emfa_ctx emfa_ctx_t;
@@ -113,7 +119,7 @@ emfa_status_t emfa_ctx_stream(const emfa_ctx_t* ctx, void** stream);
  * complex product), Z entries for the fill. */
 typedef enum {
     EMFA_KT_FILL_Z = 0,    /* impedance fill (EFIE/CFIE)                       */
-    EMFA_KT_GEMM_TF32 = 1, /* tensor-core multi-RHS product of the solvers     */
+    EMFA_KT_GEMM = 1,      /* tensor-core inner product of the solvers        */
     EMFA_KT_RESIDUAL = 2   /* accurate refinement residual b - Z x             */
 } emfa_kernel_timer_t;
 emfa_status_t emfa_ctx_set_kernel_timing(emfa_ctx_t* ctx, int on);
@@ -194,6 +200,14 @@ emfa_status_t emfa_matvec(emfa_ctx_t* ctx, int prec, int matvec, const void* Z_d
  * Errors are reported through emfa_last_error(NULL). */
 emfa_status_t emfa_matvec_tf32_noalloc(const void* Z_dev, int n, const void* X_dev, int n_rhs, void* Y_dev,
                                        void* stream);
+
+/* R = B - Z X, the accurate residual of mixed-precision iterative refinement,
+ * with the residual product of the given matvec mode (EMFA_F32: Z complex64,
+ * B complex64; EMFA_F64: Z and B complex128; X and R always complex128,
+ * n_rhs x n).  Replaces the residual `r = b - A * x` of iml::BICGSTAB and
+ * iml::GMRES (EMIterative/iml.cpp:8,173). */
+emfa_status_t emfa_residual(emfa_ctx_t* ctx, int prec, int matvec, const void* Z_dev, int n, const void* X_dev,
+                            const void* B_dev, int n_rhs, void* R_dev, void* stream);
 
 /* Solves Z X = B for n_rhs right-hand sides (B complex64 for EMFA_F32,
  * complex128 for EMFA_F64; X always complex128, n_rhs x n).  GMRES(m) or

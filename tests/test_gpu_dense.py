@@ -226,3 +226,52 @@ def test_matvec_tf32_tensor_cores(ctx, n, r):
     assert err < 3e-3, err
     # every column must be populated (no tile or RHS skipped)
     assert np.all(np.abs(Y).max(axis=1) > 0)
+
+
+@pytest.mark.parametrize("n,r", [(128, 4), (256, 32), (998, 37), (999, 5), (1920, 360)])
+def test_matvec_split_fp16_tensor_cores(ctx, n, r):
+    """Split-FP16 inner product (tcgen05 kind::f16): Zh times an FP16 copy of
+    X scaled per right-hand side, 11-bit significands on both sides, so the
+    normwise error is that of a TF32 product (~1e-3 of |Z||X|); odd orders
+    are allowed (the planes have padded rows)."""
+    import torch
+    from emfa_gb300 import api
+    rng = np.random.default_rng(n + r + 1)
+    Zn = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+    Xn = rng.standard_normal((r, n)) + 1j * rng.standard_normal((r, n))
+    # right-hand sides of very different magnitudes: each gets its own scale
+    Xn *= (10.0 ** rng.uniform(-6, 6, size=(r, 1)))
+    Z = torch.tensor(Zn * 1e3, dtype=torch.complex64, device="cuda")
+    X = torch.tensor(Xn, dtype=torch.complex64, device="cuda")
+    Y = api.matvec(ctx, Z, X, "f16x").cpu().numpy()
+    ref = (Z.cpu().numpy().astype(np.complex128) @ X.cpu().numpy().astype(np.complex128).T).T
+    err = np.linalg.norm(Y - ref, axis=1) / np.linalg.norm(ref, axis=1)
+    assert err.max() < 2e-3, err.max()
+
+
+@pytest.mark.parametrize("n,r", [(1922, 24), (1001, 3)])
+def test_residual_split_fp16(ctx, n, r):
+    """Refinement residual R = B - Z X from Zh Xh + Zh Xl + Zl Xh (a fresh
+    tensor-memory accumulator per 64-column block, compensated FP32 sums
+    across blocks, B - Z X in FP64) against the FP64 residual of the same FP32
+    matrix: error below 1e-6 of ||B|| for every right-hand side (the
+    refinement stops at 1e-6), and no worse than the FP32-product residual of
+    the CUDA-core path by more than 2x."""
+    import torch
+    from emfa_gb300 import api
+    rng = np.random.default_rng(7 + n)
+    Zc = ((rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))) * 50).astype(np.complex64)
+    Xc = (rng.standard_normal((r, n)) + 1j * rng.standard_normal((r, n))) * (10.0 ** rng.uniform(-3, 3, (r, 1)))
+    exact = np.ascontiguousarray((Zc.astype(np.complex128) @ Xc.T).T)
+    Bc = exact.astype(np.complex64)  # a consistent right-hand side: R is the FP32 rounding of B
+    Rx = Bc.astype(np.complex128) - exact
+    Z = torch.tensor(Zc, device="cuda")
+    X = torch.tensor(Xc, dtype=torch.complex128, device="cuda")
+    B = torch.tensor(Bc, device="cuda")
+    R = api.residual(ctx, Z, X, B, "f16x").cpu().numpy()
+    Rs = api.residual(ctx, Z, X, B, "f32").cpu().numpy()
+    bn = np.linalg.norm(Bc.astype(np.complex128), axis=1)
+    err = np.linalg.norm(R - Rx, axis=1) / bn
+    err_simt = np.linalg.norm(Rs - Rx, axis=1) / bn
+    assert err.max() < 1e-6, (err.max(), err_simt.max())
+    assert err.max() <= 2 * err_simt.max() + 1e-8, (err.max(), err_simt.max())
