@@ -210,9 +210,9 @@ def measured_peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
 
 
-# DRAM bytes (read + write) per launch of the TF32 product on the 7680 x 360
-# job, from one ncu capture (profiles/k_gemm_tf32_c2_7680x360.md).
-GEMM_TRAFFIC_BYTES = None
+# DRAM bytes (read + write) per launch of the split-FP16 inner product on the
+# 7680 x 360 job, from one ncu capture (profiles/k_hgemm_k_hresid_7680x360.md).
+GEMM_TRAFFIC_BYTES = 298.3e6
 
 
 _ARGS = {}
@@ -220,6 +220,13 @@ _ARGS = {}
 
 def args_matvec():
     return _ARGS.get("matvec", "auto")
+
+
+def algorithmic_gemm_bytes(res):
+    """hi plane of Z (2 bytes x n x 2n) + packed FP16 B (2 x R rows of 2n
+    halves) + complex64 output."""
+    n, r = res["n"], res["n_inc"]
+    return 2 * n * 2 * n + 2 * (2 * r) * (2 * n) + 8 * n * r
 
 
 def roofline(res):
@@ -234,7 +241,9 @@ def roofline(res):
     peak = peaks["bf16_tflops_sustained"]
     return {"kernel": "th::k_hgemm<144,1>" if args_matvec() in ("auto", "f16x") else "tc::k_gemm_tf32",
             "bound": "tensor", "achieved": round(achieved, 2), "peak": peak,
-            "unit": "TFLOP/s", "frac": round(achieved / peak, 4), "traffic": GEMM_TRAFFIC_BYTES,
+            "unit": "TFLOP/s", "frac": round(achieved / peak, 4),
+            "traffic": GEMM_TRAFFIC_BYTES if args_matvec() in ("auto", "f16x") else None,
+            "algorithmic_bytes_per_launch": algorithmic_gemm_bytes(res),
             "peak_source": "%s bf16 dense, sustained (kernel timed inside a long step)" % src,
             "operand": "fp16 (hi plane of Z) x fp16, fp32 accumulate" if args_matvec() in ("auto", "f16x")
             else "tf32 (nominal tf32 dense rate = 1/2 bf16)", "launches": n_l,
@@ -252,27 +261,37 @@ def kernel_table(res):
 
 
 def run_gemm_only(args):
-    """Micro-benchmark of the multi-RHS product alone (the inner product of the
-    solver): Z (N x N complex64, random) times 360 vectors.  Used to profile
-    the tensor-core kernel in isolation."""
+    """Micro-benchmark of the multi-RHS products alone: the inner product of
+    the solver and (split FP16) the refinement residual, Z (N x N complex64,
+    random) times R vectors, kernel time from the context's event timers.
+    Used to profile the tensor-core kernels in isolation."""
     import torch
     from emfa_gb300 import api, build
     build.build()
     n, r = args.gemm_n, args.gemm_r
+    mv = args.matvec if args.matvec != "auto" else "f16x"
     ctx = api.Context(0)
     g = torch.Generator(device="cuda").manual_seed(1)
     Z = torch.randn((n, n), dtype=torch.complex64, device="cuda", generator=g)
     X = torch.randn((r, n), dtype=torch.complex64, device="cuda", generator=g)
-    for _ in range(args.warmup):
-        api.matvec(ctx, Z, X, args.matvec if args.matvec != "auto" else "tf32")
+    Xd = X.to(torch.complex128)
+    resid = mv in ("f16x", "f32")
+    for i in range(args.warmup + args.steps):
+        if i == args.warmup:
+            ctx.kernel_timing(True)
+        api.matvec(ctx, Z, X, mv)
+        if resid:
+            api.residual(ctx, Z, Xd, X, mv)
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        api.matvec(ctx, Z, X, args.matvec if args.matvec != "auto" else "tf32")
-    torch.cuda.synchronize()
-    dt = (time.perf_counter() - t0) / max(1, args.steps)
     flops = 8.0 * n * n * r
-    print(json.dumps({"mode": "gemm", "n": n, "r": r, "ms": dt * 1e3, "tflops": flops / dt / 1e12}))
+    out = {"mode": "gemm", "matvec": mv, "n": n, "r": r}
+    for k in ("gemm", "residual"):
+        n_l, ms, _ = ctx.kernel_time(k)
+        if n_l:
+            out[k + "_ms"] = round(ms / n_l, 5)
+            out[k + "_tflops"] = round(flops / (ms / n_l * 1e-3) / 1e12, 2)
+    ctx.kernel_timing(False)
+    print(json.dumps(out))
 
 
 def run_mlfma(args):
