@@ -109,7 +109,7 @@ def run_emfa(args, workload):
     ang = incidences(n_inc)
     dirs = api.monostatic_dirs(ang)
     fp = api.fill_params("cfie", "f32", freq, alpha)
-    sp = api.solver_params("gmres", restart=30, max_iter=900, tol=1e-6, matvec=args.matvec)
+    sp = api.solver_params("gmres", restart=30, max_iter=900, tol=1e-6, matvec=args.matvec, orth=args.orth)
     stream = torch.cuda.ExternalStream(ctx.stream_ptr())
     Z = torch.empty((n, n), dtype=torch.complex64, device="cuda")
     V = torch.empty((n_inc, n), dtype=torch.complex64, device="cuda")
@@ -343,6 +343,7 @@ def main():
     ap.add_argument("--workload", default="c2_cfie_sphere_7680x360", choices=list(WORKLOADS))
     ap.add_argument("--matvec", default="auto", choices=["auto", "f32", "tf32", "f16x"])
     ap.add_argument("--check", type=int, default=1)
+    ap.add_argument("--orth", default="auto", choices=["auto", "cgs1", "cgs2"])
     ap.add_argument("--cpu-baseline", type=int, default=1)
     ap.add_argument("--mode", default="job", choices=["job", "gemm", "mlfma"])
     ap.add_argument("--mlfma-subdiv", type=int, default=6)

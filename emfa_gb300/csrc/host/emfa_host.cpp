@@ -429,7 +429,7 @@ void EFIE::solve()
     double ang[3] = {incidence_.theta, incidence_.phi, incidence_.pole};
     check(emfa_fill_v(ctx_, geom_, &fp, ang, 1, V_, nullptr), ctx_, "fillV");
     timeLog("fillV");
-    emfa_solver_params_t sp{EMFA_GMRES, 30, 100000, tol_, 1, EMFA_MV_AUTO, 0};
+    emfa_solver_params_t sp{EMFA_GMRES, 30, 100000, tol_, 1, EMFA_MV_AUTO, 0, 0};
     emfa_solve_info_t info{};
     emfa_status_t s = emfa_solve(ctx_, precision_, Z_, (int)n, V_, 1, I_, &sp, &info, nullptr);
     if (s == EMFA_ERR_NOT_CONVERGED)
@@ -481,7 +481,7 @@ void CFIE::solve()
     double ang[3] = {incidence_.theta, incidence_.phi, incidence_.pole};
     check(emfa_fill_v(ctx_, geom_, &fp, ang, 1, V_, nullptr), ctx_, "fillV");
     timeLog("fillV");
-    emfa_solver_params_t sp{EMFA_BICGSTAB, 30, 500, 0.01, 0, EMFA_MV_AUTO, 0};
+    emfa_solver_params_t sp{EMFA_BICGSTAB, 30, 500, 0.01, 0, EMFA_MV_AUTO, 0, 0};
     emfa_solve_info_t info{};
     emfa_status_t s = emfa_solve(ctx_, precision_, Z_, (int)n, V_, 1, I_, &sp, &info, nullptr);
     if (s == EMFA_ERR_NOT_CONVERGED)
@@ -548,7 +548,7 @@ void MLFMA::solve()
     double ang[3] = {incidence_.theta, incidence_.phi, incidence_.pole};
     check(emfa_mlfma_fill_v(ml_, ang, 1, V_, nullptr), ctx_, "fillVbyBox");
     timeLog("fillVbyBox");
-    emfa_solver_params_t sp{EMFA_BICGSTAB, 30, max_iter_, tol_, 0, EMFA_MV_AUTO, 0};
+    emfa_solver_params_t sp{EMFA_BICGSTAB, 30, max_iter_, tol_, 0, EMFA_MV_AUTO, 0, 0};
     emfa_solve_info_t info{};
     emfa_status_t s = emfa_mlfma_solve(ml_, V_, 1, Ibox_, &sp, &info, nullptr);
     if (s == EMFA_ERR_NOT_CONVERGED)

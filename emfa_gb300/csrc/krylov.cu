@@ -421,7 +421,7 @@ __global__ void k_update_x2(const Cx<T>* __restrict__ V, size_t vstride, int nvm
 }
 
 // per-RHS: finish Arnoldi column j, rotate, test convergence
-__global__ void k_arnoldi_finish(GmresDev s, int j, const double2* __restrict__ pnorm, int nblk)
+__global__ void k_arnoldi_finish(GmresDev s, int j, const double2* __restrict__ pnorm, int nblk, int two_pass)
 {
     int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= s.nrhs) return;
@@ -434,10 +434,15 @@ __global__ void k_arnoldi_finish(GmresDev s, int j, const double2* __restrict__ 
     for (int b = 0; b < nblk; ++b) nr2 += pnorm[(size_t)r * nblk + b].x;
     double beta = sqrt(nr2);
     double2* H = s.H + (size_t)r * (m + 1) * m;
-    // column j of H: CGS2 coefficients
+    // column j of H: Gram-Schmidt coefficients (sum of both passes for CGS2)
     for (int i = 0; i <= j; ++i) {
-        double2 a = s.hcol[(size_t)i * s.nrhs + r], b = s.y[(size_t)i * s.nrhs + r];
-        H[i * m + j] = make_double2(a.x + b.x, a.y + b.y);
+        double2 a = s.hcol[(size_t)i * s.nrhs + r];
+        if (two_pass) {
+            const double2 b = s.y[(size_t)i * s.nrhs + r];
+            a.x += b.x;
+            a.y += b.y;
+        }
+        H[i * m + j] = a;
     }
     H[(j + 1) * m + j] = make_double2(beta, 0.0);
     double* cs = s.cs + (size_t)r * m;
@@ -689,6 +694,9 @@ static emfa_status_t gmres_t(Ctx* c, LinOp& A, const void* B, int nrhs, double2*
     EMFA_CUDA(c, cudaMemsetAsync(X, 0, sizeof(double2) * vec, st));
     int max_cycles = sp->max_iter > 0 ? (sp->max_iter + m - 1) / m : 100;
     if (prec == EMFA_F32 && sp->max_refine > 0) max_cycles = std::min(max_cycles, sp->max_refine);
+    // the FP32 inner solve of the refinement only has to gain a few digits per
+    // cycle: one Gram-Schmidt pass; the plain FP64 path keeps two
+    const bool two_pass = sp->orth == 2 || (sp->orth == 0 && prec == EMFA_F64);
     int total_iters = 0, cycles = 0, converged = 0;
     int host_cnt[4];
     for (int cyc = 0; cyc < max_cycles; ++cyc) {
@@ -717,22 +725,28 @@ static emfa_status_t gmres_t(Ctx* c, LinOp& A, const void* B, int nrhs, double2*
             Cx<T>* Vj = V + (size_t)j * vec;
             // W = A V_j
             EMFA_TRY(A.apply(c, Vj, W, nrhs, st));
-            // CGS2: h1 = V^H W; W -= V h1; h2 = V^H W; W -= V h2 with |W|^2
+            // CGS1: h = V^H W; W -= V h with |W|^2.  CGS2 repeats the pair
+            // (h2 = V^H W; W -= V h2) and H gets h + h2.
             const dim3 vg(vblk, nrhs);
             const int nv = j + 1;
             const int rg = (nv * nrhs + 127) / 128;
             k_vdots<T><<<vg, 256, 0, st>>>(V, vec, nv, W, n, nrhs, vblk, partial);
             k_reduce_partials<<<rg, 128, 0, st>>>(partial, nv, nrhs, vblk, s.hcol, 0);
-            k_vupdate<T, false><<<vg, 256, 0, st>>>(V, vec, nv, s.hcol, W, n, nrhs, vblk, pnorm);
-            k_vdots<T><<<vg, 256, 0, st>>>(V, vec, nv, W, n, nrhs, vblk, partial);
-            k_reduce_partials<<<rg, 128, 0, st>>>(partial, nv, nrhs, vblk, s.y, 0);
-            k_vupdate<T, true><<<vg, 256, 0, st>>>(V, vec, nv, s.y, W, n, nrhs, vblk, pnorm);
+            if (two_pass) {
+                k_vupdate<T, false><<<vg, 256, 0, st>>>(V, vec, nv, s.hcol, W, n, nrhs, vblk, pnorm);
+                k_vdots<T><<<vg, 256, 0, st>>>(V, vec, nv, W, n, nrhs, vblk, partial);
+                k_reduce_partials<<<rg, 128, 0, st>>>(partial, nv, nrhs, vblk, s.y, 0);
+                k_vupdate<T, true><<<vg, 256, 0, st>>>(V, vec, nv, s.y, W, n, nrhs, vblk, pnorm);
+                c->kernel_launches += 3;
+            } else {
+                k_vupdate<T, true><<<vg, 256, 0, st>>>(V, vec, nv, s.hcol, W, n, nrhs, vblk, pnorm);
+            }
             EMFA_CUDA(c, cudaMemsetAsync(s.counters, 0, sizeof(int), st));
-            k_arnoldi_finish<<<(nrhs + 127) / 128, 128, 0, st>>>(s, j, pnorm, vblk);
+            k_arnoldi_finish<<<(nrhs + 127) / 128, 128, 0, st>>>(s, j, pnorm, vblk, two_pass ? 1 : 0);
             k_scale_store<Cx<T>, Cx<T>><<<grid1(vec), 256, 0, st>>>(W, s.scale, n, nrhs, V + (size_t)(j + 1) * vec);
             EMFA_CUDA(c, cudaMemcpyAsync(host_cnt, s.counters, sizeof(int), cudaMemcpyDeviceToHost, st));
             EMFA_CUDA(c, cudaStreamSynchronize(st));
-            c->kernel_launches += 8;
+            c->kernel_launches += 5;
             ++steps;
             if (host_cnt[0] == 0) break;
         }

@@ -81,6 +81,9 @@ typedef struct {
     int tol_absolute;   /* 1: ||b - Z x|| < tol, the reference GMRES criterion      */
     int matvec;         /* emfa_matvec_t                                            */
     int max_refine;     /* outer true-residual cycles for EMFA_F32 (GMRES-IR)       */
+    int orth;           /* GMRES Gram-Schmidt: 0 = auto (CGS1 for the EMFA_F32     */
+                        /* inner solve of the refinement, CGS2 for EMFA_F64),      */
+                        /* 1 = CGS1, 2 = CGS2                                      */
 } emfa_solver_params_t;
 
 typedef struct {
