@@ -211,8 +211,9 @@ def measured_peaks():
 
 
 # DRAM bytes (read + write) per launch of the split-FP16 inner product on the
-# 7680 x 360 job, from one ncu capture (profiles/k_hgemm_k_hresid_7680x360.md).
-GEMM_TRAFFIC_BYTES = 298.3e6
+# 7680 x 360 job, from one ncu capture (profiles/k_hgemm_k_hresid_7680x360.md);
+# None until the 256-row-tile kernel is captured.
+GEMM_TRAFFIC_BYTES = None
 
 
 _ARGS = {}
@@ -239,7 +240,9 @@ def roofline(res):
         return None
     achieved = flops / (ms * 1e-3) / 1e12
     peak = peaks["bf16_tflops_sustained"]
-    return {"kernel": "th::k_hgemm<144,1>" if args_matvec() in ("auto", "f16x") else "tc::k_gemm_tf32",
+    tall = 5 * ((res["n"] + 255) // 256) >= 137  # 256-row tiles fill the 152 SMs
+    return {"kernel": ("th::k_hgemm<144,2>" if tall else "th::k_hgemm<144,1>") if args_matvec() in ("auto", "f16x")
+            else "tc::k_gemm_tf32",
             "bound": "tensor", "achieved": round(achieved, 2), "peak": peak,
             "unit": "TFLOP/s", "frac": round(achieved / peak, 4),
             "traffic": GEMM_TRAFFIC_BYTES if args_matvec() in ("auto", "f16x") else None,

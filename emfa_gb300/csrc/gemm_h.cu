@@ -17,12 +17,12 @@
 //       k_hresid: a fresh accumulator per k-block, drained into compensated
 //       FP32 sums in registers (see the kernel's comment)
 //
-// Kernel k_hgemm<BN, NP>: one 128 x BN output tile per CTA, 6 warps:
-//   warp 0      TMA producer: NP planes of A (128 x 64 halves) and of B
-//               (BN x 64 halves), 128-byte swizzle, multi-stage ring
-//   warp 1      allocates tensor memory (two accumulators); one lane issues
-//               tcgen05.mma (M = 128, N = BN, K = 16): 4 per stage and plane
-//               pair, commits each stage free and each chunk's accumulator full
+// Kernel k_hgemm<BN, MS>: one (128 MS) x BN output tile per CTA, 6 warps:
+//   warp 0      TMA producer: MS blocks of A (128 x 64 halves each) and one
+//               B tile (BN x 64 halves), 128-byte swizzle, multi-stage ring
+//   warp 1      allocates tensor memory (one accumulator per row block); one
+//               lane issues tcgen05.mma (M = 128, N = BN, K = 16): 4 per stage
+//               and row block, and commits each stage free
 //   warps 2..5  epilogue: tcgen05.ld 32 lanes x 16 columns, scaled complex64
 //               stores (consecutive lanes = consecutive rows: coalesced)
 // Every wait is bounded (clock64): on timeout the kernel records a code in
@@ -46,53 +46,49 @@ constexpr int BKH = 64;  // halves per stage row = 128 bytes = one swizzle atom
 constexpr int THREADS = 192;
 constexpr int SMEM_BUDGET = 216 * 1024;
 
-template <int BN, int NP>
+// Inner product: MS row blocks of 128 (M = 128 MMAs, one accumulator each)
+// share every B tile, so a 256-row tile reads 26% fewer operand bytes per
+// FLOP than a 128-row one; operand delivery from L2, not the tensor pipe,
+// bounds this skinny product (N = 2R = 720).
+template <int BN, int MS>
 struct Smem {
-    static constexpr int A_BYTES = BM * 128;
+    static constexpr int A_BYTES = BM * 128;  // one 128-row block
     static constexpr int B_BYTES = BN * 128;
-    static constexpr int STAGE_BYTES = NP * (A_BYTES + B_BYTES);
+    static constexpr int STAGE_BYTES = MS * A_BYTES + B_BYTES;
     static constexpr int STAGES = SMEM_BUDGET / STAGE_BYTES > 8 ? 8 : SMEM_BUDGET / STAGE_BYTES;
     static constexpr int ACC = BN <= 32 ? 32 : BN <= 64 ? 64 : BN <= 128 ? 128 : 256;  // columns per accumulator
-    static constexpr int TMEM_COLS = 2 * ACC;
+    static constexpr int TMEM_COLS = MS * ACC < 32 ? 32 : MS * ACC;
     static constexpr int TOTAL = STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
 };
 
-template <int BN, int NP>
+template <int BN, int MS>
 __global__ void __launch_bounds__(THREADS, 1)
-    k_hgemm(const __grid_constant__ CUtensorMap tmA0, const __grid_constant__ CUtensorMap tmA1,
-            const __grid_constant__ CUtensorMap tmB0, const __grid_constant__ CUtensorMap tmB1,
-            float2* __restrict__ Y, size_t pstride, int M, int R, int kblocks, int kc,
-            const float* __restrict__ inv_s, const float* __restrict__ inv_t, int* __restrict__ err)
+    k_hgemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+            float2* __restrict__ Y, int M, int R, int kblocks, const float* __restrict__ inv_s,
+            const float* __restrict__ inv_t, int* __restrict__ err)
 {
-    using S = Smem<BN, NP>;
+    using S = Smem<BN, MS>;
     using namespace tc;
     extern __shared__ uint8_t smem_raw[];
     uint8_t* base = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    uint8_t* sA = base;                                // [stage][plane]
-    uint8_t* sB = base + S::STAGES * NP * S::A_BYTES;  // [stage][plane]
+    uint8_t* sA = base;                               // [stage][row block]
+    uint8_t* sB = base + S::STAGES * MS * S::A_BYTES;  // [stage]
     uint64_t* full = (uint64_t*)(base + S::STAGES * S::STAGE_BYTES);
     uint64_t* empty = full + S::STAGES;
-    uint64_t* acc_full = empty + S::STAGES;
-    uint64_t* acc_empty = acc_full + 2;
-    uint64_t* done = acc_empty + 2;
-    uint32_t* tmem_slot = (uint32_t*)(done + 1);
+    uint64_t* accum = empty + S::STAGES;
+    uint32_t* tmem_slot = (uint32_t*)(accum + 1);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     // grid x = column tiles, y = row tiles: CTAs sharing a row block of the
-    // planes run back to back and reuse it from L2
-    const int f0 = blockIdx.y * BM, c0 = blockIdx.x * BN;
-    const int nchunks = (kblocks + kc - 1) / kc;
+    // hi plane run back to back and reuse it from L2
+    const int f0 = blockIdx.y * (BM * MS), c0 = blockIdx.x * BN;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < S::STAGES; ++s) {
             mbar_init(full + s, 1);
             mbar_init(empty + s, 1);
         }
-        for (int a = 0; a < 2; ++a) {
-            mbar_init(acc_full + a, 1);
-            mbar_init(acc_empty + a, 4);  // one arrival per epilogue warp
-        }
-        mbar_init(done, 1);
+        mbar_init(accum, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     }
@@ -115,12 +111,10 @@ __global__ void __launch_bounds__(THREADS, 1)
                 if (kb >= S::STAGES && !mbar_wait(empty + s, ((kb / S::STAGES) - 1) & 1, err, 1)) break;
                 if (*(volatile int*)err) break;
                 mbar_expect_tx(full + s, S::STAGE_BYTES);
-                tma_load_2d(sA + (s * NP) * S::A_BYTES, &tmA0, full + s, kb * BKH, f0);
-                tma_load_2d(sB + (s * NP) * S::B_BYTES, &tmB0, full + s, kb * BKH, c0);
-                if (NP == 2) {
-                    tma_load_2d(sA + (s * NP + 1) * S::A_BYTES, &tmA1, full + s, kb * BKH, f0);
-                    tma_load_2d(sB + (s * NP + 1) * S::B_BYTES, &tmB1, full + s, kb * BKH, c0);
-                }
+#pragma unroll
+                for (int m = 0; m < MS; ++m)
+                    tma_load_2d(sA + (s * MS + m) * S::A_BYTES, &tmA, full + s, kb * BKH, f0 + m * BM);
+                tma_load_2d(sB + s * S::B_BYTES, &tmB, full + s, kb * BKH, c0);
                 issued = kb + 1;
             }
             // every issued stage's copy must have landed before the CTA exits
@@ -132,67 +126,52 @@ __global__ void __launch_bounds__(THREADS, 1)
             constexpr uint32_t idesc = idesc_f16(BM, BN);
             for (int kb = 0; kb < kblocks; ++kb) {
                 const int s = kb % S::STAGES;
-                const int ch = kb / kc, kin = kb - ch * kc;
-                const uint32_t acc = tmem + (uint32_t)((ch & 1) * S::ACC);
-                // the accumulator is free once the epilogue drained chunk ch - 2
-                if (kin == 0 && ch >= 2) {
-                    if (!mbar_wait(acc_empty + (ch & 1), ((ch >> 1) - 1) & 1, err, 6)) break;
-                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                }
                 if (!mbar_wait(full + s, (kb / S::STAGES) & 1, err, 3)) break;
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                const uint64_t da0 = sw128_desc(smem_u32(sA + (s * NP) * S::A_BYTES));
-                const uint64_t db0 = sw128_desc(smem_u32(sB + (s * NP) * S::B_BYTES));
-                const uint64_t da1 = NP == 2 ? sw128_desc(smem_u32(sA + (s * NP + 1) * S::A_BYTES)) : 0;
-                const uint64_t db1 = NP == 2 ? sw128_desc(smem_u32(sB + (s * NP + 1) * S::B_BYTES)) : 0;
+                const uint64_t db = sw128_desc(smem_u32(sB + s * S::B_BYTES));
 #pragma unroll
-                for (int k = 0; k < BKH / 16; ++k) {  // K = 16 halves = 32 bytes per instruction
-                    mma_f16(acc, da0 + 2 * k, db0 + 2 * k, idesc, (kin > 0 || k > 0) ? 1u : 0u);
-                    if (NP == 2) {
-                        mma_f16(acc, da0 + 2 * k, db1 + 2 * k, idesc, 1u);
-                        mma_f16(acc, da1 + 2 * k, db0 + 2 * k, idesc, 1u);
-                    }
+                for (int m = 0; m < MS; ++m) {
+                    const uint64_t da = sw128_desc(smem_u32(sA + (s * MS + m) * S::A_BYTES));
+#pragma unroll
+                    for (int k = 0; k < BKH / 16; ++k)  // K = 16 halves = 32 bytes per instruction
+                        mma_f16(tmem + (uint32_t)(m * S::ACC), da + 2 * k, db + 2 * k, idesc,
+                                (kb > 0 || k > 0) ? 1u : 0u);
                 }
                 mma_commit(empty + s);
-                if (kin == kc - 1 || kb == kblocks - 1) mma_commit(acc_full + (ch & 1));
             }
-            // every MMA issued must be complete before tensor memory is released
-            mma_commit(done);
-            mbar_wait(done, 0, err, 4);
+            // every MMA issued must be complete before the epilogue and before
+            // tensor memory is released
+            mma_commit(accum);
+            mbar_wait(accum, 0, err, 4);
         }
         __syncwarp();
     } else {
         // epilogue warps 2..5: lane quadrant (warp % 4) of tensor memory
         const int q = warp & 3;
-        const int f = f0 + 32 * q + lane;
-        const float is = *inv_s;
-#pragma unroll 1
-        for (int ch = 0; ch < nchunks; ++ch) {
-            const int a = ch & 1;
-            // one lane waits, the warp follows it: tcgen05.ld is warp-collective
-            int ok = lane == 0 ? (int)mbar_wait(acc_full + a, (ch >> 1) & 1, err, 5) : 0;
-            ok = __shfl_sync(0xffffffffu, ok, 0);
-            if (!ok) break;
+        int ok = lane == 0 ? (int)mbar_wait(accum, 0, err, 5) : 0;
+        ok = __shfl_sync(0xffffffffu, ok, 0);
+        if (ok) {
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            float2* out = Y + (size_t)ch * pstride;
+            const float is = *inv_s;
 #pragma unroll 1
-            for (int c = 0; c < BN; c += 16) {
-                float v[16];
-                tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(a * S::ACC + c), v);
-                if (f < M) {
+            for (int m = 0; m < MS; ++m) {
+                const int f = f0 + m * BM + 32 * q + lane;
+#pragma unroll 1
+                for (int c = 0; c < BN; c += 16) {
+                    float v[16];
+                    tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(m * S::ACC + c), v);
+                    if (f < M) {
 #pragma unroll
-                    for (int i = 0; i < 8; ++i) {
-                        const int r = (c0 + c) / 2 + i;
-                        if (r < R) {
-                            const float sc = is * inv_t[r];
-                            out[(size_t)r * M + f] = make_float2(v[2 * i] * sc, v[2 * i + 1] * sc);
+                        for (int i = 0; i < 8; ++i) {
+                            const int r = (c0 + c) / 2 + i;
+                            if (r < R) {
+                                const float sc = is * inv_t[r];
+                                Y[(size_t)r * M + f] = make_float2(v[2 * i] * sc, v[2 * i + 1] * sc);
+                            }
                         }
                     }
                 }
             }
-            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-            __syncwarp();
-            if (lane == 0) mbar_arrive(acc_empty + a);
         }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -557,24 +536,22 @@ static emfa_status_t make_map_h(Ctx* c, CUtensorMap* m, const void* ptr, uint64_
     return EMFA_OK;
 }
 
-template <int BN, int NP>
-static emfa_status_t launch_h(Ctx* c, const CUtensorMap& a0, const CUtensorMap& a1, const CUtensorMap& b0,
-                              const CUtensorMap& b1, float2* Y, size_t pstride, int n, int nrhs, int kc,
-                              const float* inv_s, const float* inv_t, int* err, cudaStream_t st, int timer)
+template <int BN, int MS>
+static emfa_status_t launch_h(Ctx* c, const CUtensorMap& ta, const CUtensorMap& tb, float2* Y, int n, int nrhs,
+                              const float* inv_s, const float* inv_t, int* err, cudaStream_t st)
 {
-    using S = th::Smem<BN, NP>;
+    using S = th::Smem<BN, MS>;
     static std::atomic<unsigned long long> attr_set{0};  // one bit per device
     const unsigned long long bit = 1ull << (c->device & 63);
     if (!(attr_set.load() & bit)) {
-        EMFA_CUDA(c, cudaFuncSetAttribute(th::k_hgemm<BN, NP>, cudaFuncAttributeMaxDynamicSharedMemorySize, S::TOTAL));
+        EMFA_CUDA(c, cudaFuncSetAttribute(th::k_hgemm<BN, MS>, cudaFuncAttributeMaxDynamicSharedMemorySize, S::TOTAL));
         attr_set.fetch_or(bit);
     }
-    dim3 grd((2 * nrhs + BN - 1) / BN, (n + th::BM - 1) / th::BM);
+    dim3 grd((2 * nrhs + BN - 1) / BN, (n + th::BM * MS - 1) / (th::BM * MS));
     const int kblocks = (2 * n + th::BKH - 1) / th::BKH;
     {
-        TimedLaunch tl(c, timer, st, 8.0 * n * (double)n * nrhs);
-        th::k_hgemm<BN, NP><<<grd, th::THREADS, S::TOTAL, st>>>(a0, a1, b0, b1, Y, pstride, n, nrhs, kblocks, kc,
-                                                               inv_s, inv_t, err);
+        TimedLaunch tl(c, KT_GEMM, st, 8.0 * n * (double)n * nrhs);
+        th::k_hgemm<BN, MS><<<grd, th::THREADS, S::TOTAL, st>>>(ta, tb, Y, n, nrhs, kblocks, inv_s, inv_t, err);
     }
     c->kernel_launches += 1;
     EMFA_CUDA(c, cudaGetLastError());
@@ -632,14 +609,18 @@ emfa_status_t hgemm_apply(Ctx* c, const HPlanes& h, const void* X, void* Y, int 
     EMFA_TRY(herr(c, &err));
     th::k_hpack_f32<<<nrhs, 256, 0, st>>>((const float2*)X, n, ldh, bh, inv_t);
     c->kernel_launches += 1;
-    const int BN = 2 * nrhs <= 64 ? 64 : 144;
     CUtensorMap ta, tb;
+    // 256-row tiles (two M = 128 blocks sharing each B tile) once there are
+    // enough of them to fill the SMs; 144 columns = 72 right-hand sides
+    const int sms = c->sm_count > 0 ? c->sm_count : 148;
+    const int BN = 2 * nrhs <= 64 ? 64 : 144;
+    const int col_tiles = (2 * nrhs + BN - 1) / BN;
+    const bool tall = BN == 144 && (long)col_tiles * ((n + 255) / 256) >= (long)sms * 9 / 10;
     EMFA_TRY(make_map_h(c, &ta, h.zh, 2 * (uint64_t)n, (uint64_t)n, ldh, th::BM));
     EMFA_TRY(make_map_h(c, &tb, bh, 2 * (uint64_t)n, 2 * (uint64_t)nrhs, ldh, BN));
-    const int kc = 1 << 30;  // one chunk: the whole K in one accumulator
-    if (BN == 64)
-        return launch_h<64, 1>(c, ta, ta, tb, tb, (float2*)Y, 0, n, nrhs, kc, h.inv_s, inv_t, err, st, KT_GEMM);
-    return launch_h<144, 1>(c, ta, ta, tb, tb, (float2*)Y, 0, n, nrhs, kc, h.inv_s, inv_t, err, st, KT_GEMM);
+    if (BN == 64) return launch_h<64, 1>(c, ta, tb, (float2*)Y, n, nrhs, h.inv_s, inv_t, err, st);
+    if (tall) return launch_h<144, 2>(c, ta, tb, (float2*)Y, n, nrhs, h.inv_s, inv_t, err, st);
+    return launch_h<144, 1>(c, ta, tb, (float2*)Y, n, nrhs, h.inv_s, inv_t, err, st);
 }
 
 emfa_status_t hgemm_residual(Ctx* c, const HPlanes& h, const double2* X, const void* B, bool b_is_f32, double2* R,

@@ -249,6 +249,25 @@ def test_matvec_split_fp16_tensor_cores(ctx, n, r):
     assert err.max() < 2e-3, err.max()
 
 
+def test_matvec_split_fp16_tall_tiles(ctx):
+    """Order large enough for the 256-row tiles (7000 x 360: 28 row tiles x 5
+    column tiles, the last row tile half outside the matrix), checked on a
+    sample of rows including the last ones."""
+    import torch
+    from emfa_gb300 import api
+    n, r = 7000, 360
+    g = torch.Generator(device="cuda").manual_seed(5)
+    Z = torch.randn((n, n), dtype=torch.complex64, device="cuda", generator=g)
+    X = torch.randn((r, n), dtype=torch.complex64, device="cuda", generator=g)
+    Y = api.matvec(ctx, Z, X, "f16x").cpu().numpy()
+    rows = np.concatenate([np.random.default_rng(0).choice(n - 200, 300, replace=False), np.arange(n - 200, n)])
+    Zs = Z[torch.tensor(rows, device="cuda")].cpu().numpy().astype(np.complex128)
+    ref = (Zs @ X.cpu().numpy().astype(np.complex128).T).T
+    err = np.linalg.norm(Y[:, rows] - ref) / np.linalg.norm(ref)
+    assert err < 2e-3, err
+    assert np.all(np.abs(Y[:, rows]).max(axis=0) > 0)
+
+
 @pytest.mark.parametrize("n,r", [(1922, 24), (1001, 3)])
 def test_residual_split_fp16(ctx, n, r):
     """Refinement residual R = B - Z X from Zh Xh + Zh Xl + Zl Xh (a fresh
