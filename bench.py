@@ -331,10 +331,21 @@ def run_mlfma(args):
     X, info = ml.solve(V, sp)
     torch.cuda.synchronize()
     t_solve = time.perf_counter() - t0
+    from emfa_gb300 import roofline as RM
+    peaks, src = measured_peaks()
+    b3 = RM.mlfma_matvec_bytes(geo.n, ml.nnz, ml.level_boxes.tolist(), ml.poles.tolist(), comps=3)
+    b2 = RM.mlfma_matvec_bytes(geo.n, ml.nnz, ml.level_boxes.tolist(), ml.poles.tolist(), comps=2,
+                               near_index_bytes=4)
+    gbs = b3 / (mv_ms * 1e-3) / 1e9
     print(json.dumps({"mode": "mlfma", "n_rwg": geo.n, "levels": ml.levels, "level_boxes": ml.level_boxes.tolist(),
                       "poles": ml.poles.tolist(), "near_nnz": ml.nnz, "setup_s": round(t_setup, 3),
                       "matvec_ms": round(mv_ms, 4), "solve_s": round(t_solve, 4), "iterations": info.iterations,
-                      "converged": info.converged, "rel_residual": info.max_rel_residual}))
+                      "converged": info.converged, "rel_residual": info.max_rel_residual,
+                      "roofline": {"bound": "hbm", "achieved": round(gbs, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                                   "frac": round(gbs / peaks["hbm_gbs"], 4), "peak_source": src,
+                                   "algorithmic_bytes": b3, "model": "3-component patterns (this build)",
+                                   "survey_model_bytes_2comp": b2,
+                                   "survey_model_frac": round(b2 / (mv_ms * 1e-3) / 1e9 / peaks["hbm_gbs"], 4)}}))
 
 
 def main():
