@@ -348,6 +348,107 @@ def run_mlfma(args):
                                    "survey_model_frac": round(b2 / (mv_ms * 1e-3) / 1e9 / peaks["hbm_gbs"], 4)}}))
 
 
+def _pct(v, q):
+    return float(np.percentile(np.asarray(v, dtype=np.float64), q)) if len(v) else None
+
+
+def run_batch(args):
+    """Batched engine: 64 uneven EFIE problems (ellipsoids and cubes at
+    lambda/10, 500..8000 unknowns, 200..600 MHz), 8 incidences each with
+    their monostatic RCS, all through emfa_serve at once.  Plain FP64 GPU
+    path timed on a sample of the same problems for the comparison."""
+    import torch
+    from emfa_gb300 import api, build, workloads as W
+    build.build()
+    probs = W.batch_set(seed=0, count=64, n_inc=8)
+
+    def requests():
+        return [api.RcsRequest(m, f, ang, d, kind="efie", per_rhs=True) for (m, f, ang, d) in probs]
+
+    for _ in range(max(1, args.warmup)):
+        api.serve(requests(), lanes=args.lanes)
+    walls, res, reqs = [], None, None
+    for _ in range(max(1, args.steps)):
+        reqs = requests()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res = api.serve(reqs, lanes=args.lanes)
+        walls.append(time.perf_counter() - t0)
+    solves = sum(r.angles.shape[0] for r in reqs)
+    wall = statistics.median(walls)
+    svc = [r.t_done - r.t_start for r in res]
+    ok = sum(1 for r in res if r.status == 0)
+    # plain FP64 path on a sample (4 problems, evenly spread in size), and the
+    # RCS difference of the mixed-precision engine against it
+    order = np.argsort([r.n_rwg for r in res])
+    sample = [int(order[i]) for i in np.linspace(0, len(order) - 1, 4).astype(int)]
+    ctx = api.Context(0)
+    t64, err_db, n64 = 0.0, 0.0, 0
+    for i in sample:
+        m, f, ang, d = probs[i]
+        fp = api.fill_params("efie", "f64", f, 1.0)
+        fp.edm_mode = 2
+        sp = api.solver_params("gmres", restart=250, tol=1e-5, max_iter=5000)
+        t0 = time.perf_counter()
+        out64, _, _ = api.dense_rcs(ctx, m, fp, ang, sp, d, per_rhs=True)
+        t64 += time.perf_counter() - t0
+        n64 += ang.shape[0]
+        err_db = max(err_db, float(np.abs(reqs[i].rcs - out64).max()))
+    ctx.close()
+    plain = n64 / t64
+    print(json.dumps({
+        "mode": "batch", "metric": "RCS solves/s (batched, 64 uneven EFIE problems x 8 incidences)",
+        "value": round(solves / wall, 3), "unit": "solves/s", "problems": len(reqs), "ok": ok, "solves": solves,
+        "wall_s": round(wall, 4), "lanes": args.lanes or 6,
+        "unknowns": {"min": min(r.n_rwg for r in res), "max": max(r.n_rwg for r in res),
+                     "mean": round(statistics.mean(r.n_rwg for r in res), 1)},
+        "iterations": {"p50": _pct([r.iterations for r in res], 50), "max": max(r.iterations for r in res)},
+        "service_ms": {"p50": round(1e3 * _pct(svc, 50), 2), "p99": round(1e3 * _pct(svc, 99), 2)},
+        "plain_fp64": {"solves_per_s": round(plain, 3), "sample_problems": len(sample), "sample_solves": n64},
+        "speedup_vs_plain_fp64": round(solves / wall / plain, 2),
+        "rcs_max_abs_err_db_vs_fp64": err_db,
+        "data": "synthetic, seeded (seed 0)"}))
+
+
+def run_serve(args):
+    """Served stream: Poisson arrivals (mean 200 requests/s, seeded) of
+    monostatic RCS requests, 1k..120k unknowns log-uniform on spheres,
+    ellipsoids and cubes at lambda/10, CFIE alpha 0.5; dense below 10k
+    unknowns, MLFMA above; 150 GB admission budget.  Latency = completion -
+    arrival on the host clock."""
+    import torch
+    from emfa_gb300 import api, build, workloads as W
+    build.build()
+    stream = W.served_stream(seed=0, count=args.requests, rate=200.0, n_inc=4)
+
+    def requests(scale_t=1.0):
+        return [api.RcsRequest(m, f, ang, d, kind="cfie", alpha=0.5, per_rhs=True, arrival_s=t * scale_t)
+                for (t, m, f, ang, d) in stream]
+
+    warm = [api.RcsRequest(m, f, ang, d, kind="cfie", per_rhs=True) for (t, m, f, ang, d) in stream[:6]]
+    api.serve(warm, lanes=args.lanes)
+    reqs = requests()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    res = api.serve(reqs, lanes=args.lanes, realtime=True)
+    wall = time.perf_counter() - t0
+    lat = [r.t_done - r.t_arrive for r in res]
+    solves = sum(r.angles.shape[0] for r in reqs)
+    mk = max(r.t_done for r in res)
+    dense = [r for r in res if r.method == 1]
+    ml = [r for r in res if r.method == 2]
+    print(json.dumps({
+        "mode": "serve", "metric": "RCS solves/s and p50/p99 latency (served stream)",
+        "value": round(solves / mk, 3), "unit": "solves/s", "requests": len(reqs),
+        "ok": sum(1 for r in res if r.status == 0), "solves": solves, "wall_s": round(wall, 3),
+        "arrival_span_s": round(stream[-1][0], 3), "lanes": args.lanes or 6,
+        "latency_ms": {"p50": round(1e3 * _pct(lat, 50), 1), "p99": round(1e3 * _pct(lat, 99), 1)},
+        "dense": {"requests": len(dense), "latency_p50_ms": round(1e3 * _pct([r.t_done - r.t_arrive for r in dense], 50), 1) if dense else None},
+        "mlfma": {"requests": len(ml), "latency_p50_ms": round(1e3 * _pct([r.t_done - r.t_arrive for r in ml], 50), 1) if ml else None,
+                  "max_unknowns": max((r.n_rwg for r in ml), default=0)},
+        "hbm_budget_gb": 150, "data": "synthetic, seeded (seed 0)"}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -359,7 +460,9 @@ def main():
     ap.add_argument("--check", type=int, default=1)
     ap.add_argument("--orth", default="auto", choices=["auto", "cgs1", "cgs2"])
     ap.add_argument("--cpu-baseline", type=int, default=1)
-    ap.add_argument("--mode", default="job", choices=["job", "gemm", "mlfma"])
+    ap.add_argument("--mode", default="job", choices=["job", "gemm", "mlfma", "batch", "serve"])
+    ap.add_argument("--lanes", type=int, default=0)
+    ap.add_argument("--requests", type=int, default=100)
     ap.add_argument("--mlfma-subdiv", type=int, default=6)
     ap.add_argument("--gemm-n", type=int, default=7680)
     ap.add_argument("--gemm-r", type=int, default=360)
@@ -369,6 +472,12 @@ def main():
         return
     if args.mode == "mlfma":
         run_mlfma(args)
+        return
+    if args.mode == "batch":
+        run_batch(args)
+        return
+    if args.mode == "serve":
+        run_serve(args)
         return
     rank, local, world = rank_env()
     if world > 1:

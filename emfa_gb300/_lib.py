@@ -40,6 +40,27 @@ class MlfmaParams(ctypes.Structure):
     _fields_ = [("freq", ctypes.c_double), ("alpha", ctypes.c_double), ("box_threshold", ctypes.c_double)]
 
 
+class Request(ctypes.Structure):
+    _fields_ = [("verts", ctypes.c_void_p), ("n_vert", ctypes.c_int), ("tris", ctypes.c_void_p), ("n_tri", ctypes.c_int),
+                ("kind", ctypes.c_int), ("method", ctypes.c_int), ("freq", ctypes.c_double), ("alpha", ctypes.c_double),
+                ("angles", ctypes.c_void_p), ("n_inc", ctypes.c_int), ("rcs_dirs", ctypes.c_void_p),
+                ("n_dir", ctypes.c_int), ("per_rhs_dirs", ctypes.c_int), ("tol", ctypes.c_double),
+                ("max_iter", ctypes.c_int), ("box_threshold", ctypes.c_double), ("arrival_s", ctypes.c_double),
+                ("rcs_out", ctypes.c_void_p)]
+
+
+class RequestResult(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int), ("method", ctypes.c_int), ("n_rwg", ctypes.c_int),
+                ("iterations", ctypes.c_int), ("converged", ctypes.c_int), ("max_rel_residual", ctypes.c_double),
+                ("t_arrive", ctypes.c_double), ("t_start", ctypes.c_double), ("t_done", ctypes.c_double),
+                ("hbm_estimate", ctypes.c_size_t), ("lane", ctypes.c_int)]
+
+
+class ServeOpts(ctypes.Structure):
+    _fields_ = [("lanes", ctypes.c_int), ("hbm_budget", ctypes.c_size_t), ("dense_max", ctypes.c_int),
+                ("realtime", ctypes.c_int)]
+
+
 class SolveInfo(ctypes.Structure):
     _fields_ = [("iterations", ctypes.c_int), ("cycles", ctypes.c_int), ("converged", ctypes.c_int),
                 ("max_rel_residual", ctypes.c_double), ("seconds", ctypes.c_double)]
@@ -80,6 +101,8 @@ _SIGS = {
     "emfa_matvec": (ci, [vp, ci, ci, vp, ci, vp, ci, vp, vp]),
     "emfa_matvec_tf32_noalloc": (ci, [vp, ci, vp, ci, vp, vp]),
     "emfa_ctx_set_kernel_timing": (ci, [vp, ci]),
+    "emfa_serve": (ci, [ci, ctypes.POINTER(Request), ci, ctypes.POINTER(ServeOpts), ctypes.POINTER(RequestResult)]),
+    "emfa_serve_simulate": (ci, [vp, vp, vp, ci, ctypes.POINTER(ServeOpts), vp, vp]),
     "emfa_residual": (ci, [vp, ci, ci, vp, ci, vp, vp, ci, vp, vp]),
     "emfa_ctx_kernel_time": (ci, [vp, ci, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_double),
                                   ctypes.POINTER(ctypes.c_double)]),

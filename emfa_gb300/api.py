@@ -357,3 +357,59 @@ class Mlfma:
         X = torch.empty_like(Xbox)
         self.ctx.check(L.lib().emfa_mlfma_unpermute(self.h, _ptr(Xbox), Xbox.shape[0], _ptr(X), None))
         return X
+
+
+# ---------------------------------------------------------------------------
+# batched and served solves (emfa_serve)
+# ---------------------------------------------------------------------------
+class RcsRequest:
+    """One RCS problem for serve(): a host mesh, a formulation, incidences
+    and RCS directions (per_rhs: one set of directions per incidence, e.g.
+    the monostatic one)."""
+
+    def __init__(self, mesh: TriMesh, freq: float, angles, dirs, kind="cfie", alpha=0.5, method="auto",
+                 per_rhs=False, tol=0.0, max_iter=0, box_threshold=0.25, arrival_s=0.0):
+        self.mesh = mesh
+        self.verts = np.ascontiguousarray(mesh.verts, dtype=np.float64)
+        self.tris = np.ascontiguousarray(mesh.tris, dtype=np.int32)
+        self.angles = np.ascontiguousarray(np.atleast_2d(angles), dtype=np.float64)
+        self.dirs = np.ascontiguousarray(dirs, dtype=np.float64)
+        self.n_dir = self.dirs.shape[-2] if self.dirs.ndim == 3 else self.dirs.shape[0]
+        self.rcs = np.zeros((self.angles.shape[0], self.n_dir), dtype=np.float64)
+        self.kind = L.EMFA_CFIE if kind == "cfie" else L.EMFA_EFIE
+        self.method = {"auto": 0, "dense": 1, "mlfma": 2}[method]
+        self.freq, self.alpha, self.per_rhs = float(freq), float(alpha), bool(per_rhs)
+        self.tol, self.max_iter, self.box_threshold = float(tol), int(max_iter), float(box_threshold)
+        self.arrival_s = float(arrival_s)
+
+    def c_struct(self) -> L.Request:
+        return L.Request(self.verts.ctypes.data, self.verts.shape[0], self.tris.ctypes.data, self.tris.shape[0],
+                         self.kind, self.method, self.freq, self.alpha, self.angles.ctypes.data, self.angles.shape[0],
+                         self.dirs.ctypes.data, self.n_dir, int(self.per_rhs), self.tol, self.max_iter,
+                         self.box_threshold, self.arrival_s, self.rcs.ctypes.data)
+
+
+def serve(requests, device=0, lanes=0, hbm_budget=0, dense_max=0, realtime=False):
+    """Runs the requests through emfa_serve; each request's rcs array is
+    filled in place.  Returns the per-request results (status, method,
+    unknowns, iterations, timing in seconds from the start)."""
+    n = len(requests)
+    arr = (L.Request * n)(*[r.c_struct() for r in requests])
+    res = (L.RequestResult * n)()
+    opts = L.ServeOpts(int(lanes), int(hbm_budget), int(dense_max), int(bool(realtime)))
+    L.check(L.lib().emfa_serve(int(device), arr, n, ctypes.byref(opts), res))
+    return list(res)
+
+
+def serve_simulate(arrival, duration, nbytes, lanes=6, hbm_budget=0, realtime=True):
+    """The admitter of serve() on a simulated clock: (start times, lanes)."""
+    a = np.ascontiguousarray(arrival, dtype=np.float64)
+    d = np.ascontiguousarray(duration, dtype=np.float64)
+    b = np.ascontiguousarray(nbytes, dtype=np.uint64)
+    n = a.shape[0]
+    start = np.zeros(n, dtype=np.float64)
+    lane = np.zeros(n, dtype=np.int32)
+    opts = L.ServeOpts(int(lanes), int(hbm_budget), 0, int(bool(realtime)))
+    L.check(L.lib().emfa_serve_simulate(a.ctypes.data_as(vp), d.ctypes.data_as(vp), b.ctypes.data_as(vp), n,
+                                        ctypes.byref(opts), start.ctypes.data_as(vp), lane.ctypes.data_as(vp)))
+    return start, lane

@@ -49,7 +49,7 @@ emfa_status_t ctx_alloc(Ctx* c, size_t bytes, void** p)
         c->used += bytes;
         if (c->used > c->peak) c->peak = c->used;
     }
-    cudaError_t e = cudaMalloc(p, bytes);
+    cudaError_t e = c->stream_ordered ? cudaMallocAsync(p, bytes, c->stream) : cudaMalloc(p, bytes);
     if (e != cudaSuccess) {
         std::lock_guard<std::mutex> g(c->mu);
         c->used -= bytes;
@@ -101,7 +101,10 @@ emfa_status_t ctx_workspace(Ctx* c, int slot, size_t bytes, void** p)
 void ctx_free(Ctx* c, void* p, size_t bytes)
 {
     if (!p) return;
-    cudaFree(p);
+    if (c->stream_ordered)
+        cudaFreeAsync(p, c->stream);
+    else
+        cudaFree(p);
     std::lock_guard<std::mutex> g(c->mu);
     c->used -= bytes;
 }
@@ -172,12 +175,13 @@ emfa_status_t emfa_ctx_destroy(emfa_ctx_t* ctx)
 {
     if (!ctx) return EMFA_ERR_INVALID;
     cudaSetDevice(ctx->device);
+    // buffers first: stream-ordered ones are freed on the context's stream
+    for (auto& b : ctx->ws) b.release();
+    for (auto& kv : ctx->user_bufs) ctx_free(ctx, kv.first, kv.second);
     if (ctx->stream) {
         cudaStreamSynchronize(ctx->stream);
         cudaStreamDestroy(ctx->stream);
     }
-    for (auto& b : ctx->ws) b.release();
-    for (auto& kv : ctx->user_bufs) cudaFree(kv.first);
     for (auto& t : ctx->timers) {
         for (auto e : t.start) cudaEventDestroy(e);
         for (auto e : t.stop) cudaEventDestroy(e);

@@ -100,6 +100,7 @@ struct Ctx {
     std::mutex mu;
     int sm_count = 0;
     long long kernel_launches = 0;  // kernels launched through this context
+    bool stream_ordered = false;  // allocations on `stream` (cudaMallocAsync), for lanes of the server
     bool time_kernels = false;
     KernelTimer timers[KT_COUNT];
     DevBuf ws[WS_COUNT];            // declared after mu: destroyed before it

@@ -146,7 +146,8 @@ __global__ void __launch_bounds__(KB) k_axpys(const Cx<T>* __restrict__ V, size_
 // mixed path: GB300's FP64 pipe is ~1/64 of FP32), and the per-thread sums
 // meet in FP64 across the block and across blocks.
 // ---------------------------------------------------------------------------
-constexpr int MAXV = 32;  // basis vectors per pass (GMRES restart <= 31)
+constexpr int MAXV = 32;  // basis vectors per pass of the block-dot kernels (BiCGStab)
+constexpr int MAX_RESTART = 255;  // GMRES(m): coefficients live in dynamic shared memory
 
 template <typename T> struct Acc { using type = float; };
 template <> struct Acc<double> { using type = double; };
@@ -341,12 +342,15 @@ __global__ void __launch_bounds__(256) k_vupdate(const Cx<T>* __restrict__ V, si
     using A = typename Acc<T>::type;
     const int blk = blockIdx.x, r = blockIdx.y;
     const size_t base = (size_t)r * n;
-    __shared__ A hs[2][64];
+    // coefficients (dynamic shared memory: 2 nv values, any restart length)
+    extern __shared__ unsigned char dyn_smem[];
+    A* hs0 = reinterpret_cast<A*>(dyn_smem);
+    A* hs1 = hs0 + nv;
     __shared__ double red[8];
     for (int i = threadIdx.x; i < nv; i += blockDim.x) {
         double2 t = h[(size_t)i * nrhs + r];
-        hs[0][i] = (A)t.x;
-        hs[1][i] = (A)t.y;
+        hs0[i] = (A)t.x;
+        hs1[i] = (A)t.y;
     }
     __syncthreads();
     A nr = 0;
@@ -361,14 +365,14 @@ __global__ void __launch_bounds__(256) k_vupdate(const Cx<T>* __restrict__ V, si
             for (int u = 0; u < 8; ++u) v[u] = vk[(size_t)(i + u) * vstride];
 #pragma unroll
             for (int u = 0; u < 8; ++u) {
-                const A hr = hs[0][i + u], hi = hs[1][i + u];
+                const A hr = hs0[i + u], hi = hs1[i + u];
                 sr += hr * (A)v[u].re - hi * (A)v[u].im;
                 si += hr * (A)v[u].im + hi * (A)v[u].re;
             }
         }
         for (; i < nv; ++i) {
             const Cx<T> v = vk[(size_t)i * vstride];
-            const A hr = hs[0][i], hi = hs[1][i];
+            const A hr = hs0[i], hi = hs1[i];
             sr += hr * (A)v.re - hi * (A)v.im;
             si += hr * (A)v.im + hi * (A)v.re;
         }
@@ -399,12 +403,14 @@ __global__ void k_update_x2(const Cx<T>* __restrict__ V, size_t vstride, int nvm
 {
     using A = typename Acc<T>::type;
     const int r = blockIdx.y;
-    __shared__ A ys[2][64];
+    extern __shared__ unsigned char dyn_smem[];
+    A* ys0 = reinterpret_cast<A*>(dyn_smem);  // 2 nvmax values
+    A* ys1 = ys0 + nvmax;
     const int jl = min(jlen[r], nvmax);
     for (int i = threadIdx.x; i < jl; i += blockDim.x) {
         double2 t = y[(size_t)i * nrhs + r];
-        ys[0][i] = (A)t.x;
-        ys[1][i] = (A)t.y;
+        ys0[i] = (A)t.x;
+        ys1[i] = (A)t.y;
     }
     __syncthreads();
     int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -413,8 +419,8 @@ __global__ void k_update_x2(const Cx<T>* __restrict__ V, size_t vstride, int nvm
     A sr = 0, si = 0;
     for (int i = 0; i < jl; ++i) {
         const Cx<T> v = V[(size_t)i * vstride + o];
-        sr += ys[0][i] * (A)v.re - ys[1][i] * (A)v.im;
-        si += ys[0][i] * (A)v.im + ys[1][i] * (A)v.re;
+        sr += ys0[i] * (A)v.re - ys1[i] * (A)v.im;
+        si += ys0[i] * (A)v.im + ys1[i] * (A)v.re;
     }
     double2 x = X[o];
     X[o] = make_double2(x.x + (double)sr, x.y + (double)si);
@@ -640,7 +646,7 @@ static emfa_status_t gmres_t(Ctx* c, LinOp& A, const void* B, int nrhs, double2*
                              emfa_solve_info_t* info, cudaStream_t st)
 {
     const int n = A.n, prec = A.prec;
-    const int m = std::max(1, std::min(sp->restart > 0 ? sp->restart : 30, MAXV - 1));
+    const int m = std::max(1, std::min(sp->restart > 0 ? sp->restart : 30, MAX_RESTART));
     const size_t vec = (size_t)n * nrhs;
     // vector-pass grid: ~2 CTAs per SM over (chunks of N) x (right-hand sides)
     const int sms = c->sm_count > 0 ? c->sm_count : 148;
@@ -733,13 +739,13 @@ static emfa_status_t gmres_t(Ctx* c, LinOp& A, const void* B, int nrhs, double2*
             k_vdots<T><<<vg, 256, 0, st>>>(V, vec, nv, W, n, nrhs, vblk, partial);
             k_reduce_partials<<<rg, 128, 0, st>>>(partial, nv, nrhs, vblk, s.hcol, 0);
             if (two_pass) {
-                k_vupdate<T, false><<<vg, 256, 0, st>>>(V, vec, nv, s.hcol, W, n, nrhs, vblk, pnorm);
+                k_vupdate<T, false><<<vg, 256, 2 * nv * sizeof(typename Acc<T>::type), st>>>(V, vec, nv, s.hcol, W, n, nrhs, vblk, pnorm);
                 k_vdots<T><<<vg, 256, 0, st>>>(V, vec, nv, W, n, nrhs, vblk, partial);
                 k_reduce_partials<<<rg, 128, 0, st>>>(partial, nv, nrhs, vblk, s.y, 0);
-                k_vupdate<T, true><<<vg, 256, 0, st>>>(V, vec, nv, s.y, W, n, nrhs, vblk, pnorm);
+                k_vupdate<T, true><<<vg, 256, 2 * nv * sizeof(typename Acc<T>::type), st>>>(V, vec, nv, s.y, W, n, nrhs, vblk, pnorm);
                 c->kernel_launches += 3;
             } else {
-                k_vupdate<T, true><<<vg, 256, 0, st>>>(V, vec, nv, s.hcol, W, n, nrhs, vblk, pnorm);
+                k_vupdate<T, true><<<vg, 256, 2 * nv * sizeof(typename Acc<T>::type), st>>>(V, vec, nv, s.hcol, W, n, nrhs, vblk, pnorm);
             }
             EMFA_CUDA(c, cudaMemsetAsync(s.counters, 0, sizeof(int), st));
             k_arnoldi_finish<<<(nrhs + 127) / 128, 128, 0, st>>>(s, j, pnorm, vblk, two_pass ? 1 : 0);
@@ -753,7 +759,8 @@ static emfa_status_t gmres_t(Ctx* c, LinOp& A, const void* B, int nrhs, double2*
         total_iters += steps;
         EMFA_TRY(A.check(c, st));
         k_backsolve<<<(nrhs + 127) / 128, 128, 0, st>>>(s);
-        k_update_x2<T><<<dim3((n + 255) / 256, nrhs), 256, 0, st>>>(V, vec, steps, s.y, s.jlen, X, n, nrhs);
+        k_update_x2<T><<<dim3((n + 255) / 256, nrhs), 256, 2 * std::max(1, steps) * sizeof(typename Acc<T>::type), st>>>(
+            V, vec, steps, s.y, s.jlen, X, n, nrhs);
         c->kernel_launches += 2;
         EMFA_CUDA(c, cudaGetLastError());
     }

@@ -75,7 +75,7 @@ typedef struct {
 
 typedef struct {
     int method;         /* emfa_method_t                                            */
-    int restart;        /* GMRES restart length m (reference: 30)                   */
+    int restart;        /* GMRES restart length m, 1..255 (reference: 30)           */
     int max_iter;       /* cap on inner iterations per right-hand side              */
     double tol;         /* stop when ||b - Z x|| / ||b|| < tol (or absolute, below) */
     int tol_absolute;   /* 1: ||b - Z x|| < tol, the reference GMRES criterion      */
@@ -292,6 +292,76 @@ emfa_status_t emfa_dense_rcs(emfa_ctx_t* ctx, const double* verts_host, int n_ve
                              const emfa_solver_params_t* sp, const double* rcs_dirs_host, int n_dir,
                              int per_rhs_dirs, double* rcs_out_host, double* I_out_host,
                              emfa_solve_info_t* info);
+
+/* ---- batched and served RCS solves ---------------------------------------- */
+/* Many independent RCS problems on one GPU.  No counterpart in the reference,
+ * which solves one problem per process run (solver::loadSolver,
+ * EMSolver/Solver.cpp:45-95).
+ *
+ * A request is a host mesh plus what to solve.  The engine keeps `lanes`
+ * worker lanes, each a host thread with its own context and CUDA stream, so
+ * the fills, products and solves of different problems overlap on the
+ * device.  Admission: a request becomes visible at its arrival time (all at
+ * once when realtime = 0); a free lane takes the oldest visible request whose
+ * estimated device memory fits in what the running requests leave of
+ * hbm_budget, else the oldest one that fits, so a large request does not
+ * block small ones.  Dense CFIE/EFIE with split-FP16 refinement below
+ * dense_max unknowns, MLFMA (CFIE, box order) above.  Each problem's
+ * operators and Krylov state stay on its lane's device memory until it
+ * finishes.  Device memory is stream-ordered per lane (no device-wide
+ * synchronisation between lanes). */
+typedef struct {
+    const double* verts;      /* host, n_vert x 3 */
+    int n_vert;
+    const int* tris;          /* host, n_tri x 3, 0-based */
+    int n_tri;
+    int kind;                 /* EMFA_EFIE or EMFA_CFIE                                   */
+    int method;               /* 0 auto (dense below dense_max), 1 dense, 2 MLFMA         */
+    double freq, alpha;       /* Hz; CFIE combination coefficient                         */
+    const double* angles;     /* host, n_inc x (theta, phi, pole) degrees                 */
+    int n_inc;
+    const double* rcs_dirs;   /* host unit vectors, n_dir x 3 (or n_inc x n_dir x 3)      */
+    int n_dir;
+    int per_rhs_dirs;
+    double tol;               /* relative residual target; 0 = 1e-6 dense CFIE, 1e-5 dense */
+                              /* EFIE (GMRES(250)), 1e-3 MLFMA                           */
+    int max_iter;
+    double box_threshold;     /* MLFMA finest box size in wavelengths                     */
+    double arrival_s;         /* seconds after the run starts (realtime mode)             */
+    double* rcs_out;          /* host, n_inc x n_dir dBsm, written when the request ends   */
+} emfa_request_t;
+
+typedef struct {
+    int status;               /* emfa_status_t of the request                            */
+    int method;               /* 1 dense, 2 MLFMA                                         */
+    int n_rwg;
+    int iterations;
+    int converged;            /* right-hand sides that met tol                           */
+    double max_rel_residual;
+    double t_arrive, t_start, t_done;  /* seconds from the run start                      */
+    size_t hbm_estimate;      /* bytes the admitter charged                              */
+    int lane;
+} emfa_request_result_t;
+
+typedef struct {
+    int lanes;                /* worker lanes (streams); 0 = 6                            */
+    size_t hbm_budget;        /* admission budget in bytes; 0 = 150 GB                    */
+    int dense_max;            /* largest dense problem (unknowns); 0 = 10000              */
+    int realtime;             /* 1: honour arrival_s on the host clock                   */
+} emfa_serve_opts_t;
+
+/* Runs every request to completion and fills results (one per request).
+ * Returns EMFA_OK when the engine ran; per-request failures are reported in
+ * results[i].status. */
+emfa_status_t emfa_serve(int device, const emfa_request_t* reqs, int n_req, const emfa_serve_opts_t* opts,
+                         emfa_request_result_t* results);
+
+/* The admitter of emfa_serve on the host clock of a simulation (no GPU):
+ * requests with given arrival times, durations and memory estimates, and
+ * the opts' lanes, budget and realtime flag.  start_out[i] and lane_out[i]
+ * receive when and where request i would start. */
+emfa_status_t emfa_serve_simulate(const double* arrival, const double* duration, const size_t* bytes, int n,
+                                  const emfa_serve_opts_t* opts, double* start_out, int* lane_out);
 
 #ifdef __cplusplus
 }
