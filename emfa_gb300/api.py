@@ -413,3 +413,55 @@ def serve_simulate(arrival, duration, nbytes, lanes=6, hbm_budget=0, realtime=Tr
     L.check(L.lib().emfa_serve_simulate(a.ctypes.data_as(vp), d.ctypes.data_as(vp), b.ctypes.data_as(vp), n,
                                         ctypes.byref(opts), start.ctypes.data_as(vp), lane.ctypes.data_as(vp)))
     return start, lane
+
+
+# ---------------------------------------------------------------------------
+# binary dumps
+# ---------------------------------------------------------------------------
+_DUMP_DTYPES = {np.dtype(np.complex64): 1, np.dtype(np.complex128): 2, np.dtype(np.float32): 3,
+                np.dtype(np.float64): 4, np.dtype(np.int32): 5}
+_DUMP_NP = {v: k for k, v in _DUMP_DTYPES.items()}
+
+
+def dump_save(path: str, array, name: str = "", freq: float = 0.0):
+    """Writes a 1-D or 2-D array (numpy, or a CUDA torch tensor) as an EMFA dump."""
+    on_dev = not isinstance(array, np.ndarray)
+    if on_dev:
+        torch = _torch()
+        dt = np.dtype({torch.complex64: np.complex64, torch.complex128: np.complex128, torch.float32: np.float32,
+                       torch.float64: np.float64, torch.int32: np.int32}[array.dtype])
+        shape = tuple(array.shape)
+        ptr = _ptr(array)
+    else:
+        array = np.ascontiguousarray(array)
+        dt, shape, ptr = array.dtype, array.shape, array.ctypes.data_as(vp)
+    rows, cols = (shape[0], int(np.prod(shape[1:]))) if len(shape) > 1 else (1, shape[0])
+    L.check(L.lib().emfa_dump_save(path.encode(), name.encode(), _DUMP_DTYPES[dt], rows, cols, float(freq), ptr,
+                                   int(on_dev)))
+
+
+def dump_info(path: str):
+    name = ctypes.create_string_buffer(24)
+    dt, rows, cols, freq = ctypes.c_int(), ctypes.c_size_t(), ctypes.c_size_t(), ctypes.c_double()
+    L.check(L.lib().emfa_dump_info(path.encode(), name, ctypes.byref(dt), ctypes.byref(rows), ctypes.byref(cols),
+                                   ctypes.byref(freq)))
+    return {"name": name.value.decode(), "dtype": _DUMP_NP[dt.value], "rows": rows.value, "cols": cols.value,
+            "freq": freq.value}
+
+
+def dump_load(path: str, device=None):
+    """Reads a dump into a numpy array, or into a CUDA tensor when device is given."""
+    info = dump_info(path)
+    shape = (info["rows"], info["cols"]) if info["rows"] > 1 else (info["cols"],)
+    if device is None:
+        out = np.empty(shape, dtype=info["dtype"])
+        L.check(L.lib().emfa_dump_load(path.encode(), out.ctypes.data_as(vp), out.nbytes, 0))
+        return out, info
+    torch = _torch()
+    tdt = {np.dtype(np.complex64): torch.complex64, np.dtype(np.complex128): torch.complex128,
+           np.dtype(np.float32): torch.float32, np.dtype(np.float64): torch.float64,
+           np.dtype(np.int32): torch.int32}[info["dtype"]]
+    out = torch.empty(shape, dtype=tdt, device=device)
+    torch.cuda.current_stream().synchronize()
+    L.check(L.lib().emfa_dump_load(path.encode(), _ptr(out), out.numel() * out.element_size(), 1))
+    return out, info

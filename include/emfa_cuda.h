@@ -293,6 +293,21 @@ emfa_status_t emfa_dense_rcs(emfa_ctx_t* ctx, const double* verts_host, int n_ve
                              int per_rhs_dirs, double* rcs_out_host, double* I_out_host,
                              emfa_solve_info_t* info);
 
+/* ---- binary dumps ------------------------------------------------------------ */
+/* Versioned binary dump of a matrix or vector (Z, V, I, operator arrays):
+ * a 128-byte header (magic "EMFADUMP", version, dtype, rows, cols,
+ * frequency, name, payload size, FNV-1a hash) and the row-major payload.
+ * Replaces the Armadillo ASCII dumps of EFIE::writeZIVData
+ * (EMSolver/EFIE.cpp:932-950) and CFIE::writeZIVData (EMSolver/CFIE.cpp:797-812).
+ * dtype: 1 complex64, 2 complex128, 3 float32, 4 float64, 5 int32.
+ * data_on_device: 1 when data is device memory.  Loading checks the header
+ * and the payload hash and refuses a destination smaller than the payload. */
+emfa_status_t emfa_dump_save(const char* path, const char* name, int dtype, size_t rows, size_t cols, double freq,
+                             const void* data, int data_on_device);
+emfa_status_t emfa_dump_info(const char* path, char* name_out /* 24 bytes */, int* dtype, size_t* rows,
+                             size_t* cols, double* freq);
+emfa_status_t emfa_dump_load(const char* path, void* data, size_t capacity_bytes, int data_on_device);
+
 /* ---- batched and served RCS solves ---------------------------------------- */
 /* Many independent RCS problems on one GPU.  No counterpart in the reference,
  * which solves one problem per process run (solver::loadSolver,
