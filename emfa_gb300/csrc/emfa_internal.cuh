@@ -174,6 +174,13 @@ struct Geom {
     std::vector<int> rwg;        // host, N x 6 (v1 v2 vxp vxm tp tm)
     GeomDev<float> g32;
     GeomDev<double> g64;
+    // tiled fill: the distinct triangles of each block of 16 consecutive
+    // RWGs, and each RWG's position of its two triangles in its block's list
+    bool tile_ready = false;
+    int tile_maxt = 0;
+    DevBuf tile_tris;  // int [blocks][tile_maxt]
+    DevBuf tile_nt;    // int [blocks]
+    DevBuf tile_loc;   // uint8 [N][2]
 };
 
 emfa_status_t geom_prepare_f32(Geom* g, cudaStream_t st);

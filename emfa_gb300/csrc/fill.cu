@@ -14,6 +14,10 @@
 #include "emfa_math.cuh"
 #include "fill_entry.cuh"
 
+#include <algorithm>
+#include <type_traits>
+#include <vector>
+
 namespace emfa {
 
 // ---------------------------------------------------------------------------
@@ -179,6 +183,236 @@ __global__ void __launch_bounds__(256) k_fill_z(const RwgPack<T>* __restrict__ r
 }
 
 // ---------------------------------------------------------------------------
+// tiled FP32 fill: a CTA fills a 16 x 16 block of Z.  The 9 point-pair
+// kernel values (G = e^{-jkR}/R, with R and 1/R) of every (test triangle,
+// source triangle) pair of the block are computed once into shared memory,
+// then each entry is assembled from them: consecutive RWGs share triangles,
+// so a block needs about 18 x 18 triangle pairs instead of 16 x 16 x 4.  The
+// arithmetic of every point pair, and the order of every sum, is that of
+// z_entry, except that sin/cos(kR) come from the FP32 Taylor evaluation
+// (sincos_pi_taylor, about 1.5 ulp).
+// ---------------------------------------------------------------------------
+constexpr int FT = 16;  // RWGs per tile side
+
+template <bool CFIE>
+__device__ __forceinline__ void regular_pair_staged(const float (&P)[3][3], const float4* __restrict__ Q4,
+                                                    const float (&vf)[3], const float (&vs)[3],
+                                                    const float (&nf)[3], const float4* __restrict__ K,
+                                                    const FillConst<float>& c, Cx<float>& ze, Cx<float>& zm)
+{
+    V3<float> n = v3(nf[0], nf[1], nf[2]);
+    float Q[9];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        const float4 t = Q4[q];
+        Q[3 * q] = t.x;
+        Q[3 * q + 1] = t.y;
+        Q[3 * q + 2] = t.z;
+    }
+    V3<float> rs[3];
+    float nrs[3];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        rs[q] = v3(Q[3 * q] - vs[0], Q[3 * q + 1] - vs[1], Q[3 * q + 2] - vs[2]);
+        nrs[q] = dot(n, rs[q]);
+    }
+#pragma unroll
+    for (int p = 0; p < 3; ++p) {
+        V3<float> pp = v3(P[p][0], P[p][1], P[p][2]);
+        V3<float> rf = v3(P[p][0] - vf[0], P[p][1] - vf[1], P[p][2] - vf[2]);
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            const float4 kv = K[3 * p + q];
+            const float gr = kv.x, gi = kv.y;
+            float rfrs = dot(rf, rs[q]);
+            float e = 0.25f * rfrs - c.inv_k2;
+            ze.re += e * gr;
+            ze.im += e * gi;
+            if (CFIE) {
+                V3<float> d = v3(pp.x - Q[3 * q], pp.y - Q[3 * q + 1], pp.z - Q[3 * q + 2]);
+                const float r = kv.z, rinv = kv.w;
+                float m = dot(rf, d) * nrs[q] - rfrs * dot(n, d);
+                float t = m * (rinv * rinv);
+                float kr = r * c.k;
+                float hr = gr - kr * gi, hi = gi + kr * gr;
+                zm.re += t * hr;
+                zm.im += t * hi;
+            }
+        }
+    }
+}
+
+template <bool CFIE>
+__global__ void __launch_bounds__(256) k_fill_tile(const RwgPack<float>* __restrict__ rw, int n, FillConst<float> c,
+                                                   const double2* __restrict__ sing, const float* __restrict__ tri_q3,
+                                                   const float* __restrict__ tri_n, const int* __restrict__ blk_tris,
+                                                   const int* __restrict__ blk_nt, const unsigned char* __restrict__ loc,
+                                                   int maxt, Cx<float>* __restrict__ Z, size_t ldz)
+{
+    extern __shared__ float4 sk[];  // [maxt][maxt][9] (G re, G im, R, 1/R)
+    float4* sqf = sk + (size_t)maxt * maxt * 9;  // test points [maxt][3] (x y z -)
+    float4* snf = sqf + maxt * 3;                 // test normals [maxt]
+    float4* sqs = snf + maxt;                     // source points [maxt][3]
+    const int bf = blockIdx.y, bs = blockIdx.x;
+    const int ntf = blk_nt[bf], nts = blk_nt[bs];
+    const int* tf_ids = blk_tris + (size_t)bf * maxt;
+    const int* ts_ids = blk_tris + (size_t)bs * maxt;
+    for (int i = threadIdx.x; i < ntf * 3; i += blockDim.x) {
+        const float* q = tri_q3 + 9 * (size_t)tf_ids[i / 3] + 3 * (i % 3);
+        sqf[i] = make_float4(q[0], q[1], q[2], 0.0f);
+    }
+    for (int i = threadIdx.x; i < ntf; i += blockDim.x) {
+        const float* q = tri_n + 3 * (size_t)tf_ids[i];
+        snf[i] = make_float4(q[0], q[1], q[2], 0.0f);
+    }
+    for (int i = threadIdx.x; i < nts * 3; i += blockDim.x) {
+        const float* q = tri_q3 + 9 * (size_t)ts_ids[i / 3] + 3 * (i % 3);
+        sqs[i] = make_float4(q[0], q[1], q[2], 0.0f);
+    }
+    __syncthreads();
+    // phase 1: point-pair kernel values of every triangle pair (self pairs are
+    // computed too, never read: their entries come from the FP64 table)
+    for (int pr = threadIdx.x; pr < ntf * nts; pr += blockDim.x) {
+        const int tf = pr / nts, ts = pr - tf * nts;
+        float4* out = sk + ((size_t)tf * maxt + ts) * 9;
+#pragma unroll
+        for (int p = 0; p < 3; ++p) {
+            const float4 P = sqf[3 * tf + p];
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                const float4 Q = sqs[3 * ts + q];
+                V3<float> d = v3(P.x - Q.x, P.y - Q.y, P.z - Q.z);
+                float r = sqrtf(dot(d, d));
+                float rinv = 1.0f / r;
+                float sn, cs;
+                sincos_pi_taylor(r * c.kpi, &sn, &cs);
+                out[3 * p + q] = make_float4(cs * rinv, -sn * rinv, r, rinv);
+            }
+        }
+    }
+    __syncthreads();
+    // phase 2: the entries, z_entry's loop with the staged values
+    const int f = bf * FT + (threadIdx.x >> 4), s = bs * FT + (threadIdx.x & 15);
+    if (f >= n || s >= n) return;
+    const RwgPack<float>& F = rw[f];
+    const RwgPack<float>& S = rw[s];
+    if (!CFIE && c.edm_mode != 2) {
+        V3<float> fc = divr(v3(F.cen[0][0], F.cen[0][1], F.cen[0][2]) + v3(F.cen[1][0], F.cen[1][1], F.cen[1][2]), 2.0f);
+        V3<float> sc = divr(v3(S.cen[0][0], S.cen[0][1], S.cen[0][2]) + v3(S.cen[1][0], S.cen[1][1], S.cen[1][2]), 2.0f);
+        if (norm(fc - sc) > c.thr_edm) {
+            Z[(size_t)f * ldz + s] = c.edm_mode == 1 ? edm_value(F, S, c) : cx(0.0f, 0.0f);
+            return;
+        }
+    }
+    Cx<float> ze = cx(0.0f, 0.0f), zm = cx(0.0f, 0.0f);
+    double sr = 0.0, si = 0.0;
+#pragma unroll 1
+    for (int a = 0; a < 2; ++a) {
+        const int lf = loc[2 * (size_t)f + a];
+        float P[3][3], vf[3], nf[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            const float4 t = sqf[3 * lf + i];
+            P[i][0] = t.x;
+            P[i][1] = t.y;
+            P[i][2] = t.z;
+        }
+        const float4 nn = snf[lf];
+        nf[0] = nn.x;
+        nf[1] = nn.y;
+        nf[2] = nn.z;
+#pragma unroll
+        for (int j = 0; j < 3; ++j) vf[j] = F.v[a][j];
+#pragma unroll 1
+        for (int b = 0; b < 2; ++b) {
+            const float sgn = (a == b) ? 1.0f : -1.0f;
+            if (F.tri[a] == S.tri[b]) {
+                const int id = 9 * F.tri[a] + 3 * F.e[a] + S.e[b];
+                if (CFIE) {
+                    const double2 v = sing[id];
+                    sr += (double)sgn * v.x;
+                    si += (double)sgn * v.y;
+                } else {
+                    const double2 v = sing[3 * id + ((a == 0 && b == 0) ? 0 : 1)];
+                    const double2 g = sing[3 * id + 2];
+                    sr += (double)sgn * v.x + g.x;
+                    si += (double)sgn * v.y + g.y;
+                }
+                continue;
+            }
+            const int ls = loc[2 * (size_t)s + b];
+            float vs[3] = {S.v[b][0], S.v[b][1], S.v[b][2]};
+            Cx<float> e = cx(0.0f, 0.0f), m = cx(0.0f, 0.0f);
+            regular_pair_staged<CFIE>(P, sqs + 3 * ls, vf, vs, nf, sk + ((size_t)lf * maxt + ls) * 9, c, e, m);
+            ze.re += sgn * e.re;
+            ze.im += sgn * e.im;
+            if (CFIE) {
+                zm.re += sgn * m.re;
+                zm.im += sgn * m.im;
+            }
+        }
+    }
+    const float l = F.len * S.len;
+    Cx<float> out;
+    if (CFIE) {
+        const float re = -c.ce * ze.im + c.cm * zm.re + (float)sr;
+        const float im = c.ce * ze.re + c.cm * zm.im + (float)si;
+        out = cx(re * l, im * l);
+    } else {
+        const float kz = (float)c.coef_efie * l;
+        const float re = c.ce * ze.re + (float)sr, im = c.ce * ze.im + (float)si;
+        out = cx(-kz * im, kz * re);
+    }
+    Z[(size_t)f * ldz + s] = out;
+}
+
+// per-geometry plan of the tiled fill (host, once)
+static emfa_status_t tile_plan(Ctx* c, Geom* g, cudaStream_t st)
+{
+    if (g->tile_ready) return EMFA_OK;
+    const int n = g->n, nb = (n + FT - 1) / FT;
+    std::vector<std::vector<int>> lists(nb);
+    std::vector<unsigned char> loc(2 * (size_t)n);
+    int maxt = 1;
+    for (int b = 0; b < nb; ++b) {
+        auto& L = lists[b];
+        for (int u = b * FT; u < std::min(n, (b + 1) * FT); ++u)
+            for (int a = 0; a < 2; ++a) {
+                const int t = g->rwg[6 * (size_t)u + 4 + a];
+                int idx = -1;
+                for (int i = 0; i < (int)L.size(); ++i)
+                    if (L[i] == t) {
+                        idx = i;
+                        break;
+                    }
+                if (idx < 0) {
+                    idx = (int)L.size();
+                    L.push_back(t);
+                }
+                loc[2 * (size_t)u + a] = (unsigned char)idx;
+            }
+        maxt = std::max(maxt, (int)L.size());
+    }
+    std::vector<int> flat((size_t)nb * maxt, 0), cnt(nb);
+    for (int b = 0; b < nb; ++b) {
+        cnt[b] = (int)lists[b].size();
+        std::copy(lists[b].begin(), lists[b].end(), flat.begin() + (size_t)b * maxt);
+    }
+    EMFA_TRY(g->tile_tris.alloc(c, sizeof(int) * flat.size()));
+    EMFA_TRY(g->tile_nt.alloc(c, sizeof(int) * cnt.size()));
+    EMFA_TRY(g->tile_loc.alloc(c, loc.size()));
+    EMFA_CUDA(c, cudaMemcpyAsync(g->tile_tris.ptr, flat.data(), g->tile_tris.bytes, cudaMemcpyHostToDevice, st));
+    EMFA_CUDA(c, cudaMemcpyAsync(g->tile_nt.ptr, cnt.data(), g->tile_nt.bytes, cudaMemcpyHostToDevice, st));
+    EMFA_CUDA(c, cudaMemcpyAsync(g->tile_loc.ptr, loc.data(), g->tile_loc.bytes, cudaMemcpyHostToDevice, st));
+    EMFA_CUDA(c, cudaStreamSynchronize(st));  // host staging vectors go out of scope
+    g->tile_maxt = maxt;
+    g->tile_ready = true;
+    return EMFA_OK;
+}
+
+static size_t tile_smem(int maxt) { return sizeof(float4) * ((size_t)maxt * maxt * 9 + 7 * (size_t)maxt); }
+
+// ---------------------------------------------------------------------------
 // excitation: one thread per (incidence, RWG)
 // ---------------------------------------------------------------------------
 template <typename T, bool CFIE>
@@ -243,6 +477,32 @@ static emfa_status_t fill_z_t(Ctx* c, Geom* g, GeomDev<T>& d, const emfa_fill_pa
     EMFA_TRY(ctx_workspace(c, WS_FILL, sizeof(double2) * (size_t)g->nt * (cfie ? 9 : 27), &tab));
     EMFA_TRY(build_singular_table(c, g, p, (double2*)tab, st));
     FillConst<T> fc = make_fill_const<T>(p);
+    if (std::is_same<T, float>::value) {
+        // FP32: the tiled kernel
+        EMFA_TRY(tile_plan(c, g, st));
+        const size_t sm = tile_smem(g->tile_maxt);
+        EMFA_CUDA(c, cudaFuncSetAttribute(k_fill_tile<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        EMFA_CUDA(c, cudaFuncSetAttribute(k_fill_tile<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        const dim3 grd((g->n + FT - 1) / FT, (g->n + FT - 1) / FT);
+        const FillConst<float> fc32 = make_fill_const<float>(p);
+        {
+            TimedLaunch tl(c, KT_FILL_Z, st, (double)g->n * g->n);
+            if (cfie)
+                k_fill_tile<true><<<grd, 256, sm, st>>>(
+                    dptr<RwgPack<float>>(g->g32.rwg), g->n, fc32, (const double2*)tab, dptr<float>(g->g32.tri_q3),
+                    dptr<float>(g->g32.tri_n), dptr<int>(g->tile_tris), dptr<int>(g->tile_nt),
+                    dptr<unsigned char>(g->tile_loc), g->tile_maxt, reinterpret_cast<Cx<float>*>(Z), ldz);
+            else
+                k_fill_tile<false><<<grd, 256, sm, st>>>(
+                    dptr<RwgPack<float>>(g->g32.rwg), g->n, fc32, (const double2*)tab, dptr<float>(g->g32.tri_q3),
+                    dptr<float>(g->g32.tri_n), dptr<int>(g->tile_tris), dptr<int>(g->tile_nt),
+                    dptr<unsigned char>(g->tile_loc), g->tile_maxt, reinterpret_cast<Cx<float>*>(Z), ldz);
+        }
+        c->kernel_launches += 1;
+        EMFA_CUDA(c, cudaGetLastError());
+        EMFA_CUDA(c, cudaStreamSynchronize(st));
+        return EMFA_OK;
+    }
     dim3 blk(32, 8);
     dim3 grd((g->n + 31) / 32, (g->n + 7) / 8);
     {
@@ -390,3 +650,21 @@ emfa_status_t emfa_fill_v(emfa_ctx_t* ctx, emfa_geom_t* geom, const emfa_fill_pa
 }
 
 }  // extern "C"
+
+// diagnostics: the FP32 sin/cos(pi x) of the tiled fill, for accuracy tests
+namespace {
+__global__ void k_diag_sincospi(const float* __restrict__ x, int n, float* __restrict__ s, float* __restrict__ c)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) emfa::sincos_pi_taylor(x[i], s + i, c + i);
+}
+}  // namespace
+
+extern "C" emfa_status_t emfa_diag_sincospi(const float* x_dev, int n, float* s_dev, float* c_dev, void* stream)
+{
+    if (!x_dev || !s_dev || !c_dev || n <= 0) return EMFA_ERR_INVALID;
+    k_diag_sincospi<<<(n + 255) / 256, 256, 0, (cudaStream_t)stream>>>(x_dev, n, s_dev, c_dev);
+    EMFA_CUDA(nullptr, cudaGetLastError());
+    EMFA_CUDA(nullptr, cudaStreamSynchronize((cudaStream_t)stream));
+    return EMFA_OK;
+}

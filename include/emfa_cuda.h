@@ -293,6 +293,10 @@ emfa_status_t emfa_dense_rcs(emfa_ctx_t* ctx, const double* verts_host, int n_ve
                              int per_rhs_dirs, double* rcs_out_host, double* I_out_host,
                              emfa_solve_info_t* info);
 
+/* Diagnostics: sin and cos of pi*x as the FP32 fill evaluates them (its own
+ * Taylor-series evaluation), for accuracy tests; n device floats in and out. */
+emfa_status_t emfa_diag_sincospi(const float* x_dev, int n, float* s_dev, float* c_dev, void* stream);
+
 /* ---- binary dumps ------------------------------------------------------------ */
 /* Versioned binary dump of a matrix or vector (Z, V, I, operator arrays):
  * a 128-byte header (magic "EMFADUMP", version, dtype, rows, cols,

@@ -294,3 +294,22 @@ def test_residual_split_fp16(ctx, n, r):
     err_simt = np.linalg.norm(Rs - Rx, axis=1) / bn
     assert err.max() < 1e-6, (err.max(), err_simt.max())
     assert err.max() <= 2 * err_simt.max() + 1e-8, (err.max(), err_simt.max())
+
+
+def test_fill_sincospi_accuracy(ctx):
+    """The fill's FP32 sin/cos(pi x) (Taylor series after exact reduction to
+    |r| <= 1/4) against the exact values: within 2 ulp of 1 over the
+    arguments a fill meets (|x| up to a few hundred)."""
+    import ctypes
+    import torch
+    from emfa_gb300 import _lib
+    x = torch.linspace(-300.0, 300.0, 2_000_001, dtype=torch.float32, device="cuda")
+    s = torch.empty_like(x)
+    c = torch.empty_like(x)
+    st = _lib.lib().emfa_diag_sincospi(ctypes.c_void_p(x.data_ptr()), x.numel(), ctypes.c_void_p(s.data_ptr()),
+                                       ctypes.c_void_p(c.data_ptr()), None)
+    assert st == 0
+    xd = x.cpu().numpy().astype(np.float64)
+    es = np.abs(s.cpu().numpy() - np.sin(np.pi * xd)).max()
+    ec = np.abs(c.cpu().numpy() - np.cos(np.pi * xd)).max()
+    assert es < 1.2e-7 and ec < 1.2e-7, (es, ec)
