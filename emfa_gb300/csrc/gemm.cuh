@@ -46,6 +46,10 @@ emfa_status_t hsplit_prepare(Ctx* c, const void* Z, size_t ldz, int n, HPlanes* 
 // Y (complex64) = Z X (complex64): Zh times an FP16 copy of X scaled per
 // right-hand side; accuracy of a TF32 product at the FP16 tensor rate
 emfa_status_t hgemm_apply(Ctx* c, const HPlanes& h, const void* X, void* Y, int nrhs, cudaStream_t st);
+// Vout = scale[r] W (complex64, the Krylov normalisation), packed to FP16 in
+// the same pass, then Y = Z Vout; Y may alias W (W is consumed first)
+emfa_status_t hgemm_normalize_apply(Ctx* c, const HPlanes& h, const void* W, const double* scale,
+                                    const double* wmax, void* Vout, void* Y, int nrhs, cudaStream_t st);
 // R (complex128) = B - Z X for X complex128 and B complex64 (f32b) or complex128:
 // Zh Xh + Zh Xl + Zl Xh on the tensor cores, FP32 chunk sums reduced in FP64
 emfa_status_t hgemm_residual(Ctx* c, const HPlanes& h, const double2* X, const void* B, bool b_is_f32, double2* R,
@@ -66,6 +70,11 @@ struct LinOp {
                                    cudaStream_t st) = 0;
     // error word of asynchronous device-side checks (synchronises)
     virtual emfa_status_t check(Ctx*, cudaStream_t) { return EMFA_OK; }
+    // Vout = scale[r] W (the Krylov normalisation, iteration precision), then
+    // Y = A Vout; Y may alias W.  Operators that pack their input fuse both.
+    // wmax (optional): per RHS max |Re|, |Im| of W, known from the pass that produced it
+    virtual emfa_status_t normalize_apply(Ctx* c, const void* W, const double* scale, const double* wmax, void* Vout,
+                                          void* Y, int nrhs, cudaStream_t st);
 };
 
 emfa_status_t solve_op(Ctx* c, LinOp& A, const void* B, int nrhs, void* X, const emfa_solver_params_t* sp,

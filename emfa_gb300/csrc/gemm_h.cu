@@ -260,6 +260,39 @@ __global__ void __launch_bounds__(256) k_hpack_f32(const float2* __restrict__ X,
     }
 }
 
+// Krylov normalisation fused with the packing: v = scale[r] w in FP32 (the
+// scale rounded to FP32 once: an FP64 product per element would run on
+// GB300's 1/64-rate FP64 pipe), written to Vout and packed as k_hpack_f32
+// packs it.  The FP16 scale t_r comes from
+// wmax[r] * scale[r] (max |w| recorded by the pass that produced w), so every
+// element is independent: a grid over (chunks of 1024, RHS).
+__global__ void __launch_bounds__(256) k_hpack_scale(const float2* __restrict__ W, const double* __restrict__ scale,
+                                                     const double* __restrict__ wmax, int n, size_t ldh,
+                                                     float2* __restrict__ Vout, __half* __restrict__ Bh,
+                                                     float* __restrict__ inv_t)
+{
+    const int r = blockIdx.y;
+    const float sc = (float)scale[r];
+    int e = 0;
+    frexpf((float)(wmax[r] * scale[r]) * 1.0000002f, &e);  // rounding of sc can only raise max |v| by an ulp
+    const float t = ldexpf(1.f, 14 - e);
+    if (blockIdx.x == 0 && threadIdx.x == 0) inv_t[r] = ldexpf(1.f, e - 14);
+    const float2* w = W + (size_t)r * n;
+    float2* v = Vout + (size_t)r * n;
+    __half2* h0 = reinterpret_cast<__half2*>(Bh + (size_t)(2 * r) * ldh);
+    __half2* h1 = reinterpret_cast<__half2*>(Bh + (size_t)(2 * r + 1) * ldh);
+    const int k1 = min(n, (int)(blockIdx.x + 1) * 1024);
+#pragma unroll 4
+    for (int k = blockIdx.x * 1024 + threadIdx.x; k < k1; k += 256) {
+        const float2 x = w[k];
+        const float2 y = make_float2(x.x * sc, x.y * sc);
+        v[k] = y;
+        const __half hre = __float2half_rn(t * y.x), him = __float2half_rn(t * y.y);
+        h0[k] = __halves2half2(hre, __hneg(him));
+        h1[k] = __halves2half2(him, hre);
+    }
+}
+
 __global__ void __launch_bounds__(256) k_hpack_f64(const double2* __restrict__ X, int n, size_t ldh,
                                                    __half* __restrict__ Bh, __half* __restrict__ Bl,
                                                    float* __restrict__ inv_t)
@@ -595,20 +628,12 @@ emfa_status_t hsplit_prepare(Ctx* c, const void* Z, size_t ldz, int n, HPlanes* 
     return EMFA_OK;
 }
 
-emfa_status_t hgemm_apply(Ctx* c, const HPlanes& h, const void* X, void* Y, int nrhs, cudaStream_t st)
+// the inner-product GEMM on an already packed B plane
+static emfa_status_t hgemm_run(Ctx* c, const HPlanes& h, const __half* bh, const float* inv_t, void* Y, int nrhs,
+                               int* err, cudaStream_t st)
 {
     const int n = h.n;
     const size_t ldh = h.ldh;
-    void* wp = nullptr;
-    const size_t bplane = Carver::round(sizeof(__half) * ldh * 2 * (size_t)nrhs);
-    EMFA_TRY(ctx_workspace(c, WS_HGEMM, bplane + Carver::round(sizeof(float) * nrhs) + 256, &wp));
-    Carver cv{(char*)wp};
-    __half* bh = cv.take<__half>(ldh * 2 * (size_t)nrhs);
-    float* inv_t = cv.take<float>(nrhs);
-    int* err = nullptr;
-    EMFA_TRY(herr(c, &err));
-    th::k_hpack_f32<<<nrhs, 256, 0, st>>>((const float2*)X, n, ldh, bh, inv_t);
-    c->kernel_launches += 1;
     CUtensorMap ta, tb;
     // 256-row tiles (two M = 128 blocks sharing each B tile) once there are
     // enough of them to fill the SMs; 144 columns = 72 right-hand sides
@@ -621,6 +646,43 @@ emfa_status_t hgemm_apply(Ctx* c, const HPlanes& h, const void* X, void* Y, int 
     if (BN == 64) return launch_h<64, 1>(c, ta, tb, (float2*)Y, n, nrhs, h.inv_s, inv_t, err, st);
     if (tall) return launch_h<144, 2>(c, ta, tb, (float2*)Y, n, nrhs, h.inv_s, inv_t, err, st);
     return launch_h<144, 1>(c, ta, tb, (float2*)Y, n, nrhs, h.inv_s, inv_t, err, st);
+}
+
+static emfa_status_t hgemm_bplane(Ctx* c, const HPlanes& h, int nrhs, __half** bh, float** inv_t)
+{
+    void* wp = nullptr;
+    const size_t bplane = Carver::round(sizeof(__half) * h.ldh * 2 * (size_t)nrhs);
+    EMFA_TRY(ctx_workspace(c, WS_HGEMM, bplane + Carver::round(sizeof(float) * nrhs) + 256, &wp));
+    Carver cv{(char*)wp};
+    *bh = cv.take<__half>(h.ldh * 2 * (size_t)nrhs);
+    *inv_t = cv.take<float>(nrhs);
+    return EMFA_OK;
+}
+
+emfa_status_t hgemm_apply(Ctx* c, const HPlanes& h, const void* X, void* Y, int nrhs, cudaStream_t st)
+{
+    __half* bh = nullptr;
+    float* inv_t = nullptr;
+    EMFA_TRY(hgemm_bplane(c, h, nrhs, &bh, &inv_t));
+    int* err = nullptr;
+    EMFA_TRY(herr(c, &err));
+    th::k_hpack_f32<<<nrhs, 256, 0, st>>>((const float2*)X, h.n, h.ldh, bh, inv_t);
+    c->kernel_launches += 1;
+    return hgemm_run(c, h, bh, inv_t, Y, nrhs, err, st);
+}
+
+emfa_status_t hgemm_normalize_apply(Ctx* c, const HPlanes& h, const void* W, const double* scale,
+                                    const double* wmax, void* Vout, void* Y, int nrhs, cudaStream_t st)
+{
+    __half* bh = nullptr;
+    float* inv_t = nullptr;
+    EMFA_TRY(hgemm_bplane(c, h, nrhs, &bh, &inv_t));
+    int* err = nullptr;
+    EMFA_TRY(herr(c, &err));
+    th::k_hpack_scale<<<dim3((h.n + 1023) / 1024, nrhs), 256, 0, st>>>((const float2*)W, scale, wmax, h.n, h.ldh,
+                                                                       (float2*)Vout, bh, inv_t);
+    c->kernel_launches += 1;
+    return hgemm_run(c, h, bh, inv_t, Y, nrhs, err, st);
 }
 
 emfa_status_t hgemm_residual(Ctx* c, const HPlanes& h, const double2* X, const void* B, bool b_is_f32, double2* R,

@@ -346,14 +346,14 @@ __global__ void __launch_bounds__(256) k_vupdate(const Cx<T>* __restrict__ V, si
     extern __shared__ unsigned char dyn_smem[];
     A* hs0 = reinterpret_cast<A*>(dyn_smem);
     A* hs1 = hs0 + nv;
-    __shared__ double red[8];
+    __shared__ double red[8], redm[8];
     for (int i = threadIdx.x; i < nv; i += blockDim.x) {
         double2 t = h[(size_t)i * nrhs + r];
         hs0[i] = (A)t.x;
         hs1[i] = (A)t.y;
     }
     __syncthreads();
-    A nr = 0;
+    A nr = 0, mx = 0;
     const int k0 = blk * VCHUNK, k1 = min(n, k0 + VCHUNK);
     for (int k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
         const Cx<T>* vk = V + base + k;
@@ -380,17 +380,31 @@ __global__ void __launch_bounds__(256) k_vupdate(const Cx<T>* __restrict__ V, si
         w.re = (T)((A)w.re - sr);
         w.im = (T)((A)w.im - si);
         W[base + k] = w;
-        if (NORM) nr += (A)w.re * (A)w.re + (A)w.im * (A)w.im;
+        if (NORM) {
+            nr += (A)w.re * (A)w.re + (A)w.im * (A)w.im;
+            mx = fmax(mx, fmax(fabs((A)w.re), fabs((A)w.im)));
+        }
     }
     if (NORM) {
+        // |w|^2 and max |Re|, |Im| of the block (the max sets the FP16 scale
+        // of the packed copy the next product reads)
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) nr += __shfl_xor_sync(0xffffffffu, nr, o);
-        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = (double)nr;
+        for (int o = 16; o > 0; o >>= 1) {
+            nr += __shfl_xor_sync(0xffffffffu, nr, o);
+            mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        }
+        if ((threadIdx.x & 31) == 0) {
+            red[threadIdx.x >> 5] = (double)nr;
+            redm[threadIdx.x >> 5] = (double)mx;
+        }
         __syncthreads();
         if (threadIdx.x == 0) {
-            double t = 0;
-            for (int q = 0; q < (int)(blockDim.x >> 5); ++q) t += red[q];
-            pnorm[(size_t)r * nblk + blk] = make_double2(t, 0.0);
+            double t = 0, tm = 0;
+            for (int q = 0; q < (int)(blockDim.x >> 5); ++q) {
+                t += red[q];
+                tm = fmax(tm, redm[q]);
+            }
+            pnorm[(size_t)r * nblk + blk] = make_double2(t, tm);
         }
     }
 }
@@ -426,18 +440,24 @@ __global__ void k_update_x2(const Cx<T>* __restrict__ V, size_t vstride, int nvm
     X[o] = make_double2(x.x + (double)sr, x.y + (double)si);
 }
 
-// per-RHS: finish Arnoldi column j, rotate, test convergence
+// per-RHS: finish Arnoldi column j, rotate, test convergence.  A serial FP64
+// chain per right-hand side: one RHS per warp (lane 0) spreads the chains
+// over the SMs' FP64 units instead of packing 32 of them into one warp.
 __global__ void k_arnoldi_finish(GmresDev s, int j, const double2* __restrict__ pnorm, int nblk, int two_pass)
 {
-    int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= s.nrhs) return;
+    const int r = (int)(((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    if ((threadIdx.x & 31) != 0 || r >= s.nrhs) return;
     const int m = s.m;
     if (!s.active[r]) {
         s.scale[r] = 0.0;
         return;
     }
-    double nr2 = 0.0;
-    for (int b = 0; b < nblk; ++b) nr2 += pnorm[(size_t)r * nblk + b].x;
+    double nr2 = 0.0, wm = 0.0;
+    for (int b = 0; b < nblk; ++b) {
+        nr2 += pnorm[(size_t)r * nblk + b].x;
+        wm = fmax(wm, pnorm[(size_t)r * nblk + b].y);
+    }
+    s.wmax[r] = wm;
     double beta = sqrt(nr2);
     double2* H = s.H + (size_t)r * (m + 1) * m;
     // column j of H: Gram-Schmidt coefficients (sum of both passes for CGS2)
@@ -507,19 +527,23 @@ __global__ void k_scale_store(const TI* __restrict__ W, const double* __restrict
 {
     size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     size_t tot = (size_t)n * nrhs;
+    using R = decltype(out->re);
     for (; id < tot; id += (size_t)gridDim.x * blockDim.x) {
         int r = (int)(id / n);
-        double sc = scale[r];
+        // an FP32 basis is scaled in FP32: FP64 products per element would
+        // run on GB300's 1/64-rate FP64 pipe
+        const R sc = (R)scale[r];
         double2 w = ld2(W + id);
-        out[id] = TO{(decltype(out->re))(w.x * sc), (decltype(out->re))(w.y * sc)};
+        out[id] = TO{(R)w.x * sc, (R)w.y * sc};
     }
 }
 
 // per-RHS back substitution of the rotated Hessenberg system
 __global__ void k_backsolve(GmresDev s)
 {
-    int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= s.nrhs) return;
+    // one RHS per warp (lane 0): the FP64 chains of the RHS spread over the SMs
+    const int r = (int)(((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    if ((threadIdx.x & 31) != 0 || r >= s.nrhs) return;
     const int m = s.m;
     int jl = s.jlen[r];
     const double2* H = s.H + (size_t)r * (m + 1) * m;
@@ -662,7 +686,7 @@ static emfa_status_t gmres_t(Ctx* c, LinOp& A, const void* B, int nrhs, double2*
                         Carver::round(sizeof(double2) * (size_t)nrhs * (m + 1)) * 2 +
                         Carver::round(sizeof(double2) * (size_t)nrhs * (m + 1) * std::max(nblk, (n + VCHUNK - 1) / VCHUNK)) +
                         Carver::round(sizeof(double2) * (size_t)nrhs * std::max(nblk, (n + VCHUNK - 1) / VCHUNK)) +
-                        Carver::round(sizeof(double) * 4 * (size_t)nrhs) + Carver::round(sizeof(int) * 2 * (size_t)nrhs) +
+                        Carver::round(sizeof(double) * 5 * (size_t)nrhs) + Carver::round(sizeof(int) * 2 * (size_t)nrhs) +
                         Carver::round(sizeof(int) * 4) + 4096;
     void* wsp = nullptr;
     EMFA_TRY(ctx_workspace(c, WS_KRYLOV, need, &wsp));
@@ -685,10 +709,11 @@ static emfa_status_t gmres_t(Ctx* c, LinOp& A, const void* B, int nrhs, double2*
     const int pb = std::max(nblk, (n + VCHUNK - 1) / VCHUNK);
     double2* partial = cv.take<double2>((size_t)nrhs * (m + 1) * pb);
     double2* pnorm = cv.take<double2>((size_t)nrhs * pb);
-    s.bnorm = cv.take<double>(4 * (size_t)nrhs);
+    s.bnorm = cv.take<double>(5 * (size_t)nrhs);
     s.scale = s.bnorm + nrhs;
     s.est = s.scale + nrhs;
     s.true_res = s.est + nrhs;
+    s.wmax = s.true_res + nrhs;
     s.jlen = cv.take<int>(2 * (size_t)nrhs);
     s.active = s.jlen + nrhs;
     s.counters = cv.take<int>(4);
@@ -728,9 +753,8 @@ static emfa_status_t gmres_t(Ctx* c, LinOp& A, const void* B, int nrhs, double2*
         k_scale_store<Cx<T>, double2><<<grid1(vec), 256, 0, st>>>(R, s.scale, n, nrhs, V);
         int steps = 0;
         for (int j = 0; j < m; ++j) {
-            Cx<T>* Vj = V + (size_t)j * vec;
-            // W = A V_j
-            EMFA_TRY(A.apply(c, Vj, W, nrhs, st));
+            // W = A V_j (for j > 0 done by normalize_apply at the end of the previous step)
+            if (j == 0) EMFA_TRY(A.apply(c, V, W, nrhs, st));
             // CGS1: h = V^H W; W -= V h with |W|^2.  CGS2 repeats the pair
             // (h2 = V^H W; W -= V h2) and H gets h + h2.
             const dim3 vg(vblk, nrhs);
@@ -748,17 +772,18 @@ static emfa_status_t gmres_t(Ctx* c, LinOp& A, const void* B, int nrhs, double2*
                 k_vupdate<T, true><<<vg, 256, 2 * nv * sizeof(typename Acc<T>::type), st>>>(V, vec, nv, s.hcol, W, n, nrhs, vblk, pnorm);
             }
             EMFA_CUDA(c, cudaMemsetAsync(s.counters, 0, sizeof(int), st));
-            k_arnoldi_finish<<<(nrhs + 127) / 128, 128, 0, st>>>(s, j, pnorm, vblk, two_pass ? 1 : 0);
-            k_scale_store<Cx<T>, Cx<T>><<<grid1(vec), 256, 0, st>>>(W, s.scale, n, nrhs, V + (size_t)(j + 1) * vec);
+            k_arnoldi_finish<<<(nrhs * 32 + 127) / 128, 128, 0, st>>>(s, j, pnorm, vblk, two_pass ? 1 : 0);
             EMFA_CUDA(c, cudaMemcpyAsync(host_cnt, s.counters, sizeof(int), cudaMemcpyDeviceToHost, st));
             EMFA_CUDA(c, cudaStreamSynchronize(st));
-            c->kernel_launches += 5;
+            c->kernel_launches += 4;
             ++steps;
             if (host_cnt[0] == 0) break;
+            // V_{j+1} = W / beta, then W = A V_{j+1} (one pass for operators that pack)
+            EMFA_TRY(A.normalize_apply(c, W, s.scale, s.wmax, V + (size_t)(j + 1) * vec, W, nrhs, st));
         }
         total_iters += steps;
         EMFA_TRY(A.check(c, st));
-        k_backsolve<<<(nrhs + 127) / 128, 128, 0, st>>>(s);
+        k_backsolve<<<(nrhs * 32 + 127) / 128, 128, 0, st>>>(s);
         k_update_x2<T><<<dim3((n + 255) / 256, nrhs), 256, 2 * std::max(1, steps) * sizeof(typename Acc<T>::type), st>>>(
             V, vec, steps, s.y, s.jlen, X, n, nrhs);
         c->kernel_launches += 2;
@@ -1089,6 +1114,20 @@ emfa_status_t solve_op(Ctx* c, LinOp& A, const void* B, int nrhs, void* X, const
     return gmres_t<float>(c, A, B, nrhs, (double2*)X, sp, info, st);
 }
 
+emfa_status_t LinOp::normalize_apply(Ctx* c, const void* W, const double* scale, const double*, void* Vout,
+                                     void* Y, int nrhs, cudaStream_t st)
+{
+    const size_t vec = (size_t)n * nrhs;
+    if (prec == EMFA_F64)
+        k_scale_store<Cx<double>, Cx<double>><<<grid1(vec), 256, 0, st>>>((const Cx<double>*)W, scale, n, nrhs,
+                                                                           (Cx<double>*)Vout);
+    else
+        k_scale_store<Cx<float>, Cx<float>><<<grid1(vec), 256, 0, st>>>((const Cx<float>*)W, scale, n, nrhs,
+                                                                         (Cx<float>*)Vout);
+    c->kernel_launches += 1;
+    return apply(c, Vout, Y, nrhs, st);
+}
+
 // Dense impedance matrix as a Krylov operator.  Mixed path: inner products
 // on the tensor cores (split FP16 or TF32) or FP32 CUDA cores; refinement
 // residual from the three-term split-FP16 product (F16X) or FP32 products
@@ -1123,6 +1162,13 @@ struct DenseOp : LinOp {
         k_to_f32<<<grid1(vec), 256, 0, st>>>(X, xt, vec);
         c->kernel_launches += 1;
         return cgemm_f32_chunked(c, Z, n, xt, n, nrhs, B, R, st);  // R = B - Z X
+    }
+    emfa_status_t normalize_apply(Ctx* c, const void* W, const double* scale, const double* wmax, void* Vout,
+                                  void* Y, int nrhs, cudaStream_t st) override
+    {
+        if (prec == EMFA_F32 && mode == F16X && wmax)
+            return hgemm_normalize_apply(c, hp, W, scale, wmax, Vout, Y, nrhs, st);
+        return LinOp::normalize_apply(c, W, scale, wmax, Vout, Y, nrhs, st);
     }
     emfa_status_t check(Ctx* c, cudaStream_t st) override
     {

@@ -14,6 +14,7 @@ struct GmresDev {
     double2* y;      // m x nrhs  solution of the small system (also CGS scratch)
     double2* hcol;   // (m+1) x nrhs  Arnoldi column being built
     double* bnorm;   // nrhs  ||b||
+    double* wmax;    // nrhs  max |Re|, |Im| of the orthogonalised w of the step
     double* scale;   // nrhs  1/beta of the vector being normalised (0 = inactive)
     double* est;     // nrhs  rotated residual estimate
     double* true_res;// nrhs  true relative residual at the last restart
