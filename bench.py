@@ -211,9 +211,8 @@ def measured_peaks():
 
 
 # DRAM bytes (read + write) per launch of the split-FP16 inner product on the
-# 7680 x 360 job, from one ncu capture (profiles/k_hgemm_k_hresid_7680x360.md);
-# None until the 256-row-tile kernel is captured.
-GEMM_TRAFFIC_BYTES = None
+# 7680 x 360 job, from one ncu capture (profiles/k_hgemm_k_hresid_7680x360.md).
+GEMM_TRAFFIC_BYTES = 261.3e6
 
 
 _ARGS = {}

@@ -48,7 +48,10 @@ __device__ __forceinline__ void sincos_pi(float x, float* s, float* c) { sincosp
 // then sin(pi r) = r (pi - pi^3/6 r^2 + ... + pi^9/9! r^8) and
 // cos(pi r) = 1 - pi^2/2 r^2 + ... - pi^10/10! r^10 (the first omitted terms
 // are below 2e-9 at |pi r| = pi/4), and the quadrant n mod 4 picks and signs
-// them.  All FP32: no branch, no FP64.  About 1.5 ulp against the exact values.
+// them.  All FP32 and integer: no branch, no FP64 and no float/int
+// conversion (those issue on GB300's slow FP64/conversion pipe): 2x is
+// rounded by adding 1.5 * 2^23, whose low mantissa bits then hold n mod 4.
+// Valid for |x| < 2^21.  About 1.5 ulp against the exact values.
 namespace taylor {
 constexpr double PI = 3.14159265358979323846;
 constexpr float S1 = (float)PI, S3 = (float)(-PI * PI * PI / 6.0), S5 = (float)(PI * PI * PI * PI * PI / 120.0);
@@ -63,12 +66,14 @@ constexpr float C10 = (float)(-PI * PI * PI * PI * PI * PI * PI * PI * PI * PI /
 __device__ __forceinline__ void sincos_pi_taylor(float x, float* s, float* c)
 {
     using namespace taylor;
-    const float n = rintf(2.0f * x);
+    const float big = 12582912.0f;  // 1.5 * 2^23
+    const float t = fmaf(2.0f, x, big);  // big + rint(2x), one rounding
+    const float n = t - big;            // rint(2x), exact
     const float r = fmaf(-0.5f, n, x);
     const float u = r * r;
     const float sv = r * fmaf(fmaf(fmaf(fmaf(S9, u, S7), u, S5), u, S3), u, S1);
     const float cv = fmaf(fmaf(fmaf(fmaf(fmaf(C10, u, C8), u, C6), u, C4), u, C2), u, 1.0f);
-    const int q = (int)n & 3;
+    const int q = __float_as_int(t) & 3;
     float a = (q & 1) ? cv : sv;
     float b = (q & 1) ? sv : cv;
     if (q & 2) a = -a;
