@@ -37,7 +37,8 @@ class SolverParams(ctypes.Structure):
 
 
 class MlfmaParams(ctypes.Structure):
-    _fields_ = [("freq", ctypes.c_double), ("alpha", ctypes.c_double), ("box_threshold", ctypes.c_double)]
+    _fields_ = [("freq", ctypes.c_double), ("alpha", ctypes.c_double), ("box_threshold", ctypes.c_double),
+                ("precond", ctypes.c_int), ("row_threshold", ctypes.c_double), ("col_threshold", ctypes.c_double)]
 
 
 class Request(ctypes.Structure):
@@ -116,6 +117,8 @@ _SIGS = {
     "emfa_mlfma_plan": (ci, [vp, ci, vp, ci, ctypes.POINTER(MlfmaParams), ip, vp, ci, vp, vp]),
     "emfa_mlfma_create": (ci, [vp, vp, ctypes.POINTER(MlfmaParams), ctypes.POINTER(vp)]),
     "emfa_mlfma_destroy": (ci, [vp]),
+    "emfa_mlfma_precond_csr": (ci, [vp, ctypes.POINTER(sz), vp, vp, vp]),
+    "emfa_mlfma_precond_lists": (ci, [vp, ip, ctypes.POINTER(sz), ctypes.POINTER(sz), vp, vp, vp, vp, vp]),
     "emfa_mlfma_info": (ci, [vp, ip, vp, vp, ctypes.POINTER(sz), vp]),
     "emfa_mlfma_apply": (ci, [vp, vp, vp, ci, vp]),
     "emfa_mlfma_apply_part": (ci, [vp, vp, vp, ci, vp]),

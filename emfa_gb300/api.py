@@ -266,8 +266,10 @@ def monostatic_dirs(angles) -> np.ndarray:
 # ---------------------------------------------------------------------------
 # MLFMA
 # ---------------------------------------------------------------------------
-def mlfma_params(freq=3e8, alpha=0.5, box_threshold=0.25) -> L.MlfmaParams:
-    return L.MlfmaParams(float(freq), float(alpha), float(box_threshold))
+def mlfma_params(freq=3e8, alpha=0.5, box_threshold=0.25, precond=False, row_threshold=0.9,
+                 col_threshold=0.87) -> L.MlfmaParams:
+    return L.MlfmaParams(float(freq), float(alpha), float(box_threshold), int(bool(precond)), float(row_threshold),
+                         float(col_threshold))
 
 
 def mlfma_plan(mesh: TriMesh, rwg: np.ndarray, mp: L.MlfmaParams):
@@ -357,6 +359,34 @@ class Mlfma:
         X = torch.empty_like(Xbox)
         self.ctx.check(L.lib().emfa_mlfma_unpermute(self.h, _ptr(Xbox), Xbox.shape[0], _ptr(X), None))
         return X
+
+    def precond_csr(self):
+        """SAI preconditioner as (ptr, col, val complex64) over box-order rows, or None."""
+        nnz = ctypes.c_size_t()
+        self.ctx.check(L.lib().emfa_mlfma_precond_csr(self.h, ctypes.byref(nnz), None, None, None))
+        if nnz.value == 0:
+            return None
+        ptr = np.zeros(self.geom.n + 1, dtype=np.int32)
+        col = np.zeros(nnz.value, dtype=np.int32)
+        val = np.zeros(nnz.value, dtype=np.complex64)
+        self.ctx.check(L.lib().emfa_mlfma_precond_csr(self.h, ctypes.byref(nnz), ptr.ctypes.data_as(vp),
+                                                      col.ctypes.data_as(vp), val.ctypes.data_as(vp)))
+        return ptr, col, val
+
+    def precond_lists(self):
+        """Per-box SAI lists: (rptr, rows, cptr, cols, own)."""
+        nb, nr, nc = ctypes.c_int(), ctypes.c_size_t(), ctypes.c_size_t()
+        f = L.lib().emfa_mlfma_precond_lists
+        self.ctx.check(f(self.h, ctypes.byref(nb), ctypes.byref(nr), ctypes.byref(nc), None, None, None, None, None))
+        rptr = np.zeros(nb.value + 1, dtype=np.int32)
+        rows = np.zeros(nr.value, dtype=np.int32)
+        cptr = np.zeros(nb.value + 1, dtype=np.int32)
+        cols = np.zeros(nc.value, dtype=np.int32)
+        own = np.zeros(nb.value, dtype=np.int32)
+        self.ctx.check(f(self.h, ctypes.byref(nb), ctypes.byref(nr), ctypes.byref(nc), rptr.ctypes.data_as(vp),
+                         rows.ctypes.data_as(vp), cptr.ctypes.data_as(vp), cols.ctypes.data_as(vp),
+                         own.ctypes.data_as(vp)))
+        return rptr, rows, cptr, cols, own
 
 
 # ---------------------------------------------------------------------------

@@ -518,14 +518,13 @@ void MLFMA::init(ConfigLoader* ploader)
     tol_ = ploader->getIterationThreshold();
     max_iter_ = ploader->getMaxIterationNum();
     precond_ = ploader->getPreconditioningSwitch();
-    ploader->getRowThreshold();
-    ploader->getColThreshold();
+    const float row_thr = ploader->getRowThreshold();
+    const float col_thr = ploader->getColThreshold();
     threshold_ = ploader->getMLFMABoxThreshold();
     ploader->getThreadNumber();
     ploader->getTaskFactor();
-    if (precond_)
-        logger_ << "    WARNING: preconditioning (SAI) is not available in this build; solving unpreconditioned\n";
-    emfa_mlfma_params_t mp{(double)incidence_.freq, (double)alpha_, (double)threshold_};
+    emfa_mlfma_params_t mp{(double)incidence_.freq, (double)alpha_, (double)threshold_, precond_ ? 1 : 0,
+                           (double)row_thr, (double)col_thr};
     check(emfa_mlfma_create(ctx_, geom_, &mp, &ml_), ctx_, "MLFMA init");
     check(emfa_mlfma_info(ml_, &levels_, nullptr, nullptr, nullptr, nullptr), ctx_, "MLFMA info");
     logger_ << ploader->getReport();

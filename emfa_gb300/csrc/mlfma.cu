@@ -171,6 +171,12 @@ struct emfa_mlfma {
     emfa::DevBuf near_val;         // float2 [nnz]
     size_t nnz = 0;
     emfa::DevBuf tmp_in, tmp_out;  // complex64 scratch for residuals
+    // SAI preconditioner P (CSR over box-order rows), built when p.precond
+    bool precond = false;
+    size_t sai_nnz = 0;
+    std::vector<int> sai_rptr, sai_rows, sai_cptr, sai_cols, sai_own;  // host copies of the lists
+    emfa::DevBuf csr_ptr, csr_col, csr_val;  // int [n+1], int [nnz], float2 [nnz]
+    emfa::DevBuf pre_tmp, pre_b;             // complex64 scratch: Z x, P b
 };
 
 namespace emfa {
@@ -394,6 +400,160 @@ __global__ void k_f64_to_f32(const double2* __restrict__ X, float2* __restrict__
 }
 
 // ---------------------------------------------------------------------------
+// SAI preconditioner (MLFMA::parallelPreconditioner, EMSolver/MLFMA.cpp:1346-1391)
+// ---------------------------------------------------------------------------
+// near-field entry Z(uf, us) in box order, zero when the boxes are not near
+__device__ __forceinline__ float2 near_entry(int uf, int us, const int* __restrict__ box_of,
+                                             const int* __restrict__ box_off, const int* __restrict__ near_ptr,
+                                             const int* __restrict__ near_box, const int* __restrict__ near_col,
+                                             const int* __restrict__ row_cols, const size_t* __restrict__ row_base,
+                                             const float2* __restrict__ val)
+{
+    const int bf = box_of[uf], bs = box_of[us];
+    for (int sl = near_ptr[bf]; sl < near_ptr[bf + 1]; ++sl)
+        if (near_box[sl] == bs)
+            return val[row_base[bf] + (size_t)(uf - box_off[bf]) * row_cols[bf] + near_col[sl] + (us - box_off[bs])];
+    return make_float2(0.f, 0.f);
+}
+
+__device__ __forceinline__ float2 cconjmul(float2 a, float2 b)  // conj(a) b
+{
+    return make_float2(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x);
+}
+
+__device__ __forceinline__ float2 warp_sum2(float2 v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+        v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+    }
+    return v;
+}
+
+// One CTA (4 warps) per finest box: A = Z_near(rows, cols) (m x n, column
+// major in shared memory), complex Householder QR, then for each unknown u
+// of the box the least-squares column P(cols, u) = R^-1 Q^H e_(own + u),
+// written to its CSR slot.  FP32, as the reference's value_t.
+__global__ void __launch_bounds__(128) k_sai(const int* __restrict__ rptr, const int* __restrict__ rows,
+                                             const int* __restrict__ cptr, const int* __restrict__ cols,
+                                             const int* __restrict__ own, const int* __restrict__ box_cnt,
+                                             const size_t* __restrict__ ebase, const int* __restrict__ dest,
+                                             const int* __restrict__ box_of, const int* __restrict__ box_off,
+                                             const int* __restrict__ near_ptr, const int* __restrict__ near_box,
+                                             const int* __restrict__ near_col, const int* __restrict__ row_cols,
+                                             const size_t* __restrict__ row_base, const float2* __restrict__ val,
+                                             int max_rows, int max_cols, float2* __restrict__ csr_val)
+{
+    extern __shared__ float2 sm[];
+    const int b = blockIdx.x;
+    const int m = rptr[b + 1] - rptr[b], n = cptr[b + 1] - cptr[b], nb = box_cnt[b], o = own[b];
+    const int* R = rows + rptr[b];
+    const int* C = cols + cptr[b];
+    float2* A = sm;                                        // [n][m]
+    float2* rd = A + (size_t)max_rows * max_cols;          // R diagonal [n]
+    float* tau = reinterpret_cast<float*>(rd + max_cols);  // [n]
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float2* bv = reinterpret_cast<float2*>(tau + max_cols + (max_cols & 1)) + (size_t)warp * (max_rows + max_cols);
+    float2* yv = bv + max_rows;
+    for (int idx = threadIdx.x; idx < m * n; idx += blockDim.x) {
+        const int f = idx % m, s = idx / m;
+        A[idx] = near_entry(R[f], C[s], box_of, box_off, near_ptr, near_box, near_col, row_cols, row_base, val);
+    }
+    __syncthreads();
+    for (int j = 0; j < n; ++j) {
+        float2* aj = A + (size_t)j * m;
+        if (warp == 0) {
+            float xs = 0.f;
+            for (int i = j + lane; i < m; i += 32) xs += aj[i].x * aj[i].x + aj[i].y * aj[i].y;
+#pragma unroll
+            for (int q = 16; q > 0; q >>= 1) xs += __shfl_xor_sync(0xffffffffu, xs, q);
+            if (lane == 0) {
+                // H_j x = al e_j with al = -e^(i arg x0) |x|: no cancellation in v0
+                const float xn = sqrtf(xs);
+                const float2 x0 = aj[j];
+                const float ax = sqrtf(x0.x * x0.x + x0.y * x0.y);
+                const float2 al = ax > 0.f ? make_float2(-x0.x / ax * xn, -x0.y / ax * xn) : make_float2(-xn, 0.f);
+                const float2 v0 = make_float2(x0.x - al.x, x0.y - al.y);
+                const float vn = xs - ax * ax + v0.x * v0.x + v0.y * v0.y;
+                aj[j] = v0;
+                rd[j] = al;
+                tau[j] = vn > 0.f ? 2.f / vn : 0.f;
+            }
+        }
+        __syncthreads();
+        const float t = tau[j];
+        for (int k = j + 1 + warp; k < n; k += 4) {
+            float2* ak = A + (size_t)k * m;
+            float2 s = make_float2(0.f, 0.f);
+            for (int i = j + lane; i < m; i += 32) {
+                const float2 p = cconjmul(aj[i], ak[i]);
+                s.x += p.x;
+                s.y += p.y;
+            }
+            s = warp_sum2(s);
+            for (int i = j + lane; i < m; i += 32) {
+                const float2 v = aj[i];
+                ak[i].x -= t * (s.x * v.x - s.y * v.y);
+                ak[i].y -= t * (s.x * v.y + s.y * v.x);
+            }
+        }
+        __syncthreads();
+    }
+    for (int u = warp; u < nb; u += 4) {
+        for (int i = lane; i < m; i += 32) bv[i] = make_float2(i == o + u ? 1.f : 0.f, 0.f);
+        __syncwarp();
+        for (int j = 0; j < n; ++j) {  // b <- H_j b: Q^H e
+            const float2* aj = A + (size_t)j * m;
+            float2 s = make_float2(0.f, 0.f);
+            for (int i = j + lane; i < m; i += 32) {
+                const float2 p = cconjmul(aj[i], bv[i]);
+                s.x += p.x;
+                s.y += p.y;
+            }
+            s = warp_sum2(s);
+            const float t = tau[j];
+            for (int i = j + lane; i < m; i += 32) {
+                const float2 v = aj[i];
+                bv[i].x -= t * (s.x * v.x - s.y * v.y);
+                bv[i].y -= t * (s.x * v.y + s.y * v.x);
+            }
+            __syncwarp();
+        }
+        for (int i = n - 1; i >= 0; --i) {  // R y = b (R above the diagonal in A, diagonal in rd)
+            float2 s = make_float2(0.f, 0.f);
+            for (int k = i + 1 + lane; k < n; k += 32) {
+                const float2 r = A[(size_t)k * m + i], y = yv[k];
+                s.x += r.x * y.x - r.y * y.y;
+                s.y += r.x * y.y + r.y * y.x;
+            }
+            s = warp_sum2(s);
+            if (lane == 0) {
+                const float2 d = rd[i];
+                const float dd = d.x * d.x + d.y * d.y;
+                const float2 num = make_float2(bv[i].x - s.x, bv[i].y - s.y);
+                yv[i] = dd > 0.f ? make_float2((num.x * d.x + num.y * d.y) / dd, (num.y * d.x - num.x * d.y) / dd)
+                                 : make_float2(0.f, 0.f);
+            }
+            __syncwarp();
+        }
+        for (int c = lane; c < n; c += 32) csr_val[dest[ebase[b] + (size_t)u * n + c]] = yv[c];
+        __syncwarp();
+    }
+}
+
+// y = P x, P in CSR (row per thread)
+__global__ void k_sai_apply(const int* __restrict__ ptr, const int* __restrict__ col, const float2* __restrict__ val,
+                            const float2* __restrict__ x, int n, float2* __restrict__ y)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float2 acc = make_float2(0.f, 0.f);
+    for (int k = ptr[i]; k < ptr[i + 1]; ++k) acc = caddf(acc, cmulf(val[k], x[col[k]]));
+    y[i] = acc;
+}
+
+// ---------------------------------------------------------------------------
 // host build
 // ---------------------------------------------------------------------------
 template <typename T>
@@ -415,6 +575,7 @@ struct Plan {
     std::vector<std::vector<float>> gt, gp, gw, kd;
     std::vector<int> perm, box_of, off, cnt;
     std::vector<float> cen;
+    std::vector<float> cp;  // RWG centres (v1 + v2) / 2, RWG order
 };
 
 static bool build_plan(const std::vector<double>& verts, int nv, const std::vector<int>& rwg, int n,
@@ -456,7 +617,8 @@ static bool build_plan(const std::vector<double>& verts, int nv, const std::vect
     float root[3];
     for (int d = 0; d < 3; ++d) root[d] = (bmin[d] + bmax[d]) * 0.5f;
     // RWG centres: (v1 + v2) / 2
-    std::vector<float> cp(3 * (size_t)n);
+    std::vector<float>& cp = P.cp;
+    cp.assign(3 * (size_t)n, 0.f);
     for (int u = 0; u < n; ++u)
         for (int d = 0; d < 3; ++d) cp[3 * u + d] = (vf[3 * rwg[6 * u] + d] + vf[3 * rwg[6 * u + 1] + d]) * 0.5f;
     // octree (buildBox)
@@ -571,6 +733,105 @@ static bool build_plan(const std::vector<double>& verts, int nv, const std::vect
         }
     }
     return true;
+}
+
+// SAI lists (MLFMA::setBoxParameter and parallelPreconditioner, EMSolver/MLFMA.cpp:719-741,1346-1370):
+// per finest box, the near unknowns whose centre lies within row / col
+// threshold x finest box length of the box centre, in near-box order; then
+// the batched QR on the device and P in CSR over box-order rows
+static emfa_status_t sai_build(emfa_mlfma* M, const Plan& P, cudaStream_t st)
+{
+    Ctx* c = M->ctx;
+    if (!(M->p.row_threshold >= 0.87) || !(M->p.col_threshold >= 0.87)) {
+        set_error(c, "MLFMA preconditioner: row_threshold and col_threshold must be >= 0.87 (a box's own "
+                     "unknowns lie within sqrt(3)/2 box lengths of its centre)");
+        return EMFA_ERR_INVALID;
+    }
+    const auto& fin = P.lb[P.L];
+    const float bl = P.blen[P.L];
+    const float thr_r = (float)M->p.row_threshold * bl, thr_c = (float)M->p.col_threshold * bl;
+    const int nbox = (int)fin.size(), n = M->n;
+    auto& rptr = M->sai_rptr;
+    auto& rows = M->sai_rows;
+    auto& cptr = M->sai_cptr;
+    auto& cols = M->sai_cols;
+    auto& own = M->sai_own;
+    rptr.assign(1, 0);
+    cptr.assign(1, 0);
+    rows.clear();
+    cols.clear();
+    own.clear();
+    std::vector<size_t> ebase;
+    size_t nnz = 0;
+    int max_rows = 1, max_cols = 1;
+    for (int b = 0; b < nbox; ++b) {
+        int o = -1;
+        for (int nb : fin[b].near) {
+            if (nb == b) o = (int)(rows.size() - rptr.back());
+            for (size_t i = 0; i < fin[nb].unk.size(); ++i) {
+                const float dist = mh::fnorm3(&P.cp[3 * (size_t)fin[nb].unk[i]], fin[b].c);
+                const int idx = fin[nb].offset + (int)i;
+                if (dist <= thr_r) rows.push_back(idx);
+                if (dist <= thr_c) cols.push_back(idx);
+            }
+        }
+        rptr.push_back((int)rows.size());
+        cptr.push_back((int)cols.size());
+        own.push_back(o);
+        const int m = rptr[b + 1] - rptr[b], nc = cptr[b + 1] - cptr[b];
+        max_rows = std::max(max_rows, m);
+        max_cols = std::max(max_cols, nc);
+        ebase.push_back(nnz);
+        nnz += (size_t)nc * fin[b].unk.size();
+    }
+    // CSR of P over rows = cols[c], columns = the box's own unknowns, the
+    // entries of a row in the order the boxes produce them
+    std::vector<int> cnt(n + 1, 0), dest(std::max<size_t>(nnz, 1)), ccol(std::max<size_t>(nnz, 1));
+    for (int b = 0; b < nbox; ++b)
+        for (size_t u = 0; u < fin[b].unk.size(); ++u)
+            for (int k = cptr[b]; k < cptr[b + 1]; ++k) cnt[cols[k] + 1] += 1;
+    for (int i = 0; i < n; ++i) cnt[i + 1] += cnt[i];
+    std::vector<int> fillp(cnt.begin(), cnt.end() - 1);
+    for (int b = 0; b < nbox; ++b)
+        for (size_t u = 0; u < fin[b].unk.size(); ++u)
+            for (int k = cptr[b]; k < cptr[b + 1]; ++k) {
+                const size_t e = ebase[b] + u * (size_t)(cptr[b + 1] - cptr[b]) + (k - cptr[b]);
+                const int pos = fillp[cols[k]]++;
+                dest[e] = pos;
+                ccol[pos] = fin[b].offset + (int)u;
+            }
+    const size_t smem = sizeof(float2) * ((size_t)max_rows * max_cols + max_cols) +
+                        sizeof(float) * (max_cols + (max_cols & 1)) + sizeof(float2) * 4 * (size_t)(max_rows + max_cols);
+    if (smem > 220 * 1024) {
+        set_error(c, "MLFMA preconditioner: a near block of " + std::to_string(max_rows) + " x " +
+                         std::to_string(max_cols) + " does not fit in shared memory (use smaller boxes)");
+        return EMFA_ERR_UNSUPPORTED;
+    }
+    M->sai_nnz = nnz;
+    DevBuf d_rptr, d_rows, d_cptr, d_cols, d_own, d_ebase, d_dest;
+    EMFA_TRY(upload(c, d_rptr, rptr, st));
+    EMFA_TRY(upload(c, d_rows, rows, st));
+    EMFA_TRY(upload(c, d_cptr, cptr, st));
+    EMFA_TRY(upload(c, d_cols, cols, st));
+    EMFA_TRY(upload(c, d_own, own, st));
+    EMFA_TRY(upload(c, d_ebase, ebase, st));
+    EMFA_TRY(upload(c, d_dest, dest, st));
+    EMFA_TRY(upload(c, M->csr_ptr, cnt, st));
+    EMFA_TRY(upload(c, M->csr_col, ccol, st));
+    EMFA_TRY(M->csr_val.alloc(c, sizeof(float2) * std::max<size_t>(nnz, 1)));
+    EMFA_TRY(M->pre_tmp.alloc(c, sizeof(float2) * (size_t)n));
+    EMFA_CUDA(c, cudaFuncSetAttribute(k_sai, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_sai<<<nbox, 128, smem, st>>>(dptr<int>(d_rptr), dptr<int>(d_rows), dptr<int>(d_cptr), dptr<int>(d_cols),
+                                   dptr<int>(d_own), dptr<int>(M->box_cnt), dptr<size_t>(d_ebase), dptr<int>(d_dest),
+                                   dptr<int>(M->box_of), dptr<int>(M->box_off), dptr<int>(M->near_ptr),
+                                   dptr<int>(M->near_box), dptr<int>(M->near_col), dptr<int>(M->row_cols),
+                                   dptr<size_t>(M->row_base), dptr<float2>(M->near_val), max_rows, max_cols,
+                                   dptr<float2>(M->csr_val));
+    c->kernel_launches += 1;
+    EMFA_CUDA(c, cudaGetLastError());
+    EMFA_CUDA(c, cudaStreamSynchronize(st));  // the list buffers and host vectors are released on return
+    M->precond = true;
+    return EMFA_OK;
 }
 
 static emfa_status_t mlfma_build(emfa_mlfma* M, cudaStream_t st)
@@ -815,6 +1076,7 @@ static emfa_status_t mlfma_build(emfa_mlfma* M, cudaStream_t st)
         EMFA_CUDA(c, cudaGetLastError());
         EMFA_CUDA(c, cudaStreamSynchronize(st));
     }
+    if (M->p.precond) EMFA_TRY(sai_build(M, P, st));
     EMFA_CUDA(c, cudaGetLastError());
     EMFA_CUDA(c, cudaStreamSynchronize(st));
     return EMFA_OK;
@@ -862,12 +1124,33 @@ static emfa_status_t mlfma_apply1(emfa_mlfma* M, const float2* x, float2* y, cud
 }
 
 // MLFMA as a Krylov operator (iteration vectors complex64, box order)
+// y = P x for n_rhs vectors
+static emfa_status_t sai_apply(emfa_mlfma* M, const float2* x, float2* y, int nrhs, cudaStream_t st)
+{
+    for (int r = 0; r < nrhs; ++r)
+        k_sai_apply<<<(M->n + 255) / 256, 256, 0, st>>>(dptr<int>(M->csr_ptr), dptr<int>(M->csr_col),
+                                                          dptr<float2>(M->csr_val), x + (size_t)r * M->n, M->n,
+                                                          y + (size_t)r * M->n);
+    M->ctx->kernel_launches += nrhs;
+    EMFA_CUDA(M->ctx, cudaGetLastError());
+    return EMFA_OK;
+}
+
 struct MlfmaOp : LinOp {
     emfa_mlfma* M = nullptr;
+    bool pre = false;  // left-preconditioned operator P Z
     emfa_status_t apply(Ctx*, const void* X, void* Y, int nrhs, cudaStream_t st) override
     {
-        for (int r = 0; r < nrhs; ++r)
-            EMFA_TRY(mlfma_apply1(M, (const float2*)X + (size_t)r * n, (float2*)Y + (size_t)r * n, st));
+        for (int r = 0; r < nrhs; ++r) {
+            const float2* x = (const float2*)X + (size_t)r * n;
+            float2* y = (float2*)Y + (size_t)r * n;
+            if (pre) {
+                EMFA_TRY(mlfma_apply1(M, x, dptr<float2>(M->pre_tmp), st));
+                EMFA_TRY(sai_apply(M, dptr<float2>(M->pre_tmp), y, 1, st));
+            } else {
+                EMFA_TRY(mlfma_apply1(M, x, y, st));
+            }
+        }
         return EMFA_OK;
     }
     emfa_status_t residual(Ctx* c, const double2* X, const void* B, double2* R, int nrhs, float2* xt,
@@ -1006,7 +1289,47 @@ emfa_status_t emfa_mlfma_solve(emfa_mlfma_t* M, const void* B_dev, int n_rhs, vo
     A.M = M;
     A.n = M->n;
     A.prec = EMFA_F32;
-    return solve_op(c, A, B_dev, n_rhs, X_dev, sp, info, st);
+    A.pre = M->precond;
+    const void* B = B_dev;
+    if (M->precond) {  // V <- P V (MLFMA::iterativeSolve, MLFMA.cpp:407-408)
+        const size_t bytes = sizeof(float2) * (size_t)M->n * n_rhs;
+        if (M->pre_b.bytes < bytes) EMFA_TRY(M->pre_b.alloc(c, bytes));
+        EMFA_TRY(sai_apply(M, (const float2*)B_dev, dptr<float2>(M->pre_b), n_rhs, st));
+        B = M->pre_b.ptr;
+    }
+    return solve_op(c, A, B, n_rhs, X_dev, sp, info, st);
+}
+
+emfa_status_t emfa_mlfma_precond_csr(const emfa_mlfma_t* M, size_t* nnz, int* ptr_host, int* col_host,
+                                     void* val_host)
+{
+    if (!M || !nnz) return EMFA_ERR_INVALID;
+    *nnz = M->precond ? M->sai_nnz : 0;
+    if (!M->precond || !ptr_host) return EMFA_OK;
+    Ctx* c = M->ctx;
+    EMFA_CUDA(c, cudaSetDevice(c->device));
+    EMFA_CUDA(c, cudaStreamSynchronize(c->stream));
+    EMFA_CUDA(c, cudaMemcpy(ptr_host, M->csr_ptr.ptr, sizeof(int) * (M->n + 1), cudaMemcpyDeviceToHost));
+    if (col_host) EMFA_CUDA(c, cudaMemcpy(col_host, M->csr_col.ptr, sizeof(int) * M->sai_nnz, cudaMemcpyDeviceToHost));
+    if (val_host)
+        EMFA_CUDA(c, cudaMemcpy(val_host, M->csr_val.ptr, sizeof(float2) * M->sai_nnz, cudaMemcpyDeviceToHost));
+    return EMFA_OK;
+}
+
+emfa_status_t emfa_mlfma_precond_lists(const emfa_mlfma_t* M, int* nbox, size_t* nrows, size_t* ncols, int* rptr,
+                                       int* rows, int* cptr, int* cols, int* own)
+{
+    if (!M || !nbox || !nrows || !ncols) return EMFA_ERR_INVALID;
+    *nbox = M->precond ? (int)M->sai_own.size() : 0;
+    *nrows = M->sai_rows.size();
+    *ncols = M->sai_cols.size();
+    if (!M->precond) return EMFA_OK;
+    if (rptr) std::copy(M->sai_rptr.begin(), M->sai_rptr.end(), rptr);
+    if (rows) std::copy(M->sai_rows.begin(), M->sai_rows.end(), rows);
+    if (cptr) std::copy(M->sai_cptr.begin(), M->sai_cptr.end(), cptr);
+    if (cols) std::copy(M->sai_cols.begin(), M->sai_cols.end(), cols);
+    if (own) std::copy(M->sai_own.begin(), M->sai_own.end(), own);
+    return EMFA_OK;
 }
 
 emfa_status_t emfa_mlfma_unpermute(emfa_mlfma_t* M, const void* X_box_dev, int n_rhs, void* X_rwg_dev, void* stream)

@@ -128,7 +128,7 @@ emfa_status_t run_mlfma(Ctx* c, Geom* g, const emfa_request_t& r, int n, emfa_re
 {
     cudaStream_t st = c->stream;
     const double alpha = r.kind == EMFA_CFIE ? r.alpha : 1.0;
-    emfa_mlfma_params_t mp{r.freq, alpha, r.box_threshold > 0 ? r.box_threshold : 0.25};
+    emfa_mlfma_params_t mp{r.freq, alpha, r.box_threshold > 0 ? r.box_threshold : 0.25, 0, 0.9, 0.87};
     emfa_mlfma_t* M = nullptr;
     EMFA_TRY(emfa_mlfma_create(static_cast<emfa_ctx_t*>(c), static_cast<emfa_geom_t*>(g), &mp, &M));
     struct Guard {

@@ -247,6 +247,12 @@ typedef struct {
     double freq;           /* Hz                                                     */
     double alpha;          /* CFIE combination (alpha:)                              */
     double box_threshold;  /* finest box side in wavelengths (mlfma_box_threshold:)  */
+    int precond;           /* 1: build the SAI preconditioner (preconditioning:) and  */
+                           /* solve P Z x = P b (MLFMA::calculatePreconditioner,      */
+                           /* EMSolver/MLFMA.cpp:1294-1391, applied at :407-408,506)  */
+    double row_threshold;  /* SAI rows / columns: near unknowns whose centre lies     */
+    double col_threshold;  /* within this many finest-box lengths of the box centre   */
+                           /* (row_threshold:, col_threshold:; MLFMA.cpp:719-720)     */
 } emfa_mlfma_params_t;
 
 /* Host only (no GPU): the octree plan the operator is built on -- finest
@@ -276,6 +282,15 @@ emfa_status_t emfa_mlfma_fill_v(emfa_mlfma_t* mlfma, const double* angles_host, 
  * B complex64, X complex128, box order. */
 emfa_status_t emfa_mlfma_solve(emfa_mlfma_t* mlfma, const void* B_dev, int n_rhs, void* X_dev,
                                const emfa_solver_params_t* sp, emfa_solve_info_t* info, void* stream);
+/* The SAI preconditioner of an operator created with precond = 1: P in CSR
+ * over box-order rows (ptr n+1 ints, col and val nnz entries, val complex64);
+ * with ptr_host NULL only nnz is returned (0 without a preconditioner). */
+emfa_status_t emfa_mlfma_precond_csr(const emfa_mlfma_t* mlfma, size_t* nnz, int* ptr_host, int* col_host,
+                                     void* val_host);
+/* Its per-box lists: rows and columns (box-order unknowns, CSR by box) and the
+ * position of the box's own unknowns in its rows; NULL arrays: sizes only. */
+emfa_status_t emfa_mlfma_precond_lists(const emfa_mlfma_t* mlfma, int* nbox, size_t* nrows, size_t* ncols,
+                                       int* rptr, int* rows, int* cptr, int* cols, int* own);
 /* X_rwg[r][perm[u]] = X_box[r][u], complex128. */
 emfa_status_t emfa_mlfma_unpermute(emfa_mlfma_t* mlfma, const void* X_box_dev, int n_rhs, void* X_rwg_dev,
                                    void* stream);

@@ -212,3 +212,26 @@ def load_dump(outdir, prec=32):
         d["near_rc"] = np.fromfile(p, np.int32).reshape(-1, 2)
         d["near_val"] = np.fromfile(os.path.join(outdir, "near_val.bin"), cdt)
     return d
+
+
+def sai_preconditioner(Znear, rptr, rows, cptr, cols, own):
+    """Restatement of MLFMA::parallelPreconditioner (EMSolver/MLFMA.cpp:1346-1391),
+    in complex128 with numpy's QR.  Per finest box b: A = Znear(rows_b, cols_b),
+    A = Q R (economy), and P(cols_b, unknowns of b) = R^-1 Q(own rows, :)^H
+    (Armadillo's .t() of a complex matrix is the conjugate transpose).  Znear
+    is the box-order near-field matrix (zero off the near pattern, as the
+    reference's sparse nearZ_); the box lists are the ones of
+    MLFMA::preparepreconditioner (MLFMA.cpp:1320-1344).  Returns dense P."""
+    n = Znear.shape[0]
+    nbox = len(own)
+    offs = [int(rows[rptr[b] + own[b]]) for b in range(nbox)]
+    cnts = [(offs[b + 1] if b + 1 < nbox else n) - offs[b] for b in range(nbox)]
+    P = np.zeros((n, n), dtype=np.complex128)
+    for b in range(nbox):
+        r = rows[rptr[b]:rptr[b + 1]]
+        c = cols[cptr[b]:cptr[b + 1]]
+        A = Znear[np.ix_(r, c)].astype(np.complex128)
+        Q, R = np.linalg.qr(A)
+        sel = Q[own[b]:own[b] + cnts[b], :]
+        P[np.ix_(c, np.arange(offs[b], offs[b] + cnts[b]))] = np.linalg.solve(R, sel.conj().T)
+    return P

@@ -76,16 +76,19 @@ def test_launcher_end_to_end_vs_reference(emfa_lib, solver):
 
 
 @pytest.mark.gpu
-def test_launcher_mlfma_vs_reference(emfa_lib):
-    """MLFMA through CONFIG.yml: bistatic RCS within 0.1 dB of the reference's
-    own MLFMA run on the same mesh."""
+@pytest.mark.parametrize("precond", ["false", "true"])
+def test_launcher_mlfma_vs_reference(emfa_lib, precond):
+    """MLFMA through CONFIG.yml, without and with the SAI preconditioner
+    (preconditioning: true, row/col thresholds 0.9/0.87): bistatic RCS within
+    0.1 dB of the reference's own (unpreconditioned) MLFMA run on the same
+    mesh."""
     g = load_golden("sphere3_mlfma")
     d = tempfile.mkdtemp()
     nas = os.path.join(d, "sph.nas")
     M.write_nas(M.TriMesh(g["verts"], g["tris"]), nas)
     cfg = os.path.join(d, "CONFIG.yml")
     M.write_config(cfg, EMSolver="MLFMA", mesh_path=nas, frequency="3e8", alpha="0.5", mlfma_box_threshold="0.25",
-                   iteration_threshold="1e-3", max_iteration_number="200")
+                   iteration_threshold="1e-3", max_iteration_number="200", preconditioning=precond)
     r = run([cfg], cwd=d)
     assert "Exit State: OK" in r.stdout, r.stdout[-2000:] + r.stderr[-2000:]
     out = os.path.join(d, "sph_MLFMA_CFIE_0.5")
