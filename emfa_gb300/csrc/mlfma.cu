@@ -138,14 +138,23 @@ static float fnorm3(const float* a, const float* b)
 struct MLevel {
     int nbox = 0, L = 0, K = 0;
     float len = 0;
-    DevBuf parent, oct;                 // int per box
+    DevBuf parent, oct;                 // parent index and octant per box (int)
     DevBuf child_ptr, child_idx;        // CSR children (int)
-    DevBuf far_ptr, far_box, far_off;   // CSR far lists (int)
+    DevBuf far_ptr, far;                // CSR far lists: int2 {source box, offset index}
     DevBuf trans;                       // float2 [343][K]
-    DevBuf up, down;                    // C3f [nbox][K]
+    DevBuf up, down;                    // planar float2 [nbox][3][K]
     DevBuf ip_col, ip_w;                // interpolation to this level from the level below: [K][9]
-    DevBuf an_ptr, an_kp, an_w;         // anterpolation from the level above, transposed stencil
+    // anterpolation from the level above, as two transposed 1-D Lagrange
+    // stencils: theta (CSR over this level's theta index: parent theta, weight)
+    // and phi (CSR over this level's phi index: parent phi, weight)
+    DevBuf th_ptr, th_src, th_w, ph_ptr, ph_src, ph_w;
+    int rows = 0;                       // phi rows per CTA of the downward pass (even)
+    size_t down_smem = 0;               // shared bytes per CTA (theta-pass rows)
+    DevBuf down_win;                    // int2 per chunk: parent phi rows its phi stencils read
     DevBuf up_phase;                    // float2 [8][K]: exp(-j k k.(parent - child)) for the level below
+    int up_bs = 0;                      // interpolation from the level below: samples per CTA,
+    size_t up_smem = 0;                 //   shared bytes per CTA,
+    DevBuf up_win;                      //   int2 per chunk: window of the children's samples it reads
     std::vector<float> w_host;          // quadrature weights (host)
 };
 
@@ -169,6 +178,7 @@ struct emfa_mlfma {
     emfa::DevBuf near_ptr, near_box, near_col, row_cols;  // CSR near lists, column base per slot, C_b per box
     emfa::DevBuf row_base;         // size_t per finest box: first value of the box's rows
     emfa::DevBuf near_val;         // float2 [nnz]
+    emfa::DevBuf near_cbase, near_cidx;  // per finest box: first entry, column unknowns of its near rows
     size_t nnz = 0;
     emfa::DevBuf tmp_in, tmp_out;  // complex64 scratch for residuals
     // SAI preconditioner P (CSR over box-order rows), built when p.precond
@@ -266,81 +276,201 @@ __global__ void k_near_fill(const RwgPack<float>* __restrict__ rw, const int* __
     }
 }
 
+// Level patterns (up and down) are planar: box b's component c occupies
+// float2 [(3 b + c) K, (3 b + c + 1) K), so a warp reads 32 consecutive
+// samples of one plane at once.
+
 // finest aggregation: CTA per finest box, threads over samples
 __global__ void k_agg_finest(const float2* __restrict__ x, const C3f* __restrict__ rad,
                              const int* __restrict__ box_off, const int* __restrict__ box_cnt, int K,
-                             C3f* __restrict__ out)
+                             float2* __restrict__ out)
 {
     const int b = blockIdx.x;
     const int o = box_off[b], cnt = box_cnt[b];
     for (int kk = threadIdx.x; kk < K; kk += blockDim.x) {
         C3f acc = c3zero();
         for (int u = 0; u < cnt; ++u) c3fma(acc, x[o + u], rad[(size_t)(o + u) * K + kk]);
-        out[(size_t)b * K + kk] = acc;
+        float2* ob = out + (size_t)3 * b * K + kk;
+        ob[0] = acc.x;
+        ob[K] = acc.y;
+        ob[2 * K] = acc.z;
     }
 }
 
-// interpolation + phase shift: parent (b, k) gathers its children's patterns
-__global__ void k_upward(const C3f* __restrict__ child, int Kc, const int* __restrict__ child_ptr,
-                         const int* __restrict__ child_idx, const int* __restrict__ child_oct,
-                         const int* __restrict__ ip_col, const float* __restrict__ ip_w,
-                         const float2* __restrict__ phase, int nbox, int K, C3f* __restrict__ out)
+// interpolation + phase shift: CTA per (parent box, chunk of parent samples).
+// The children's samples that the chunk's 9-point Lagrange stencils touch
+// (window [win.x, win.y), computed per chunk on the host) are staged in
+// shared memory, as many children per pass as UP_TILE samples allow.
+constexpr int UP_TILE = 4096;  // staged samples per pass: 96 KB
+__global__ void __launch_bounds__(256) k_upward(const float2* __restrict__ child, int Kc,
+                                                const int* __restrict__ child_ptr, const int* __restrict__ child_idx,
+                                                const int* __restrict__ child_oct, const int* __restrict__ ip_col,
+                                                const float* __restrict__ ip_w, const int2* __restrict__ win,
+                                                const float2* __restrict__ phase, int K, float2* __restrict__ out)
 {
-    size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (id >= (size_t)nbox * K) return;
-    const int b = (int)(id / K), kp = (int)(id % K);
-    C3f acc = c3zero();
-    for (int ci = child_ptr[b]; ci < child_ptr[b + 1]; ++ci) {
-        const int c = child_idx[ci];
-        const C3f* src = child + (size_t)c * Kc;
-        C3f v = c3zero();
+    extern __shared__ float2 s_pat[];  // [child in pass][3][tile]
+    const int b = blockIdx.x;
+    const int kp = blockIdx.y * blockDim.x + threadIdx.x;
+    const bool act = kp < K;
+    const int2 w2 = win[blockIdx.y];
+    const int W = w2.y - w2.x;
+    int col[9];
+    float w[9];
 #pragma unroll
-        for (int t = 0; t < 9; ++t) {
-            const float w = ip_w[kp * 9 + t];
-            const C3f& s = src[ip_col[kp * 9 + t]];
-            v.x = caddf(v.x, cscalef(s.x, w));
-            v.y = caddf(v.y, cscalef(s.y, w));
-            v.z = caddf(v.z, cscalef(s.z, w));
-        }
-        c3fma(acc, phase[child_oct[c] * K + kp], v);
+    for (int t = 0; t < 9; ++t) {
+        col[t] = act ? ip_col[kp * 9 + t] - w2.x : 0;
+        w[t] = act ? ip_w[kp * 9 + t] : 0.f;
     }
-    out[id] = acc;
-}
-
-// translation from far boxes (+ anterpolation from the parent level)
-__global__ void k_downward(const C3f* __restrict__ up, const int* __restrict__ far_ptr,
-                           const int* __restrict__ far_box, const int* __restrict__ far_off,
-                           const float2* __restrict__ trans, int nbox, int K, const C3f* __restrict__ pdown, int Kp,
-                           const int* __restrict__ parent, const int* __restrict__ oct,
-                           const int* __restrict__ an_ptr, const int* __restrict__ an_kp,
-                           const float* __restrict__ an_w, const float2* __restrict__ pphase, C3f* __restrict__ out)
-{
-    size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (id >= (size_t)nbox * K) return;
-    const int b = (int)(id / K), kk = (int)(id % K);
+    const int c0 = child_ptr[b], nch = child_ptr[b + 1] - c0;
+    const int per = W <= UP_TILE ? max(1, min(nch, UP_TILE / max(W, 1))) : 1;  // children per pass
     C3f acc = c3zero();
-    for (int f = far_ptr[b]; f < far_ptr[b + 1]; ++f)
-        c3fma(acc, trans[(size_t)far_off[f] * K + kk], up[(size_t)far_box[f] * K + kk]);
-    if (pdown) {
-        const C3f* src = pdown + (size_t)parent[b] * Kp;
-        const int o = oct[b];
-        for (int a = an_ptr[kk]; a < an_ptr[kk + 1]; ++a) {
-            const int kp = an_kp[a];
-            float2 ph = pphase[o * Kp + kp];
-            ph = make_float2(ph.x * an_w[a], -ph.y * an_w[a]);  // conj: exp(+j k k.(parent - child))
-            c3fma(acc, ph, src[kp]);
+    for (int cb = 0; cb < nch; cb += per) {
+        const int nb = min(per, nch - cb);
+        C3f v = c3zero();  // one child's stencil sum (nb == 1 may take several tiles)
+        for (int t0 = 0; t0 < W; t0 += UP_TILE) {
+            const int nt = min(UP_TILE, W - t0);
+            __syncthreads();  // the previous pass has been read
+            for (int cc = 0; cc < nb; ++cc) {
+                const float2* src = child + (size_t)3 * child_idx[c0 + cb + cc] * Kc + w2.x + t0;
+                float2* dst = s_pat + (size_t)cc * 3 * nt;
+                for (int q = threadIdx.x; q < 3 * nt; q += blockDim.x) {
+                    const int comp = q / nt, r = q - comp * nt;
+                    dst[q] = src[(size_t)comp * Kc + r];
+                }
+            }
+            __syncthreads();
+            for (int cc = 0; cc < nb; ++cc) {
+                const float2* sp = s_pat + (size_t)cc * 3 * nt;
+#pragma unroll
+                for (int t = 0; t < 9; ++t) {
+                    const int r = col[t] - t0;
+                    if ((unsigned)r < (unsigned)nt) {
+                        v.x = caddf(v.x, cscalef(sp[r], w[t]));
+                        v.y = caddf(v.y, cscalef(sp[nt + r], w[t]));
+                        v.z = caddf(v.z, cscalef(sp[2 * nt + r], w[t]));
+                    }
+                }
+                if (nb > 1 || t0 + nt >= W) {  // this child's sum is complete
+                    if (act) c3fma(acc, phase[child_oct[child_idx[c0 + cb + cc]] * K + kp], v);
+                    v = c3zero();
+                }
+            }
         }
     }
-    out[id] = acc;
+    if (act) {
+        float2* ob = out + (size_t)3 * b * K + kp;
+        ob[0] = acc.x;
+        ob[K] = acc.y;
+        ob[2 * K] = acc.z;
+    }
 }
 
-// disaggregation + near field: warp per unknown (box order)
+// translation from far boxes + anterpolation from the parent: CTA per (box,
+// chunk of phi rows [pc0, pc0 + R)), i.e. the contiguous samples
+// [pc0 L, (pc0 + R) L) of the box (samples k = pc L + tc, phi-major).
+//   1. theta pass (boxes below the top level): for the parent phi rows
+//      pp in [win.x, win.y) that the chunk's phi stencils read, and every theta
+//      column tc: h[comp][pp - win.x][tc] = sum over the transposed theta
+//      stencil of w * conj(phase_oct(pp, t)) * parent(pp, t), into shared memory;
+//   2. per pair of samples (16-byte loads of the planar patterns and of the
+//      translation table): the far boxes' translated patterns in far-list
+//      order, then the transposed phi stencil over h.
+__device__ __forceinline__ void cfma2(float4& acc, float4 t, float4 v)
+{
+    acc.x += t.x * v.x - t.y * v.y;
+    acc.y += t.x * v.y + t.y * v.x;
+    acc.z += t.z * v.z - t.w * v.w;
+    acc.w += t.z * v.w + t.w * v.z;
+}
+
+__global__ void k_downward(const float4* __restrict__ up, const int* __restrict__ far_ptr,
+                           const int2* __restrict__ far, const float4* __restrict__ trans, int L, int R,
+                           const float2* __restrict__ pdown, int Lp, const int2* __restrict__ win,
+                           const int* __restrict__ parent, const int* __restrict__ oct,
+                           const float2* __restrict__ pphase, const int* __restrict__ th_ptr,
+                           const int* __restrict__ th_src, const float* __restrict__ th_w,
+                           const int* __restrict__ ph_ptr, const int* __restrict__ ph_src,
+                           const float* __restrict__ ph_w, float4* __restrict__ out)
+{
+    extern __shared__ float2 s_h[];  // [3][rows of the window][L]
+    const int b = blockIdx.x;
+    const int K = 2 * L * L, K2 = K >> 1;
+    const int pc0 = blockIdx.y * R;
+    const int npair = (min(R, 2 * L - pc0) * L) >> 1;
+    int2 w2 = make_int2(0, 0);
+    int hsz = 0;
+    if (pdown) {
+        w2 = win[blockIdx.y];
+        hsz = (w2.y - w2.x) * L;
+        const int Kp = 2 * Lp * Lp;
+        const float2* src = pdown + (size_t)3 * parent[b] * Kp;
+        const float2* ph0 = pphase + (size_t)oct[b] * Kp;
+        for (int i = threadIdx.x; i < hsz; i += blockDim.x) {
+            const int r = i / L, tc = i - r * L;
+            const int base = (w2.x + r) * Lp;
+            float2 sx = make_float2(0, 0), sy = sx, sz = sx;
+            for (int a = th_ptr[tc]; a < th_ptr[tc + 1]; ++a) {
+                const int kp = base + th_src[a];
+                const float w = th_w[a];
+                float2 ph = ph0[kp];
+                ph = make_float2(ph.x * w, -ph.y * w);  // conj: exp(+j k k.(parent - child))
+                sx = caddf(sx, cmulf(ph, src[kp]));
+                sy = caddf(sy, cmulf(ph, src[Kp + kp]));
+                sz = caddf(sz, cmulf(ph, src[2 * Kp + kp]));
+            }
+            s_h[i] = sx;
+            s_h[hsz + i] = sy;
+            s_h[2 * hsz + i] = sz;
+        }
+        __syncthreads();
+    }
+    const int f0 = far_ptr[b], f1 = far_ptr[b + 1];
+    for (int i = threadIdx.x; i < npair; i += blockDim.x) {
+        const int q = ((pc0 * L) >> 1) + i;  // pair index: samples 2q, 2q + 1
+        float4 ax = make_float4(0, 0, 0, 0), ay = ax, az = ax;
+        for (int f = f0; f < f1; ++f) {
+            const int2 e = far[f];
+            const float4 t = trans[(size_t)e.y * K2 + q];
+            const float4* sp = up + (size_t)3 * e.x * K2 + q;
+            cfma2(ax, t, sp[0]);
+            cfma2(ay, t, sp[K2]);
+            cfma2(az, t, sp[2 * K2]);
+        }
+        if (pdown) {
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int kk = 2 * q + h;
+                const int pc = kk / L, tc = kk - pc * L;
+                float2 sx = make_float2(0, 0), sy = sx, sz = sx;
+                for (int a = ph_ptr[pc]; a < ph_ptr[pc + 1]; ++a) {
+                    const int r = (ph_src[a] - w2.x) * L + tc;
+                    const float w = ph_w[a];
+                    sx = caddf(sx, cscalef(s_h[r], w));
+                    sy = caddf(sy, cscalef(s_h[hsz + r], w));
+                    sz = caddf(sz, cscalef(s_h[2 * hsz + r], w));
+                }
+                if (h == 0) {
+                    ax.x += sx.x; ax.y += sx.y; ay.x += sy.x; ay.y += sy.y; az.x += sz.x; az.y += sz.y;
+                } else {
+                    ax.z += sx.x; ax.w += sx.y; ay.z += sy.x; ay.w += sy.y; az.z += sz.x; az.w += sz.y;
+                }
+            }
+        }
+        float4* ob = out + (size_t)3 * b * K2 + q;
+        ob[0] = ax;
+        ob[K2] = ay;
+        ob[2 * K2] = az;
+    }
+}
+
+// disaggregation + near field: warp per unknown (box order).  The near row of
+// unknown u is contiguous in val (row_cols[b] values); its column unknowns are
+// listed once per box in near_cidx.
 __global__ void k_disagg_near(const float2* __restrict__ x, const C3f* __restrict__ rec,
-                              const C3f* __restrict__ down, const float* __restrict__ coeff, int K,
+                              const float2* __restrict__ down, const float* __restrict__ coeff, int K,
                               const int* __restrict__ box_of, const int* __restrict__ box_off,
-                              const int* __restrict__ box_cnt, const int* __restrict__ near_ptr,
-                              const int* __restrict__ near_box, const int* __restrict__ near_col,
                               const int* __restrict__ row_cols, const size_t* __restrict__ row_base,
+                              const int* __restrict__ near_cbase, const int* __restrict__ near_cidx,
                               const float2* __restrict__ val, int n, int skip_near, float2* __restrict__ y)
 {
     const int warp = (int)(((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
@@ -348,18 +478,19 @@ __global__ void k_disagg_near(const float2* __restrict__ x, const C3f* __restric
     const int u = warp, b = box_of[u];
     float2 acc = make_float2(0, 0);
     const C3f* rr = rec + (size_t)u * K;
-    const C3f* dd = down + (size_t)b * K;
+    const float2* dd = down + (size_t)3 * b * K;
+#pragma unroll 4
     for (int kk = lane; kk < K; kk += 32) {
-        const C3f r = rr[kk], d = dd[kk];
-        float2 t = caddf(caddf(cmulf(r.x, d.x), cmulf(r.y, d.y)), cmulf(r.z, d.z));
+        const C3f r = rr[kk];
+        float2 t = caddf(caddf(cmulf(r.x, dd[kk]), cmulf(r.y, dd[K + kk])), cmulf(r.z, dd[2 * K + kk]));
         acc = caddf(acc, cscalef(t, coeff[kk]));
     }
-    const float2* vrow = val + row_base[b] + (size_t)(u - box_off[b]) * row_cols[b];
-    for (int sl = skip_near ? near_ptr[b + 1] : near_ptr[b]; sl < near_ptr[b + 1]; ++sl) {
-        const int nb = near_box[sl];
-        const int s0 = box_off[nb], ns = box_cnt[nb];
-        const float2* vr = vrow + near_col[sl];
-        for (int q = lane; q < ns; q += 32) acc = caddf(acc, cmulf(vr[q], x[s0 + q]));
+    if (!skip_near) {
+        const int rc = row_cols[b];
+        const float2* vrow = val + row_base[b] + (size_t)(u - box_off[b]) * rc;
+        const int* ci = near_cidx + near_cbase[b];
+#pragma unroll 4
+        for (int j = lane; j < rc; j += 32) acc = caddf(acc, cmulf(vrow[j], x[ci[j]]));
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -542,6 +673,49 @@ __global__ void __launch_bounds__(128) k_sai(const int* __restrict__ rptr, const
     }
 }
 
+// translation operator of every far-box offset at every sample (FP64, the
+// host recurrences of parallelLevelTrans, MLFMA.cpp:1191-1222): thread per
+// (offset, sample); hl holds each offset's spherical Hankel values
+__global__ void k_trans_table(const double2* __restrict__ hl, const int* __restrict__ minl, int lmax,
+                              const float* __restrict__ kd, int K, double len, float2* __restrict__ tr)
+{
+    const size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= (size_t)343 * K) return;
+    const int off = (int)(id / K), kk = (int)(id % K);
+    const int ml = minl[off];
+    if (ml < 0) {  // near offsets: no translation
+        tr[id] = make_float2(0.f, 0.f);
+        return;
+    }
+    const int dx = off / 49 - 3, dy = (off / 7) % 7 - 3, dz = off % 7 - 3;
+    const double D0 = dx * len, D1 = dy * len, D2 = dz * len;
+    const double Dn = sqrt(D0 * D0 + D1 * D1 + D2 * D2);
+    const double ct = ((double)kd[3 * kk] * D0 + (double)kd[3 * kk + 1] * D1 + (double)kd[3 * kk + 2] * D2) / Dn;
+    const double2* h = hl + (size_t)off * (lmax + 1);
+    double vr = 0.0, vi = 0.0, p0 = 1.0, p1 = ct;
+    for (int q = 0; q <= ml; ++q) {
+        double Pq = q == 0 ? 1.0 : ct;
+        if (q >= 2) {
+            Pq = ((2 * q - 1) * ct * p1 - (q - 1) * p0) / q;
+            p0 = p1;
+            p1 = Pq;
+        }
+        // (2q+1) (-j)^q h_q P_q
+        const double2 hq = h[q];
+        double ar, ai;
+        switch (q & 3) {
+            case 0: ar = hq.x; ai = hq.y; break;
+            case 1: ar = hq.y; ai = -hq.x; break;
+            case 2: ar = -hq.x; ai = -hq.y; break;
+            default: ar = -hq.y; ai = hq.x; break;
+        }
+        const double w = (2.0 * q + 1) * Pq;
+        vr += w * ar;
+        vi += w * ai;
+    }
+    tr[id] = make_float2((float)vr, (float)vi);
+}
+
 // y = P x, P in CSR (row per thread)
 __global__ void k_sai_apply(const int* __restrict__ ptr, const int* __restrict__ col, const float2* __restrict__ val,
                             const float2* __restrict__ x, int n, float2* __restrict__ y)
@@ -556,6 +730,15 @@ __global__ void k_sai_apply(const int* __restrict__ ptr, const int* __restrict__
 // ---------------------------------------------------------------------------
 // host build
 // ---------------------------------------------------------------------------
+// phi rows per CTA of the downward pass: an even count giving chunks of about
+// 256 samples (sample pairs never straddle a chunk)
+static int down_rows(int L)
+{
+    const int nchunk = (2 * L * L + 255) / 256;
+    const int r = (2 * L + nchunk - 1) / nchunk;
+    return r + (r & 1);
+}
+
 template <typename T>
 static emfa_status_t upload(Ctx* c, DevBuf& b, const std::vector<T>& v, cudaStream_t st)
 {
@@ -573,6 +756,7 @@ struct Plan {
     std::vector<std::vector<mh::Box>> lb;
     std::vector<int> poles;
     std::vector<std::vector<float>> gt, gp, gw, kd;
+    std::vector<std::vector<float>> wt1, wp1;  // 1-D Gauss weights in theta and phi (gw = wp1 x wt1)
     std::vector<int> perm, box_of, off, cnt;
     std::vector<float> cen;
     std::vector<float> cp;  // RWG centres (v1 + v2) / 2, RWG order
@@ -700,6 +884,8 @@ static bool build_plan(const std::vector<double>& verts, int nv, const std::vect
     auto& gw = P.gw;
     auto& kd = P.kd;
     gt.assign(nl, {});
+    P.wt1.assign(nl, {});
+    P.wp1.assign(nl, {});
     gp.assign(nl, {});
     gw.assign(nl, {});
     kd.assign(nl, {});
@@ -713,6 +899,8 @@ static bool build_plan(const std::vector<double>& verts, int nv, const std::vect
         mh::gauss_legendre(2 * Pm, rp, wp);
         gt[i] = rt;
         gp[i] = rp;
+        P.wt1[i] = wt;
+        P.wp1[i] = wp;
         gw[i].resize(2 * (size_t)Pm * Pm);
         kd[i].resize(3 * 2 * (size_t)Pm * Pm);
         size_t q = 0;
@@ -876,6 +1064,10 @@ static emfa_status_t mlfma_build(emfa_mlfma* M, cudaStream_t st)
         ml.len = P.blen[l];
         ml.w_host = gw[i];
     }
+    // the staged interpolation tiles exceed the default 48 KB of shared memory
+    EMFA_CUDA(c, cudaFuncSetAttribute(k_upward, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)(sizeof(float2) * 3 * UP_TILE)));
+    EMFA_CUDA(c, cudaFuncSetAttribute(k_downward, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     // per-level device tables
     for (int l = 2; l <= L; ++l) {
         const int i = l - 2;
@@ -902,47 +1094,55 @@ static emfa_status_t mlfma_build(emfa_mlfma* M, cudaStream_t st)
             }
         EMFA_TRY(upload(c, ml.parent, par, st));
         EMFA_TRY(upload(c, ml.oct, oc, st));
-        EMFA_TRY(upload(c, ml.far_ptr, fptr, st));
-        EMFA_TRY(upload(c, ml.far_box, fbox, st));
-        EMFA_TRY(upload(c, ml.far_off, foff, st));
+        {
+            std::vector<int2> fe(fbox.size());
+            for (size_t f = 0; f < fbox.size(); ++f) fe[f] = make_int2(fbox[f], foff[f]);
+            EMFA_TRY(upload(c, ml.far_ptr, fptr, st));
+            EMFA_TRY(upload(c, ml.far, fe, st));
+        }
         EMFA_TRY(upload(c, ml.child_ptr, cptr, st));
         EMFA_TRY(upload(c, ml.child_idx, cidx, st));
         // translation operators per offset: sum_l (2l+1)(-j)^l h_l^(2)(kD) P_l(k.D/|D|),
-        // l <= min(poles, floor(kD)) (MLFMA.cpp:1203-1219), evaluated in FP64
-        std::vector<float2> tr((size_t)343 * K, make_float2(0, 0));
-        for (int dx = -3; dx <= 3; ++dx)
-            for (int dy = -3; dy <= 3; ++dy)
-                for (int dz = -3; dz <= 3; ++dz) {
-                    if (std::abs(dx) <= 1 && std::abs(dy) <= 1 && std::abs(dz) <= 1) continue;
-                    const int off = ((dx + 3) * 7 + (dy + 3)) * 7 + (dz + 3);
-                    double D[3] = {dx * (double)ml.len, dy * (double)ml.len, dz * (double)ml.len};
-                    double Dn = std::sqrt(D[0] * D[0] + D[1] * D[1] + D[2] * D[2]);
-                    double x = (double)k * Dn;
-                    int minL = (int)std::min((float)ml.L, (float)(k * (float)Dn));
-                    std::vector<std::complex<double>> hl(minL + 1);
-                    hl[0] = std::complex<double>(std::sin(x), std::cos(x)) / x;
-                    if (minL >= 1) hl[1] = std::complex<double>(std::sin(x) / x - std::cos(x), std::cos(x) / x + std::sin(x)) / x;
-                    for (int q = 2; q <= minL; ++q) hl[q] = ((2.0 * q - 1) / x) * hl[q - 1] - hl[q - 2];
-                    for (int kk = 0; kk < K; ++kk) {
-                        double ct = (kd[i][3 * kk] * D[0] + kd[i][3 * kk + 1] * D[1] + kd[i][3 * kk + 2] * D[2]) / Dn;
-                        std::complex<double> val(0, 0);
-                        double p0 = 1, p1 = ct;
-                        const std::complex<double> jl[4] = {{1, 0}, {0, -1}, {-1, 0}, {0, 1}};
-                        for (int q = 0; q <= minL; ++q) {
-                            double Pq = q == 0 ? 1 : q == 1 ? ct : 0;
-                            if (q >= 2) {
-                                Pq = ((2 * q - 1) * ct * p1 - (q - 1) * p0) / q;
-                                p0 = p1;
-                                p1 = Pq;
-                            }
-                            val += (2.0 * q + 1) * jl[q % 4] * hl[q] * Pq;
-                        }
-                        tr[(size_t)off * K + kk] = make_float2((float)val.real(), (float)val.imag());
+        // l <= min(poles, floor(kD)) (MLFMA.cpp:1203-1219), in FP64: the Hankel
+        // recurrence per offset here, the Legendre sums per sample on the device
+        {
+            const int lmax = ml.L;
+            std::vector<double2> hlv((size_t)343 * (lmax + 1), make_double2(0, 0));
+            std::vector<int> minl(343, -1);
+            for (int dx = -3; dx <= 3; ++dx)
+                for (int dy = -3; dy <= 3; ++dy)
+                    for (int dz = -3; dz <= 3; ++dz) {
+                        if (std::abs(dx) <= 1 && std::abs(dy) <= 1 && std::abs(dz) <= 1) continue;
+                        const int off = ((dx + 3) * 7 + (dy + 3)) * 7 + (dz + 3);
+                        double D[3] = {dx * (double)ml.len, dy * (double)ml.len, dz * (double)ml.len};
+                        double Dn = std::sqrt(D[0] * D[0] + D[1] * D[1] + D[2] * D[2]);
+                        double x = (double)k * Dn;
+                        int minL = (int)std::min((float)ml.L, (float)(k * (float)Dn));
+                        minL = std::min(minL, lmax);
+                        std::vector<std::complex<double>> hl(minL + 1);
+                        hl[0] = std::complex<double>(std::sin(x), std::cos(x)) / x;
+                        if (minL >= 1)
+                            hl[1] = std::complex<double>(std::sin(x) / x - std::cos(x), std::cos(x) / x + std::sin(x)) / x;
+                        for (int q = 2; q <= minL; ++q) hl[q] = ((2.0 * q - 1) / x) * hl[q - 1] - hl[q - 2];
+                        for (int q = 0; q <= minL; ++q)
+                            hlv[(size_t)off * (lmax + 1) + q] = make_double2(hl[q].real(), hl[q].imag());
+                        minl[off] = minL;
                     }
-                }
-        EMFA_TRY(upload(c, ml.trans, tr, st));
-        EMFA_TRY(ml.up.alloc(c, sizeof(C3f) * (size_t)ml.nbox * K));
-        EMFA_TRY(ml.down.alloc(c, sizeof(C3f) * (size_t)ml.nbox * K));
+            DevBuf d_hl, d_minl, d_kd;
+            EMFA_TRY(upload(c, d_hl, hlv, st));
+            EMFA_TRY(upload(c, d_minl, minl, st));
+            EMFA_TRY(upload(c, d_kd, kd[i], st));
+            EMFA_TRY(ml.trans.alloc(c, sizeof(float2) * (size_t)343 * K));
+            const size_t tot = (size_t)343 * K;
+            k_trans_table<<<(unsigned)((tot + 127) / 128), 128, 0, st>>>(dptr<double2>(d_hl), dptr<int>(d_minl), lmax,
+                                                                         dptr<float>(d_kd), K, (double)ml.len,
+                                                                         dptr<float2>(ml.trans));
+            c->kernel_launches += 1;
+            EMFA_CUDA(c, cudaGetLastError());
+            EMFA_CUDA(c, cudaStreamSynchronize(st));  // host vectors and the small tables are released next
+        }
+        EMFA_TRY(ml.up.alloc(c, sizeof(float2) * 3 * (size_t)ml.nbox * K));
+        EMFA_TRY(ml.down.alloc(c, sizeof(float2) * 3 * (size_t)ml.nbox * K));
     }
     // interpolation level i+1 (child, fewer samples) -> level i (parent), i = 0..nl-2
     for (int i = 0; i + 1 < nl; ++i) {
@@ -969,6 +1169,28 @@ static emfa_status_t mlfma_build(emfa_mlfma* M, cudaStream_t st)
             }
         EMFA_TRY(upload(c, pm.ip_col, col, st));
         EMFA_TRY(upload(c, pm.ip_w, w, st));
+        {
+            // CTA chunks of at most 256 parent samples (whole warps, as even as
+            // possible) and the window of child samples each chunk reads
+            const int chunks = (Kp + 255) / 256;
+            pm.up_bs = 32 * ((Kp + 32 * chunks - 1) / (32 * chunks));
+            const int nchunk = (Kp + pm.up_bs - 1) / pm.up_bs;
+            std::vector<int2> win(nchunk);
+            size_t most = 0;
+            for (int ch = 0; ch < nchunk; ++ch) {
+                int lo = cm.K, hi = 0;
+                for (int kp = ch * pm.up_bs; kp < std::min(Kp, (ch + 1) * pm.up_bs); ++kp)
+                    for (int q = 0; q < 9; ++q) {
+                        lo = std::min(lo, col[(size_t)kp * 9 + q]);
+                        hi = std::max(hi, col[(size_t)kp * 9 + q] + 1);
+                    }
+                win[ch] = make_int2(lo, hi);
+                const int W = hi - lo;
+                most = std::max(most, (size_t)(W <= UP_TILE ? std::min(8, UP_TILE / std::max(W, 1)) * W : UP_TILE));
+            }
+            pm.up_smem = sizeof(float2) * 3 * most;
+            EMFA_TRY(upload(c, pm.up_win, win, st));
+        }
         // phases for the children of level i: exp(-j k kp . (parent - child)), per octant
         std::vector<float2> ph((size_t)8 * Kp);
         for (int o = 0; o < 8; ++o) {
@@ -981,26 +1203,64 @@ static emfa_status_t mlfma_build(emfa_mlfma* M, cudaStream_t st)
             }
         }
         EMFA_TRY(upload(c, pm.up_phase, ph, st));
-        // anterpolation into level i+1: transpose of the stencil, weight * w_parent / w_child
-        const int Kc = cm.K;
-        std::vector<std::vector<std::pair<int, float>>> tpos(Kc);
-        for (int kp = 0; kp < Kp; ++kp)
-            for (int q = 0; q < 9; ++q) {
-                int kc = col[(size_t)kp * 9 + q];
-                tpos[kc].push_back({kp, w[(size_t)kp * 9 + q] * gw[i][kp] / gw[i + 1][kc]});
+        // anterpolation into level i+1: the transposed theta and phi Lagrange
+        // stencils, each weight scaled by w_parent / w_child of its own axis
+        // (the 2-D weights are products: gw = wp x wt)
+        {
+            const int Lp = pm.L;
+            auto transpose = [](const std::vector<int>& loc, const std::vector<float>& el, int np, int nc,
+                                const std::vector<float>& wpar, const std::vector<float>& wch, std::vector<int>& ptr,
+                                std::vector<int>& src, std::vector<float>& wt) {
+                std::vector<std::vector<std::pair<int, float>>> lst(nc);
+                for (int x = 0; x < np; ++x)
+                    for (int q = 0; q < 3; ++q) {
+                        const int y = loc[3 * x + q];
+                        lst[y].push_back({x, el[3 * x + q] * wpar[x] / wch[y]});
+                    }
+                ptr.assign(1, 0);
+                src.clear();
+                wt.clear();
+                for (int y = 0; y < nc; ++y) {
+                    for (auto& e : lst[y]) {
+                        src.push_back(e.first);
+                        wt.push_back(e.second);
+                    }
+                    ptr.push_back((int)src.size());
+                }
+            };
+            std::vector<int> tptr, tsrc, pptr, psrc;
+            std::vector<float> tw, pw;
+            transpose(tloc, tel, Lp, Lc, P.wt1[i], P.wt1[i + 1], tptr, tsrc, tw);
+            transpose(ploc, pel, 2 * Lp, 2 * Lc, P.wp1[i], P.wp1[i + 1], pptr, psrc, pw);
+            EMFA_TRY(upload(c, cm.th_ptr, tptr, st));
+            EMFA_TRY(upload(c, cm.th_src, tsrc, st));
+            EMFA_TRY(upload(c, cm.th_w, tw, st));
+            EMFA_TRY(upload(c, cm.ph_ptr, pptr, st));
+            EMFA_TRY(upload(c, cm.ph_src, psrc, st));
+            EMFA_TRY(upload(c, cm.ph_w, pw, st));
+            // phi-row chunks of about 256 samples, and the parent rows each reads
+            cm.rows = down_rows(Lc);
+            const int nchunk = (2 * Lc + cm.rows - 1) / cm.rows;
+            std::vector<int2> dw(nchunk);
+            int most = 0;
+            for (int ch = 0; ch < nchunk; ++ch) {
+                int lo = 2 * Lp, hi = 0;
+                for (int pc = ch * cm.rows; pc < std::min(2 * Lc, (ch + 1) * cm.rows); ++pc)
+                    for (int a = pptr[pc]; a < pptr[pc + 1]; ++a) {
+                        lo = std::min(lo, psrc[a]);
+                        hi = std::max(hi, psrc[a] + 1);
+                    }
+                if (hi <= lo) lo = hi = 0;
+                dw[ch] = make_int2(lo, hi);
+                most = std::max(most, hi - lo);
             }
-        std::vector<int> aptr{0}, akp;
-        std::vector<float> aw;
-        for (int kc = 0; kc < Kc; ++kc) {
-            for (auto& e : tpos[kc]) {
-                akp.push_back(e.first);
-                aw.push_back(e.second);
+            cm.down_smem = sizeof(float2) * 3 * (size_t)most * Lc;
+            if (cm.down_smem > 200 * 1024) {
+                set_error(c, "mlfma: anterpolation rows exceed shared memory (level too large)");
+                return EMFA_ERR_UNSUPPORTED;
             }
-            aptr.push_back((int)akp.size());
+            EMFA_TRY(upload(c, cm.down_win, dw, st));
         }
-        EMFA_TRY(upload(c, cm.an_ptr, aptr, st));
-        EMFA_TRY(upload(c, cm.an_kp, akp, st));
-        EMFA_TRY(upload(c, cm.an_w, aw, st));
     }
     // finest-level data
     MLevel& fl = M->lv[nl - 1];
@@ -1054,6 +1314,17 @@ static emfa_status_t mlfma_build(emfa_mlfma* M, cudaStream_t st)
         nnz += (size_t)cols * fin[b].unk.size();
     }
     M->nnz = nnz;
+    {
+        // column unknowns of each box's near rows, in value order
+        std::vector<int> cbase{0}, cidx;
+        for (size_t b = 0; b < fin.size(); ++b) {
+            for (int nb : fin[b].near)
+                for (int q = 0; q < cnt_h[nb]; ++q) cidx.push_back(off_h[nb] + q);
+            cbase.push_back((int)cidx.size());
+        }
+        EMFA_TRY(upload(c, M->near_cbase, cbase, st));
+        EMFA_TRY(upload(c, M->near_cidx, cidx, st));
+    }
     EMFA_TRY(upload(c, M->near_ptr, nptr, st));
     EMFA_TRY(upload(c, M->near_box, nbox, st));
     EMFA_TRY(upload(c, M->near_col, ncol, st));
@@ -1090,34 +1361,35 @@ static emfa_status_t mlfma_apply1(emfa_mlfma* M, const float2* x, float2* y, cud
     MLevel& fl = M->lv[nl - 1];
     const int Kf = fl.K;
     k_agg_finest<<<fl.nbox, 128, 0, st>>>(x, dptr<C3f>(M->rad), dptr<int>(M->box_off), dptr<int>(M->box_cnt), Kf,
-                                          dptr<C3f>(fl.up));
+                                          dptr<float2>(fl.up));
     for (int i = nl - 2; i >= 0; --i) {
         MLevel& pm = M->lv[i];
         MLevel& cm = M->lv[i + 1];
-        size_t tot = (size_t)pm.nbox * pm.K;
-        k_upward<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(dptr<C3f>(cm.up), cm.K, dptr<int>(pm.child_ptr),
-                                                               dptr<int>(pm.child_idx), dptr<int>(cm.oct),
-                                                               dptr<int>(pm.ip_col), dptr<float>(pm.ip_w),
-                                                               dptr<float2>(pm.up_phase), pm.nbox, pm.K,
-                                                               dptr<C3f>(pm.up));
+        const dim3 grid((unsigned)pm.nbox, (unsigned)((pm.K + pm.up_bs - 1) / pm.up_bs));
+        k_upward<<<grid, pm.up_bs, pm.up_smem, st>>>(dptr<float2>(cm.up), cm.K, dptr<int>(pm.child_ptr),
+                                                     dptr<int>(pm.child_idx), dptr<int>(cm.oct), dptr<int>(pm.ip_col),
+                                                     dptr<float>(pm.ip_w), dptr<int2>(pm.up_win),
+                                                     dptr<float2>(pm.up_phase), pm.K, dptr<float2>(pm.up));
     }
     for (int i = 0; i < nl; ++i) {
         MLevel& ml = M->lv[i];
-        size_t tot = (size_t)ml.nbox * ml.K;
         const bool top = i == 0;
         MLevel& pm = M->lv[top ? 0 : i - 1];
-        k_downward<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(
-            dptr<C3f>(ml.up), dptr<int>(ml.far_ptr), dptr<int>(ml.far_box), dptr<int>(ml.far_off),
-            dptr<float2>(ml.trans), ml.nbox, ml.K, top ? nullptr : dptr<C3f>(pm.down), pm.K, dptr<int>(ml.parent),
-            dptr<int>(ml.oct), dptr<int>(ml.an_ptr), dptr<int>(ml.an_kp), dptr<float>(ml.an_w),
-            dptr<float2>(pm.up_phase), dptr<C3f>(ml.down));
+        const int R = down_rows(ml.L);
+        const int bs = std::min(256, 32 * ((R * ml.L / 2 + 31) / 32));
+        const dim3 grid((unsigned)ml.nbox, (unsigned)((2 * ml.L + R - 1) / R));
+        k_downward<<<grid, bs, top ? 0 : ml.down_smem, st>>>(
+            dptr<float4>(ml.up), dptr<int>(ml.far_ptr), dptr<int2>(ml.far), dptr<float4>(ml.trans), ml.L, R,
+            top ? nullptr : dptr<float2>(pm.down), pm.L, dptr<int2>(ml.down_win), dptr<int>(ml.parent),
+            dptr<int>(ml.oct), dptr<float2>(pm.up_phase), dptr<int>(ml.th_ptr), dptr<int>(ml.th_src),
+            dptr<float>(ml.th_w), dptr<int>(ml.ph_ptr), dptr<int>(ml.ph_src), dptr<float>(ml.ph_w),
+            dptr<float4>(ml.down));
     }
     const int n = M->n;
     k_disagg_near<<<(unsigned)(((size_t)n * 32 + 255) / 256), 256, 0, st>>>(
-        x, dptr<C3f>(M->rec), dptr<C3f>(fl.down), dptr<float>(M->coeff), parts == 1 ? 0 : Kf, dptr<int>(M->box_of),
-        dptr<int>(M->box_off), dptr<int>(M->box_cnt), dptr<int>(M->near_ptr), dptr<int>(M->near_box),
-        dptr<int>(M->near_col), dptr<int>(M->row_cols), dptr<size_t>(M->row_base), dptr<float2>(M->near_val), n,
-        parts == 2 ? 1 : 0, y);
+        x, dptr<C3f>(M->rec), dptr<float2>(fl.down), dptr<float>(M->coeff), parts == 1 ? 0 : Kf, dptr<int>(M->box_of),
+        dptr<int>(M->box_off), dptr<int>(M->row_cols), dptr<size_t>(M->row_base), dptr<int>(M->near_cbase),
+        dptr<int>(M->near_cidx), dptr<float2>(M->near_val), n, parts == 2 ? 1 : 0, y);
     c->kernel_launches += 2 * nl + 1;
     EMFA_CUDA(c, cudaGetLastError());
     return EMFA_OK;
