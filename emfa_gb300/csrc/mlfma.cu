@@ -143,7 +143,10 @@ struct MLevel {
     DevBuf far_ptr, far;                // CSR far lists: int2 {source box, offset index}
     DevBuf trans;                       // float2 [343][K]
     DevBuf up, down;                    // planar float2 [nbox][3][K]
-    DevBuf ip_col, ip_w;                // interpolation to this level from the level below: [K][9]
+    // interpolation to this level from the level below, separable: 3-point
+    // Lagrange stencils in theta (per theta index of this level: child theta,
+    // weight) and in phi (per phi index: child phi row, weight)
+    DevBuf ip_tl, ip_te, ip_pl, ip_pe;
     // anterpolation from the level above, as two transposed 1-D Lagrange
     // stencils: theta (CSR over this level's theta index: parent theta, weight)
     // and phi (CSR over this level's phi index: parent phi, weight)
@@ -152,9 +155,10 @@ struct MLevel {
     size_t down_smem = 0;               // shared bytes per CTA (theta-pass rows)
     DevBuf down_win;                    // int2 per chunk: parent phi rows its phi stencils read
     DevBuf up_phase;                    // float2 [8][K]: exp(-j k k.(parent - child)) for the level below
-    int up_bs = 0;                      // interpolation from the level below: samples per CTA,
-    size_t up_smem = 0;                 //   shared bytes per CTA,
-    DevBuf up_win;                      //   int2 per chunk: window of the children's samples it reads
+    int up_rows = 0;                    // interpolation from the level below: phi rows per CTA,
+    size_t up_child_bytes = 0;          //   shared bytes of one child's theta pass,
+    int up_batch = 0;                   //   children per shared-memory pass,
+    DevBuf up_win;                      //   int2 per chunk: the child phi rows it reads
     std::vector<float> w_host;          // quadrature weights (host)
 };
 
@@ -297,65 +301,74 @@ __global__ void k_agg_finest(const float2* __restrict__ x, const C3f* __restrict
     }
 }
 
-// interpolation + phase shift: CTA per (parent box, chunk of parent samples).
-// The children's samples that the chunk's 9-point Lagrange stencils touch
-// (window [win.x, win.y), computed per chunk on the host) are staged in
-// shared memory, as many children per pass as UP_TILE samples allow.
-constexpr int UP_TILE = 4096;  // staged samples per pass: 96 KB
-__global__ void __launch_bounds__(256) k_upward(const float2* __restrict__ child, int Kc,
-                                                const int* __restrict__ child_ptr, const int* __restrict__ child_idx,
-                                                const int* __restrict__ child_oct, const int* __restrict__ ip_col,
-                                                const float* __restrict__ ip_w, const int2* __restrict__ win,
-                                                const float2* __restrict__ phase, int K, float2* __restrict__ out)
+// interpolation + phase shift: CTA per (parent box, chunk of parent phi rows
+// [pp0, pp0 + R)); thread per parent sample (pp, t), k = pp Lp + t.  The
+// Lagrange stencil is separable: per child (in batches that fit shared memory)
+//   1. theta pass: u[row][t] = sum_it tel(t, it) child(row, tloc(t, it)) for
+//      the child phi rows [win.x, win.y) the chunk reads, into shared memory;
+//   2. phi pass: parent(pp, t) += phase_oct(pp, t) sum_ip pel(pp, ip) u[ploc(pp, ip)][t].
+__global__ void k_upward(const float2* __restrict__ child, int Lc, const int* __restrict__ child_ptr,
+                         const int* __restrict__ child_idx, const int* __restrict__ child_oct,
+                         const int* __restrict__ tl, const float* __restrict__ te, const int* __restrict__ pl,
+                         const float* __restrict__ pe, const int2* __restrict__ win, int batch,
+                         const float2* __restrict__ phase, int Lp, int R, float2* __restrict__ out)
 {
-    extern __shared__ float2 s_pat[];  // [child in pass][3][tile]
+    extern __shared__ float2 s_u[];  // [child in batch][3][rows of the window][Lp]
     const int b = blockIdx.x;
-    const int kp = blockIdx.y * blockDim.x + threadIdx.x;
-    const bool act = kp < K;
+    const int Kc = 2 * Lc * Lc, K = 2 * Lp * Lp;
+    const int pp0 = blockIdx.y * R;
+    const int nr = min(R, 2 * Lp - pp0);
     const int2 w2 = win[blockIdx.y];
-    const int W = w2.y - w2.x;
-    int col[9];
-    float w[9];
+    const int usz = (w2.y - w2.x) * Lp;  // one plane of one child
+    const int it = threadIdx.x;
+    const bool act = it < nr * Lp;
+    const int pp = pp0 + (act ? it / Lp : 0), t = act ? it % Lp : 0;
+    const int kp = pp * Lp + t;
+    int prow[3];
+    float pw[3];
 #pragma unroll
-    for (int t = 0; t < 9; ++t) {
-        col[t] = act ? ip_col[kp * 9 + t] - w2.x : 0;
-        w[t] = act ? ip_w[kp * 9 + t] : 0.f;
+    for (int ip = 0; ip < 3; ++ip) {
+        prow[ip] = (pl[3 * pp + ip] - w2.x) * Lp + t;
+        pw[ip] = pe[3 * pp + ip];
     }
     const int c0 = child_ptr[b], nch = child_ptr[b + 1] - c0;
-    const int per = W <= UP_TILE ? max(1, min(nch, UP_TILE / max(W, 1))) : 1;  // children per pass
     C3f acc = c3zero();
-    for (int cb = 0; cb < nch; cb += per) {
-        const int nb = min(per, nch - cb);
-        C3f v = c3zero();  // one child's stencil sum (nb == 1 may take several tiles)
-        for (int t0 = 0; t0 < W; t0 += UP_TILE) {
-            const int nt = min(UP_TILE, W - t0);
-            __syncthreads();  // the previous pass has been read
-            for (int cc = 0; cc < nb; ++cc) {
-                const float2* src = child + (size_t)3 * child_idx[c0 + cb + cc] * Kc + w2.x + t0;
-                float2* dst = s_pat + (size_t)cc * 3 * nt;
-                for (int q = threadIdx.x; q < 3 * nt; q += blockDim.x) {
-                    const int comp = q / nt, r = q - comp * nt;
-                    dst[q] = src[(size_t)comp * Kc + r];
-                }
-            }
-            __syncthreads();
-            for (int cc = 0; cc < nb; ++cc) {
-                const float2* sp = s_pat + (size_t)cc * 3 * nt;
+    for (int cb = 0; cb < nch; cb += batch) {
+        const int nb = min(batch, nch - cb);
+        __syncthreads();  // the previous batch has been read
+        for (int cc = 0; cc < nb; ++cc) {
+            const float2* src = child + (size_t)3 * child_idx[c0 + cb + cc] * Kc;
+            float2* dst = s_u + (size_t)cc * 3 * usz;
+            for (int i = threadIdx.x; i < usz; i += blockDim.x) {
+                const int r = i / Lp, tt = i - r * Lp;
+                const int base = (w2.x + r) * Lc;
+                float2 vx = make_float2(0, 0), vy = vx, vz = vx;
 #pragma unroll
-                for (int t = 0; t < 9; ++t) {
-                    const int r = col[t] - t0;
-                    if ((unsigned)r < (unsigned)nt) {
-                        v.x = caddf(v.x, cscalef(sp[r], w[t]));
-                        v.y = caddf(v.y, cscalef(sp[nt + r], w[t]));
-                        v.z = caddf(v.z, cscalef(sp[2 * nt + r], w[t]));
-                    }
+                for (int q = 0; q < 3; ++q) {
+                    const int kc = base + tl[3 * tt + q];
+                    const float w = te[3 * tt + q];
+                    vx = caddf(vx, cscalef(src[kc], w));
+                    vy = caddf(vy, cscalef(src[Kc + kc], w));
+                    vz = caddf(vz, cscalef(src[2 * Kc + kc], w));
                 }
-                if (nb > 1 || t0 + nt >= W) {  // this child's sum is complete
-                    if (act) c3fma(acc, phase[child_oct[child_idx[c0 + cb + cc]] * K + kp], v);
-                    v = c3zero();
-                }
+                dst[i] = vx;
+                dst[usz + i] = vy;
+                dst[2 * usz + i] = vz;
             }
         }
+        __syncthreads();
+        if (act)
+            for (int cc = 0; cc < nb; ++cc) {
+                const float2* u = s_u + (size_t)cc * 3 * usz;
+                C3f v = c3zero();
+#pragma unroll
+                for (int ip = 0; ip < 3; ++ip) {
+                    v.x = caddf(v.x, cscalef(u[prow[ip]], pw[ip]));
+                    v.y = caddf(v.y, cscalef(u[usz + prow[ip]], pw[ip]));
+                    v.z = caddf(v.z, cscalef(u[2 * usz + prow[ip]], pw[ip]));
+                }
+                c3fma(acc, phase[child_oct[child_idx[c0 + cb + cc]] * K + kp], v);
+            }
     }
     if (act) {
         float2* ob = out + (size_t)3 * b * K + kp;
@@ -1064,9 +1077,8 @@ static emfa_status_t mlfma_build(emfa_mlfma* M, cudaStream_t st)
         ml.len = P.blen[l];
         ml.w_host = gw[i];
     }
-    // the staged interpolation tiles exceed the default 48 KB of shared memory
-    EMFA_CUDA(c, cudaFuncSetAttribute(k_upward, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)(sizeof(float2) * 3 * UP_TILE)));
+    // the interpolation and anterpolation passes may use more than the default 48 KB of shared memory
+    EMFA_CUDA(c, cudaFuncSetAttribute(k_upward, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
     EMFA_CUDA(c, cudaFuncSetAttribute(k_downward, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     // per-level device tables
     for (int l = 2; l <= L; ++l) {
@@ -1153,42 +1165,32 @@ static emfa_status_t mlfma_build(emfa_mlfma* M, cudaStream_t st)
         mh::lagrange(gt[i + 1], gt[i], tloc, tel);
         mh::lagrange(gp[i + 1], gp[i], ploc, pel);
         const int Kp = pm.K, Lc = cm.L;
-        std::vector<int> col((size_t)Kp * 9);
-        std::vector<float> w((size_t)Kp * 9);
-        size_t row = 0;
-        for (int pp = 0; pp < 2 * pm.L; ++pp)
-            for (int t = 0; t < pm.L; ++t, ++row) {
-                int q = 0;
-                for (int ip = 0; ip < 3; ++ip) {
-                    int base = ploc[3 * pp + ip] * Lc;
-                    for (int it = 0; it < 3; ++it, ++q) {
-                        col[row * 9 + q] = base + tloc[3 * t + it];
-                        w[row * 9 + q] = pel[3 * pp + ip] * tel[3 * t + it];
-                    }
-                }
-            }
-        EMFA_TRY(upload(c, pm.ip_col, col, st));
-        EMFA_TRY(upload(c, pm.ip_w, w, st));
+        EMFA_TRY(upload(c, pm.ip_tl, tloc, st));
+        EMFA_TRY(upload(c, pm.ip_te, tel, st));
+        EMFA_TRY(upload(c, pm.ip_pl, ploc, st));
+        EMFA_TRY(upload(c, pm.ip_pe, pel, st));
         {
-            // CTA chunks of at most 256 parent samples (whole warps, as even as
-            // possible) and the window of child samples each chunk reads
-            const int chunks = (Kp + 255) / 256;
-            pm.up_bs = 32 * ((Kp + 32 * chunks - 1) / (32 * chunks));
-            const int nchunk = (Kp + pm.up_bs - 1) / pm.up_bs;
+            // phi-row chunks of about 256 parent samples and the child rows each reads
+            pm.up_rows = down_rows(pm.L);
+            const int nchunk = (2 * pm.L + pm.up_rows - 1) / pm.up_rows;
             std::vector<int2> win(nchunk);
-            size_t most = 0;
+            int most = 0;
             for (int ch = 0; ch < nchunk; ++ch) {
-                int lo = cm.K, hi = 0;
-                for (int kp = ch * pm.up_bs; kp < std::min(Kp, (ch + 1) * pm.up_bs); ++kp)
-                    for (int q = 0; q < 9; ++q) {
-                        lo = std::min(lo, col[(size_t)kp * 9 + q]);
-                        hi = std::max(hi, col[(size_t)kp * 9 + q] + 1);
+                int lo = 2 * Lc, hi = 0;
+                for (int pp = ch * pm.up_rows; pp < std::min(2 * pm.L, (ch + 1) * pm.up_rows); ++pp)
+                    for (int ip = 0; ip < 3; ++ip) {
+                        lo = std::min(lo, ploc[3 * pp + ip]);
+                        hi = std::max(hi, ploc[3 * pp + ip] + 1);
                     }
                 win[ch] = make_int2(lo, hi);
-                const int W = hi - lo;
-                most = std::max(most, (size_t)(W <= UP_TILE ? std::min(8, UP_TILE / std::max(W, 1)) * W : UP_TILE));
+                most = std::max(most, hi - lo);
             }
-            pm.up_smem = sizeof(float2) * 3 * most;
+            pm.up_child_bytes = sizeof(float2) * 3 * (size_t)most * pm.L;
+            pm.up_batch = (int)std::min<size_t>(8, (96 * 1024) / pm.up_child_bytes);
+            if (pm.up_batch < 1) {
+                set_error(c, "mlfma: interpolation rows exceed shared memory (level too large)");
+                return EMFA_ERR_UNSUPPORTED;
+            }
             EMFA_TRY(upload(c, pm.up_win, win, st));
         }
         // phases for the children of level i: exp(-j k kp . (parent - child)), per octant
@@ -1365,11 +1367,13 @@ static emfa_status_t mlfma_apply1(emfa_mlfma* M, const float2* x, float2* y, cud
     for (int i = nl - 2; i >= 0; --i) {
         MLevel& pm = M->lv[i];
         MLevel& cm = M->lv[i + 1];
-        const dim3 grid((unsigned)pm.nbox, (unsigned)((pm.K + pm.up_bs - 1) / pm.up_bs));
-        k_upward<<<grid, pm.up_bs, pm.up_smem, st>>>(dptr<float2>(cm.up), cm.K, dptr<int>(pm.child_ptr),
-                                                     dptr<int>(pm.child_idx), dptr<int>(cm.oct), dptr<int>(pm.ip_col),
-                                                     dptr<float>(pm.ip_w), dptr<int2>(pm.up_win),
-                                                     dptr<float2>(pm.up_phase), pm.K, dptr<float2>(pm.up));
+        const int R = pm.up_rows;
+        const int bs = 32 * ((R * pm.L + 31) / 32);
+        const dim3 grid((unsigned)pm.nbox, (unsigned)((2 * pm.L + R - 1) / R));
+        k_upward<<<grid, bs, pm.up_child_bytes * pm.up_batch, st>>>(
+            dptr<float2>(cm.up), cm.L, dptr<int>(pm.child_ptr), dptr<int>(pm.child_idx), dptr<int>(cm.oct),
+            dptr<int>(pm.ip_tl), dptr<float>(pm.ip_te), dptr<int>(pm.ip_pl), dptr<float>(pm.ip_pe),
+            dptr<int2>(pm.up_win), pm.up_batch, dptr<float2>(pm.up_phase), pm.L, R, dptr<float2>(pm.up));
     }
     for (int i = 0; i < nl; ++i) {
         MLevel& ml = M->lv[i];
