@@ -34,6 +34,20 @@ void set_error(Ctx* ctx, const std::string& msg)
     set_global_error(msg);
 }
 
+emfa_status_t ensure_smem_raw(Ctx* c, const void* func, size_t bytes)
+{
+    static std::mutex mu;
+    static std::map<std::pair<const void*, int>, size_t> limit;
+    int dev = c ? c->device : 0;
+    if (!c) EMFA_CUDA(c, cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> g(mu);
+    size_t& cur = limit[std::make_pair(func, dev)];
+    if (cur >= bytes) return EMFA_OK;
+    EMFA_CUDA(c, cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    cur = bytes;
+    return EMFA_OK;
+}
+
 emfa_status_t ctx_alloc(Ctx* c, size_t bytes, void** p)
 {
     {

@@ -109,6 +109,17 @@ struct Ctx {
 
 emfa_status_t ctx_workspace(Ctx* c, int slot, size_t bytes, void** p);
 
+// Raises the kernel's dynamic shared-memory limit on the context's device to
+// at least `bytes`; the limit never goes down.  Lanes of the server launch
+// the same kernels concurrently with different sizes, and a limit lowered by
+// one lane between another lane's raise and its launch fails that launch.
+emfa_status_t ensure_smem_raw(Ctx* c, const void* func, size_t bytes);
+template <typename F>
+inline emfa_status_t ensure_smem(Ctx* c, F* func, size_t bytes)
+{
+    return ensure_smem_raw(c, reinterpret_cast<const void*>(func), bytes);
+}
+
 // Brackets one kernel launch with events on its stream when the context's
 // kernel timing is on; does nothing otherwise.
 class TimedLaunch {

@@ -481,8 +481,8 @@ static emfa_status_t fill_z_t(Ctx* c, Geom* g, GeomDev<T>& d, const emfa_fill_pa
         // FP32: the tiled kernel
         EMFA_TRY(tile_plan(c, g, st));
         const size_t sm = tile_smem(g->tile_maxt);
-        EMFA_CUDA(c, cudaFuncSetAttribute(k_fill_tile<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-        EMFA_CUDA(c, cudaFuncSetAttribute(k_fill_tile<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        EMFA_TRY(ensure_smem(c, k_fill_tile<true>, sm));
+        EMFA_TRY(ensure_smem(c, k_fill_tile<false>, sm));
         const dim3 grd((g->n + FT - 1) / FT, (g->n + FT - 1) / FT);
         const FillConst<float> fc32 = make_fill_const<float>(p);
         {

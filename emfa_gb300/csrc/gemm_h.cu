@@ -574,12 +574,7 @@ static emfa_status_t launch_h(Ctx* c, const CUtensorMap& ta, const CUtensorMap& 
                               const float* inv_s, const float* inv_t, int* err, cudaStream_t st)
 {
     using S = th::Smem<BN, MS>;
-    static std::atomic<unsigned long long> attr_set{0};  // one bit per device
-    const unsigned long long bit = 1ull << (c->device & 63);
-    if (!(attr_set.load() & bit)) {
-        EMFA_CUDA(c, cudaFuncSetAttribute(th::k_hgemm<BN, MS>, cudaFuncAttributeMaxDynamicSharedMemorySize, S::TOTAL));
-        attr_set.fetch_or(bit);
-    }
+    EMFA_TRY(ensure_smem(c, th::k_hgemm<BN, MS>, S::TOTAL));
     dim3 grd((2 * nrhs + BN - 1) / BN, (n + th::BM * MS - 1) / (th::BM * MS));
     const int kblocks = (2 * n + th::BKH - 1) / th::BKH;
     {
@@ -707,12 +702,7 @@ emfa_status_t hgemm_residual(Ctx* c, const HPlanes& h, const double2* X, const v
     EMFA_TRY(make_map_h(c, &a1, h.zl, 2 * (uint64_t)n, (uint64_t)n, ldh, th::BM));
     EMFA_TRY(make_map_h(c, &b0, bh, 2 * (uint64_t)n, 2 * (uint64_t)nrhs, ldh, th::RBN));
     EMFA_TRY(make_map_h(c, &b1, bl, 2 * (uint64_t)n, 2 * (uint64_t)nrhs, ldh, th::RBN));
-    static std::atomic<unsigned long long> attr_set{0};
-    const unsigned long long bit = 1ull << (c->device & 63);
-    if (!(attr_set.load() & bit)) {
-        EMFA_CUDA(c, cudaFuncSetAttribute(th::k_hresid, cudaFuncAttributeMaxDynamicSharedMemorySize, S::TOTAL));
-        attr_set.fetch_or(bit);
-    }
+    EMFA_TRY(ensure_smem(c, th::k_hresid, S::TOTAL));
     dim3 grd((2 * nrhs + th::RBN - 1) / th::RBN, (n + th::BM - 1) / th::BM);
     const int kblocks = (2 * n + th::BKH - 1) / th::BKH;
     {

@@ -210,11 +210,7 @@ static emfa_status_t launch_tc(Ctx* c, const CUtensorMap& ta, const CUtensorMap&
                                int* err, cudaStream_t st)
 {
     using S = tc::Smem<BN>;
-    static bool attr = false;
-    if (!attr) {
-        EMFA_CUDA(c, cudaFuncSetAttribute(tc::k_gemm_tf32<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, S::TOTAL));
-        attr = true;
-    }
+    EMFA_TRY(ensure_smem(c, tc::k_gemm_tf32<BN>, S::TOTAL));
     dim3 grd((2 * nrhs + BN - 1) / BN, (n + tc::BM - 1) / tc::BM);
     int kblocks = (2 * n + tc::BK - 1) / tc::BK;
     {

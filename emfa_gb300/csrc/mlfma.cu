@@ -1021,7 +1021,7 @@ static emfa_status_t sai_build(emfa_mlfma* M, const Plan& P, cudaStream_t st)
     EMFA_TRY(upload(c, M->csr_col, ccol, st));
     EMFA_TRY(M->csr_val.alloc(c, sizeof(float2) * std::max<size_t>(nnz, 1)));
     EMFA_TRY(M->pre_tmp.alloc(c, sizeof(float2) * (size_t)n));
-    EMFA_CUDA(c, cudaFuncSetAttribute(k_sai, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    EMFA_TRY(ensure_smem(c, k_sai, smem));
     k_sai<<<nbox, 128, smem, st>>>(dptr<int>(d_rptr), dptr<int>(d_rows), dptr<int>(d_cptr), dptr<int>(d_cols),
                                    dptr<int>(d_own), dptr<int>(M->box_cnt), dptr<size_t>(d_ebase), dptr<int>(d_dest),
                                    dptr<int>(M->box_of), dptr<int>(M->box_off), dptr<int>(M->near_ptr),
@@ -1078,8 +1078,8 @@ static emfa_status_t mlfma_build(emfa_mlfma* M, cudaStream_t st)
         ml.w_host = gw[i];
     }
     // the interpolation and anterpolation passes may use more than the default 48 KB of shared memory
-    EMFA_CUDA(c, cudaFuncSetAttribute(k_upward, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
-    EMFA_CUDA(c, cudaFuncSetAttribute(k_downward, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    EMFA_TRY(ensure_smem(c, k_upward, 96 * 1024));
+    EMFA_TRY(ensure_smem(c, k_downward, 200 * 1024));
     // per-level device tables
     for (int l = 2; l <= L; ++l) {
         const int i = l - 2;
