@@ -20,7 +20,7 @@ STATUS = {0: "EMFA_OK", 1: "EMFA_ERR_INVALID", 2: "EMFA_ERR_CUDA", 3: "EMFA_ERR_
           4: "EMFA_ERR_NOT_CONVERGED", 5: "EMFA_ERR_MESH", 6: "EMFA_ERR_UNSUPPORTED", 7: "EMFA_ERR_TIMEOUT"}
 EMFA_F32, EMFA_F64 = 0, 1
 EMFA_EFIE, EMFA_CFIE = 0, 1
-EMFA_GMRES, EMFA_BICGSTAB = 0, 1
+EMFA_GMRES, EMFA_BICGSTAB, EMFA_LU = 0, 1, 2
 EMFA_MV_AUTO, EMFA_MV_F64, EMFA_MV_F32, EMFA_MV_TF32, EMFA_MV_F16X = 0, 1, 2, 3, 4
 
 

@@ -45,8 +45,9 @@ def solver_params(method="gmres", restart=30, max_iter=600, tol=1e-6, tol_absolu
                   max_refine=0, orth="auto") -> L.SolverParams:
     mv = {"auto": 0, "f64": 1, "f32": 2, "tf32": 3, "f16x": 4}[matvec]
     og = {"auto": 0, "cgs1": 1, "cgs2": 2}[orth]
-    return L.SolverParams(L.EMFA_BICGSTAB if method == "bicgstab" else L.EMFA_GMRES, int(restart), int(max_iter),
-                          float(tol), int(bool(tol_absolute)), mv, int(max_refine), og)
+    meth = {"gmres": L.EMFA_GMRES, "bicgstab": L.EMFA_BICGSTAB, "lu": L.EMFA_LU}[method]
+    return L.SolverParams(meth, int(restart), int(max_iter), float(tol), int(bool(tol_absolute)), mv, int(max_refine),
+                          og)
 
 
 class Context:

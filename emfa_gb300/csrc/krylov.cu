@@ -18,6 +18,7 @@
 #include "emfa_math.cuh"
 #include "gemm.cuh"
 #include "krylov.cuh"
+#include "lu.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -1177,6 +1178,103 @@ struct DenseOp : LinOp {
     }
 };
 
+__global__ void k_add_f32_c128(double2* __restrict__ X, const float2* __restrict__ D, size_t tot)
+{
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < tot; i += (size_t)gridDim.x * blockDim.x) {
+        const float2 d = D[i];
+        X[i].x += (double)d.x;
+        X[i].y += (double)d.y;
+    }
+}
+
+// Dense solve by LU with FP64 iterative refinement (EMFA_LU): factor Z once in
+// FP32 (lu.cu), x = (LU)^-1 b, then per pass the true residual r = b - Z x
+// from the operator's refinement residual (FP64-accurate) and x += (LU)^-1 r,
+// until every right-hand side meets the tolerance.  A zero pivot, or a pass
+// that fails to halve the worst residual, hands the remaining correction to
+// GMRES-IR on the same operator.
+static emfa_status_t lu_refined(Ctx* c, LinOp& A, const void* Z, const void* B, int nrhs, double2* X,
+                                const emfa_solver_params_t* sp, emfa_solve_info_t* info, cudaStream_t st)
+{
+    const int n = A.n;
+    const size_t vec = (size_t)n * nrhs;
+    LuFactor F;
+    EMFA_TRY(lu_factor(c, Z, n, F, st));
+    int zero_pivot = 0;
+    EMFA_TRY(lu_zero_pivot(c, F, &zero_pivot, st));
+    DevBuf work, d32, r64, r32, db, nb, rr;
+    EMFA_TRY(work.alloc(c, sizeof(float2) * 2 * vec));
+    EMFA_TRY(d32.alloc(c, sizeof(float2) * vec));
+    EMFA_TRY(r64.alloc(c, sizeof(double2) * vec));
+    EMFA_TRY(r32.alloc(c, sizeof(float2) * vec));
+    EMFA_TRY(db.alloc(c, sizeof(double2) * vec));
+    EMFA_TRY(nb.alloc(c, sizeof(double2) * nrhs));
+    EMFA_TRY(rr.alloc(c, sizeof(double) * nrhs));
+    k_to_f64<<<grid1(vec), 256, 0, st>>>((const float2*)B, dptr<double2>(r64), vec);
+    EMFA_TRY(dots_d(c, dptr<double2>(r64), dptr<double2>(r64), n, nrhs, dptr<double2>(db), dptr<double2>(nb), st));
+    if (zero_pivot == 0) {
+        EMFA_TRY(lu_apply(c, F, (const float2*)B, nrhs, dptr<float2>(d32), dptr<float2>(work), st));
+        k_to_f64<<<grid1(vec), 256, 0, st>>>(dptr<float2>(d32), X, vec);
+    } else {
+        EMFA_CUDA(c, cudaMemsetAsync(X, 0, sizeof(double2) * vec, st));
+    }
+    c->kernel_launches += 2;
+    const int passes = sp->max_refine > 0 ? sp->max_refine : 10;
+    std::vector<double> rel(nrhs);
+    double prev = 1e300, worst = 1e300;
+    int pass = 0;
+    for (;; ++pass) {
+        EMFA_TRY(A.residual(c, X, B, dptr<double2>(r64), nrhs, dptr<float2>(r32), st));
+        k_norm_ratio<<<(nrhs + 127) / 128, 128, 0, st>>>(dptr<double2>(r64), dptr<double2>(nb), n, nrhs,
+                                                         dptr<double>(rr));
+        EMFA_CUDA(c, cudaMemcpyAsync(rel.data(), rr.ptr, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, st));
+        EMFA_CUDA(c, cudaStreamSynchronize(st));
+        c->kernel_launches += 1;
+        worst = *std::max_element(rel.begin(), rel.end());
+        if (worst < sp->tol) {
+            if (info) {
+                info->converged = nrhs;
+                info->iterations = pass;
+                info->cycles = pass + 1;
+                info->max_rel_residual = worst;
+            }
+            return EMFA_OK;
+        }
+        if (zero_pivot != 0 || pass >= passes || !(worst < 0.5 * prev)) break;
+        prev = worst;
+        k_to_f32<<<grid1(vec), 256, 0, st>>>(dptr<double2>(r64), dptr<float2>(r32), vec);
+        EMFA_TRY(lu_apply(c, F, dptr<float2>(r32), nrhs, dptr<float2>(d32), dptr<float2>(work), st));
+        k_add_f32_c128<<<grid1(vec), 256, 0, st>>>(X, dptr<float2>(d32), vec);
+        c->kernel_launches += 2;
+    }
+    // the factor did not carry the solve: GMRES-IR on the correction A d = r
+    F.release();
+    work.release();
+    k_to_f32<<<grid1(vec), 256, 0, st>>>(dptr<double2>(r64), dptr<float2>(r32), vec);
+    c->kernel_launches += 1;
+    emfa_solver_params_t sp2 = *sp;
+    sp2.method = EMFA_GMRES;
+    sp2.tol = std::min(0.5, sp->tol / std::max(worst, 1e-30));
+    emfa_solve_info_t in2{};
+    emfa_status_t s = gmres_t<float>(c, A, dptr<float2>(r32), nrhs, dptr<double2>(db), &sp2, &in2, st);
+    if (s != EMFA_OK && s != EMFA_ERR_NOT_CONVERGED) return s;
+    k_add_c128<<<grid1(vec), 256, 0, st>>>(X, dptr<double2>(db), vec);
+    EMFA_TRY(A.residual(c, X, B, dptr<double2>(r64), nrhs, dptr<float2>(r32), st));
+    k_norm_ratio<<<(nrhs + 127) / 128, 128, 0, st>>>(dptr<double2>(r64), dptr<double2>(nb), n, nrhs, dptr<double>(rr));
+    EMFA_CUDA(c, cudaMemcpyAsync(rel.data(), rr.ptr, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, st));
+    EMFA_CUDA(c, cudaStreamSynchronize(st));
+    c->kernel_launches += 2;
+    int conv = 0;
+    for (double v : rel) conv += v < sp->tol;
+    if (info) {
+        info->iterations = pass + in2.iterations;
+        info->cycles = pass + 1 + in2.cycles;
+        info->converged = conv;
+        info->max_rel_residual = *std::max_element(rel.begin(), rel.end());
+    }
+    return conv == nrhs ? EMFA_OK : EMFA_ERR_NOT_CONVERGED;
+}
+
 // matvec mode of the dense operator; TF32 needs even n and a 16-byte aligned Z
 static int dense_mode(int prec, int matvec, const void* Z, int n)
 {
@@ -1195,6 +1293,7 @@ emfa_status_t solve_dense(Ctx* c, int prec, const void* Z, int n, const void* B,
     A.Z = Z;
     A.mode = dense_mode(prec, sp->matvec, Z, n);
     EMFA_TRY(A.prepare(c, st));
+    if (sp->method == EMFA_LU) return lu_refined(c, A, Z, B, nrhs, (double2*)X, sp, info, st);
     return solve_op(c, A, B, nrhs, X, sp, info, st);
 }
 }  // namespace emfa
@@ -1262,9 +1361,13 @@ emfa_status_t emfa_solve(emfa_ctx_t* ctx, int prec, const void* Z_dev, int n, co
         set_error(ctx, "emfa_solve: bad arguments");
         return EMFA_ERR_INVALID;
     }
-    if (sp->method != EMFA_GMRES && sp->method != EMFA_BICGSTAB) {
-        set_error(ctx, "emfa_solve: method must be EMFA_GMRES or EMFA_BICGSTAB");
+    if (sp->method != EMFA_GMRES && sp->method != EMFA_BICGSTAB && sp->method != EMFA_LU) {
+        set_error(ctx, "emfa_solve: method must be EMFA_GMRES, EMFA_BICGSTAB or EMFA_LU");
         return EMFA_ERR_INVALID;
+    }
+    if (sp->method == EMFA_LU && prec != EMFA_F32) {
+        set_error(ctx, "emfa_solve: EMFA_LU factors in FP32 and refines in FP64; it takes EMFA_F32 operands");
+        return EMFA_ERR_UNSUPPORTED;
     }
     EMFA_CUDA(ctx, cudaSetDevice(ctx->device));
     cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;

@@ -10,11 +10,11 @@
 //              fits in what the running requests leave of the budget, else
 //              the oldest one that fits; a request larger than the whole
 //              budget runs alone once nothing else does
-//   methods    dense (fill, split-FP16 GMRES-IR, RCS) up to dense_max
-//              unknowns: CFIE GMRES(30) to 1e-6, EFIE GMRES(250) to 1e-5 by
-//              default; MLFMA (CFIE operator, GMRES(30) to 1e-3 in box
-//              order) above; each problem keeps its operators and Krylov
-//              state on its lane until it finishes
+//   methods    dense up to dense_max unknowns: fill, then CFIE split-FP16
+//              GMRES(30)-IR to 1e-6, EFIE FP32 LU with FP64 refinement to
+//              1e-5 by default, then RCS; MLFMA (CFIE operator, GMRES(30) to
+//              1e-3 in box order) above; each problem keeps its operators and
+//              Krylov state on its lane until it finishes
 #include "emfa_internal.cuh"
 #include "gemm.cuh"
 
@@ -54,8 +54,9 @@ struct Engine {
 };
 
 // Device bytes a request holds while it runs (upper estimates).
-//   dense: Z complex64 + its two FP16 planes (16 N^2), Krylov basis and
-//          vectors (~40 N R complex64), packed right-hand sides, geometry
+//   dense: Z complex64 + its two FP16 planes (16 N^2), for EFIE also the LU
+//          factor (8 N^2), Krylov basis and vectors (~40 N R complex64),
+//          packed right-hand sides, geometry
 //   MLFMA: radiation + receive patterns (2 x 3 x complex64 x K_f, K_f <= 160
 //          at a 0.25-wavelength finest box), near field (~110 entries a
 //          row), level patterns, Krylov state
@@ -67,7 +68,7 @@ size_t estimate_bytes(const emfa_request_t& r, int dense_max, int* method)
     *method = m;
     double b;
     if (m == 1)
-        b = 16.0 * N * N + 40.0 * 8 * N * R + 16.0 * 2 * N * R + 2048.0 * N;
+        b = (r.kind == EMFA_EFIE ? 24.0 : 16.0) * N * N + 40.0 * 8 * N * R + 16.0 * 2 * N * R + 2048.0 * N;
     else
         b = 2.0 * 3 * 8 * 160 * N + 110.0 * 8 * N + 1500.0 * N + 40.0 * 8 * N * R + 2048.0 * N;
     return (size_t)(b * 1.1) + (64u << 20);
@@ -100,12 +101,15 @@ emfa_status_t run_dense(Ctx* c, Geom* g, const emfa_request_t& r, int n, emfa_re
     cudaStream_t st = c->stream;
     // pairs beyond 3 wavelengths by ordinary quadrature (the reference zeroes them)
     emfa_fill_params_t fp{r.kind, EMFA_F32, r.freq, r.kind == EMFA_CFIE ? r.alpha : 1.0, 0.0, 0.0, 2};
-    // EFIE (first kind) is ill-conditioned on these meshes: GMRES(30) stalls
-    // near 1e-3 and the FP32 matrix resolves residuals to about 1e-6, so EFIE
-    // gets a long restart and 1e-5 by default; CFIE GMRES(30) to 1e-6
+    // EFIE (first kind) is ill-conditioned on these meshes: restarted GMRES
+    // needs hundreds of iterations, so EFIE is factored (FP32 LU, FP64
+    // refinement, GMRES(250)-IR if the refinement stalls) and solved to 1e-5
+    // by default (the FP32 matrix resolves residuals to about 1e-6); CFIE
+    // converges in tens of GMRES(30) iterations, to 1e-6
     const bool efie = r.kind == EMFA_EFIE;
-    emfa_solver_params_t sp{EMFA_GMRES, efie ? 250 : 30, r.max_iter > 0 ? r.max_iter : (efie ? 5000 : 3000),
-                            r.tol > 0 ? r.tol : (efie ? 1e-5 : 1e-6), 0, EMFA_MV_AUTO, 0, 0};
+    emfa_solver_params_t sp{efie ? EMFA_LU : EMFA_GMRES, efie ? 250 : 30,
+                            r.max_iter > 0 ? r.max_iter : (efie ? 5000 : 3000), r.tol > 0 ? r.tol : (efie ? 1e-5 : 1e-6),
+                            0, EMFA_MV_AUTO, 0, 0};
     DevBuf Z, V, X;
     EMFA_TRY(Z.alloc(c, 8 * (size_t)n * n));
     EMFA_TRY(V.alloc(c, 8 * (size_t)n * r.n_inc));

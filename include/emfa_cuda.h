@@ -39,7 +39,11 @@ typedef enum {
 
 typedef enum { EMFA_F32 = 0, EMFA_F64 = 1 } emfa_precision_t;
 typedef enum { EMFA_EFIE = 0, EMFA_CFIE = 1 } emfa_kind_t;
-typedef enum { EMFA_GMRES = 0, EMFA_BICGSTAB = 1 } emfa_method_t;
+/* EMFA_LU: dense only (emfa_solve, EMFA_F32): FP32 LU of Z, then FP64
+ * iterative refinement on the true residual, GMRES-IR if the refinement
+ * stalls.  No counterpart in the reference, whose dense solves are iterative
+ * (EMSolver/EFIE.cpp:89 has a commented-out Eigen LU). */
+typedef enum { EMFA_GMRES = 0, EMFA_BICGSTAB = 1, EMFA_LU = 2 } emfa_method_t;
 typedef enum {
     EMFA_MV_AUTO = 0,  /* F64: FP64 SIMT; F32: EMFA_MV_F16X                          */
     EMFA_MV_F64 = 1,   /* FP64 complex GEMM on CUDA cores (plain path)               */
