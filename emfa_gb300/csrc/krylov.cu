@@ -1026,18 +1026,27 @@ __global__ void k_add_c128(double2* __restrict__ X, const double2* __restrict__ 
     if (id < tot) X[id] = make_double2(X[id].x + D[id].x, X[id].y + D[id].y);
 }
 
-__global__ void k_norm_ratio(const double2* __restrict__ R, const double2* __restrict__ B2, int n, int nrhs,
-                             double* __restrict__ out)
+// out[r] = ||R_r|| / ||B_r|| with B2 holding ||B_r||^2 in .x: CTA per RHS
+// (256 threads), FP64 sums
+__global__ void __launch_bounds__(256) k_norm_ratio(const double2* __restrict__ R, const double2* __restrict__ B2,
+                                                    int n, int nrhs, double* __restrict__ out)
 {
-    // out[r] = ||R_r|| / ||B_r|| with B2 holding ||B_r||^2 in .x (one thread per RHS, FP64)
-    int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= nrhs) return;
+    __shared__ double ws[8];
+    const int r = blockIdx.x;
     double s = 0;
-    for (int k = 0; k < n; ++k) {
-        double2 v = R[(size_t)r * n + k];
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const double2 v = R[(size_t)r * n + k];
         s += v.x * v.x + v.y * v.y;
     }
-    out[r] = B2[r].x > 0 ? sqrt(s / B2[r].x) : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0;
+        for (int w = 0; w < 8; ++w) t += ws[w];
+        out[r] = B2[r].x > 0 ? sqrt(t / B2[r].x) : 0.0;
+    }
 }
 
 // BiCGStab with FP32 products: the recursively updated residual drifts from
@@ -1065,7 +1074,7 @@ static emfa_status_t bicgstab_refined(Ctx* c, LinOp& A, const void* B, int nrhs,
     std::vector<double> rel(nrhs);
     for (int pass = 0; pass < passes; ++pass) {
         EMFA_TRY(A.residual(c, X, B, dptr<double2>(rb), nrhs, dptr<float2>(xt), st));
-        k_norm_ratio<<<(nrhs + 127) / 128, 128, 0, st>>>(dptr<double2>(rb), dptr<double2>(nb), A.n, nrhs,
+        k_norm_ratio<<<nrhs, 256, 0, st>>>(dptr<double2>(rb), dptr<double2>(nb), A.n, nrhs,
                                                          dptr<double>(rr));
         EMFA_CUDA(c, cudaMemcpyAsync(rel.data(), rr.ptr, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, st));
         EMFA_CUDA(c, cudaStreamSynchronize(st));
@@ -1225,7 +1234,7 @@ static emfa_status_t lu_refined(Ctx* c, LinOp& A, const void* Z, const void* B, 
     int pass = 0;
     for (;; ++pass) {
         EMFA_TRY(A.residual(c, X, B, dptr<double2>(r64), nrhs, dptr<float2>(r32), st));
-        k_norm_ratio<<<(nrhs + 127) / 128, 128, 0, st>>>(dptr<double2>(r64), dptr<double2>(nb), n, nrhs,
+        k_norm_ratio<<<nrhs, 256, 0, st>>>(dptr<double2>(r64), dptr<double2>(nb), n, nrhs,
                                                          dptr<double>(rr));
         EMFA_CUDA(c, cudaMemcpyAsync(rel.data(), rr.ptr, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, st));
         EMFA_CUDA(c, cudaStreamSynchronize(st));
@@ -1260,7 +1269,7 @@ static emfa_status_t lu_refined(Ctx* c, LinOp& A, const void* Z, const void* B, 
     if (s != EMFA_OK && s != EMFA_ERR_NOT_CONVERGED) return s;
     k_add_c128<<<grid1(vec), 256, 0, st>>>(X, dptr<double2>(db), vec);
     EMFA_TRY(A.residual(c, X, B, dptr<double2>(r64), nrhs, dptr<float2>(r32), st));
-    k_norm_ratio<<<(nrhs + 127) / 128, 128, 0, st>>>(dptr<double2>(r64), dptr<double2>(nb), n, nrhs, dptr<double>(rr));
+    k_norm_ratio<<<nrhs, 256, 0, st>>>(dptr<double2>(r64), dptr<double2>(nb), n, nrhs, dptr<double>(rr));
     EMFA_CUDA(c, cudaMemcpyAsync(rel.data(), rr.ptr, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, st));
     EMFA_CUDA(c, cudaStreamSynchronize(st));
     c->kernel_launches += 2;

@@ -305,24 +305,29 @@ constexpr int RC = 8;  // right-hand sides per CTA of a sweep step
 // One step of the forward (dir 0, L) or backward (dir 1, U) sweep for block
 // k0: x = inv W[block] for the CTA's right-hand sides (CTA x = 0 stores it in
 // Out), then W[rows] -= A[rows][block] x on the CTA's 64-row chunk of the rows
-// after (dir 0) or before (dir 1) the block.
+// after (dir 0) or before (dir 1) the block.  The block's inverse, then the
+// chunk's 64 x 64 slice of A, are staged in shared memory.
 __global__ void __launch_bounds__(256) k_lu_sweep(const float2* __restrict__ A, int n, int k0, int nb,
                                                   const float2* __restrict__ inv, int dir, int nrhs,
                                                   float2* __restrict__ W, float2* __restrict__ Out)
 {
+    __shared__ float2 M[NB][LDS];  // inverse of the block, then the chunk's slice of A
+    __shared__ float2 ws[RC][NB];
     __shared__ float2 xs[RC][NB];
-    __shared__ float2 As[NB][LDS];
     const int tid = threadIdx.x;
     const int rb = blockIdx.y * RC, nr = min(RC, nrhs - rb);
     const float2* iv = inv + (size_t)(k0 / NB) * NB * NB;
-    // x = inv w for this block (inv is zero outside nb)
+    for (int q = tid; q < NB * NB; q += blockDim.x) M[q / NB][q % NB] = iv[q];
+    for (int q = tid; q < RC * NB; q += blockDim.x) {
+        const int r = q / NB, j = q % NB;
+        ws[r][j] = (r < nr && j < nb) ? W[(size_t)(rb + r) * n + k0 + j] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
     for (int q = tid; q < RC * NB; q += blockDim.x) {
         const int r = q / NB, i = q % NB;
         float2 s = make_float2(0.f, 0.f);
-        if (r < nr && i < nb) {
-            const float2* w = W + (size_t)(rb + r) * n + k0;
-            for (int j = 0; j < nb; ++j) s = cfma(iv[i * NB + j], w[j], s);
-        }
+#pragma unroll 8
+        for (int j = 0; j < NB; ++j) s = cfma(M[i][j], ws[r][j], s);
         xs[r][i] = s;
     }
     __syncthreads();
@@ -335,17 +340,17 @@ __global__ void __launch_bounds__(256) k_lu_sweep(const float2* __restrict__ A, 
     const int lo = dir == 0 ? k0 + nb : 0, hi = dir == 0 ? n : k0;
     const int m0 = lo + blockIdx.x * NB;
     const int nm = min(NB, hi - m0);
-    if (nm <= 0) return;  // no barrier follows
+    if (nm <= 0) return;  // uniform over the CTA; no barrier follows
     for (int q = tid; q < NB * NB; q += blockDim.x) {
         const int i = q / NB, j = q % NB;
-        As[i][j] = (i < nm && j < nb) ? A[(size_t)(m0 + i) * n + k0 + j] : make_float2(0.f, 0.f);
+        M[i][j] = (i < nm && j < nb) ? A[(size_t)(m0 + i) * n + k0 + j] : make_float2(0.f, 0.f);
     }
     __syncthreads();
     for (int q = tid; q < nm * nr; q += blockDim.x) {
         const int i = q % nm, r = q / nm;
         float2 s = make_float2(0.f, 0.f);
 #pragma unroll 8
-        for (int j = 0; j < NB; ++j) s = cfma(As[i][j], xs[r][j], s);
+        for (int j = 0; j < NB; ++j) s = cfma(M[i][j], xs[r][j], s);
         float2* w = W + (size_t)(rb + r) * n + m0 + i;
         *w = make_float2(w->x - s.x, w->y - s.y);
     }
