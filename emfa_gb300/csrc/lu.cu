@@ -12,6 +12,9 @@
 //   k_lu_rowperm  the block's row exchanges applied to the other columns
 //   k_lu_small    U12 = L11^-1 A12 and L21 = A21 U11^-1 with those inverses
 //   k_lu_update   A22 -= L21 U12, 64 x 64 CTA tiles, K = 64
+// with a one-block lookahead: the next block's 64 columns are updated first,
+// and that block's k_lu_diag (one CTA, latency bound) runs while a helper
+// stream updates the remaining columns.
 // Solve for many right-hand sides (RHS-major, (r, u) at r n + u): gather by
 // the row permutation, then one launch per block for the forward (L) sweep
 // and one per block for the backward (U) sweep.  Each CTA applies the block's
@@ -243,15 +246,15 @@ __global__ void __launch_bounds__(256) k_lu_small(float2* __restrict__ A, int n,
         }
 }
 
-// trailing update A22 -= L21 U12 on the 64 x 64 tile (blockIdx.y, blockIdx.x)
-// of [k1, n)^2, K = nb <= 64
-__global__ void __launch_bounds__(256) k_lu_update(float2* __restrict__ A, int n, int k0, int nb)
+// trailing update A22 -= L21 U12 on the 64 x 64 tile (blockIdx.y, blockIdx.x +
+// ct0) of [k1, n)^2, K = nb <= 64
+__global__ void __launch_bounds__(256) k_lu_update(float2* __restrict__ A, int n, int k0, int nb, int ct0)
 {
     extern __shared__ float2 s_lu[];
     float2* As = s_lu;          // [k][LDS]: L21 tile, transposed
     float2* Bs = As + NB * LDS; // [k][LDS]: U12 tile
     const int k1 = k0 + nb, m = n - k1, tid = threadIdx.x;
-    const int r0 = blockIdx.y * NB, c0 = blockIdx.x * NB;
+    const int r0 = blockIdx.y * NB, c0 = (blockIdx.x + ct0) * NB;
     for (int q = tid; q < NB * NB; q += blockDim.x) {
         const int i = q / NB, k = q % NB;  // L21: row i, column k (coalesced along k)
         As[k * LDS + i] = (r0 + i < m && k < nb) ? A[(size_t)(k1 + r0 + i) * n + k0 + k] : make_float2(0.f, 0.f);
@@ -389,22 +392,55 @@ emfa_status_t lu_factor(Ctx* c, const void* Z, int n, LuFactor& F, cudaStream_t 
     if (Z != A) EMFA_CUDA(c, cudaMemcpyAsync(A, Z, sizeof(float2) * (size_t)n * n, cudaMemcpyDeviceToDevice, st));
     EMFA_CUDA(c, cudaMemsetAsync(F.info.ptr, 0, sizeof(int), st));
     const size_t s2 = 2 * sizeof(float2) * NB * LDS, s3 = 3 * sizeof(float2) * NB * LDS;
-    for (int kb = 0; kb < F.nblk; ++kb) {
-        const int k0 = kb * NB, nb = std::min(NB, n - k0), rest = n - k0 - nb;
+    // helper stream and events of the lookahead (released on every return)
+    struct Aux {
+        cudaStream_t s = nullptr;
+        cudaEvent_t panel = nullptr, rest = nullptr;
+        ~Aux()
+        {
+            if (panel) cudaEventDestroy(panel);
+            if (rest) cudaEventDestroy(rest);
+            if (s) cudaStreamDestroy(s);
+        }
+    } aux;
+    if (F.nblk > 2) {
+        EMFA_CUDA(c, cudaStreamCreateWithFlags(&aux.s, cudaStreamNonBlocking));
+        EMFA_CUDA(c, cudaEventCreateWithFlags(&aux.panel, cudaEventDisableTiming));
+        EMFA_CUDA(c, cudaEventCreateWithFlags(&aux.rest, cudaEventDisableTiming));
+    }
+    auto diag = [&](int kb) {
+        const int k0 = kb * NB, nb = std::min(NB, n - k0);
         k_lu_diag<<<1, 256, s3, st>>>(A, n, k0, nb, dptr<int>(F.perm), dptr<float2>(F.linv), dptr<float2>(F.uinv),
                                       dptr<int>(F.info));
         c->kernel_launches += 1;
+    };
+    diag(0);
+    for (int kb = 0; kb < F.nblk; ++kb) {
+        const int k0 = kb * NB, nb = std::min(NB, n - k0), rest = n - k0 - nb;
         if (n - nb > 0) {
             k_lu_rowperm<<<(n - nb + 31) / 32, 256, 0, st>>>(A, n, k0, nb, dptr<int>(F.perm));
             c->kernel_launches += 1;
         }
-        if (rest > 0) {
-            const unsigned ch = (unsigned)((rest + NB - 1) / NB);
-            k_lu_small<<<ch, 256, s2, st>>>(A, n, k0, nb, dptr<float2>(F.linv), 0);
-            k_lu_small<<<ch, 256, s2, st>>>(A, n, k0, nb, dptr<float2>(F.uinv), 1);
-            k_lu_update<<<dim3(ch, ch), 256, s2, st>>>(A, n, k0, nb);
-            c->kernel_launches += 3;
+        if (rest <= 0) continue;
+        const unsigned ch = (unsigned)((rest + NB - 1) / NB);
+        k_lu_small<<<ch, 256, s2, st>>>(A, n, k0, nb, dptr<float2>(F.linv), 0);
+        k_lu_small<<<ch, 256, s2, st>>>(A, n, k0, nb, dptr<float2>(F.uinv), 1);
+        c->kernel_launches += 2;
+        if (aux.s && ch > 1) {
+            // the next block's columns, then its diagonal block on st while
+            // the other columns are updated on the helper stream
+            k_lu_update<<<dim3(1, ch), 256, s2, st>>>(A, n, k0, nb, 0);
+            EMFA_CUDA(c, cudaEventRecord(aux.panel, st));
+            EMFA_CUDA(c, cudaStreamWaitEvent(aux.s, aux.panel, 0));
+            k_lu_update<<<dim3(ch - 1, ch), 256, s2, aux.s>>>(A, n, k0, nb, 1);
+            EMFA_CUDA(c, cudaEventRecord(aux.rest, aux.s));
+            diag(kb + 1);
+            EMFA_CUDA(c, cudaStreamWaitEvent(st, aux.rest, 0));
+        } else {
+            k_lu_update<<<dim3(ch, ch), 256, s2, st>>>(A, n, k0, nb, 0);
+            diag(kb + 1);
         }
+        c->kernel_launches += aux.s && ch > 1 ? 2 : 1;
     }
     EMFA_CUDA(c, cudaGetLastError());
     return EMFA_OK;
