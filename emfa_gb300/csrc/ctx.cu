@@ -181,6 +181,13 @@ emfa_status_t emfa_ctx_create(int device, size_t hbm_budget_bytes, emfa_ctx_t** 
         delete c;
         return EMFA_ERR_CUDA;
     }
+    e = cudaHostAlloc((void**)&c->pinned, 64 * sizeof(int), cudaHostAllocDefault);
+    if (e != cudaSuccess) {
+        set_global_error(std::string("cudaHostAlloc: ") + cudaGetErrorString(e));
+        cudaStreamDestroy(c->stream);
+        delete c;
+        return EMFA_ERR_CUDA;
+    }
     *out = c;
     return EMFA_OK;
 }
@@ -200,6 +207,7 @@ emfa_status_t emfa_ctx_destroy(emfa_ctx_t* ctx)
         for (auto e : t.start) cudaEventDestroy(e);
         for (auto e : t.stop) cudaEventDestroy(e);
     }
+    if (ctx->pinned) cudaFreeHost(ctx->pinned);
     delete ctx;
     return EMFA_OK;
 }

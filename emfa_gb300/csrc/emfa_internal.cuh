@@ -105,6 +105,7 @@ struct Ctx {
     KernelTimer timers[KT_COUNT];
     DevBuf ws[WS_COUNT];            // declared after mu: destroyed before it
     std::map<void*, size_t> user_bufs;  // emfa_device_alloc'ed buffers
+    int* pinned = nullptr;          // page-locked host words for asynchronous status reads (64 ints)
 };
 
 emfa_status_t ctx_workspace(Ctx* c, int slot, size_t bytes, void** p);

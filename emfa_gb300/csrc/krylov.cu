@@ -731,6 +731,22 @@ static emfa_status_t gmres_t(Ctx* c, LinOp& A, const void* B, int nrhs, double2*
     const bool two_pass = sp->orth == 2 || (sp->orth == 0 && prec == EMFA_F64);
     int total_iters = 0, cycles = 0, converged = 0;
     int host_cnt[4];
+    // Arnoldi steps are checked one step late: step j and the operator
+    // application for step j + 1 are queued before the host reads step j-1's
+    // count of active right-hand sides (a page-locked word behind an event),
+    // so the device never waits for the host between steps.  The step queued
+    // after the last active one does nothing for converged right-hand sides
+    // (k_arnoldi_finish skips them).
+    struct StepEvents {
+        cudaEvent_t e[2] = {nullptr, nullptr};
+        ~StepEvents()
+        {
+            for (auto x : e)
+                if (x) cudaEventDestroy(x);
+        }
+    } sev;
+    for (auto& x : sev.e) EMFA_CUDA(c, cudaEventCreateWithFlags(&x, cudaEventDisableTiming));
+    volatile int* slot = c->pinned;
     for (int cyc = 0; cyc < max_cycles; ++cyc) {
         // true residual R = B - Z X (X = 0 on the first cycle: R = B)
         if (cyc == 0) {
@@ -774,11 +790,18 @@ static emfa_status_t gmres_t(Ctx* c, LinOp& A, const void* B, int nrhs, double2*
             }
             EMFA_CUDA(c, cudaMemsetAsync(s.counters, 0, sizeof(int), st));
             k_arnoldi_finish<<<(nrhs * 32 + 127) / 128, 128, 0, st>>>(s, j, pnorm, vblk, two_pass ? 1 : 0);
-            EMFA_CUDA(c, cudaMemcpyAsync(host_cnt, s.counters, sizeof(int), cudaMemcpyDeviceToHost, st));
-            EMFA_CUDA(c, cudaStreamSynchronize(st));
+            EMFA_CUDA(c, cudaMemcpyAsync((void*)(slot + (j & 1)), s.counters, sizeof(int), cudaMemcpyDeviceToHost, st));
+            EMFA_CUDA(c, cudaEventRecord(sev.e[j & 1], st));
             c->kernel_launches += 4;
             ++steps;
-            if (host_cnt[0] == 0) break;
+            if (j > 0) {
+                EMFA_CUDA(c, cudaEventSynchronize(sev.e[(j - 1) & 1]));
+                if (slot[(j - 1) & 1] == 0) {  // step j (queued) found nothing active
+                    --steps;
+                    break;
+                }
+            }
+            if (j + 1 == m) break;
             // V_{j+1} = W / beta, then W = A V_{j+1} (one pass for operators that pack)
             EMFA_TRY(A.normalize_apply(c, W, s.scale, s.wmax, V + (size_t)(j + 1) * vec, W, nrhs, st));
         }
