@@ -175,6 +175,7 @@ struct emfa_mlfma {
     std::vector<int> level_boxes;  // boxes per level 0..L
     std::vector<int> poles;        // multipoles per level 2..L
     std::vector<emfa::MLevel> lv;  // index level - 2
+    int rcap = 1;                  // right-hand sides the level patterns hold (one apply chunk)
     emfa::DevBuf perm_d, box_of;   // int [n]
     emfa::DevBuf rad, rec;         // C3f [n][Kf]
     emfa::DevBuf coeff;            // float [Kf]
@@ -284,20 +285,34 @@ __global__ void k_near_fill(const RwgPack<float>* __restrict__ rw, const int* __
 // float2 [(3 b + c) K, (3 b + c + 1) K), so a warp reads 32 consecutive
 // samples of one plane at once.
 
-// finest aggregation: CTA per finest box, threads over samples
-__global__ void k_agg_finest(const float2* __restrict__ x, const C3f* __restrict__ rad,
+// finest aggregation: CTA per finest box, threads over samples; each
+// radiation pattern is read once for up to RB right-hand sides (nr of them:
+// x[r][u] at r n + u, patterns of RHS r at out + r ostride)
+template <int RB>
+__global__ void k_agg_finest(const float2* __restrict__ x, int n, int nr, const C3f* __restrict__ rad,
                              const int* __restrict__ box_off, const int* __restrict__ box_cnt, int K,
-                             float2* __restrict__ out)
+                             float2* __restrict__ out, size_t ostride)
 {
     const int b = blockIdx.x;
     const int o = box_off[b], cnt = box_cnt[b];
     for (int kk = threadIdx.x; kk < K; kk += blockDim.x) {
-        C3f acc = c3zero();
-        for (int u = 0; u < cnt; ++u) c3fma(acc, x[o + u], rad[(size_t)(o + u) * K + kk]);
-        float2* ob = out + (size_t)3 * b * K + kk;
-        ob[0] = acc.x;
-        ob[K] = acc.y;
-        ob[2 * K] = acc.z;
+        C3f acc[RB];
+#pragma unroll
+        for (int r = 0; r < RB; ++r) acc[r] = c3zero();
+        for (int u = 0; u < cnt; ++u) {
+            const C3f rv = rad[(size_t)(o + u) * K + kk];
+#pragma unroll
+            for (int r = 0; r < RB; ++r)
+                if (r < nr) c3fma(acc[r], x[(size_t)r * n + o + u], rv);
+        }
+#pragma unroll
+        for (int r = 0; r < RB; ++r)
+            if (r < nr) {
+                float2* ob = out + r * ostride + (size_t)3 * b * K + kk;
+                ob[0] = acc[r].x;
+                ob[K] = acc[r].y;
+                ob[2 * K] = acc[r].z;
+            }
     }
 }
 
@@ -311,9 +326,12 @@ __global__ void k_upward(const float2* __restrict__ child, int Lc, const int* __
                          const int* __restrict__ child_idx, const int* __restrict__ child_oct,
                          const int* __restrict__ tl, const float* __restrict__ te, const int* __restrict__ pl,
                          const float* __restrict__ pe, const int2* __restrict__ win, int batch,
-                         const float2* __restrict__ phase, int Lp, int R, float2* __restrict__ out)
+                         const float2* __restrict__ phase, int Lp, int R, float2* __restrict__ out, size_t cstride,
+                         size_t ostride)
 {
     extern __shared__ float2 s_u[];  // [child in batch][3][rows of the window][Lp]
+    child += blockIdx.z * cstride;  // right-hand side blockIdx.z
+    out += blockIdx.z * ostride;
     const int b = blockIdx.x;
     const int Kc = 2 * Lc * Lc, K = 2 * Lp * Lp;
     const int pp0 = blockIdx.y * R;
@@ -403,9 +421,13 @@ __global__ void k_downward(const float4* __restrict__ up, const int* __restrict_
                            const float2* __restrict__ pphase, const int* __restrict__ th_ptr,
                            const int* __restrict__ th_src, const float* __restrict__ th_w,
                            const int* __restrict__ ph_ptr, const int* __restrict__ ph_src,
-                           const float* __restrict__ ph_w, float4* __restrict__ out)
+                           const float* __restrict__ ph_w, float4* __restrict__ out, size_t ustride, size_t pstride)
 {
     extern __shared__ float2 s_h[];  // [3][rows of the window][L]
+    // right-hand side blockIdx.z: strides in complex64 (this level, parent level)
+    up += blockIdx.z * (ustride / 2);
+    out += blockIdx.z * (ustride / 2);
+    if (pdown) pdown += blockIdx.z * pstride;
     const int b = blockIdx.x;
     const int K = 2 * L * L, K2 = K >> 1;
     const int pc0 = blockIdx.y * R;
@@ -476,11 +498,14 @@ __global__ void k_downward(const float4* __restrict__ up, const int* __restrict_
     }
 }
 
-// disaggregation + near field: warp per unknown (box order).  The near row of
-// unknown u is contiguous in val (row_cols[b] values); its column unknowns are
-// listed once per box in near_cidx.
-__global__ void k_disagg_near(const float2* __restrict__ x, const C3f* __restrict__ rec,
-                              const float2* __restrict__ down, const float* __restrict__ coeff, int K,
+// disaggregation + near field: warp per unknown (box order), for up to RB
+// right-hand sides (nr of them; x, y at r n, down patterns at r dstride): the
+// receive pattern and the near row are read once.  The near row of unknown u
+// is contiguous in val (row_cols[b] values); its column unknowns are listed
+// once per box in near_cidx.
+template <int RB>
+__global__ void k_disagg_near(const float2* __restrict__ x, int nr, const C3f* __restrict__ rec,
+                              const float2* __restrict__ down, size_t dstride, const float* __restrict__ coeff, int K,
                               const int* __restrict__ box_of, const int* __restrict__ box_off,
                               const int* __restrict__ row_cols, const size_t* __restrict__ row_base,
                               const int* __restrict__ near_cbase, const int* __restrict__ near_cidx,
@@ -489,28 +514,46 @@ __global__ void k_disagg_near(const float2* __restrict__ x, const C3f* __restric
     const int warp = (int)(((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
     if (warp >= n) return;
     const int u = warp, b = box_of[u];
-    float2 acc = make_float2(0, 0);
+    float2 acc[RB];
+#pragma unroll
+    for (int r = 0; r < RB; ++r) acc[r] = make_float2(0, 0);
     const C3f* rr = rec + (size_t)u * K;
     const float2* dd = down + (size_t)3 * b * K;
 #pragma unroll 4
     for (int kk = lane; kk < K; kk += 32) {
-        const C3f r = rr[kk];
-        float2 t = caddf(caddf(cmulf(r.x, dd[kk]), cmulf(r.y, dd[K + kk])), cmulf(r.z, dd[2 * K + kk]));
-        acc = caddf(acc, cscalef(t, coeff[kk]));
+        const C3f rv = rr[kk];
+        const float cf = coeff[kk];
+#pragma unroll
+        for (int r = 0; r < RB; ++r)
+            if (r < nr) {
+                const float2* d = dd + r * dstride;
+                const float2 t = caddf(caddf(cmulf(rv.x, d[kk]), cmulf(rv.y, d[K + kk])), cmulf(rv.z, d[2 * K + kk]));
+                acc[r] = caddf(acc[r], cscalef(t, cf));
+            }
     }
     if (!skip_near) {
         const int rc = row_cols[b];
         const float2* vrow = val + row_base[b] + (size_t)(u - box_off[b]) * rc;
         const int* ci = near_cidx + near_cbase[b];
 #pragma unroll 4
-        for (int j = lane; j < rc; j += 32) acc = caddf(acc, cmulf(vrow[j], x[ci[j]]));
+        for (int j = lane; j < rc; j += 32) {
+            const float2 v = vrow[j];
+            const int cj = ci[j];
+#pragma unroll
+            for (int r = 0; r < RB; ++r)
+                if (r < nr) acc[r] = caddf(acc[r], cmulf(v, x[(size_t)r * n + cj]));
+        }
     }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
-        acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
+    for (int r = 0; r < RB; ++r) {
+        if (r >= nr) break;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            acc[r].x += __shfl_xor_sync(0xffffffffu, acc[r].x, o);
+            acc[r].y += __shfl_xor_sync(0xffffffffu, acc[r].y, o);
+        }
+        if (lane == 0) y[(size_t)r * n + u] = acc[r];
     }
-    if (lane == 0) y[u] = acc;
 }
 
 __global__ void k_gather_c64(const float2* __restrict__ src, const int* __restrict__ idx, int n, int nrhs,
@@ -1355,25 +1398,70 @@ static emfa_status_t mlfma_build(emfa_mlfma* M, cudaStream_t st)
     return EMFA_OK;
 }
 
-// y = Z x for one vector (box order, complex64); parts: 0 near + far, 1 near, 2 far
-static emfa_status_t mlfma_apply1(emfa_mlfma* M, const float2* x, float2* y, cudaStream_t st, int parts = 0)
+// right-hand sides per pass of the operator's kernels
+constexpr int RHS_CHUNK = 8;
+
+// level patterns for nr right-hand sides (scratch: grown, never copied)
+static emfa_status_t reserve_rhs(emfa_mlfma* M, int nr)
 {
-    Ctx* c = M->ctx;
+    if (nr <= M->rcap) return EMFA_OK;
+    for (auto& ml : M->lv) {
+        const size_t per = sizeof(float2) * 3 * (size_t)ml.nbox * ml.K;
+        EMFA_TRY(ml.up.alloc(M->ctx, per * nr));
+        EMFA_TRY(ml.down.alloc(M->ctx, per * nr));
+    }
+    M->rcap = nr;
+    return EMFA_OK;
+}
+
+template <int RB>
+static void launch_agg_disagg(emfa_mlfma* M, bool agg, const float2* x, int nr, float2* y, int parts, cudaStream_t st)
+{
     const int nl = M->levels - 1;
     MLevel& fl = M->lv[nl - 1];
-    const int Kf = fl.K;
-    k_agg_finest<<<fl.nbox, 128, 0, st>>>(x, dptr<C3f>(M->rad), dptr<int>(M->box_off), dptr<int>(M->box_cnt), Kf,
-                                          dptr<float2>(fl.up));
+    const int Kf = fl.K, n = M->n;
+    const size_t lstride = (size_t)3 * fl.nbox * Kf;
+    if (agg)
+        k_agg_finest<RB><<<fl.nbox, 128, 0, st>>>(x, n, nr, dptr<C3f>(M->rad), dptr<int>(M->box_off),
+                                                  dptr<int>(M->box_cnt), Kf, dptr<float2>(fl.up), lstride);
+    else
+        k_disagg_near<RB><<<(unsigned)(((size_t)n * 32 + 255) / 256), 256, 0, st>>>(
+            x, nr, dptr<C3f>(M->rec), dptr<float2>(fl.down), lstride, dptr<float>(M->coeff), parts == 1 ? 0 : Kf,
+            dptr<int>(M->box_of), dptr<int>(M->box_off), dptr<int>(M->row_cols), dptr<size_t>(M->row_base),
+            dptr<int>(M->near_cbase), dptr<int>(M->near_cidx), dptr<float2>(M->near_val), n, parts == 2 ? 1 : 0, y);
+}
+
+static void agg_disagg(emfa_mlfma* M, bool agg, const float2* x, int nr, float2* y, int parts, cudaStream_t st)
+{
+    if (nr <= 1)
+        launch_agg_disagg<1>(M, agg, x, nr, y, parts, st);
+    else if (nr <= 2)
+        launch_agg_disagg<2>(M, agg, x, nr, y, parts, st);
+    else if (nr <= 4)
+        launch_agg_disagg<4>(M, agg, x, nr, y, parts, st);
+    else
+        launch_agg_disagg<8>(M, agg, x, nr, y, parts, st);
+}
+
+// y = Z x for nr <= RHS_CHUNK vectors (RHS-major, box order, complex64);
+// parts: 0 near + far, 1 near, 2 far
+static emfa_status_t mlfma_apply(emfa_mlfma* M, const float2* x, float2* y, int nr, cudaStream_t st, int parts = 0)
+{
+    Ctx* c = M->ctx;
+    EMFA_TRY(reserve_rhs(M, nr));
+    const int nl = M->levels - 1;
+    agg_disagg(M, true, x, nr, y, parts, st);
     for (int i = nl - 2; i >= 0; --i) {
         MLevel& pm = M->lv[i];
         MLevel& cm = M->lv[i + 1];
         const int R = pm.up_rows;
         const int bs = 32 * ((R * pm.L + 31) / 32);
-        const dim3 grid((unsigned)pm.nbox, (unsigned)((2 * pm.L + R - 1) / R));
+        const dim3 grid((unsigned)pm.nbox, (unsigned)((2 * pm.L + R - 1) / R), (unsigned)nr);
         k_upward<<<grid, bs, pm.up_child_bytes * pm.up_batch, st>>>(
             dptr<float2>(cm.up), cm.L, dptr<int>(pm.child_ptr), dptr<int>(pm.child_idx), dptr<int>(cm.oct),
             dptr<int>(pm.ip_tl), dptr<float>(pm.ip_te), dptr<int>(pm.ip_pl), dptr<float>(pm.ip_pe),
-            dptr<int2>(pm.up_win), pm.up_batch, dptr<float2>(pm.up_phase), pm.L, R, dptr<float2>(pm.up));
+            dptr<int2>(pm.up_win), pm.up_batch, dptr<float2>(pm.up_phase), pm.L, R, dptr<float2>(pm.up),
+            (size_t)3 * cm.nbox * cm.K, (size_t)3 * pm.nbox * pm.K);
     }
     for (int i = 0; i < nl; ++i) {
         MLevel& ml = M->lv[i];
@@ -1381,19 +1469,15 @@ static emfa_status_t mlfma_apply1(emfa_mlfma* M, const float2* x, float2* y, cud
         MLevel& pm = M->lv[top ? 0 : i - 1];
         const int R = down_rows(ml.L);
         const int bs = std::min(256, 32 * ((R * ml.L / 2 + 31) / 32));
-        const dim3 grid((unsigned)ml.nbox, (unsigned)((2 * ml.L + R - 1) / R));
+        const dim3 grid((unsigned)ml.nbox, (unsigned)((2 * ml.L + R - 1) / R), (unsigned)nr);
         k_downward<<<grid, bs, top ? 0 : ml.down_smem, st>>>(
             dptr<float4>(ml.up), dptr<int>(ml.far_ptr), dptr<int2>(ml.far), dptr<float4>(ml.trans), ml.L, R,
             top ? nullptr : dptr<float2>(pm.down), pm.L, dptr<int2>(ml.down_win), dptr<int>(ml.parent),
             dptr<int>(ml.oct), dptr<float2>(pm.up_phase), dptr<int>(ml.th_ptr), dptr<int>(ml.th_src),
             dptr<float>(ml.th_w), dptr<int>(ml.ph_ptr), dptr<int>(ml.ph_src), dptr<float>(ml.ph_w),
-            dptr<float4>(ml.down));
+            dptr<float4>(ml.down), (size_t)3 * ml.nbox * ml.K, (size_t)3 * pm.nbox * pm.K);
     }
-    const int n = M->n;
-    k_disagg_near<<<(unsigned)(((size_t)n * 32 + 255) / 256), 256, 0, st>>>(
-        x, dptr<C3f>(M->rec), dptr<float2>(fl.down), dptr<float>(M->coeff), parts == 1 ? 0 : Kf, dptr<int>(M->box_of),
-        dptr<int>(M->box_off), dptr<int>(M->row_cols), dptr<size_t>(M->row_base), dptr<int>(M->near_cbase),
-        dptr<int>(M->near_cidx), dptr<float2>(M->near_val), n, parts == 2 ? 1 : 0, y);
+    agg_disagg(M, false, x, nr, y, parts, st);
     c->kernel_launches += 2 * nl + 1;
     EMFA_CUDA(c, cudaGetLastError());
     return EMFA_OK;
@@ -1417,16 +1501,17 @@ struct MlfmaOp : LinOp {
     bool pre = false;  // left-preconditioned operator P Z
     emfa_status_t apply(Ctx*, const void* X, void* Y, int nrhs, cudaStream_t st) override
     {
-        for (int r = 0; r < nrhs; ++r) {
-            const float2* x = (const float2*)X + (size_t)r * n;
-            float2* y = (float2*)Y + (size_t)r * n;
-            if (pre) {
-                EMFA_TRY(mlfma_apply1(M, x, dptr<float2>(M->pre_tmp), st));
-                EMFA_TRY(sai_apply(M, dptr<float2>(M->pre_tmp), y, 1, st));
-            } else {
-                EMFA_TRY(mlfma_apply1(M, x, y, st));
+        if (pre) {
+            // P (Z x): one right-hand side at a time through the preconditioner's scratch
+            for (int r = 0; r < nrhs; ++r) {
+                EMFA_TRY(mlfma_apply(M, (const float2*)X + (size_t)r * n, dptr<float2>(M->pre_tmp), 1, st));
+                EMFA_TRY(sai_apply(M, dptr<float2>(M->pre_tmp), (float2*)Y + (size_t)r * n, 1, st));
             }
+            return EMFA_OK;
         }
+        for (int r0 = 0; r0 < nrhs; r0 += RHS_CHUNK)
+            EMFA_TRY(mlfma_apply(M, (const float2*)X + (size_t)r0 * n, (float2*)Y + (size_t)r0 * n,
+                                 std::min(RHS_CHUNK, nrhs - r0), st));
         return EMFA_OK;
     }
     emfa_status_t residual(Ctx* c, const double2* X, const void* B, double2* R, int nrhs, float2* xt,
@@ -1519,7 +1604,7 @@ emfa_status_t emfa_mlfma_apply_part(emfa_mlfma_t* M, const void* x_dev, void* y_
     Ctx* c = M->ctx;
     EMFA_CUDA(c, cudaSetDevice(c->device));
     cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
-    return mlfma_apply1(M, (const float2*)x_dev, (float2*)y_dev, st, part);
+    return mlfma_apply(M, (const float2*)x_dev, (float2*)y_dev, 1, st, part);
 }
 
 emfa_status_t emfa_mlfma_apply(emfa_mlfma_t* M, const void* x_dev, void* y_dev, int n_rhs, void* stream)

@@ -59,7 +59,8 @@ struct Engine {
 //          packed right-hand sides, geometry
 //   MLFMA: radiation + receive patterns (2 x 3 x complex64 x K_f, K_f <= 160
 //          at a 0.25-wavelength finest box), near field (~110 entries a
-//          row), level patterns, Krylov state
+//          row), level patterns (about 2 KB an unknown for each right-hand
+//          side of an operator pass, at most 8), Krylov state
 size_t estimate_bytes(const emfa_request_t& r, int dense_max, int* method)
 {
     const double N = 1.5 * r.n_tri + 16;  // closed surface: 3 edges per triangle, each shared
@@ -70,7 +71,7 @@ size_t estimate_bytes(const emfa_request_t& r, int dense_max, int* method)
     if (m == 1)
         b = (r.kind == EMFA_EFIE ? 24.0 : 16.0) * N * N + 40.0 * 8 * N * R + 16.0 * 2 * N * R + 2048.0 * N;
     else
-        b = 2.0 * 3 * 8 * 160 * N + 110.0 * 8 * N + 1500.0 * N + 40.0 * 8 * N * R + 2048.0 * N;
+        b = 2.0 * 3 * 8 * 160 * N + 110.0 * 8 * N + 2000.0 * N * std::min(R, 8.0) + 40.0 * 8 * N * R + 2048.0 * N;
     return (size_t)(b * 1.1) + (64u << 20);
 }
 

@@ -85,6 +85,23 @@ def test_operator_matches_reference(ops, name):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("nr", [3, 8, 10])
+def test_multi_rhs_apply_equals_single(ops, nr):
+    """Several right-hand sides in one operator pass (up to 8 per pass; 10
+    = 8 + 2) give each vector's single-RHS product exactly: per right-hand
+    side the kernels sum in the same order."""
+    import torch
+    g, geo, ml = ops[CASES[0]]
+    rng = np.random.default_rng(nr)
+    X = torch.tensor((rng.standard_normal((nr, geo.n)) + 1j * rng.standard_normal((nr, geo.n))).astype(np.complex64),
+                     device="cuda")
+    Y = ml.apply(X).cpu().numpy()
+    for r in range(nr):
+        y1 = ml.apply(X[r:r + 1].contiguous())[0].cpu().numpy()
+        assert np.array_equal(Y[r], y1), (r, np.abs(Y[r] - y1).max())
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("name", CASES)
 def test_excitation_box_order(ops, name):
     g, geo, ml = ops[name]
