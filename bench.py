@@ -155,7 +155,7 @@ def run_emfa(args, workload):
         if world > 1:
             torch.distributed.barrier()
     total_ms = start.elapsed_time(end)
-    launches = (ctx.launches() - l0) // max(1, args.steps)
+    launches = ctx.launches() - l0  # every library kernel launched in the timed region
     kernels = {k: ctx.kernel_time(k) for k in ctx.KERNEL_TIMERS}
     ctx.kernel_timing(False)
     if world > 1:
@@ -558,6 +558,7 @@ def main():
                    "converged": res["infos"][-1][2], "max_rel_residual": res["infos"][-1][3]},
         "e2e": {k: (round(v, 3) if isinstance(v, float) else v) for k, v in res["e2e"].items()},
         "gpu_launches": res["launches"],
+        "gpu_launches_per_step": res["launches"] // max(1, args.steps),
         "clocks": res["clocks"],
         "accuracy": res["acc"],
         "roofline": roofline(res),
