@@ -105,6 +105,7 @@ _SIGS = {
     "emfa_serve": (ci, [ci, ctypes.POINTER(Request), ci, ctypes.POINTER(ServeOpts), ctypes.POINTER(RequestResult)]),
     "emfa_serve_simulate": (ci, [vp, vp, vp, ci, ctypes.POINTER(ServeOpts), vp, vp]),
     "emfa_diag_sincospi": (ci, [vp, ci, vp, vp, vp]),
+    "emfa_diag_wait_timeout": (ci, [vp, ctypes.POINTER(ci)]),
     "emfa_dump_save": (ci, [ctypes.c_char_p, ctypes.c_char_p, ci, sz, sz, ctypes.c_double, vp, ci]),
     "emfa_dump_info": (ci, [ctypes.c_char_p, ctypes.c_char_p, ip, ctypes.POINTER(sz), ctypes.POINTER(sz),
                             ctypes.POINTER(ctypes.c_double)]),

@@ -165,6 +165,17 @@ __global__ void k_pack_b(const float2* __restrict__ X, int n, int nrhs, float2* 
     }
 }
 
+// the pipelines' bounded wait on a barrier nothing arrives on (no copy or MMA
+// in flight): records `code` once the short limit passes
+__global__ void k_diag_wait(int* err, int code, long long limit)
+{
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x != 0) return;
+    mbar_init(&bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    mbar_wait(&bar, 0, err, code, limit);
+}
+
 }  // namespace tc
 
 PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
@@ -300,3 +311,26 @@ emfa_status_t cgemm_tf32_scratch(const void* Z, size_t ldz, const void* X, int n
 }
 
 }  // namespace emfa
+
+extern "C" emfa_status_t emfa_diag_wait_timeout(emfa_ctx_t* ctx, int* code_out)
+{
+    using namespace emfa;
+    if (!ctx || !code_out) return EMFA_ERR_INVALID;
+    EMFA_CUDA(ctx, cudaSetDevice(ctx->device));
+    void* ep = nullptr;
+    EMFA_TRY(ctx_workspace(ctx, WS_GEMM_ERR, 64, &ep));
+    int* err = (int*)ep;
+    cudaStream_t st = ctx->stream;
+    EMFA_CUDA(ctx, cudaMemsetAsync(err, 0, sizeof(int), st));
+    tc::k_diag_wait<<<1, 32, 0, st>>>(err, 42, 2000000LL);  // about 1 ms
+    ctx->kernel_launches += 1;
+    EMFA_CUDA(ctx, cudaGetLastError());
+    EMFA_CUDA(ctx, cudaMemcpyAsync(code_out, err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    EMFA_CUDA(ctx, cudaStreamSynchronize(st));
+    EMFA_CUDA(ctx, cudaMemsetAsync(err, 0, sizeof(int), st));  // the product kernels start from a clear word
+    if (*code_out) {
+        set_error(ctx, "emfa_diag_wait_timeout: the bounded wait gave up (stage " + std::to_string(*code_out) + ")");
+        return EMFA_ERR_TIMEOUT;
+    }
+    return EMFA_OK;
+}

@@ -315,6 +315,11 @@ emfa_status_t emfa_dense_rcs(emfa_ctx_t* ctx, const double* verts_host, int n_ve
 /* Diagnostics: sin and cos of pi*x as the FP32 fill evaluates them (its own
  * Taylor-series evaluation), for accuracy tests; n device floats in and out. */
 emfa_status_t emfa_diag_sincospi(const float* x_dev, int n, float* s_dev, float* c_dev, void* stream);
+/* Diagnostics: the bounded wait of the tensor-core pipelines on a barrier
+ * that nothing arrives on, with a 1 ms limit: returns EMFA_ERR_TIMEOUT and
+ * *code_out = 42 (the stage code it recorded); the context stays usable.
+ * No counterpart in the reference (it has no device code). */
+emfa_status_t emfa_diag_wait_timeout(emfa_ctx_t* ctx, int* code_out);
 
 /* ---- binary dumps ------------------------------------------------------------ */
 /* Versioned binary dump of a matrix or vector (Z, V, I, operator arrays):

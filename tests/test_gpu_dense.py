@@ -313,3 +313,23 @@ def test_fill_sincospi_accuracy(ctx):
     es = np.abs(s.cpu().numpy() - np.sin(np.pi * xd)).max()
     ec = np.abs(c.cpu().numpy() - np.cos(np.pi * xd)).max()
     assert es < 1.2e-7 and ec < 1.2e-7, (es, ec)
+
+
+def test_bounded_wait_gives_up_and_context_survives(ctx):
+    """The tensor-core pipelines' bounded mbarrier wait, on a barrier that
+    nothing arrives on (no copy in flight): the kernel records its stage code
+    and returns, the call reports EMFA_ERR_TIMEOUT, and the same context then
+    runs a tensor-core product correctly."""
+    import ctypes
+    import torch
+    from emfa_gb300 import api, _lib as L
+    code = ctypes.c_int(0)
+    st = L.lib().emfa_diag_wait_timeout(ctx.h, ctypes.byref(code))
+    assert st == 7 and code.value == 42, (st, code.value)
+    assert b"gave up" in L.lib().emfa_last_error(ctx.h)
+    rng = np.random.default_rng(3)
+    Z = (rng.standard_normal((256, 256)) + 1j * rng.standard_normal((256, 256))).astype(np.complex64)
+    X = (rng.standard_normal((4, 256)) + 1j * rng.standard_normal((4, 256))).astype(np.complex64)
+    Y = api.matvec(ctx, torch.from_numpy(Z).cuda(), torch.from_numpy(X).cuda(), "tf32").cpu().numpy()
+    ref = X.astype(np.complex128) @ Z.astype(np.complex128).T
+    assert np.linalg.norm(Y - ref) / np.linalg.norm(ref) < 3e-3
