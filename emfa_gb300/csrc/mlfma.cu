@@ -142,7 +142,7 @@ struct MLevel {
     DevBuf child_ptr, child_idx;        // CSR children (int)
     DevBuf far_ptr, far;                // CSR far lists: int2 {source box, offset index}
     DevBuf trans;                       // float2 [343][K]
-    DevBuf up, down;                    // planar float2 [nbox][3][K]
+    DevBuf up, down;                    // planar float2 [right-hand side][nbox][3][K]
     // interpolation to this level from the level below, separable: 3-point
     // Lagrange stencils in theta (per theta index of this level: child theta,
     // weight) and in phi (per phi index: child phi row, weight)
@@ -151,7 +151,6 @@ struct MLevel {
     // stencils: theta (CSR over this level's theta index: parent theta, weight)
     // and phi (CSR over this level's phi index: parent phi, weight)
     DevBuf th_ptr, th_src, th_w, ph_ptr, ph_src, ph_w;
-    int rows = 0;                       // phi rows per CTA of the downward pass (even)
     size_t down_smem = 0;               // shared bytes per CTA (theta-pass rows)
     DevBuf down_win;                    // int2 per chunk: parent phi rows its phi stencils read
     DevBuf up_phase;                    // float2 [8][K]: exp(-j k k.(parent - child)) for the level below
@@ -159,7 +158,6 @@ struct MLevel {
     size_t up_child_bytes = 0;          //   shared bytes of one child's theta pass,
     int up_batch = 0;                   //   children per shared-memory pass,
     DevBuf up_win;                      //   int2 per chunk: the child phi rows it reads
-    std::vector<float> w_host;          // quadrature weights (host)
 };
 
 }  // namespace emfa
@@ -1118,7 +1116,6 @@ static emfa_status_t mlfma_build(emfa_mlfma* M, cudaStream_t st)
         ml.L = P.poles[i];
         ml.K = 2 * ml.L * ml.L;
         ml.len = P.blen[l];
-        ml.w_host = gw[i];
     }
     // the interpolation and anterpolation passes may use more than the default 48 KB of shared memory
     EMFA_TRY(ensure_smem(c, k_upward, 96 * 1024));
@@ -1284,13 +1281,13 @@ static emfa_status_t mlfma_build(emfa_mlfma* M, cudaStream_t st)
             EMFA_TRY(upload(c, cm.ph_src, psrc, st));
             EMFA_TRY(upload(c, cm.ph_w, pw, st));
             // phi-row chunks of about 256 samples, and the parent rows each reads
-            cm.rows = down_rows(Lc);
-            const int nchunk = (2 * Lc + cm.rows - 1) / cm.rows;
+            const int rows = down_rows(Lc);
+            const int nchunk = (2 * Lc + rows - 1) / rows;
             std::vector<int2> dw(nchunk);
             int most = 0;
             for (int ch = 0; ch < nchunk; ++ch) {
                 int lo = 2 * Lp, hi = 0;
-                for (int pc = ch * cm.rows; pc < std::min(2 * Lc, (ch + 1) * cm.rows); ++pc)
+                for (int pc = ch * rows; pc < std::min(2 * Lc, (ch + 1) * rows); ++pc)
                     for (int a = pptr[pc]; a < pptr[pc + 1]; ++a) {
                         lo = std::min(lo, psrc[a]);
                         hi = std::max(hi, psrc[a] + 1);
