@@ -50,10 +50,10 @@ def _random(n, nrhs, seed):
     return Z, B
 
 
-@pytest.mark.parametrize("n,nrhs", [(1, 1), (63, 3), (64, 8), (65, 1), (130, 9), (1000, 8), (1537, 17)])
+@pytest.mark.parametrize("n,nrhs", [(1, 1), (63, 3), (64, 8), (65, 1), (130, 9), (1000, 8), (1537, 17), (700, 100)])
 def test_lu_random_matches_numpy(ctx, n, nrhs):
-    """Block edges (n = 63, 64, 65, a ragged last block), one to 17
-    right-hand sides (more than one sweep chunk of 8)."""
+    """Block edges (n = 63, 64, 65, a ragged last block), one to 100
+    right-hand sides (several sweep chunks of 8, a ragged last chunk)."""
     Z, B = _random(n, nrhs, n)
     X, info = _solve(ctx, Z, B)
     assert info.converged == nrhs, (info.iterations, info.max_rel_residual)
