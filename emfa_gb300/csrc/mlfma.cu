@@ -301,11 +301,11 @@ __global__ void k_agg_finest(const float2* __restrict__ x, int n, int nr, const 
             const C3f rv = rad[(size_t)(o + u) * K + kk];
 #pragma unroll
             for (int r = 0; r < RB; ++r)
-                if (r < nr) c3fma(acc[r], x[(size_t)r * n + o + u], rv);
+                if (RB == 1 || r < nr) c3fma(acc[r], x[(size_t)r * n + o + u], rv);
         }
 #pragma unroll
         for (int r = 0; r < RB; ++r)
-            if (r < nr) {
+            if (RB == 1 || r < nr) {
                 float2* ob = out + r * ostride + (size_t)3 * b * K + kk;
                 ob[0] = acc[r].x;
                 ob[K] = acc[r].y;
@@ -523,7 +523,7 @@ __global__ void k_disagg_near(const float2* __restrict__ x, int nr, const C3f* _
         const float cf = coeff[kk];
 #pragma unroll
         for (int r = 0; r < RB; ++r)
-            if (r < nr) {
+            if (RB == 1 || r < nr) {
                 const float2* d = dd + r * dstride;
                 const float2 t = caddf(caddf(cmulf(rv.x, d[kk]), cmulf(rv.y, d[K + kk])), cmulf(rv.z, d[2 * K + kk]));
                 acc[r] = caddf(acc[r], cscalef(t, cf));
@@ -539,12 +539,12 @@ __global__ void k_disagg_near(const float2* __restrict__ x, int nr, const C3f* _
             const int cj = ci[j];
 #pragma unroll
             for (int r = 0; r < RB; ++r)
-                if (r < nr) acc[r] = caddf(acc[r], cmulf(v, x[(size_t)r * n + cj]));
+                if (RB == 1 || r < nr) acc[r] = caddf(acc[r], cmulf(v, x[(size_t)r * n + cj]));
         }
     }
 #pragma unroll
     for (int r = 0; r < RB; ++r) {
-        if (r >= nr) break;
+        if (RB > 1 && r >= nr) break;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             acc[r].x += __shfl_xor_sync(0xffffffffu, acc[r].x, o);
