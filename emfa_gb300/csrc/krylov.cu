@@ -309,29 +309,42 @@ __global__ void __launch_bounds__(256) k_vdots(const Cx<T>* __restrict__ V, size
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const size_t base = (size_t)r * n;
     const int k0 = blk * VCHUNK, k1 = min(n, k0 + VCHUNK);
-    for (int i = warp; i < nv; i += 8) {
-        const Cx<T>* vi = V + (size_t)i * vstride + base;
-        A re = 0, im = 0;
+    // two basis vectors per warp pass (i and i + 8): twice the loads in
+    // flight, and one reduction's latency hides behind the other's loads
+    for (int i = warp; i < nv; i += 16) {
+        const bool two = i + 8 < nv;
+        const Cx<T>* va = V + (size_t)i * vstride + base;
+        const Cx<T>* vb = V + (size_t)(two ? i + 8 : i) * vstride + base;
+        A re = 0, im = 0, re2 = 0, im2 = 0;
         for (int k = k0 + lane; k < k1; k += 128) {
-            Cx<T> v[4], w[4];
+            Cx<T> a[4], b[4], w[4];
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
                 const int kk = k + 32 * u;
-                v[u] = kk < k1 ? vi[kk] : Cx<T>{T(0), T(0)};
-                w[u] = kk < k1 ? W[base + kk] : Cx<T>{T(0), T(0)};
+                const bool in = kk < k1;
+                a[u] = in ? va[kk] : Cx<T>{T(0), T(0)};
+                b[u] = in && two ? vb[kk] : Cx<T>{T(0), T(0)};
+                w[u] = in ? W[base + kk] : Cx<T>{T(0), T(0)};
             }
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
-                re += (A)v[u].re * (A)w[u].re + (A)v[u].im * (A)w[u].im;
-                im += (A)v[u].re * (A)w[u].im - (A)v[u].im * (A)w[u].re;
+                re += (A)a[u].re * (A)w[u].re + (A)a[u].im * (A)w[u].im;
+                im += (A)a[u].re * (A)w[u].im - (A)a[u].im * (A)w[u].re;
+                re2 += (A)b[u].re * (A)w[u].re + (A)b[u].im * (A)w[u].im;
+                im2 += (A)b[u].re * (A)w[u].im - (A)b[u].im * (A)w[u].re;
             }
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             re += __shfl_xor_sync(0xffffffffu, re, o);
             im += __shfl_xor_sync(0xffffffffu, im, o);
+            re2 += __shfl_xor_sync(0xffffffffu, re2, o);
+            im2 += __shfl_xor_sync(0xffffffffu, im2, o);
         }
-        if (lane == 0) partial[((size_t)i * nrhs + r) * nblk + blk] = make_double2((double)re, (double)im);
+        if (lane == 0) {
+            partial[((size_t)i * nrhs + r) * nblk + blk] = make_double2((double)re, (double)im);
+            if (two) partial[((size_t)(i + 8) * nrhs + r) * nblk + blk] = make_double2((double)re2, (double)im2);
+        }
     }
 }
 
