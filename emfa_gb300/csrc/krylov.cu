@@ -535,6 +535,100 @@ __global__ void k_arnoldi_finish(GmresDev s, int j, const double2* __restrict__ 
 }
 
 // V_out[r][k] = scale[r] * W[r][k]
+// k_arnoldi_finish for restarts of at most 32: warp per RHS, lane i holds
+// entry i of the new Hessenberg column and rotation i (loaded together), the
+// previous rotations run through shuffles instead of a chain of dependent
+// memory accesses, and the column is written back at once.  Same arithmetic,
+// in the same order, as k_arnoldi_finish.
+__device__ __forceinline__ double2 shfl_d2(double2 v, int src)
+{
+    return make_double2(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
+}
+
+__global__ void k_arnoldi_finish_warp(GmresDev s, int j, const double2* __restrict__ pnorm, int nblk, int two_pass)
+{
+    const int r = (int)(((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (r >= s.nrhs) return;  // whole warps
+    const int m = s.m;
+    if (!s.active[r]) {
+        if (lane == 0) s.scale[r] = 0.0;
+        return;
+    }
+    double beta = 0.0;
+    if (lane == 0) {
+        double nr2 = 0.0, wm = 0.0;
+        for (int b = 0; b < nblk; ++b) {
+            nr2 += pnorm[(size_t)r * nblk + b].x;
+            wm = fmax(wm, pnorm[(size_t)r * nblk + b].y);
+        }
+        s.wmax[r] = wm;
+        beta = sqrt(nr2);
+    }
+    beta = __shfl_sync(0xffffffffu, beta, 0);
+    double2* H = s.H + (size_t)r * (m + 1) * m;
+    double* cs = s.cs + (size_t)r * m;
+    double2* sn = s.sn + (size_t)r * m;
+    double2 h = make_double2(0.0, 0.0);
+    if (lane <= j) {
+        h = s.hcol[(size_t)lane * s.nrhs + r];
+        if (two_pass) {
+            const double2 b = s.y[(size_t)lane * s.nrhs + r];
+            h.x += b.x;
+            h.y += b.y;
+        }
+    }
+    const double cl = lane < j ? cs[lane] : 0.0;
+    const double2 sl = lane < j ? sn[lane] : make_double2(0.0, 0.0);
+    // previous rotations: [x; y] <- [c x + s y; -conj(s) x + c y] on entries (i, i + 1)
+    for (int i = 0; i < j; ++i) {
+        const double2 y = shfl_d2(h, i + 1), x = shfl_d2(h, i);
+        const double c = __shfl_sync(0xffffffffu, cl, i);
+        const double2 sv = shfl_d2(sl, i);
+        if (lane == i)
+            h = make_double2(c * x.x + sv.x * y.x - sv.y * y.y, c * x.y + sv.x * y.y + sv.y * y.x);
+        else if (lane == i + 1)
+            h = make_double2(-(sv.x * x.x + sv.y * x.y) + c * y.x, -(sv.x * x.y - sv.y * x.x) + c * y.y);
+    }
+    if (lane == j) {
+        const double2 a = h;
+        const double b = beta;
+        const double aa = hypot(a.x, a.y);
+        const double nu = hypot(aa, b);
+        double c;
+        double2 sv;
+        if (aa == 0.0) {
+            c = 0.0;
+            sv = make_double2(1.0, 0.0);
+            h = make_double2(b, 0.0);
+        } else {
+            c = aa / nu;
+            const double2 ph = make_double2(a.x / aa, a.y / aa);
+            sv = make_double2(ph.x * b / nu, ph.y * b / nu);
+            h = make_double2(ph.x * nu, ph.y * nu);
+        }
+        H[(j + 1) * m + j] = make_double2(0.0, 0.0);
+        cs[j] = c;
+        sn[j] = sv;
+        double2* g = s.g + (size_t)r * (m + 1);
+        const double2 gj = g[j];
+        g[j + 1] = make_double2(-(sv.x * gj.x + sv.y * gj.y), -(sv.x * gj.y - sv.y * gj.x));
+        g[j] = make_double2(c * gj.x, c * gj.y);
+        const double res = hypot(g[j + 1].x, g[j + 1].y);
+        s.jlen[r] = j + 1;
+        s.est[r] = res;
+        const double thr = s.tol_abs ? s.tol : s.tol * s.bnorm[r];
+        const bool breakdown = beta <= 1e-14 * s.bnorm[r];
+        if (res < thr || breakdown || j + 1 == m) {
+            s.active[r] = 0;
+            s.scale[r] = 0.0;
+        } else {
+            s.scale[r] = 1.0 / beta;
+            atomicAdd(s.counters, 1);
+        }
+    }
+    if (lane <= j) H[lane * m + j] = h;
+}
+
 template <typename TO, typename TI>
 __global__ void k_scale_store(const TI* __restrict__ W, const double* __restrict__ scale, int n, int nrhs,
                               TO* __restrict__ out)
@@ -802,7 +896,10 @@ static emfa_status_t gmres_t(Ctx* c, LinOp& A, const void* B, int nrhs, double2*
                 k_vupdate<T, true><<<vg, 256, 2 * nv * sizeof(typename Acc<T>::type), st>>>(V, vec, nv, s.hcol, W, n, nrhs, vblk, pnorm);
             }
             EMFA_CUDA(c, cudaMemsetAsync(s.counters, 0, sizeof(int), st));
-            k_arnoldi_finish<<<(nrhs * 32 + 127) / 128, 128, 0, st>>>(s, j, pnorm, vblk, two_pass ? 1 : 0);
+            if (m <= 32)
+                k_arnoldi_finish_warp<<<(nrhs * 32 + 127) / 128, 128, 0, st>>>(s, j, pnorm, vblk, two_pass ? 1 : 0);
+            else
+                k_arnoldi_finish<<<(nrhs * 32 + 127) / 128, 128, 0, st>>>(s, j, pnorm, vblk, two_pass ? 1 : 0);
             EMFA_CUDA(c, cudaMemcpyAsync((void*)(slot + (j & 1)), s.counters, sizeof(int), cudaMemcpyDeviceToHost, st));
             EMFA_CUDA(c, cudaEventRecord(sev.e[j & 1], st));
             c->kernel_launches += 4;
