@@ -348,10 +348,14 @@ __global__ void __launch_bounds__(256) k_vdots(const Cx<T>* __restrict__ V, size
     }
 }
 
+// With `partial` (the block partials of k_vdots) the coefficients are summed
+// here, over the blocks in order as k_reduce_partials does, and block 0 also
+// stores them in h; without it they are read from h.
 template <typename T, bool NORM>
 __global__ void __launch_bounds__(256) k_vupdate(const Cx<T>* __restrict__ V, size_t vstride, int nv,
-                                                 const double2* __restrict__ h, Cx<T>* __restrict__ W, int n,
-                                                 int nrhs, int nblk, double2* __restrict__ pnorm)
+                                                 double2* __restrict__ h, const double2* __restrict__ partial,
+                                                 Cx<T>* __restrict__ W, int n, int nrhs, int nblk,
+                                                 double2* __restrict__ pnorm)
 {
     using A = typename Acc<T>::type;
     const int blk = blockIdx.x, r = blockIdx.y;
@@ -362,7 +366,18 @@ __global__ void __launch_bounds__(256) k_vupdate(const Cx<T>* __restrict__ V, si
     A* hs1 = hs0 + nv;
     __shared__ double red[8], redm[8];
     for (int i = threadIdx.x; i < nv; i += blockDim.x) {
-        double2 t = h[(size_t)i * nrhs + r];
+        double2 t;
+        if (partial) {
+            const double2* p = partial + ((size_t)i * nrhs + r) * nblk;
+            t = make_double2(0.0, 0.0);
+            for (int b = 0; b < nblk; ++b) {
+                t.x += p[b].x;
+                t.y += p[b].y;
+            }
+            if (blk == 0) h[(size_t)i * nrhs + r] = t;
+        } else {
+            t = h[(size_t)i * nrhs + r];
+        }
         hs0[i] = (A)t.x;
         hs1[i] = (A)t.y;
     }
@@ -883,17 +898,17 @@ static emfa_status_t gmres_t(Ctx* c, LinOp& A, const void* B, int nrhs, double2*
             // (h2 = V^H W; W -= V h2) and H gets h + h2.
             const dim3 vg(vblk, nrhs);
             const int nv = j + 1;
-            const int rg = (nv * nrhs + 127) / 128;
+            // the updates sum the dots' block partials themselves (block 0 keeps
+            // the coefficients in s.hcol / s.y for the Arnoldi finish)
+            const size_t hsm = 2 * nv * sizeof(typename Acc<T>::type);
             k_vdots<T><<<vg, 256, 0, st>>>(V, vec, nv, W, n, nrhs, vblk, partial);
-            k_reduce_partials<<<rg, 128, 0, st>>>(partial, nv, nrhs, vblk, s.hcol, 0);
             if (two_pass) {
-                k_vupdate<T, false><<<vg, 256, 2 * nv * sizeof(typename Acc<T>::type), st>>>(V, vec, nv, s.hcol, W, n, nrhs, vblk, pnorm);
+                k_vupdate<T, false><<<vg, 256, hsm, st>>>(V, vec, nv, s.hcol, partial, W, n, nrhs, vblk, pnorm);
                 k_vdots<T><<<vg, 256, 0, st>>>(V, vec, nv, W, n, nrhs, vblk, partial);
-                k_reduce_partials<<<rg, 128, 0, st>>>(partial, nv, nrhs, vblk, s.y, 0);
-                k_vupdate<T, true><<<vg, 256, 2 * nv * sizeof(typename Acc<T>::type), st>>>(V, vec, nv, s.y, W, n, nrhs, vblk, pnorm);
-                c->kernel_launches += 3;
+                k_vupdate<T, true><<<vg, 256, hsm, st>>>(V, vec, nv, s.y, partial, W, n, nrhs, vblk, pnorm);
+                c->kernel_launches += 2;
             } else {
-                k_vupdate<T, true><<<vg, 256, 2 * nv * sizeof(typename Acc<T>::type), st>>>(V, vec, nv, s.hcol, W, n, nrhs, vblk, pnorm);
+                k_vupdate<T, true><<<vg, 256, hsm, st>>>(V, vec, nv, s.hcol, partial, W, n, nrhs, vblk, pnorm);
             }
             EMFA_CUDA(c, cudaMemsetAsync(s.counters, 0, sizeof(int), st));
             if (m <= 32)
@@ -902,7 +917,7 @@ static emfa_status_t gmres_t(Ctx* c, LinOp& A, const void* B, int nrhs, double2*
                 k_arnoldi_finish<<<(nrhs * 32 + 127) / 128, 128, 0, st>>>(s, j, pnorm, vblk, two_pass ? 1 : 0);
             EMFA_CUDA(c, cudaMemcpyAsync((void*)(slot + (j & 1)), s.counters, sizeof(int), cudaMemcpyDeviceToHost, st));
             EMFA_CUDA(c, cudaEventRecord(sev.e[j & 1], st));
-            c->kernel_launches += 4;
+            c->kernel_launches += 3;
             ++steps;
             if (j > 0) {
                 EMFA_CUDA(c, cudaEventSynchronize(sev.e[(j - 1) & 1]));
