@@ -7,15 +7,17 @@
 //   near / far lists                setBoxParameter (MLFMA.cpp:807-866)
 //   multipoles, Gauss-Legendre      getMultipoleNumber / levelRootsAndWeights (MLFMA.cpp:877-915)
 //   3x3 Lagrange stencils           calculateInterpolationMtr / lagrangeIPWeights (MLFMA.cpp:917-1002)
-//   translation operators           parallelLevelTrans (MLFMA.cpp:1191-1222), tabulated once per
-//                                   distinct box offset (at most 7^3 per level) instead of per box pair
 // Device (FP32 patterns, 3 Cartesian components as in the reference):
-//   k_radrec     radiation / receive patterns (MLFMA.cpp:1244-1292,1393-1422)
-//   k_near_fill  near-field CFIE blocks per (field box, near box) (MLFMA.cpp:1004-1131)
-//   per mat-vec (MLFMA.cpp:454-686):
+//   k_trans_table  translation operators (parallelLevelTrans, MLFMA.cpp:1191-1222) in FP64, once
+//                  per distinct box offset (at most 7^3 per level) instead of per box pair
+//   k_radrec       radiation / receive patterns (MLFMA.cpp:1244-1292,1393-1422)
+//   k_near_fill    near-field CFIE blocks per (field box, near box) (MLFMA.cpp:1004-1131)
+//   per mat-vec (MLFMA.cpp:454-686), up to 8 right-hand sides per pass, level patterns planar:
 //     k_agg_finest    finest-level aggregation
-//     k_upward        interpolation + shift, child -> parent (gather over children)
-//     k_downward      translation from far boxes + anterpolation from the parent (gather)
+//     k_upward        interpolation + shift, child -> parent: the 3 x 3 Lagrange stencil as two
+//                     1-D passes (theta into shared memory, then phi)
+//     k_downward      translation from far boxes + anterpolation from the parent (transposed
+//                     stencil as two 1-D passes), by chunks of phi rows
 //     k_disagg_near   disaggregation at the finest level fused with the near-field product
 #include "emfa_internal.cuh"
 #include "emfa_math.cuh"
