@@ -148,7 +148,7 @@ def test_solve_current_vs_direct(ctx, name, prec, method):
     Z = api.fill_z(geo, fp)
     V = api.fill_v(geo, fp, angles(g))
     # FP32 matrices: the true residual is resolved to ~1e-7, so 1e-6 (the
-    # BASELINE tolerance) for them; FP64 matrices go to 1e-9
+    # target tolerance) for them; FP64 matrices go to 1e-9
     sp = api.solver_params(method, tol=1e-6 if prec == "f32" else 1e-9, max_iter=2000)
     X, info = api.solve(ctx, Z, V, sp)
     assert info.converged == 1, (info.iterations, info.max_rel_residual)
