@@ -11,10 +11,15 @@
 //                 then explicit inverses of its unit-lower and upper factors
 //   k_lu_rowperm  the block's row exchanges applied to the other columns
 //   k_lu_small    U12 = L11^-1 A12 and L21 = A21 U11^-1 with those inverses
-//   k_lu_update   A22 -= L21 U12, 64 x 64 CTA tiles, K = 64
+//   k_lu_pack     split-FP16 operand planes of U12 and L21, scaled per
+//                 column / row by powers of two
+//   k_lu_update_tc  A22 -= L21 U12 on the tensor cores (tcgen05, K = 128
+//                 real), tiles of 256 rows x 64 complex columns of A22 moved
+//                 through shared memory by TMA
 // with a one-block lookahead: the next block's 64 columns are updated first,
-// and that block's k_lu_diag (one CTA, latency bound) runs while a helper
-// stream updates the remaining columns.
+// and that block's k_lu_diag (one CTA, latency bound) runs on a high-priority
+// stream while the remaining columns are updated.  Rows of the factor are
+// padded to an even number of complex elements (16-byte TMA strides).
 // Solve for many right-hand sides (RHS-major, (r, u) at r n + u): gather by
 // the row permutation, then one launch per block for the forward (L) sweep
 // and one per block for the backward (U) sweep.  Each CTA applies the block's
@@ -24,7 +29,11 @@
 // A pivot that is exactly zero is replaced by 1e-30 and recorded in the
 // factor's info word, so the caller can fall back to an iterative solve.
 #include "emfa_internal.cuh"
+#include "gemm.cuh"
 #include "lu.cuh"
+#include "tcgen05.cuh"
+
+#include <cuda_fp16.h>
 
 #include <algorithm>
 
@@ -49,7 +58,7 @@ __device__ __forceinline__ float2 cinv(float2 a)
 // Pivoted LU of the diagonal block [k0, k0 + nb)^2 and the inverses of its
 // factors.  perm[k0 + i] = the original row now at k0 + i (rows of earlier
 // blocks never move into this one, so original = k0 + local index).
-__global__ void __launch_bounds__(256) k_lu_diag(float2* __restrict__ A, int n, int k0, int nb, int* __restrict__ perm,
+__global__ void __launch_bounds__(256) k_lu_diag(float2* __restrict__ A, int n, int lda, int k0, int nb, int* __restrict__ perm,
                                                  float2* __restrict__ linv, float2* __restrict__ uinv,
                                                  int* __restrict__ info)
 {
@@ -63,7 +72,7 @@ __global__ void __launch_bounds__(256) k_lu_diag(float2* __restrict__ A, int n, 
     const int tid = threadIdx.x;
     for (int q = tid; q < NB * NB; q += blockDim.x) {
         const int i = q / NB, j = q % NB;
-        D[i * LDS + j] = (i < nb && j < nb) ? A[(size_t)(k0 + i) * n + k0 + j] : make_float2(0.f, 0.f);
+        D[i * LDS + j] = (i < nb && j < nb) ? A[(size_t)(k0 + i) * lda + k0 + j] : make_float2(0.f, 0.f);
     }
     if (tid < NB) lp[tid] = tid;
     __syncthreads();
@@ -127,7 +136,7 @@ __global__ void __launch_bounds__(256) k_lu_diag(float2* __restrict__ A, int n, 
     }
     for (int q = tid; q < nb * nb; q += blockDim.x) {
         const int i = q / nb, j = q % nb;
-        A[(size_t)(k0 + i) * n + k0 + j] = D[i * LDS + j];
+        A[(size_t)(k0 + i) * lda + k0 + j] = D[i * LDS + j];
     }
     if (tid < nb) {
         perm[k0 + tid] = k0 + lp[tid];
@@ -166,7 +175,7 @@ __global__ void __launch_bounds__(256) k_lu_diag(float2* __restrict__ A, int n, 
 
 // rows [k0, k0 + nb) of the columns outside the diagonal block, reordered
 // by the block's permutation; CTA per 32 columns
-__global__ void __launch_bounds__(256) k_lu_rowperm(float2* __restrict__ A, int n, int k0, int nb,
+__global__ void __launch_bounds__(256) k_lu_rowperm(float2* __restrict__ A, int n, int lda, int k0, int nb,
                                                     const int* __restrict__ perm)
 {
     __shared__ float2 T[NB][33];
@@ -181,20 +190,20 @@ __global__ void __launch_bounds__(256) k_lu_rowperm(float2* __restrict__ A, int 
         const int r = q / 32, cl = q % 32, cc = cc0 + cl;
         if (cc >= n - nb) continue;
         const int c = cc < k0 ? cc : cc + nb;
-        T[r][cl] = A[(size_t)perm[k0 + r] * n + c];
+        T[r][cl] = A[(size_t)perm[k0 + r] * lda + c];
     }
     __syncthreads();
     for (int q = threadIdx.x; q < nb * 32; q += blockDim.x) {
         const int r = q / 32, cl = q % 32, cc = cc0 + cl;
         if (cc >= n - nb) continue;
         const int c = cc < k0 ? cc : cc + nb;
-        A[(size_t)(k0 + r) * n + c] = T[r][cl];
+        A[(size_t)(k0 + r) * lda + c] = T[r][cl];
     }
 }
 
 // mode 0: U12 = L11^-1 A12 on the 64-column chunk blockIdx.x of [k0 + nb, n);
 // mode 1: L21 = A21 U11^-1 on the 64-row chunk blockIdx.x of [k0 + nb, n)
-__global__ void __launch_bounds__(256) k_lu_small(float2* __restrict__ A, int n, int k0, int nb,
+__global__ void __launch_bounds__(256) k_lu_small(float2* __restrict__ A, int n, int lda, int k0, int nb,
                                                   const float2* __restrict__ inv, int mode)
 {
     extern __shared__ float2 s_lu[];
@@ -209,9 +218,9 @@ __global__ void __launch_bounds__(256) k_lu_small(float2* __restrict__ A, int n,
         X[i * LDS + j] = iv[q];
         float2 v = make_float2(0.f, 0.f);
         if (mode == 0) {
-            if (i < nb && j < ne) v = A[(size_t)(k0 + i) * n + e0 + j];
+            if (i < nb && j < ne) v = A[(size_t)(k0 + i) * lda + e0 + j];
         } else {
-            if (i < ne && j < nb) v = A[(size_t)(e0 + i) * n + k0 + j];
+            if (i < ne && j < nb) v = A[(size_t)(e0 + i) * lda + k0 + j];
         }
         Y[i * LDS + j] = v;
     }
@@ -239,58 +248,290 @@ __global__ void __launch_bounds__(256) k_lu_small(float2* __restrict__ A, int n,
         for (int b = 0; b < 4; ++b) {
             const int i = ty + 16 * a, j = tx + 16 * b;
             if (mode == 0) {
-                if (i < nb && j < ne) A[(size_t)(k0 + i) * n + e0 + j] = acc[a][b];
+                if (i < nb && j < ne) A[(size_t)(k0 + i) * lda + e0 + j] = acc[a][b];
             } else {
-                if (i < ne && j < nb) A[(size_t)(e0 + i) * n + k0 + j] = acc[a][b];
+                if (i < ne && j < nb) A[(size_t)(e0 + i) * lda + k0 + j] = acc[a][b];
             }
         }
 }
 
-// trailing update A22 -= L21 U12 on the 64 x 64 tile (blockIdx.y, blockIdx.x +
-// ct0) of [k1, n)^2, K = nb <= 64
-__global__ void __launch_bounds__(256) k_lu_update(float2* __restrict__ A, int n, int k0, int nb, int ct0)
+// ---------------------------------------------------------------------------
+// Trailing update on the tensor cores: A22 -= L21 U12 as one real GEMM with
+// split-FP16 operands (tcgen05.mma kind::f16, FP32 accumulation in tensor
+// memory).  The accumulator is laid out transposed, D[real column][row], so
+// that the epilogue's 32 lanes read and write 32 consecutive floats of a row
+// of A22 (coalesced):
+//   U operand row 2j   = t_j (Re u_kj, -Im u_kj)_k     (K = 2 nb = 128 halves)
+//   U operand row 2j+1 = t_j (Im u_kj,  Re u_kj)_k
+//   L operand row i    = s_i (Re l_ik,  Im l_ik)_k
+//   D[2j + e][i] = t_j s_i (Re, Im)_e (L21 U12)_ij
+// with t_j, s_i powers of two per column of U12 and per row of L21 (largest
+// |Re|, |Im| scaled into [2^14, 2^15)), each operand split into hi = fp16(x)
+// and lo = fp16(x - hi), and D = Uh Lh + Uh Ll + Ul Lh (the lo-lo term is
+// below 2^-21 of the product).
+// ---------------------------------------------------------------------------
+namespace lutc {
+constexpr int TM = 128;                                  // real columns of A22 per tile (MMA M): 64 complex
+constexpr int TN = 256;                                  // rows of A22 per tile (MMA N)
+constexpr int KH = 2 * NB;                               // halves per operand row
+constexpr int U_BYTES = TM * 128;                        // one 64-half K slice of one U plane
+constexpr int L_BYTES = TN * 128;                        // one K slice of one L plane
+constexpr int STAGE = 2 * U_BYTES + 2 * L_BYTES;         // both planes of both operands: 96 KB
+constexpr int C_BYTES = 64 * 128 * 4;                    // 64 rows x 64 complex of A22: three fill the stage
+constexpr int SMEM = STAGE + 1024 /*align*/ + 256 /*barriers*/;
+constexpr int THREADS = 320;                             // producer, MMA, 8 epilogue warps
+constexpr int TMEM_COLS = TN;
+}  // namespace lutc
+
+__device__ __forceinline__ float2 col_max_scale(float m)
 {
-    extern __shared__ float2 s_lu[];
-    float2* As = s_lu;          // [k][LDS]: L21 tile, transposed
-    float2* Bs = As + NB * LDS; // [k][LDS]: U12 tile
-    const int k1 = k0 + nb, m = n - k1, tid = threadIdx.x;
-    const int r0 = blockIdx.y * NB, c0 = (blockIdx.x + ct0) * NB;
-    for (int q = tid; q < NB * NB; q += blockDim.x) {
-        const int i = q / NB, k = q % NB;  // L21: row i, column k (coalesced along k)
-        As[k * LDS + i] = (r0 + i < m && k < nb) ? A[(size_t)(k1 + r0 + i) * n + k0 + k] : make_float2(0.f, 0.f);
-        const int kk = q / NB, j = q % NB;  // U12: row kk, column j (coalesced along j)
-        Bs[kk * LDS + j] = (kk < nb && c0 + j < m) ? A[(size_t)(k0 + kk) * n + k1 + c0 + j] : make_float2(0.f, 0.f);
+    int e = 0;
+    frexpf(m, &e);  // m = f 2^e, f in [0.5, 1); m = 0 gives e = 0
+    return make_float2(ldexpf(1.f, 15 - e), ldexpf(1.f, e - 15));
+}
+
+__device__ __forceinline__ uint32_t h2_bits(__half2 h) { return *reinterpret_cast<uint32_t*>(&h); }
+
+// hi/lo FP16 pairs of (a, b)
+__device__ __forceinline__ void split2(float a, float b, uint32_t& hi, uint32_t& lo)
+{
+    const __half ha = __float2half_rn(a), hb = __float2half_rn(b);
+    hi = h2_bits(__halves2half2(ha, hb));
+    lo = h2_bits(__halves2half2(__float2half_rn(a - __half2float(ha)), __float2half_rn(b - __half2float(hb))));
+}
+
+// Operand planes of step k0 (nb = 64).  blockIdx.y = 0: rows of L21, one warp
+// per row; blockIdx.y = 1: columns of U12, 32 per CTA, staged and transposed
+// in shared memory so that each warp writes 512 contiguous bytes.  Operand
+// rows are indexed from k1 = k0 + nb; plane p of the U operand starts at row
+// p 2n, of the L operand at row p n.
+__global__ void __launch_bounds__(256) k_lu_pack(const float2* __restrict__ A, int n, int lda, int k0, int nb,
+                                                 __half* __restrict__ Uop, __half* __restrict__ Lop,
+                                                 float* __restrict__ inv_t, float* __restrict__ inv_s)
+{
+    const int k1 = k0 + nb, m = n - k1;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (blockIdx.y == 0) {
+        const int i = blockIdx.x * 8 + warp;
+        if (i >= m) return;
+        const float2* row = A + (size_t)(k1 + i) * lda + k0;
+        const float2 a = 2 * lane < nb ? row[2 * lane] : make_float2(0.f, 0.f);
+        const float2 b = 2 * lane + 1 < nb ? row[2 * lane + 1] : make_float2(0.f, 0.f);
+        float mx = fmaxf(fmaxf(fabsf(a.x), fabsf(a.y)), fmaxf(fabsf(b.x), fabsf(b.y)));
+        for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        const float2 sc = col_max_scale(mx);
+        if (lane == 0) inv_s[i] = sc.y;
+        uint2 h, l;
+        split2(sc.x * a.x, sc.x * a.y, h.x, l.x);
+        split2(sc.x * b.x, sc.x * b.y, h.y, l.y);
+        reinterpret_cast<uint2*>(Lop + (size_t)i * lutc::KH)[lane] = h;
+        reinterpret_cast<uint2*>(Lop + ((size_t)n + i) * lutc::KH)[lane] = l;
+        return;
+    }
+    __shared__ float2 T[NB][33];
+    __shared__ float ts[32];
+    const int j0 = blockIdx.x * 32;
+    if (j0 >= m) return;  // uniform over the CTA
+    for (int q = threadIdx.x; q < NB * 32; q += blockDim.x) {
+        const int k = q >> 5, c = q & 31;
+        T[k][c] = (k < nb && j0 + c < m) ? A[(size_t)(k0 + k) * lda + k1 + j0 + c] : make_float2(0.f, 0.f);
     }
     __syncthreads();
-    const int tx = tid & 15, ty = tid >> 4;
-    float2 acc[4][4];
-#pragma unroll
-    for (int a = 0; a < 4; ++a)
-#pragma unroll
-        for (int b = 0; b < 4; ++b) acc[a][b] = make_float2(0.f, 0.f);
-#pragma unroll 4
-    for (int k = 0; k < NB; ++k) {
-        float2 l[4], r[4];
-#pragma unroll
-        for (int a = 0; a < 4; ++a) l[a] = As[k * LDS + ty + 16 * a];
-#pragma unroll
-        for (int b = 0; b < 4; ++b) r[b] = Bs[k * LDS + tx + 16 * b];
-#pragma unroll
-        for (int a = 0; a < 4; ++a)
-#pragma unroll
-            for (int b = 0; b < 4; ++b) acc[a][b] = cfma(l[a], r[b], acc[a][b]);
-    }
-#pragma unroll
-    for (int a = 0; a < 4; ++a)
-#pragma unroll
-        for (int b = 0; b < 4; ++b) {
-            const int i = r0 + ty + 16 * a, j = c0 + tx + 16 * b;
-            if (i < m && j < m) {
-                float2* p = A + (size_t)(k1 + i) * n + k1 + j;
-                const float2 v = *p;
-                *p = make_float2(v.x - acc[a][b].x, v.y - acc[a][b].y);
-            }
+    for (int c = warp * 4; c < warp * 4 + 4; ++c) {
+        const float2 a = T[lane][c], b = T[lane + 32][c];
+        float mx = fmaxf(fmaxf(fabsf(a.x), fabsf(a.y)), fmaxf(fabsf(b.x), fabsf(b.y)));
+        for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        if (lane == 0) {
+            const float2 sc = col_max_scale(mx);
+            ts[c] = sc.x;
+            if (j0 + c < m) inv_t[j0 + c] = sc.y;
         }
+    }
+    __syncthreads();
+    // item (column c, part e, 16-byte chunk ch of the 256-byte row): 4 k values
+    for (int q = threadIdx.x; q < 32 * 2 * 16; q += blockDim.x) {
+        const int c = q >> 5, e = (q >> 4) & 1, ch = q & 15, j = j0 + c;
+        if (j >= m) continue;
+        const float t = ts[c];
+        uint4 h, l;
+        uint32_t* hp = &h.x;
+        uint32_t* lp = &l.x;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const float2 v = T[4 * ch + u][c];
+            if (e == 0)
+                split2(t * v.x, -(t * v.y), hp[u], lp[u]);
+            else
+                split2(t * v.y, t * v.x, hp[u], lp[u]);
+        }
+        const size_t r = (size_t)(2 * j + e);
+        reinterpret_cast<uint4*>(Uop + r * lutc::KH)[ch] = h;
+        reinterpret_cast<uint4*>(Uop + ((size_t)2 * n + r) * lutc::KH)[ch] = l;
+    }
+}
+
+// A22 -= L21 U12 on the tile of 64 complex columns (blockIdx.x + ct0) and
+// 256 rows (blockIdx.y) of [k1, n)^2, two CTAs per SM:
+//   warp 0      TMA producer: K slice 0, then (once its MMAs are done) slice
+//               1, of Uh, Ul (128 rows) and Lh, Ll (256 rows), 128-byte swizzle
+//   warp 1      allocates 256 tensor-memory columns; one lane issues
+//               tcgen05.mma M = 128, N = 256, K = 16: 12 per slice
+//   warps 2..9  epilogue.  Once the MMAs are done, the operand buffer holds
+//               three 64-row chunks of the tile of A22 (TMA loads, 32 KB
+//               each; the fourth chunk takes the first slot once that slot's
+//               store has read it).  Per chunk each warp takes a quadrant of
+//               the tensor-memory lanes (32 real columns) and 32 rows and
+//               subtracts the scaled accumulator in shared memory; one thread
+//               stores the chunk back with TMA.  Rows and columns past the
+//               matrix are zero-filled on load and clipped on store.
+// Every wait is bounded; on timeout the kernel records a code in *err, skips
+// the stores that would follow, drains its copies and MMAs and frees tensor
+// memory.
+__global__ void __launch_bounds__(lutc::THREADS, 2)
+    k_lu_update_tc(const __grid_constant__ CUtensorMap tmU, const __grid_constant__ CUtensorMap tmL,
+                   const __grid_constant__ CUtensorMap tmC, int n, int k1, int ct0, const float* __restrict__ inv_t,
+                   const float* __restrict__ inv_s, int* __restrict__ err)
+{
+    using namespace tc;
+    extern __shared__ uint8_t smem_raw[];
+    __shared__ float rs[lutc::TN];  // 1 / s_i of the tile's rows
+    __shared__ int eok;
+    uint8_t* base = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint8_t* sUh = base;
+    uint8_t* sUl = sUh + lutc::U_BYTES;
+    uint8_t* sLh = sUl + lutc::U_BYTES;
+    uint8_t* sLl = sLh + lutc::L_BYTES;
+    uint64_t* full = (uint64_t*)(base + lutc::STAGE);
+    uint64_t* empty = full + 1;
+    uint64_t* accum = empty + 1;
+    uint64_t* cfull = accum + 1;  // [3] chunk slots of A22
+    uint32_t* tmem_slot = (uint32_t*)(cfull + 3);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int m = n - k1;
+    const int cc0 = (blockIdx.x + ct0) * 64, r0 = blockIdx.y * lutc::TN;
+
+    if (threadIdx.x == 0) {
+        mbar_init(full, 1);
+        mbar_init(empty, 1);
+        mbar_init(accum, 1);
+        for (int c = 0; c < 3; ++c) mbar_init(cfull + c, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        fence_proxy_async();
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(lutc::TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    for (int q = threadIdx.x; q < lutc::TN; q += blockDim.x) rs[q] = r0 + q < m ? inv_s[r0 + q] : 0.f;
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            int issued = 0;
+            for (int s = 0; s < 2; ++s) {
+                if (s == 1 && !mbar_wait(empty, 0, err, 11)) break;
+                if (*(volatile int*)err) break;
+                mbar_expect_tx(full, lutc::STAGE);
+                tma_load_2d(sUh, &tmU, full, 64 * s, 2 * cc0);
+                tma_load_2d(sUl, &tmU, full, 64 * s, 2 * n + 2 * cc0);
+                tma_load_2d(sLh, &tmL, full, 64 * s, r0);
+                tma_load_2d(sLl, &tmL, full, 64 * s, n + r0);
+                issued = s + 1;
+            }
+            // the last issued copy must have landed before the CTA exits
+            if (issued) mbar_wait(full, (issued - 1) & 1, err, 12);
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            constexpr uint32_t idesc = idesc_f16(lutc::TM, lutc::TN);
+            for (int s = 0; s < 2; ++s) {
+                if (!mbar_wait(full, s & 1, err, 13)) break;
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint64_t uh = sw128_desc(smem_u32(sUh)), ul = sw128_desc(smem_u32(sUl));
+                const uint64_t lh = sw128_desc(smem_u32(sLh)), ll = sw128_desc(smem_u32(sLl));
+#pragma unroll
+                for (int k = 0; k < 4; ++k)  // K = 16 halves = 32 bytes per instruction
+                    mma_f16(tmem, uh + 2 * k, lh + 2 * k, idesc, (s > 0 || k > 0) ? 1u : 0u);
+#pragma unroll
+                for (int k = 0; k < 4; ++k) mma_f16(tmem, uh + 2 * k, ll + 2 * k, idesc, 1u);
+#pragma unroll
+                for (int k = 0; k < 4; ++k) mma_f16(tmem, ul + 2 * k, lh + 2 * k, idesc, 1u);
+                if (s == 0) mma_commit(empty);
+            }
+            // every MMA issued must be complete before the epilogue and before
+            // tensor memory is released
+            mma_commit(accum);
+            mbar_wait(accum, 0, err, 14);
+        }
+        __syncwarp();
+    } else {
+        const int q = warp & 3, hf = (warp - 2) >> 2;
+        const bool leader = threadIdx.x == 64;
+        const int l = 32 * q + lane;  // lane of tensor memory: real column of the tile
+        const int jc = cc0 + (l >> 1);  // complex column, from k1
+        const float itj = jc < m ? inv_t[jc] : 0.f;
+        const int xC = 2 * (k1 + cc0), yC = k1 + r0;  // tile origin in the float view of A
+        if (leader) {
+            // the operand buffer is free once the MMAs are done
+            int ok = (int)mbar_wait(accum, 0, err, 15);
+            if (ok) ok = *(volatile int*)err == 0;
+            if (ok)
+                for (int c = 0; c < 3; ++c) {
+                    mbar_expect_tx(cfull + c, lutc::C_BYTES);
+                    tma_load_2d(base + c * lutc::C_BYTES, &tmC, cfull + c, xC, yC + 64 * c);
+                }
+            eok = ok;
+        }
+        asm volatile("bar.sync 1, 256;" ::: "memory");
+        if (eok) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll 1
+            for (int c = 0; c < 4; ++c) {
+                const int slot = c % 3;
+                float* cs = (float*)(base + slot * lutc::C_BYTES);  // [64][128] floats
+                int got = 0;
+                if (lane == 0) got = *(volatile int*)err == 0 && mbar_wait(cfull + slot, c / 3, err, 16);
+                got = __shfl_sync(0xffffffffu, got, 0);
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int rr = 32 * hf + 16 * h;  // first row of the group, in the chunk
+                    float acc[16];
+                    tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(64 * c + rr), acc);
+                    if (got) {
+#pragma unroll
+                        for (int r = 0; r < 16; ++r) {
+                            float* p = cs + (rr + r) * 128 + l;
+                            *p = *p - acc[r] * (itj * rs[64 * c + rr + r]);
+                        }
+                    }
+                }
+                fence_proxy_async();
+                asm volatile("bar.sync 1, 256;" ::: "memory");
+                if (leader && *(volatile int*)err == 0) {
+                    tma_store_2d(&tmC, cs, xC, yC + 64 * c);
+                    bulk_store_commit();
+                    if (c == 0) {
+                        bulk_store_wait_read();  // slot 0 takes the last chunk
+                        mbar_expect_tx(cfull, lutc::C_BYTES);
+                        tma_load_2d(base, &tmC, cfull, xC, yC + 192);
+                    }
+                }
+            }
+            if (leader) bulk_store_wait();
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 1) {
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(lutc::TMEM_COLS)
+                     : "memory");
+    }
 }
 
 // W[r][i] = B[r][perm[i]]
@@ -310,7 +551,7 @@ constexpr int RC = 8;  // right-hand sides per CTA of a sweep step
 // Out), then W[rows] -= A[rows][block] x on the CTA's 64-row chunk of the rows
 // after (dir 0) or before (dir 1) the block.  The block's inverse, then the
 // chunk's 64 x 64 slice of A, are staged in shared memory.
-__global__ void __launch_bounds__(256) k_lu_sweep(const float2* __restrict__ A, int n, int k0, int nb,
+__global__ void __launch_bounds__(256) k_lu_sweep(const float2* __restrict__ A, int n, int lda, int k0, int nb,
                                                   const float2* __restrict__ inv, int dir, int nrhs,
                                                   float2* __restrict__ W, float2* __restrict__ Out)
 {
@@ -346,7 +587,7 @@ __global__ void __launch_bounds__(256) k_lu_sweep(const float2* __restrict__ A, 
     if (nm <= 0) return;  // uniform over the CTA; no barrier follows
     for (int q = tid; q < NB * NB; q += blockDim.x) {
         const int i = q / NB, j = q % NB;
-        M[i][j] = (i < nm && j < nb) ? A[(size_t)(m0 + i) * n + k0 + j] : make_float2(0.f, 0.f);
+        M[i][j] = (i < nm && j < nb) ? A[(size_t)(m0 + i) * lda + k0 + j] : make_float2(0.f, 0.f);
     }
     __syncthreads();
     for (int q = tid; q < nm * nr; q += blockDim.x) {
@@ -361,17 +602,69 @@ __global__ void __launch_bounds__(256) k_lu_sweep(const float2* __restrict__ A, 
 
 }  // namespace
 
+// trailing-update operands: U planes [2][2n][128] and L planes [2][n][128]
+// halves, then 1/t_j and 1/s_i (n floats each)
+static size_t ops_bytes(int n) { return (size_t)6 * n * lutc::KH * sizeof(__half) + 2 * sizeof(float) * (size_t)n; }
+
 size_t lu_bytes(int n)
 {
     const size_t nblk = (size_t)(n + NB - 1) / NB;
-    return sizeof(float2) * (size_t)n * n + sizeof(int) * (size_t)n + 2 * sizeof(float2) * nblk * NB * NB + 256 * 4;
+    return sizeof(float2) * (size_t)(n + (n & 1)) * n + sizeof(int) * (size_t)n + 2 * sizeof(float2) * nblk * NB * NB + 256 * 4 +
+           ops_bytes(n);
+}
+
+// FP16 operand map: rows of 128 halves (256 bytes), box 64 halves x box_rows,
+// 128-byte swizzle, zero fill past the last row
+static emfa_status_t ops_map(Ctx* c, CUtensorMap* m, const void* ptr, uint64_t rows, uint32_t box_rows)
+{
+    auto fn = tensor_map_encoder();
+    if (!fn) {
+        set_error(c, "cuTensorMapEncodeTiled unavailable");
+        return EMFA_ERR_CUDA;
+    }
+    cuuint64_t dims[2] = {(cuuint64_t)lutc::KH, rows};
+    cuuint64_t strides[1] = {(cuuint64_t)lutc::KH * sizeof(__half)};
+    cuuint32_t box[2] = {64, box_rows};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, const_cast<void*>(ptr), dims, strides, box, estr,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        set_error(c, "lu_factor: cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+        return EMFA_ERR_CUDA;
+    }
+    return EMFA_OK;
+}
+
+// A as a float matrix of n rows x 2n columns, rows lda complex apart; box
+// 128 floats (64 complex) x 64 rows, no swizzle; loads past the matrix read
+// zeros and stores there are clipped
+static emfa_status_t tile_map(Ctx* c, CUtensorMap* m, const void* A, int n, int lda)
+{
+    auto fn = tensor_map_encoder();
+    if (!fn) {
+        set_error(c, "cuTensorMapEncodeTiled unavailable");
+        return EMFA_ERR_CUDA;
+    }
+    cuuint64_t dims[2] = {2 * (cuuint64_t)n, (cuuint64_t)n};
+    cuuint64_t strides[1] = {(cuuint64_t)lda * sizeof(float2)};
+    cuuint32_t box[2] = {128, 64};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(A), dims, strides, box, estr,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        set_error(c, "lu_factor: cuTensorMapEncodeTiled (A) failed (" + std::to_string((int)r) + ")");
+        return EMFA_ERR_CUDA;
+    }
+    return EMFA_OK;
 }
 
 static emfa_status_t lu_set_smem(Ctx* c)
 {
     EMFA_TRY(ensure_smem(c, k_lu_diag, 3 * sizeof(float2) * NB * LDS));
     EMFA_TRY(ensure_smem(c, k_lu_small, 2 * sizeof(float2) * NB * LDS));
-    return ensure_smem(c, k_lu_update, 2 * sizeof(float2) * NB * LDS);
+    return ensure_smem(c, k_lu_update_tc, lutc::SMEM);
 }
 
 emfa_status_t lu_factor(Ctx* c, const void* Z, int n, LuFactor& F, cudaStream_t st)
@@ -382,65 +675,90 @@ emfa_status_t lu_factor(Ctx* c, const void* Z, int n, LuFactor& F, cudaStream_t 
     }
     EMFA_TRY(lu_set_smem(c));
     F.n = n;
+    F.lda = n + (n & 1);  // rows 16-byte aligned: the update moves tiles of A with TMA
     F.nblk = (n + NB - 1) / NB;
-    EMFA_TRY(F.a.alloc(c, sizeof(float2) * (size_t)n * n));
+    const int lda = F.lda;
+    EMFA_TRY(F.a.alloc(c, sizeof(float2) * (size_t)lda * n));
     EMFA_TRY(F.perm.alloc(c, sizeof(int) * (size_t)n));
     EMFA_TRY(F.linv.alloc(c, sizeof(float2) * (size_t)F.nblk * NB * NB));
     EMFA_TRY(F.uinv.alloc(c, sizeof(float2) * (size_t)F.nblk * NB * NB));
     EMFA_TRY(F.info.alloc(c, 256));
+    EMFA_TRY(F.ops.alloc(c, ops_bytes(n)));
     float2* A = dptr<float2>(F.a);
-    if (Z != A) EMFA_CUDA(c, cudaMemcpyAsync(A, Z, sizeof(float2) * (size_t)n * n, cudaMemcpyDeviceToDevice, st));
-    EMFA_CUDA(c, cudaMemsetAsync(F.info.ptr, 0, sizeof(int), st));
+    __half* Uop = dptr<__half>(F.ops);
+    __half* Lop = Uop + (size_t)4 * n * lutc::KH;
+    float* inv_t = (float*)(Lop + (size_t)2 * n * lutc::KH);
+    float* inv_s = inv_t + n;
+    int* info = dptr<int>(F.info);
+    CUtensorMap tmU, tmL, tmC;
+    EMFA_TRY(ops_map(c, &tmU, Uop, (uint64_t)4 * n, lutc::TM));
+    EMFA_TRY(ops_map(c, &tmL, Lop, (uint64_t)2 * n, lutc::TN));
+    EMFA_TRY(tile_map(c, &tmC, A, n, lda));
+    EMFA_CUDA(c, cudaMemcpy2DAsync(A, sizeof(float2) * (size_t)lda, Z, sizeof(float2) * (size_t)n,
+                                   sizeof(float2) * (size_t)n, (size_t)n, cudaMemcpyDeviceToDevice, st));
+    EMFA_CUDA(c, cudaMemsetAsync(info, 0, 2 * sizeof(int), st));
     const size_t s2 = 2 * sizeof(float2) * NB * LDS, s3 = 3 * sizeof(float2) * NB * LDS;
-    // helper stream and events of the lookahead (released on every return)
+    // lookahead: the next diagonal block is factored on a high-priority
+    // stream while the rest of the trailing matrix is updated on st, so its
+    // one CTA is scheduled ahead of the update's waiting tiles (released on
+    // every return)
     struct Aux {
         cudaStream_t s = nullptr;
-        cudaEvent_t panel = nullptr, rest = nullptr;
+        cudaEvent_t panel = nullptr, diag = nullptr;
         ~Aux()
         {
             if (panel) cudaEventDestroy(panel);
-            if (rest) cudaEventDestroy(rest);
+            if (diag) cudaEventDestroy(diag);
             if (s) cudaStreamDestroy(s);
         }
     } aux;
     if (F.nblk > 2) {
-        EMFA_CUDA(c, cudaStreamCreateWithFlags(&aux.s, cudaStreamNonBlocking));
+        int lo = 0, hi = 0;
+        EMFA_CUDA(c, cudaDeviceGetStreamPriorityRange(&lo, &hi));
+        EMFA_CUDA(c, cudaStreamCreateWithPriority(&aux.s, cudaStreamNonBlocking, hi));
         EMFA_CUDA(c, cudaEventCreateWithFlags(&aux.panel, cudaEventDisableTiming));
-        EMFA_CUDA(c, cudaEventCreateWithFlags(&aux.rest, cudaEventDisableTiming));
+        EMFA_CUDA(c, cudaEventCreateWithFlags(&aux.diag, cudaEventDisableTiming));
     }
-    auto diag = [&](int kb) {
+    auto diag = [&](int kb, cudaStream_t s) {
         const int k0 = kb * NB, nb = std::min(NB, n - k0);
-        k_lu_diag<<<1, 256, s3, st>>>(A, n, k0, nb, dptr<int>(F.perm), dptr<float2>(F.linv), dptr<float2>(F.uinv),
-                                      dptr<int>(F.info));
+        k_lu_diag<<<1, 256, s3, s>>>(A, n, lda, k0, nb, dptr<int>(F.perm), dptr<float2>(F.linv), dptr<float2>(F.uinv),
+                                     info);
         c->kernel_launches += 1;
     };
-    diag(0);
+    // A22 -= L21 U12 on column tiles [ct0, ct0 + nct) (64 complex columns each)
+    auto update = [&](int k1, int ct0, int nct, cudaStream_t s) {
+        const unsigned rt = (unsigned)((n - k1 + lutc::TN - 1) / lutc::TN);
+        k_lu_update_tc<<<dim3((unsigned)nct, rt), lutc::THREADS, lutc::SMEM, s>>>(tmU, tmL, tmC, n, k1, ct0,
+                                                                                   inv_t, inv_s, info + 1);
+        c->kernel_launches += 1;
+    };
+    diag(0, st);
     for (int kb = 0; kb < F.nblk; ++kb) {
         const int k0 = kb * NB, nb = std::min(NB, n - k0), rest = n - k0 - nb;
         if (n - nb > 0) {
-            k_lu_rowperm<<<(n - nb + 31) / 32, 256, 0, st>>>(A, n, k0, nb, dptr<int>(F.perm));
+            k_lu_rowperm<<<(n - nb + 31) / 32, 256, 0, st>>>(A, n, lda, k0, nb, dptr<int>(F.perm));
             c->kernel_launches += 1;
         }
         if (rest <= 0) continue;
         const unsigned ch = (unsigned)((rest + NB - 1) / NB);
-        k_lu_small<<<ch, 256, s2, st>>>(A, n, k0, nb, dptr<float2>(F.linv), 0);
-        k_lu_small<<<ch, 256, s2, st>>>(A, n, k0, nb, dptr<float2>(F.uinv), 1);
-        c->kernel_launches += 2;
+        k_lu_small<<<ch, 256, s2, st>>>(A, n, lda, k0, nb, dptr<float2>(F.linv), 0);
+        k_lu_small<<<ch, 256, s2, st>>>(A, n, lda, k0, nb, dptr<float2>(F.uinv), 1);
+        k_lu_pack<<<dim3((unsigned)((rest + 7) / 8), 2), 256, 0, st>>>(A, n, lda, k0, nb, Uop, Lop, inv_t, inv_s);
+        c->kernel_launches += 3;
         if (aux.s && ch > 1) {
-            // the next block's columns, then its diagonal block on st while
-            // the other columns are updated on the helper stream
-            k_lu_update<<<dim3(1, ch), 256, s2, st>>>(A, n, k0, nb, 0);
+            // the next block's columns, then its diagonal block on the
+            // high-priority stream while the other columns are updated
+            update(k0 + nb, 0, 1, st);
             EMFA_CUDA(c, cudaEventRecord(aux.panel, st));
             EMFA_CUDA(c, cudaStreamWaitEvent(aux.s, aux.panel, 0));
-            k_lu_update<<<dim3(ch - 1, ch), 256, s2, aux.s>>>(A, n, k0, nb, 1);
-            EMFA_CUDA(c, cudaEventRecord(aux.rest, aux.s));
-            diag(kb + 1);
-            EMFA_CUDA(c, cudaStreamWaitEvent(st, aux.rest, 0));
+            diag(kb + 1, aux.s);
+            EMFA_CUDA(c, cudaEventRecord(aux.diag, aux.s));
+            update(k0 + nb, 1, (int)ch - 1, st);
+            EMFA_CUDA(c, cudaStreamWaitEvent(st, aux.diag, 0));
         } else {
-            k_lu_update<<<dim3(ch, ch), 256, s2, st>>>(A, n, k0, nb, 0);
-            diag(kb + 1);
+            update(k0 + nb, 0, (int)ch, st);
+            diag(kb + 1, st);
         }
-        c->kernel_launches += aux.s && ch > 1 ? 2 : 1;
     }
     EMFA_CUDA(c, cudaGetLastError());
     return EMFA_OK;
@@ -448,8 +766,15 @@ emfa_status_t lu_factor(Ctx* c, const void* Z, int n, LuFactor& F, cudaStream_t 
 
 emfa_status_t lu_zero_pivot(Ctx* c, const LuFactor& F, int* first, cudaStream_t st)
 {
-    EMFA_CUDA(c, cudaMemcpyAsync(first, F.info.ptr, sizeof(int), cudaMemcpyDeviceToHost, st));
+    int h[2] = {0, 0};
+    EMFA_CUDA(c, cudaMemcpyAsync(h, F.info.ptr, sizeof(h), cudaMemcpyDeviceToHost, st));
     EMFA_CUDA(c, cudaStreamSynchronize(st));
+    *first = h[0];
+    if (h[1]) {
+        set_error(c, "lu_factor: a wait of the tensor-core trailing update timed out (stage " + std::to_string(h[1]) +
+                         ")");
+        return EMFA_ERR_TIMEOUT;
+    }
     return EMFA_OK;
 }
 
@@ -466,12 +791,12 @@ emfa_status_t lu_apply(Ctx* c, const LuFactor& F, const float2* B, int nrhs, flo
     for (int kb = 0; kb < F.nblk; ++kb) {
         const int k0 = kb * NB, nb = std::min(NB, n - k0), rows = n - k0 - nb;
         k_lu_sweep<<<dim3((unsigned)std::max(1, (rows + NB - 1) / NB), gy), 256, 0, st>>>(
-            A, n, k0, nb, dptr<float2>(F.linv), 0, nrhs, W, Y);
+            A, n, F.lda, k0, nb, dptr<float2>(F.linv), 0, nrhs, W, Y);
     }
     for (int kb = F.nblk - 1; kb >= 0; --kb) {
         const int k0 = kb * NB, nb = std::min(NB, n - k0);
         k_lu_sweep<<<dim3((unsigned)std::max(1, (k0 + NB - 1) / NB), gy), 256, 0, st>>>(
-            A, n, k0, nb, dptr<float2>(F.uinv), 1, nrhs, Y, X);
+            A, n, F.lda, k0, nb, dptr<float2>(F.uinv), 1, nrhs, Y, X);
     }
     c->kernel_launches += 1 + 2 * F.nblk;
     EMFA_CUDA(c, cudaGetLastError());
