@@ -7,7 +7,7 @@
 // Factorisation, FP32 complex, blocked right-looking, block LU_NB = 64, row
 // exchanges within each diagonal block (the rows of block k only trade places
 // among themselves).  One step per diagonal block:
-//   k_lu_diag     one CTA: pivoted LU of the diagonal block in shared memory,
+//   k_lu_diag     one CTA: pivoted LU of the diagonal block in registers,
 //                 then explicit inverses of its unit-lower and upper factors
 //   k_lu_rowperm  the block's row exchanges applied to the other columns
 //   k_lu_small    U12 = L11^-1 A12 and L21 = A21 U11^-1 with those inverses
@@ -58,118 +58,243 @@ __device__ __forceinline__ float2 cinv(float2 a)
 // Pivoted LU of the diagonal block [k0, k0 + nb)^2 and the inverses of its
 // factors.  perm[k0 + i] = the original row now at k0 + i (rows of earlier
 // blocks never move into this one, so original = k0 + local index).
-__global__ void __launch_bounds__(256) k_lu_diag(float2* __restrict__ A, int n, int lda, int k0, int nb, int* __restrict__ perm,
-                                                 float2* __restrict__ linv, float2* __restrict__ uinv,
-                                                 int* __restrict__ info)
+//
+// Factorisation in registers: warp w holds the block's rows w, w + 8, ...,
+// w + 56 and lane l its columns l and l + 32.  Rows never move: a pivot row
+// only leaves the active set, and its step number is its position in the
+// factor.  One column step takes two barriers: the pivot row is published in
+// shared memory, then every active row takes its multiplier from the lane
+// holding the pivot column (a shuffle) and updates its columns; the lane
+// holding the next column offers its warp's pivot candidate (largest |.|^2,
+// lowest row on ties).
+// Inverses: the 8 x 8 diagonal blocks of L and U by substitution (a thread
+// per column), then three merge levels of the 2 x 2 block inverse,
+//   [L11 0; L21 L22]^-1 = [X11 0; -X22 L21 X11  X22],
+//   [U11 U12; 0 U22]^-1 = [Y11 -Y11 U12 Y22; 0 Y22],
+// each two rounds of small products over all block pairs at once.
+__global__ void __launch_bounds__(256) k_lu_diag(float2* __restrict__ A, int n, int lda, int k0, int nb,
+                                                 int* __restrict__ perm, float2* __restrict__ linv,
+                                                 float2* __restrict__ uinv, int* __restrict__ info)
 {
     extern __shared__ float2 s_lu[];
-    float2* D = s_lu;               // [NB][LDS] the block, then its factors
+    float2* D = s_lu;               // [NB][LDS] the factors, in factor order
     float2* WL = D + NB * LDS;      // [NB][LDS] L^-1
     float2* WU = WL + NB * LDS;     // [NB][LDS] U^-1
-    __shared__ int lp[NB];
-    __shared__ int piv_row;
+    float2* TM = WU + NB * LDS;     // [2048] products of a merge level
+    __shared__ float2 urow[NB];     // the step's pivot row
+    __shared__ float cval[8];       // each warp's pivot candidate
+    __shared__ int crow[8];
+    __shared__ int pos[NB];         // factor position of each row
+    __shared__ int ord[NB];         // row at each factor position
     __shared__ float2 invd[NB];
-    const int tid = threadIdx.x;
-    for (int q = tid; q < NB * NB; q += blockDim.x) {
-        const int i = q / NB, j = q % NB;
-        D[i * LDS + j] = (i < nb && j < nb) ? A[(size_t)(k0 + i) * lda + k0 + j] : make_float2(0.f, 0.f);
+    const int tid = threadIdx.x, w = tid >> 5, l = tid & 31;
+    float2 d[8][2];
+    unsigned act = 0;  // bit k: row w + 8k not yet a pivot row
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const int r = w + 8 * k;
+        if (r < nb) act |= 1u << k;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int c = l + 32 * h;
+            d[k][h] = (r < nb && c < nb) ? A[(size_t)(k0 + r) * lda + k0 + c] : make_float2(0.f, 0.f);
+        }
     }
-    if (tid < NB) lp[tid] = tid;
+    for (int q = tid; q < NB * LDS; q += blockDim.x) {
+        WL[q] = make_float2(0.f, 0.f);
+        WU[q] = make_float2(0.f, 0.f);
+    }
+    if (tid < NB) pos[tid] = tid;  // rows past nb keep their own place
+    // candidates for column 0: lane 0 of each warp
+    if (l == 0) {
+        float best = -1.f;
+        int br = NB;
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            if (act >> k & 1) {
+                const float m2 = d[k][0].x * d[k][0].x + d[k][0].y * d[k][0].y;
+                if (br == NB || m2 > best) {
+                    best = m2;
+                    br = w + 8 * k;
+                }
+            }
+        cval[w] = best;
+        crow[w] = br;
+    }
     __syncthreads();
     for (int j = 0; j < nb; ++j) {
-        // pivot: largest |D[i][j]|^2 over i >= j (lowest index on ties), warp 0
-        if (tid < 32) {
-            float best = -1.f;
-            int bi = j;
-            for (int i = j + tid; i < nb; i += 32) {
-                const float2 v = D[i * LDS + j];
-                const float m = v.x * v.x + v.y * v.y;
-                if (m > best) {
-                    best = m;
-                    bi = i;
-                }
-            }
+        // the pivot row p: every thread reduces the eight candidates alike
+        float best = -1.f;
+        int p = NB;
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                const float ob = __shfl_xor_sync(0xffffffffu, best, o);
-                const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-                if (ob > best || (ob == best && oi < bi)) {
-                    best = ob;
-                    bi = oi;
+        for (int v = 0; v < 8; ++v) {
+            const float cv = cval[v];
+            const int cr = crow[v];
+            // a warp without active rows offers row NB; the first real
+            // candidate is taken even if its value is NaN
+            if (cr < NB && (p == NB || cv > best || (cv == best && cr < p))) {
+                best = cv;
+                p = cr;
+            }
+        }
+        if ((p & 7) == w) {
+            const int kp = p >> 3;
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+                if (k == kp) {
+                    urow[l] = d[k][0];
+                    urow[l + 32] = d[k][1];
+                    act &= ~(1u << k);
                 }
-            }
-            if (tid == 0) piv_row = bi;
+        }
+        if (tid == 0) {
+            ord[j] = p;
+            pos[p] = j;
         }
         __syncthreads();
-        const int p = piv_row;
-        if (p != j) {
-            for (int c = tid; c < nb; c += blockDim.x) {
-                const float2 t = D[j * LDS + c];
-                D[j * LDS + c] = D[p * LDS + c];
-                D[p * LDS + c] = t;
-            }
-            if (tid == 0) {
-                const int t = lp[j];
-                lp[j] = lp[p];
-                lp[p] = t;
-            }
-        }
-        __syncthreads();
-        float2 pv = D[j * LDS + j];
+        float2 pv = urow[j];
         if (pv.x == 0.f && pv.y == 0.f) {
             if (tid == 0) atomicCAS(info, 0, k0 + j + 1);
             pv = make_float2(1e-30f, 0.f);
         }
         const float2 ipv = cinv(pv);
-        __syncthreads();  // every thread has read the pivot
-        for (int i = j + 1 + tid; i < nb; i += blockDim.x) D[i * LDS + j] = cm(D[i * LDS + j], ipv);
-        if (tid == 0) D[j * LDS + j] = pv;
-        __syncthreads();
-        const int w = nb - j - 1;
-        for (int q = tid; q < w * w; q += blockDim.x) {
-            const int i = j + 1 + q / w, c = j + 1 + q % w;
-            const float2 l = D[i * LDS + j], u = D[j * LDS + c];
-            D[i * LDS + c] = make_float2(D[i * LDS + c].x - (l.x * u.x - l.y * u.y),
-                                         D[i * LDS + c].y - (l.x * u.y + l.y * u.x));
+        const int hj = j >> 5, lj = j & 31;
+        const float2 u0 = urow[l], u1 = urow[l + 32];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            if (!(act >> k & 1)) continue;  // uniform over the warp
+            const float2 own = hj ? d[k][1] : d[k][0];
+            float2 lm;
+            lm.x = __shfl_sync(0xffffffffu, own.x, lj);
+            lm.y = __shfl_sync(0xffffffffu, own.y, lj);
+            lm = cm(lm, ipv);
+            if (l > j) d[k][0] = make_float2(d[k][0].x - (lm.x * u0.x - lm.y * u0.y), d[k][0].y - (lm.x * u0.y + lm.y * u0.x));
+            if (l + 32 > j)
+                d[k][1] = make_float2(d[k][1].x - (lm.x * u1.x - lm.y * u1.y), d[k][1].y - (lm.x * u1.y + lm.y * u1.x));
+            if (l == lj) {
+                if (hj)
+                    d[k][1] = lm;
+                else
+                    d[k][0] = lm;
+            }
+        }
+        // the pivot row keeps its value; a replaced zero pivot is stored
+        if ((p & 7) == w && l == lj) {
+            const int kp = p >> 3;
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+                if (k == kp) {
+                    if (hj)
+                        d[k][1] = pv;
+                    else
+                        d[k][0] = pv;
+                }
+        }
+        // candidates for column j + 1
+        const int j1 = j + 1;
+        if (j1 < nb && l == (j1 & 31)) {
+            const int h1 = j1 >> 5;
+            float b1 = -1.f;
+            int r1 = NB;
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+                if (act >> k & 1) {
+                    const float2 v = h1 ? d[k][1] : d[k][0];
+                    const float m2 = v.x * v.x + v.y * v.y;
+                    if (r1 == NB || m2 > b1) {
+                        b1 = m2;
+                        r1 = w + 8 * k;
+                    }
+                }
+            cval[w] = b1;
+            crow[w] = r1;
         }
         __syncthreads();
     }
-    for (int q = tid; q < nb * nb; q += blockDim.x) {
-        const int i = q / nb, j = q % nb;
-        A[(size_t)(k0 + i) * lda + k0 + j] = D[i * LDS + j];
-    }
-    if (tid < nb) {
-        perm[k0 + tid] = k0 + lp[tid];
-        invd[tid] = cinv(D[tid * LDS + tid]);
-    }
-    __syncthreads();
-    // column c of L^-1 (threads 0..63) and of U^-1 (threads 64..127); entries
-    // outside the block (nb < NB) stay zero
-    if (tid < NB) {
-        const int c = tid;
-        for (int i = 0; i < NB; ++i) {
-            float2 s = make_float2(0.f, 0.f);
-            for (int k = 0; k < i; ++k) s = cfma(D[i * LDS + k], WL[k * LDS + c], s);
-            float2 x = make_float2(0.f, 0.f);
-            if (c < nb && i < nb && i >= c) x = (i == c) ? make_float2(1.f, 0.f) : make_float2(-s.x, -s.y);
-            WL[i * LDS + c] = x;
-        }
-    } else if (tid < 2 * NB) {
-        const int c = tid - NB;
-        for (int i = NB - 1; i >= 0; --i) {
-            float2 s = make_float2(0.f, 0.f);
-            for (int k = i + 1; k < NB; ++k) s = cfma(D[i * LDS + k], WU[k * LDS + c], s);
-            float2 x = make_float2(0.f, 0.f);
-            if (c < nb && i <= c) x = cm(make_float2((i == c ? 1.f : 0.f) - s.x, -s.y), invd[i]);
-            WU[i * LDS + c] = x;
+    // the factors in factor order: shared memory (rows and columns past nb
+    // are zero) and A
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const int r = w + 8 * k;
+        const int i = pos[r];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int c = l + 32 * h;
+            D[i * LDS + c] = d[k][h];
+            if (r < nb && c < nb) A[(size_t)(k0 + i) * lda + k0 + c] = d[k][h];
         }
     }
+    if (tid < nb) perm[k0 + tid] = k0 + ord[tid];
     __syncthreads();
+    if (tid < NB) invd[tid] = tid < nb ? cinv(D[tid * LDS + tid]) : make_float2(1.f, 0.f);
+    if (tid >= nb && tid < NB) D[tid * LDS + tid] = make_float2(1.f, 0.f);  // identity past the block
+    __syncthreads();
+    // 8 x 8 diagonal blocks: threads 0..63 columns of L^-1, 64..127 of U^-1
+    if (tid < 2 * NB) {
+        const int t = tid & 63, b0 = t & ~7, c = t & 7;
+        float2 x[8];
+        if (tid < NB) {
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                float2 s = make_float2(0.f, 0.f);
+#pragma unroll
+                for (int k = 0; k < 8; ++k)
+                    if (k >= c && k < i) s = cfma(D[(b0 + i) * LDS + b0 + k], x[k], s);
+                x[i] = i < c ? make_float2(0.f, 0.f) : i == c ? make_float2(1.f, 0.f) : make_float2(-s.x, -s.y);
+            }
+#pragma unroll
+            for (int i = 0; i < 8; ++i) WL[(b0 + i) * LDS + b0 + c] = x[i];
+        } else {
+#pragma unroll
+            for (int i = 7; i >= 0; --i) {
+                float2 s = make_float2(0.f, 0.f);
+#pragma unroll
+                for (int k = 0; k < 8; ++k)
+                    if (k > i && k <= c) s = cfma(D[(b0 + i) * LDS + b0 + k], x[k], s);
+                x[i] = i > c ? make_float2(0.f, 0.f)
+                             : cm(make_float2((i == c ? 1.f : 0.f) - s.x, -s.y), invd[b0 + i]);
+            }
+#pragma unroll
+            for (int i = 0; i < 8; ++i) WU[(b0 + i) * LDS + b0 + c] = x[i];
+        }
+    }
+    __syncthreads();
+    for (int b = 8; b < NB; b *= 2) {
+        const int pairs = (NB / 2) / b, per = pairs * b * b;
+        // T = L21 X11 (L) and T = Y11 U12 (U) for every pair of b-blocks
+        for (int q = tid; q < 2 * per; q += blockDim.x) {
+            const int mat = q / per, rem = q % per, pr = rem / (b * b), r = (rem / b) % b, c = rem % b;
+            const int i0 = pr * 2 * b;
+            float2 s = make_float2(0.f, 0.f);
+            if (mat == 0)
+                for (int k = 0; k < b; ++k) s = cfma(D[(i0 + b + r) * LDS + i0 + k], WL[(i0 + k) * LDS + i0 + c], s);
+            else
+                for (int k = 0; k < b; ++k) s = cfma(WU[(i0 + r) * LDS + i0 + k], D[(i0 + k) * LDS + i0 + b + c], s);
+            TM[q] = s;
+        }
+        __syncthreads();
+        // X21 = -X22 T (L) and Y12 = -T Y22 (U)
+        for (int q = tid; q < 2 * per; q += blockDim.x) {
+            const int mat = q / per, rem = q % per, pr = rem / (b * b), r = (rem / b) % b, c = rem % b;
+            const int i0 = pr * 2 * b;
+            const float2* T = TM + mat * per + pr * b * b;
+            float2 s = make_float2(0.f, 0.f);
+            if (mat == 0) {
+                for (int k = 0; k < b; ++k) s = cfma(WL[(i0 + b + r) * LDS + i0 + b + k], T[k * b + c], s);
+                WL[(i0 + b + r) * LDS + i0 + c] = make_float2(-s.x, -s.y);
+            } else {
+                for (int k = 0; k < b; ++k) s = cfma(T[r * b + k], WU[(i0 + b + k) * LDS + i0 + b + c], s);
+                WU[(i0 + r) * LDS + i0 + b + c] = make_float2(-s.x, -s.y);
+            }
+        }
+        __syncthreads();
+    }
     const size_t kb = (size_t)(k0 / NB) * NB * NB;
     for (int q = tid; q < NB * NB; q += blockDim.x) {
         const int i = q / NB, j = q % NB;
-        linv[kb + q] = WL[i * LDS + j];
-        uinv[kb + q] = WU[i * LDS + j];
+        const bool in = i < nb && j < nb;
+        linv[kb + q] = in ? WL[i * LDS + j] : make_float2(0.f, 0.f);
+        uinv[kb + q] = in ? WU[i * LDS + j] : make_float2(0.f, 0.f);
     }
 }
 
@@ -660,9 +785,13 @@ static emfa_status_t tile_map(Ctx* c, CUtensorMap* m, const void* A, int n, int 
     return EMFA_OK;
 }
 
+// three padded 64 x 64 blocks and the merge products (2048): about 116 KB,
+// so the CTA fits on an SM beside one CTA of the trailing update
+static size_t diag_smem() { return sizeof(float2) * (3 * NB * LDS + 2048); }
+
 static emfa_status_t lu_set_smem(Ctx* c)
 {
-    EMFA_TRY(ensure_smem(c, k_lu_diag, 3 * sizeof(float2) * NB * LDS));
+    EMFA_TRY(ensure_smem(c, k_lu_diag, diag_smem()));
     EMFA_TRY(ensure_smem(c, k_lu_small, 2 * sizeof(float2) * NB * LDS));
     return ensure_smem(c, k_lu_update_tc, lutc::SMEM);
 }
@@ -697,7 +826,7 @@ emfa_status_t lu_factor(Ctx* c, const void* Z, int n, LuFactor& F, cudaStream_t 
     EMFA_CUDA(c, cudaMemcpy2DAsync(A, sizeof(float2) * (size_t)lda, Z, sizeof(float2) * (size_t)n,
                                    sizeof(float2) * (size_t)n, (size_t)n, cudaMemcpyDeviceToDevice, st));
     EMFA_CUDA(c, cudaMemsetAsync(info, 0, 2 * sizeof(int), st));
-    const size_t s2 = 2 * sizeof(float2) * NB * LDS, s3 = 3 * sizeof(float2) * NB * LDS;
+    const size_t s2 = 2 * sizeof(float2) * NB * LDS;
     // lookahead: the next diagonal block is factored on a high-priority
     // stream while the rest of the trailing matrix is updated on st, so its
     // one CTA is scheduled ahead of the update's waiting tiles (released on
@@ -721,7 +850,7 @@ emfa_status_t lu_factor(Ctx* c, const void* Z, int n, LuFactor& F, cudaStream_t 
     }
     auto diag = [&](int kb, cudaStream_t s) {
         const int k0 = kb * NB, nb = std::min(NB, n - k0);
-        k_lu_diag<<<1, 256, s3, s>>>(A, n, lda, k0, nb, dptr<int>(F.perm), dptr<float2>(F.linv), dptr<float2>(F.uinv),
+        k_lu_diag<<<1, 256, diag_smem(), s>>>(A, n, lda, k0, nb, dptr<int>(F.perm), dptr<float2>(F.linv), dptr<float2>(F.uinv),
                                      info);
         c->kernel_launches += 1;
     };
