@@ -9,17 +9,19 @@
 // among themselves).  One step per diagonal block:
 //   k_lu_diag     one CTA: pivoted LU of the diagonal block in registers,
 //                 then explicit inverses of its unit-lower and upper factors
-//   k_lu_rowperm  the block's row exchanges applied to the other columns
-//   k_lu_small    U12 = L11^-1 A12 and L21 = A21 U11^-1 with those inverses
-//   k_lu_pack     split-FP16 operand planes of U12 and L21, scaled per
-//                 column / row by powers of two
+//   k_lu_panels   U12 = L11^-1 P A12 and L21 = A21 U11^-1 with those
+//                 inverses (P the block's row exchange, applied by reading
+//                 A12 through the permutation), and their split-FP16
+//                 operand planes, scaled per column / row by powers of two
 //   k_lu_update_tc  A22 -= L21 U12 on the tensor cores (tcgen05, K = 128
 //                 real), tiles of 256 rows x 64 complex columns of A22 moved
 //                 through shared memory by TMA
 // with a one-block lookahead: the next block's 64 columns are updated first,
 // and that block's k_lu_diag (one CTA, latency bound) runs on a high-priority
-// stream while the remaining columns are updated.  Rows of the factor are
-// padded to an even number of complex elements (16-byte TMA strides).
+// stream while the remaining columns are updated.  The row exchanges reach
+// the columns left of each block in one pass at the end (k_lu_rowperm_left).
+// Rows of the factor are padded to an even number of complex elements
+// (16-byte TMA strides).
 // Solve for many right-hand sides (RHS-major, (r, u) at r n + u): gather by
 // the row permutation, then one launch per block for the forward (L) sweep
 // and one per block for the backward (U) sweep.  Each CTA applies the block's
@@ -59,22 +61,28 @@ __device__ __forceinline__ float2 cinv(float2 a)
 // factors.  perm[k0 + i] = the original row now at k0 + i (rows of earlier
 // blocks never move into this one, so original = k0 + local index).
 //
-// Factorisation in registers: warp w holds the block's rows w, w + 8, ...,
-// w + 56 and lane l its columns l and l + 32.  Rows never move: a pivot row
-// only leaves the active set, and its step number is its position in the
-// factor.  One column step takes two barriers: the pivot row is published in
-// shared memory, then every active row takes its multiplier from the lane
-// holding the pivot column (a shuffle) and updates its columns; the lane
+// Factorisation in registers: warp w (of 16) holds the block's rows w,
+// w + 16, w + 32, w + 48 and lane l its columns l and l + 32.  Rows never
+// move: a pivot row only leaves the active set, and its step number is its
+// position in the factor.  One column step takes two barriers: the pivot row
+// is published in shared memory, then every active row takes its multiplier
+// from the lane holding the pivot column (a shuffle) and updates its columns
+// (branch-free: an inactive row subtracts a zero multiplier); the lane
 // holding the next column offers its warp's pivot candidate (largest |.|^2,
-// lowest row on ties).
+// lowest row on ties), and every warp reduces the 16 candidates with
+// shuffles.
 // Inverses: the 8 x 8 diagonal blocks of L and U by substitution (a thread
 // per column), then three merge levels of the 2 x 2 block inverse,
 //   [L11 0; L21 L22]^-1 = [X11 0; -X22 L21 X11  X22],
 //   [U11 U12; 0 U22]^-1 = [Y11 -Y11 U12 Y22; 0 Y22],
 // each two rounds of small products over all block pairs at once.
-__global__ void __launch_bounds__(256) k_lu_diag(float2* __restrict__ A, int n, int lda, int k0, int nb,
-                                                 int* __restrict__ perm, float2* __restrict__ linv,
-                                                 float2* __restrict__ uinv, int* __restrict__ info)
+constexpr int DIAG_THREADS = 512;
+constexpr int DW = DIAG_THREADS / 32;  // warps; rows per warp NB / DW
+constexpr int DR = NB / DW;
+
+__global__ void __launch_bounds__(DIAG_THREADS) k_lu_diag(float2* __restrict__ A, int n, int lda, int k0, int nb,
+                                                          int* __restrict__ perm, float2* __restrict__ linv,
+                                                          float2* __restrict__ uinv, int* __restrict__ info)
 {
     extern __shared__ float2 s_lu[];
     float2* D = s_lu;               // [NB][LDS] the factors, in factor order
@@ -82,17 +90,17 @@ __global__ void __launch_bounds__(256) k_lu_diag(float2* __restrict__ A, int n, 
     float2* WU = WL + NB * LDS;     // [NB][LDS] U^-1
     float2* TM = WU + NB * LDS;     // [2048] products of a merge level
     __shared__ float2 urow[NB];     // the step's pivot row
-    __shared__ float cval[8];       // each warp's pivot candidate
-    __shared__ int crow[8];
+    __shared__ float cval[DW];      // each warp's pivot candidate
+    __shared__ int crow[DW];
     __shared__ int pos[NB];         // factor position of each row
     __shared__ int ord[NB];         // row at each factor position
     __shared__ float2 invd[NB];
     const int tid = threadIdx.x, w = tid >> 5, l = tid & 31;
-    float2 d[8][2];
-    unsigned act = 0;  // bit k: row w + 8k not yet a pivot row
+    float2 d[DR][2];
+    unsigned act = 0;  // bit k: row w + DW k not yet a pivot row
 #pragma unroll
-    for (int k = 0; k < 8; ++k) {
-        const int r = w + 8 * k;
+    for (int k = 0; k < DR; ++k) {
+        const int r = w + DW * k;
         if (r < nb) act |= 1u << k;
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
@@ -105,47 +113,50 @@ __global__ void __launch_bounds__(256) k_lu_diag(float2* __restrict__ A, int n, 
         WU[q] = make_float2(0.f, 0.f);
     }
     if (tid < NB) pos[tid] = tid;  // rows past nb keep their own place
-    // candidates for column 0: lane 0 of each warp
-    if (l == 0) {
-        float best = -1.f;
+    // the candidate of this warp's rows in column j (lane j % 32 holds it)
+    auto offer = [&](int j) {
+        const int h = j >> 5;
+        float b = -1.f;
         int br = NB;
 #pragma unroll
-        for (int k = 0; k < 8; ++k)
+        for (int k = 0; k < DR; ++k)
             if (act >> k & 1) {
-                const float m2 = d[k][0].x * d[k][0].x + d[k][0].y * d[k][0].y;
-                if (br == NB || m2 > best) {
-                    best = m2;
-                    br = w + 8 * k;
+                const float2 v = h ? d[k][1] : d[k][0];
+                const float m2 = v.x * v.x + v.y * v.y;
+                if (br == NB || m2 > b) {  // the first active row is taken even if NaN
+                    b = m2;
+                    br = w + DW * k;
                 }
             }
-        cval[w] = best;
+        cval[w] = b;
         crow[w] = br;
-    }
+    };
+    if (l == 0) offer(0);
     __syncthreads();
     for (int j = 0; j < nb; ++j) {
-        // the pivot row p: every thread reduces the eight candidates alike
-        float best = -1.f;
-        int p = NB;
+        // the pivot row p: each warp reduces the candidates alike; lane 0's
+        // result is taken by all lanes
+        float best = l < DW ? cval[l] : -1.f;
+        int p = l < DW ? crow[l] : NB;
 #pragma unroll
-        for (int v = 0; v < 8; ++v) {
-            const float cv = cval[v];
-            const int cr = crow[v];
-            // a warp without active rows offers row NB; the first real
-            // candidate is taken even if its value is NaN
-            if (cr < NB && (p == NB || cv > best || (cv == best && cr < p))) {
-                best = cv;
-                p = cr;
+        for (int o = DW / 2; o > 0; o >>= 1) {
+            const float ob = __shfl_xor_sync(0xffffffffu, best, o);
+            const int op = __shfl_xor_sync(0xffffffffu, p, o);
+            if (op < NB && (p == NB || ob > best || (ob == best && op < p))) {
+                best = ob;
+                p = op;
             }
         }
-        if ((p & 7) == w) {
-            const int kp = p >> 3;
+        p = __shfl_sync(0xffffffffu, p, 0);
+        const int kp = p / DW;
+        if (p % DW == w) {
 #pragma unroll
-            for (int k = 0; k < 8; ++k)
+            for (int k = 0; k < DR; ++k)
                 if (k == kp) {
                     urow[l] = d[k][0];
                     urow[l + 32] = d[k][1];
-                    act &= ~(1u << k);
                 }
+            act &= ~(1u << kp);
         }
         if (tid == 0) {
             ord[j] = p;
@@ -160,29 +171,26 @@ __global__ void __launch_bounds__(256) k_lu_diag(float2* __restrict__ A, int n, 
         const float2 ipv = cinv(pv);
         const int hj = j >> 5, lj = j & 31;
         const float2 u0 = urow[l], u1 = urow[l + 32];
+        const bool up0 = l > j, up1 = l + 32 > j;
 #pragma unroll
-        for (int k = 0; k < 8; ++k) {
-            if (!(act >> k & 1)) continue;  // uniform over the warp
+        for (int k = 0; k < DR; ++k) {
+            const bool a = act >> k & 1;
             const float2 own = hj ? d[k][1] : d[k][0];
             float2 lm;
             lm.x = __shfl_sync(0xffffffffu, own.x, lj);
             lm.y = __shfl_sync(0xffffffffu, own.y, lj);
             lm = cm(lm, ipv);
-            if (l > j) d[k][0] = make_float2(d[k][0].x - (lm.x * u0.x - lm.y * u0.y), d[k][0].y - (lm.x * u0.y + lm.y * u0.x));
-            if (l + 32 > j)
-                d[k][1] = make_float2(d[k][1].x - (lm.x * u1.x - lm.y * u1.y), d[k][1].y - (lm.x * u1.y + lm.y * u1.x));
-            if (l == lj) {
-                if (hj)
-                    d[k][1] = lm;
-                else
-                    d[k][0] = lm;
-            }
+            if (!a) lm = make_float2(0.f, 0.f);
+            const float2 n0 = make_float2(d[k][0].x - (lm.x * u0.x - lm.y * u0.y), d[k][0].y - (lm.x * u0.y + lm.y * u0.x));
+            const float2 n1 = make_float2(d[k][1].x - (lm.x * u1.x - lm.y * u1.y), d[k][1].y - (lm.x * u1.y + lm.y * u1.x));
+            const bool st = a && l == lj;  // this lane keeps the multiplier
+            d[k][0] = (st && !hj) ? lm : up0 ? n0 : d[k][0];
+            d[k][1] = (st && hj) ? lm : up1 ? n1 : d[k][1];
         }
         // the pivot row keeps its value; a replaced zero pivot is stored
-        if ((p & 7) == w && l == lj) {
-            const int kp = p >> 3;
+        if (p % DW == w && l == lj) {
 #pragma unroll
-            for (int k = 0; k < 8; ++k)
+            for (int k = 0; k < DR; ++k)
                 if (k == kp) {
                     if (hj)
                         d[k][1] = pv;
@@ -190,32 +198,14 @@ __global__ void __launch_bounds__(256) k_lu_diag(float2* __restrict__ A, int n, 
                         d[k][0] = pv;
                 }
         }
-        // candidates for column j + 1
-        const int j1 = j + 1;
-        if (j1 < nb && l == (j1 & 31)) {
-            const int h1 = j1 >> 5;
-            float b1 = -1.f;
-            int r1 = NB;
-#pragma unroll
-            for (int k = 0; k < 8; ++k)
-                if (act >> k & 1) {
-                    const float2 v = h1 ? d[k][1] : d[k][0];
-                    const float m2 = v.x * v.x + v.y * v.y;
-                    if (r1 == NB || m2 > b1) {
-                        b1 = m2;
-                        r1 = w + 8 * k;
-                    }
-                }
-            cval[w] = b1;
-            crow[w] = r1;
-        }
+        if (j + 1 < nb && l == ((j + 1) & 31)) offer(j + 1);
         __syncthreads();
     }
     // the factors in factor order: shared memory (rows and columns past nb
     // are zero) and A
 #pragma unroll
-    for (int k = 0; k < 8; ++k) {
-        const int r = w + 8 * k;
+    for (int k = 0; k < DR; ++k) {
+        const int r = w + DW * k;
         const int i = pos[r];
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
@@ -298,86 +288,31 @@ __global__ void __launch_bounds__(256) k_lu_diag(float2* __restrict__ A, int n, 
     }
 }
 
-// rows [k0, k0 + nb) of the columns outside the diagonal block, reordered
-// by the block's permutation; CTA per 32 columns
-__global__ void __launch_bounds__(256) k_lu_rowperm(float2* __restrict__ A, int n, int lda, int k0, int nb,
-                                                    const int* __restrict__ perm)
+// The row exchanges of every diagonal block applied to the columns left of
+// the block (the factor's L part), once the factorisation is done: the
+// exchanges stay within a block and those columns are final by then.  CTA
+// per (32 columns, block).
+__global__ void __launch_bounds__(256) k_lu_rowperm_left(float2* __restrict__ A, int n, int lda,
+                                                         const int* __restrict__ perm)
 {
     __shared__ float2 T[NB][33];
     __shared__ int moved;
+    const int k0 = blockIdx.y * NB, nb = min(NB, n - k0), c0 = blockIdx.x * 32;
+    if (c0 >= k0) return;  // uniform over the CTA
     if (threadIdx.x == 0) moved = 0;
     __syncthreads();
     if (threadIdx.x < nb && perm[k0 + threadIdx.x] != k0 + (int)threadIdx.x) moved = 1;
     __syncthreads();
     if (!moved) return;
-    const int cc0 = blockIdx.x * 32;
     for (int q = threadIdx.x; q < nb * 32; q += blockDim.x) {
-        const int r = q / 32, cl = q % 32, cc = cc0 + cl;
-        if (cc >= n - nb) continue;
-        const int c = cc < k0 ? cc : cc + nb;
-        T[r][cl] = A[(size_t)perm[k0 + r] * lda + c];
+        const int r = q / 32, c = c0 + q % 32;
+        if (c < k0) T[r][q % 32] = A[(size_t)perm[k0 + r] * lda + c];
     }
     __syncthreads();
     for (int q = threadIdx.x; q < nb * 32; q += blockDim.x) {
-        const int r = q / 32, cl = q % 32, cc = cc0 + cl;
-        if (cc >= n - nb) continue;
-        const int c = cc < k0 ? cc : cc + nb;
-        A[(size_t)(k0 + r) * lda + c] = T[r][cl];
+        const int r = q / 32, c = c0 + q % 32;
+        if (c < k0) A[(size_t)(k0 + r) * lda + c] = T[r][q % 32];
     }
-}
-
-// mode 0: U12 = L11^-1 A12 on the 64-column chunk blockIdx.x of [k0 + nb, n);
-// mode 1: L21 = A21 U11^-1 on the 64-row chunk blockIdx.x of [k0 + nb, n)
-__global__ void __launch_bounds__(256) k_lu_small(float2* __restrict__ A, int n, int lda, int k0, int nb,
-                                                  const float2* __restrict__ inv, int mode)
-{
-    extern __shared__ float2 s_lu[];
-    float2* X = s_lu;           // [NB][LDS] the inverse
-    float2* Y = X + NB * LDS;   // [NB][LDS] the panel chunk
-    const int k1 = k0 + nb, tid = threadIdx.x;
-    const int e0 = k1 + blockIdx.x * NB;  // first column (mode 0) or row (mode 1) of the chunk
-    const int ne = min(NB, n - e0);
-    const float2* iv = inv + (size_t)(k0 / NB) * NB * NB;
-    for (int q = tid; q < NB * NB; q += blockDim.x) {
-        const int i = q / NB, j = q % NB;
-        X[i * LDS + j] = iv[q];
-        float2 v = make_float2(0.f, 0.f);
-        if (mode == 0) {
-            if (i < nb && j < ne) v = A[(size_t)(k0 + i) * lda + e0 + j];
-        } else {
-            if (i < ne && j < nb) v = A[(size_t)(e0 + i) * lda + k0 + j];
-        }
-        Y[i * LDS + j] = v;
-    }
-    __syncthreads();
-    const int tx = tid & 15, ty = tid >> 4;
-    float2 acc[4][4];
-#pragma unroll
-    for (int a = 0; a < 4; ++a)
-#pragma unroll
-        for (int b = 0; b < 4; ++b) acc[a][b] = make_float2(0.f, 0.f);
-    for (int k = 0; k < NB; ++k) {
-        float2 l[4], r[4];
-#pragma unroll
-        for (int a = 0; a < 4; ++a) l[a] = mode == 0 ? X[(ty + 16 * a) * LDS + k] : Y[(ty + 16 * a) * LDS + k];
-#pragma unroll
-        for (int b = 0; b < 4; ++b) r[b] = mode == 0 ? Y[k * LDS + tx + 16 * b] : X[k * LDS + tx + 16 * b];
-#pragma unroll
-        for (int a = 0; a < 4; ++a)
-#pragma unroll
-            for (int b = 0; b < 4; ++b) acc[a][b] = cfma(l[a], r[b], acc[a][b]);
-    }
-#pragma unroll
-    for (int a = 0; a < 4; ++a)
-#pragma unroll
-        for (int b = 0; b < 4; ++b) {
-            const int i = ty + 16 * a, j = tx + 16 * b;
-            if (mode == 0) {
-                if (i < nb && j < ne) A[(size_t)(k0 + i) * lda + e0 + j] = acc[a][b];
-            } else {
-                if (i < ne && j < nb) A[(size_t)(e0 + i) * lda + k0 + j] = acc[a][b];
-            }
-        }
 }
 
 // ---------------------------------------------------------------------------
@@ -425,73 +360,126 @@ __device__ __forceinline__ void split2(float a, float b, uint32_t& hi, uint32_t&
     lo = h2_bits(__halves2half2(__float2half_rn(a - __half2float(ha)), __float2half_rn(b - __half2float(hb))));
 }
 
-// Operand planes of step k0 (nb = 64).  blockIdx.y = 0: rows of L21, one warp
-// per row; blockIdx.y = 1: columns of U12, 32 per CTA, staged and transposed
-// in shared memory so that each warp writes 512 contiguous bytes.  Operand
-// rows are indexed from k1 = k0 + nb; plane p of the U operand starts at row
-// p 2n, of the L operand at row p n.
-__global__ void __launch_bounds__(256) k_lu_pack(const float2* __restrict__ A, int n, int lda, int k0, int nb,
-                                                 __half* __restrict__ Uop, __half* __restrict__ Lop,
-                                                 float* __restrict__ inv_t, float* __restrict__ inv_s)
+// Panels of step k0, written to A and packed as the trailing update's
+// split-FP16 operand planes (rows indexed from k1 = k0 + nb; plane p of the U
+// operand starts at row p 2n, of the L operand at row p n):
+//   blockIdx.y = 0: U12 = L11^-1 P A12 on the 64-column chunk blockIdx.x,
+//                   P the diagonal block's row exchange (row perm[k0 + i] of
+//                   A12 is read for row i)
+//   blockIdx.y = 1: L21 = A21 U11^-1 on the 64-row chunk blockIdx.x
+// The chunk's product is kept in shared memory, scaled per column of U12 /
+// row of L21, and written as 16-byte pieces of contiguous operand rows.
+__global__ void __launch_bounds__(256) k_lu_panels(float2* __restrict__ A, int n, int lda, int k0, int nb,
+                                                   const int* __restrict__ perm, const float2* __restrict__ linv,
+                                                   const float2* __restrict__ uinv, __half* __restrict__ Uop,
+                                                   __half* __restrict__ Lop, float* __restrict__ inv_t,
+                                                   float* __restrict__ inv_s)
 {
-    const int k1 = k0 + nb, m = n - k1;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (blockIdx.y == 0) {
-        const int i = blockIdx.x * 8 + warp;
-        if (i >= m) return;
-        const float2* row = A + (size_t)(k1 + i) * lda + k0;
-        const float2 a = 2 * lane < nb ? row[2 * lane] : make_float2(0.f, 0.f);
-        const float2 b = 2 * lane + 1 < nb ? row[2 * lane + 1] : make_float2(0.f, 0.f);
-        float mx = fmaxf(fmaxf(fabsf(a.x), fabsf(a.y)), fmaxf(fabsf(b.x), fabsf(b.y)));
-        for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-        const float2 sc = col_max_scale(mx);
-        if (lane == 0) inv_s[i] = sc.y;
-        uint2 h, l;
-        split2(sc.x * a.x, sc.x * a.y, h.x, l.x);
-        split2(sc.x * b.x, sc.x * b.y, h.y, l.y);
-        reinterpret_cast<uint2*>(Lop + (size_t)i * lutc::KH)[lane] = h;
-        reinterpret_cast<uint2*>(Lop + ((size_t)n + i) * lutc::KH)[lane] = l;
-        return;
-    }
-    __shared__ float2 T[NB][33];
-    __shared__ float ts[32];
-    const int j0 = blockIdx.x * 32;
-    if (j0 >= m) return;  // uniform over the CTA
-    for (int q = threadIdx.x; q < NB * 32; q += blockDim.x) {
-        const int k = q >> 5, c = q & 31;
-        T[k][c] = (k < nb && j0 + c < m) ? A[(size_t)(k0 + k) * lda + k1 + j0 + c] : make_float2(0.f, 0.f);
+    extern __shared__ float2 s_lu[];
+    float2* X = s_lu;           // [NB][LDS] the inverse
+    float2* Y = X + NB * LDS;   // [NB][LDS] the chunk, then the product
+    __shared__ float sc[NB];    // scale of each product column (U12) or row (L21)
+    const int mode = blockIdx.y;
+    const int k1 = k0 + nb, tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int e0 = k1 + blockIdx.x * NB;  // first column (U12) or row (L21) of the chunk
+    const int ne = min(NB, n - e0);
+    const float2* iv = (mode == 0 ? linv : uinv) + (size_t)(k0 / NB) * NB * NB;
+    for (int q = tid; q < NB * NB; q += blockDim.x) {
+        const int i = q / NB, j = q % NB;
+        X[i * LDS + j] = iv[q];
+        float2 v = make_float2(0.f, 0.f);
+        if (mode == 0) {
+            if (i < nb && j < ne) v = A[(size_t)perm[k0 + i] * lda + e0 + j];
+        } else {
+            if (i < ne && j < nb) v = A[(size_t)(e0 + i) * lda + k0 + j];
+        }
+        Y[i * LDS + j] = v;
     }
     __syncthreads();
-    for (int c = warp * 4; c < warp * 4 + 4; ++c) {
-        const float2 a = T[lane][c], b = T[lane + 32][c];
+    const int tx = tid & 15, ty = tid >> 4;
+    float2 acc[4][4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) acc[a][b] = make_float2(0.f, 0.f);
+    for (int k = 0; k < NB; ++k) {
+        float2 l[4], r[4];
+#pragma unroll
+        for (int a = 0; a < 4; ++a) l[a] = mode == 0 ? X[(ty + 16 * a) * LDS + k] : Y[(ty + 16 * a) * LDS + k];
+#pragma unroll
+        for (int b = 0; b < 4; ++b) r[b] = mode == 0 ? Y[k * LDS + tx + 16 * b] : X[k * LDS + tx + 16 * b];
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+            for (int b = 0; b < 4; ++b) acc[a][b] = cfma(l[a], r[b], acc[a][b]);
+    }
+    __syncthreads();  // Y is overwritten by the product
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            const int i = ty + 16 * a, j = tx + 16 * b;
+            // entries past the chunk or the block are zero products
+            Y[i * LDS + j] = acc[a][b];
+            if (mode == 0) {
+                if (i < nb && j < ne) A[(size_t)(k0 + i) * lda + e0 + j] = acc[a][b];
+            } else {
+                if (i < ne && j < nb) A[(size_t)(e0 + i) * lda + k0 + j] = acc[a][b];
+            }
+        }
+    __syncthreads();
+    // scales: per column of U12 (mode 0) or row of L21 (mode 1), 8 per warp
+    for (int c = warp * 8; c < warp * 8 + 8; ++c) {
+        const float2 a = mode == 0 ? Y[lane * LDS + c] : Y[c * LDS + lane];
+        const float2 b = mode == 0 ? Y[(lane + 32) * LDS + c] : Y[c * LDS + lane + 32];
         float mx = fmaxf(fmaxf(fabsf(a.x), fabsf(a.y)), fmaxf(fabsf(b.x), fabsf(b.y)));
         for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
         if (lane == 0) {
-            const float2 sc = col_max_scale(mx);
-            ts[c] = sc.x;
-            if (j0 + c < m) inv_t[j0 + c] = sc.y;
+            const float2 s2 = col_max_scale(mx);
+            sc[c] = s2.x;
+            if (c < ne) (mode == 0 ? inv_t : inv_s)[e0 - k1 + c] = s2.y;
         }
     }
     __syncthreads();
-    // item (column c, part e, 16-byte chunk ch of the 256-byte row): 4 k values
-    for (int q = threadIdx.x; q < 32 * 2 * 16; q += blockDim.x) {
-        const int c = q >> 5, e = (q >> 4) & 1, ch = q & 15, j = j0 + c;
-        if (j >= m) continue;
-        const float t = ts[c];
-        uint4 h, l;
-        uint32_t* hp = &h.x;
-        uint32_t* lp = &l.x;
+    if (mode == 0) {
+        // item (column c, part e, 16-byte piece ch of the 256-byte row): 4 k values
+        for (int q = tid; q < NB * 2 * 16; q += blockDim.x) {
+            const int c = q >> 5, e = (q >> 4) & 1, ch = q & 15;
+            if (c >= ne) continue;
+            const float t = sc[c];
+            uint4 h, lo;
+            uint32_t* hp = &h.x;
+            uint32_t* lp = &lo.x;
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            const float2 v = T[4 * ch + u][c];
-            if (e == 0)
-                split2(t * v.x, -(t * v.y), hp[u], lp[u]);
-            else
-                split2(t * v.y, t * v.x, hp[u], lp[u]);
+            for (int u = 0; u < 4; ++u) {
+                const float2 v = Y[(4 * ch + u) * LDS + c];
+                if (e == 0)
+                    split2(t * v.x, -(t * v.y), hp[u], lp[u]);
+                else
+                    split2(t * v.y, t * v.x, hp[u], lp[u]);
+            }
+            const size_t r = (size_t)(2 * (e0 - k1 + c) + e);
+            reinterpret_cast<uint4*>(Uop + r * lutc::KH)[ch] = h;
+            reinterpret_cast<uint4*>(Uop + ((size_t)2 * n + r) * lutc::KH)[ch] = lo;
         }
-        const size_t r = (size_t)(2 * j + e);
-        reinterpret_cast<uint4*>(Uop + r * lutc::KH)[ch] = h;
-        reinterpret_cast<uint4*>(Uop + ((size_t)2 * n + r) * lutc::KH)[ch] = l;
+    } else {
+        // item (row i, 16-byte piece ch): 4 k values
+        for (int q = tid; q < NB * 16; q += blockDim.x) {
+            const int i = q >> 4, ch = q & 15;
+            if (i >= ne) continue;
+            const float s = sc[i];
+            uint4 h, lo;
+            uint32_t* hp = &h.x;
+            uint32_t* lp = &lo.x;
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const float2 v = Y[i * LDS + 4 * ch + u];
+                split2(s * v.x, s * v.y, hp[u], lp[u]);
+            }
+            const size_t r = (size_t)(e0 - k1 + i);
+            reinterpret_cast<uint4*>(Lop + r * lutc::KH)[ch] = h;
+            reinterpret_cast<uint4*>(Lop + ((size_t)n + r) * lutc::KH)[ch] = lo;
+        }
     }
 }
 
@@ -792,7 +780,7 @@ static size_t diag_smem() { return sizeof(float2) * (3 * NB * LDS + 2048); }
 static emfa_status_t lu_set_smem(Ctx* c)
 {
     EMFA_TRY(ensure_smem(c, k_lu_diag, diag_smem()));
-    EMFA_TRY(ensure_smem(c, k_lu_small, 2 * sizeof(float2) * NB * LDS));
+    EMFA_TRY(ensure_smem(c, k_lu_panels, 2 * sizeof(float2) * NB * LDS));
     return ensure_smem(c, k_lu_update_tc, lutc::SMEM);
 }
 
@@ -850,7 +838,7 @@ emfa_status_t lu_factor(Ctx* c, const void* Z, int n, LuFactor& F, cudaStream_t 
     }
     auto diag = [&](int kb, cudaStream_t s) {
         const int k0 = kb * NB, nb = std::min(NB, n - k0);
-        k_lu_diag<<<1, 256, diag_smem(), s>>>(A, n, lda, k0, nb, dptr<int>(F.perm), dptr<float2>(F.linv), dptr<float2>(F.uinv),
+        k_lu_diag<<<1, DIAG_THREADS, diag_smem(), s>>>(A, n, lda, k0, nb, dptr<int>(F.perm), dptr<float2>(F.linv), dptr<float2>(F.uinv),
                                      info);
         c->kernel_launches += 1;
     };
@@ -864,16 +852,11 @@ emfa_status_t lu_factor(Ctx* c, const void* Z, int n, LuFactor& F, cudaStream_t 
     diag(0, st);
     for (int kb = 0; kb < F.nblk; ++kb) {
         const int k0 = kb * NB, nb = std::min(NB, n - k0), rest = n - k0 - nb;
-        if (n - nb > 0) {
-            k_lu_rowperm<<<(n - nb + 31) / 32, 256, 0, st>>>(A, n, lda, k0, nb, dptr<int>(F.perm));
-            c->kernel_launches += 1;
-        }
         if (rest <= 0) continue;
         const unsigned ch = (unsigned)((rest + NB - 1) / NB);
-        k_lu_small<<<ch, 256, s2, st>>>(A, n, lda, k0, nb, dptr<float2>(F.linv), 0);
-        k_lu_small<<<ch, 256, s2, st>>>(A, n, lda, k0, nb, dptr<float2>(F.uinv), 1);
-        k_lu_pack<<<dim3((unsigned)((rest + 7) / 8), 2), 256, 0, st>>>(A, n, lda, k0, nb, Uop, Lop, inv_t, inv_s);
-        c->kernel_launches += 3;
+        k_lu_panels<<<dim3(ch, 2), 256, s2, st>>>(A, n, lda, k0, nb, dptr<int>(F.perm), dptr<float2>(F.linv),
+                                                   dptr<float2>(F.uinv), Uop, Lop, inv_t, inv_s);
+        c->kernel_launches += 1;
         if (aux.s && ch > 1) {
             // the next block's columns, then its diagonal block on the
             // high-priority stream while the other columns are updated
@@ -888,6 +871,11 @@ emfa_status_t lu_factor(Ctx* c, const void* Z, int n, LuFactor& F, cudaStream_t 
             update(k0 + nb, 0, (int)ch, st);
             diag(kb + 1, st);
         }
+    }
+    if (F.nblk > 1) {
+        k_lu_rowperm_left<<<dim3((unsigned)(F.nblk - 1) * (NB / 32), (unsigned)F.nblk), 256, 0, st>>>(
+            A, n, lda, dptr<int>(F.perm));
+        c->kernel_launches += 1;
     }
     EMFA_CUDA(c, cudaGetLastError());
     return EMFA_OK;
