@@ -64,13 +64,15 @@ __device__ __forceinline__ float2 cinv(float2 a)
 // Factorisation in registers: warp w (of 16) holds the block's rows w,
 // w + 16, w + 32, w + 48 and lane l its columns l and l + 32.  Rows never
 // move: a pivot row only leaves the active set, and its step number is its
-// position in the factor.  One column step takes two barriers: the pivot row
-// is published in shared memory, then every active row takes its multiplier
-// from the lane holding the pivot column (a shuffle) and updates its columns
-// (branch-free: an inactive row subtracts a zero multiplier); the lane
-// holding the next column offers its warp's pivot candidate (largest |.|^2,
-// lowest row on ties), and every warp reduces the 16 candidates with
-// shuffles.
+// position in the factor.  One column step takes two barriers:
+//   1. the pivot row's warp publishes the row (its entries up to the pivot
+//      column as zeros) and the pivot's reciprocal in shared memory
+//   2. every active row takes its multiplier from the lane holding the pivot
+//      column (a shuffle) and updates both columns of each lane without a
+//      branch (an inactive row subtracts a zero multiplier); the lane holding
+//      the next column offers its warp's pivot candidate as a 64-bit key
+//      (|.|^2 bits, then the inverted row: lowest row on ties) to a shared
+//      atomicMax
 // Inverses: the 8 x 8 diagonal blocks of L and U by substitution (a thread
 // per column), then three merge levels of the 2 x 2 block inverse,
 //   [L11 0; L21 L22]^-1 = [X11 0; -X22 L21 X11  X22],
@@ -89,9 +91,9 @@ __global__ void __launch_bounds__(DIAG_THREADS) k_lu_diag(float2* __restrict__ A
     float2* WL = D + NB * LDS;      // [NB][LDS] L^-1
     float2* WU = WL + NB * LDS;     // [NB][LDS] U^-1
     float2* TM = WU + NB * LDS;     // [2048] products of a merge level
-    __shared__ float2 urow[NB];     // the step's pivot row
-    __shared__ float cval[DW];      // each warp's pivot candidate
-    __shared__ int crow[DW];
+    __shared__ float2 urow[NB];     // the step's pivot row, zero up to the pivot column
+    __shared__ float2 sipv;         // 1 / pivot
+    __shared__ unsigned long long skey[2];  // pivot candidates of the step, by parity
     __shared__ int pos[NB];         // factor position of each row
     __shared__ int ord[NB];         // row at each factor position
     __shared__ float2 invd[NB];
@@ -113,90 +115,72 @@ __global__ void __launch_bounds__(DIAG_THREADS) k_lu_diag(float2* __restrict__ A
         WU[q] = make_float2(0.f, 0.f);
     }
     if (tid < NB) pos[tid] = tid;  // rows past nb keep their own place
-    // the candidate of this warp's rows in column j (lane j % 32 holds it)
+    if (tid == 0) skey[0] = skey[1] = 0ull;
+    // this warp's candidate in column j (run by the lane holding column j)
     auto offer = [&](int j) {
         const int h = j >> 5;
-        float b = -1.f;
-        int br = NB;
+        unsigned long long key = 0ull;
 #pragma unroll
         for (int k = 0; k < DR; ++k)
             if (act >> k & 1) {
                 const float2 v = h ? d[k][1] : d[k][0];
-                const float m2 = v.x * v.x + v.y * v.y;
-                if (br == NB || m2 > b) {  // the first active row is taken even if NaN
-                    b = m2;
-                    br = w + DW * k;
-                }
+                const unsigned long long kk = (unsigned long long)__float_as_uint(v.x * v.x + v.y * v.y) << 32 |
+                                              (unsigned)(NB - 1 - (w + DW * k));
+                key = kk > key ? kk : key;
             }
-        cval[w] = b;
-        crow[w] = br;
+        if (key) atomicMax(&skey[j & 1], key);
     };
+    __syncthreads();
     if (l == 0) offer(0);
     __syncthreads();
     for (int j = 0; j < nb; ++j) {
-        // the pivot row p: each warp reduces the candidates alike; lane 0's
-        // result is taken by all lanes
-        float best = l < DW ? cval[l] : -1.f;
-        int p = l < DW ? crow[l] : NB;
-#pragma unroll
-        for (int o = DW / 2; o > 0; o >>= 1) {
-            const float ob = __shfl_xor_sync(0xffffffffu, best, o);
-            const int op = __shfl_xor_sync(0xffffffffu, p, o);
-            if (op < NB && (p == NB || ob > best || (ob == best && op < p))) {
-                best = ob;
-                p = op;
-            }
-        }
-        p = __shfl_sync(0xffffffffu, p, 0);
+        const int hj = j >> 5, lj = j & 31;
+        // a key is nonzero for any active row: the low word is NB - 1 - row
+        const int p = NB - 1 - (int)(skey[j & 1] & 0xffffffffull);
         const int kp = p / DW;
         if (p % DW == w) {
 #pragma unroll
             for (int k = 0; k < DR; ++k)
                 if (k == kp) {
-                    urow[l] = d[k][0];
-                    urow[l + 32] = d[k][1];
+                    urow[l] = l > j ? d[k][0] : make_float2(0.f, 0.f);
+                    urow[l + 32] = l + 32 > j ? d[k][1] : make_float2(0.f, 0.f);
+                    if (l == lj) {
+                        float2 pv = hj ? d[k][1] : d[k][0];
+                        if (pv.x == 0.f && pv.y == 0.f) {
+                            atomicCAS(info, 0, k0 + j + 1);
+                            pv = make_float2(1e-30f, 0.f);
+                            if (hj)
+                                d[k][1] = pv;
+                            else
+                                d[k][0] = pv;
+                        }
+                        sipv = cinv(pv);
+                    }
                 }
             act &= ~(1u << kp);
         }
         if (tid == 0) {
             ord[j] = p;
             pos[p] = j;
+            skey[(j + 1) & 1] = 0ull;  // last read in step j - 1
         }
         __syncthreads();
-        float2 pv = urow[j];
-        if (pv.x == 0.f && pv.y == 0.f) {
-            if (tid == 0) atomicCAS(info, 0, k0 + j + 1);
-            pv = make_float2(1e-30f, 0.f);
-        }
-        const float2 ipv = cinv(pv);
-        const int hj = j >> 5, lj = j & 31;
-        const float2 u0 = urow[l], u1 = urow[l + 32];
-        const bool up0 = l > j, up1 = l + 32 > j;
+        const float2 ipv = sipv, u0 = urow[l], u1 = urow[l + 32];
 #pragma unroll
         for (int k = 0; k < DR; ++k) {
-            const bool a = act >> k & 1;
             const float2 own = hj ? d[k][1] : d[k][0];
             float2 lm;
             lm.x = __shfl_sync(0xffffffffu, own.x, lj);
             lm.y = __shfl_sync(0xffffffffu, own.y, lj);
-            lm = cm(lm, ipv);
-            if (!a) lm = make_float2(0.f, 0.f);
-            const float2 n0 = make_float2(d[k][0].x - (lm.x * u0.x - lm.y * u0.y), d[k][0].y - (lm.x * u0.y + lm.y * u0.x));
-            const float2 n1 = make_float2(d[k][1].x - (lm.x * u1.x - lm.y * u1.y), d[k][1].y - (lm.x * u1.y + lm.y * u1.x));
-            const bool st = a && l == lj;  // this lane keeps the multiplier
-            d[k][0] = (st && !hj) ? lm : up0 ? n0 : d[k][0];
-            d[k][1] = (st && hj) ? lm : up1 ? n1 : d[k][1];
-        }
-        // the pivot row keeps its value; a replaced zero pivot is stored
-        if (p % DW == w && l == lj) {
-#pragma unroll
-            for (int k = 0; k < DR; ++k)
-                if (k == kp) {
-                    if (hj)
-                        d[k][1] = pv;
-                    else
-                        d[k][0] = pv;
-                }
+            lm = (act >> k & 1) ? cm(lm, ipv) : make_float2(0.f, 0.f);
+            d[k][0] = make_float2(d[k][0].x - (lm.x * u0.x - lm.y * u0.y), d[k][0].y - (lm.x * u0.y + lm.y * u0.x));
+            d[k][1] = make_float2(d[k][1].x - (lm.x * u1.x - lm.y * u1.y), d[k][1].y - (lm.x * u1.y + lm.y * u1.x));
+            if (l == lj && (act >> k & 1)) {
+                if (hj)
+                    d[k][1] = lm;
+                else
+                    d[k][0] = lm;
+            }
         }
         if (j + 1 < nb && l == ((j + 1) & 31)) offer(j + 1);
         __syncthreads();
