@@ -274,8 +274,12 @@ extern "C" emfa_status_t emfa_serve(int device, const emfa_request_t* reqs, int 
         E.arr[i] = E.o.realtime ? reqs[i].arrival_s : 0.0;
         E.order.push_back(i);
     }
-    std::stable_sort(E.order.begin(), E.order.end(),
-                     [&](int a, int b) { return E.arrival(a) < E.arrival(b); });
+    // by arrival; requests that arrive together (a whole batch) largest
+    // first, so no large problem starts last and runs alone
+    std::stable_sort(E.order.begin(), E.order.end(), [&](int a, int b) {
+        if (E.arrival(a) != E.arrival(b)) return E.arrival(a) < E.arrival(b);
+        return E.est[a] > E.est[b];
+    });
     // lanes free and reallocate per problem: keep freed memory in the pool
     // (this process's pool: the threshold and the cached memory go back at the end)
     cudaSetDevice(device);
@@ -316,7 +320,10 @@ extern "C" emfa_status_t emfa_serve_simulate(const double* arrival, const double
         E.arr[i] = E.o.realtime ? arrival[i] : 0.0;
         E.order.push_back(i);
     }
-    std::stable_sort(E.order.begin(), E.order.end(), [&](int a, int b) { return E.arr[a] < E.arr[b]; });
+    std::stable_sort(E.order.begin(), E.order.end(), [&](int a, int b) {
+        if (E.arr[a] != E.arr[b]) return E.arr[a] < E.arr[b];
+        return E.est[a] > E.est[b];
+    });
     std::vector<double> free_at(E.o.lanes, 0.0);
     std::vector<std::pair<double, int>> run;  // (end time, request)
     double t = 0.0;

@@ -24,11 +24,22 @@ def test_admitter_fifo_when_everything_fits(emfa_lib):
 
 def test_admitter_budget_lets_small_requests_pass_a_large_one(emfa_lib):
     from emfa_gb300 import api
-    # request 1 needs 8 GB with 6 GB free: the later 1 GB requests go first
+    # all arrive together: the largest (request 1, 8 GB) starts first; request
+    # 0 needs 4 GB with 2 GB free, so the 1 GB requests go ahead of it
     start, _ = api.serve_simulate([0.0, 0.0, 0.0, 0.0], [5, 5, 1, 1], [4 * GB, 8 * GB, GB, GB], lanes=3,
                                   hbm_budget=10 * GB, realtime=False)
-    assert start[0] == 0.0 and start[2] == 0.0 and start[3] == 0.0
-    assert start[1] == 5.0  # admitted once request 0 gave its 4 GB back
+    assert start[1] == 0.0 and start[2] == 0.0 and start[3] == 0.0
+    assert start[0] == 5.0  # admitted once request 1 gave its 8 GB back
+
+
+def test_admitter_takes_a_batch_largest_first(emfa_lib):
+    from emfa_gb300 import api
+    # one lane, everything present at once: by size, largest first; with
+    # arrivals apart, by arrival
+    start, _ = api.serve_simulate([0.0, 0.0, 0.0], [1, 2, 3], [GB, 3 * GB, 2 * GB], lanes=1, realtime=False)
+    assert np.allclose(start, [5.0, 0.0, 2.0])
+    start, _ = api.serve_simulate([0.0, 0.1, 0.2], [1, 2, 3], [GB, 3 * GB, 2 * GB], lanes=1, realtime=True)
+    assert np.allclose(start, [0.0, 1.0, 3.0])
 
 
 def test_admitter_oversized_request_runs_alone(emfa_lib):
