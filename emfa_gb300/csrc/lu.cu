@@ -61,26 +61,85 @@ __device__ __forceinline__ float2 cinv(float2 a)
 // factors.  perm[k0 + i] = the original row now at k0 + i (rows of earlier
 // blocks never move into this one, so original = k0 + local index).
 //
-// Factorisation in registers: warp w (of 16) holds the block's rows w,
-// w + 16, w + 32, w + 48 and lane l its columns l and l + 32.  Rows never
-// move: a pivot row only leaves the active set, and its step number is its
-// position in the factor.  One column step takes two barriers:
-//   1. the pivot row's warp publishes the row (its entries up to the pivot
-//      column as zeros) and the pivot's reciprocal in shared memory
-//   2. every active row takes its multiplier from the lane holding the pivot
-//      column (a shuffle) and updates both columns of each lane without a
-//      branch (an inactive row subtracts a zero multiplier); the lane holding
-//      the next column offers its warp's pivot candidate as a 64-bit key
-//      (|.|^2 bits, then the inverted row: lowest row on ties) to a shared
-//      atomicMax
+// Factorisation by 16-column panels.  Rows never move: a pivot row only
+// leaves the active set, and its step number is its position in the factor
+// (ord, pos).  Per panel:
+//   1. warp 0 holds the panel (lane l: rows l and l + 32, 16 columns) in
+//      registers and runs its 16 column steps with warp barriers only: the
+//      pivot is the largest |.|^2 among active rows (a 64-bit key, |.|^2 bits
+//      then the inverted row, so the lowest row wins ties, reduced by
+//      shuffles); the pivot lane publishes its row, every lane scales and
+//      updates its own rows
+//   2. all warps: the panel's pivot rows on the columns to its right
+//      (unit-lower triangular solve, a thread per column), then the rank-16
+//      update of the active rows there
 // Inverses: the 8 x 8 diagonal blocks of L and U by substitution (a thread
 // per column), then three merge levels of the 2 x 2 block inverse,
 //   [L11 0; L21 L22]^-1 = [X11 0; -X22 L21 X11  X22],
 //   [U11 U12; 0 U22]^-1 = [Y11 -Y11 U12 Y22; 0 Y22],
 // each two rounds of small products over all block pairs at once.
 constexpr int DIAG_THREADS = 512;
-constexpr int DW = DIAG_THREADS / 32;  // warps; rows per warp NB / DW
-constexpr int DR = NB / DW;
+constexpr int PW = 16;  // panel width
+
+// One merge level of the blocked inverses: for every pair of b-blocks on the
+// diagonal, T = L21 X11 and T = Y11 U12, then X21 = -X22 T and Y12 = -T Y22.
+// A thread takes NI items (an entry of T, then of X21 or Y12) and runs their
+// b-long sums side by side.
+template <int b>
+__device__ __forceinline__ void diag_merge(const float2* __restrict__ D, float2* __restrict__ WL,
+                                           float2* __restrict__ WU, float2* __restrict__ TM)
+{
+    constexpr int pairs = (NB / 2) / b, per = pairs * b * b, NI = (2 * per + DIAG_THREADS - 1) / DIAG_THREADS;
+    const int tid = threadIdx.x;
+    int mat[NI], pr[NI], r[NI], c[NI];
+#pragma unroll
+    for (int it = 0; it < NI; ++it) {
+        const int q = tid + it * DIAG_THREADS;  // 2 per is a multiple of the block: every q is an item
+        const int rem = q % per;
+        mat[it] = q / per;
+        pr[it] = rem / (b * b);
+        r[it] = (rem / b) % b;
+        c[it] = rem % b;
+    }
+    float2 s[NI];
+#pragma unroll
+    for (int it = 0; it < NI; ++it) s[it] = make_float2(0.f, 0.f);
+#pragma unroll 4
+    for (int k = 0; k < b; ++k)
+#pragma unroll
+        for (int it = 0; it < NI; ++it) {
+            const int i0 = pr[it] * 2 * b;
+            if (mat[it] == 0)
+                s[it] = cfma(D[(i0 + b + r[it]) * LDS + i0 + k], WL[(i0 + k) * LDS + i0 + c[it]], s[it]);
+            else
+                s[it] = cfma(WU[(i0 + r[it]) * LDS + i0 + k], D[(i0 + k) * LDS + i0 + b + c[it]], s[it]);
+        }
+#pragma unroll
+    for (int it = 0; it < NI; ++it) TM[tid + it * DIAG_THREADS] = s[it];
+    __syncthreads();
+#pragma unroll
+    for (int it = 0; it < NI; ++it) s[it] = make_float2(0.f, 0.f);
+#pragma unroll 4
+    for (int k = 0; k < b; ++k)
+#pragma unroll
+        for (int it = 0; it < NI; ++it) {
+            const int i0 = pr[it] * 2 * b;
+            const float2* T = TM + mat[it] * per + pr[it] * b * b;
+            if (mat[it] == 0)
+                s[it] = cfma(WL[(i0 + b + r[it]) * LDS + i0 + b + k], T[k * b + c[it]], s[it]);
+            else
+                s[it] = cfma(T[r[it] * b + k], WU[(i0 + b + k) * LDS + i0 + b + c[it]], s[it]);
+        }
+#pragma unroll
+    for (int it = 0; it < NI; ++it) {
+        const int i0 = pr[it] * 2 * b;
+        if (mat[it] == 0)
+            WL[(i0 + b + r[it]) * LDS + i0 + c[it]] = make_float2(-s[it].x, -s[it].y);
+        else
+            WU[(i0 + r[it]) * LDS + i0 + b + c[it]] = make_float2(-s[it].x, -s[it].y);
+    }
+    __syncthreads();
+}
 
 __global__ void __launch_bounds__(DIAG_THREADS) k_lu_diag(float2* __restrict__ A, int n, int lda, int k0, int nb,
                                                           int* __restrict__ perm, float2* __restrict__ linv,
@@ -88,117 +147,154 @@ __global__ void __launch_bounds__(DIAG_THREADS) k_lu_diag(float2* __restrict__ A
 {
     extern __shared__ float2 s_lu[];
     float2* D = s_lu;               // [NB][LDS] the factors, in factor order
-    float2* WL = D + NB * LDS;      // [NB][LDS] L^-1
+    float2* WL = D + NB * LDS;      // [NB][LDS] the block by original row while it is factored, then L^-1
     float2* WU = WL + NB * LDS;     // [NB][LDS] U^-1
     float2* TM = WU + NB * LDS;     // [2048] products of a merge level
-    __shared__ float2 urow[NB];     // the step's pivot row, zero up to the pivot column
-    __shared__ float2 sipv;         // 1 / pivot
-    __shared__ unsigned long long skey[2];  // pivot candidates of the step, by parity
-    __shared__ int pos[NB];         // factor position of each row
+    __shared__ float2 prow[PW];     // the step's pivot row within the panel
+    __shared__ int pos[NB];         // factor position of each row (NB + row while active)
     __shared__ int ord[NB];         // row at each factor position
     __shared__ float2 invd[NB];
     const int tid = threadIdx.x, w = tid >> 5, l = tid & 31;
-    float2 d[DR][2];
-    unsigned act = 0;  // bit k: row w + DW k not yet a pivot row
+    float2* W = WL;
+    for (int q = tid; q < NB * NB; q += blockDim.x) {
+        const int i = q / NB, j = q % NB;
+        W[i * LDS + j] = (i < nb && j < nb) ? A[(size_t)(k0 + i) * lda + k0 + j] : make_float2(0.f, 0.f);
+    }
+    if (tid < NB) pos[tid] = NB + tid;
+    __syncthreads();
+    unsigned act = (l < nb ? 1u : 0u) | (l + 32 < nb ? 2u : 0u);  // warp 0: rows l, l + 32 still active
+    for (int c0 = 0; c0 < nb; c0 += PW) {
+        if (w == 0) {
+            float2 x[2][PW];
 #pragma unroll
-    for (int k = 0; k < DR; ++k) {
-        const int r = w + DW * k;
-        if (r < nb) act |= 1u << k;
+            for (int r = 0; r < 2; ++r)
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const int c = l + 32 * h;
-            d[k][h] = (r < nb && c < nb) ? A[(size_t)(k0 + r) * lda + k0 + c] : make_float2(0.f, 0.f);
+                for (int c = 0; c < PW; ++c) x[r][c] = W[(l + 32 * r) * LDS + c0 + c];
+#pragma unroll
+            for (int jj = 0; jj < PW; ++jj) {
+                const int j = c0 + jj;
+                if (j < nb) {  // uniform
+                    unsigned long long key = 0ull;
+#pragma unroll
+                    for (int r = 0; r < 2; ++r)
+                        if (act >> r & 1) {
+                            const float m2 = x[r][jj].x * x[r][jj].x + x[r][jj].y * x[r][jj].y;
+                            const unsigned long long kk =
+                                (unsigned long long)__float_as_uint(m2) << 32 | (unsigned)(NB - 1 - (l + 32 * r));
+                            key = kk > key ? kk : key;
+                        }
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) {
+                        const unsigned long long ok = __shfl_xor_sync(0xffffffffu, key, o);
+                        key = ok > key ? ok : key;
+                    }
+                    // a key is nonzero for any active row but row 63 with a zero
+                    // entry, which the empty key names as well
+                    const int p = NB - 1 - (int)(key & 0xffffffffull);
+                    const int pl = p & 31, pr = p >> 5;
+                    if (l == pl) {
+#pragma unroll
+                        for (int c = jj; c < PW; ++c) prow[c] = pr ? x[1][c] : x[0][c];
+                    }
+                    __syncwarp();
+                    float2 pv = prow[jj];
+                    if (pv.x == 0.f && pv.y == 0.f) {
+                        if (l == 0) atomicCAS(info, 0, k0 + j + 1);
+                        pv = make_float2(1e-30f, 0.f);
+                        if (l == pl) {
+                            if (pr)
+                                x[1][jj] = pv;
+                            else
+                                x[0][jj] = pv;
+                        }
+                    }
+                    if (l == pl) act &= ~(1u << pr);
+                    const float2 ipv = cinv(pv);
+#pragma unroll
+                    for (int r = 0; r < 2; ++r)
+                        if (act >> r & 1) {
+                            const float2 lm = cm(x[r][jj], ipv);
+                            x[r][jj] = lm;
+#pragma unroll
+                            for (int c = jj + 1; c < PW; ++c) {
+                                const float2 u = prow[c];
+                                x[r][c] = make_float2(x[r][c].x - (lm.x * u.x - lm.y * u.y),
+                                                      x[r][c].y - (lm.x * u.y + lm.y * u.x));
+                            }
+                        }
+                    if (l == 0) {
+                        ord[j] = p;
+                        pos[p] = j;
+                    }
+                    __syncwarp();
+                }
+            }
+#pragma unroll
+            for (int r = 0; r < 2; ++r)
+#pragma unroll
+                for (int c = 0; c < PW; ++c) W[(l + 32 * r) * LDS + c0 + c] = x[r][c];
+        }
+        __syncthreads();
+        const int c1 = c0 + PW, pe = min(PW, nb - c0);  // columns right of the panel; its pivots
+        if (c1 < nb) {
+            // the panel's pivot rows on the columns right of it: forward
+            // substitution with the panel's unit-lower part, four lanes per
+            // column (lane sub keeps the solved entries k = sub mod 4)
+            if (w < (4 * (nb - c1) + 31) / 32) {  // whole warps
+                const int sub = tid & 3, c = c1 + (tid >> 2), cc = min(c, NB - 1);
+                float2 u[PW / 4];
+#pragma unroll
+                for (int t = 0; t < PW / 4; ++t) u[t] = make_float2(0.f, 0.f);
+#pragma unroll
+                for (int i = 0; i < PW; ++i) {
+                    if (i < pe) {  // uniform
+                        const int ri = ord[c0 + i];
+                        float2 part = make_float2(0.f, 0.f);
+#pragma unroll
+                        for (int t = 0; t < PW / 4; ++t)
+                            if (sub + 4 * t < i) part = cfma(W[ri * LDS + c0 + sub + 4 * t], u[t], part);
+                        part.x += __shfl_xor_sync(0xffffffffu, part.x, 1);
+                        part.y += __shfl_xor_sync(0xffffffffu, part.y, 1);
+                        part.x += __shfl_xor_sync(0xffffffffu, part.x, 2);
+                        part.y += __shfl_xor_sync(0xffffffffu, part.y, 2);
+                        const float2 a = W[ri * LDS + cc];
+                        const float2 v = make_float2(a.x - part.x, a.y - part.y);
+                        if ((i & 3) == sub) u[i >> 2] = v;
+                        if (sub == 0 && c < nb) W[ri * LDS + c] = v;
+                    }
+                }
+            }
+            __syncthreads();
+            // rank-pe update of the active rows right of the panel
+            const int nc = nb - c1;
+            for (int q = tid; q < NB * nc; q += blockDim.x) {
+                const int r = q / nc, c = c1 + q % nc;
+                if (r >= nb || pos[r] < NB) continue;
+                float2 s = W[r * LDS + c];
+                for (int k = 0; k < pe; ++k) {
+                    const float2 lk = W[r * LDS + c0 + k], uk = W[ord[c0 + k] * LDS + c];
+                    s = make_float2(s.x - (lk.x * uk.x - lk.y * uk.y), s.y - (lk.x * uk.y + lk.y * uk.x));
+                }
+                W[r * LDS + c] = s;
+            }
+            __syncthreads();
         }
     }
+    // the factors in factor order: shared memory (rows and columns past nb
+    // are zero) and A
+    for (int q = tid; q < NB * NB; q += blockDim.x) {
+        const int r = q / NB, c = q % NB;
+        const int i = r < nb ? pos[r] : r;
+        const float2 v = W[r * LDS + c];
+        D[i * LDS + c] = v;
+        if (r < nb && c < nb) A[(size_t)(k0 + i) * lda + k0 + c] = v;
+    }
+    if (tid < nb) perm[k0 + tid] = k0 + ord[tid];
+    __syncthreads();
     for (int q = tid; q < NB * LDS; q += blockDim.x) {
         WL[q] = make_float2(0.f, 0.f);
         WU[q] = make_float2(0.f, 0.f);
     }
-    if (tid < NB) pos[tid] = tid;  // rows past nb keep their own place
-    if (tid == 0) skey[0] = skey[1] = 0ull;
-    // this warp's candidate in column j (run by the lane holding column j)
-    auto offer = [&](int j) {
-        const int h = j >> 5;
-        unsigned long long key = 0ull;
-#pragma unroll
-        for (int k = 0; k < DR; ++k)
-            if (act >> k & 1) {
-                const float2 v = h ? d[k][1] : d[k][0];
-                const unsigned long long kk = (unsigned long long)__float_as_uint(v.x * v.x + v.y * v.y) << 32 |
-                                              (unsigned)(NB - 1 - (w + DW * k));
-                key = kk > key ? kk : key;
-            }
-        if (key) atomicMax(&skey[j & 1], key);
-    };
-    __syncthreads();
-    if (l == 0) offer(0);
-    __syncthreads();
-    for (int j = 0; j < nb; ++j) {
-        const int hj = j >> 5, lj = j & 31;
-        // a key is nonzero for any active row: the low word is NB - 1 - row
-        const int p = NB - 1 - (int)(skey[j & 1] & 0xffffffffull);
-        const int kp = p / DW;
-        if (p % DW == w) {
-#pragma unroll
-            for (int k = 0; k < DR; ++k)
-                if (k == kp) {
-                    urow[l] = l > j ? d[k][0] : make_float2(0.f, 0.f);
-                    urow[l + 32] = l + 32 > j ? d[k][1] : make_float2(0.f, 0.f);
-                    if (l == lj) {
-                        float2 pv = hj ? d[k][1] : d[k][0];
-                        if (pv.x == 0.f && pv.y == 0.f) {
-                            atomicCAS(info, 0, k0 + j + 1);
-                            pv = make_float2(1e-30f, 0.f);
-                            if (hj)
-                                d[k][1] = pv;
-                            else
-                                d[k][0] = pv;
-                        }
-                        sipv = cinv(pv);
-                    }
-                }
-            act &= ~(1u << kp);
-        }
-        if (tid == 0) {
-            ord[j] = p;
-            pos[p] = j;
-            skey[(j + 1) & 1] = 0ull;  // last read in step j - 1
-        }
-        __syncthreads();
-        const float2 ipv = sipv, u0 = urow[l], u1 = urow[l + 32];
-#pragma unroll
-        for (int k = 0; k < DR; ++k) {
-            const float2 own = hj ? d[k][1] : d[k][0];
-            float2 lm;
-            lm.x = __shfl_sync(0xffffffffu, own.x, lj);
-            lm.y = __shfl_sync(0xffffffffu, own.y, lj);
-            lm = (act >> k & 1) ? cm(lm, ipv) : make_float2(0.f, 0.f);
-            d[k][0] = make_float2(d[k][0].x - (lm.x * u0.x - lm.y * u0.y), d[k][0].y - (lm.x * u0.y + lm.y * u0.x));
-            d[k][1] = make_float2(d[k][1].x - (lm.x * u1.x - lm.y * u1.y), d[k][1].y - (lm.x * u1.y + lm.y * u1.x));
-            if (l == lj && (act >> k & 1)) {
-                if (hj)
-                    d[k][1] = lm;
-                else
-                    d[k][0] = lm;
-            }
-        }
-        if (j + 1 < nb && l == ((j + 1) & 31)) offer(j + 1);
-        __syncthreads();
-    }
-    // the factors in factor order: shared memory (rows and columns past nb
-    // are zero) and A
-#pragma unroll
-    for (int k = 0; k < DR; ++k) {
-        const int r = w + DW * k;
-        const int i = pos[r];
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const int c = l + 32 * h;
-            D[i * LDS + c] = d[k][h];
-            if (r < nb && c < nb) A[(size_t)(k0 + i) * lda + k0 + c] = d[k][h];
-        }
-    }
-    if (tid < nb) perm[k0 + tid] = k0 + ord[tid];
     __syncthreads();
     if (tid < NB) invd[tid] = tid < nb ? cinv(D[tid * LDS + tid]) : make_float2(1.f, 0.f);
     if (tid >= nb && tid < NB) D[tid * LDS + tid] = make_float2(1.f, 0.f);  // identity past the block
@@ -233,36 +329,9 @@ __global__ void __launch_bounds__(DIAG_THREADS) k_lu_diag(float2* __restrict__ A
         }
     }
     __syncthreads();
-    for (int b = 8; b < NB; b *= 2) {
-        const int pairs = (NB / 2) / b, per = pairs * b * b;
-        // T = L21 X11 (L) and T = Y11 U12 (U) for every pair of b-blocks
-        for (int q = tid; q < 2 * per; q += blockDim.x) {
-            const int mat = q / per, rem = q % per, pr = rem / (b * b), r = (rem / b) % b, c = rem % b;
-            const int i0 = pr * 2 * b;
-            float2 s = make_float2(0.f, 0.f);
-            if (mat == 0)
-                for (int k = 0; k < b; ++k) s = cfma(D[(i0 + b + r) * LDS + i0 + k], WL[(i0 + k) * LDS + i0 + c], s);
-            else
-                for (int k = 0; k < b; ++k) s = cfma(WU[(i0 + r) * LDS + i0 + k], D[(i0 + k) * LDS + i0 + b + c], s);
-            TM[q] = s;
-        }
-        __syncthreads();
-        // X21 = -X22 T (L) and Y12 = -T Y22 (U)
-        for (int q = tid; q < 2 * per; q += blockDim.x) {
-            const int mat = q / per, rem = q % per, pr = rem / (b * b), r = (rem / b) % b, c = rem % b;
-            const int i0 = pr * 2 * b;
-            const float2* T = TM + mat * per + pr * b * b;
-            float2 s = make_float2(0.f, 0.f);
-            if (mat == 0) {
-                for (int k = 0; k < b; ++k) s = cfma(WL[(i0 + b + r) * LDS + i0 + b + k], T[k * b + c], s);
-                WL[(i0 + b + r) * LDS + i0 + c] = make_float2(-s.x, -s.y);
-            } else {
-                for (int k = 0; k < b; ++k) s = cfma(T[r * b + k], WU[(i0 + b + k) * LDS + i0 + b + c], s);
-                WU[(i0 + r) * LDS + i0 + b + c] = make_float2(-s.x, -s.y);
-            }
-        }
-        __syncthreads();
-    }
+    diag_merge<8>(D, WL, WU, TM);
+    diag_merge<16>(D, WL, WU, TM);
+    diag_merge<32>(D, WL, WU, TM);
     const size_t kb = (size_t)(k0 / NB) * NB * NB;
     for (int q = tid; q < NB * NB; q += blockDim.x) {
         const int i = q / NB, j = q % NB;
