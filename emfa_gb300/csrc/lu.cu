@@ -386,7 +386,7 @@ __global__ void __launch_bounds__(256) k_lu_rowperm_left(float2* __restrict__ A,
 namespace lutc {
 constexpr int TM = 128;                                  // real columns of A22 per tile (MMA M): 64 complex
 constexpr int TN = 256;                                  // rows of A22 per tile (MMA N)
-constexpr int KH = 2 * NB;                               // halves per operand row
+constexpr int KH = 4 * NB;                               // halves per operand row: two blocks' panels
 constexpr int U_BYTES = TM * 128;                        // one 64-half K slice of one U plane
 constexpr int L_BYTES = TN * 128;                        // one K slice of one L plane
 constexpr int STAGE = 2 * U_BYTES + 2 * L_BYTES;         // both planes of both operands: 96 KB
@@ -426,7 +426,7 @@ __global__ void __launch_bounds__(256) k_lu_panels(float2* __restrict__ A, int n
                                                    const int* __restrict__ perm, const float2* __restrict__ linv,
                                                    const float2* __restrict__ uinv, __half* __restrict__ Uop,
                                                    __half* __restrict__ Lop, float* __restrict__ inv_t,
-                                                   float* __restrict__ inv_s)
+                                                   float* __restrict__ inv_s, int pack)
 {
     extern __shared__ float2 s_lu[];
     float2* X = s_lu;           // [NB][LDS] the inverse
@@ -480,6 +480,7 @@ __global__ void __launch_bounds__(256) k_lu_panels(float2* __restrict__ A, int n
                 if (i < ne && j < nb) A[(size_t)(e0 + i) * lda + k0 + j] = acc[a][b];
             }
         }
+    if (!pack) return;  // uniform: the pair's operands are packed by k_lu_pack2
     __syncthreads();
     // scales: per column of U12 (mode 0) or row of L21 (mode 1), 8 per warp
     for (int c = warp * 8; c < warp * 8 + 8; ++c) {
@@ -536,10 +537,94 @@ __global__ void __launch_bounds__(256) k_lu_panels(float2* __restrict__ A, int n
     }
 }
 
+// Operand planes of a pair of blocks s0 and s0 + 64 for the update of
+// [k2, n)^2, k2 = s0 + 128: U operand rows (from k2) hold U12 of both blocks
+// (rows s0 .. s0 + 127 of A), L operand rows L21 of both (columns s0 ..
+// s0 + 127), K = 128 complex, with one power-of-two scale per column / row
+// over both blocks.  blockIdx.y = 0: rows of L21, one warp per row;
+// blockIdx.y = 1: 32 columns of U12 per CTA, staged and transposed in
+// shared memory.
+__global__ void __launch_bounds__(256) k_lu_pack2(const float2* __restrict__ A, int n, int lda, int s0,
+                                                  __half* __restrict__ Uop, __half* __restrict__ Lop,
+                                                  float* __restrict__ inv_t, float* __restrict__ inv_s)
+{
+    const int k2 = s0 + 2 * NB, m = n - k2;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (blockIdx.y == 0) {
+        const int i = blockIdx.x * 8 + warp;
+        if (i >= m) return;
+        const float2* row = A + (size_t)(k2 + i) * lda + s0 + 4 * lane;
+        float2 v[4];
+        float mx = 0.f;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            v[u] = row[u];
+            mx = fmaxf(mx, fmaxf(fabsf(v[u].x), fabsf(v[u].y)));
+        }
+        for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        const float2 sc = col_max_scale(mx);
+        if (lane == 0) inv_s[i] = sc.y;
+        uint4 h, l;
+        uint32_t* hp = &h.x;
+        uint32_t* lp = &l.x;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) split2(sc.x * v[u].x, sc.x * v[u].y, hp[u], lp[u]);
+        reinterpret_cast<uint4*>(Lop + (size_t)i * lutc::KH)[lane] = h;
+        reinterpret_cast<uint4*>(Lop + ((size_t)n + i) * lutc::KH)[lane] = l;
+        return;
+    }
+    __shared__ float2 T[2 * NB][33];
+    __shared__ float ts[32];
+    const int j0 = blockIdx.x * 32;
+    if (j0 >= m) return;  // uniform over the CTA
+    for (int q = threadIdx.x; q < 2 * NB * 32; q += blockDim.x) {
+        const int k = q >> 5, c = q & 31;
+        T[k][c] = j0 + c < m ? A[(size_t)(s0 + k) * lda + k2 + j0 + c] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    for (int c = warp * 4; c < warp * 4 + 4; ++c) {
+        float mx = 0.f;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const float2 a = T[lane + 32 * u][c];
+            mx = fmaxf(mx, fmaxf(fabsf(a.x), fabsf(a.y)));
+        }
+        for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        if (lane == 0) {
+            const float2 sc = col_max_scale(mx);
+            ts[c] = sc.x;
+            if (j0 + c < m) inv_t[j0 + c] = sc.y;
+        }
+    }
+    __syncthreads();
+    // item (column c, part e, 16-byte piece ch of the 512-byte row): 4 k values
+    for (int q = threadIdx.x; q < 32 * 2 * 32; q += blockDim.x) {
+        const int c = q >> 6, e = (q >> 5) & 1, ch = q & 31, j = j0 + c;
+        if (j >= m) continue;
+        const float t = ts[c];
+        uint4 h, l;
+        uint32_t* hp = &h.x;
+        uint32_t* lp = &l.x;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const float2 v = T[4 * ch + u][c];
+            if (e == 0)
+                split2(t * v.x, -(t * v.y), hp[u], lp[u]);
+            else
+                split2(t * v.y, t * v.x, hp[u], lp[u]);
+        }
+        const size_t r = (size_t)(2 * j + e);
+        reinterpret_cast<uint4*>(Uop + r * lutc::KH)[ch] = h;
+        reinterpret_cast<uint4*>(Uop + ((size_t)2 * n + r) * lutc::KH)[ch] = l;
+    }
+}
+
 // A22 -= L21 U12 on the tile of 64 complex columns (blockIdx.x + ct0) and
-// 256 rows (blockIdx.y) of [k1, n)^2, two CTAs per SM:
-//   warp 0      TMA producer: K slice 0, then (once its MMAs are done) slice
-//               1, of Uh, Ul (128 rows) and Lh, Ll (256 rows), 128-byte swizzle
+// 256 rows (blockIdx.y) of [k1, n)^2, two CTAs per SM.  nslices K slices of
+// 64 halves: 2 for one block's panels (K = 64 complex), 4 for two blocks'.
+//   warp 0      TMA producer: each K slice, once the MMAs of the one before
+//               are done, of Uh, Ul (128 rows) and Lh, Ll (256 rows), 128-byte
+//               swizzle
 //   warp 1      allocates 256 tensor-memory columns; one lane issues
 //               tcgen05.mma M = 128, N = 256, K = 16: 12 per slice
 //   warps 2..9  epilogue.  Once the MMAs are done, the operand buffer holds
@@ -555,8 +640,8 @@ __global__ void __launch_bounds__(256) k_lu_panels(float2* __restrict__ A, int n
 // memory.
 __global__ void __launch_bounds__(lutc::THREADS, 2)
     k_lu_update_tc(const __grid_constant__ CUtensorMap tmU, const __grid_constant__ CUtensorMap tmL,
-                   const __grid_constant__ CUtensorMap tmC, int n, int k1, int ct0, const float* __restrict__ inv_t,
-                   const float* __restrict__ inv_s, int* __restrict__ err)
+                   const __grid_constant__ CUtensorMap tmC, int n, int k1, int ct0, int nslices,
+                   const float* __restrict__ inv_t, const float* __restrict__ inv_s, int* __restrict__ err)
 {
     using namespace tc;
     extern __shared__ uint8_t smem_raw[];
@@ -600,8 +685,8 @@ __global__ void __launch_bounds__(lutc::THREADS, 2)
     if (warp == 0) {
         if (lane == 0) {
             int issued = 0;
-            for (int s = 0; s < 2; ++s) {
-                if (s == 1 && !mbar_wait(empty, 0, err, 11)) break;
+            for (int s = 0; s < nslices; ++s) {
+                if (s > 0 && !mbar_wait(empty, (s - 1) & 1, err, 11)) break;
                 if (*(volatile int*)err) break;
                 mbar_expect_tx(full, lutc::STAGE);
                 tma_load_2d(sUh, &tmU, full, 64 * s, 2 * cc0);
@@ -616,7 +701,7 @@ __global__ void __launch_bounds__(lutc::THREADS, 2)
     } else if (warp == 1) {
         if (lane == 0) {
             constexpr uint32_t idesc = idesc_f16(lutc::TM, lutc::TN);
-            for (int s = 0; s < 2; ++s) {
+            for (int s = 0; s < nslices; ++s) {
                 if (!mbar_wait(full, s & 1, err, 13)) break;
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                 const uint64_t uh = sw128_desc(smem_u32(sUh)), ul = sw128_desc(smem_u32(sUl));
@@ -628,7 +713,7 @@ __global__ void __launch_bounds__(lutc::THREADS, 2)
                 for (int k = 0; k < 4; ++k) mma_f16(tmem, uh + 2 * k, ll + 2 * k, idesc, 1u);
 #pragma unroll
                 for (int k = 0; k < 4; ++k) mma_f16(tmem, ul + 2 * k, lh + 2 * k, idesc, 1u);
-                if (s == 0) mma_commit(empty);
+                if (s + 1 < nslices) mma_commit(empty);
             }
             // every MMA issued must be complete before the epilogue and before
             // tensor memory is released
@@ -802,17 +887,17 @@ static emfa_status_t ops_map(Ctx* c, CUtensorMap* m, const void* ptr, uint64_t r
     return EMFA_OK;
 }
 
-// A as a float matrix of n rows x 2n columns, rows lda complex apart; box
-// 128 floats (64 complex) x 64 rows, no swizzle; loads past the matrix read
-// zeros and stores there are clipped
-static emfa_status_t tile_map(Ctx* c, CUtensorMap* m, const void* A, int n, int lda)
+// A as a float matrix of `rows` rows x 2n columns, rows lda complex apart;
+// box 128 floats (64 complex) x 64 rows, no swizzle; loads past the matrix
+// (or past `rows`) read zeros and stores there are clipped
+static emfa_status_t tile_map(Ctx* c, CUtensorMap* m, const void* A, int n, int lda, int rows)
 {
     auto fn = tensor_map_encoder();
     if (!fn) {
         set_error(c, "cuTensorMapEncodeTiled unavailable");
         return EMFA_ERR_CUDA;
     }
-    cuuint64_t dims[2] = {2 * (cuuint64_t)n, (cuuint64_t)n};
+    cuuint64_t dims[2] = {2 * (cuuint64_t)n, (cuuint64_t)rows};
     cuuint64_t strides[1] = {(cuuint64_t)lda * sizeof(float2)};
     cuuint32_t box[2] = {128, 64};
     cuuint32_t estr[2] = {1, 1};
@@ -863,7 +948,7 @@ emfa_status_t lu_factor(Ctx* c, const void* Z, int n, LuFactor& F, cudaStream_t 
     CUtensorMap tmU, tmL, tmC;
     EMFA_TRY(ops_map(c, &tmU, Uop, (uint64_t)4 * n, lutc::TM));
     EMFA_TRY(ops_map(c, &tmL, Lop, (uint64_t)2 * n, lutc::TN));
-    EMFA_TRY(tile_map(c, &tmC, A, n, lda));
+    EMFA_TRY(tile_map(c, &tmC, A, n, lda, n));
     EMFA_CUDA(c, cudaMemcpy2DAsync(A, sizeof(float2) * (size_t)lda, Z, sizeof(float2) * (size_t)n,
                                    sizeof(float2) * (size_t)n, (size_t)n, cudaMemcpyDeviceToDevice, st));
     EMFA_CUDA(c, cudaMemsetAsync(info, 0, 2 * sizeof(int), st));
@@ -895,35 +980,75 @@ emfa_status_t lu_factor(Ctx* c, const void* Z, int n, LuFactor& F, cudaStream_t 
                                      info);
         c->kernel_launches += 1;
     };
-    // A22 -= L21 U12 on column tiles [ct0, ct0 + nct) (64 complex columns each)
-    auto update = [&](int k1, int ct0, int nct, cudaStream_t s) {
-        const unsigned rt = (unsigned)((n - k1 + lutc::TN - 1) / lutc::TN);
-        k_lu_update_tc<<<dim3((unsigned)nct, rt), lutc::THREADS, lutc::SMEM, s>>>(tmU, tmL, tmC, n, k1, ct0,
-                                                                                   inv_t, inv_s, info + 1);
+    // A22 -= L21 U12 on column tiles [ct0, ct0 + nct) (64 complex columns
+    // each) and row tiles [0, rt) of [k1, n)^2, clipped to the rows of tm
+    auto update = [&](const CUtensorMap& tm, int k1, int ct0, int nct, int rt, int nslices, cudaStream_t s) {
+        k_lu_update_tc<<<dim3((unsigned)nct, (unsigned)rt), lutc::THREADS, lutc::SMEM, s>>>(
+            tmU, tmL, tm, n, k1, ct0, nslices, inv_t, inv_s, info + 1);
         c->kernel_launches += 1;
     };
-    diag(0, st);
-    for (int kb = 0; kb < F.nblk; ++kb) {
-        const int k0 = kb * NB, nb = std::min(NB, n - k0), rest = n - k0 - nb;
-        if (rest <= 0) continue;
-        const unsigned ch = (unsigned)((rest + NB - 1) / NB);
+    auto row_tiles = [&](int k1) { return (n - k1 + lutc::TN - 1) / lutc::TN; };
+    auto panels = [&](int k0, int nb, int pack) {
+        const unsigned ch = (unsigned)((n - k0 - nb + NB - 1) / NB);
         k_lu_panels<<<dim3(ch, 2), 256, s2, st>>>(A, n, lda, k0, nb, dptr<int>(F.perm), dptr<float2>(F.linv),
-                                                   dptr<float2>(F.uinv), Uop, Lop, inv_t, inv_s);
+                                                   dptr<float2>(F.uinv), Uop, Lop, inv_t, inv_s, pack);
         c->kernel_launches += 1;
+    };
+    // the next diagonal block on the high-priority stream once st has
+    // updated its columns; st waits for it before it goes on
+    auto diag_aside = [&](int kb) -> emfa_status_t {
+        EMFA_CUDA(c, cudaEventRecord(aux.panel, st));
+        EMFA_CUDA(c, cudaStreamWaitEvent(aux.s, aux.panel, 0));
+        diag(kb, aux.s);
+        EMFA_CUDA(c, cudaEventRecord(aux.diag, aux.s));
+        return EMFA_OK;
+    };
+    diag(0, st);
+    int kb = 0;
+    while (kb < F.nblk) {
+        const int k0 = kb * NB, nb = std::min(NB, n - k0), rest = n - k0 - nb;
+        if (rest <= 0) break;
+        const int k1 = k0 + nb, ch = (rest + NB - 1) / NB;
+        if (aux.s && F.nblk - kb - 1 >= 2) {
+            // blocks kb and kb + 1 as a pair: block kb's update of the next
+            // block's columns and rows only, then one K = 128 update of the
+            // rest with both blocks' panels (A22 is read and written once
+            // for the two)
+            const int k2 = k1 + NB, ch2 = (n - k2 + NB - 1) / NB;
+            panels(k0, nb, 1);
+            update(tmC, k1, 0, 1, row_tiles(k1), 2, st);  // columns of block kb + 1
+            EMFA_TRY(diag_aside(kb + 1));
+            CUtensorMap tmR;                              // rows of block kb + 1
+            EMFA_TRY(tile_map(c, &tmR, A, n, lda, k2));
+            update(tmR, k1, 1, ch - 1, 1, 2, st);
+            EMFA_CUDA(c, cudaStreamWaitEvent(st, aux.diag, 0));
+            panels(k1, NB, 0);
+            k_lu_pack2<<<dim3((unsigned)((n - k2 + 7) / 8), 2), 256, 0, st>>>(A, n, lda, k0, Uop, Lop, inv_t, inv_s);
+            c->kernel_launches += 1;
+            update(tmC, k2, 0, 1, row_tiles(k2), 4, st);  // columns of block kb + 2
+            if (ch2 > 1) {
+                EMFA_TRY(diag_aside(kb + 2));
+                update(tmC, k2, 1, ch2 - 1, row_tiles(k2), 4, st);
+                EMFA_CUDA(c, cudaStreamWaitEvent(st, aux.diag, 0));
+            } else {
+                diag(kb + 2, st);
+            }
+            kb += 2;
+            continue;
+        }
+        panels(k0, nb, 1);
         if (aux.s && ch > 1) {
             // the next block's columns, then its diagonal block on the
             // high-priority stream while the other columns are updated
-            update(k0 + nb, 0, 1, st);
-            EMFA_CUDA(c, cudaEventRecord(aux.panel, st));
-            EMFA_CUDA(c, cudaStreamWaitEvent(aux.s, aux.panel, 0));
-            diag(kb + 1, aux.s);
-            EMFA_CUDA(c, cudaEventRecord(aux.diag, aux.s));
-            update(k0 + nb, 1, (int)ch - 1, st);
+            update(tmC, k1, 0, 1, row_tiles(k1), 2, st);
+            EMFA_TRY(diag_aside(kb + 1));
+            update(tmC, k1, 1, ch - 1, row_tiles(k1), 2, st);
             EMFA_CUDA(c, cudaStreamWaitEvent(st, aux.diag, 0));
         } else {
-            update(k0 + nb, 0, (int)ch, st);
+            update(tmC, k1, 0, ch, row_tiles(k1), 2, st);
             diag(kb + 1, st);
         }
+        kb += 1;
     }
     if (F.nblk > 1) {
         k_lu_rowperm_left<<<dim3((unsigned)(F.nblk - 1) * (NB / 32), (unsigned)F.nblk), 256, 0, st>>>(
