@@ -18,25 +18,44 @@ namespace emfa {
 // = the opposite corners.  Boundary (never paired) edges are dropped.
 int build_rwg_host(const int* tris, int n_tri, std::vector<int>& out, std::string* err)
 {
+    // Open half-edges by directed key (u, v), in an open-addressing table
+    // whose slots head a chain of the half-edges with that key (a manifold
+    // mesh has one); a triangle that brings the reverse edge (v, u) closes
+    // every half-edge of the chain and frees the key.
     struct Tmp { int v1, v2, vxp, vxm, tp, tm; };
     std::vector<Tmp> tmp;
     tmp.reserve((size_t)3 * n_tri);
-    std::unordered_map<uint64_t, std::vector<int>> open;
-    open.reserve((size_t)3 * n_tri);
+    std::vector<int> nxt;  // next half-edge of the same key, -1 at the end
+    nxt.reserve((size_t)3 * n_tri);
+    size_t cap = 16;
+    while (cap < (size_t)6 * n_tri) cap <<= 1;
+    const uint64_t EMPTY = ~0ull, GONE = ~0ull - 1;  // no vertex index reaches these keys
+    struct Slot { uint64_t key; int head, tail; };     // one cache access per probe
+    std::vector<Slot> tab(cap, Slot{EMPTY, -1, -1});
     auto key = [](int a, int b) { return ((uint64_t)(uint32_t)a << 32) | (uint32_t)b; };
+    auto slot_of = [&](uint64_t k) {
+        uint64_t h = k * 0x9E3779B97F4A7C15ull;
+        return (size_t)(h >> 20) & (cap - 1);
+    };
+    auto find = [&](uint64_t k) -> long {
+        for (size_t i = slot_of(k);; i = (i + 1) & (cap - 1)) {
+            if (tab[i].key == k) return (long)i;
+            if (tab[i].key == EMPTY) return -1;
+        }
+    };
     for (int t = 0; t < n_tri; ++t) {
         int a = tris[3 * t], b = tris[3 * t + 1], c = tris[3 * t + 2];
         int corner[3][3] = {{a, b, c}, {b, c, a}, {c, a, b}};
         bool fresh[3] = {true, true, true};
         for (int e = 0; e < 3; ++e) {
-            auto it = open.find(key(corner[e][1], corner[e][0]));
-            if (it == open.end()) continue;
-            for (int idx : it->second) {
+            const long sl = find(key(corner[e][1], corner[e][0]));
+            if (sl < 0) continue;
+            for (int idx = tab[sl].head; idx >= 0; idx = nxt[idx]) {
                 tmp[idx].vxm = corner[e][2];
                 tmp[idx].tm = t;
             }
             fresh[e] = false;
-            open.erase(it);
+            tab[sl].key = GONE;
         }
         for (int e = 0; e < 3; ++e) {
             if (!fresh[e]) continue;
@@ -45,11 +64,23 @@ int build_rwg_host(const int* tris, int n_tri, std::vector<int>& out, std::strin
                 if (err) *err = "degenerate triangle " + std::to_string(t);
                 return -1;
             }
-            open[key(u, v)].push_back((int)tmp.size());
+            const uint64_t k = key(u, v);
+            const int idx = (int)tmp.size();
             tmp.push_back(Tmp{u, v, corner[e][2], -1, t, -1});
+            nxt.push_back(-1);
+            const long sl = find(k);
+            if (sl >= 0) {  // a chain: append, keeping the order of insertion
+                nxt[tab[sl].tail] = idx;
+                tab[sl].tail = idx;
+                continue;
+            }
+            size_t i = slot_of(k);
+            while (tab[i].key != EMPTY && tab[i].key != GONE) i = (i + 1) & (cap - 1);
+            tab[i] = Slot{k, idx, idx};
         }
     }
     out.clear();
+    out.reserve(tmp.size() * 6);
     for (const Tmp& s : tmp) {
         if (s.tm == -1) continue;
         out.insert(out.end(), {s.v1, s.v2, s.vxp, s.vxm, s.tp, s.tm});
