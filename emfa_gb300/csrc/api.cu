@@ -33,19 +33,21 @@ extern "C" emfa_status_t emfa_dense_rcs(emfa_ctx_t* ctx, const double* verts_hos
         emfa_geom_t* g;
         ~GeomGuard() { emfa_geom_destroy(g); }
     } guard{g};
+    // Z, V and X stay in the context's workspace for the next job (released
+    // with the context): a job then allocates nothing of its size
     const size_t es = fp->precision == EMFA_F64 ? 16 : 8;
-    DevBuf Z, V, X;
-    EMFA_TRY(Z.alloc(ctx, es * (size_t)n * n));
-    EMFA_TRY(V.alloc(ctx, es * (size_t)n * n_inc));
-    EMFA_TRY(X.alloc(ctx, 16 * (size_t)n * n_inc));
-    EMFA_TRY(launch_fill_z(ctx, g, fp, Z.ptr, n, st));
-    EMFA_TRY(launch_fill_v(ctx, g, fp, angles_host, n_inc, V.ptr, st));
-    emfa_status_t ss = solve_dense(ctx, fp->precision, Z.ptr, n, V.ptr, n_inc, X.ptr, sp, info, st);
+    void *Z = nullptr, *V = nullptr, *X = nullptr;
+    EMFA_TRY(ctx_workspace(ctx, WS_DENSE_Z, es * (size_t)n * n, &Z));
+    EMFA_TRY(ctx_workspace(ctx, WS_DENSE_V, es * (size_t)n * n_inc, &V));
+    EMFA_TRY(ctx_workspace(ctx, WS_DENSE_X, 16 * (size_t)n * n_inc, &X));
+    EMFA_TRY(launch_fill_z(ctx, g, fp, Z, n, st));
+    EMFA_TRY(launch_fill_v(ctx, g, fp, angles_host, n_inc, V, st));
+    emfa_status_t ss = solve_dense(ctx, fp->precision, Z, n, V, n_inc, X, sp, info, st);
     if (ss != EMFA_OK && ss != EMFA_ERR_NOT_CONVERGED) return ss;
     if (rcs_dirs_host && n_dir > 0 && rcs_out_host)
-        EMFA_TRY(launch_rcs(ctx, g, fp, X.ptr, n_inc, rcs_dirs_host, n_dir, per_rhs_dirs, rcs_out_host, st));
+        EMFA_TRY(launch_rcs(ctx, g, fp, X, n_inc, rcs_dirs_host, n_dir, per_rhs_dirs, rcs_out_host, st));
     if (I_out_host)
-        EMFA_CUDA(ctx, cudaMemcpyAsync(I_out_host, X.ptr, 16 * (size_t)n * n_inc, cudaMemcpyDeviceToHost, st));
+        EMFA_CUDA(ctx, cudaMemcpyAsync(I_out_host, X, 16 * (size_t)n * n_inc, cudaMemcpyDeviceToHost, st));
     EMFA_CUDA(ctx, cudaStreamSynchronize(st));
     return ss;
 }

@@ -76,10 +76,20 @@ struct DevBuf {
 };
 
 template <typename T> inline T* dptr(const DevBuf& b) { return reinterpret_cast<T*>(b.ptr); }
+// a region of a DevBuf (not owning)
+struct DevView {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+};
+template <typename T> inline T* dptr(const DevView& b) { return reinterpret_cast<T*>(b.ptr); }
 
 // Workspace slots: buffers a context keeps between calls so repeated fills,
 // products and solves do not allocate.  A slot grows when a call needs more.
-enum WorkspaceSlot { WS_GEMM_B = 0, WS_GEMM_ERR, WS_KRYLOV, WS_FILL, WS_RCS, WS_ZPLANES, WS_HGEMM, WS_COUNT };
+enum WorkspaceSlot {
+    WS_GEMM_B = 0, WS_GEMM_ERR, WS_KRYLOV, WS_FILL, WS_RCS, WS_ZPLANES, WS_HGEMM,
+    WS_DENSE_Z, WS_DENSE_V, WS_DENSE_X,  // emfa_dense_rcs: the job's matrix, excitation and currents
+    WS_COUNT
+};
 
 // Kernels the context can time with CUDA events (emfa_ctx_set_kernel_timing).
 enum KernelTimerId { KT_FILL_Z = 0, KT_GEMM, KT_RESIDUAL, KT_COUNT };
@@ -169,13 +179,15 @@ struct RwgPack {
 template <typename T>
 struct GeomDev {
     bool ready = false;
-    DevBuf verts;   // V x 3
-    DevBuf tris;    // T x 3 int
-    DevBuf tri_q3;  // T x 3 x 3
-    DevBuf tri_q7;  // T x 7 x 3
-    DevBuf tri_n;   // T x 3
-    DevBuf tri_area;  // T
-    DevBuf rwg;     // N x RwgPack<T>
+    DevBuf block;     // one allocation holding the arrays below
+    DevView verts;    // V x 3
+    DevView tris;     // T x 3 int
+    DevView tri_q3;   // T x 3 x 3
+    DevView tri_q7;   // T x 7 x 3
+    DevView tri_n;    // T x 3
+    DevView tri_area;  // T
+    DevView rwg;      // N x RwgPack<T>
+    DevView rwg_tab;  // N x 6 int, the RWG table as uploaded
 };
 
 struct Geom {
@@ -184,16 +196,21 @@ struct Geom {
     std::vector<double> verts;   // host, V x 3
     std::vector<int> tris;       // host, T x 3
     std::vector<int> rwg;        // host, N x 6 (v1 v2 vxp vxm tp tm)
+    DevBuf vd;                   // device copy of verts (FP64), uploaded once
     GeomDev<float> g32;
     GeomDev<double> g64;
     // tiled fill: the distinct triangles of each block of 16 consecutive
     // RWGs, and each RWG's position of its two triangles in its block's list
     bool tile_ready = false;
     int tile_maxt = 0;
-    DevBuf tile_tris;  // int [blocks][tile_maxt]
-    DevBuf tile_nt;    // int [blocks]
-    DevBuf tile_loc;   // uint8 [N][2]
+    DevBuf tile_block;  // one allocation holding the three arrays below
+    DevView tile_tris;  // int [blocks][tile_maxt]
+    DevView tile_nt;    // int [blocks]
+    DevView tile_loc;   // uint8 [N][2]
 };
+
+// the FP64 vertices on the device (uploaded on first use)
+emfa_status_t geom_vd(Geom* g, cudaStream_t st);
 
 emfa_status_t geom_prepare_f32(Geom* g, cudaStream_t st);
 emfa_status_t geom_prepare_f64(Geom* g, cudaStream_t st);

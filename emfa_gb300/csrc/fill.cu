@@ -398,9 +398,11 @@ static emfa_status_t tile_plan(Ctx* c, Geom* g, cudaStream_t st)
         cnt[b] = (int)lists[b].size();
         std::copy(lists[b].begin(), lists[b].end(), flat.begin() + (size_t)b * maxt);
     }
-    EMFA_TRY(g->tile_tris.alloc(c, sizeof(int) * flat.size()));
-    EMFA_TRY(g->tile_nt.alloc(c, sizeof(int) * cnt.size()));
-    EMFA_TRY(g->tile_loc.alloc(c, loc.size()));
+    const size_t b0 = (sizeof(int) * flat.size() + 255) & ~(size_t)255, b1 = (sizeof(int) * cnt.size() + 255) & ~(size_t)255;
+    EMFA_TRY(g->tile_block.alloc(c, b0 + b1 + loc.size()));
+    g->tile_tris = DevView{g->tile_block.ptr, sizeof(int) * flat.size()};
+    g->tile_nt = DevView{(char*)g->tile_block.ptr + b0, sizeof(int) * cnt.size()};
+    g->tile_loc = DevView{(char*)g->tile_block.ptr + b0 + b1, loc.size()};
     EMFA_CUDA(c, cudaMemcpyAsync(g->tile_tris.ptr, flat.data(), g->tile_tris.bytes, cudaMemcpyHostToDevice, st));
     EMFA_CUDA(c, cudaMemcpyAsync(g->tile_nt.ptr, cnt.data(), g->tile_nt.bytes, cudaMemcpyHostToDevice, st));
     EMFA_CUDA(c, cudaMemcpyAsync(g->tile_loc.ptr, loc.data(), g->tile_loc.bytes, cudaMemcpyHostToDevice, st));
@@ -527,10 +529,9 @@ emfa_status_t build_singular_table(Ctx* c, Geom* g, const emfa_fill_params_t* p,
         EMFA_TRY(geom_prepare_f64(g, st));
     else
         EMFA_TRY(geom_prepare_f32(g, st));
-    // the table's vertices and k: the fill precision's k, in FP64 arithmetic
-    DevBuf vd;
-    EMFA_TRY(vd.alloc(c, sizeof(double) * 3 * (size_t)g->nv));
-    EMFA_CUDA(c, cudaMemcpyAsync(vd.ptr, g->verts.data(), vd.bytes, cudaMemcpyHostToDevice, st));
+    // the table's vertices (the geometry's FP64 copy) and k: the fill
+    // precision's k, in FP64 arithmetic
+    EMFA_TRY(geom_vd(g, st));
     SingConst sc;
     sc.k = p->precision == EMFA_F64 ? Phys<double>::wavenumber(p->freq) : (double)Phys<float>::wavenumber(p->freq);
     sc.inv_k2 = 1.0 / (sc.k * sc.k);
@@ -542,10 +543,9 @@ emfa_status_t build_singular_table(Ctx* c, Geom* g, const emfa_fill_params_t* p,
     sc.sig_im = p->sigma_im;
     sc.cfie = cfie;
     const int* tris = p->precision == EMFA_F64 ? dptr<int>(g->g64.tris) : dptr<int>(g->g32.tris);
-    k_singular_table<<<(9 * g->nt + 127) / 128, 128, 0, st>>>(dptr<double>(vd), tris, g->nt, sc, tab);
+    k_singular_table<<<(9 * g->nt + 127) / 128, 128, 0, st>>>(dptr<double>(g->vd), tris, g->nt, sc, tab);
     c->kernel_launches += 1;
     EMFA_CUDA(c, cudaGetLastError());
-    EMFA_CUDA(c, cudaStreamSynchronize(st));  // vd is released on return
     return EMFA_OK;
 }
 

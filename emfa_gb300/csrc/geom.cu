@@ -163,33 +163,48 @@ __global__ void k_pack_rwg(const double* __restrict__ vd, const int* __restrict_
     out[u] = pk;
 }
 
+emfa_status_t geom_vd(Geom* g, cudaStream_t st)
+{
+    if (g->vd.ptr) return EMFA_OK;
+    EMFA_TRY(g->vd.alloc(g->ctx, sizeof(double) * 3 * g->nv));
+    // pageable source: the copy is staged before the call returns
+    EMFA_CUDA(g->ctx, cudaMemcpyAsync(g->vd.ptr, g->verts.data(), g->vd.bytes, cudaMemcpyHostToDevice, st));
+    return EMFA_OK;
+}
+
 template <typename T>
 static emfa_status_t geom_prepare(Geom* g, GeomDev<T>& d, cudaStream_t st)
 {
     if (d.ready) return EMFA_OK;
     Ctx* c = g->ctx;
-    DevBuf vd, td, rd;
-    EMFA_TRY(vd.alloc(c, sizeof(double) * 3 * g->nv));
-    EMFA_TRY(rd.alloc(c, sizeof(int) * 6 * (size_t)g->n));
-    EMFA_TRY(d.tris.alloc(c, sizeof(int) * 3 * (size_t)g->nt));
-    EMFA_TRY(d.verts.alloc(c, sizeof(T) * 3 * (size_t)g->nv));
-    EMFA_TRY(d.tri_q3.alloc(c, sizeof(T) * 9 * (size_t)g->nt));
-    EMFA_TRY(d.tri_q7.alloc(c, sizeof(T) * 21 * (size_t)g->nt));
-    EMFA_TRY(d.tri_n.alloc(c, sizeof(T) * 3 * (size_t)g->nt));
-    EMFA_TRY(d.tri_area.alloc(c, sizeof(T) * (size_t)g->nt));
-    EMFA_TRY(d.rwg.alloc(c, sizeof(RwgPack<T>) * (size_t)g->n));
-    EMFA_CUDA(c, cudaMemcpyAsync(vd.ptr, g->verts.data(), vd.bytes, cudaMemcpyHostToDevice, st));
+    EMFA_TRY(geom_vd(g, st));
+    DevView* parts[8] = {&d.tris, &d.verts, &d.tri_q3, &d.tri_q7, &d.tri_n, &d.tri_area, &d.rwg, &d.rwg_tab};
+    const size_t sizes[8] = {sizeof(int) * 3 * (size_t)g->nt, sizeof(T) * 3 * (size_t)g->nv,
+                             sizeof(T) * 9 * (size_t)g->nt,   sizeof(T) * 21 * (size_t)g->nt,
+                             sizeof(T) * 3 * (size_t)g->nt,   sizeof(T) * (size_t)g->nt,
+                             sizeof(RwgPack<T>) * (size_t)g->n, sizeof(int) * 6 * (size_t)g->n};
+    size_t total = 0;
+    for (size_t b : sizes) total += (b + 255) & ~(size_t)255;
+    EMFA_TRY(d.block.alloc(c, total));
+    size_t off = 0;
+    for (int i = 0; i < 8; ++i) {
+        parts[i]->ptr = (char*)d.block.ptr + off;
+        parts[i]->bytes = sizes[i];
+        off += (sizes[i] + 255) & ~(size_t)255;
+    }
     EMFA_CUDA(c, cudaMemcpyAsync(d.tris.ptr, g->tris.data(), d.tris.bytes, cudaMemcpyHostToDevice, st));
-    EMFA_CUDA(c, cudaMemcpyAsync(rd.ptr, g->rwg.data(), rd.bytes, cudaMemcpyHostToDevice, st));
+    EMFA_CUDA(c, cudaMemcpyAsync(d.rwg_tab.ptr, g->rwg.data(), d.rwg_tab.bytes, cudaMemcpyHostToDevice, st));
     int m = g->nt > g->nv ? g->nt : g->nv;
-    k_pack_tris<T><<<(m + 127) / 128, 128, 0, st>>>(dptr<double>(vd), dptr<int>(d.tris), g->nt, dptr<T>(d.verts),
+    k_pack_tris<T><<<(m + 127) / 128, 128, 0, st>>>(dptr<double>(g->vd), dptr<int>(d.tris), g->nt, dptr<T>(d.verts),
                                                     dptr<T>(d.tri_q3), dptr<T>(d.tri_q7), dptr<T>(d.tri_n),
                                                     dptr<T>(d.tri_area), g->nv);
-    k_pack_rwg<T><<<(g->n + 127) / 128, 128, 0, st>>>(dptr<double>(vd), dptr<int>(d.tris), dptr<int>(rd), g->n,
-                                                      dptr<T>(d.tri_q3), dptr<T>(d.tri_n), dptr<RwgPack<T>>(d.rwg));
+    k_pack_rwg<T><<<(g->n + 127) / 128, 128, 0, st>>>(dptr<double>(g->vd), dptr<int>(d.tris), dptr<int>(d.rwg_tab),
+                                                      g->n, dptr<T>(d.tri_q3), dptr<T>(d.tri_n),
+                                                      dptr<RwgPack<T>>(d.rwg));
     c->kernel_launches += 2;
     EMFA_CUDA(c, cudaGetLastError());
-    EMFA_CUDA(c, cudaStreamSynchronize(st));  // vd/rd are released on return
+    // later users may run on other streams: the arrays are complete on return
+    EMFA_CUDA(c, cudaStreamSynchronize(st));
     d.ready = true;
     return EMFA_OK;
 }
