@@ -305,7 +305,9 @@ emfa_status_t emfa_mlfma_unpermute(emfa_mlfma_t* mlfma, const void* X_box_dev, i
  * emfa_rcs; rcs_out_host is n_inc x n_dir dBsm; I_out_host (optional,
  * complex128 n_inc x N) receives the currents.  This is what
  * solver::invoke_solver<EFIE|CFIE> (EMSolver/Solver.h:20-29) runs:
- * init -> solve -> output. */
+ * init -> solve -> output.  The job's matrix, excitation and currents stay
+ * in the context's workspace after the call (reused by the next job, released
+ * with the context; emfa_ctx_memory counts them). */
 emfa_status_t emfa_dense_rcs(emfa_ctx_t* ctx, const double* verts_host, int n_vert, const int* tris_host,
                              int n_tri, const emfa_fill_params_t* fp, const double* angles_host, int n_inc,
                              const emfa_solver_params_t* sp, const double* rcs_dirs_host, int n_dir,
