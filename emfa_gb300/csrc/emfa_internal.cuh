@@ -88,6 +88,7 @@ template <typename T> inline T* dptr(const DevView& b) { return reinterpret_cast
 enum WorkspaceSlot {
     WS_GEMM_B = 0, WS_GEMM_ERR, WS_KRYLOV, WS_FILL, WS_RCS, WS_ZPLANES, WS_HGEMM,
     WS_DENSE_Z, WS_DENSE_V, WS_DENSE_X,  // emfa_dense_rcs: the job's matrix, excitation and currents
+    WS_LU_WAVE,                          // tickets and flags of the LU's triangular solves
     WS_COUNT
 };
 

@@ -1388,6 +1388,7 @@ static emfa_status_t lu_refined(Ctx* c, LinOp& A, const void* Z, const void* B, 
         EMFA_CUDA(c, cudaStreamSynchronize(st));
         c->kernel_launches += 1;
         worst = *std::max_element(rel.begin(), rel.end());
+        if (zero_pivot == 0) EMFA_TRY(lu_check_solves(c, F, st));
         if (worst < sp->tol) {
             if (info) {
                 info->converged = nrhs;

@@ -23,10 +23,9 @@
 // Rows of the factor are padded to an even number of complex elements
 // (16-byte TMA strides).
 // Solve for many right-hand sides (RHS-major, (r, u) at r n + u): gather by
-// the row permutation, then one launch per block for the forward (L) sweep
-// and one per block for the backward (U) sweep.  Each CTA applies the block's
-// explicit inverse to the block's right-hand sides and updates its own rows
-// below (above) the block.
+// the row permutation, then one launch for the forward (L) and one for the
+// backward (U) sweep (k_lu_wave): a CTA per row block, in wavefront order,
+// applies the block's explicit inverse once the blocks before it are solved.
 //
 // A pivot that is exactly zero is replaced by 1e-30 and recorded in the
 // factor's info word, so the caller can fall back to an iterative solve.
@@ -797,58 +796,139 @@ __global__ void k_lu_gather(const float2* __restrict__ B, const int* __restrict_
 
 constexpr int RC = 8;  // right-hand sides per CTA of a sweep step
 
-// One step of the forward (dir 0, L) or backward (dir 1, U) sweep for block
-// k0: x = inv W[block] for the CTA's right-hand sides (CTA x = 0 stores it in
-// Out), then W[rows] -= A[rows][block] x on the CTA's 64-row chunk of the rows
-// after (dir 0) or before (dir 1) the block.  The block's inverse, then the
-// chunk's 64 x 64 slice of A, are staged in shared memory.
-__global__ void __launch_bounds__(256) k_lu_sweep(const float2* __restrict__ A, int n, int lda, int k0, int nb,
-                                                  const float2* __restrict__ inv, int dir, int nrhs,
-                                                  float2* __restrict__ W, float2* __restrict__ Out)
+// Both triangular solves as one launch each, in wavefront order.  A CTA
+// takes a ticket when it starts: ticket t is row block t of the forward (L)
+// sweep, block nblk - 1 - t of the backward (U) sweep, so a CTA only waits for
+// blocks whose CTAs started before it.  Row block k:
+//   acc = W[block k] - sum over the blocks j before k (forward: j < k;
+//         backward: j > k) of A[block k][block j] x_j
+//   x_k = inv_k acc, stored in Out, then the block's flag is raised
+// Each x_j is read once its flag is up (bounded wait: on timeout, or once
+// any wait has given up, the kernel records an error and stops waiting); the
+// 64 x 64 blocks of A stream through a cp.async double buffer.  RC right-hand
+// sides per CTA (blockIdx.y).  Thread: row i = tid / 4, right-hand sides
+// 2 (tid % 4) and the next.
+constexpr int WLD = NB + 2;  // tile row stride in float2: 16-byte aligned, 8 rows on distinct banks
+
+__device__ __forceinline__ void cp_async16(void* dst, const void* src, int src_bytes)
 {
-    __shared__ float2 M[NB][LDS];  // inverse of the block, then the chunk's slice of A
-    __shared__ float2 ws[RC][NB];
-    __shared__ float2 xs[RC][NB];
-    const int tid = threadIdx.x;
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(tc::smem_u32(dst)), "l"(src), "r"(src_bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+// tile rows [r0, r0 + 64) x columns [c0, c0 + 64) of A into T (rows past n
+// or columns past n read as zeros)
+__device__ __forceinline__ void tile_async(float2* T, const float2* __restrict__ A, int n, int lda, int r0, int c0)
+{
+    for (int q = threadIdx.x; q < NB * (NB / 2); q += blockDim.x) {
+        const int i = q / (NB / 2), c = 2 * (q % (NB / 2));  // 16-byte piece: two complex
+        const int r = r0 + i, cc = c0 + c;
+        const int nv = (r < n) ? max(0, min(2, n - cc)) : 0;  // valid complex in the piece
+        // clamped source stays 16-byte aligned: lda and the column are even
+        const float2* src = A + (size_t)min(r, n - 1) * lda + min(cc, (n - 1) & ~1);
+        cp_async16(T + i * WLD + c, src, 8 * nv);
+    }
+}
+
+template <int DIR>
+__global__ void __launch_bounds__(256) k_lu_wave(const float2* __restrict__ A, int n, int lda, int nblk,
+                                                 const float2* __restrict__ inv, int nrhs,
+                                                 const float2* __restrict__ W, float2* __restrict__ Out,
+                                                 int* __restrict__ ticket, int* __restrict__ flag,
+                                                 int* __restrict__ err, long long limit)
+{
+    extern __shared__ float2 s_w[];
+    float2* T0 = s_w;                 // [NB][WLD] tile buffers
+    float2* T1 = T0 + NB * WLD;
+    __shared__ float2 xs[NB][RC];     // x_j of the tile, then acc
+    __shared__ int s_t, s_ok;
+    const int tid = threadIdx.x, i = tid >> 2, r = 2 * (tid & 3);
+    if (tid == 0) s_t = atomicAdd(ticket + blockIdx.y, 1);
+    __syncthreads();
+    const int t = s_t;
+    const int k = DIR == 0 ? t : nblk - 1 - t;
+    const int k0 = k * NB, nbk = min(NB, n - k0);
     const int rb = blockIdx.y * RC, nr = min(RC, nrhs - rb);
-    const float2* iv = inv + (size_t)(k0 / NB) * NB * NB;
-    for (int q = tid; q < NB * NB; q += blockDim.x) M[q / NB][q % NB] = iv[q];
-    for (int q = tid; q < RC * NB; q += blockDim.x) {
-        const int r = q / NB, j = q % NB;
-        ws[r][j] = (r < nr && j < nb) ? W[(size_t)(rb + r) * n + k0 + j] : make_float2(0.f, 0.f);
+    int* fl = flag + (size_t)blockIdx.y * nblk;
+    float2 acc[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+        acc[h] = (i < nbk && r + h < nr) ? W[(size_t)(rb + r + h) * n + k0 + i] : make_float2(0.f, 0.f);
+    // the blocks this row block depends on, in the order they are solved
+    const int nd = DIR == 0 ? k : nblk - 1 - k;
+    auto dep = [&](int s) { return DIR == 0 ? s : nblk - 1 - s; };
+    if (nd > 0) {
+        tile_async(T0, A, n, lda, k0, dep(0) * NB);
+        cp_async_commit();
     }
-    __syncthreads();
-    for (int q = tid; q < RC * NB; q += blockDim.x) {
-        const int r = q / NB, i = q % NB;
-        float2 s = make_float2(0.f, 0.f);
-#pragma unroll 8
-        for (int j = 0; j < NB; ++j) s = cfma(M[i][j], ws[r][j], s);
-        xs[r][i] = s;
-    }
-    __syncthreads();
-    if (blockIdx.x == 0)
-        for (int q = tid; q < RC * NB; q += blockDim.x) {
-            const int r = q / NB, i = q % NB;
-            if (r < nr && i < nb) Out[(size_t)(rb + r) * n + k0 + i] = xs[r][i];
+    bool ok = true;
+    for (int s = 0; s < nd; ++s) {
+        float2* T = (s & 1) ? T1 : T0;
+        if (s + 1 < nd) tile_async((s & 1) ? T0 : T1, A, n, lda, k0, dep(s + 1) * NB);
+        cp_async_commit();
+        const int j = dep(s), j0 = j * NB, nbj = min(NB, n - j0);
+        if (tid == 0) {
+            int got = ok;
+            if (got) {
+                const long long t0 = clock64();
+                while (*(volatile int*)(fl + j) == 0) {
+                    if (*(volatile int*)err || clock64() - t0 > limit) {
+                        atomicCAS(err, 0, 21);
+                        got = 0;
+                        break;
+                    }
+                }
+            }
+            __threadfence();
+            s_ok = got;
         }
-    // rows of this CTA's chunk
-    const int lo = dir == 0 ? k0 + nb : 0, hi = dir == 0 ? n : k0;
-    const int m0 = lo + blockIdx.x * NB;
-    const int nm = min(NB, hi - m0);
-    if (nm <= 0) return;  // uniform over the CTA; no barrier follows
-    for (int q = tid; q < NB * NB; q += blockDim.x) {
-        const int i = q / NB, j = q % NB;
-        M[i][j] = (i < nm && j < nb) ? A[(size_t)(m0 + i) * lda + k0 + j] : make_float2(0.f, 0.f);
-    }
-    __syncthreads();
-    for (int q = tid; q < nm * nr; q += blockDim.x) {
-        const int i = q % nm, r = q / nm;
-        float2 s = make_float2(0.f, 0.f);
+        __syncthreads();
+        ok = s_ok;
+        if (ok)
+            for (int q = tid; q < NB * RC; q += blockDim.x) {
+                const int c = q / RC, rr = q % RC;
+                xs[c][rr] = (c < nbj && rr < nr) ? __ldcg(Out + (size_t)(rb + rr) * n + j0 + c) : make_float2(0.f, 0.f);
+            }
+        cp_async_wait<1>();
+        __syncthreads();
+        if (ok) {
+            // the block's 64-term product on its own, then subtracted (the
+            // rounding of a sweep that updates W block by block)
+            float2 p[2] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
 #pragma unroll 8
-        for (int j = 0; j < NB; ++j) s = cfma(M[i][j], xs[r][j], s);
-        float2* w = W + (size_t)(rb + r) * n + m0 + i;
-        *w = make_float2(w->x - s.x, w->y - s.y);
+            for (int c = 0; c < NB; ++c) {
+                const float2 l = T[i * WLD + c];
+#pragma unroll
+                for (int h = 0; h < 2; ++h) p[h] = cfma(l, xs[c][r + h], p[h]);
+            }
+#pragma unroll
+            for (int h = 0; h < 2; ++h) acc[h] = make_float2(acc[h].x - p[h].x, acc[h].y - p[h].y);
+        }
+        __syncthreads();
     }
+    cp_async_wait<0>();
+    // x_k = inv_k acc
+#pragma unroll
+    for (int h = 0; h < 2; ++h) xs[i][r + h] = acc[h];
+    const float2* iv = inv + (size_t)k * NB * NB;
+    for (int q = tid; q < NB * NB; q += blockDim.x) T0[(q / NB) * WLD + q % NB] = iv[q];
+    __syncthreads();
+    float2 x[2] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+#pragma unroll 8
+    for (int c = 0; c < NB; ++c) {
+        const float2 m = T0[i * WLD + c];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) x[h] = cfma(m, xs[c][r + h], x[h]);
+    }
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+        if (i < nbk && r + h < nr) Out[(size_t)(rb + r + h) * n + k0 + i] = x[h];
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) atomicExch(fl + k, 1);
 }
 
 }  // namespace
@@ -919,6 +999,8 @@ static emfa_status_t lu_set_smem(Ctx* c)
 {
     EMFA_TRY(ensure_smem(c, k_lu_diag, diag_smem()));
     EMFA_TRY(ensure_smem(c, k_lu_panels, 2 * sizeof(float2) * NB * LDS));
+    EMFA_TRY(ensure_smem(c, k_lu_wave<0>, sizeof(float2) * 2 * NB * WLD));
+    EMFA_TRY(ensure_smem(c, k_lu_wave<1>, sizeof(float2) * 2 * NB * WLD));
     return ensure_smem(c, k_lu_update_tc, lutc::SMEM);
 }
 
@@ -951,7 +1033,7 @@ emfa_status_t lu_factor(Ctx* c, const void* Z, int n, LuFactor& F, cudaStream_t 
     EMFA_TRY(tile_map(c, &tmC, A, n, lda, n));
     EMFA_CUDA(c, cudaMemcpy2DAsync(A, sizeof(float2) * (size_t)lda, Z, sizeof(float2) * (size_t)n,
                                    sizeof(float2) * (size_t)n, (size_t)n, cudaMemcpyDeviceToDevice, st));
-    EMFA_CUDA(c, cudaMemsetAsync(info, 0, 2 * sizeof(int), st));
+    EMFA_CUDA(c, cudaMemsetAsync(info, 0, 3 * sizeof(int), st));
     const size_t s2 = 2 * sizeof(float2) * NB * LDS;
     // lookahead: the next diagonal block is factored on a high-priority
     // stream while the rest of the trailing matrix is updated on st, so its
@@ -1059,6 +1141,18 @@ emfa_status_t lu_factor(Ctx* c, const void* Z, int n, LuFactor& F, cudaStream_t 
     return EMFA_OK;
 }
 
+emfa_status_t lu_check_solves(Ctx* c, const LuFactor& F, cudaStream_t st)
+{
+    int h = 0;
+    EMFA_CUDA(c, cudaMemcpyAsync(&h, dptr<int>(F.info) + 2, sizeof(int), cudaMemcpyDeviceToHost, st));
+    EMFA_CUDA(c, cudaStreamSynchronize(st));
+    if (h) {
+        set_error(c, "lu_apply: a wait of the triangular solves timed out (code " + std::to_string(h) + ")");
+        return EMFA_ERR_TIMEOUT;
+    }
+    return EMFA_OK;
+}
+
 emfa_status_t lu_zero_pivot(Ctx* c, const LuFactor& F, int* first, cudaStream_t st)
 {
     int h[2] = {0, 0};
@@ -1078,22 +1172,27 @@ emfa_status_t lu_apply(Ctx* c, const LuFactor& F, const float2* B, int nrhs, flo
 {
     const int n = F.n;
     const size_t tot = (size_t)n * nrhs;
-    float2* W = work;           // permuted right-hand sides, then the forward sweep's residue
+    float2* W = work;           // permuted right-hand sides
     float2* Y = work + tot;     // L^-1 P b
     const float2* A = dptr<float2>(F.a);
+    const int gy = (nrhs + RC - 1) / RC;
+    // tickets and flags of both sweeps: 2 (gy + gy nblk) ints
+    void* wp = nullptr;
+    const size_t words = 2 * ((size_t)gy + (size_t)gy * F.nblk);
+    EMFA_TRY(ctx_workspace(c, WS_LU_WAVE, sizeof(int) * words, &wp));
+    int* tk = (int*)wp;
+    int* fl = tk + 2 * gy;
+    EMFA_CUDA(c, cudaMemsetAsync(tk, 0, sizeof(int) * words, st));
     k_lu_gather<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(B, dptr<int>(F.perm), n, nrhs, W);
-    const unsigned gy = (unsigned)((nrhs + RC - 1) / RC);
-    for (int kb = 0; kb < F.nblk; ++kb) {
-        const int k0 = kb * NB, nb = std::min(NB, n - k0), rows = n - k0 - nb;
-        k_lu_sweep<<<dim3((unsigned)std::max(1, (rows + NB - 1) / NB), gy), 256, 0, st>>>(
-            A, n, F.lda, k0, nb, dptr<float2>(F.linv), 0, nrhs, W, Y);
-    }
-    for (int kb = F.nblk - 1; kb >= 0; --kb) {
-        const int k0 = kb * NB, nb = std::min(NB, n - k0);
-        k_lu_sweep<<<dim3((unsigned)std::max(1, (k0 + NB - 1) / NB), gy), 256, 0, st>>>(
-            A, n, F.lda, k0, nb, dptr<float2>(F.uinv), 1, nrhs, Y, X);
-    }
-    c->kernel_launches += 1 + 2 * F.nblk;
+    const size_t sm = sizeof(float2) * 2 * NB * WLD;
+    const long long limit = 2000000000LL;  // about 1 s
+    k_lu_wave<0><<<dim3((unsigned)F.nblk, (unsigned)gy), 256, sm, st>>>(A, n, F.lda, F.nblk, dptr<float2>(F.linv),
+                                                                        nrhs, W, Y, tk, fl, dptr<int>(F.info) + 2,
+                                                                        limit);
+    k_lu_wave<1><<<dim3((unsigned)F.nblk, (unsigned)gy), 256, sm, st>>>(
+        A, n, F.lda, F.nblk, dptr<float2>(F.uinv), nrhs, Y, X, tk + gy, fl + (size_t)gy * F.nblk,
+        dptr<int>(F.info) + 2, limit);
+    c->kernel_launches += 3;
     EMFA_CUDA(c, cudaGetLastError());
     return EMFA_OK;
 }
