@@ -33,8 +33,59 @@ struct SingConst {
 // source signs +1).  proj selects the projected edge-distance form of
 // eZ{pm,mp,mm}Singular (EFIE.cpp:344-368) instead of eZppSingular's direct
 // form (EFIE.cpp:260-283); both are the same integral.
+// The edge integrals of the singular EFIE term at quadrature point p of the
+// triangle (Is1, a vector, and Is2), with the points' distances taken
+// directly (proj false) or through their projections on the triangle's
+// plane (proj true): they depend on neither RWG, so one evaluation serves
+// the triangle's 9 (test edge, source edge) pairs.
+__device__ static void efie_edge_integrals(const V3<double>* v, int p, bool proj, V3<double>* Is1_out,
+                                           double* Is2_out)
+{
+    V3<double> g[3];
+    gauss3(v[0], v[1], v[2], g);
+    V3<double> n = normalized(cross(v[1] - v[0], v[2] - v[0]));
+    double Is2 = 0.0;
+    V3<double> Is1 = v3(0.0, 0.0, 0.0);
+    V3<double> rou = g[p] - n * dot(n, g[p]);
+    for (int i = 0; i < 3; ++i) {
+        V3<double> a = v[(i + 1) % 3], b = v[i];
+        V3<double> li = a - b;
+        V3<double> rou_p = a - n * dot(n, a);
+        V3<double> rou_m = b - n * dot(n, b);
+        V3<double> ui = normalized(cross(li, n));
+        V3<double> l1 = normalized(li);
+        double p0 = fabs(dot(b - g[p], ui));
+        double d = dot(g[p] - b, n);
+        double lp, lm, rp, rm;
+        if (!proj) {
+            lp = dot(a - g[p], l1);
+            lm = dot(b - g[p], l1);
+            rp = norm(g[p] - a);
+            rm = norm(g[p] - b);
+        } else {
+            lp = dot(rou_p - rou, l1);
+            lm = dot(rou_m - rou, l1);
+            rp = sqrt(p0 * p0 + d * d + lp * lp);
+            rm = sqrt(p0 * p0 + d * d + lm * lm);
+        }
+        if (p0 < 1e-10) continue;
+        V3<double> pi = normalized((rou_p - rou) - l1 * lp);
+        double r02 = p0 * p0 + d * d;
+        double lg = log((rp + lp) / (rm + lm));
+        Is1 = Is1 + (ui * 0.5) * (r02 * lg + lp * rp - lm * rm);
+        double ad = fabs(d);
+        Is2 += dot(pi, ui) * (p0 * lg - ad * (atan((p0 * lp) / (r02 + ad * rp)) - atan((p0 * lm) / (r02 + ad * rm))));
+    }
+    *Is1_out = Is1;
+    *Is2_out = Is2;
+}
+
+// EFIE self term (EFIE.cpp:139-296) of one (test edge, source edge) pair from
+// the triangle's edge integrals Is[p] = (Is1, Is2) of one variant: the
+// regular part over the 3 x 3 point pairs, then the singular part point by
+// point, in the order of the reference's loops.
 __device__ static Cx<double> efie_self(const V3<double>* v, V3<double> vf, V3<double> vs, const SingConst& c,
-                                       bool proj)
+                                       const double (*Is)[4])
 {
     V3<double> g[3];
     gauss3(v[0], v[1], v[2], g);
@@ -42,7 +93,6 @@ __device__ static Cx<double> efie_self(const V3<double>* v, V3<double> vf, V3<do
     double k = c.k;
     Cx<double> ze1 = cx(0.0, 0.0);
     double ze2 = 0.0;
-    V3<double> n = normalized(cross(v[1] - v[0], v[2] - v[0]));
     for (int p = 0; p < 3; ++p) {
         V3<double> rf = g[p] - vf;
         for (int q = 0; q < 3; ++q) {
@@ -52,38 +102,8 @@ __device__ static Cx<double> efie_self(const V3<double>* v, V3<double> vf, V3<do
             double s = c.w * c.w * (0.25 * dot(rf, rs) - c.inv_k2);
             ze1 = ze1 + coff * s;
         }
-        double Is2 = 0.0;
-        V3<double> Is1 = v3(0.0, 0.0, 0.0);
-        V3<double> rou = g[p] - n * dot(n, g[p]);
-        for (int i = 0; i < 3; ++i) {
-            V3<double> a = v[(i + 1) % 3], b = v[i];
-            V3<double> li = a - b;
-            V3<double> rou_p = a - n * dot(n, a);
-            V3<double> rou_m = b - n * dot(n, b);
-            V3<double> ui = normalized(cross(li, n));
-            V3<double> l1 = normalized(li);
-            double p0 = fabs(dot(b - g[p], ui));
-            double d = dot(g[p] - b, n);
-            double lp, lm, rp, rm;
-            if (!proj) {
-                lp = dot(a - g[p], l1);
-                lm = dot(b - g[p], l1);
-                rp = norm(g[p] - a);
-                rm = norm(g[p] - b);
-            } else {
-                lp = dot(rou_p - rou, l1);
-                lm = dot(rou_m - rou, l1);
-                rp = sqrt(p0 * p0 + d * d + lp * lp);
-                rm = sqrt(p0 * p0 + d * d + lm * lm);
-            }
-            if (p0 < 1e-10) continue;
-            V3<double> pi = normalized((rou_p - rou) - l1 * lp);
-            double r02 = p0 * p0 + d * d;
-            double lg = log((rp + lp) / (rm + lm));
-            Is1 = Is1 + (ui * 0.5) * (r02 * lg + lp * rp - lm * rm);
-            double ad = fabs(d);
-            Is2 += dot(pi, ui) * (p0 * lg - ad * (atan((p0 * lp) / (r02 + ad * rp)) - atan((p0 * lm) / (r02 + ad * rm))));
-        }
+        const V3<double> Is1 = v3(Is[p][0], Is[p][1], Is[p][2]);
+        const double Is2 = Is[p][3];
         ze2 += c.w * (0.25 * dot(rf, Is1 + (g[p] - vs) * Is2) - Is2 * c.inv_k2);
     }
     return cx(ze1.re + ze2 / S, ze1.im);
@@ -143,25 +163,46 @@ __device__ static Cx<double> cfie_self(const V3<double>* v, V3<double> vf, V3<do
     return cx(c.alpha * ze.re + (1.0 - c.alpha) * c.z0 * zmv, c.alpha * ze.im);
 }
 
-// table layout per (t, ef, es): EFIE {A_direct, A_proj, B_sigma}, CFIE {S}
-__global__ void k_singular_table(const double* __restrict__ vd, const int* __restrict__ tris, int nt, SingConst c,
-                                 double2* __restrict__ tab)
+// table layout per (t, ef, es): EFIE {A_direct, A_proj, B_sigma}, CFIE {S}.
+// A CTA of SING_TRIS triangles x 9 (ef, es) threads; for EFIE, 6 threads of
+// each triangle first evaluate its edge integrals (3 points x 2 variants).
+constexpr int SING_TRIS = 14;
+__global__ void __launch_bounds__(9 * SING_TRIS) k_singular_table(const double* __restrict__ vd,
+                                                                  const int* __restrict__ tris, int nt,
+                                                                  SingConst c, double2* __restrict__ tab)
 {
-    int id = blockIdx.x * blockDim.x + threadIdx.x;
-    if (id >= 9 * nt) return;
-    int t = id / 9, ef = (id % 9) / 3, es = id % 3;
+    __shared__ double sIs[SING_TRIS][2][3][4];  // [triangle][variant][point][Is1 xyz, Is2]
+    const int tl = threadIdx.x / 9, combo = threadIdx.x % 9;
+    const int t = blockIdx.x * SING_TRIS + tl;
+    const bool valid = t < nt;
     V3<double> v[3];
-    for (int j = 0; j < 3; ++j) {
-        int i = tris[3 * t + j];
-        v[j] = v3(vd[3 * i], vd[3 * i + 1], vd[3 * i + 2]);
+    if (valid)
+        for (int j = 0; j < 3; ++j) {
+            int i = tris[3 * t + j];
+            v[j] = v3(vd[3 * i], vd[3 * i + 1], vd[3 * i + 2]);
+        }
+    if (!c.cfie) {
+        if (valid && combo < 6) {
+            V3<double> Is1;
+            double Is2;
+            efie_edge_integrals(v, combo % 3, combo >= 3, &Is1, &Is2);
+            double* o = sIs[tl][combo / 3][combo % 3];
+            o[0] = Is1.x;
+            o[1] = Is1.y;
+            o[2] = Is1.z;
+            o[3] = Is2;
+        }
+        __syncthreads();
     }
+    if (!valid) return;
+    const int id = 9 * t + combo, ef = combo / 3, es = combo % 3;
     V3<double> vf = v[ef], vs = v[es];
     if (c.cfie) {
         Cx<double> s = cfie_self(v, vf, vs, c);
         tab[id] = make_double2(s.re, s.im);
     } else {
-        Cx<double> a = efie_self(v, vf, vs, c, false);
-        Cx<double> b = efie_self(v, vf, vs, c, true);
+        Cx<double> a = efie_self(v, vf, vs, c, sIs[tl][0]);
+        Cx<double> b = efie_self(v, vf, vs, c, sIs[tl][1]);
         Cx<double> sg = efie_sigma(v, vf, vs, c);
         tab[3 * id] = make_double2(a.re, a.im);
         tab[3 * id + 1] = make_double2(b.re, b.im);
@@ -543,7 +584,8 @@ emfa_status_t build_singular_table(Ctx* c, Geom* g, const emfa_fill_params_t* p,
     sc.sig_im = p->sigma_im;
     sc.cfie = cfie;
     const int* tris = p->precision == EMFA_F64 ? dptr<int>(g->g64.tris) : dptr<int>(g->g32.tris);
-    k_singular_table<<<(9 * g->nt + 127) / 128, 128, 0, st>>>(dptr<double>(g->vd), tris, g->nt, sc, tab);
+    k_singular_table<<<(g->nt + SING_TRIS - 1) / SING_TRIS, 9 * SING_TRIS, 0, st>>>(dptr<double>(g->vd), tris, g->nt,
+                                                                                   sc, tab);
     c->kernel_launches += 1;
     EMFA_CUDA(c, cudaGetLastError());
     return EMFA_OK;
