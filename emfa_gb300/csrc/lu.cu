@@ -14,11 +14,15 @@
 //                 A12 through the permutation), and their split-FP16
 //                 operand planes, scaled per column / row by powers of two
 //   k_lu_update_tc  A22 -= L21 U12 on the tensor cores (tcgen05, K = 128
-//                 real), tiles of 256 rows x 64 complex columns of A22 moved
-//                 through shared memory by TMA
+//                 real per block), tiles of 256 rows x 64 complex columns of
+//                 A22 moved through shared memory by TMA
 // with a one-block lookahead: the next block's 64 columns are updated first,
 // and that block's k_lu_diag (one CTA, latency bound) runs on a high-priority
-// stream while the remaining columns are updated.  The row exchanges reach
+// stream while the remaining columns are updated.  While two or more blocks
+// follow, blocks go in pairs: the first block updates only the second
+// block's columns and rows, and one pass with both blocks' panels
+// (k_lu_pack2, K = 128 complex) updates the rest, so A22 is read and
+// written once per two blocks.  The row exchanges reach
 // the columns left of each block in one pass at the end (k_lu_rowperm_left).
 // Rows of the factor are padded to an even number of complex elements
 // (16-byte TMA strides).
@@ -794,7 +798,7 @@ __global__ void k_lu_gather(const float2* __restrict__ B, const int* __restrict_
     W[id] = B[(size_t)r * n + perm[i]];
 }
 
-constexpr int RC = 8;  // right-hand sides per CTA of a sweep step
+constexpr int RC = 8;  // right-hand sides per CTA of a triangular solve
 
 // Both triangular solves as one launch each, in wavefront order.  A CTA
 // takes a ticket when it starts: ticket t is row block t of the forward (L)
