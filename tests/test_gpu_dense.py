@@ -209,6 +209,26 @@ def test_dense_rcs_end_to_end_vs_reference(ctx):
         assert np.linalg.norm(I[0] - Istar) / np.linalg.norm(Istar) < 1e-4
 
 
+def test_dense_rcs_jobs_of_different_sizes_share_the_context(ctx):
+    """emfa_dense_rcs keeps Z, V and X in the context's workspace between
+    jobs: jobs that grow and shrink in one context give what each gives in a
+    context of its own."""
+    from emfa_gb300 import api
+    fp = api.fill_params("cfie", "f32", 3e8, 0.5)
+    sp = api.solver_params("gmres", tol=1e-6)
+    ang = np.array([[0.0, 0.0, 0.0], [90.0, 30.0, 0.0]])
+    dirs = api.bistatic_dirs()
+    meshes = [M.icosphere(2, 0.3), M.icosphere(3, 0.5), M.icosphere(2, 0.3)]
+    shared = [api.dense_rcs(ctx, m, fp, ang, sp, dirs)[0] for m in meshes]
+    for m, got in zip(meshes, shared):
+        own = api.Context(0)
+        try:
+            alone = api.dense_rcs(own, m, fp, ang, sp, dirs)[0]
+        finally:
+            own.close()
+        assert np.abs(got - alone).max() < 1e-6, np.abs(got - alone).max()
+
+
 @pytest.mark.parametrize("n,r", [(128, 4), (256, 32), (998, 37), (1920, 360)])
 def test_matvec_tf32_tensor_cores(ctx, n, r):
     """tcgen05 TF32 product against an FP64 product of the same inputs.
