@@ -190,6 +190,9 @@ def run_emfa(args, workload):
                "checked_incidences": int(len(sub_idx)),
                "plain_fp64_seconds_for_checked": round(t64, 3),
                "plain_fp64_solves_per_s": round(len(sub_idx) / t64, 3)}
+    torch.cuda.synchronize()
+    geo.close()  # geometry before its context, not left to the interpreter's shutdown
+    ctx.close()
     p50 = statistics.median(step_ms)
     p99 = float(np.percentile(step_ms, 99))
     return {
