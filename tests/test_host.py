@@ -52,6 +52,28 @@ def test_rwg_builder_open_mesh(emfa_lib, oracle_mod):
         assert {v1, v2, vp} == set(tris[tp]) and {v1, v2, vm} == set(tris[tm])
 
 
+@pytest.mark.parametrize("case", ["duplicated", "flipped", "both", "shuffled_both"])
+def test_rwg_builder_non_manifold_matches_oracle(emfa_lib, oracle_mod, case):
+    """Meshes where a directed edge is open in several triangles at once
+    (duplicated triangles) or never closes (flipped triangles): every open
+    half-edge that a later triangle's reversed edge matches is closed by it,
+    as the reference's scan does."""
+    from emfa_gb300 import api
+    rng = np.random.default_rng(len(case))
+    tris = M.icosphere(2, 1.0).tris.copy()
+    if case in ("duplicated", "both", "shuffled_both"):
+        tris = np.concatenate([tris, tris[rng.choice(len(tris), 12, replace=False)]])
+    if case in ("flipped", "both", "shuffled_both"):
+        idx = rng.choice(len(tris), 9, replace=False)
+        tris[idx] = tris[idx][:, ::-1]
+    if case == "shuffled_both":
+        tris = tris[rng.permutation(len(tris))]
+    tris = np.ascontiguousarray(tris, dtype=np.int32)
+    r = api.build_rwg(tris)
+    assert r.shape[0] > 0
+    assert np.array_equal(r, oracle_mod.build_rwg(tris))
+
+
 def test_rwg_builder_errors(emfa_lib):
     import ctypes
     tris = np.array([[0, 1, 1]], dtype=np.int32)
