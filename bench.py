@@ -389,7 +389,7 @@ def run_mlfma(args):
                       "converged": info.converged, "rel_residual": info.max_rel_residual, "sai": sai,
                       "roofline": {"bound": "hbm", "achieved": round(gbs, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
                                    "frac": round(gbs / peaks["hbm_gbs"], 4), "peak_source": src,
-                                   "algorithmic_bytes": b3, "model": "3-component patterns (this build)",
+                                   "algorithmic_bytes": b3, "model": "3-component patterns (x, y, z as stored)",
                                    "model_bytes_2comp_theta_phi": b2,
                                    "model_frac_2comp_theta_phi": round(b2 / (mv_ms * 1e-3) / 1e9 / peaks["hbm_gbs"], 4)}}))
 

@@ -224,7 +224,7 @@ void Mesh::loadMeshFile(const std::string& path)
 {
     std::string suffix = path.substr(path.find_last_of('.') + 1);
     if (suffix != "nas")
-        throw FileError("cannot identify mesh file type: " + suffix + " (this build reads .nas meshes)");
+        throw FileError("cannot identify mesh file type: " + suffix + " (only .nas meshes are read)");
     std::ifstream in(path);
     if (in.fail()) throw FileError("fail loading nas mesh file: " + path);
     const auto maxs = std::numeric_limits<std::streamsize>::max();
@@ -302,7 +302,7 @@ void EM::init(ConfigLoader* ploader)
     t_start_ = t_prev_ = std::chrono::steady_clock::now();
     rtype_ = ploader->getResultType();
     incidence_ = ploader->getInc();
-    if (rtype_ == policy::Rad) throw ConfigInvalid("this build computes scattering results (BistaticRCS)");
+    if (rtype_ == policy::Rad) throw ConfigInvalid("only scattering results (BistaticRCS) are computed");
     scattering_ = ploader->getSca();
     ploader->getNearfield();
     std::string mesh_file = ploader->getMeshPath();

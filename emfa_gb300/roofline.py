@@ -45,7 +45,7 @@ def mlfma_matvec_bytes(n: int, nnz: int, level_boxes, poles, comps: int = 3, nea
 
     level_boxes[l] counts the boxes of level l (0 = root); poles lists L for
     levels 2..finest, and a level samples K = 2 L^2 directions.
-    comps = 3 is this build's Cartesian patterns (the reference's).  comps = 2
+    comps = 3 is the Cartesian patterns stored here (the reference's layout).  comps = 2
     with near_index_bytes = 4 is the 2-component theta/phi byte model.
     """
     ks = [2 * p * p for p in poles]
