@@ -407,6 +407,137 @@ __global__ void __launch_bounds__(256) k_fill_tile(const RwgPack<float>* __restr
     Z[(size_t)f * ldz + s] = out;
 }
 
+// Symmetric EFIE fill (edm_mode 0 or 2): the regular part of an EFIE entry,
+//   sum over the triangle pairs of sum_pq (rf.rs/4 - 1/k^2) G(P_p, Q_q),
+// does not change when test and source trade places, so a CTA fills a tile
+// on or above the diagonal of tiles and, off the diagonal, the mirrored tile
+// from the same regular sums (staged through shared memory and stored a row
+// at a time).  The FP64 self terms of pairs that share a triangle are not
+// symmetric: the mirrored entry takes them from the table with the roles of
+// the two RWGs exchanged.  Far pairs zeroed under edm_mode 0 are zero both
+// ways (the centre distance is the same).
+__global__ void __launch_bounds__(256) k_fill_tile_sym(const RwgPack<float>* __restrict__ rw, int n,
+                                                       FillConst<float> c, const double2* __restrict__ sing,
+                                                       const float* __restrict__ tri_q3,
+                                                       const int* __restrict__ blk_tris,
+                                                       const int* __restrict__ blk_nt,
+                                                       const unsigned char* __restrict__ loc, int maxt, int nb,
+                                                       Cx<float>* __restrict__ Z, size_t ldz)
+{
+    extern __shared__ float4 sk[];  // [maxt][maxt][9] (G re, G im, R, 1/R)
+    float4* sqf = sk + (size_t)maxt * maxt * 9;  // test points [maxt][3]
+    float4* sqs = sqf + maxt * 3;                 // source points [maxt][3]
+    __shared__ Cx<float> zt[FT][FT + 1];          // the mirrored tile, [s][f]
+    // tile (bf, bs), bf <= bs, from the linear index: row bf holds nb - bf tiles
+    const long long li = blockIdx.x;
+    int bf = (int)(((2.0 * nb + 1.0) - sqrt((2.0 * nb + 1.0) * (2.0 * nb + 1.0) - 8.0 * (double)li)) / 2.0);
+    auto row0 = [&](int b) { return (long long)b * nb - (long long)b * (b - 1) / 2; };
+    while (bf > 0 && row0(bf) > li) --bf;
+    while (bf + 1 < nb && row0(bf + 1) <= li) ++bf;
+    const int bs = bf + (int)(li - row0(bf));
+    const int ntf = blk_nt[bf], nts = blk_nt[bs];
+    const int* tf_ids = blk_tris + (size_t)bf * maxt;
+    const int* ts_ids = blk_tris + (size_t)bs * maxt;
+    for (int i = threadIdx.x; i < ntf * 3; i += blockDim.x) {
+        const float* q = tri_q3 + 9 * (size_t)tf_ids[i / 3] + 3 * (i % 3);
+        sqf[i] = make_float4(q[0], q[1], q[2], 0.0f);
+    }
+    for (int i = threadIdx.x; i < nts * 3; i += blockDim.x) {
+        const float* q = tri_q3 + 9 * (size_t)ts_ids[i / 3] + 3 * (i % 3);
+        sqs[i] = make_float4(q[0], q[1], q[2], 0.0f);
+    }
+    __syncthreads();
+    for (int pr = threadIdx.x; pr < ntf * nts; pr += blockDim.x) {
+        const int tf = pr / nts, ts = pr - tf * nts;
+        float4* out = sk + ((size_t)tf * maxt + ts) * 9;
+#pragma unroll
+        for (int p = 0; p < 3; ++p) {
+            const float4 P = sqf[3 * tf + p];
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                const float4 Q = sqs[3 * ts + q];
+                V3<float> d = v3(P.x - Q.x, P.y - Q.y, P.z - Q.z);
+                float r = sqrtf(dot(d, d));
+                float rinv = 1.0f / r;
+                float sn, cs;
+                sincos_pi_taylor(r * c.kpi, &sn, &cs);
+                out[3 * p + q] = make_float4(cs * rinv, -sn * rinv, r, rinv);
+            }
+        }
+    }
+    __syncthreads();
+    const int ty = threadIdx.x >> 4, tx = threadIdx.x & 15;
+    const int f = bf * FT + ty, s = bs * FT + tx;
+    const bool mirror = bf != bs;
+    Cx<float> out = cx(0.0f, 0.0f), out_t = cx(0.0f, 0.0f);
+    if (f < n && s < n) {
+        const RwgPack<float>& F = rw[f];
+        const RwgPack<float>& S = rw[s];
+        bool zeroed = false;
+        if (c.edm_mode == 0) {
+            V3<float> fc = divr(v3(F.cen[0][0], F.cen[0][1], F.cen[0][2]) + v3(F.cen[1][0], F.cen[1][1], F.cen[1][2]), 2.0f);
+            V3<float> sc = divr(v3(S.cen[0][0], S.cen[0][1], S.cen[0][2]) + v3(S.cen[1][0], S.cen[1][1], S.cen[1][2]), 2.0f);
+            zeroed = norm(fc - sc) > c.thr_edm;
+        }
+        if (!zeroed) {
+            Cx<float> ze = cx(0.0f, 0.0f), zm = cx(0.0f, 0.0f);
+            double sr = 0.0, si = 0.0, sr_t = 0.0, si_t = 0.0;
+#pragma unroll 1
+            for (int a = 0; a < 2; ++a) {
+                const int lf = loc[2 * (size_t)f + a];
+                float P[3][3], vf[3], nf[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+                for (int i = 0; i < 3; ++i) {
+                    const float4 t = sqf[3 * lf + i];
+                    P[i][0] = t.x;
+                    P[i][1] = t.y;
+                    P[i][2] = t.z;
+                }
+#pragma unroll
+                for (int j = 0; j < 3; ++j) vf[j] = F.v[a][j];
+#pragma unroll 1
+                for (int b = 0; b < 2; ++b) {
+                    const float sgn = (a == b) ? 1.0f : -1.0f;
+                    if (F.tri[a] == S.tri[b]) {
+                        const int id = 9 * F.tri[a] + 3 * F.e[a] + S.e[b];
+                        const double2 v = sing[3 * id + ((a == 0 && b == 0) ? 0 : 1)];
+                        const double2 g = sing[3 * id + 2];
+                        sr += (double)sgn * v.x + g.x;
+                        si += (double)sgn * v.y + g.y;
+                        // the mirrored entry: test s (side b), source f (side a)
+                        const int it = 9 * S.tri[b] + 3 * S.e[b] + F.e[a];
+                        const double2 vt = sing[3 * it + ((b == 0 && a == 0) ? 0 : 1)];
+                        const double2 gt = sing[3 * it + 2];
+                        sr_t += (double)sgn * vt.x + gt.x;
+                        si_t += (double)sgn * vt.y + gt.y;
+                        continue;
+                    }
+                    const int ls = loc[2 * (size_t)s + b];
+                    float vs[3] = {S.v[b][0], S.v[b][1], S.v[b][2]};
+                    Cx<float> e = cx(0.0f, 0.0f), m = cx(0.0f, 0.0f);
+                    regular_pair_staged<false>(P, sqs + 3 * ls, vf, vs, nf, sk + ((size_t)lf * maxt + ls) * 9, c, e,
+                                               m);
+                    ze.re += sgn * e.re;
+                    ze.im += sgn * e.im;
+                }
+            }
+            const float kz = (float)c.coef_efie * (F.len * S.len);
+            float re = c.ce * ze.re + (float)sr, im = c.ce * ze.im + (float)si;
+            out = cx(-kz * im, kz * re);
+            re = c.ce * ze.re + (float)sr_t;
+            im = c.ce * ze.im + (float)si_t;
+            out_t = cx(-kz * im, kz * re);
+        }
+        Z[(size_t)f * ldz + s] = out;
+    }
+    if (!mirror) return;  // uniform over the CTA
+    zt[tx][ty] = out_t;  // Z[s][f]
+    __syncthreads();
+    // row s = bs 16 + ty of the mirrored tile, columns f = bf 16 + tx
+    const int sr_ = bs * FT + ty, fc_ = bf * FT + tx;
+    if (sr_ < n && fc_ < n) Z[(size_t)sr_ * ldz + fc_] = zt[ty][tx];
+}
+
 // per-geometry plan of the tiled fill (host, once)
 static emfa_status_t tile_plan(Ctx* c, Geom* g, cudaStream_t st)
 {
@@ -526,6 +657,7 @@ static emfa_status_t fill_z_t(Ctx* c, Geom* g, GeomDev<T>& d, const emfa_fill_pa
         const size_t sm = tile_smem(g->tile_maxt);
         EMFA_TRY(ensure_smem(c, k_fill_tile<true>, sm));
         EMFA_TRY(ensure_smem(c, k_fill_tile<false>, sm));
+        EMFA_TRY(ensure_smem(c, k_fill_tile_sym, sm));
         const dim3 grd((g->n + FT - 1) / FT, (g->n + FT - 1) / FT);
         const FillConst<float> fc32 = make_fill_const<float>(p);
         {
@@ -535,7 +667,13 @@ static emfa_status_t fill_z_t(Ctx* c, Geom* g, GeomDev<T>& d, const emfa_fill_pa
                     dptr<RwgPack<float>>(g->g32.rwg), g->n, fc32, (const double2*)tab, dptr<float>(g->g32.tri_q3),
                     dptr<float>(g->g32.tri_n), dptr<int>(g->tile_tris), dptr<int>(g->tile_nt),
                     dptr<unsigned char>(g->tile_loc), g->tile_maxt, reinterpret_cast<Cx<float>*>(Z), ldz);
-            else
+            else if (p->edm_mode != 1) {
+                const int nb = (g->n + FT - 1) / FT;
+                k_fill_tile_sym<<<(unsigned)((long long)nb * (nb + 1) / 2), 256, sm, st>>>(
+                    dptr<RwgPack<float>>(g->g32.rwg), g->n, fc32, (const double2*)tab, dptr<float>(g->g32.tri_q3),
+                    dptr<int>(g->tile_tris), dptr<int>(g->tile_nt), dptr<unsigned char>(g->tile_loc), g->tile_maxt,
+                    nb, reinterpret_cast<Cx<float>*>(Z), ldz);
+            } else
                 k_fill_tile<false><<<grd, 256, sm, st>>>(
                     dptr<RwgPack<float>>(g->g32.rwg), g->n, fc32, (const double2*)tab, dptr<float>(g->g32.tri_q3),
                     dptr<float>(g->g32.tri_n), dptr<int>(g->tile_tris), dptr<int>(g->tile_nt),
