@@ -10,6 +10,10 @@
 // vertex) and the frequency, so they are tabulated once per fill in FP64
 // (9 entries per triangle) and looked up by the entry kernel; the regular
 // pairs run in the fill precision (FP32 for the mixed path, FP64 plain).
+// FP32 entries come from tiled kernels (k_fill_tile: the kernel values of a
+// 16 x 16 block's triangle pairs staged once); the EFIE one, whose regular
+// part is symmetric, fills the upper triangle of tiles and mirrors it
+// (k_fill_tile_sym).
 #include "emfa_internal.cuh"
 #include "emfa_math.cuh"
 #include "fill_entry.cuh"
@@ -21,7 +25,8 @@
 namespace emfa {
 
 // ---------------------------------------------------------------------------
-// singular self terms, FP64, one thread per (triangle, field corner, source corner)
+// singular self terms, FP64, one thread per (triangle, field corner, source
+// corner); for EFIE the triangle's edge integrals are evaluated once first
 // ---------------------------------------------------------------------------
 struct SingConst {
     double k, inv_k2, w, alpha, z0, pi;
