@@ -39,7 +39,9 @@ typedef enum {
 
 typedef enum { EMFA_F32 = 0, EMFA_F64 = 1 } emfa_precision_t;
 typedef enum { EMFA_EFIE = 0, EMFA_CFIE = 1 } emfa_kind_t;
-/* EMFA_LU: dense only (emfa_solve, EMFA_F32): FP32 LU of Z, then FP64
+/* EMFA_LU: dense only (emfa_solve, EMFA_F32): FP32 LU of Z (row exchanges
+ * within 64-row diagonal blocks; trailing updates on the tensor cores with
+ * split-FP16 operands, about 2^-21 of the largest product term), then FP64
  * iterative refinement on the true residual, GMRES-IR if the refinement
  * stalls.  No counterpart in the reference, whose dense solves are iterative
  * (EMSolver/EFIE.cpp:89 has a commented-out Eigen LU). */
