@@ -169,6 +169,32 @@ def run_reference(mode, config_path, outdir, arg, prec=32, cwd=None, timeout=360
     return r.stdout
 
 
+def run_reference_args(mode, config_path, outdir, args, prec=32, timeout=7200):
+    """Run a harness mode that takes several trailing arguments (``big``,
+    ``rcs_of``), in a scratch cwd like run_reference."""
+    exe = ref_binary(prec)
+    if exe is None:
+        raise FileNotFoundError("reference binary not built (oracle/build_ref.sh)")
+    cwd = tempfile.mkdtemp(prefix="emfa_ref_")
+    r = subprocess.run([exe, mode, os.path.abspath(config_path), os.path.abspath(outdir)] + [str(a) for a in args],
+                       cwd=cwd, stdin=subprocess.DEVNULL, capture_output=True, text=True, timeout=timeout)
+    if r.returncode != 0:
+        raise RuntimeError("reference failed (%d): %s" % (r.returncode, r.stderr[-2000:]))
+    return r.stdout
+
+
+def closed_form_vector(n, a=7919, b=104729, prec=32):
+    """The seeded test vector of the harness's MLFMA mode with seed 0:
+    x_i = ((i a) mod 2001 - 1000) / 1000 + j ((i b) mod 2003 - 1001) / 1001,
+    each part one correctly rounded division, so numpy and the reference's
+    C++ give the same bits."""
+    dt = np.float32 if prec == 32 else np.float64
+    i = np.arange(n, dtype=np.int64)
+    re = ((i * a) % 2001 - 1000).astype(dt) / dt(1000)
+    im = ((i * b) % 2003 - 1001).astype(dt) / dt(1001)
+    return (re + 1j * im).astype(np.complex64 if prec == 32 else np.complex128)
+
+
 def time_reference(config_path, kind, rows, solve=0, prec=32, timeout=3600):
     exe = ref_binary(prec)
     cwd = tempfile.mkdtemp(prefix="emfa_ref_")

@@ -10,6 +10,9 @@
 //   emfa_ref_<f32|f64> mlfma <config> <outdir> <seed>
 //   emfa_ref_<f32|f64> time  <config> <efie|cfie> <rows> <solve:0|1>
 //   emfa_ref_<f32|f64> stages <config> <rows> <gemv_reps>
+//   emfa_ref_<f32|f64> big   <config> <outdir> <efie|cfie> <incfile> [solve:0|1]
+//   emfa_ref_<f32|f64> job   <config>
+//   emfa_ref_<f32|f64> rcs_of <config> <outdir> <efie|cfie> <ifile> <dirfile> <mono|bi|config>
 //
 // The harness calls the same member functions EFIE::solve (EFIE.cpp:54-99),
 // CFIE::solve (CFIE.cpp:53-88) and MLFMA::solve (MLFMA.cpp:67-106) call, in
@@ -25,6 +28,8 @@
 #include <list>
 #include <unordered_map>
 #include <random>
+#include <array>
+#include <string>
 #include <cstdio>
 #include <cstring>
 #include <experimental/filesystem>
@@ -251,7 +256,12 @@ static int run_mlfma(ConfigLoader& loader, unsigned seed)
     std::mt19937 gen(seed);
     std::uniform_real_distribution<double> U(-1.0, 1.0);
     Qcx_vec x(n);
-    for (int i = 0; i < n; ++i) x(i) = Complex((value_t)U(gen), (value_t)U(gen));
+    // seed 0: a closed form that numpy reproduces bit for bit (integers, then
+    // one correctly rounded division), so large fixtures need not store x
+    for (int i = 0; i < n; ++i)
+        x(i) = seed ? Complex((value_t)U(gen), (value_t)U(gen))
+                    : Complex((value_t)(((long long)i * 7919) % 2001 - 1000) / (value_t)1000,
+                              (value_t)(((long long)i * 104729) % 2003 - 1001) / (value_t)1001);
     dump("mv_x.bin", x.memptr(), n);
     Qcx_vec y = s.matrixVectorMultiply(x);
     dump("mv_y.bin", y.memptr(), n);
@@ -263,6 +273,199 @@ static int run_mlfma(ConfigLoader& loader, unsigned seed)
     dump("I.bin", s.I_.memptr(), n);
     dump_rcs(s);
     s.clear();  // joins the ThreadPool, as solver::invoke_solver does
+    return 0;
+}
+
+// Incidences for the multi-incidence modes: a text file of "theta phi pole"
+// lines (degrees).  Each one is applied through the reference's own
+// EM::init (EM.cpp:25-41) on the loader's dictionary, so the incidence
+// vectors are the ones a config with those values gives.
+static std::vector<std::array<std::string, 3>> read_incidences(const char* path)
+{
+    std::vector<std::array<std::string, 3>> out;
+    FILE* f = std::fopen(path, "r");
+    if (!f) { std::perror(path); std::exit(2); }
+    char a[64], b[64], c[64];
+    while (std::fscanf(f, "%63s %63s %63s", a, b, c) == 3) out.push_back({a, b, c});
+    std::fclose(f);
+    return out;
+}
+
+static void set_incidence(ConfigLoader& loader, EM& s, const std::array<std::string, 3>& inc)
+{
+    loader.dict_.at("theta:").value = inc[0];
+    loader.dict_.at("phi:").value = inc[1];
+    loader.dict_.at("pole:").value = inc[2];
+    s.EM::init(&loader);
+}
+
+// Solver-specific access for the multi-incidence modes: EFIE solves
+// Z_eigen/V_eigen/I_eigen (EFIE.cpp:79), CFIE its Armadillo Z/V/I (CFIE.cpp:76).
+static void fill_z_rows(EFIE& e, int n, std::vector<Complex>& zb)
+{
+    e.Z.zeros(n, n);
+    e.Z_eigen.setZero(n, n);
+    e.fillZ();
+    for (int f = 0; f < n; ++f)
+        for (int c = 0; c < n; ++c) zb[(size_t)f * n + c] = e.Z_eigen(f, c);
+}
+
+static void fill_z_rows(CFIE& s, int n, std::vector<Complex>& zb)
+{
+    s.fillZ();
+    for (int f = 0; f < n; ++f)
+        for (int c = 0; c < n; ++c) zb[(size_t)f * n + c] = s.Z(f, c);
+}
+
+static const Complex* fill_v_once(EFIE& e, int n)
+{
+    e.V.zeros(n);
+    e.V_eigen.setZero(n);
+    e.fillV();
+    return e.V_eigen.data();
+}
+
+static const Complex* fill_v_once(CFIE& s, int)
+{
+    s.fillV();
+    return s.V.memptr();
+}
+
+static void set_current(EFIE& e, int n, const Complex* c)
+{
+    e.I_eigen.resize(n);
+    for (int u = 0; u < n; ++u) e.I_eigen(u) = c[u];
+}
+
+static void set_current(CFIE& s, int n, const Complex* c)
+{
+    s.I.set_size(n);
+    for (int u = 0; u < n; ++u) s.I(u) = c[u];
+}
+
+// Full-size dense dump: one fill, then the excitation of every incidence in
+// <incfile>.  Writes Z.bin (row-major, the matrix the reference solves),
+// V.bin (incidence-major), inc.bin (k, e, h, wavenumber per incidence).
+static int stock_solve(EFIE&, int) { return -1; }
+
+// CFIE::solve's own solve (CFIE.cpp:76): BiCGStab to 0.01, at most 500 steps
+static int stock_solve(CFIE& s, int)
+{
+    int iters = 0;
+    iml::BICGSTAB(s.Z, s.V, s.I, 0.01f, 500, iters);
+    return iters;
+}
+
+template <typename S>
+static int run_big(ConfigLoader& loader, const char* incfile, bool solve)
+{
+    S s;
+    s.init(&loader);
+    dump_geometry(s);
+    int n = s.unknowns_;
+    auto incs = read_incidences(incfile);
+    std::vector<Complex> zb((size_t)n * n), vall;
+    std::vector<value_t> incv;
+    fill_z_rows(s, n, zb);
+    dump("Z.bin", zb.data(), zb.size());
+    std::vector<Complex>().swap(zb);
+    std::vector<int> iters;
+    for (auto& inc : incs) {
+        set_incidence(loader, s, inc);
+        const Complex* v = fill_v_once(s, n);
+        vall.insert(vall.end(), v, v + n);
+        if (solve) iters.push_back(stock_solve(s, n));
+        value_t iv[10] = {s.inc_k_.x, s.inc_k_.y, s.inc_k_.z, s.inc_e_.x, s.inc_e_.y, s.inc_e_.z,
+                          s.inc_h_.x, s.inc_h_.y, s.inc_h_.z, s.k_};
+        incv.insert(incv.end(), iv, iv + 10);
+    }
+    dump("V.bin", vall.data(), vall.size());
+    dump("inc.bin", incv.data(), incv.size());
+    if (solve) dump("iters.bin", iters.data(), iters.size());
+    return 0;
+}
+
+// One stock CFIE job of the reference as one process runs it, timed per
+// stage with the reference's own functions in CFIE::solve / CFIE::output
+// order (CFIE.cpp:53-88): init (mesh + RWG), fillZ, fillV, BiCGStab to 0.01,
+// then the RCS in the monostatic direction -k_inc through getBiRCS.  Prints
+// one JSON record.
+static int run_job(ConfigLoader& loader)
+{
+    using clk = std::chrono::steady_clock;
+    auto sec = [](clk::time_point a) { return std::chrono::duration<double>(clk::now() - a).count(); };
+    auto t0 = clk::now();
+    CFIE s;
+    s.init(&loader);
+    const double t_init = sec(t0);
+    t0 = clk::now();
+    s.fillZ();
+    const double t_fill = sec(t0);
+    t0 = clk::now();
+    s.fillV();
+    const double t_fillv = sec(t0);
+    t0 = clk::now();
+    int iters = 0;
+    const bool ok = iml::BICGSTAB(s.Z, s.V, s.I, 0.01f, 500, iters);
+    const double t_solve = sec(t0);
+    t0 = clk::now();
+    const value_t rcs = s.getBiRCS(VectorR3(-s.inc_k_.x, -s.inc_k_.y, -s.inc_k_.z));
+    const double t_rcs = sec(t0);
+    std::printf("{\"n\": %d, \"init_s\": %.6f, \"fill_s\": %.6f, \"fillv_s\": %.6f, \"solve_s\": %.6f, "
+                "\"rcs_s\": %.6f, \"iters\": %d, \"converged\": %d, \"rcs_db\": %.6f}\n",
+                s.unknowns_, t_init, t_fill, t_fillv, t_solve, t_rcs, iters, ok ? 1 : 0, (double)rcs);
+    return 0;
+}
+
+// RCS of given currents through the reference's getBiRCS (EFIE.cpp:788-832,
+// CFIE.cpp:643-685): <ifile> holds n_cur currents of the solver's order
+// (binary Complex), <dirfile> n_dir directions (x y z per line).  "mono":
+// current i at direction i (n_cur == n_dir); "bi": every current at every
+// direction; "config": every current at the config's bistatic directions
+// (dirfile unused).
+template <typename S>
+static int run_rcs_of(ConfigLoader& loader, const char* ifile, const char* dirfile, const std::string& pairing)
+{
+    S s;
+    s.init(&loader);
+    int n = s.unknowns_;
+    std::vector<Complex> cur;
+    {
+        FILE* f = std::fopen(ifile, "rb");
+        if (!f) { std::perror(ifile); std::exit(2); }
+        Complex c;
+        while (std::fread(&c, sizeof c, 1, f) == 1) cur.push_back(c);
+        std::fclose(f);
+    }
+    std::vector<VectorR3> dirs;
+    if (pairing == "config") {  // the config's bistatic directions (Result.h:59-98)
+        dirs = rcs_directions(s.scattering_);
+        std::vector<value_t> kd;
+        for (auto& d : dirs) { kd.push_back(d.x); kd.push_back(d.y); kd.push_back(d.z); }
+        dump("rcs_dirs.bin", kd.data(), kd.size());
+    } else {
+        FILE* f = std::fopen(dirfile, "r");
+        if (!f) { std::perror(dirfile); std::exit(2); }
+        double x, y, z;
+        while (std::fscanf(f, "%lf %lf %lf", &x, &y, &z) == 3)
+            dirs.emplace_back((value_t)x, (value_t)y, (value_t)z);
+        std::fclose(f);
+    }
+    size_t n_cur = cur.size() / n;
+    if (pairing == "mono" && n_cur != dirs.size()) {
+        std::fprintf(stderr, "rcs_of: %zu currents, %zu directions\n", n_cur, dirs.size());
+        return 1;
+    }
+    std::vector<value_t> out;
+    for (size_t i = 0; i < n_cur; ++i) {
+        set_current(s, n, &cur[i * n]);
+        if (pairing == "mono") {
+            out.push_back(s.getBiRCS(dirs[i]));
+        } else {
+            for (auto& d : dirs) out.push_back(s.getBiRCS(d));
+        }
+    }
+    dump("rcs.bin", out.data(), out.size());
     return 0;
 }
 
@@ -359,8 +562,8 @@ static int run_stages(ConfigLoader& loader, int rows, int reps)
 
 int main(int argc, char** argv)
 {
-    if (argc < 4) {
-        std::fprintf(stderr, "usage: %s rwg|efie|cfie|mlfma|time <config> <outdir|kind> [arg]\n", argv[0]);
+    if (argc < 3 || (argc < 4 && std::string(argv[1]) != "job")) {
+        std::fprintf(stderr, "usage: %s rwg|efie|cfie|mlfma|time|stages|big|rcs_of|job <config> ...\n", argv[0]);
         return 1;
     }
     std::string mode = argv[1];
@@ -369,6 +572,7 @@ int main(int argc, char** argv)
         loader.load(argv[2]);
         if (mode == "time")
             return run_time(loader, argv[3], argc > 4 ? std::atoi(argv[4]) : 64, argc > 5 ? std::atoi(argv[5]) : 0);
+        if (mode == "job") return run_job(loader);
         if (mode == "stages")
             return run_stages(loader, std::atoi(argv[3]), argc > 4 ? std::atoi(argv[4]) : 3);
         g_out = argv[3];
@@ -382,6 +586,16 @@ int main(int argc, char** argv)
         if (mode == "efie") return run_efie(loader, argc > 4 ? std::atof(argv[4]) : 1e-3);
         if (mode == "cfie") return run_cfie(loader, argc > 4 ? std::atof(argv[4]) : 1e-2);
         if (mode == "mlfma") return run_mlfma(loader, argc > 4 ? (unsigned)std::atoi(argv[4]) : 1u);
+        if (mode == "big" && argc > 5) {
+            std::string kind = argv[4];
+            const bool solve = argc > 6 && std::atoi(argv[6]) != 0;
+            return kind == "efie" ? run_big<EFIE>(loader, argv[5], solve) : run_big<CFIE>(loader, argv[5], solve);
+        }
+        if (mode == "rcs_of" && argc > 7) {
+            std::string kind = argv[4];
+            return kind == "efie" ? run_rcs_of<EFIE>(loader, argv[5], argv[6], argv[7])
+                                  : run_rcs_of<CFIE>(loader, argv[5], argv[6], argv[7]);
+        }
     } catch (const std::exception& e) {
         std::fprintf(stderr, "reference error: %s\n", e.what());
         return 3;

@@ -123,3 +123,45 @@ def test_oracle_vs_live_reference(oracle_mod, solver):
         inc = O.incidence(60, 10, 90, prec)
         V = O.fill_v(geo, k, inc, cfie=solver == "cfie", alpha=cfg_float(0.6))[0]
         assert np.abs(V - d["V"]).max() <= (1e-14 if prec == 64 else 1e-6) * np.abs(d["V"]).max()
+
+
+@pytest.mark.parametrize("name", ["c1_efie_sphere_1920", "c2_cfie_sphere_7680"])
+def test_config_fixture_is_self_consistent(name):
+    """The full-size fixtures: Z times the closed-form vectors agrees with the
+    stored rows; I* solves the FP64 system; the mesh generator still gives
+    the mesh the reference ran on."""
+    import hashlib
+    from emfa_gb300 import mesh as M
+    from oracle import oracle as O
+    g = load_golden(name)
+    n = g["Zrows_f64"].shape[1]
+    xs = np.stack([O.closed_form_vector(n, prec=64), O.closed_form_vector(n, 6007, 15485863, prec=64)])
+    rows = g["Zrows_index"]
+    for tag, tol in (("f64", 1e-13), ("f32", 1e-6)):
+        part = (g["Zrows_" + tag].astype(np.complex128) @ xs.T).T
+        assert np.abs(part - g["Zx_" + tag][:, rows]).max() <= tol * np.abs(part).max()
+    assert float(g["Istar_resid"]) < 1e-12
+    m = (M.icosphere(3, 0.5) if name.startswith("c1") else M.icosphere(4, 1.0))
+    h = hashlib.sha256()
+    h.update(np.ascontiguousarray(m.verts, dtype=np.float64).tobytes())
+    h.update(np.ascontiguousarray(m.tris, dtype=np.int32).tobytes())
+    assert h.hexdigest() == str(g["mesh_sha256"])
+    rwg = O.build_rwg(m.tris)
+    assert hashlib.sha256(np.ascontiguousarray(rwg, dtype=np.int32).tobytes()).hexdigest() == str(g["rwg_sha256"])
+
+
+def test_mie_series():
+    """The analytic PEC-sphere series: the Rayleigh limit (backscatter
+    9 pi a^2 (ka)^4 as ka -> 0) and the reference's C1 discretisation,
+    which it must bound within 0.2 dB over all 541 directions."""
+    from oracle import mie
+    a, f = 0.01, 3e8  # ka = 0.063
+    k = 2 * np.pi * f / 299792458.0
+    back = mie.pec_sphere_rcs_db(a, f, [0, 0, -1.0], [1.0, 0, 0], [[0, 0, 1.0]])[0]
+    rayleigh = 10 * np.log10(9 * np.pi * a * a * (k * a) ** 4)
+    assert abs(back - rayleigh) < 0.05, (back, rayleigh)
+    g = load_golden("c1_efie_sphere_1920")
+    inc = g["inc_f64"][0]
+    exact = mie.pec_sphere_rcs_db(0.5, 3e8, inc[:3], inc[3:6], g["rcs_dirs_f64"])
+    err = np.abs(g["rcs_f64"][0] - exact)
+    assert err.max() < 0.2 and np.median(err) < 0.1, (err.max(), np.median(err))
