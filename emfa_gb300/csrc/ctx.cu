@@ -63,7 +63,9 @@ emfa_status_t ctx_alloc(Ctx* c, size_t bytes, void** p)
         c->used += bytes;
         if (c->used > c->peak) c->peak = c->used;
     }
-    cudaError_t e = c->stream_ordered ? cudaMallocAsync(p, bytes, c->stream) : cudaMalloc(p, bytes);
+    cudaError_t e = !c->stream_ordered ? cudaMalloc(p, bytes)
+                    : c->pool           ? cudaMallocFromPoolAsync(p, bytes, c->pool, c->stream)
+                                        : cudaMallocAsync(p, bytes, c->stream);
     if (e != cudaSuccess) {
         std::lock_guard<std::mutex> g(c->mu);
         c->used -= bytes;
@@ -99,6 +101,39 @@ TimedLaunch::TimedLaunch(Ctx* c, int id, cudaStream_t st, double work) : c_(c), 
 TimedLaunch::~TimedLaunch()
 {
     if (stop_) cudaEventRecord(stop_, st_);
+}
+
+namespace {
+std::mutex& refs_mutex()
+{
+    static std::mutex m;
+    return m;
+}
+}  // namespace
+
+void ctx_retain(Ctx* c)
+{
+    std::lock_guard<std::mutex> g(refs_mutex());
+    c->refs += 1;
+}
+
+void ctx_release(Ctx* c)
+{
+    {
+        std::lock_guard<std::mutex> g(refs_mutex());
+        if (--c->refs > 0) return;
+    }
+    cudaSetDevice(c->device);
+    if (c->stream) {
+        cudaStreamSynchronize(c->stream);
+        cudaStreamDestroy(c->stream);
+    }
+    for (auto& t : c->timers) {
+        for (auto e : t.start) cudaEventDestroy(e);
+        for (auto e : t.stop) cudaEventDestroy(e);
+    }
+    if (c->pinned) cudaFreeHost(c->pinned);
+    delete static_cast<emfa_ctx_t*>(c);
 }
 
 emfa_status_t ctx_workspace(Ctx* c, int slot, size_t bytes, void** p)
@@ -196,19 +231,12 @@ emfa_status_t emfa_ctx_destroy(emfa_ctx_t* ctx)
 {
     if (!ctx) return EMFA_ERR_INVALID;
     cudaSetDevice(ctx->device);
-    // buffers first: stream-ordered ones are freed on the context's stream
+    // the context's own buffers now (stream-ordered ones are freed on its
+    // stream); the stream and the struct when no geometry or operator holds it
     for (auto& b : ctx->ws) b.release();
     for (auto& kv : ctx->user_bufs) ctx_free(ctx, kv.first, kv.second);
-    if (ctx->stream) {
-        cudaStreamSynchronize(ctx->stream);
-        cudaStreamDestroy(ctx->stream);
-    }
-    for (auto& t : ctx->timers) {
-        for (auto e : t.start) cudaEventDestroy(e);
-        for (auto e : t.stop) cudaEventDestroy(e);
-    }
-    if (ctx->pinned) cudaFreeHost(ctx->pinned);
-    delete ctx;
+    ctx->user_bufs.clear();
+    ctx_release(ctx);
     return EMFA_OK;
 }
 

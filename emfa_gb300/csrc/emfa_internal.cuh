@@ -102,6 +102,11 @@ struct KernelTimer {
 };
 
 struct Ctx {
+    // Handles that hold this context: the caller's (until emfa_ctx_destroy)
+    // and one per live geometry or MLFMA operator.  The stream, events and the
+    // struct itself go when the last one is dropped, so a child destroyed after
+    // its context (finalizers in any order) still finds them.
+    int refs = 1;
     int device = 0;
     size_t budget = 0;      // bytes the context may hold (0 = unlimited)
     size_t used = 0;
@@ -112,6 +117,7 @@ struct Ctx {
     int sm_count = 0;
     long long kernel_launches = 0;  // kernels launched through this context
     bool stream_ordered = false;  // allocations on `stream` (cudaMallocAsync), for lanes of the server
+    cudaMemPool_t pool = nullptr;  // with stream_ordered: the pool to allocate from (null: the device's)
     bool time_kernels = false;
     KernelTimer timers[KT_COUNT];
     DevBuf ws[WS_COUNT];            // declared after mu: destroyed before it
@@ -120,6 +126,10 @@ struct Ctx {
 };
 
 emfa_status_t ctx_workspace(Ctx* c, int slot, size_t bytes, void** p);
+
+// Reference counting of a context by the objects created on it (ctx.cu).
+void ctx_retain(Ctx* c);
+void ctx_release(Ctx* c);
 
 // Raises the kernel's dynamic shared-memory limit on the context's device to
 // at least `bytes`; the limit never goes down.  Lanes of the server launch
@@ -193,6 +203,7 @@ struct GeomDev {
 
 struct Geom {
     Ctx* ctx = nullptr;
+    int refs = 1;  // the caller's handle + one per MLFMA operator built on it
     int nv = 0, nt = 0, n = 0;
     std::vector<double> verts;   // host, V x 3
     std::vector<int> tris;       // host, T x 3
@@ -215,6 +226,10 @@ emfa_status_t geom_vd(Geom* g, cudaStream_t st);
 
 emfa_status_t geom_prepare_f32(Geom* g, cudaStream_t st);
 emfa_status_t geom_prepare_f64(Geom* g, cudaStream_t st);
+// Reference counting of a geometry by the MLFMA operators built on it
+// (geom.cu); the last release frees it and drops its hold on the context.
+void geom_retain(Geom* g);
+void geom_release(Geom* g);
 
 // RWG (common edge) construction, EMComponent/CommonEdge.cpp:74-106,704-743
 int build_rwg_host(const int* tris, int n_tri, std::vector<int>& rwg_out, std::string* err);

@@ -212,6 +212,26 @@ static emfa_status_t geom_prepare(Geom* g, GeomDev<T>& d, cudaStream_t st)
 emfa_status_t geom_prepare_f32(Geom* g, cudaStream_t st) { return geom_prepare<float>(g, g->g32, st); }
 emfa_status_t geom_prepare_f64(Geom* g, cudaStream_t st) { return geom_prepare<double>(g, g->g64, st); }
 
+void geom_retain(Geom* g)
+{
+    std::lock_guard<std::mutex> lk(g->ctx->mu);
+    g->refs += 1;
+}
+
+// The geometry's device arrays are freed through its context, which it
+// holds until then; the context may already be closed by its caller.
+void geom_release(Geom* g)
+{
+    Ctx* c = g->ctx;
+    {
+        std::lock_guard<std::mutex> lk(c->mu);
+        if (--g->refs > 0) return;
+    }
+    cudaSetDevice(c->device);
+    delete static_cast<emfa_geom_t*>(g);
+    ctx_release(c);
+}
+
 }  // namespace emfa
 
 using namespace emfa;
@@ -267,6 +287,7 @@ emfa_status_t emfa_geom_create(emfa_ctx_t* ctx, const double* verts_host, int n_
     }
     emfa_geom_t* g = new emfa_geom_t();
     g->ctx = ctx;
+    ctx_retain(ctx);
     g->nv = n_vert;
     g->nt = n_tri;
     g->n = n_rwg;
@@ -280,8 +301,7 @@ emfa_status_t emfa_geom_create(emfa_ctx_t* ctx, const double* verts_host, int n_
 emfa_status_t emfa_geom_destroy(emfa_geom_t* geom)
 {
     if (!geom) return EMFA_ERR_INVALID;
-    cudaSetDevice(geom->ctx->device);
-    delete geom;
+    geom_release(geom);
     return EMFA_OK;
 }
 

@@ -1548,6 +1548,9 @@ emfa_status_t emfa_mlfma_create(emfa_ctx_t* ctx, emfa_geom_t* geom, const emfa_m
         delete M;
         return s;
     }
+    // the operator holds its geometry (and through it the context) until it
+    // is destroyed, whatever order the caller closes them in
+    geom_retain(geom);
     *out = M;
     return EMFA_OK;
 }
@@ -1581,7 +1584,9 @@ emfa_status_t emfa_mlfma_destroy(emfa_mlfma_t* M)
     if (!M) return EMFA_ERR_INVALID;
     cudaSetDevice(M->ctx->device);
     cudaStreamSynchronize(M->ctx->stream);
+    emfa::Geom* g = M->geom;
     delete M;
+    geom_release(g);
     return EMFA_OK;
 }
 
