@@ -59,7 +59,7 @@ class RequestResult(ctypes.Structure):
 
 class ServeOpts(ctypes.Structure):
     _fields_ = [("lanes", ctypes.c_int), ("hbm_budget", ctypes.c_size_t), ("dense_max", ctypes.c_int),
-                ("realtime", ctypes.c_int)]
+                ("realtime", ctypes.c_int), ("max_wait_s", ctypes.c_double)]
 
 
 class SolveInfo(ctypes.Structure):

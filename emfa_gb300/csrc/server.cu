@@ -8,8 +8,12 @@
 //   admitter   a request becomes visible at its arrival time; a free lane
 //              takes the oldest visible request whose device-memory estimate
 //              fits in what the running requests leave of the budget, else
-//              the oldest one that fits; a request larger than the whole
-//              budget runs alone once nothing else does
+//              the oldest one that fits; a request that has waited
+//              max_wait_s holds later ones back until it fits; a request
+//              larger than the whole budget runs alone once nothing else does
+//   memory     lanes allocate stream-ordered from one memory pool created for
+//              the run (not the device's default pool, which other users of
+//              cudaMallocAsync in the process share), destroyed at its end
 //   methods    dense up to dense_max unknowns: fill, then CFIE split-FP16
 //              GMRES(30)-IR to 1e-6, EFIE FP32 LU with FP64 refinement to
 //              1e-5 by default, then RCS; MLFMA (CFIE operator, GMRES(30) to
@@ -49,6 +53,7 @@ struct Engine {
     std::mutex mu;
     std::condition_variable cv;
     Clock::time_point t0;
+    cudaMemPool_t pool = nullptr;  // the lanes' stream-ordered allocations
     double now() const { return std::chrono::duration<double>(Clock::now() - t0).count(); }
     double arrival(int i) const { return arr[i]; }
 };
@@ -75,7 +80,11 @@ size_t estimate_bytes(const emfa_request_t& r, int dense_max, int* method)
     return (size_t)(b * 1.1) + (64u << 20);
 }
 
-// oldest visible request that fits; else, with nothing running, the oldest visible one
+// The oldest visible request that fits; else the oldest later one that fits;
+// else, with nothing running, the oldest visible one.  Once the oldest
+// visible request has waited max_wait_s without fitting, later ones are held
+// back until it fits, so a large request cannot starve behind a stream of
+// small ones that never lets the budget drain.
 int choose(Engine& E, double t)
 {
     const size_t budget = E.o.hbm_budget;
@@ -83,8 +92,11 @@ int choose(Engine& E, double t)
     for (int i : E.order) {
         if (E.taken[i]) continue;
         if (E.arrival(i) > t) break;
-        if (oldest < 0) oldest = i;
         if (E.in_use + E.est[i] <= budget) return i;
+        if (oldest < 0) {
+            oldest = i;
+            if (t - E.arrival(i) >= E.o.max_wait_s) break;
+        }
     }
     if (oldest >= 0 && E.running == 0) return oldest;
     return -1;
@@ -194,7 +206,10 @@ void lane_main(Engine* E, int lane)
     cudaSetDevice(E->device);
     emfa_ctx_t* ctx = nullptr;
     const emfa_status_t cs = emfa_ctx_create(E->device, 0, &ctx);
-    if (cs == EMFA_OK) ctx->stream_ordered = true;
+    if (cs == EMFA_OK) {
+        ctx->stream_ordered = true;
+        ctx->pool = E->pool;
+    }
     for (;;) {
         int pick = -1;
         {
@@ -262,6 +277,7 @@ extern "C" emfa_status_t emfa_serve(int device, const emfa_request_t* reqs, int 
     E.o.lanes = std::min(E.o.lanes, 64);
     if (E.o.hbm_budget == 0) E.o.hbm_budget = (size_t)150 << 30;
     if (E.o.dense_max <= 0) E.o.dense_max = 10000;
+    if (!(E.o.max_wait_s > 0)) E.o.max_wait_s = 2.0;
     E.est.resize(n_req);
     E.method.resize(n_req);
     E.arr.resize(n_req);
@@ -280,27 +296,23 @@ extern "C" emfa_status_t emfa_serve(int device, const emfa_request_t* reqs, int 
         if (E.arrival(a) != E.arrival(b)) return E.arrival(a) < E.arrival(b);
         return E.est[a] > E.est[b];
     });
-    // lanes free and reallocate per problem: keep freed memory in the pool
-    // (this process's pool: the threshold and the cached memory go back at the end)
+    // lanes free and reallocate per problem: a pool of the run's own keeps
+    // freed memory for the next problem (release threshold at its maximum);
+    // it is destroyed, with what it holds, when the run ends
     cudaSetDevice(device);
-    cudaMemPool_t pool = nullptr;
-    uint64_t old_thr = 0;
-    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
-        cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &old_thr);
-        uint64_t thr = UINT64_MAX;
-        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
-    } else {
-        pool = nullptr;
-    }
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = device;
+    EMFA_CUDA(nullptr, cudaMemPoolCreate(&E.pool, &props));
+    uint64_t thr = UINT64_MAX;
+    cudaMemPoolSetAttribute(E.pool, cudaMemPoolAttrReleaseThreshold, &thr);
     E.t0 = Clock::now();
     std::vector<std::thread> th;
     for (int l = 0; l < E.o.lanes; ++l) th.emplace_back(lane_main, &E, l);
     for (auto& t : th) t.join();
-    if (pool) {
-        cudaDeviceSynchronize();
-        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &old_thr);
-        cudaMemPoolTrimTo(pool, 0);
-    }
+    cudaDeviceSynchronize();  // the lanes' asynchronous frees have completed
+    cudaMemPoolDestroy(E.pool);
     return EMFA_OK;
 }
 
@@ -313,6 +325,7 @@ extern "C" emfa_status_t emfa_serve_simulate(const double* arrival, const double
     if (opts) E.o = *opts;
     if (E.o.lanes <= 0) E.o.lanes = 6;
     if (E.o.hbm_budget == 0) E.o.hbm_budget = (size_t)150 << 30;
+    if (!(E.o.max_wait_s > 0)) E.o.max_wait_s = 2.0;
     E.est.assign(bytes, bytes + n);
     E.arr.resize(n);
     E.taken.assign(n, 0);

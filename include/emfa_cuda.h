@@ -200,13 +200,16 @@ emfa_status_t emfa_matvec(emfa_ctx_t* ctx, int prec, int matvec, const void* Z_d
  * n * n_rhs <= EMFA_NOALLOC_MAX_ELEMS; larger products return
  * EMFA_ERR_INVALID with a message saying so (use emfa_matvec for them).
  * The first call on a device, made with that device current, looks the array
- * up (loading this part of the library's device code there) and sets the
- * kernels' shared-memory limit; make that first call before any stream
- * capture.  Calls on one device share the array, so two calls that overlap in
+ * up and sets the kernels' shared-memory limit; make that first call before
+ * any stream capture.  With lazy module loading (the CUDA default) that first
+ * call is also when the driver loads this part of the library's device code
+ * on the device and reserves the array (16 MiB and one 256-byte line); the
+ * array then stays reserved until the process exits, and later calls reserve
+ * nothing.  Calls on one device share the array, so two calls that overlap in
  * time (different streams, or different host threads) race and corrupt each
- * other's result: order them.  stream NULL is the default stream; the call
- * synchronises `stream` before it returns, to read the kernel's error word.
- * Errors are reported through emfa_last_error(NULL). */
+ * other's result: order them.  stream NULL is the default stream; every call
+ * copies the kernel's error word to host memory and synchronises `stream`
+ * before it returns.  Errors are reported through emfa_last_error(NULL). */
 emfa_status_t emfa_matvec_tf32_noalloc(const void* Z_dev, int n, const void* X_dev, int n_rhs, void* Y_dev,
                                        void* stream);
 
@@ -395,6 +398,8 @@ typedef struct {
     size_t hbm_budget;        /* admission budget in bytes; 0 = 150 GB                    */
     int dense_max;            /* largest dense problem (unknowns); 0 = 10000              */
     int realtime;             /* 1: honour arrival_s on the host clock                   */
+    double max_wait_s;        /* a request that has waited this long without fitting the
+                                 budget holds later ones back until it fits; 0 = 2 s    */
 } emfa_serve_opts_t;
 
 /* Runs every request to completion and fills results (one per request).

@@ -50,6 +50,24 @@ def test_admitter_oversized_request_runs_alone(emfa_lib):
     assert start[0] == pytest.approx(1.5)
 
 
+def test_admitter_age_limit_keeps_a_large_request_from_starving(emfa_lib):
+    from emfa_gb300 import api
+    # a 3 GB request every 0.5 s, each running 1 s: two run at any time (6 GB
+    # of a 10 GB budget), so the 8 GB request that arrived at 0.2 s never fits
+    # while the stream lasts ...
+    small = [0.5 * i for i in range(11)]
+    arr = [0.2] + small
+    dur = [1.0] * len(arr)
+    nb = [8 * GB] + [3 * GB] * len(small)
+    start, _ = api.serve_simulate(arr, dur, nb, lanes=8, hbm_budget=10 * GB, max_wait_s=1e9)
+    assert start[0] > 5.0
+    # ... unless, once it has waited max_wait_s, later requests are held back:
+    # the small ones of 0.5 s and 1.0 s finish at 1.5 s and 2.0 s, and it starts
+    start, _ = api.serve_simulate(arr, dur, nb, lanes=8, hbm_budget=10 * GB, max_wait_s=1.0)
+    assert start[0] == pytest.approx(2.0)
+    assert all(s >= 3.0 for s, a in zip(start[1:], small) if 1.2 <= a < 3.0)
+
+
 def test_admitter_honours_arrivals(emfa_lib):
     from emfa_gb300 import api
     arr = [0.0, 2.0, 2.5]

@@ -13,7 +13,8 @@ import ctypes
 import numpy as np
 import pytest
 
-SIZES = [(998, 37), (1920, 360), (256, 1)]
+# (2048, 512) is n * n_rhs exactly at EMFA_NOALLOC_MAX_ELEMS
+SIZES = [(998, 37), (1920, 360), (256, 1), (2048, 512)]
 
 
 def _ptr(t):
@@ -54,6 +55,30 @@ def test_noalloc_matches_context_entry_point(emfa_lib, ctx, n, nrhs):
         assert _rel(y_new, y_ctx) < 1e-6, (call, _rel(y_new, y_ctx))
         y64 = X.astype(np.complex128) @ Z.astype(np.complex128).T
         assert _rel(y_new, y64) < 3e-3, (call, _rel(y_new, y64))
+
+
+@pytest.mark.gpu
+def test_noalloc_call_reserves_no_device_memory(emfa_lib, ctx):
+    """After a first call on the device (which may make the driver load this
+    part of the library and reserve its static array), further calls change
+    neither the device's free memory nor torch's allocator counters."""
+    import torch
+    L = emfa_lib
+    n, nrhs = 1920, 360
+    _, _, Zd, Xd = _inputs(n, nrhs, 5)
+    Y = torch.empty((nrhs, n), dtype=torch.complex64, device="cuda")
+    assert L.emfa_matvec_tf32_noalloc(_ptr(Zd), n, _ptr(Xd), nrhs, _ptr(Y), None) == 0
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    stats0 = torch.cuda.memory_stats()
+    for _ in range(3):
+        assert L.emfa_matvec_tf32_noalloc(_ptr(Zd), n, _ptr(Xd), nrhs, _ptr(Y), None) == 0
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    stats1 = torch.cuda.memory_stats()
+    assert free1 == free0, (free0, free1)
+    for key in ("allocation.all.allocated", "segment.all.allocated", "reserved_bytes.all.current"):
+        assert stats1.get(key, 0) == stats0.get(key, 0), key
 
 
 @pytest.mark.gpu
