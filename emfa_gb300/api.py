@@ -57,6 +57,9 @@ class Context:
         self.device = device
 
     def close(self):
+        """Releases the caller's hold on the context; geometries and MLFMA
+        operators still open on it keep its stream until they are closed."""
+        self._ext = None
         if self.h:
             L.lib().emfa_ctx_destroy(self.h)
             self.h = vp()
@@ -87,6 +90,15 @@ class Context:
         s = vp()
         self.check(L.lib().emfa_ctx_stream(self.h, ctypes.byref(s)))
         return s.value or 0
+
+    def join_torch(self):
+        """Makes torch's current stream wait for the work queued so far on
+        the context's stream (no host wait), so torch reads of a result
+        written there see it."""
+        torch = _torch()
+        if getattr(self, "_ext", None) is None:
+            self._ext = torch.cuda.ExternalStream(self.stream_ptr(), device="cuda:%d" % self.device)
+        torch.cuda.current_stream().wait_stream(self._ext)
 
     KERNEL_TIMERS = {"fill_z": 0, "gemm": 1, "residual": 2}
 
@@ -140,6 +152,7 @@ def fill_z(geom: Geometry, fp: L.FillParams, out=None):
     Z = out if out is not None else torch.empty((n, n), dtype=dt, device="cuda:%d" % geom.ctx.device)
     torch.cuda.current_stream().synchronize()
     geom.ctx.check(L.lib().emfa_fill_z(geom.ctx.h, geom.h, ctypes.byref(fp), _ptr(Z), Z.stride(0), None))
+    geom.ctx.join_torch()
     return Z
 
 
@@ -149,8 +162,10 @@ def fill_v(geom: Geometry, fp: L.FillParams, angles, out=None):
     a = np.ascontiguousarray(np.atleast_2d(angles), dtype=np.float64)
     dt = torch.complex128 if fp.precision == L.EMFA_F64 else torch.complex64
     V = out if out is not None else torch.empty((a.shape[0], geom.n), dtype=dt, device="cuda:%d" % geom.ctx.device)
+    torch.cuda.current_stream().synchronize()  # an `out` written on torch's stream
     geom.ctx.check(L.lib().emfa_fill_v(geom.ctx.h, geom.h, ctypes.byref(fp), a.ctypes.data_as(vp), a.shape[0],
                                        _ptr(V), None))
+    geom.ctx.join_torch()
     return V
 
 
@@ -342,6 +357,7 @@ class Mlfma:
         V = torch.empty((a.shape[0], self.geom.n), dtype=torch.complex64, device="cuda:%d" % self.ctx.device)
         torch.cuda.current_stream().synchronize()
         self.ctx.check(L.lib().emfa_mlfma_fill_v(self.h, a.ctypes.data_as(vp), a.shape[0], _ptr(V), None))
+        self.ctx.join_torch()
         return V
 
     def solve(self, B, sp: L.SolverParams):
@@ -420,19 +436,19 @@ class RcsRequest:
                          self.box_threshold, self.arrival_s, self.rcs.ctypes.data)
 
 
-def serve(requests, device=0, lanes=0, hbm_budget=0, dense_max=0, realtime=False):
+def serve(requests, device=0, lanes=0, hbm_budget=0, dense_max=0, realtime=False, max_wait_s=0.0):
     """Runs the requests through emfa_serve; each request's rcs array is
     filled in place.  Returns the per-request results (status, method,
     unknowns, iterations, timing in seconds from the start)."""
     n = len(requests)
     arr = (L.Request * n)(*[r.c_struct() for r in requests])
     res = (L.RequestResult * n)()
-    opts = L.ServeOpts(int(lanes), int(hbm_budget), int(dense_max), int(bool(realtime)))
+    opts = L.ServeOpts(int(lanes), int(hbm_budget), int(dense_max), int(bool(realtime)), float(max_wait_s))
     L.check(L.lib().emfa_serve(int(device), arr, n, ctypes.byref(opts), res))
     return list(res)
 
 
-def serve_simulate(arrival, duration, nbytes, lanes=6, hbm_budget=0, realtime=True):
+def serve_simulate(arrival, duration, nbytes, lanes=6, hbm_budget=0, realtime=True, max_wait_s=0.0):
     """The admitter of serve() on a simulated clock: (start times, lanes)."""
     a = np.ascontiguousarray(arrival, dtype=np.float64)
     d = np.ascontiguousarray(duration, dtype=np.float64)
@@ -440,7 +456,7 @@ def serve_simulate(arrival, duration, nbytes, lanes=6, hbm_budget=0, realtime=Tr
     n = a.shape[0]
     start = np.zeros(n, dtype=np.float64)
     lane = np.zeros(n, dtype=np.int32)
-    opts = L.ServeOpts(int(lanes), int(hbm_budget), 0, int(bool(realtime)))
+    opts = L.ServeOpts(int(lanes), int(hbm_budget), 0, int(bool(realtime)), float(max_wait_s))
     L.check(L.lib().emfa_serve_simulate(a.ctypes.data_as(vp), d.ctypes.data_as(vp), b.ctypes.data_as(vp), n,
                                         ctypes.byref(opts), start.ctypes.data_as(vp), lane.ctypes.data_as(vp)))
     return start, lane

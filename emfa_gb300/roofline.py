@@ -20,6 +20,17 @@ def split_fp16_inner_bytes(n: int, nrhs: int) -> float:
     return 2.0 * n * 2 * n + 2.0 * (2 * nrhs) * (2 * n) + 8.0 * n * nrhs
 
 
+# DRAM bytes (read + write) of one launch of the split-FP16 inner product at
+# n = 7680, R = 360, from an ncu capture of that kernel at that size (one
+# pass); the algorithmic figure is split_fp16_inner_bytes(7680, 360).
+INNER_TRAFFIC_7680x360 = 261.3e6
+
+
+def fp32_nominal_tflops(sm_count: int = 152, sm_mhz: float = 2070.0) -> float:
+    """Nominal FP32 FMA rate: 128 lanes per SM, 2 FLOP per FMA."""
+    return sm_count * 128 * 2 * sm_mhz * 1e6 / 1e12
+
+
 def fill_flops(n_tri: int, cfie: bool) -> float:
     """Regular-pair fill counted per unique triangle pair: 9 point pairs per
     pair, 75 FLOP per point pair for CFIE and 40 for EFIE (sqrt, sin, cos
