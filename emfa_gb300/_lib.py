@@ -27,7 +27,7 @@ EMFA_MV_AUTO, EMFA_MV_F64, EMFA_MV_F32, EMFA_MV_TF32, EMFA_MV_F16X = 0, 1, 2, 3,
 class FillParams(ctypes.Structure):
     _fields_ = [("kind", ctypes.c_int), ("precision", ctypes.c_int), ("freq", ctypes.c_double),
                 ("alpha", ctypes.c_double), ("sigma_re", ctypes.c_double), ("sigma_im", ctypes.c_double),
-                ("edm_mode", ctypes.c_int)]
+                ("edm_mode", ctypes.c_int), ("discretisation", ctypes.c_int)]
 
 
 class SolverParams(ctypes.Structure):
@@ -38,7 +38,8 @@ class SolverParams(ctypes.Structure):
 
 class MlfmaParams(ctypes.Structure):
     _fields_ = [("freq", ctypes.c_double), ("alpha", ctypes.c_double), ("box_threshold", ctypes.c_double),
-                ("precond", ctypes.c_int), ("row_threshold", ctypes.c_double), ("col_threshold", ctypes.c_double)]
+                ("precond", ctypes.c_int), ("row_threshold", ctypes.c_double), ("col_threshold", ctypes.c_double),
+                ("truncation", ctypes.c_int)]
 
 
 class Request(ctypes.Structure):
@@ -134,7 +135,7 @@ _SIGS = {
 def header_symbols() -> list[str]:
     """Every function the public header declares."""
     txt = open(HEADER).read()
-    return sorted(set(re.findall(r"\b(emfa_[a-z0-9_]+)\s*\(", txt)))
+    return sorted(set(n for n in re.findall(r"\b(emfa_[a-z0-9_]+)\s*\(", txt) if not n.endswith("_t")))
 
 
 def lib():

@@ -35,10 +35,15 @@ def build_rwg(tris: np.ndarray) -> np.ndarray:
     return out[: n.value].copy()
 
 
-def fill_params(kind="cfie", precision="f32", freq=3e8, alpha=0.5, sigma=(0.0, 0.0), edm_mode=0) -> L.FillParams:
+def fill_params(kind="cfie", precision="f32", freq=3e8, alpha=0.5, sigma=(0.0, 0.0), edm_mode=0,
+                discretisation="reference") -> L.FillParams:
+    """discretisation: "reference" (3 x 3 points, self-pair extraction, as
+    the reference) or "config" (7 x 7 points, self and edge-adjacent pair
+    extraction; EFIE)."""
     return L.FillParams(L.EMFA_CFIE if kind == "cfie" else L.EMFA_EFIE,
                         L.EMFA_F64 if precision == "f64" else L.EMFA_F32,
-                        float(freq), float(alpha), float(sigma[0]), float(sigma[1]), int(edm_mode))
+                        float(freq), float(alpha), float(sigma[0]), float(sigma[1]), int(edm_mode),
+                        {"reference": 0, "config": 1}[discretisation])
 
 
 def solver_params(method="gmres", restart=30, max_iter=600, tol=1e-6, tol_absolute=False, matvec="auto",
@@ -283,9 +288,11 @@ def monostatic_dirs(angles) -> np.ndarray:
 # MLFMA
 # ---------------------------------------------------------------------------
 def mlfma_params(freq=3e8, alpha=0.5, box_threshold=0.25, precond=False, row_threshold=0.9,
-                 col_threshold=0.87) -> L.MlfmaParams:
+                 col_threshold=0.87, truncation="reference") -> L.MlfmaParams:
+    """truncation: "reference" (int(kd + 6 kd^(1/3)), as the reference) or
+    "config" (int(kd + 1.8 d0^(2/3) kd^(1/3)), d0 = 3)."""
     return L.MlfmaParams(float(freq), float(alpha), float(box_threshold), int(bool(precond)), float(row_threshold),
-                         float(col_threshold))
+                         float(col_threshold), {"reference": 0, "config": 1}[truncation])
 
 
 def mlfma_plan(mesh: TriMesh, rwg: np.ndarray, mp: L.MlfmaParams):

@@ -209,6 +209,8 @@ struct Geom {
     std::vector<int> tris;       // host, T x 3
     std::vector<int> rwg;        // host, N x 6 (v1 v2 vxp vxm tp tm)
     DevBuf vd;                   // device copy of verts (FP64), uploaded once
+    bool nbr_ready = false;      // edge neighbours of each triangle (3 int, -1 where none),
+    DevBuf nbr;                  //   for the configuration's discretisation
     GeomDev<float> g32;
     GeomDev<double> g64;
     // tiled fill: the distinct triangles of each block of 16 consecutive

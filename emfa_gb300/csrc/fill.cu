@@ -216,6 +216,207 @@ __global__ void __launch_bounds__(9 * SING_TRIS) k_singular_table(const double* 
 }
 
 // ---------------------------------------------------------------------------
+// The configuration's discretisation (EMFA_DISC_CONFIG, EFIE): 7 x 7-point
+// regular pairs, and singularity extraction on self AND edge-adjacent
+// triangle pairs, where the reference (Q2) extracts on self pairs only
+// (EMSolver/EFIE.cpp:655-662) and uses 3 x 3 points elsewhere.
+//
+// For a singular pair (field triangle Tf, source triangle Ts) and field /
+// source free vertices vf, vs, with G = exp(-jkR)/R = 1/R + Gs(R):
+//   smooth   sum_p sum_q w_p w_q [(P_p - vf).(Q_q - vs)/4 - 1/k^2] Gs(R_pq),
+//            Gs(R) = (exp(-jkR) - 1)/R = (-2 sin^2(kR/2) - j sin kR)/R,
+//            Gs(0) = -jk
+//   singular sum_p w_p [(P_p - vf).(I_rho(P_p) + (rho_p - vs) I_1(P_p))/4
+//                       - I_1(P_p)/k^2] / A_s
+// with I_1(r) = int_Ts 1/R dS', I_rho(r) = int_Ts (rho' - rho)/R dS' (rho the
+// projection of r on the plane of Ts) in closed form for any r, on or off
+// the plane (Wilton, Rao, Glisson, Schaubert, Al-Bundak and Butler, IEEE
+// Trans. Antennas Propag. 32 (1984) 276-281, eqs. for the scalar and vector
+// potential integrals).  w are the reference's 7-point weights (sum 1), so
+// the value is in the units of the regular sums: the entry is
+// j k Z0 / 4pi l_f l_s sum over the RWGs' four triangle pairs.
+// ---------------------------------------------------------------------------
+// ln((R+ + l+) / (R- + l-)) without the cancellation of R + l for l < 0:
+// there R + l = R0^2 / (R - l)
+__device__ static double log_ratio(double lp, double rp, double lm, double rm, double r02)
+{
+    const double a = lp >= 0 ? rp + lp : r02 / (rp - lp);
+    const double b = lm >= 0 ? rm + lm : r02 / (rm - lm);
+    return log(a / b);
+}
+
+__device__ void potential_integrals(const V3<double>* v, V3<double> r, double* I1_out, V3<double>* Irho_out)
+{
+    const V3<double> n = normalized(cross(v[1] - v[0], v[2] - v[0]));
+    const double h = dot(r - v[0], n), ah = fabs(h);
+    const V3<double> rho = r - n * h;
+    double I1 = 0.0;
+    V3<double> Ir = v3(0.0, 0.0, 0.0);
+    for (int i = 0; i < 3; ++i) {
+        const V3<double> b = v[i], a = v[(i + 1) % 3];
+        const V3<double> l = normalized(a - b);
+        const V3<double> u = cross(l, n);  // in-plane, pointing out of the triangle
+        const double lp = dot(a - rho, l), lm = dot(b - rho, l);
+        const double t = dot(b - rho, u);  // signed distance of rho from the edge's line
+        const double p0 = fabs(t);
+        const double r02 = p0 * p0 + h * h;
+        const double rp = sqrt(r02 + lp * lp), rm = sqrt(r02 + lm * lm);
+        const double lg = r02 > 0 ? log_ratio(lp, rp, lm, rm, r02) : 0.0;
+        Ir = Ir + u * (0.5 * (r02 * lg + lp * rp - lm * rm));
+        if (p0 > 0) {
+            const double sg = t > 0 ? 1.0 : -1.0;
+            I1 += sg * (p0 * lg - ah * (atan(p0 * lp / (r02 + ah * rp)) - atan(p0 * lm / (r02 + ah * rm))));
+        }
+    }
+    *I1_out = I1;
+    *Irho_out = Ir;
+}
+
+// one configuration-table value (unsigned), FP64
+__device__ static Cx<double> efie_cfg_pair(const V3<double>* tf, const V3<double>* ts, V3<double> vf, V3<double> vs,
+                                           bool self, const SingConst& c)
+{
+    V3<double> P[7], Q[7];
+    gauss7(tf[0], tf[1], tf[2], P);
+    gauss7(ts[0], ts[1], ts[2], Q);
+    const double As = tri_area(ts[0], ts[1], ts[2]);
+    const V3<double> ns = normalized(cross(ts[1] - ts[0], ts[2] - ts[0]));
+    double zr = 0.0, zi = 0.0, sing = 0.0;
+    for (int p = 0; p < 7; ++p) {
+        const double wp = gauss7_weight<double>(p);
+        const V3<double> rf = P[p] - vf;
+        for (int q = 0; q < 7; ++q) {
+            const double wq = gauss7_weight<double>(q);
+            const double R = norm(P[p] - Q[q]);
+            const double e = wp * wq * (0.25 * dot(rf, Q[q] - vs) - c.inv_k2);
+            if (R > 0) {
+                double sn, cs;
+                sincos(0.5 * c.k * R, &sn, &cs);
+                zr += e * (-2.0 * sn * sn / R);
+                zi += e * (-2.0 * sn * cs / R);
+            } else {
+                zi += e * (-c.k);
+            }
+        }
+        double I1;
+        V3<double> Ir;
+        potential_integrals(ts, P[p], &I1, &Ir);
+        const V3<double> rho = P[p] - ns * dot(P[p] - ts[0], ns);
+        sing += wp * (0.25 * dot(rf, Ir + (rho - vs) * I1) - I1 * c.inv_k2);
+    }
+    zr += sing / As;
+    if (self && sqrt(c.sig_re * c.sig_re + c.sig_im * c.sig_im) > 1e-8) {
+        // surface-impedance term (EFIE.cpp:297-306) with the 7-point rule
+        double acc = 0.0;
+        for (int i = 0; i < 7; ++i) acc += gauss7_weight<double>(i) * dot(P[i] - vf, P[i] - vs);
+        const double den = As * c.k * c.z0;
+        zr += c.pi * c.sig_im / den * acc;
+        zi -= c.pi * c.sig_re / den * acc;
+    }
+    return cx(zr, zi);
+}
+
+// table: per triangle t, 4 slots (0 the triangle itself, 1..3 its edge
+// neighbours in nbr order) x 9 (field corner, source corner); a thread per
+// value
+__global__ void __launch_bounds__(144) k_config_table(const double* __restrict__ vd, const int* __restrict__ tris,
+                                                      const int* __restrict__ nbr, int nt, SingConst c,
+                                                      double2* __restrict__ tab)
+{
+    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= 36 * nt) return;
+    const int t = id / 36, slot = (id / 9) % 4, ef = (id / 3) % 3, es = id % 3;
+    const int s = slot == 0 ? t : nbr[3 * t + slot - 1];
+    if (s < 0) {
+        tab[id] = make_double2(0.0, 0.0);
+        return;
+    }
+    V3<double> tf[3], ts[3];
+    for (int j = 0; j < 3; ++j) {
+        int a = tris[3 * t + j], b = tris[3 * s + j];
+        tf[j] = v3(vd[3 * a], vd[3 * a + 1], vd[3 * a + 2]);
+        ts[j] = v3(vd[3 * b], vd[3 * b + 1], vd[3 * b + 2]);
+    }
+    const Cx<double> z = efie_cfg_pair(tf, ts, tf[ef], ts[es], slot == 0, c);
+    tab[id] = make_double2(z.re, z.im);
+}
+
+// one entry in the configuration's discretisation (EFIE): the far-pair
+// branch as z_entry; pairs of one triangle or of edge neighbours from the
+// table, the others by the 7 x 7-point rule in T
+template <typename T>
+__device__ __forceinline__ Cx<T> z_entry_cfg(const RwgPack<T>& F, const RwgPack<T>& S, const FillConst<T>& c,
+                                             const double2* __restrict__ tab, const int* __restrict__ nbr,
+                                             const T* __restrict__ q7)
+{
+    if (c.edm_mode != 2) {
+        V3<T> fc = divr(v3(F.cen[0][0], F.cen[0][1], F.cen[0][2]) + v3(F.cen[1][0], F.cen[1][1], F.cen[1][2]), T(2));
+        V3<T> sc = divr(v3(S.cen[0][0], S.cen[0][1], S.cen[0][2]) + v3(S.cen[1][0], S.cen[1][1], S.cen[1][2]), T(2));
+        if (norm(fc - sc) > c.thr_edm) return c.edm_mode == 1 ? edm_value(F, S, c) : cx(T(0), T(0));
+    }
+    T zr = 0, zi = 0;
+    double sr = 0.0, si = 0.0;
+#pragma unroll 1
+    for (int a = 0; a < 2; ++a) {
+        const int tf = F.tri[a];
+        const T* Pp = q7 + (size_t)21 * tf;
+        const V3<T> vf = v3(F.v[a][0], F.v[a][1], F.v[a][2]);
+#pragma unroll 1
+        for (int b = 0; b < 2; ++b) {
+            const T sgn = (a == b) ? T(1) : T(-1);
+            const int ts = S.tri[b];
+            const int slot = ts == tf ? 0
+                             : nbr[3 * tf] == ts ? 1
+                             : nbr[3 * tf + 1] == ts ? 2
+                             : nbr[3 * tf + 2] == ts ? 3 : -1;
+            if (slot >= 0) {
+                const double2 v = tab[(size_t)36 * tf + 9 * slot + 3 * F.e[a] + S.e[b]];
+                sr += (double)sgn * v.x;
+                si += (double)sgn * v.y;
+                continue;
+            }
+            const T* Qp = q7 + (size_t)21 * ts;
+            const V3<T> vs = v3(S.v[b][0], S.v[b][1], S.v[b][2]);
+            T er = 0, ei = 0;
+#pragma unroll 1
+            for (int p = 0; p < 7; ++p) {
+                const V3<T> P = v3(Pp[3 * p], Pp[3 * p + 1], Pp[3 * p + 2]);
+                const V3<T> rf = P - vf;
+                const T wp = gauss7_weight<T>(p);
+#pragma unroll
+                for (int q = 0; q < 7; ++q) {
+                    const V3<T> Q = v3(Qp[3 * q], Qp[3 * q + 1], Qp[3 * q + 2]);
+                    const V3<T> d = P - Q;
+                    const T r = sqrt(dot(d, d));
+                    const T rinv = T(1) / r;
+                    T sn, cs;
+                    sincos_pi(r * c.kpi, &sn, &cs);
+                    const T e = wp * gauss7_weight<T>(q) * (T(0.25) * dot(rf, Q - vs) - c.inv_k2);
+                    er += e * cs * rinv;
+                    ei -= e * sn * rinv;
+                }
+            }
+            zr += sgn * er;
+            zi += sgn * ei;
+        }
+    }
+    const T kz = (T)c.coef_efie * (F.len * S.len);
+    const T re = zr + (T)sr, im = zi + (T)si;
+    return cx(-kz * im, kz * re);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_fill_z_cfg(const RwgPack<T>* __restrict__ rw, int n, FillConst<T> c,
+                                                    const double2* __restrict__ tab, const int* __restrict__ nbr,
+                                                    const T* __restrict__ q7, Cx<T>* __restrict__ Z, size_t ldz)
+{
+    int s = blockIdx.x * 32 + threadIdx.x;
+    int f = blockIdx.y * blockDim.y + threadIdx.y;
+    if (s >= n || f >= n) return;
+    Z[(size_t)f * ldz + s] = z_entry_cfg<T>(rw[f], rw[s], c, tab, nbr, q7);
+}
+
+// ---------------------------------------------------------------------------
 // entry kernel: one thread per Z(f, s); a warp runs 32 consecutive s of one f
 // ---------------------------------------------------------------------------
 template <typename T, bool CFIE>
@@ -646,11 +847,85 @@ __global__ void k_fill_v(const RwgPack<T>* __restrict__ rw, const T* __restrict_
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
+static SingConst sing_const(const emfa_fill_params_t* p)
+{
+    SingConst sc;
+    sc.k = p->precision == EMFA_F64 ? Phys<double>::wavenumber(p->freq) : (double)Phys<float>::wavenumber(p->freq);
+    sc.inv_k2 = 1.0 / (sc.k * sc.k);
+    sc.w = 1.0 / 3.0;
+    sc.alpha = p->alpha;
+    sc.pi = 3.14159265358979323846;
+    sc.z0 = 120.0 * sc.pi;
+    sc.sig_re = p->sigma_re;
+    sc.sig_im = p->sigma_im;
+    sc.cfie = p->kind == EMFA_CFIE;
+    return sc;
+}
+
+// Each triangle's edge neighbours (up to 3, -1 where none), from the RWG
+// table in RWG order: the RWG of an edge joins its + and - triangles.  A
+// triangle with more than 3 RWG neighbours (a non-manifold mesh) keeps the
+// first 3; the rest are filled as regular pairs.
+static emfa_status_t geom_neighbours(Ctx* c, Geom* g, cudaStream_t st)
+{
+    if (g->nbr_ready) return EMFA_OK;
+    std::vector<int> nb((size_t)3 * g->nt, -1);
+    auto add = [&](int t, int o) {
+        for (int j = 0; j < 3; ++j) {
+            if (nb[3 * t + j] == o) return;
+            if (nb[3 * t + j] < 0) {
+                nb[3 * t + j] = o;
+                return;
+            }
+        }
+    };
+    for (int u = 0; u < g->n; ++u) {
+        const int tp = g->rwg[6 * u + 4], tm = g->rwg[6 * u + 5];
+        add(tp, tm);
+        add(tm, tp);
+    }
+    EMFA_TRY(g->nbr.alloc(c, sizeof(int) * nb.size()));
+    EMFA_CUDA(c, cudaMemcpyAsync(g->nbr.ptr, nb.data(), sizeof(int) * nb.size(), cudaMemcpyHostToDevice, st));
+    EMFA_CUDA(c, cudaStreamSynchronize(st));  // nb is a host temporary
+    g->nbr_ready = true;
+    return EMFA_OK;
+}
+
+// The configuration's discretisation: FP64 table of self and edge-adjacent
+// pairs, then one thread per entry with 7 x 7-point regular pairs.
+template <typename T>
+static emfa_status_t fill_z_cfg(Ctx* c, Geom* g, GeomDev<T>& d, const emfa_fill_params_t* p, void* Z, size_t ldz,
+                                cudaStream_t st)
+{
+    EMFA_TRY(geom_neighbours(c, g, st));
+    EMFA_TRY(geom_vd(g, st));
+    void* tab = nullptr;
+    EMFA_TRY(ctx_workspace(c, WS_FILL, sizeof(double2) * (size_t)g->nt * 36, &tab));
+    const SingConst sc = sing_const(p);
+    k_config_table<<<(36 * g->nt + 143) / 144, 144, 0, st>>>(dptr<double>(g->vd), dptr<int>(d.tris),
+                                                             dptr<int>(g->nbr), g->nt, sc, (double2*)tab);
+    c->kernel_launches += 1;
+    EMFA_CUDA(c, cudaGetLastError());
+    FillConst<T> fc = make_fill_const<T>(p);
+    dim3 blk(32, 8);
+    dim3 grd((g->n + 31) / 32, (g->n + 7) / 8);
+    {
+        TimedLaunch tl(c, KT_FILL_Z, st, (double)g->n * g->n);
+        k_fill_z_cfg<T><<<grd, blk, 0, st>>>(dptr<RwgPack<T>>(d.rwg), g->n, fc, (const double2*)tab,
+                                             dptr<int>(g->nbr), dptr<T>(d.tri_q7), reinterpret_cast<Cx<T>*>(Z), ldz);
+    }
+    c->kernel_launches += 1;
+    EMFA_CUDA(c, cudaGetLastError());
+    EMFA_CUDA(c, cudaStreamSynchronize(st));
+    return EMFA_OK;
+}
+
 template <typename T>
 static emfa_status_t fill_z_t(Ctx* c, Geom* g, GeomDev<T>& d, const emfa_fill_params_t* p, void* Z, size_t ldz,
                               cudaStream_t st)
 {
     const bool cfie = p->kind == EMFA_CFIE;
+    if (p->discretisation == EMFA_DISC_CONFIG) return fill_z_cfg<T>(c, g, d, p, Z, ldz, st);
     // singular table (FP64), 9 (CFIE) or 27 (EFIE) double2 per triangle
     void* tab = nullptr;
     EMFA_TRY(ctx_workspace(c, WS_FILL, sizeof(double2) * (size_t)g->nt * (cfie ? 9 : 27), &tab));
@@ -708,7 +983,6 @@ static emfa_status_t fill_z_t(Ctx* c, Geom* g, GeomDev<T>& d, const emfa_fill_pa
 
 emfa_status_t build_singular_table(Ctx* c, Geom* g, const emfa_fill_params_t* p, double2* tab, cudaStream_t st)
 {
-    const bool cfie = p->kind == EMFA_CFIE;
     if (p->precision == EMFA_F64)
         EMFA_TRY(geom_prepare_f64(g, st));
     else
@@ -716,16 +990,7 @@ emfa_status_t build_singular_table(Ctx* c, Geom* g, const emfa_fill_params_t* p,
     // the table's vertices (the geometry's FP64 copy) and k: the fill
     // precision's k, in FP64 arithmetic
     EMFA_TRY(geom_vd(g, st));
-    SingConst sc;
-    sc.k = p->precision == EMFA_F64 ? Phys<double>::wavenumber(p->freq) : (double)Phys<float>::wavenumber(p->freq);
-    sc.inv_k2 = 1.0 / (sc.k * sc.k);
-    sc.w = 1.0 / 3.0;
-    sc.alpha = p->alpha;
-    sc.pi = 3.14159265358979323846;
-    sc.z0 = 120.0 * sc.pi;
-    sc.sig_re = p->sigma_re;
-    sc.sig_im = p->sigma_im;
-    sc.cfie = cfie;
+    const SingConst sc = sing_const(p);
     const int* tris = p->precision == EMFA_F64 ? dptr<int>(g->g64.tris) : dptr<int>(g->g32.tris);
     k_singular_table<<<(g->nt + SING_TRIS - 1) / SING_TRIS, 9 * SING_TRIS, 0, st>>>(dptr<double>(g->vd), tris, g->nt,
                                                                                    sc, tab);
@@ -798,6 +1063,14 @@ static emfa_status_t check_fill(emfa_ctx_t* ctx, emfa_geom_t* geom, const emfa_f
     if (!(p->freq > 0)) {
         set_error(ctx, "fill: frequency must be positive");
         return EMFA_ERR_INVALID;
+    }
+    if (p->discretisation != EMFA_DISC_REFERENCE && p->discretisation != EMFA_DISC_CONFIG) {
+        set_error(ctx, "fill: discretisation must be EMFA_DISC_REFERENCE or EMFA_DISC_CONFIG");
+        return EMFA_ERR_INVALID;
+    }
+    if (p->discretisation == EMFA_DISC_CONFIG && p->kind != EMFA_EFIE) {
+        set_error(ctx, "fill: EMFA_DISC_CONFIG (7-point rule, adjacent-pair extraction) is built for EFIE only");
+        return EMFA_ERR_UNSUPPORTED;
     }
     if (p->edm_mode < 0 || p->edm_mode > 2) {
         set_error(ctx, "fill: edm_mode must be 0, 1 or 2");

@@ -4,7 +4,8 @@
 // for many right-hand sides at once.
 //
 // 64 (f) x 64 (r) CTA tile, 16-wide K slices staged through shared memory,
-// 4 x 4 complex outputs per thread.  ACC selects the accumulation:
+// 4 x 4 complex outputs per thread; up to 16 right-hand sides a warp-per-row
+// GEMV instead.  ACC selects the accumulation:
 //   float / double : plain accumulation in that type
 //   CHUNKED        : FP32 products and sums over 64-wide K chunks, chunk sums
 //                    accumulated in FP64 (the refinement residual of the
@@ -13,6 +14,8 @@
 #include "emfa_internal.cuh"
 #include "emfa_math.cuh"
 #include "gemm.cuh"
+
+#include <algorithm>
 
 namespace emfa {
 
@@ -100,8 +103,84 @@ __global__ void __launch_bounds__(256) k_cgemm(const Cx<T>* __restrict__ Z, size
     }
 }
 
+// Few right-hand sides (the 64-wide tile above would leave most of its RHS
+// columns empty): a warp per RPW rows of Z, lanes striding k, up to RB
+// right-hand sides per launch accumulated in registers, then reduced by
+// shuffles.  Each warp reads its rows once (coalesced 512-byte segments for
+// complex128) and the RHS entries from L1/L2; FP64 is bound by the FMA rate.
+template <typename T, int RB, int RPW>
+__global__ void __launch_bounds__(256) k_cgemv(const Cx<T>* __restrict__ Z, size_t ldz, const Cx<T>* __restrict__ X,
+                                               int n, int nrhs, Cx<T>* __restrict__ Y)
+{
+    const int warp = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    const int f0 = warp * RPW;
+    if (f0 >= n) return;
+    T ar[RPW][RB], ai[RPW][RB];
+#pragma unroll
+    for (int i = 0; i < RPW; ++i)
+#pragma unroll
+        for (int r = 0; r < RB; ++r) ar[i][r] = ai[i][r] = T(0);
+    for (int k = lane; k < n; k += 32) {
+        Cx<T> z[RPW];
+#pragma unroll
+        for (int i = 0; i < RPW; ++i) z[i] = f0 + i < n ? Z[(size_t)(f0 + i) * ldz + k] : cx(T(0), T(0));
+#pragma unroll
+        for (int r = 0; r < RB; ++r)
+            if (r < nrhs) {
+                const Cx<T> x = X[(size_t)r * n + k];
+#pragma unroll
+                for (int i = 0; i < RPW; ++i) {
+                    ar[i][r] = fma(z[i].re, x.re, ar[i][r]);
+                    ar[i][r] = fma(-z[i].im, x.im, ar[i][r]);
+                    ai[i][r] = fma(z[i].re, x.im, ai[i][r]);
+                    ai[i][r] = fma(z[i].im, x.re, ai[i][r]);
+                }
+            }
+    }
+#pragma unroll
+    for (int i = 0; i < RPW; ++i)
+#pragma unroll
+        for (int r = 0; r < RB; ++r) {
+            if (r >= nrhs) break;
+            T re = ar[i][r], im = ai[i][r];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                re += __shfl_xor_sync(0xffffffffu, re, o);
+                im += __shfl_xor_sync(0xffffffffu, im, o);
+            }
+            if (lane == 0 && f0 + i < n) Y[(size_t)r * n + f0 + i] = cx(re, im);
+        }
+}
+
+// up to 16 right-hand sides: GEMV launches of 8; more: the tiled kernel
+template <typename T>
+static emfa_status_t cgemv_chunks(Ctx* c, const void* Z, size_t ldz, const void* X, int n, int nrhs, void* Y,
+                                  cudaStream_t st)
+{
+    constexpr int RPW = sizeof(T) == 8 ? 1 : 4;
+    const int warps = (n + RPW - 1) / RPW;
+    for (int r0 = 0; r0 < nrhs; r0 += 8) {
+        const int nr = std::min(8, nrhs - r0);
+        const Cx<T>* x = (const Cx<T>*)X + (size_t)r0 * n;
+        Cx<T>* y = (Cx<T>*)Y + (size_t)r0 * n;
+        const int grd = (warps + 7) / 8;
+        if (nr == 1)
+            k_cgemv<T, 1, RPW><<<grd, 256, 0, st>>>((const Cx<T>*)Z, ldz, x, n, nr, y);
+        else if (nr <= 2)
+            k_cgemv<T, 2, RPW><<<grd, 256, 0, st>>>((const Cx<T>*)Z, ldz, x, n, nr, y);
+        else if (nr <= 4)
+            k_cgemv<T, 4, RPW><<<grd, 256, 0, st>>>((const Cx<T>*)Z, ldz, x, n, nr, y);
+        else
+            k_cgemv<T, 8, RPW><<<grd, 256, 0, st>>>((const Cx<T>*)Z, ldz, x, n, nr, y);
+        c->kernel_launches += 1;
+        EMFA_CUDA(c, cudaGetLastError());
+    }
+    return EMFA_OK;
+}
+
 emfa_status_t cgemm_f32(Ctx* c, const void* Z, size_t ldz, const void* X, int n, int nrhs, void* Y, cudaStream_t st)
 {
+    if (nrhs <= 16) return cgemv_chunks<float>(c, Z, ldz, X, n, nrhs, Y, st);
     dim3 grd((n + 63) / 64, (nrhs + 63) / 64);
     k_cgemm<float, false><<<grd, 256, 0, st>>>((const Cx<float>*)Z, ldz, (const Cx<float>*)X, n, nrhs, (Cx<float>*)Y,
                                                nullptr, nullptr);
@@ -112,6 +191,7 @@ emfa_status_t cgemm_f32(Ctx* c, const void* Z, size_t ldz, const void* X, int n,
 
 emfa_status_t cgemm_f64(Ctx* c, const void* Z, size_t ldz, const void* X, int n, int nrhs, void* Y, cudaStream_t st)
 {
+    if (nrhs <= 16) return cgemv_chunks<double>(c, Z, ldz, X, n, nrhs, Y, st);
     dim3 grd((n + 63) / 64, (nrhs + 63) / 64);
     k_cgemm<double, false><<<grd, 256, 0, st>>>((const Cx<double>*)Z, ldz, (const Cx<double>*)X, n, nrhs,
                                                 (Cx<double>*)Y, nullptr, nullptr);

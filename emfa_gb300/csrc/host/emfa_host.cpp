@@ -317,6 +317,9 @@ void EM::init(ConfigLoader* ploader)
         dir_ = mesh_file.substr(0, pd);
         folder_name_ = mesh_file.substr(pd + 1, pos_suffix - pd - 1);
     }
+    inc_angles_ = {incidence_.theta, incidence_.phi, incidence_.pole};
+    n_inc_ = 1;
+    if (rtype_ == policy::MonoRCS) planMonostatic();
     mesh_.loadMeshFile(mesh_file);
     int cap = 3 * mesh_.triangles() / 2 + 16, n = 0;
     rwg_.assign((size_t)6 * cap, 0);
@@ -392,6 +395,62 @@ void EM::writeBistatic(const emfa_fill_params_t& fp, const void* I_dev)
     }
 }
 
+// The sweep of Result::getMonostaticRCS (EMComponent/Result.h:106-155): for
+// each phi cut the theta rows, then phi = 0..359 at theta = 90, in float
+// arithmetic as the reference steps its angles.  Direction (theta, phi) is
+// seen from the incidence at the same angles: the reference's incident wave
+// travels along -r_hat(theta, phi) (EMSolver/EM.cpp:33), so the backscatter
+// direction is r_hat(theta, phi); the polarisation is the config's pole.
+void EM::planMonostatic()
+{
+    const float d2r = 3.14159265358979323846f / 180.0f;
+    const auto& sca = scattering_;
+    inc_angles_.clear();
+    mono_dirs_.clear();
+    mono_files_.clear();
+    int phi_num = static_cast<int>((sca.phi_to - sca.phi_from) / sca.phi_delta) + 1;
+    for (int i = 0; i < phi_num; ++i) {
+        float phi_deg = sca.phi_from + i * sca.phi_delta;
+        float phi = phi_deg * d2r;
+        float cosp = (float)std::cos((double)phi), sinp = (float)std::sin((double)phi);
+        std::string str = std::to_string(phi_deg);
+        mono_files_.push_back({"monostatic_rcs_phi_" + str.substr(0, str.find('.')) + ".dat", {}});
+        for (float td = sca.theta_from; td <= sca.theta_to; td += sca.theta_delta) {
+            double th = (double)(td * d2r);
+            mono_dirs_.insert(mono_dirs_.end(), {(double)(float)(std::sin(th) * cosp),
+                                                 (double)(float)(std::sin(th) * sinp), (double)(float)std::cos(th)});
+            inc_angles_.insert(inc_angles_.end(), {(double)td, (double)phi_deg, (double)incidence_.pole});
+            mono_files_.back().angles.push_back(td);
+        }
+    }
+    mono_files_.push_back({"monostatic_rcs_theta_90.dat", {}});
+    for (float pd = 0; pd < 360; pd += 1) {
+        double p = (double)(pd * d2r);
+        mono_dirs_.insert(mono_dirs_.end(), {(double)(float)std::cos(p), (double)(float)std::sin(p), 0.0});
+        inc_angles_.insert(inc_angles_.end(), {90.0, (double)pd, (double)incidence_.pole});
+        mono_files_.back().angles.push_back(pd);
+    }
+    n_inc_ = (int)inc_angles_.size() / 3;
+    if (n_inc_ > 65535) throw ConfigInvalid("monostatic sweep: more than 65535 incidences");
+}
+
+// One emfa_rcs call for all incidences, each at its own backscatter
+// direction; the files keep the reference's layout (same header and columns
+// as the bistatic files).
+void EM::writeMonostatic(const emfa_fill_params_t& fp, const void* I_dev)
+{
+    std::vector<double> rcs(n_inc_);
+    check(emfa_rcs(ctx_, geom_, &fp, I_dev, n_inc_, mono_dirs_.data(), 1, 1, rcs.data(), nullptr), ctx_,
+          "emfa_rcs");
+    size_t k = 0;
+    for (auto& fl : mono_files_) {
+        std::ofstream o(dir_ + "/" + fl.name);
+        o << std::right << std::fixed << std::setprecision(4);
+        o << std::setw(10) << "Theta\t" << std::setw(10) << "RCS(dBm^2)\n";
+        for (float ang : fl.angles) o << std::setw(10) << ang << '\t' << std::setw(10) << (float)rcs[k++] << '\n';
+    }
+}
+
 static std::string make_folder(const std::string& dir, const std::string& name)
 {
     std::string d = dir + '/' + name;
@@ -411,6 +470,10 @@ void EFIE::init(ConfigLoader* ploader)
     ploader->getArray_x();
     ploader->getArray_y();
     tol_ = std::atof(ploader->getGpu("gpu_efie_tol:", "1e-3").c_str());
+    const std::string disc = ploader->getGpu("gpu_discretisation:", "reference");
+    if (disc != "reference" && disc != "config")
+        throw ConfigInvalid("gpu_discretisation: must be reference or config");
+    disc_ = disc == "config" ? EMFA_DISC_CONFIG : EMFA_DISC_REFERENCE;
     logger_ << ploader->getReport();
     reportInfo(logger_);
     timeLog("init");
@@ -419,19 +482,18 @@ void EFIE::init(ConfigLoader* ploader)
 void EFIE::solve()
 {
     const size_t es = precision_ == EMFA_F64 ? 16 : 8;
-    const size_t n = unknowns_;
+    const size_t n = unknowns_, r = n_inc_;
     check(emfa_device_alloc(ctx_, es * n * n, &Z_), ctx_, "alloc Z");
-    check(emfa_device_alloc(ctx_, es * n, &V_), ctx_, "alloc V");
-    check(emfa_device_alloc(ctx_, 16 * n, &I_), ctx_, "alloc I");
-    emfa_fill_params_t fp{EMFA_EFIE, precision_, (double)incidence_.freq, 1.0, sigma_.real(), sigma_.imag(), 0};
+    check(emfa_device_alloc(ctx_, es * n * r, &V_), ctx_, "alloc V");
+    check(emfa_device_alloc(ctx_, 16 * n * r, &I_), ctx_, "alloc I");
+    emfa_fill_params_t fp{EMFA_EFIE, precision_, (double)incidence_.freq, 1.0, sigma_.real(), sigma_.imag(), 0, disc_};
     check(emfa_fill_z(ctx_, geom_, &fp, Z_, n, nullptr), ctx_, "fillZ");
     timeLog("fillZ");
-    double ang[3] = {incidence_.theta, incidence_.phi, incidence_.pole};
-    check(emfa_fill_v(ctx_, geom_, &fp, ang, 1, V_, nullptr), ctx_, "fillV");
+    check(emfa_fill_v(ctx_, geom_, &fp, inc_angles_.data(), n_inc_, V_, nullptr), ctx_, "fillV");
     timeLog("fillV");
     emfa_solver_params_t sp{EMFA_GMRES, 30, 100000, tol_, 1, EMFA_MV_AUTO, 0, 0};
     emfa_solve_info_t info{};
-    emfa_status_t s = emfa_solve(ctx_, precision_, Z_, (int)n, V_, 1, I_, &sp, &info, nullptr);
+    emfa_status_t s = emfa_solve(ctx_, precision_, Z_, (int)n, V_, n_inc_, I_, &sp, &info, nullptr);
     if (s == EMFA_ERR_NOT_CONVERGED)
         logger_ << "    WARNING: Iteration cannot converge\n";
     else
@@ -443,9 +505,14 @@ void EFIE::solve()
 
 void EFIE::output()
 {
-    emfa_fill_params_t fp{EMFA_EFIE, precision_, (double)incidence_.freq, 1.0, sigma_.real(), sigma_.imag(), 0};
-    writeBistatic(fp, I_);
-    timeLog("getBistaticRCS");
+    emfa_fill_params_t fp{EMFA_EFIE, precision_, (double)incidence_.freq, 1.0, sigma_.real(), sigma_.imag(), 0, disc_};
+    if (rtype_ == policy::MonoRCS) {
+        writeMonostatic(fp, I_);
+        timeLog("getMonostaticRCS");
+    } else {
+        writeBistatic(fp, I_);
+        timeLog("getBistaticRCS");
+    }
 }
 
 void EFIE::clear()
@@ -461,6 +528,7 @@ void CFIE::init(ConfigLoader* ploader)
 {
     EM::init(ploader);
     alpha_ = ploader->getAlpha();
+    tol_ = std::atof(ploader->getGpu("gpu_cfie_tol:", "0.01").c_str());
     dir_ = make_folder(dir_, folder_name_ + "_CFIE_" + std::to_string(alpha_).substr(0, 3));
     logger_.open(dir_ + "/sca_runtime.log");
     logger_ << ploader->getReport();
@@ -471,19 +539,18 @@ void CFIE::init(ConfigLoader* ploader)
 void CFIE::solve()
 {
     const size_t es = precision_ == EMFA_F64 ? 16 : 8;
-    const size_t n = unknowns_;
+    const size_t n = unknowns_, r = n_inc_;
     check(emfa_device_alloc(ctx_, es * n * n, &Z_), ctx_, "alloc Z");
-    check(emfa_device_alloc(ctx_, es * n, &V_), ctx_, "alloc V");
-    check(emfa_device_alloc(ctx_, 16 * n, &I_), ctx_, "alloc I");
+    check(emfa_device_alloc(ctx_, es * n * r, &V_), ctx_, "alloc V");
+    check(emfa_device_alloc(ctx_, 16 * n * r, &I_), ctx_, "alloc I");
     emfa_fill_params_t fp{EMFA_CFIE, precision_, (double)incidence_.freq, (double)alpha_, 0, 0, 0};
     check(emfa_fill_z(ctx_, geom_, &fp, Z_, n, nullptr), ctx_, "fillZ");
     timeLog("fillZ");
-    double ang[3] = {incidence_.theta, incidence_.phi, incidence_.pole};
-    check(emfa_fill_v(ctx_, geom_, &fp, ang, 1, V_, nullptr), ctx_, "fillV");
+    check(emfa_fill_v(ctx_, geom_, &fp, inc_angles_.data(), n_inc_, V_, nullptr), ctx_, "fillV");
     timeLog("fillV");
-    emfa_solver_params_t sp{EMFA_BICGSTAB, 30, 500, 0.01, 0, EMFA_MV_AUTO, 0, 0};
+    emfa_solver_params_t sp{EMFA_BICGSTAB, 30, 500, tol_, 0, EMFA_MV_AUTO, 0, 0};
     emfa_solve_info_t info{};
-    emfa_status_t s = emfa_solve(ctx_, precision_, Z_, (int)n, V_, 1, I_, &sp, &info, nullptr);
+    emfa_status_t s = emfa_solve(ctx_, precision_, Z_, (int)n, V_, n_inc_, I_, &sp, &info, nullptr);
     if (s == EMFA_ERR_NOT_CONVERGED)
         logger_ << "    WARNING: Iteration cannot converge\n";
     else
@@ -497,8 +564,13 @@ void CFIE::solve()
 void CFIE::output()
 {
     emfa_fill_params_t fp{EMFA_CFIE, precision_, (double)incidence_.freq, (double)alpha_, 0, 0, 0};
-    writeBistatic(fp, I_);
-    timeLog("getBistaticRCS");
+    if (rtype_ == policy::MonoRCS) {
+        writeMonostatic(fp, I_);
+        timeLog("getMonostaticRCS");
+    } else {
+        writeBistatic(fp, I_);
+        timeLog("getBistaticRCS");
+    }
 }
 
 void CFIE::clear()
@@ -523,8 +595,11 @@ void MLFMA::init(ConfigLoader* ploader)
     threshold_ = ploader->getMLFMABoxThreshold();
     ploader->getThreadNumber();
     ploader->getTaskFactor();
+    const std::string trunc = ploader->getGpu("gpu_mlfma_truncation:", "reference");
+    if (trunc != "reference" && trunc != "config")
+        throw ConfigInvalid("gpu_mlfma_truncation: must be reference or config");
     emfa_mlfma_params_t mp{(double)incidence_.freq, (double)alpha_, (double)threshold_, precond_ ? 1 : 0,
-                           (double)row_thr, (double)col_thr};
+                           (double)row_thr, (double)col_thr, trunc == "config" ? 1 : 0};
     check(emfa_mlfma_create(ctx_, geom_, &mp, &ml_), ctx_, "MLFMA init");
     check(emfa_mlfma_info(ml_, &levels_, nullptr, nullptr, nullptr, nullptr), ctx_, "MLFMA info");
     logger_ << ploader->getReport();
@@ -540,31 +615,35 @@ void MLFMA::reportInfo(std::ostream& strm) const
 
 void MLFMA::solve()
 {
-    const size_t n = unknowns_;
-    check(emfa_device_alloc(ctx_, 8 * n, &V_), ctx_, "alloc V");
-    check(emfa_device_alloc(ctx_, 16 * n, &Ibox_), ctx_, "alloc I");
-    check(emfa_device_alloc(ctx_, 16 * n, &I_), ctx_, "alloc I");
-    double ang[3] = {incidence_.theta, incidence_.phi, incidence_.pole};
-    check(emfa_mlfma_fill_v(ml_, ang, 1, V_, nullptr), ctx_, "fillVbyBox");
+    const size_t n = unknowns_, r = n_inc_;
+    check(emfa_device_alloc(ctx_, 8 * n * r, &V_), ctx_, "alloc V");
+    check(emfa_device_alloc(ctx_, 16 * n * r, &Ibox_), ctx_, "alloc I");
+    check(emfa_device_alloc(ctx_, 16 * n * r, &I_), ctx_, "alloc I");
+    check(emfa_mlfma_fill_v(ml_, inc_angles_.data(), n_inc_, V_, nullptr), ctx_, "fillVbyBox");
     timeLog("fillVbyBox");
     emfa_solver_params_t sp{EMFA_BICGSTAB, 30, max_iter_, tol_, 0, EMFA_MV_AUTO, 0, 0};
     emfa_solve_info_t info{};
-    emfa_status_t s = emfa_mlfma_solve(ml_, V_, 1, Ibox_, &sp, &info, nullptr);
+    emfa_status_t s = emfa_mlfma_solve(ml_, V_, n_inc_, Ibox_, &sp, &info, nullptr);
     if (s == EMFA_ERR_NOT_CONVERGED)
         logger_ << "    WARNING: Iteration cannot converge\n";
     else
         check(s, ctx_, "iterativeSolve");
     logger_ << "    Iterative number: " << info.iterations << '\n';
     std::cout << "    Iterative number: " << info.iterations << std::endl;
-    check(emfa_mlfma_unpermute(ml_, Ibox_, 1, I_, nullptr), ctx_, "unpermute");
+    check(emfa_mlfma_unpermute(ml_, Ibox_, n_inc_, I_, nullptr), ctx_, "unpermute");
     timeLog("iterativeSolve");
 }
 
 void MLFMA::output()
 {
     emfa_fill_params_t fp{EMFA_CFIE, EMFA_F32, (double)incidence_.freq, (double)alpha_, 0, 0, 0};
-    writeBistatic(fp, I_);
-    timeLog("getBistaticRCS");
+    if (rtype_ == policy::MonoRCS) {
+        writeMonostatic(fp, I_);
+        timeLog("getMonostaticRCS");
+    } else {
+        writeBistatic(fp, I_);
+        timeLog("getBistaticRCS");
+    }
 }
 
 void MLFMA::clear()

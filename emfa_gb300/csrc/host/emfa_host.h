@@ -109,6 +109,20 @@ protected:
     void timeLog(const std::string& what);
     void openContext(component::ConfigLoader* ploader);
     void writeBistatic(const emfa_fill_params_t& fp, const void* I_dev);
+    // MonostaticRCS: one incidence per direction of Result::getMonostaticRCS
+    // (EMComponent/Result.h:106-155), in its order -- the phi cuts over theta,
+    // then the theta = 90 ring -- each seen from its backscatter direction
+    void planMonostatic();
+    void writeMonostatic(const emfa_fill_params_t& fp, const void* I_dev);
+    // the run's incidences (theta, phi, pole in degrees, n_inc_ of them)
+    std::vector<double> inc_angles_;
+    int n_inc_ = 1;
+    struct RcsFile {
+        std::string name;
+        std::vector<float> angles;
+    };
+    std::vector<RcsFile> mono_files_;
+    std::vector<double> mono_dirs_;  // n_inc_ x 3, the backscatter direction of each incidence
     component::policy::ResultType rtype_ = component::policy::BiRCS;
     component::Incidence incidence_{};
     component::Scattering scattering_{};
@@ -134,6 +148,7 @@ public:
 private:
     std::complex<float> sigma_;
     float tol_ = 1e-3f;
+    int disc_ = EMFA_DISC_REFERENCE;  // gpu_discretisation: reference | config
     void* Z_ = nullptr;
     void* V_ = nullptr;
     void* I_ = nullptr;
@@ -148,6 +163,7 @@ public:
 
 private:
     float alpha_ = 1.0f;
+    float tol_ = 0.01f;
     void* Z_ = nullptr;
     void* V_ = nullptr;
     void* I_ = nullptr;

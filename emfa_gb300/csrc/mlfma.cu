@@ -948,7 +948,9 @@ static bool build_plan(const std::vector<double>& verts, int nv, const std::vect
     for (int l = 2; l <= L; ++l) {
         int i = l - 2;
         float kdl = 1.732051f * k * blen[l];
-        int Pm = (int)(kdl + 6 * cbrtf(kdl));
+        // the reference's rule, or the excess-bandwidth rule of the
+        // configuration (d0 = 3 digits: d0^(2/3) = 9^(1/3))
+        int Pm = prm.truncation == 1 ? (int)(kdl + 1.8f * cbrtf(9.0f) * cbrtf(kdl)) : (int)(kdl + 6 * cbrtf(kdl));
         P.poles[i] = Pm;
         std::vector<float> rt, wt, rp, wp;
         mh::gauss_legendre(Pm, rt, wt);
@@ -1534,7 +1536,8 @@ extern "C" {
 
 emfa_status_t emfa_mlfma_create(emfa_ctx_t* ctx, emfa_geom_t* geom, const emfa_mlfma_params_t* p, emfa_mlfma_t** out)
 {
-    if (!ctx || !geom || !p || !out || !(p->freq > 0) || !(p->box_threshold > 0)) {
+    if (!ctx || !geom || !p || !out || !(p->freq > 0) || !(p->box_threshold > 0) ||
+        (p->truncation != 0 && p->truncation != 1)) {
         set_error(ctx, "emfa_mlfma_create: bad arguments");
         return EMFA_ERR_INVALID;
     }
@@ -1560,6 +1563,10 @@ emfa_status_t emfa_mlfma_plan(const double* verts_host, int n_vert, const int* r
                               int* perm)
 {
     if (!verts_host || !rwg_host || !p || n_vert <= 0 || n_rwg <= 0 || !levels) return EMFA_ERR_INVALID;
+    if (p->truncation != 0 && p->truncation != 1) {
+        set_global_error("emfa_mlfma_plan: truncation must be 0 or 1");
+        return EMFA_ERR_INVALID;
+    }
     std::vector<double> v(verts_host, verts_host + 3 * (size_t)n_vert);
     std::vector<int> r(rwg_host, rwg_host + 6 * (size_t)n_rwg);
     Plan P;

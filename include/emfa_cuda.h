@@ -59,6 +59,15 @@ typedef enum {
                        /* FP32 sums across blocks, B - Z x formed in FP64            */
 } emfa_matvec_t;
 
+/* Discretisation of the EFIE fill.  EMFA_DISC_REFERENCE: the reference's own,
+ * 3 x 3-point regular pairs and singularity extraction on self pairs only
+ * (EMSolver/EFIE.cpp:139-160,231-542,655-662).  EMFA_DISC_CONFIG: the
+ * discretisation the benchmark configurations state, 7 x 7-point regular
+ * pairs and singularity extraction on self and edge-adjacent triangle pairs
+ * (closed-form potential integrals for points on or off the source plane);
+ * EFIE only.  No counterpart in the reference. */
+typedef enum { EMFA_DISC_REFERENCE = 0, EMFA_DISC_CONFIG = 1 } emfa_discretisation_t;
+
 typedef struct emfa_ctx emfa_ctx_t;
 typedef struct emfa_geom emfa_geom_t;
 typedef struct emfa_mlfma emfa_mlfma_t;
@@ -77,6 +86,7 @@ typedef struct {
     int edm_mode;       /* EFIE pairs farther than 3 lambda: 0 = zero, as in the    */
                         /* matrix the reference solves; 1 = equivalent-dipole value;*/
                         /* 2 = ordinary quadrature (no far-pair branch)             */
+    int discretisation; /* emfa_discretisation_t; 0 is the reference's              */
 } emfa_fill_params_t;
 
 typedef struct {
@@ -262,6 +272,11 @@ typedef struct {
     double row_threshold;  /* SAI rows / columns: near unknowns whose centre lies     */
     double col_threshold;  /* within this many finest-box lengths of the box centre   */
                            /* (row_threshold:, col_threshold:; MLFMA.cpp:719-720)     */
+    int truncation;        /* multipoles per level from kd = sqrt(3) k box side:      */
+                           /* 0 = the reference's int(kd + 6 kd^(1/3))                */
+                           /* (MLFMA::getMultipoleNumber, MLFMA.cpp:877-881);         */
+                           /* 1 = the configuration's int(kd + 1.8 d0^(2/3) kd^(1/3)) */
+                           /* with d0 = 3 digits (no counterpart in the reference)    */
 } emfa_mlfma_params_t;
 
 /* Host only (no GPU): the octree plan the operator is built on -- finest

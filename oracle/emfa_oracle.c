@@ -573,3 +573,141 @@ void PFX(incidence)(r_t theta_deg, r_t phi_deg, r_t pole_deg, r_t* out9)
     r_t o[9] = {kk.x, kk.y, kk.z, ee.x, ee.y, ee.z, hh.x, hh.y, hh.z};
     memcpy(out9, o, sizeof o);
 }
+
+/* ---- the configurations' discretisation of the EFIE (not the reference's):
+ * 7 x 7-point regular pairs, singularity extraction on self and
+ * edge-adjacent triangle pairs.  For a singular pair, with
+ * G = e^{-jkR}/R = 1/R + Gs(R), Gs = (e^{-jkR} - 1)/R (Gs(0) = -jk):
+ *   sum_p sum_q w_p w_q [(P_p - vf).(Q_q - vs)/4 - 1/k^2] Gs(R_pq)
+ * + sum_p w_p [(P_p - vf).(I_rho(P_p) + (rho_p - vs) I_1(P_p))/4
+ *              - I_1(P_p)/k^2] / A_s
+ * where I_1 = int 1/R and I_rho = int (rho' - rho)/R over the source
+ * triangle are the closed forms of Wilton et al. (IEEE Trans. Antennas
+ * Propag. 32, 1984, pp. 276-281) for an observation point anywhere.  Pairs
+ * are adjacent when the triangles share two vertex indices. ---- */
+void PFX(potential_integrals)(const r_t* tri9, const r_t* r3, r_t* I1_out, r_t* Irho3)
+{
+    v3 t[3] = {V(tri9[0], tri9[1], tri9[2]), V(tri9[3], tri9[4], tri9[5]), V(tri9[6], tri9[7], tri9[8])};
+    v3 r = V(r3[0], r3[1], r3[2]);
+    v3 n = vnormalize(vcross(vsub(t[1], t[0]), vsub(t[2], t[0])));
+    r_t h = vdot(vsub(r, t[0]), n), ah = fabs(h);
+    v3 rho = vsub(r, vmul(n, h));
+    r_t I1 = 0;
+    v3 Ir = V(0, 0, 0);
+    for (int i = 0; i < 3; ++i) {
+        v3 b = t[i], a = t[(i + 1) % 3];
+        v3 l = vnormalize(vsub(a, b));
+        v3 u = vcross(l, n);
+        r_t lp = vdot(vsub(a, rho), l), lm = vdot(vsub(b, rho), l);
+        r_t sd = vdot(vsub(b, rho), u);
+        r_t p0 = fabs(sd);
+        r_t r02 = p0 * p0 + h * h;
+        r_t rp = sqrt(r02 + lp * lp), rm = sqrt(r02 + lm * lm);
+        r_t lg = 0;
+        if (r02 > 0) {
+            /* R + l, written R0^2 / (R - l) where l < 0 (no cancellation) */
+            r_t fa = lp >= 0 ? rp + lp : r02 / (rp - lp);
+            r_t fb = lm >= 0 ? rm + lm : r02 / (rm - lm);
+            lg = log(fa / fb);
+        }
+        Ir = vadd(Ir, vmul(u, (r_t)0.5 * (r02 * lg + lp * rp - lm * rm)));
+        if (p0 > 0) {
+            r_t sg = sd > 0 ? ONE : -ONE;
+            I1 += sg * (p0 * lg - ah * (atan(p0 * lp / (r02 + ah * rp)) - atan(p0 * lm / (r02 + ah * rm))));
+        }
+    }
+    *I1_out = I1;
+    Irho3[0] = Ir.x;
+    Irho3[1] = Ir.y;
+    Irho3[2] = Ir.z;
+}
+
+static cx efie_cfg_pair(r_t k, cx sigma, const v3* vf3, const v3* vs3, v3 vf, v3 vs, int self, int singular)
+{
+    v3 P[7], Q[7];
+    gauss7(vf3[0], vf3[1], vf3[2], P);
+    gauss7(vs3[0], vs3[1], vs3[2], Q);
+    r_t ik2 = ONE / (k * k);
+    cx z = C(0, 0);
+    for (int p = 0; p < 7; ++p) {
+        v3 rf = vsub(P[p], vf);
+        for (int q = 0; q < 7; ++q) {
+            r_t R = vnorm(vsub(P[p], Q[q]));
+            r_t e = w7c(p) * w7c(q) * ((r_t)0.25 * vdot(rf, vsub(Q[q], vs)) - ik2);
+            cx g;
+            if (!singular) {
+                g = cdivr(expmj(k * R), R);
+            } else if (R > 0) {
+                r_t sh = sin((r_t)0.5 * k * R);
+                g = C((r_t)-2 * sh * sh / R, -sin(k * R) / R);
+            } else {
+                g = C(0, -k);
+            }
+            z = cadd(z, cscale(g, e));
+        }
+    }
+    if (singular) {
+        r_t As = tri_area(vs3[0], vs3[1], vs3[2]);
+        v3 ns = vnormalize(vcross(vsub(vs3[1], vs3[0]), vsub(vs3[2], vs3[0])));
+        r_t tri9[9] = {vs3[0].x, vs3[0].y, vs3[0].z, vs3[1].x, vs3[1].y, vs3[1].z, vs3[2].x, vs3[2].y, vs3[2].z};
+        r_t acc = 0;
+        for (int p = 0; p < 7; ++p) {
+            r_t r3[3] = {P[p].x, P[p].y, P[p].z}, I1, Ir3[3];
+            PFX(potential_integrals)(tri9, r3, &I1, Ir3);
+            v3 rho = vsub(P[p], vmul(ns, vdot(vsub(P[p], vs3[0]), ns)));
+            v3 rs = vadd(V(Ir3[0], Ir3[1], Ir3[2]), vmul(vsub(rho, vs), I1));
+            acc += w7c(p) * ((r_t)0.25 * vdot(vsub(P[p], vf), rs) - I1 * ik2);
+        }
+        z.re += acc / As;
+        if (self && sqrt(sigma.re * sigma.re + sigma.im * sigma.im) > (r_t)1e-8) {
+            r_t s2 = 0;
+            for (int i = 0; i < 7; ++i) s2 += w7c(i) * vdot(vsub(P[i], vf), vsub(P[i], vs));
+            r_t den = As * k * Z0_;
+            z.re += PI_ * sigma.im / den * s2;
+            z.im -= PI_ * sigma.re / den * s2;
+        }
+    }
+    return z;
+}
+
+static int shares_edge(const int* a, const int* b)
+{
+    int c = 0;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) c += a[i] == b[j];
+    return c >= 2;
+}
+
+void PFX(fill_z_efie_cfg)(const r_t* verts, const int* tris, const int* rwg, const r_t* len, int n, r_t k,
+                           r_t sig_re, r_t sig_im, r_t* Zout)
+{
+    mesh_t m = {verts, tris, rwg, len, n};
+    cx sigma = C(sig_re, sig_im);
+    cx coef = C(0, k * Z0_ / PI4_);
+    for (int f = 0; f < n; ++f) {
+        const int* rf = rwg + 6 * f;
+        v3 vff[2] = {vtx(&m, rf[2]), vtx(&m, rf[3])};
+        v3 tf[2][3];
+        tri3(&m, rf[4], tf[0]);
+        tri3(&m, rf[5], tf[1]);
+        for (int s = 0; s < n; ++s) {
+            const int* rs = rwg + 6 * s;
+            v3 vss[2] = {vtx(&m, rs[2]), vtx(&m, rs[3])};
+            v3 ts[2][3];
+            tri3(&m, rs[4], ts[0]);
+            tri3(&m, rs[5], ts[1]);
+            cx sum = C(0, 0);
+            for (int a = 0; a < 2; ++a)
+                for (int b = 0; b < 2; ++b) {
+                    int ia = rf[4 + a], ib = rs[4 + b];
+                    int self = ia == ib;
+                    int sing = self || shares_edge(tris + 3 * ia, tris + 3 * ib);
+                    cx z = efie_cfg_pair(k, sigma, tf[a], ts[b], vff[a], vss[b], self, sing);
+                    sum = cadd(sum, cscale(z, a == b ? ONE : -ONE));
+                }
+            cx zz = cmul(cscale(cscale(coef, len[f]), len[s]), sum);
+            Zout[2 * ((size_t)f * n + s)] = zz.re;
+            Zout[2 * ((size_t)f * n + s) + 1] = zz.im;
+        }
+    }
+}

@@ -112,6 +112,29 @@ def fill_z_cfie(g: Geometry, k, alpha):
     return Z[..., 0] + 1j * Z[..., 1]
 
 
+def fill_z_efie_cfg(g: Geometry, k, sigma=(0.0, 0.0)):
+    """EFIE in the configurations' discretisation (not the reference's): 7 x
+    7-point regular pairs, singularity extraction on self and edge-adjacent
+    pairs (emfa_oracle.c, fill_z_efie_cfg)."""
+    dt, ct, pf = _rt(g.prec)
+    Z = np.zeros((g.n, g.n, 2), dtype=dt)
+    getattr(lib(), pf + "fill_z_efie_cfg")(_p(g.verts), _p(g.tris), _p(g.rwg), _p(g.len), ctypes.c_int(g.n), ct(k),
+                                           ct(sigma[0]), ct(sigma[1]), _p(Z))
+    return Z[..., 0] + 1j * Z[..., 1]
+
+
+def potential_integrals(tri, r, prec=64):
+    """(int_T 1/R dS', int_T (rho' - rho)/R dS') for triangle tri (3 x 3) and
+    observation point r, by the closed forms the configuration fill uses."""
+    dt, _, pf = _rt(prec)
+    t = np.ascontiguousarray(tri, dtype=dt).reshape(9)
+    rr = np.ascontiguousarray(r, dtype=dt).reshape(3)
+    i1 = np.zeros(1, dtype=dt)
+    ir = np.zeros(3, dtype=dt)
+    getattr(lib(), pf + "potential_integrals")(_p(t), _p(rr), _p(i1), _p(ir))
+    return float(i1[0]), ir.astype(np.float64)
+
+
 def fill_v(g: Geometry, k, inc, cfie=False, alpha=1.0):
     dt, ct, pf = _rt(g.prec)
     inc = np.ascontiguousarray(np.atleast_2d(inc), dtype=dt)

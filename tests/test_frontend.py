@@ -95,3 +95,54 @@ def test_launcher_mlfma_vs_reference(emfa_lib, precond):
     lines = open(os.path.join(out, "bistatic_rcs_phi_0.dat")).read().splitlines()
     vals = np.array([float(l.split()[1]) for l in lines[1:]])
     assert np.abs(vals - g["rcs"][:181]).max() < 0.1
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("solver", ["efie", "cfie"])
+def test_launcher_monostatic_sweep(emfa_lib, oracle_mod, solver):
+    """result_type: MonostaticRCS writes the reference's monostatic layout
+    (Result::getMonostaticRCS, EMComponent/Result.h:106-155): one file per phi
+    cut over theta, then the theta = 90 ring, each value the backscatter RCS
+    of its own incidence, all solved as one block of right-hand sides.  Each
+    of the 374 values is checked against a separate solve of that incidence
+    by the oracle restatement of the reference's fill, excitation and RCS
+    (FP64, direct solve), within 0.01 dB; the solver runs to a tight
+    tolerance (gpu_efie_tol / gpu_cfie_tol) in FP64."""
+    O = oracle_mod
+    g = load_golden("sphere1_" + solver)
+    d = tempfile.mkdtemp()
+    nas = os.path.join(d, "sph.nas")
+    M.write_nas(M.TriMesh(g["verts"], g["tris"]), nas)
+    cfg = os.path.join(d, "CONFIG.yml")
+    M.write_config(cfg, EMSolver=solver.upper(), mesh_path=nas, frequency="3e8", alpha="0.5",
+                   result_type="MonostaticRCS", theta_from="0", theta_to="180", theta_delta="30", phi_from="0",
+                   phi_to="90", phi_delta="90", pole="0", gpu_precision="f64", gpu_efie_tol="1e-10",
+                   gpu_cfie_tol="1e-10")
+    r = run([cfg], cwd=d)
+    assert "Exit State: OK" in r.stdout, r.stdout[-2000:] + r.stderr[-2000:]
+    out = os.path.join(d, "sph_EFIE" if solver == "efie" else "sph_CFIE_0.5")
+    angles, vals = [], []
+    for fn, phi in (("monostatic_rcs_phi_0.dat", 0.0), ("monostatic_rcs_phi_90.dat", 90.0),
+                    ("monostatic_rcs_theta_90.dat", None)):
+        lines = open(os.path.join(out, fn)).read().splitlines()
+        assert lines[0].split() == ["Theta", "RCS(dBm^2)"]
+        rows = [l.split() for l in lines[1:]]
+        assert len(rows) == (7 if phi is not None else 360)
+        for a, v in rows:
+            angles.append((float(a), phi) if phi is not None else (90.0, float(a)))
+            vals.append(float(v))
+    assert not os.path.exists(os.path.join(out, "bistatic_rcs_phi_0.dat"))
+    ang = np.array(angles)
+    og = O.Geometry(g["verts"], g["tris"], g["rwg"], 64)
+    k = O.wavenumber(3e8, 64)
+    if solver == "efie":
+        Z = O.fill_z_efie(og, k)
+    else:
+        Z = O.fill_z_cfie(og, k, 0.5)
+    inc = np.stack([O.incidence(t, p, 0.0, prec=64) for t, p in ang])
+    V = O.fill_v(og, k, inc, cfie=solver == "cfie", alpha=0.5)
+    I = np.linalg.solve(Z, V.T).T
+    th, ph = np.deg2rad(ang[:, 0]), np.deg2rad(ang[:, 1])
+    dirs = np.stack([np.sin(th) * np.cos(ph), np.sin(th) * np.sin(ph), np.cos(th)], 1)
+    ref = np.array([O.rcs(og, k, I[i:i + 1], dirs[i:i + 1])[0, 0] for i in range(len(ang))])
+    assert np.abs(np.array(vals) - ref).max() < 0.01, np.abs(np.array(vals) - ref).max()

@@ -321,3 +321,26 @@ def test_c3_solve_and_rcs(c3):
     keep = ref > ref.max() - 20.0
     assert np.abs(r - ref)[keep].max() < 0.1, np.abs(r - ref)[keep].max()
     del torch
+
+
+def test_c1_config_discretisation_against_mie(dense):
+    """C1 in the discretisation the configuration states (7-point rule,
+    self and edge-adjacent extraction): FP64 fill, GMRES to 1e-8; its
+    bistatic RCS against the Mie series is no worse than the reference
+    discretisation's (0.18 dB), and both errors are reported by the bench."""
+    from emfa_gb300 import api
+    from oracle import mie
+    c, g = dense["c1_efie_sphere_1920"], dense["c1_efie_sphere_1920"]["g"]
+    c.pop("Z32", None)
+    c.pop("Z64", None)
+    fp = api.fill_params("efie", "f64", 3e8, 1.0, discretisation="config")
+    Z = api.fill_z(c["geo"], fp)
+    V = api.fill_v(c["geo"], fp, angles(g))
+    X, info = api.solve(c["geo"].ctx, Z, V, api.solver_params("gmres", restart=30, tol=1e-8, max_iter=20000))
+    assert info.converged == 1
+    d = g["rcs_dirs_f64"].astype(np.float64)
+    r = api.rcs(c["geo"], fp, X, d)[0]
+    inc = g["inc_f64"][0]
+    exact = mie.pec_sphere_rcs_db(0.5, 3e8, inc[:3], inc[3:6], d)
+    ref_err = np.abs(g["rcs_f64"][0] - exact).max()
+    assert np.abs(r - exact).max() <= ref_err, (np.abs(r - exact).max(), ref_err)

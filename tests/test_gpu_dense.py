@@ -353,3 +353,30 @@ def test_bounded_wait_gives_up_and_context_survives(ctx):
     Y = api.matvec(ctx, torch.from_numpy(Z).cuda(), torch.from_numpy(X).cuda(), "tf32").cpu().numpy()
     ref = X.astype(np.complex128) @ Z.astype(np.complex128).T
     assert np.linalg.norm(Y - ref) / np.linalg.norm(ref) < 3e-3
+
+
+@pytest.mark.parametrize("name", ["sphere1_efie", "sphere2_cfie"])
+def test_config_discretisation_fill_matches_oracle(ctx, oracle_mod, name):
+    """EMFA_DISC_CONFIG (7 x 7 points, self and edge-adjacent extraction):
+    the FP64 GPU fill against the oracle's FP64 restatement of the same
+    rule, floored per entry 1e-11; the FP32 fill normwise within 2e-5 (the
+    FP32 regular pairs) of the FP64 oracle."""
+    from emfa_gb300 import api
+    g = load_golden(name)
+    geo = golden_geometry(ctx, g)
+    og = oracle_mod.Geometry(g["verts"], g["tris"], g["rwg"], 64)
+    Zo = oracle_mod.fill_z_efie_cfg(og, oracle_mod.wavenumber(3e8, 64))
+    fp = api.fill_params("efie", "f64", 3e8, 1.0, edm_mode=2, discretisation="config")
+    Z = api.fill_z(geo, fp).cpu().numpy()
+    assert floored_rel(Z, Zo).max() < 1e-11, floored_rel(Z, Zo).max()
+    fp32 = api.fill_params("efie", "f32", 3e8, 1.0, edm_mode=2, discretisation="config")
+    Z32 = api.fill_z(geo, fp32).cpu().numpy()
+    assert np.linalg.norm(Z32 - Zo) / np.linalg.norm(Zo) < 2e-5
+
+
+def test_config_discretisation_rejects_cfie(ctx):
+    from emfa_gb300 import api, _lib
+    g = load_golden("sphere1_cfie")
+    geo = golden_geometry(ctx, g)
+    with pytest.raises(_lib.EmfaError):
+        api.fill_z(geo, api.fill_params("cfie", "f32", 3e8, 0.5, discretisation="config"))

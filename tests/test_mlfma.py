@@ -206,3 +206,52 @@ def test_sai_preconditioned_solve(ops, sai, method):
     a, b = X1.cpu().numpy()[0], X0.cpu().numpy()[0]
     assert np.linalg.norm(a - b) / np.linalg.norm(b) < 2e-3
     assert i1.iterations < i0.iterations, (i1.iterations, i0.iterations)
+
+
+def test_plan_with_the_configuration_truncation(emfa_lib):
+    """truncation "config" (int(kd + 1.8 d0^(2/3) kd^(1/3)), d0 = 3): the same
+    tree and box order as the reference's rule, fewer multipoles per level,
+    and exactly the formula's count given the reference's (both from the
+    same kd = sqrt(3) k side, with side halving per level)."""
+    from emfa_gb300 import api
+    g = load_golden("sphere3_mlfma")
+    mesh = M.TriMesh(g["verts"], g["tris"])
+    p_ref = params(g)
+    m = g["meta"]
+    p_cfg = api.mlfma_params(float(m["frequency"]), float(np.float32(float(m["alpha"]))),
+                             float(np.float32(float(m["mlfma_box_threshold"]))), truncation="config")
+    lev_r, lb_r, poles_r, perm_r = api.mlfma_plan(mesh, g["rwg"], p_ref)
+    lev_c, lb_c, poles_c, perm_c = api.mlfma_plan(mesh, g["rwg"], p_cfg)
+    assert lev_r == lev_c and np.array_equal(lb_r, lb_c) and np.array_equal(perm_r, perm_c)
+    assert np.all(poles_c < poles_r)
+    # kd of the finest level from its reference count, then each coarser level doubles it
+    for i in range(len(poles_r)):
+        kd_lo = [x for x in np.linspace(0.1, 200, 400001) if int(x + 6 * np.cbrt(x)) == poles_r[i]]
+        lo, hi = min(kd_lo), max(kd_lo)
+        cands = {int(x + 1.8 * np.cbrt(9.0) * np.cbrt(x)) for x in np.linspace(lo, hi, 200)}
+        assert poles_c[i] in cands, (i, poles_c[i], cands)
+
+
+@pytest.mark.gpu
+def test_solve_with_the_configuration_truncation(ops):
+    """The operator with the configuration's multipole truncation: GMRES to
+    1e-4 gives a bistatic RCS within 0.1 dB of the reference-truncation
+    operator's over the pattern's top 20 dB."""
+    import torch
+    from emfa_gb300 import api
+    g, geo, ml = ops["sphere3_mlfma"]
+    m = g["meta"]
+    mlc = api.Mlfma(geo, api.mlfma_params(float(m["frequency"]), float(np.float32(float(m["alpha"]))),
+                                          float(np.float32(float(m["mlfma_box_threshold"]))), truncation="config"))
+    sp = api.solver_params("gmres", restart=30, tol=1e-4, max_iter=300)
+    fp = api.fill_params("cfie", "f32", float(m["frequency"]), 0.5)
+    dirs = g["rcs_dirs"].astype(np.float64)
+    out = []
+    for op in (ml, mlc):
+        X, info = op.solve(op.fill_v(angles(g)), sp)
+        assert info.converged == 1
+        out.append(api.rcs(geo, fp, op.unpermute(X), dirs)[0])
+    mlc.close()
+    keep = out[0] > out[0].max() - 20.0
+    assert np.abs(out[0] - out[1])[keep].max() < 0.1, np.abs(out[0] - out[1])[keep].max()
+    del torch

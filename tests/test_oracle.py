@@ -165,3 +165,134 @@ def test_mie_series():
     exact = mie.pec_sphere_rcs_db(0.5, 3e8, inc[:3], inc[3:6], g["rcs_dirs_f64"])
     err = np.abs(g["rcs_f64"][0] - exact)
     assert err.max() < 0.2 and np.median(err) < 0.1, (err.max(), np.median(err))
+
+
+def _polar_potentials(tri, r, nq=400):
+    """int_T 1/R and int_T (rho' - rho)/R by the polar form about the
+    projection rho of r, reduced to 1-D integrals along the edges (the
+    angle integral parameterised by the edge point), Gauss-Legendre in the
+    edge parameter: an evaluation independent of the closed forms."""
+    tri = np.asarray(tri, dtype=np.float64)
+    n = np.cross(tri[1] - tri[0], tri[2] - tri[0])
+    n /= np.linalg.norm(n)
+    h = float(np.dot(r - tri[0], n))
+    rho = r - h * n
+    x, w = np.polynomial.legendre.leggauss(nq)
+    s, w = 0.5 * (x + 1), 0.5 * w
+    I1, Ir = 0.0, np.zeros(3)
+    for i in range(3):
+        b, a = tri[i], tri[(i + 1) % 3]
+        e = b[None, :] + s[:, None] * (a - b)[None, :]
+        d = e - rho[None, :]
+        rm = np.linalg.norm(d, axis=1)
+        dth = np.cross(d, (a - b)[None, :]) @ n / rm ** 2  # d theta / d s, signed
+        R = np.sqrt(rm ** 2 + h * h)
+        f1 = R - abs(h)
+        f2 = 0.5 * rm * R - (0.5 * h * h * np.log((rm + R) / abs(h)) if h != 0 else 0.0)
+        I1 += np.sum(w * f1 * dth)
+        Ir += np.sum((w * f2 * dth / rm)[:, None] * d, axis=0)
+    return I1, Ir
+
+
+@pytest.mark.parametrize("point", ["inside_in_plane", "outside_in_plane", "above_inside", "above_outside",
+                                   "near_edge_off_plane", "across_an_edge"])
+def test_potential_integrals_closed_form(oracle_mod, point):
+    """The closed-form scalar and vector potential integrals of the
+    configuration fill, for observation points on and off the source plane,
+    against the polar-form evaluation (relative 1e-10)."""
+    tri = np.array([[0.0, 0.0, 0.0], [0.11, 0.01, 0.02], [0.03, 0.09, -0.01]])
+    c = tri.mean(0)
+    n = np.cross(tri[1] - tri[0], tri[2] - tri[0])
+    n /= np.linalg.norm(n)
+    pts = {"inside_in_plane": c + 0.2 * (tri[1] - c), "outside_in_plane": c + 1.7 * (tri[2] - c),
+           "above_inside": c + 0.03 * n, "above_outside": c + 1.4 * (tri[1] - c) - 0.05 * n,
+           "near_edge_off_plane": 0.5 * (tri[0] + tri[1]) + 0.001 * n - 0.002 * (c - tri[0]),
+           "across_an_edge": 0.5 * (tri[1] + tri[2]) + 0.4 * (0.5 * (tri[1] + tri[2]) - c) + 0.01 * n}
+    r = pts[point]
+    I1, Ir = oracle_mod.potential_integrals(tri, r)
+    J1, Jr = _polar_potentials(tri, r)
+    assert abs(I1 - J1) <= 1e-10 * abs(J1), (I1, J1)
+    assert np.linalg.norm(Ir - Jr) <= 1e-10 * np.linalg.norm(Jr), (Ir, Jr)
+
+
+def _sub7(tri, level):
+    """7-point rule (the reference's, weights summing to 1) on the 4^level
+    pieces of a triangle: points and weights relative to the whole."""
+    tris = [np.asarray(tri, dtype=np.float64)]
+    for _ in range(level):
+        out = []
+        for t in tris:
+            a, b, c = t
+            ab, bc, ca = 0.5 * (a + b), 0.5 * (b + c), 0.5 * (c + a)
+            out += [np.array([a, ab, ca]), np.array([ab, b, bc]), np.array([ca, bc, c]), np.array([ab, bc, ca])]
+        tris = out
+    g7 = np.array([[0.333333333333333, 0.333333333333333], [0.797426985353087, 0.101286507323456],
+                   [0.101286507323456, 0.797426985353087], [0.101286507323456, 0.101286507323456],
+                   [0.470142064105115, 0.470142064105115], [0.470142064105115, 0.059715871789770],
+                   [0.059715871789770, 0.470142064105115]])
+    w7 = 2 * np.array([0.1125] + [0.062969590272413] * 3 + [0.066197076394253] * 3)
+    pts = np.concatenate([g7[:, :1] * t[0] + g7[:, 1:] * t[1] + (1 - g7.sum(1, keepdims=True)) * t[2] for t in tris])
+    wts = np.tile(w7, len(tris)) / len(tris)
+    return pts, wts
+
+
+def _adjacent_rwg_pair_entry(O, m, rwg, k, u, s, lo, li, lr):
+    """Z(u, s) of the EFIE with every edge-adjacent triangle pair's inner
+    integral as the closed-form 1/R part plus the bounded remainder
+    (e^{-jkR} - 1)/R by the 7-point rule on 4^li pieces, other pairs by the
+    7-point rule on 4^lr pieces, the outer integral on 4^lo pieces."""
+    V = m.verts
+    total = 0j
+    for a, sa in ((0, 1.0), (1, -1.0)):
+        tf = V[m.tris[rwg[u, 4 + a]]]
+        vf = V[rwg[u, 2 + a]]
+        P, wp = _sub7(tf, lo)
+        for b, sb in ((0, 1.0), (1, -1.0)):
+            ts = V[m.tris[rwg[s, 4 + b]]]
+            vs = V[rwg[s, 2 + b]]
+            adjacent = len(set(m.tris[rwg[u, 4 + a]]) & set(m.tris[rwg[s, 4 + b]])) == 2
+            Q, wq = _sub7(ts, li if adjacent else lr)
+            R = np.linalg.norm(P[:, None, :] - Q[None, :, :], axis=2)
+            e = 0.25 * ((P - vf) @ (Q - vs).T) - 1.0 / k ** 2
+            if not adjacent:
+                total += sa * sb * np.sum(wp[:, None] * wq[None, :] * e * np.exp(-1j * k * R) / R)
+                continue
+            total += sa * sb * np.sum(wp[:, None] * wq[None, :] * e * (np.exp(-1j * k * R) - 1) / R)
+            area = 0.5 * np.linalg.norm(np.cross(ts[1] - ts[0], ts[2] - ts[0]))
+            n = np.cross(ts[1] - ts[0], ts[2] - ts[0])
+            n /= np.linalg.norm(n)
+            for p in range(len(P)):
+                I1, Ir = O.potential_integrals(ts, P[p])
+                rho = P[p] - n * np.dot(P[p] - ts[0], n)
+                total += sa * sb * wp[p] * (0.25 * np.dot(P[p] - vf, Ir + (rho - vs) * I1) - I1 / k ** 2) / area
+    ln = np.linalg.norm(V[rwg[:, 0]] - V[rwg[:, 1]], axis=1)
+    return 1j * k * 120 * np.pi / (4 * np.pi) * ln[u] * ln[s] * total
+
+
+def test_config_fill_on_adjacent_pairs(oracle_mod):
+    """An RWG pair whose triangles are edge-adjacent (icosphere 1):
+    - assembly: the configuration fill equals the same rule written out here
+      (7 outer points x [closed-form 1/R part + 7-point remainder]) to 1e-12;
+    - accuracy: against the converged integral (outer on 4^4 pieces, inner
+      remainder on 4^5, unchanged to 1e-8 at 4^6), the configuration rule
+      is within 5e-3 (2.4e-3 measured) and 10x closer than the reference's
+      3 x 3-point rule without adjacent extraction (2.8e-2)."""
+    from emfa_gb300 import mesh as M
+    O = oracle_mod
+    m = M.icosphere(1, 0.5)
+    rwg = O.build_rwg(m.tris)
+    g = O.Geometry(m.verts, m.tris, rwg, 64)
+    k = O.wavenumber(3e8, 64)
+    Zc = O.fill_z_efie_cfg(g, k)
+    Zr = O.fill_z_efie(g, k, edm_mode=2)
+    u = 0
+    tp, tm = rwg[u, 4], rwg[u, 5]
+    s = [s for s in range(len(rwg)) if s != u and len({tp, tm} & {rwg[s, 4], rwg[s, 5]}) == 0
+         and any(len(set(m.tris[a]) & set(m.tris[b])) == 2 for a in (tp, tm) for b in (rwg[s, 4], rwg[s, 5]))][0]
+    same_rule = _adjacent_rwg_pair_entry(O, m, rwg, k, u, s, 0, 0, 0)
+    assert abs(Zc[u, s] - same_rule) <= 1e-12 * abs(same_rule)
+    exact = _adjacent_rwg_pair_entry(O, m, rwg, k, u, s, 4, 5, 4)
+    err_cfg = abs(Zc[u, s] - exact) / abs(exact)
+    err_ref = abs(Zr[u, s] - exact) / abs(exact)
+    assert err_cfg < 5e-3, (err_cfg, err_ref)
+    assert 10 * err_cfg < err_ref, (err_cfg, err_ref)
