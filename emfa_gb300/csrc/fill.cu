@@ -13,7 +13,8 @@
 // FP32 entries come from tiled kernels (k_fill_tile: the kernel values of a
 // 16 x 16 block's triangle pairs staged once); the EFIE one, whose regular
 // part is symmetric, fills the upper triangle of tiles and mirrors it
-// (k_fill_tile_sym).
+// (k_fill_tile_sym); the CFIE one fills a tile and its mirror from the same
+// staged values, the EFIE part once for both (k_fill_tile_cfie_sym).
 #include "emfa_internal.cuh"
 #include "emfa_math.cuh"
 #include "fill_entry.cuh"
@@ -744,6 +745,181 @@ __global__ void __launch_bounds__(256) k_fill_tile_sym(const RwgPack<float>* __r
     if (sr_ < n && fc_ < n) Z[(size_t)sr_ * ldz + fc_] = zt[ty][tx];
 }
 
+// Symmetric-pair CFIE fill: a CTA takes a tile pair (bf <= bs) and fills
+// both Z(bf, bs) and, off the diagonal, Z(bs, bf).  With d = P - Q,
+// rf = P - vf and rs = Q - vs, an entry's regular pair sums
+//   EFIE part  (rf.rs/4 - 1/k^2) G            (the same both ways)
+//   MFIE part  m H,  m = (rf.d)(nf.rs) - (rf.rs)(nf.d)        for Z(f, s)
+//              m' H, m' = (rf.rs)(ns.d) - (rs.d)(ns.rf)       for Z(s, f)
+// (the test field of Z(s, f) is Q on the source triangle, its source P,
+// so d changes sign), with G = e^{-jkR}/R and H = (1 + jkR) G / R^2 the
+// same both ways.  G and H of every point pair of the tiles' triangle pairs
+// are staged once (16 bytes a point pair, so three CTAs fit an SM); nf.d
+// and ns.d are formed per entry from d.  Self pairs take the FP64 table
+// with the field and source corners exchanged for the mirrored entry.  The
+// mirrored tile is staged through shared memory and stored a row at a time.
+__global__ void __launch_bounds__(256, 3) k_fill_tile_cfie_sym(const RwgPack<float>* __restrict__ rw, int n,
+                                                               FillConst<float> c, const double2* __restrict__ sing,
+                                                               const float* __restrict__ tri_q3,
+                                                               const float* __restrict__ tri_n,
+                                                               const int* __restrict__ blk_tris,
+                                                               const int* __restrict__ blk_nt,
+                                                               const unsigned char* __restrict__ loc, int maxt,
+                                                               int nb, Cx<float>* __restrict__ Z, size_t ldz)
+{
+    extern __shared__ float4 sk[];               // [maxt][maxt][9] (G re, G im, H re, H im)
+    float4* sqf = sk + (size_t)maxt * maxt * 9;  // test points [maxt][3]
+    float4* sqs = sqf + maxt * 3;                // source points [maxt][3]
+    float4* snf = sqs + maxt * 3;                // test normals [maxt]
+    float4* sns = snf + maxt;                    // source normals [maxt]
+    __shared__ Cx<float> zt[FT][FT + 1];         // the mirrored tile, [s][f]
+    const long long li = blockIdx.x;
+    int bf = (int)(((2.0 * nb + 1.0) - sqrt((2.0 * nb + 1.0) * (2.0 * nb + 1.0) - 8.0 * (double)li)) / 2.0);
+    auto row0 = [&](int b) { return (long long)b * nb - (long long)b * (b - 1) / 2; };
+    while (bf > 0 && row0(bf) > li) --bf;
+    while (bf + 1 < nb && row0(bf + 1) <= li) ++bf;
+    const int bs = bf + (int)(li - row0(bf));
+    const int ntf = blk_nt[bf], nts = blk_nt[bs];
+    const int* tf_ids = blk_tris + (size_t)bf * maxt;
+    const int* ts_ids = blk_tris + (size_t)bs * maxt;
+    for (int i = threadIdx.x; i < ntf * 3; i += blockDim.x) {
+        const float* q = tri_q3 + 9 * (size_t)tf_ids[i / 3] + 3 * (i % 3);
+        sqf[i] = make_float4(q[0], q[1], q[2], 0.0f);
+    }
+    for (int i = threadIdx.x; i < nts * 3; i += blockDim.x) {
+        const float* q = tri_q3 + 9 * (size_t)ts_ids[i / 3] + 3 * (i % 3);
+        sqs[i] = make_float4(q[0], q[1], q[2], 0.0f);
+    }
+    for (int i = threadIdx.x; i < ntf; i += blockDim.x) {
+        const float* q = tri_n + 3 * (size_t)tf_ids[i];
+        snf[i] = make_float4(q[0], q[1], q[2], 0.0f);
+    }
+    for (int i = threadIdx.x; i < nts; i += blockDim.x) {
+        const float* q = tri_n + 3 * (size_t)ts_ids[i];
+        sns[i] = make_float4(q[0], q[1], q[2], 0.0f);
+    }
+    __syncthreads();
+    for (int pr = threadIdx.x; pr < ntf * nts; pr += blockDim.x) {
+        const int tf = pr / nts, ts = pr - tf * nts;
+        float4* o4 = sk + ((size_t)tf * maxt + ts) * 9;
+#pragma unroll
+        for (int p = 0; p < 3; ++p) {
+            const float4 P = sqf[3 * tf + p];
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                const float4 Q = sqs[3 * ts + q];
+                const float dx = P.x - Q.x, dy = P.y - Q.y, dz = P.z - Q.z;
+                const float r = sqrtf(dx * dx + dy * dy + dz * dz);
+                const float rinv = 1.0f / r;
+                float sn, cs;
+                sincos_pi_taylor(r * c.kpi, &sn, &cs);
+                const float gr = cs * rinv, gi = -sn * rinv;
+                const float kr = r * c.k, r2 = rinv * rinv;
+                o4[3 * p + q] = make_float4(gr, gi, (gr - kr * gi) * r2, (gi + kr * gr) * r2);
+            }
+        }
+    }
+    __syncthreads();
+    const int ty = threadIdx.x >> 4, tx = threadIdx.x & 15;
+    const int f = bf * FT + ty, s = bs * FT + tx;
+    const bool mirror = bf != bs;
+    Cx<float> out = cx(0.0f, 0.0f), out_t = cx(0.0f, 0.0f);
+    if (f < n && s < n) {
+        const RwgPack<float>& F = rw[f];
+        const RwgPack<float>& S = rw[s];
+        float zer = 0, zei = 0, zmr = 0, zmi = 0, ztr = 0, zti = 0;
+        double sr = 0.0, si = 0.0, sr_t = 0.0, si_t = 0.0;
+#pragma unroll 1
+        for (int a = 0; a < 2; ++a) {
+            const int lf = loc[2 * (size_t)f + a];
+            float P[3][3], rf[3][3];
+            const float4 nf = snf[lf];
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                const float4 t = sqf[3 * lf + i];
+                P[i][0] = t.x;
+                P[i][1] = t.y;
+                P[i][2] = t.z;
+                rf[i][0] = t.x - F.v[a][0];
+                rf[i][1] = t.y - F.v[a][1];
+                rf[i][2] = t.z - F.v[a][2];
+            }
+#pragma unroll 1
+            for (int b = 0; b < 2; ++b) {
+                const float sgn = (a == b) ? 1.0f : -1.0f;
+                if (F.tri[a] == S.tri[b]) {
+                    const double2 v = sing[9 * F.tri[a] + 3 * F.e[a] + S.e[b]];
+                    sr += (double)sgn * v.x;
+                    si += (double)sgn * v.y;
+                    const double2 vt = sing[9 * S.tri[b] + 3 * S.e[b] + F.e[a]];
+                    sr_t += (double)sgn * vt.x;
+                    si_t += (double)sgn * vt.y;
+                    continue;
+                }
+                const int ls = loc[2 * (size_t)s + b];
+                const float4 ns = sns[ls];
+                float Q[3][3], rs[3][3], nfrs[3], nsrf[3];
+#pragma unroll
+                for (int q = 0; q < 3; ++q) {
+                    const float4 t = sqs[3 * ls + q];
+                    Q[q][0] = t.x;
+                    Q[q][1] = t.y;
+                    Q[q][2] = t.z;
+                    rs[q][0] = t.x - S.v[b][0];
+                    rs[q][1] = t.y - S.v[b][1];
+                    rs[q][2] = t.z - S.v[b][2];
+                    nfrs[q] = nf.x * rs[q][0] + nf.y * rs[q][1] + nf.z * rs[q][2];
+                }
+#pragma unroll
+                for (int p = 0; p < 3; ++p) nsrf[p] = ns.x * rf[p][0] + ns.y * rf[p][1] + ns.z * rf[p][2];
+                const float4* K4 = sk + ((size_t)lf * maxt + ls) * 9;
+                float er = 0, ei = 0, mr = 0, mi = 0, tr = 0, ti = 0;
+#pragma unroll
+                for (int p = 0; p < 3; ++p)
+#pragma unroll
+                    for (int q = 0; q < 3; ++q) {
+                        const float4 g = K4[3 * p + q];
+                        const float dx = P[p][0] - Q[q][0], dy = P[p][1] - Q[q][1], dz = P[p][2] - Q[q][2];
+                        const float nfd = nf.x * dx + nf.y * dy + nf.z * dz;
+                        const float nsd = ns.x * dx + ns.y * dy + ns.z * dz;
+                        const float rfrs = rf[p][0] * rs[q][0] + rf[p][1] * rs[q][1] + rf[p][2] * rs[q][2];
+                        const float rfd = rf[p][0] * dx + rf[p][1] * dy + rf[p][2] * dz;
+                        const float rsd = rs[q][0] * dx + rs[q][1] * dy + rs[q][2] * dz;
+                        const float e = 0.25f * rfrs - c.inv_k2;
+                        er += e * g.x;
+                        ei += e * g.y;
+                        const float m = rfd * nfrs[q] - rfrs * nfd;
+                        const float mt = rfrs * nsd - rsd * nsrf[p];
+                        mr += m * g.z;
+                        mi += m * g.w;
+                        tr += mt * g.z;
+                        ti += mt * g.w;
+                    }
+                zer += sgn * er;
+                zei += sgn * ei;
+                zmr += sgn * mr;
+                zmi += sgn * mi;
+                ztr += sgn * tr;
+                zti += sgn * ti;
+            }
+        }
+        const float l = F.len * S.len;
+        out = cx((-c.ce * zei + c.cm * zmr + (float)sr) * l, (c.ce * zer + c.cm * zmi + (float)si) * l);
+        out_t = cx((-c.ce * zei + c.cm * ztr + (float)sr_t) * l, (c.ce * zer + c.cm * zti + (float)si_t) * l);
+        Z[(size_t)f * ldz + s] = out;
+    }
+    if (!mirror) return;  // uniform over the CTA
+    zt[tx][ty] = out_t;  // Z[s][f]
+    __syncthreads();
+    const int sr_ = bs * FT + ty, fc_ = bf * FT + tx;
+    if (sr_ < n && fc_ < n) Z[(size_t)sr_ * ldz + fc_] = zt[ty][tx];
+}
+
+static size_t tile_smem_cfie_sym(int maxt)
+{
+    return sizeof(float4) * ((size_t)maxt * maxt * 9 + 8 * (size_t)maxt);
+}
+
 // per-geometry plan of the tiled fill (host, once)
 static emfa_status_t tile_plan(Ctx* c, Geom* g, cudaStream_t st)
 {
@@ -935,19 +1111,22 @@ static emfa_status_t fill_z_t(Ctx* c, Geom* g, GeomDev<T>& d, const emfa_fill_pa
         // FP32: the tiled kernel
         EMFA_TRY(tile_plan(c, g, st));
         const size_t sm = tile_smem(g->tile_maxt);
+        const size_t sm_c = tile_smem_cfie_sym(g->tile_maxt);
         EMFA_TRY(ensure_smem(c, k_fill_tile<true>, sm));
         EMFA_TRY(ensure_smem(c, k_fill_tile<false>, sm));
         EMFA_TRY(ensure_smem(c, k_fill_tile_sym, sm));
+        EMFA_TRY(ensure_smem(c, k_fill_tile_cfie_sym, sm_c));
         const dim3 grd((g->n + FT - 1) / FT, (g->n + FT - 1) / FT);
         const FillConst<float> fc32 = make_fill_const<float>(p);
         {
             TimedLaunch tl(c, KT_FILL_Z, st, (double)g->n * g->n);
-            if (cfie)
-                k_fill_tile<true><<<grd, 256, sm, st>>>(
+            if (cfie) {
+                const int nb = (g->n + FT - 1) / FT;
+                k_fill_tile_cfie_sym<<<(unsigned)((long long)nb * (nb + 1) / 2), 256, sm_c, st>>>(
                     dptr<RwgPack<float>>(g->g32.rwg), g->n, fc32, (const double2*)tab, dptr<float>(g->g32.tri_q3),
                     dptr<float>(g->g32.tri_n), dptr<int>(g->tile_tris), dptr<int>(g->tile_nt),
-                    dptr<unsigned char>(g->tile_loc), g->tile_maxt, reinterpret_cast<Cx<float>*>(Z), ldz);
-            else if (p->edm_mode != 1) {
+                    dptr<unsigned char>(g->tile_loc), g->tile_maxt, nb, reinterpret_cast<Cx<float>*>(Z), ldz);
+            } else if (p->edm_mode != 1) {
                 const int nb = (g->n + FT - 1) / FT;
                 k_fill_tile_sym<<<(unsigned)((long long)nb * (nb + 1) / 2), 256, sm, st>>>(
                     dptr<RwgPack<float>>(g->g32.rwg), g->n, fc32, (const double2*)tab, dptr<float>(g->g32.tri_q3),
