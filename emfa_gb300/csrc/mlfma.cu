@@ -7,7 +7,9 @@
 //   near / far lists                setBoxParameter (MLFMA.cpp:807-866)
 //   multipoles, Gauss-Legendre      getMultipoleNumber / levelRootsAndWeights (MLFMA.cpp:877-915)
 //   3x3 Lagrange stencils           calculateInterpolationMtr / lagrangeIPWeights (MLFMA.cpp:917-1002)
-// Device (FP32 patterns, 3 Cartesian components as in the reference):
+// Device (FP32 patterns; level patterns in 3 Cartesian components as in the
+// reference, the transverse radiation / receive patterns in 2, theta and phi
+// of each sample's own basis):
 //   k_trans_table  translation operators (parallelLevelTrans, MLFMA.cpp:1191-1222) in FP64, once
 //                  per distinct box offset (at most 7^3 per level) instead of per box pair
 //   k_radrec       radiation / receive patterns (MLFMA.cpp:1244-1292,1393-1422)
@@ -32,6 +34,10 @@ namespace emfa {
 
 struct C3f {
     float2 x, y, z;
+};
+// a transverse pattern in the (theta, phi) basis of its sample direction
+struct C2f {
+    float2 t, p;
 };
 
 __device__ __forceinline__ float2 cmulf(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
@@ -177,7 +183,8 @@ struct emfa_mlfma {
     std::vector<emfa::MLevel> lv;  // index level - 2
     int rcap = 1;                  // right-hand sides the level patterns hold (one apply chunk)
     emfa::DevBuf perm_d, box_of;   // int [n]
-    emfa::DevBuf rad, rec;         // C3f [n][Kf]
+    emfa::DevBuf rad, rec;         // C2f [n][Kf]: theta, phi components in each sample's basis
+    emfa::DevBuf tp;               // float [Kf][6]: theta_hat, phi_hat of the finest samples
     emfa::DevBuf coeff;            // float [Kf]
     emfa::DevBuf box_off, box_cnt; // finest boxes: first unknown, count
     emfa::DevBuf near_ptr, near_box, near_col, row_cols;  // CSR near lists, column base per slot, C_b per box
@@ -199,11 +206,15 @@ namespace emfa {
 // ---------------------------------------------------------------------------
 // device kernels
 // ---------------------------------------------------------------------------
-// radiation / receive patterns of every unknown (box order) at every finest sample
+// radiation / receive patterns of every unknown (box order) at every finest
+// sample.  Both are transverse (k . rad = 0: rad is projected off k; the
+// receive pattern is alpha conj(rad) plus k x (...)), so they are stored as
+// their theta and phi components in the sample's own basis (tp: theta_hat,
+// phi_hat per sample), 16 bytes a sample instead of the 24 of x, y, z.
 __global__ void k_radrec(const RwgPack<float>* __restrict__ rw, const int* __restrict__ perm,
                          const int* __restrict__ box_of, const float* __restrict__ centers,
-                         const float* __restrict__ kdir, int n, int K, float k, float alpha, C3f* __restrict__ rad,
-                         C3f* __restrict__ rec)
+                         const float* __restrict__ kdir, const float* __restrict__ tp, int n, int K, float k,
+                         float alpha, C2f* __restrict__ rad, C2f* __restrict__ rec)
 {
     size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (id >= (size_t)n * K) return;
@@ -243,16 +254,20 @@ __global__ void k_radrec(const RwgPack<float>* __restrict__ rw, const int* __res
     float2 hy = make_float2(kh.z * rh[0].x - kh.x * rh[2].x, kh.z * rh[0].y - kh.x * rh[2].y);
     float2 hz = make_float2(kh.x * rh[1].x - kh.y * rh[0].x, kh.x * rh[1].y - kh.y * rh[0].y);
     const float h = R.len / 2;
-    C3f o;
+    const float b = 1.0f - alpha;
+    const float* e = tp + 6 * kk;  // theta_hat, phi_hat
+    C3f o, q;
     o.x = cscalef(ra[0], h);
     o.y = cscalef(ra[1], h);
     o.z = cscalef(ra[2], h);
-    rad[id] = o;
-    const float b = 1.0f - alpha;
-    o.x = make_float2(h * (alpha * ra[0].x + b * hx.x), h * (-alpha * ra[0].y + b * hx.y));
-    o.y = make_float2(h * (alpha * ra[1].x + b * hy.x), h * (-alpha * ra[1].y + b * hy.y));
-    o.z = make_float2(h * (alpha * ra[2].x + b * hz.x), h * (-alpha * ra[2].y + b * hz.y));
-    rec[id] = o;
+    q.x = make_float2(h * (alpha * ra[0].x + b * hx.x), h * (-alpha * ra[0].y + b * hx.y));
+    q.y = make_float2(h * (alpha * ra[1].x + b * hy.x), h * (-alpha * ra[1].y + b * hy.y));
+    q.z = make_float2(h * (alpha * ra[2].x + b * hz.x), h * (-alpha * ra[2].y + b * hz.y));
+    auto proj = [](const C3f& v, const float* u) {
+        return make_float2(u[0] * v.x.x + u[1] * v.y.x + u[2] * v.z.x, u[0] * v.x.y + u[1] * v.y.y + u[2] * v.z.y);
+    };
+    rad[id] = C2f{proj(o, e), proj(o, e + 3)};
+    rec[id] = C2f{proj(q, e), proj(q, e + 3)};
 }
 
 // near-field blocks: thread per (field unknown, near-slot); values row-major
@@ -288,30 +303,36 @@ __global__ void k_near_fill(const RwgPack<float>* __restrict__ rw, const int* __
 // finest aggregation: CTA per finest box, threads over samples; each
 // radiation pattern is read once for up to RB right-hand sides (nr of them:
 // x[r][u] at r n + u, patterns of RHS r at out + r ostride)
+// (the box's theta and phi sums, then expanded to x, y, z once per sample)
 template <int RB>
-__global__ void k_agg_finest(const float2* __restrict__ x, int n, int nr, const C3f* __restrict__ rad,
-                             const int* __restrict__ box_off, const int* __restrict__ box_cnt, int K,
-                             float2* __restrict__ out, size_t ostride)
+__global__ void k_agg_finest(const float2* __restrict__ x, int n, int nr, const C2f* __restrict__ rad,
+                             const float* __restrict__ tp, const int* __restrict__ box_off,
+                             const int* __restrict__ box_cnt, int K, float2* __restrict__ out, size_t ostride)
 {
     const int b = blockIdx.x;
     const int o = box_off[b], cnt = box_cnt[b];
     for (int kk = threadIdx.x; kk < K; kk += blockDim.x) {
-        C3f acc[RB];
+        float2 at[RB], ap[RB];
 #pragma unroll
-        for (int r = 0; r < RB; ++r) acc[r] = c3zero();
+        for (int r = 0; r < RB; ++r) at[r] = ap[r] = make_float2(0, 0);
         for (int u = 0; u < cnt; ++u) {
-            const C3f rv = rad[(size_t)(o + u) * K + kk];
+            const C2f rv = rad[(size_t)(o + u) * K + kk];
 #pragma unroll
             for (int r = 0; r < RB; ++r)
-                if (RB == 1 || r < nr) c3fma(acc[r], x[(size_t)r * n + o + u], rv);
+                if (RB == 1 || r < nr) {
+                    const float2 xv = x[(size_t)r * n + o + u];
+                    at[r] = caddf(at[r], cmulf(xv, rv.t));
+                    ap[r] = caddf(ap[r], cmulf(xv, rv.p));
+                }
         }
+        const float* e = tp + 6 * kk;
 #pragma unroll
         for (int r = 0; r < RB; ++r)
             if (RB == 1 || r < nr) {
                 float2* ob = out + r * ostride + (size_t)3 * b * K + kk;
-                ob[0] = acc[r].x;
-                ob[K] = acc[r].y;
-                ob[2 * K] = acc[r].z;
+                ob[0] = caddf(cscalef(at[r], e[0]), cscalef(ap[r], e[3]));
+                ob[K] = caddf(cscalef(at[r], e[1]), cscalef(ap[r], e[4]));
+                ob[2 * K] = caddf(cscalef(at[r], e[2]), cscalef(ap[r], e[5]));
             }
     }
 }
@@ -504,8 +525,9 @@ __global__ void k_downward(const float4* __restrict__ up, const int* __restrict_
 // is contiguous in val (row_cols[b] values); its column unknowns are listed
 // once per box in near_cidx.
 template <int RB>
-__global__ void k_disagg_near(const float2* __restrict__ x, int nr, const C3f* __restrict__ rec,
-                              const float2* __restrict__ down, size_t dstride, const float* __restrict__ coeff, int K,
+__global__ void k_disagg_near(const float2* __restrict__ x, int nr, const C2f* __restrict__ rec,
+                              const float* __restrict__ tp, const float2* __restrict__ down, size_t dstride,
+                              const float* __restrict__ coeff, int K,
                               const int* __restrict__ box_of, const int* __restrict__ box_off,
                               const int* __restrict__ row_cols, const size_t* __restrict__ row_base,
                               const int* __restrict__ near_cbase, const int* __restrict__ near_cidx,
@@ -517,17 +539,22 @@ __global__ void k_disagg_near(const float2* __restrict__ x, int nr, const C3f* _
     float2 acc[RB];
 #pragma unroll
     for (int r = 0; r < RB; ++r) acc[r] = make_float2(0, 0);
-    const C3f* rr = rec + (size_t)u * K;
+    const C2f* rr = rec + (size_t)u * K;
     const float2* dd = down + (size_t)3 * b * K;
 #pragma unroll 4
     for (int kk = lane; kk < K; kk += 32) {
-        const C3f rv = rr[kk];
+        const C2f rv = rr[kk];
         const float cf = coeff[kk];
+        const float* e = tp + 6 * kk;
 #pragma unroll
         for (int r = 0; r < RB; ++r)
             if (RB == 1 || r < nr) {
                 const float2* d = dd + r * dstride;
-                const float2 t = caddf(caddf(cmulf(rv.x, d[kk]), cmulf(rv.y, d[K + kk])), cmulf(rv.z, d[2 * K + kk]));
+                const float2 dx = d[kk], dy = d[K + kk], dz = d[2 * K + kk];
+                // theta and phi components of the down pattern at this sample
+                const float2 dt = caddf(caddf(cscalef(dx, e[0]), cscalef(dy, e[1])), cscalef(dz, e[2]));
+                const float2 dp = caddf(caddf(cscalef(dx, e[3]), cscalef(dy, e[4])), cscalef(dz, e[5]));
+                const float2 t = caddf(cmulf(rv.t, dt), cmulf(rv.p, dp));
                 acc[r] = caddf(acc[r], cscalef(t, cf));
             }
     }
@@ -1331,14 +1358,31 @@ static emfa_status_t mlfma_build(emfa_mlfma* M, cudaStream_t st)
     EMFA_TRY(upload(c, cen_d, cen_h, st));
     EMFA_TRY(upload(c, kdir_d, kd[nl - 1], st));
     EMFA_TRY(geom_prepare_f32(g, st));
-    EMFA_TRY(M->rad.alloc(c, sizeof(C3f) * (size_t)n * Kf));
-    EMFA_TRY(M->rec.alloc(c, sizeof(C3f) * (size_t)n * Kf));
+    // theta_hat, phi_hat of every finest sample direction (FP64 from the
+    // sample's float direction, stored in float): phi_hat = z x k / |z x k|,
+    // theta_hat = phi_hat x k (the Gauss-Legendre theta nodes avoid the poles)
+    {
+        std::vector<float> tp((size_t)6 * Kf);
+        const auto& kv = kd[nl - 1];
+        for (int kk = 0; kk < Kf; ++kk) {
+            const double kx = kv[3 * kk], ky = kv[3 * kk + 1], kz = kv[3 * kk + 2];
+            const double rho = std::sqrt(kx * kx + ky * ky);
+            const double px = -ky / rho, py = kx / rho;
+            const double tx = py * kz, ty = -px * kz, tz = px * ky - py * kx;
+            const double tv[6] = {tx, ty, tz, px, py, 0.0};
+            for (int j = 0; j < 6; ++j) tp[6 * (size_t)kk + j] = (float)tv[j];
+        }
+        EMFA_TRY(upload(c, M->tp, tp, st));
+    }
+    EMFA_TRY(M->rad.alloc(c, sizeof(C2f) * (size_t)n * Kf));
+    EMFA_TRY(M->rec.alloc(c, sizeof(C2f) * (size_t)n * Kf));
     {
         size_t tot = (size_t)n * Kf;
         k_radrec<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(dptr<RwgPack<float>>(g->g32.rwg), dptr<int>(M->perm_d),
                                                                dptr<int>(M->box_of), dptr<float>(cen_d),
-                                                               dptr<float>(kdir_d), n, Kf, k, (float)M->p.alpha,
-                                                               dptr<C3f>(M->rad), dptr<C3f>(M->rec));
+                                                               dptr<float>(kdir_d), dptr<float>(M->tp), n, Kf, k,
+                                                               (float)M->p.alpha, dptr<C2f>(M->rad),
+                                                               dptr<C2f>(M->rec));
         c->kernel_launches += 1;
     }
     // near field: CSR of near boxes, column bases, row bases
@@ -1423,11 +1467,13 @@ static void launch_agg_disagg(emfa_mlfma* M, bool agg, const float2* x, int nr, 
     const int Kf = fl.K, n = M->n;
     const size_t lstride = (size_t)3 * fl.nbox * Kf;
     if (agg)
-        k_agg_finest<RB><<<fl.nbox, 128, 0, st>>>(x, n, nr, dptr<C3f>(M->rad), dptr<int>(M->box_off),
-                                                  dptr<int>(M->box_cnt), Kf, dptr<float2>(fl.up), lstride);
+        k_agg_finest<RB><<<fl.nbox, 128, 0, st>>>(x, n, nr, dptr<C2f>(M->rad), dptr<float>(M->tp),
+                                                  dptr<int>(M->box_off), dptr<int>(M->box_cnt), Kf,
+                                                  dptr<float2>(fl.up), lstride);
     else
         k_disagg_near<RB><<<(unsigned)(((size_t)n * 32 + 255) / 256), 256, 0, st>>>(
-            x, nr, dptr<C3f>(M->rec), dptr<float2>(fl.down), lstride, dptr<float>(M->coeff), parts == 1 ? 0 : Kf,
+            x, nr, dptr<C2f>(M->rec), dptr<float>(M->tp), dptr<float2>(fl.down), lstride, dptr<float>(M->coeff),
+            parts == 1 ? 0 : Kf,
             dptr<int>(M->box_of), dptr<int>(M->box_off), dptr<int>(M->row_cols), dptr<size_t>(M->row_base),
             dptr<int>(M->near_cbase), dptr<int>(M->near_cidx), dptr<float2>(M->near_val), n, parts == 2 ? 1 : 0, y);
 }

@@ -43,7 +43,8 @@ def fill_bytes(n: int, fp64: bool = False) -> float:
     return float(n) * n * (16 if fp64 else 8)
 
 
-def mlfma_matvec_bytes(n: int, nnz: int, level_boxes, poles, comps: int = 3, near_index_bytes: int = 0) -> float:
+def mlfma_matvec_bytes(n: int, nnz: int, level_boxes, poles, comps: int = 3, near_index_bytes: int = 0,
+                       radrec_comps: int | None = None) -> float:
     """Compulsory bytes of one MLFMA product.
 
     - Near-field values, nnz x (8 + index bytes).
@@ -56,14 +57,18 @@ def mlfma_matvec_bytes(n: int, nnz: int, level_boxes, poles, comps: int = 3, nea
 
     level_boxes[l] counts the boxes of level l (0 = root); poles lists L for
     levels 2..finest, and a level samples K = 2 L^2 directions.
-    comps = 3 is the Cartesian patterns stored here (the reference's layout).  comps = 2
+    comps = 3 is Cartesian level patterns (the reference's layout); comps = 2
     with near_index_bytes = 4 is the 2-component theta/phi byte model.
+    radrec_comps (default: comps) counts the radiation / receive patterns
+    apart: this build stores them as 2 components (theta, phi) and the level
+    patterns as 3.
     """
+    rr = comps if radrec_comps is None else radrec_comps
     ks = [2 * p * p for p in poles]
     boxes = list(level_boxes)[2:]
     kf = ks[-1]
     near = nnz * (8.0 + near_index_bytes)
-    radrec = 2.0 * n * kf * comps * 8
+    radrec = 2.0 * n * kf * rr * 8
     levels = sum(b * k * comps * 8.0 for b, k in zip(boxes, ks)) * 4
     trans = sum(343.0 * k * 8 for k in ks)
     return near + radrec + levels + trans + 2.0 * n * 8
