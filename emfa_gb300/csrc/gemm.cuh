@@ -70,6 +70,13 @@ struct LinOp {
                                    cudaStream_t st) = 0;
     // error word of asynchronous device-side checks (synchronises)
     virtual emfa_status_t check(Ctx*, cudaStream_t) { return EMFA_OK; }
+    // fraction of a restart's residual target at which GMRES's inner steps
+    // stop: below 1 where apply() is less accurate than residual(), so the
+    // implicit residual must undershoot for the true one to meet the target
+    virtual double inner_margin() const { return 1.0; }
+    // default per-cycle reduction of GMRES-IR's inner solve (0: none, iterate
+    // to the target)
+    virtual double inner_reduction() const { return 0.0; }
     // Vout = scale[r] W (the Krylov normalisation, iteration precision), then
     // Y = A Vout; Y may alias W.  Operators that pack their input fuse both.
     // wmax (optional): per RHS max |Re|, |Im| of W, known from the pass that produced it

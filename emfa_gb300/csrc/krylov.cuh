@@ -7,6 +7,8 @@ namespace emfa {
 struct GmresDev {
     int m, nrhs, tol_abs;
     double tol;
+    double inner;    // the Arnoldi steps stop at inner x the restart's threshold,
+    double red;      //   or at red x the cycle's starting residual if that is larger
     double2* H;      // nrhs x (m+1) x m, row-major per RHS
     double* cs;      // nrhs x m  Givens cosines
     double2* sn;     // nrhs x m  Givens sines

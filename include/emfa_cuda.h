@@ -100,6 +100,12 @@ typedef struct {
     int orth;           /* GMRES Gram-Schmidt: 0 = auto (CGS1 for the EMFA_F32     */
                         /* inner solve of the refinement, CGS2 for EMFA_F64),      */
                         /* 1 = CGS1, 2 = CGS2                                      */
+    double inner_reduction; /* GMRES refinement with reduced-precision products:  */
+                        /* a cycle's inner steps stop once the implicit residual   */
+                        /* falls below this fraction of the cycle's starting true  */
+                        /* residual, or below the target; 0 = the operator's       */
+                        /* default (1e-2 for the tensor-core dense products),      */
+                        /* < 0 = iterate to the target                             */
 } emfa_solver_params_t;
 
 typedef struct {
