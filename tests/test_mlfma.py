@@ -233,25 +233,28 @@ def test_plan_with_the_configuration_truncation(emfa_lib):
 
 
 @pytest.mark.gpu
-def test_solve_with_the_configuration_truncation(ops):
-    """The operator with the configuration's multipole truncation: GMRES to
-    1e-4 gives a bistatic RCS within 0.1 dB of the reference-truncation
-    operator's over the pattern's top 20 dB."""
+@pytest.mark.parametrize("name", CASES)
+def test_operator_with_the_configuration_truncation(ops, name):
+    """The operator with the configuration's multipole truncation against
+    the dense CFIE product of the same mesh: on these small meshes (finest
+    boxes of 0.16-0.2 wavelength) the reference's own MLFMA formulation is
+    already 4-9 % off the dense product (its Gauss-Legendre phi samples and
+    clamped stencils); the configuration's rule, with fewer multipoles,
+    adds at most a quarter to that error."""
     import torch
     from emfa_gb300 import api
-    g, geo, ml = ops["sphere3_mlfma"]
+    g, geo, ml = ops[name]
     m = g["meta"]
-    mlc = api.Mlfma(geo, api.mlfma_params(float(m["frequency"]), float(np.float32(float(m["alpha"]))),
-                                          float(np.float32(float(m["mlfma_box_threshold"]))), truncation="config"))
-    sp = api.solver_params("gmres", restart=30, tol=1e-4, max_iter=300)
-    fp = api.fill_params("cfie", "f32", float(m["frequency"]), 0.5)
-    dirs = g["rcs_dirs"].astype(np.float64)
-    out = []
+    f, a = float(m["frequency"]), float(np.float32(float(m["alpha"])))
+    mlc = api.Mlfma(geo, api.mlfma_params(f, a, float(np.float32(float(m["mlfma_box_threshold"]))),
+                                          truncation="config"))
+    assert np.all(mlc.poles < ml.poles)
+    Z = api.fill_z(geo, api.fill_params("cfie", "f64", f, a))
+    x = torch.tensor(g["mv_x"], device="cuda")[None]
+    errs = []
     for op in (ml, mlc):
-        X, info = op.solve(op.fill_v(angles(g)), sp)
-        assert info.converged == 1
-        out.append(api.rcs(geo, fp, op.unpermute(X), dirs)[0])
+        y = op.unpermute(op.apply(x).to(torch.complex128))[0]
+        yd = Z @ op.unpermute(x.to(torch.complex128))[0]
+        errs.append(float(torch.linalg.norm(y - yd) / torch.linalg.norm(yd)))
     mlc.close()
-    keep = out[0] > out[0].max() - 20.0
-    assert np.abs(out[0] - out[1])[keep].max() < 0.1, np.abs(out[0] - out[1])[keep].max()
-    del torch
+    assert errs[1] <= 1.25 * errs[0], errs
