@@ -698,7 +698,7 @@ def main():
     ap.add_argument("--workload", default="c2_cfie_sphere_7680x360", choices=list(WORKLOADS))
     ap.add_argument("--matvec", default="auto", choices=["auto", "f32", "tf32", "f16x"])
     ap.add_argument("--check", type=int, default=1)
-    ap.add_argument("--orth", default="auto", choices=["auto", "cgs1", "cgs2"])
+    ap.add_argument("--orth", default="auto", choices=["auto", "cgs1", "cgs2", "cgs1_split", "cgs1_fused"])
     ap.add_argument("--inner-reduction", type=float, default=0.0,
                     help="GMRES refinement: per-cycle inner reduction (0 = the solver's default, <0 = none)")
     ap.add_argument("--cpu-baseline", type=int, default=1)

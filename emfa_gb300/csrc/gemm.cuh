@@ -50,6 +50,26 @@ emfa_status_t hgemm_apply(Ctx* c, const HPlanes& h, const void* X, void* Y, int 
 // the same pass, then Y = Z Vout; Y may alias W (W is consumed first)
 emfa_status_t hgemm_normalize_apply(Ctx* c, const HPlanes& h, const void* W, const double* scale,
                                     const double* wmax, void* Vout, void* Y, int nrhs, cudaStream_t st);
+// The FP16 rows the inner product reads as its B operand: right-hand side r
+// is rows 2r = (Re, -Im) and 2r+1 = (Im, Re) of bh, ldh halves apart, scaled
+// by t_r = 1 / inv_t[r].  A producer that packs them itself (the fused
+// Arnoldi step) then runs the product from them.
+struct HPack {
+    __half* bh = nullptr;
+    float* inv_t = nullptr;
+    size_t ldh = 0;
+};
+emfa_status_t hgemm_pack_target(Ctx* c, const HPlanes& h, int nrhs, HPack* out);
+emfa_status_t hgemm_apply_packed(Ctx* c, const HPlanes& h, const HPack& p, void* Y, int nrhs, cudaStream_t st);
+// exponent e of the FP16 scale t = 2^(14 - e) of v = scale w, from wmax =
+// max |Re|, |Im| of w: max |t v| < 2^14 (the FP32 rounding of scale can raise
+// max |v| by an ulp, hence the factor)
+__device__ __forceinline__ int hpack_exponent(double wmax, double scale)
+{
+    int e = 0;
+    frexpf((float)(wmax * scale) * 1.0000002f, &e);
+    return e;
+}
 // R (complex128) = B - Z X for X complex128 and B complex64 (f32b) or complex128:
 // Zh Xh + Zh Xl + Zl Xh on the tensor cores, FP32 chunk sums reduced in FP64
 emfa_status_t hgemm_residual(Ctx* c, const HPlanes& h, const double2* X, const void* B, bool b_is_f32, double2* R,
@@ -82,6 +102,11 @@ struct LinOp {
     // wmax (optional): per RHS max |Re|, |Im| of W, known from the pass that produced it
     virtual emfa_status_t normalize_apply(Ctx* c, const void* W, const double* scale, const double* wmax, void* Vout,
                                           void* Y, int nrhs, cudaStream_t st);
+    // Operators whose apply() packs its input to FP16 rows: where the rows
+    // go (false: the operator does not pack), and Y = A V from rows a
+    // producer has written there
+    virtual bool pack_target(Ctx*, int, HPack*) { return false; }
+    virtual emfa_status_t apply_packed(Ctx*, const HPack&, void*, int, cudaStream_t) { return EMFA_ERR_UNSUPPORTED; }
 };
 
 emfa_status_t solve_op(Ctx* c, LinOp& A, const void* B, int nrhs, void* X, const emfa_solver_params_t* sp,

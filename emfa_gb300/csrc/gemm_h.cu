@@ -273,8 +273,7 @@ __global__ void __launch_bounds__(256) k_hpack_scale(const float2* __restrict__ 
 {
     const int r = blockIdx.y;
     const float sc = (float)scale[r];
-    int e = 0;
-    frexpf((float)(wmax[r] * scale[r]) * 1.0000002f, &e);  // rounding of sc can only raise max |v| by an ulp
+    const int e = hpack_exponent(wmax[r], scale[r]);
     const float t = ldexpf(1.f, 14 - e);
     if (blockIdx.x == 0 && threadIdx.x == 0) inv_t[r] = ldexpf(1.f, e - 14);
     const float2* w = W + (size_t)r * n;
@@ -678,6 +677,20 @@ emfa_status_t hgemm_normalize_apply(Ctx* c, const HPlanes& h, const void* W, con
                                                                        (float2*)Vout, bh, inv_t);
     c->kernel_launches += 1;
     return hgemm_run(c, h, bh, inv_t, Y, nrhs, err, st);
+}
+
+emfa_status_t hgemm_pack_target(Ctx* c, const HPlanes& h, int nrhs, HPack* out)
+{
+    EMFA_TRY(hgemm_bplane(c, h, nrhs, &out->bh, &out->inv_t));
+    out->ldh = h.ldh;
+    return EMFA_OK;
+}
+
+emfa_status_t hgemm_apply_packed(Ctx* c, const HPlanes& h, const HPack& p, void* Y, int nrhs, cudaStream_t st)
+{
+    int* err = nullptr;
+    EMFA_TRY(herr(c, &err));
+    return hgemm_run(c, h, p.bh, p.inv_t, Y, nrhs, err, st);
 }
 
 emfa_status_t hgemm_residual(Ctx* c, const HPlanes& h, const double2* X, const void* B, bool b_is_f32, double2* R,

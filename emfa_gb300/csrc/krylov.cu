@@ -21,6 +21,7 @@
 #include "lu.cuh"
 
 #include <algorithm>
+#include <type_traits>
 #include <cmath>
 
 namespace emfa {
@@ -560,38 +561,15 @@ __device__ __forceinline__ double2 shfl_d2(double2 v, int src)
     return make_double2(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
 }
 
-__global__ void k_arnoldi_finish_warp(GmresDev s, int j, const double2* __restrict__ pnorm, int nblk, int two_pass)
+// Arnoldi column j of right-hand side r (one warp): lane i <= j holds the
+// Gram-Schmidt coefficient h_i, beta = ||w||.  Applies the previous
+// rotations, forms the new one, updates g and tests convergence.
+__device__ void arnoldi_column(const GmresDev& s, int r, int j, double2 h, double beta)
 {
-    const int r = (int)(((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
-    if (r >= s.nrhs) return;  // whole warps
-    const int m = s.m;
-    if (!s.active[r]) {
-        if (lane == 0) s.scale[r] = 0.0;
-        return;
-    }
-    double beta = 0.0;
-    if (lane == 0) {
-        double nr2 = 0.0, wm = 0.0;
-        for (int b = 0; b < nblk; ++b) {
-            nr2 += pnorm[(size_t)r * nblk + b].x;
-            wm = fmax(wm, pnorm[(size_t)r * nblk + b].y);
-        }
-        s.wmax[r] = wm;
-        beta = sqrt(nr2);
-    }
-    beta = __shfl_sync(0xffffffffu, beta, 0);
+    const int lane = threadIdx.x & 31, m = s.m;
     double2* H = s.H + (size_t)r * (m + 1) * m;
     double* cs = s.cs + (size_t)r * m;
     double2* sn = s.sn + (size_t)r * m;
-    double2 h = make_double2(0.0, 0.0);
-    if (lane <= j) {
-        h = s.hcol[(size_t)lane * s.nrhs + r];
-        if (two_pass) {
-            const double2 b = s.y[(size_t)lane * s.nrhs + r];
-            h.x += b.x;
-            h.y += b.y;
-        }
-    }
     const double cl = lane < j ? cs[lane] : 0.0;
     const double2 sl = lane < j ? sn[lane] : make_double2(0.0, 0.0);
     // previous rotations: [x; y] <- [c x + s y; -conj(s) x + c y] on entries (i, i + 1)
@@ -643,6 +621,266 @@ __global__ void k_arnoldi_finish_warp(GmresDev s, int j, const double2* __restri
         }
     }
     if (lane <= j) H[lane * m + j] = h;
+}
+
+__global__ void k_arnoldi_finish_warp(GmresDev s, int j, const double2* __restrict__ pnorm, int nblk, int two_pass)
+{
+    const int r = (int)(((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (r >= s.nrhs) return;  // whole warps
+    if (!s.active[r]) {
+        if (lane == 0) s.scale[r] = 0.0;
+        return;
+    }
+    double beta = 0.0;
+    if (lane == 0) {
+        double nr2 = 0.0, wm = 0.0;
+        for (int b = 0; b < nblk; ++b) {
+            nr2 += pnorm[(size_t)r * nblk + b].x;
+            wm = fmax(wm, pnorm[(size_t)r * nblk + b].y);
+        }
+        s.wmax[r] = wm;
+        beta = sqrt(nr2);
+    }
+    beta = __shfl_sync(0xffffffffu, beta, 0);
+    double2 h = make_double2(0.0, 0.0);
+    if (lane <= j) {
+        h = s.hcol[(size_t)lane * s.nrhs + r];
+        if (two_pass) {
+            const double2 b = s.y[(size_t)lane * s.nrhs + r];
+            h.x += b.x;
+            h.y += b.y;
+        }
+    }
+    arnoldi_column(s, r, j, h, beta);
+}
+
+// ---------------------------------------------------------------------------
+// One Arnoldi step in one launch (FP32 basis, CGS1): a cluster of CS <= 8
+// CTAs per right-hand side, CTA `rank` owning elements [rank slice,
+// (rank + 1) slice) of the N, E per thread, held in registers throughout.
+//   1. w and the basis slices are staged in shared memory by asynchronous
+//      copies (up to 104 KB a CTA, all in flight at once); partial
+//      coefficients h_i = V_i^H w over the slice, a warp per vector (FP32
+//      within the warp), published in shared memory in FP64
+//   2. cluster barrier; every CTA sums the cluster's partials in rank order
+//      from distributed shared memory (the same FP64 sums in every CTA)
+//   3. w -= sum_i h_i V_i over the slice, from the staged slices (a restart
+//      longer than the staging holds reads its earlier vectors again from
+//      L2: the cluster read them microseconds before).  |w|^2 and
+//      max |Re|, |Im| partials
+//   4. cluster barrier; beta = ||w||; v = w / beta goes to V_{j+1} and, for
+//      operators that pack their input, to the FP16 rows of the next product
+//      (the packing k_hpack_scale does: same scale, same rounding)
+//   5. the first CTA's warp 0 finishes the Arnoldi column (arnoldi_column)
+// W is read once and never written: the next product reads the packed rows
+// (or V_{j+1}).  A right-hand side that is no longer active writes nothing
+// (its V_{j+1} is past its basis length; its rows in the product's operand
+// still hold its last, finite vector).  Replaces k_vdots, k_vupdate,
+// k_arnoldi_finish_warp and the normalisation pass: one launch instead of
+// four, the basis read once from HBM, W once.  Each CTA's work is a chain
+// (staging, two cluster barriers, FP64 sums on one thread, the Givens
+// column on the first CTA), so the step is faster where launches and
+// latency dominate (tens of right-hand sides) and the separate passes are
+// faster for hundreds; the solver picks by the grid size.
+// ---------------------------------------------------------------------------
+constexpr int AS_THREADS = 512;
+constexpr int AS_WARPS = AS_THREADS / 32;
+constexpr int AS_MAXV = 32;     // restart lengths up to 32 (one coefficient per lane in arnoldi_column)
+constexpr int AS_MAX_CLUSTER = 8;
+constexpr int AS_STAGE_BYTES = 104 * 1024;  // staged slices a CTA: two CTAs an SM
+
+__device__ __forceinline__ void cluster_arrive() { asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory"); }
+__device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory"); }
+// a double2 in the shared memory of CTA `rank` of the cluster, at the
+// address `local` has in this CTA
+__device__ __forceinline__ double2 ld_cluster_d2(const double2* local, int rank)
+{
+    const uint32_t a = (uint32_t)__cvta_generic_to_shared(local);
+    uint32_t ra;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(a), "r"(rank));
+    double x, y;
+    asm volatile("ld.shared::cluster.v2.f64 {%0, %1}, [%2];" : "=d"(x), "=d"(y) : "r"(ra) : "memory");
+    return make_double2(x, y);
+}
+
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"((uint32_t)__cvta_generic_to_shared(smem)), "l"(gmem)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all()
+{
+    asm volatile("cp.async.commit_group;" ::: "memory");
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+}
+
+template <int E>
+__global__ void __launch_bounds__(AS_THREADS, 2)
+    k_arnoldi_step(GmresDev s, int j, const float2* __restrict__ V, size_t vstride, const float2* __restrict__ W,
+                   int n, int slice, int sv, float2* __restrict__ Vout, HPack pk)
+{
+    constexpr int SW = AS_THREADS * E;  // elements of a staged slice (>= slice)
+    extern __shared__ float2 stage[];   // w, then sv basis slices
+    float2* sW = stage;
+    float2* sV = stage + SW;
+    __shared__ double2 hpart[AS_MAXV];  // this CTA's partial coefficients (read by the cluster)
+    __shared__ double2 hs[AS_MAXV];     // the cluster's sums
+    __shared__ float2 hf[AS_MAXV];
+    __shared__ double2 nred[AS_WARPS];
+    __shared__ double2 npart;           // this CTA's |w|^2 and max (read by the cluster)
+    __shared__ double2 ntot;            // beta and max |Re|, |Im| of w
+    __shared__ float nscale[2];         // 1 / beta and the FP16 scale t
+
+    const int r = blockIdx.y, rank = blockIdx.x, csize = gridDim.x;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    if (!s.active[r]) {  // the same branch in every CTA of the cluster: no barrier is left waiting
+        if (rank == 0 && tid == 0) s.scale[r] = 0.0;
+        return;
+    }
+    const int nv = j + 1;
+    const int k0 = rank * slice, len = min(n, k0 + slice) - k0;  // len >= 1 for every rank
+    const float2* Vs = V + (size_t)r * n + k0;                    // this slice of basis vector 0
+    const float2* Ws = W + (size_t)r * n + k0;
+
+    // 1. partial coefficients.  Each round stages (asynchronous copies, all
+    // in flight at once) up to sv basis slices, and w in the first; warp q
+    // then reduces the round's vectors q, q + 16 from shared memory.
+    int vlast = 0;  // first basis vector of the last round (still staged)
+    for (int v0 = 0; v0 < nv; v0 += sv) {
+        const int v1 = min(nv, v0 + sv);
+        vlast = v0;
+        if (v0 > 0) __syncthreads();  // the previous round's reads are done
+        if (v0 == 0)
+            for (int k = tid; k < len; k += AS_THREADS) cp_async8(sW + k, Ws + k);
+        for (int i = v0; i < v1; ++i)
+            for (int k = tid; k < len; k += AS_THREADS) cp_async8(sV + (size_t)(i - v0) * SW + k, Vs + (size_t)i * vstride + k);
+        cp_async_wait_all();
+        __syncthreads();
+        for (int i = v0 + warp; i < v1; i += AS_WARPS) {
+            const float2* vi = sV + (size_t)(i - v0) * SW;
+            float ar = 0.f, ai = 0.f;
+#pragma unroll 4
+            for (int k = lane; k < len; k += 32) {
+                const float2 a = vi[k], x = sW[k];
+                ar += a.x * x.x + a.y * x.y;
+                ai += a.x * x.y - a.y * x.x;
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                ar += __shfl_xor_sync(0xffffffffu, ar, o);
+                ai += __shfl_xor_sync(0xffffffffu, ai, o);
+            }
+            if (lane == 0) hpart[i] = make_double2((double)ar, (double)ai);
+        }
+    }
+    // 2. the cluster's sums (the barrier also orders this CTA's own writes)
+    cluster_arrive();
+    cluster_wait();
+    if (tid < AS_MAXV) {
+        double2 t = make_double2(0.0, 0.0);
+        if (tid < nv)
+            for (int c = 0; c < csize; ++c) {
+                const double2 p = ld_cluster_d2(&hpart[tid], c);
+                t.x += p.x;
+                t.y += p.y;
+            }
+        hs[tid] = t;
+        hf[tid] = make_float2((float)t.x, (float)t.y);
+    }
+    __syncthreads();
+
+    // 3. w -= V h: the last round's slices from shared memory, earlier rounds'
+    // (restarts longer than sv) again from global memory, where they were
+    // read microseconds earlier
+    float2 w[E];
+    float nr = 0.f, mx = 0.f;
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+        const int k = tid + e * AS_THREADS;
+        w[e] = make_float2(0.f, 0.f);
+        if (k >= len) continue;
+        float sr = 0.f, si = 0.f;
+#pragma unroll 4
+        for (int i = 0; i < vlast; ++i) {
+            const float2 v = Vs[(size_t)i * vstride + k];
+            const float2 h = hf[i];
+            sr += h.x * v.x - h.y * v.y;
+            si += h.x * v.y + h.y * v.x;
+        }
+#pragma unroll 4
+        for (int i = vlast; i < nv; ++i) {
+            const float2 v = sV[(size_t)(i - vlast) * SW + k];
+            const float2 h = hf[i];
+            sr += h.x * v.x - h.y * v.y;
+            si += h.x * v.y + h.y * v.x;
+        }
+        const float2 x = sW[k];
+        w[e] = make_float2(x.x - sr, x.y - si);
+        nr += w[e].x * w[e].x + w[e].y * w[e].y;
+        mx = fmaxf(mx, fmaxf(fabsf(w[e].x), fabsf(w[e].y)));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        nr += __shfl_xor_sync(0xffffffffu, nr, o);
+        mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    }
+    if (lane == 0) nred[warp] = make_double2((double)nr, (double)mx);
+    __syncthreads();
+    if (tid == 0) {
+        double t = 0.0, tm = 0.0;
+        for (int q = 0; q < AS_WARPS; ++q) {
+            t += nred[q].x;
+            tm = fmax(tm, nred[q].y);
+        }
+        npart = make_double2(t, tm);
+    }
+    // 4. beta and the normalised vector
+    cluster_arrive();
+    cluster_wait();
+    if (tid == 0) {
+        // one thread: FP64 square roots and divisions per thread would queue
+        // on the 1/64-rate FP64 pipe
+        double nr2 = 0.0, wm = 0.0;
+        for (int c = 0; c < csize; ++c) {
+            const double2 p = ld_cluster_d2(&npart, c);
+            nr2 += p.x;
+            wm = fmax(wm, p.y);
+        }
+        const double beta = sqrt(nr2);
+        const double scale = beta > 0.0 ? 1.0 / beta : 0.0;
+        ntot = make_double2(beta, wm);
+        nscale[0] = (float)scale;
+        nscale[1] = 1.f;
+        if (pk.bh) {
+            const int ex = hpack_exponent(wm, scale);
+            nscale[1] = ldexpf(1.f, 14 - ex);
+            if (rank == 0) pk.inv_t[r] = ldexpf(1.f, ex - 14);
+        }
+    }
+    __syncthreads();
+    cluster_arrive();  // this CTA's reads of the others' shared memory are done
+    const float sc = nscale[0], t = nscale[1];
+    __half2* h0 = pk.bh ? reinterpret_cast<__half2*>(pk.bh + (size_t)(2 * r) * pk.ldh) + k0 : nullptr;
+    __half2* h1 = pk.bh ? reinterpret_cast<__half2*>(pk.bh + (size_t)(2 * r + 1) * pk.ldh) + k0 : nullptr;
+    float2* vo = Vout + (size_t)r * n + k0;
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+        const int k = tid + e * AS_THREADS;
+        if (k >= len) continue;
+        const float2 y = make_float2(w[e].x * sc, w[e].y * sc);
+        vo[k] = y;
+        if (h0) {
+            const __half hre = __float2half_rn(t * y.x), him = __float2half_rn(t * y.y);
+            h0[k] = __halves2half2(hre, __hneg(him));
+            h1[k] = __halves2half2(him, hre);
+        }
+    }
+    // 5. the Arnoldi column
+    if (rank == 0 && warp == 0) {
+        if (lane == 0) s.wmax[r] = ntot.y;
+        arnoldi_column(s, r, j, lane <= j ? hs[lane] : make_double2(0.0, 0.0), ntot.x);
+    }
+    cluster_wait();  // no CTA leaves while another may still read its shared memory
 }
 
 template <typename TO, typename TI>
@@ -789,6 +1027,55 @@ static emfa_status_t dots(Ctx* c, const Cx<T>* V, size_t vstride, int nv, const 
 
 static int grid1(size_t tot) { return (int)std::min<size_t>((tot + 255) / 256, 8192); }
 
+// cluster shape of the fused Arnoldi step for N unknowns: CTAs per
+// right-hand side, elements per CTA and per thread (0: N too large)
+struct StepShape {
+    int cs = 0, slice = 0, e = 0;
+};
+static StepShape step_shape(int n)
+{
+    StepShape sh;
+    sh.cs = std::min(AS_MAX_CLUSTER, std::max(1, (n + 1023) / 1024));
+    sh.slice = (n + sh.cs - 1) / sh.cs;
+    const int e = (sh.slice + AS_THREADS - 1) / AS_THREADS;
+    sh.e = e <= 1 ? 1 : e <= 2 ? 2 : e <= 4 ? 4 : 0;
+    return sh;
+}
+
+template <int E>
+static emfa_status_t launch_step_e(Ctx* c, const StepShape& sh, int nrhs, cudaStream_t st, const GmresDev& s, int j,
+                                   const float2* V, size_t vstride, const float2* W, int n, float2* Vout,
+                                   const HPack& pk)
+{
+    const int sw = AS_THREADS * E;  // staged slice
+    const int sv = std::min(AS_MAXV, AS_STAGE_BYTES / (int)(sizeof(float2) * sw) - 1);
+    const size_t smem = sizeof(float2) * (size_t)sw * (sv + 1);
+    EMFA_TRY(ensure_smem(c, k_arnoldi_step<E>, smem));
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(sh.cs, nrhs);
+    cfg.blockDim = dim3(AS_THREADS);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = sh.cs;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    EMFA_CUDA(c, cudaLaunchKernelEx(&cfg, k_arnoldi_step<E>, s, j, V, vstride, W, n, sh.slice, sv, Vout, pk));
+    return EMFA_OK;
+}
+
+static emfa_status_t launch_arnoldi_step(Ctx* c, const StepShape& sh, int nrhs, cudaStream_t st, const GmresDev& s,
+                                         int j, const float2* V, size_t vstride, const float2* W, int n, float2* Vout,
+                                         const HPack& pk)
+{
+    if (sh.e == 1) return launch_step_e<1>(c, sh, nrhs, st, s, j, V, vstride, W, n, Vout, pk);
+    if (sh.e == 2) return launch_step_e<2>(c, sh, nrhs, st, s, j, V, vstride, W, n, Vout, pk);
+    return launch_step_e<4>(c, sh, nrhs, st, s, j, V, vstride, W, n, Vout, pk);
+}
+
 template <typename T>
 static emfa_status_t gmres_t(Ctx* c, LinOp& A, const void* B, int nrhs, double2* X, const emfa_solver_params_t* sp,
                              emfa_solve_info_t* info, cudaStream_t st)
@@ -859,6 +1146,17 @@ static emfa_status_t gmres_t(Ctx* c, LinOp& A, const void* B, int nrhs, double2*
     // the FP32 inner solve of the refinement only has to gain a few digits per
     // cycle: one Gram-Schmidt pass; the plain FP64 path keeps two
     const bool two_pass = sp->orth == 2 || (sp->orth == 0 && prec == EMFA_F64);
+    // CGS1 on an FP32 basis: one fused launch per Arnoldi step (k_arnoldi_step)
+    // where the restart and N fit it and its clusters fill at most about two
+    // waves of CTAs; orth 3 keeps the separate passes.  Measured GMRES(30)
+    // solves (split-FP16 products, 18 steps): fused 10-15 % faster for 1 to
+    // 64 right-hand sides at N = 2000, 4000 and 7680; 4-8 % slower for 360,
+    // where the separate passes' thousands of independent CTAs hide memory
+    // latency better than two staged CTAs an SM between cluster barriers.
+    const StepShape sh = step_shape(n);
+    // orth 4 takes the fused step whatever the grid size (for measurement)
+    const bool fused = std::is_same<T, float>::value && !two_pass && sp->orth != 3 && m <= AS_MAXV && sh.e > 0 &&
+                       ((long)nrhs * sh.cs <= 4L * sms || sp->orth == 4);
     int total_iters = 0, cycles = 0, converged = 0;
     int host_cnt[4];
     // Arnoldi steps are checked one step late: step j and the operator
@@ -906,26 +1204,38 @@ static emfa_status_t gmres_t(Ctx* c, LinOp& A, const void* B, int nrhs, double2*
             // (h2 = V^H W; W -= V h2) and H gets h + h2.
             const dim3 vg(vblk, nrhs);
             const int nv = j + 1;
-            // the updates sum the dots' block partials themselves (block 0 keeps
-            // the coefficients in s.hcol / s.y for the Arnoldi finish)
-            const size_t hsm = 2 * nv * sizeof(typename Acc<T>::type);
-            k_vdots<T><<<vg, 256, 0, st>>>(V, vec, nv, W, n, nrhs, vblk, partial);
-            if (two_pass) {
-                k_vupdate<T, false><<<vg, 256, hsm, st>>>(V, vec, nv, s.hcol, partial, W, n, nrhs, vblk, pnorm);
-                k_vdots<T><<<vg, 256, 0, st>>>(V, vec, nv, W, n, nrhs, vblk, partial);
-                k_vupdate<T, true><<<vg, 256, hsm, st>>>(V, vec, nv, s.y, partial, W, n, nrhs, vblk, pnorm);
-                c->kernel_launches += 2;
+            HPack pk;
+            bool packs = false;
+            if (fused) {
+                // V_{j+1} and the next product's operand come out of the step
+                packs = A.pack_target(c, nrhs, &pk);
+                if (!packs) pk = HPack{};
+                EMFA_CUDA(c, cudaMemsetAsync(s.counters, 0, sizeof(int), st));
+                EMFA_TRY(launch_arnoldi_step(c, sh, nrhs, st, s, j, (const float2*)V, vec, (const float2*)W, n,
+                                             (float2*)(V + (size_t)(j + 1) * vec), pk));
+                c->kernel_launches += 1;
             } else {
-                k_vupdate<T, true><<<vg, 256, hsm, st>>>(V, vec, nv, s.hcol, partial, W, n, nrhs, vblk, pnorm);
+                // the updates sum the dots' block partials themselves (block 0
+                // keeps the coefficients in s.hcol / s.y for the Arnoldi finish)
+                const size_t hsm = 2 * nv * sizeof(typename Acc<T>::type);
+                k_vdots<T><<<vg, 256, 0, st>>>(V, vec, nv, W, n, nrhs, vblk, partial);
+                if (two_pass) {
+                    k_vupdate<T, false><<<vg, 256, hsm, st>>>(V, vec, nv, s.hcol, partial, W, n, nrhs, vblk, pnorm);
+                    k_vdots<T><<<vg, 256, 0, st>>>(V, vec, nv, W, n, nrhs, vblk, partial);
+                    k_vupdate<T, true><<<vg, 256, hsm, st>>>(V, vec, nv, s.y, partial, W, n, nrhs, vblk, pnorm);
+                    c->kernel_launches += 2;
+                } else {
+                    k_vupdate<T, true><<<vg, 256, hsm, st>>>(V, vec, nv, s.hcol, partial, W, n, nrhs, vblk, pnorm);
+                }
+                EMFA_CUDA(c, cudaMemsetAsync(s.counters, 0, sizeof(int), st));
+                if (m <= 32)
+                    k_arnoldi_finish_warp<<<(nrhs * 32 + 127) / 128, 128, 0, st>>>(s, j, pnorm, vblk, two_pass ? 1 : 0);
+                else
+                    k_arnoldi_finish<<<(nrhs * 32 + 127) / 128, 128, 0, st>>>(s, j, pnorm, vblk, two_pass ? 1 : 0);
+                c->kernel_launches += 3;
             }
-            EMFA_CUDA(c, cudaMemsetAsync(s.counters, 0, sizeof(int), st));
-            if (m <= 32)
-                k_arnoldi_finish_warp<<<(nrhs * 32 + 127) / 128, 128, 0, st>>>(s, j, pnorm, vblk, two_pass ? 1 : 0);
-            else
-                k_arnoldi_finish<<<(nrhs * 32 + 127) / 128, 128, 0, st>>>(s, j, pnorm, vblk, two_pass ? 1 : 0);
             EMFA_CUDA(c, cudaMemcpyAsync((void*)(slot + (j & 1)), s.counters, sizeof(int), cudaMemcpyDeviceToHost, st));
             EMFA_CUDA(c, cudaEventRecord(sev.e[j & 1], st));
-            c->kernel_launches += 3;
             ++steps;
             if (j > 0) {
                 EMFA_CUDA(c, cudaEventSynchronize(sev.e[(j - 1) & 1]));
@@ -935,8 +1245,14 @@ static emfa_status_t gmres_t(Ctx* c, LinOp& A, const void* B, int nrhs, double2*
                 }
             }
             if (j + 1 == m) break;
-            // V_{j+1} = W / beta, then W = A V_{j+1} (one pass for operators that pack)
-            EMFA_TRY(A.normalize_apply(c, W, s.scale, s.wmax, V + (size_t)(j + 1) * vec, W, nrhs, st));
+            // V_{j+1} = W / beta, then W = A V_{j+1} (one pass for operators that
+            // pack; the fused step has normalised and packed already)
+            if (fused && packs)
+                EMFA_TRY(A.apply_packed(c, pk, W, nrhs, st));
+            else if (fused)
+                EMFA_TRY(A.apply(c, V + (size_t)(j + 1) * vec, W, nrhs, st));
+            else
+                EMFA_TRY(A.normalize_apply(c, W, s.scale, s.wmax, V + (size_t)(j + 1) * vec, W, nrhs, st));
         }
         total_iters += steps;
         EMFA_TRY(A.check(c, st));
@@ -1347,6 +1663,14 @@ struct DenseOp : LinOp {
         if (prec == EMFA_F32 && mode == F16X && wmax)
             return hgemm_normalize_apply(c, hp, W, scale, wmax, Vout, Y, nrhs, st);
         return LinOp::normalize_apply(c, W, scale, wmax, Vout, Y, nrhs, st);
+    }
+    bool pack_target(Ctx* c, int nrhs, HPack* p) override
+    {
+        return prec == EMFA_F32 && mode == F16X && hgemm_pack_target(c, hp, nrhs, p) == EMFA_OK;
+    }
+    emfa_status_t apply_packed(Ctx* c, const HPack& p, void* Y, int nrhs, cudaStream_t st) override
+    {
+        return hgemm_apply_packed(c, hp, p, Y, nrhs, st);
     }
     emfa_status_t check(Ctx* c, cudaStream_t st) override
     {

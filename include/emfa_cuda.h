@@ -99,7 +99,11 @@ typedef struct {
     int max_refine;     /* outer true-residual cycles for EMFA_F32 (GMRES-IR)       */
     int orth;           /* GMRES Gram-Schmidt: 0 = auto (CGS1 for the EMFA_F32     */
                         /* inner solve of the refinement, CGS2 for EMFA_F64),      */
-                        /* 1 = CGS1, 2 = CGS2                                      */
+                        /* 1 = CGS1, 2 = CGS2, 3 = CGS1 in separate passes (the    */
+                        /* FP32 CGS1 step is otherwise one fused launch for        */
+                        /* restarts up to 32, N up to 16384 and n_rhs x ceil(N /   */
+                        /* 1024) (at most 8) up to 4 x the SM count), 4 = CGS1     */
+                        /* fused whatever n_rhs (restart and N as for 1)           */
     double inner_reduction; /* GMRES refinement with reduced-precision products:  */
                         /* a cycle's inner steps stop once the implicit residual   */
                         /* falls below this fraction of the cycle's starting true  */

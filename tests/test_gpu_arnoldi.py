@@ -1,0 +1,130 @@
+"""The fused Arnoldi step (k_arnoldi_step: a cluster of CTAs per right-hand
+side; Gram-Schmidt coefficients summed through distributed shared memory;
+update, normalisation and FP16 packing in the same launch) against the same
+CGS1 step as separate passes (orth "cgs1_split").
+
+The two forms sum the coefficients in different orders (FP32 within a warp,
+FP64 across warps, CTAs and blocks in both), so their iterates agree to
+rounding.  Tolerances: both meet the target (true residual 1e-6), iteration
+counts within one step, solutions within 1e-5 of each other (relative L2; the
+test matrices have condition numbers near 2).
+
+Shapes cover every cluster form: one CTA per right-hand side (N <= 1024),
+clusters of 2, 3 and 8, one to four elements per thread, the largest N the
+fused step takes (16384) and one past it (the separate passes again).  The
+right-hand-side counts keep the grids small enough for the fused step
+(n_rhs x CTAs per right-hand side <= 4 x the SM count); the last test checks
+the choice by grid size.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _system(n, nrhs, seed):
+    """Z = 2 I + 0.7 G / sqrt(n) (G complex normal: eigenvalues in a disk of
+    radius ~0.7 about 2, ~20 GMRES steps to 1e-6), random right-hand sides
+    of different scales, and one zero right-hand side (inactive from the
+    start)."""
+    import torch
+    g = torch.Generator(device="cuda")
+    g.manual_seed(seed)
+    Z = torch.randn(n, n, dtype=torch.complex64, device="cuda", generator=g) * (0.7 / np.sqrt(n))
+    Z.diagonal().add_(2.0)
+    B = torch.randn(nrhs, n, dtype=torch.complex64, device="cuda", generator=g)
+    B *= torch.logspace(-3, 3, nrhs, device="cuda").to(torch.complex64)[:, None]
+    B[nrhs // 2] = 0
+    return Z, B
+
+
+def _solve(ctx, Z, B, orth, matvec, restart=30):
+    from emfa_gb300 import api
+    sp = api.solver_params("gmres", restart=restart, tol=1e-6, max_iter=2000, matvec=matvec, orth=orth)
+    X, info = api.solve(ctx, Z, B, sp)
+    return X, info
+
+
+def _true_residual(Z, B, X):
+    import torch
+    R = B.to(torch.complex128) - X @ Z.to(torch.complex128).T
+    nb = torch.linalg.norm(B.to(torch.complex128), dim=1)
+    nr = torch.linalg.norm(R, dim=1)
+    return torch.where(nb > 0, nr / torch.where(nb > 0, nb, 1), nr).cpu().numpy()
+
+
+@pytest.mark.parametrize("n,nrhs,matvec", [
+    (300, 40, "f16x"),     # one CTA per right-hand side, one element per thread
+    (1500, 24, "f16x"),    # clusters of 2
+    (2500, 12, "f32"),     # clusters of 3, unpacked operator (FP32 CUDA-core product)
+    (7680, 16, "f16x"),    # clusters of 8, two elements per thread
+    (7680, 6, "tf32"),
+    (12000, 6, "f16x"),    # four elements per thread
+    (16384, 4, "f16x"),    # the largest N of the fused step
+    (16385, 3, "f16x"),    # separate passes
+])
+def test_fused_step_matches_separate_passes(ctx, n, nrhs, matvec):
+    import torch
+    Z, B = _system(n, nrhs, seed=n)
+    Xf, inf_f = _solve(ctx, Z, B, "cgs1", matvec)
+    Xs, inf_s = _solve(ctx, Z, B, "cgs1_split", matvec)
+    assert inf_f.converged == nrhs and inf_s.converged == nrhs
+    assert abs(inf_f.iterations - inf_s.iterations) <= 1, (inf_f.iterations, inf_s.iterations)
+    assert inf_f.iterations >= 10  # the step ran many times, across several basis lengths
+    rf, rs = _true_residual(Z, B, Xf), _true_residual(Z, B, Xs)
+    assert rf.max() < 1e-6 and rs.max() < 1e-6, (rf.max(), rs.max())
+    zero = nrhs // 2
+    assert torch.count_nonzero(Xf[zero]) == 0
+    d = torch.linalg.norm(Xf - Xs, dim=1) / torch.linalg.norm(Xs, dim=1).clamp_min(1e-300)
+    d[zero] = 0
+    assert d.max().item() < 1e-5, d.max().item()
+
+
+def test_fused_step_restart_boundaries(ctx):
+    """Restart lengths 1, 2, 7 and 32 (the longest the fused step takes; 33
+    goes back to the separate passes): the last step of a cycle and the
+    restart from the true residual."""
+    Z, B = _system(4096, 8, seed=7)
+    for m in (1, 2, 7, 32, 33):
+        Xf, inf_f = _solve(ctx, Z, B, "cgs1", "f16x", restart=m)
+        Xs, inf_s = _solve(ctx, Z, B, "cgs1_split", "f16x", restart=m)
+        assert inf_f.converged == 8 and inf_s.converged == 8, m
+        assert abs(inf_f.iterations - inf_s.iterations) <= max(1, inf_s.iterations // 20), (m, inf_f.iterations,
+                                                                                             inf_s.iterations)
+        rf = _true_residual(Z, B, Xf)
+        assert rf.max() < 1e-6, (m, rf.max())
+
+
+def test_fused_step_reproducible(ctx):
+    """Fixed-order sums: the same solve twice gives the same bits."""
+    import torch
+    Z, B = _system(7680, 10, seed=3)
+    X1, i1 = _solve(ctx, Z, B, "cgs1", "f16x")
+    X2, i2 = _solve(ctx, Z, B, "cgs1", "f16x")
+    assert i1.iterations == i2.iterations
+    assert torch.equal(X1, X2)
+
+
+def _launches(ctx, Z, B, orth):
+    before = ctx.launches()
+    X, info = _solve(ctx, Z, B, orth, "f16x")
+    return ctx.launches() - before, info
+
+
+def test_auto_choice_by_grid_size(ctx):
+    """Tens of right-hand sides take the fused step (one launch a step);
+    hundreds at N = 7680 (clusters of 8: more than four CTAs an SM) take the
+    separate passes (coefficients, update, column, normalisation: four)."""
+    Z, B = _system(7680, 400, seed=11)
+    few = B[:16].contiguous()
+    n_auto, i_auto = _launches(ctx, Z, few, "cgs1")
+    n_split, i_split = _launches(ctx, Z, few, "cgs1_split")
+    assert i_auto.iterations == i_split.iterations
+    # at least two launches fewer per Arnoldi step (three kernels become one)
+    assert n_split - n_auto >= 2 * i_split.iterations, (n_auto, n_split, i_split.iterations)
+    n_auto, i_auto = _launches(ctx, Z, B, "cgs1")
+    n_split, i_split = _launches(ctx, Z, B, "cgs1_split")
+    assert i_auto.iterations == i_split.iterations and n_auto == n_split
+    # orth "cgs1_fused" takes the fused step at any grid size, same solution
+    n_fused, i_fused = _launches(ctx, Z, B, "cgs1_fused")
+    assert abs(i_fused.iterations - i_split.iterations) <= 1 and n_split - n_fused >= 2 * i_fused.iterations
