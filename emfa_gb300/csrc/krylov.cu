@@ -351,7 +351,9 @@ __global__ void __launch_bounds__(256) k_vdots(const Cx<T>* __restrict__ V, size
 
 // With `partial` (the block partials of k_vdots) the coefficients are summed
 // here, over the blocks in order as k_reduce_partials does, and block 0 also
-// stores them in h; without it they are read from h.
+// stores them in h; without it they are read from h.  The right-hand sides
+// are taken last first: k_vdots ran them first to last, so the basis slices
+// it read last (up to the L2's size, ~100 MB) are read again from L2.
 template <typename T, bool NORM>
 __global__ void __launch_bounds__(256) k_vupdate(const Cx<T>* __restrict__ V, size_t vstride, int nv,
                                                  double2* __restrict__ h, const double2* __restrict__ partial,
@@ -359,7 +361,7 @@ __global__ void __launch_bounds__(256) k_vupdate(const Cx<T>* __restrict__ V, si
                                                  double2* __restrict__ pnorm)
 {
     using A = typename Acc<T>::type;
-    const int blk = blockIdx.x, r = blockIdx.y;
+    const int blk = blockIdx.x, r = nrhs - 1 - (int)blockIdx.y;
     const size_t base = (size_t)r * n;
     // coefficients (dynamic shared memory: 2 nv values, any restart length)
     extern __shared__ unsigned char dyn_smem[];
@@ -652,6 +654,67 @@ __global__ void k_arnoldi_finish_warp(GmresDev s, int j, const double2* __restri
         }
     }
     arnoldi_column(s, r, j, h, beta);
+}
+
+// Last kernel of the separate-pass CGS1 step (FP32 basis, restarts up to
+// 32): one CTA per right-hand side.  Warp 0 finishes the Arnoldi column (as
+// k_arnoldi_finish_warp, single pass) while the other warps write
+// V_{j+1} = W / beta and, for operators that pack their input, the FP16
+// rows of the next product (as k_hpack_scale): the column's serial FP64
+// chain and the normalisation's stream overlap.  A right-hand side that
+// this step finds converged is normalised all the same (its V_{j+1} lies
+// past its basis length); one that was already inactive writes nothing.
+__global__ void __launch_bounds__(256) k_finish_pack(GmresDev s, int j, const double2* __restrict__ pnorm, int nblk,
+                                                     const float2* __restrict__ W, int n, float2* __restrict__ Vout,
+                                                     HPack pk)
+{
+    __shared__ double sbeta;
+    __shared__ float nscale[2];
+    const int r = blockIdx.x, tid = threadIdx.x, lane = tid & 31;
+    if (!s.active[r]) {
+        if (tid == 0) s.scale[r] = 0.0;
+        return;
+    }
+    if (tid == 0) {
+        double nr2 = 0.0, wm = 0.0;
+        for (int b = 0; b < nblk; ++b) {
+            nr2 += pnorm[(size_t)r * nblk + b].x;
+            wm = fmax(wm, pnorm[(size_t)r * nblk + b].y);
+        }
+        s.wmax[r] = wm;
+        const double beta = sqrt(nr2);
+        const double scale = beta > 0.0 ? 1.0 / beta : 0.0;
+        sbeta = beta;
+        nscale[0] = (float)scale;
+        nscale[1] = 1.f;
+        if (pk.bh) {
+            const int ex = hpack_exponent(wm, scale);
+            nscale[1] = ldexpf(1.f, 14 - ex);
+            pk.inv_t[r] = ldexpf(1.f, ex - 14);
+        }
+    }
+    __syncthreads();
+    if (tid < 32) {
+        const double2 h = lane <= j ? s.hcol[(size_t)lane * s.nrhs + r] : make_double2(0.0, 0.0);
+        arnoldi_column(s, r, j, h, sbeta);
+        return;
+    }
+    const float sc = nscale[0], t = nscale[1];
+    const float2* w = W + (size_t)r * n;
+    float2* v = Vout + (size_t)r * n;
+    __half2* h0 = pk.bh ? reinterpret_cast<__half2*>(pk.bh + (size_t)(2 * r) * pk.ldh) : nullptr;
+    __half2* h1 = pk.bh ? reinterpret_cast<__half2*>(pk.bh + (size_t)(2 * r + 1) * pk.ldh) : nullptr;
+#pragma unroll 4
+    for (int k = tid - 32; k < n; k += blockDim.x - 32) {
+        const float2 x = w[k];
+        const float2 y = make_float2(x.x * sc, x.y * sc);
+        v[k] = y;
+        if (h0) {
+            const __half hre = __float2half_rn(t * y.x), him = __float2half_rn(t * y.y);
+            h0[k] = __halves2half2(hre, __hneg(him));
+            h1[k] = __halves2half2(him, hre);
+        }
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -1157,6 +1220,9 @@ static emfa_status_t gmres_t(Ctx* c, LinOp& A, const void* B, int nrhs, double2*
     // orth 4 takes the fused step whatever the grid size (for measurement)
     const bool fused = std::is_same<T, float>::value && !two_pass && sp->orth != 3 && m <= AS_MAXV && sh.e > 0 &&
                        ((long)nrhs * sh.cs <= 4L * sms || sp->orth == 4);
+    // separate passes on an FP32 basis with one Gram-Schmidt pass end in
+    // k_finish_pack (column, normalisation and packing in one launch)
+    const bool finish_pack = std::is_same<T, float>::value && !fused && !two_pass && m <= 32;
     int total_iters = 0, cycles = 0, converged = 0;
     int host_cnt[4];
     // Arnoldi steps are checked one step late: step j and the operator
@@ -1206,10 +1272,15 @@ static emfa_status_t gmres_t(Ctx* c, LinOp& A, const void* B, int nrhs, double2*
             const int nv = j + 1;
             HPack pk;
             bool packs = false;
-            if (fused) {
-                // V_{j+1} and the next product's operand come out of the step
+            // the step normalises V_{j+1} itself (fused, or separate passes
+            // ending in k_finish_pack); otherwise normalize_apply does
+            const bool normalises = fused || finish_pack;
+            if (normalises) {
                 packs = A.pack_target(c, nrhs, &pk);
                 if (!packs) pk = HPack{};
+            }
+            if (fused) {
+                // V_{j+1} and the next product's operand come out of the step
                 EMFA_CUDA(c, cudaMemsetAsync(s.counters, 0, sizeof(int), st));
                 EMFA_TRY(launch_arnoldi_step(c, sh, nrhs, st, s, j, (const float2*)V, vec, (const float2*)W, n,
                                              (float2*)(V + (size_t)(j + 1) * vec), pk));
@@ -1228,7 +1299,10 @@ static emfa_status_t gmres_t(Ctx* c, LinOp& A, const void* B, int nrhs, double2*
                     k_vupdate<T, true><<<vg, 256, hsm, st>>>(V, vec, nv, s.hcol, partial, W, n, nrhs, vblk, pnorm);
                 }
                 EMFA_CUDA(c, cudaMemsetAsync(s.counters, 0, sizeof(int), st));
-                if (m <= 32)
+                if (finish_pack)
+                    k_finish_pack<<<nrhs, 256, 0, st>>>(s, j, pnorm, vblk, (const float2*)W, n,
+                                                        (float2*)(V + (size_t)(j + 1) * vec), pk);
+                else if (m <= 32)
                     k_arnoldi_finish_warp<<<(nrhs * 32 + 127) / 128, 128, 0, st>>>(s, j, pnorm, vblk, two_pass ? 1 : 0);
                 else
                     k_arnoldi_finish<<<(nrhs * 32 + 127) / 128, 128, 0, st>>>(s, j, pnorm, vblk, two_pass ? 1 : 0);
@@ -1247,9 +1321,9 @@ static emfa_status_t gmres_t(Ctx* c, LinOp& A, const void* B, int nrhs, double2*
             if (j + 1 == m) break;
             // V_{j+1} = W / beta, then W = A V_{j+1} (one pass for operators that
             // pack; the fused step has normalised and packed already)
-            if (fused && packs)
+            if (normalises && packs)
                 EMFA_TRY(A.apply_packed(c, pk, W, nrhs, st));
-            else if (fused)
+            else if (normalises)
                 EMFA_TRY(A.apply(c, V + (size_t)(j + 1) * vec, W, nrhs, st));
             else
                 EMFA_TRY(A.normalize_apply(c, W, s.scale, s.wmax, V + (size_t)(j + 1) * vec, W, nrhs, st));
