@@ -337,7 +337,8 @@ __global__ void __launch_bounds__(256) k_hpack_f64(const double2* __restrict__ X
 // hi x hi products last; eight epilogue warps drain each k-block into
 // Kahan-compensated FP32 sums in registers (56 columns each) while the next
 // k-block accumulates in the second buffer, and the last step forms
-// B - sum / (s t) in FP64.
+// B - sum / (s t) in FP64.  A drain releases the accumulator as soon as its
+// 56 columns are in registers, before the sums.
 // ---------------------------------------------------------------------------
 constexpr int RBN = 112;  // 56 columns per epilogue warp: the sums fit the 168 registers of a 10-warp block
 constexpr int RTHREADS = 320;  // producer, MMA, 8 epilogue warps
@@ -452,7 +453,10 @@ __global__ void __launch_bounds__(RTHREADS, 1)
         const int col0 = 56 * h;
         // Kahan sums: sum - cmp is the running total.  cmp stays below half an
         // ulp of sum, so bf16 holds it to 2^-32 of the total (84 registers for
-        // 56 columns instead of 112)
+        // 56 columns instead of 112).  The accumulator's 56 columns come in
+        // one round trip (tmem_ld56: three loads, one wait), so a k-block's
+        // drain pays one tensor-memory latency instead of seven, and the
+        // accumulator is released as soon as they are in registers.
         float sum[56];
         __nv_bfloat162 cmp[28];
 #pragma unroll
@@ -470,25 +474,21 @@ __global__ void __launch_bounds__(RTHREADS, 1)
                 break;
             }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-#pragma unroll
-            for (int g = 0; g < 7; ++g) {
-                float v[8];
-                tmem_ld8(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(a * S::ACC + col0 + 8 * g), v);
-#pragma unroll
-                for (int i = 0; i < 8; i += 2) {
-                    const int j = 8 * g + i;
-                    const float2 c = __bfloat1622float2(cmp[j / 2]);
-                    const float y0 = __fsub_rn(v[i], c.x), y1 = __fsub_rn(v[i + 1], c.y);
-                    const float t0 = __fadd_rn(sum[j], y0), t1 = __fadd_rn(sum[j + 1], y1);
-                    cmp[j / 2] = __floats2bfloat162_rn(__fsub_rn(__fsub_rn(t0, sum[j]), y0),
-                                                       __fsub_rn(__fsub_rn(t1, sum[j + 1]), y1));
-                    sum[j] = t0;
-                    sum[j + 1] = t1;
-                }
-            }
+            float v[56];
+            tmem_ld56(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(a * S::ACC + col0), v);
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
             __syncwarp();
             if (lane == 0) mbar_arrive(acc_empty + a);
+#pragma unroll
+            for (int i = 0; i < 56; i += 2) {
+                const float2 c = __bfloat1622float2(cmp[i / 2]);
+                const float y0 = __fsub_rn(v[i], c.x), y1 = __fsub_rn(v[i + 1], c.y);
+                const float t0 = __fadd_rn(sum[i], y0), t1 = __fadd_rn(sum[i + 1], y1);
+                cmp[i / 2] = __floats2bfloat162_rn(__fsub_rn(__fsub_rn(t0, sum[i]), y0),
+                                                   __fsub_rn(__fsub_rn(t1, sum[i + 1]), y1));
+                sum[i] = t0;
+                sum[i + 1] = t1;
+            }
         }
         if (ok) {
             // the stage ring is idle once the last accumulator was drained: park
