@@ -325,6 +325,29 @@ __global__ void __launch_bounds__(256) k_hpack_f64(const double2* __restrict__ X
     }
 }
 
+// Two FP32 additions in one instruction (add/sub.rn.f32x2), round to nearest
+// like __fadd_rn / __fsub_rn: the residual's Kahan sums run on column pairs
+__device__ __forceinline__ unsigned long long pk2(float2 v)
+{
+    return ((unsigned long long)__float_as_uint(v.y) << 32) | __float_as_uint(v.x);
+}
+__device__ __forceinline__ float2 upk2(unsigned long long u)
+{
+    return make_float2(__uint_as_float((unsigned)u), __uint_as_float((unsigned)(u >> 32)));
+}
+__device__ __forceinline__ float2 fadd2_rn(float2 a, float2 b)
+{
+    unsigned long long z;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(z) : "l"(pk2(a)), "l"(pk2(b)));
+    return upk2(z);
+}
+__device__ __forceinline__ float2 fsub2_rn(float2 a, float2 b)
+{
+    unsigned long long z;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(z) : "l"(pk2(a)), "l"(pk2(b)));
+    return upk2(z);
+}
+
 // ---------------------------------------------------------------------------
 // refinement residual R = B - Z X, Z X ~ (Zh Xh + Zh Xl + Zl Xh) / (s t)
 //
@@ -454,15 +477,19 @@ __global__ void __launch_bounds__(RTHREADS, 1)
         // Kahan sums: sum - cmp is the running total.  cmp stays below half an
         // ulp of sum, so bf16 holds it to 2^-32 of the total (84 registers for
         // 56 columns instead of 112).  The accumulator's 56 columns come in
-        // one round trip (tmem_ld56: three loads, one wait), so a k-block's
-        // drain pays one tensor-memory latency instead of seven, and the
-        // accumulator is released as soon as they are in registers.
-        float sum[56];
+        // one round trip (tmem_ld56: three loads, one wait), the accumulator
+        // is released as soon as they are in registers, and the sums run on
+        // column pairs (f32x2: two additions an instruction).  The drain is
+        // issue-bound: it sets the kernel's pace (0.81 ms with seven round
+        // trips and scalar sums, 0.62 ms so).  FP32 compensation (two
+        // instructions a column) spills at the 168 registers ten warps leave.
+        float2 sum[28];  // columns 2i, 2i + 1
         __nv_bfloat162 cmp[28];
 #pragma unroll
-        for (int i = 0; i < 56; ++i) sum[i] = 0.f;
-#pragma unroll
-        for (int i = 0; i < 28; ++i) cmp[i] = __floats2bfloat162_rn(0.f, 0.f);
+        for (int i = 0; i < 28; ++i) {
+            sum[i] = make_float2(0.f, 0.f);
+            cmp[i] = __floats2bfloat162_rn(0.f, 0.f);
+        }
         bool ok = true;
 #pragma unroll 1
         for (int kb = 0; kb < kblocks; ++kb) {
@@ -480,14 +507,12 @@ __global__ void __launch_bounds__(RTHREADS, 1)
             __syncwarp();
             if (lane == 0) mbar_arrive(acc_empty + a);
 #pragma unroll
-            for (int i = 0; i < 56; i += 2) {
-                const float2 c = __bfloat1622float2(cmp[i / 2]);
-                const float y0 = __fsub_rn(v[i], c.x), y1 = __fsub_rn(v[i + 1], c.y);
-                const float t0 = __fadd_rn(sum[i], y0), t1 = __fadd_rn(sum[i + 1], y1);
-                cmp[i / 2] = __floats2bfloat162_rn(__fsub_rn(__fsub_rn(t0, sum[i]), y0),
-                                                   __fsub_rn(__fsub_rn(t1, sum[i + 1]), y1));
-                sum[i] = t0;
-                sum[i + 1] = t1;
+            for (int i = 0; i < 28; ++i) {
+                const float2 y = fsub2_rn(make_float2(v[2 * i], v[2 * i + 1]), __bfloat1622float2(cmp[i]));
+                const float2 t = fadd2_rn(sum[i], y);
+                const float2 cn = fsub2_rn(fsub2_rn(t, sum[i]), y);
+                cmp[i] = __floats2bfloat162_rn(cn.x, cn.y);
+                sum[i] = t;
             }
         }
         if (ok) {
@@ -497,9 +522,9 @@ __global__ void __launch_bounds__(RTHREADS, 1)
 #pragma unroll
             for (int i = 0; i < 28; ++i) {
                 const float2 cf = __bfloat1622float2(cmp[i]);
-                park[4 * i] = sum[2 * i];
+                park[4 * i] = sum[i].x;
                 park[4 * i + 1] = cf.x;
-                park[4 * i + 2] = sum[2 * i + 1];
+                park[4 * i + 2] = sum[i].y;
                 park[4 * i + 3] = cf.y;
             }
             if (f < M) {
