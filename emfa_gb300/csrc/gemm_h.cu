@@ -153,16 +153,21 @@ __global__ void __launch_bounds__(THREADS, 1)
         if (ok) {
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const float is = *inv_s;
+            // 48 columns a round trip where BN allows (144 = 3 x 48), else 16
+            constexpr int CW = BN % 48 == 0 ? 48 : 16;
 #pragma unroll 1
             for (int m = 0; m < MS; ++m) {
                 const int f = f0 + m * BM + 32 * q + lane;
 #pragma unroll 1
-                for (int c = 0; c < BN; c += 16) {
-                    float v[16];
-                    tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(m * S::ACC + c), v);
+                for (int c = 0; c < BN; c += CW) {
+                    float v[CW];
+                    if constexpr (CW == 48)
+                        tmem_ld48(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(m * S::ACC + c), v);
+                    else
+                        tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(m * S::ACC + c), v);
                     if (f < M) {
 #pragma unroll
-                        for (int i = 0; i < 8; ++i) {
+                        for (int i = 0; i < CW / 2; ++i) {
                             const int r = (c0 + c) / 2 + i;
                             if (r < R) {
                                 const float sc = is * inv_t[r];
