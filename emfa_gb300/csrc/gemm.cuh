@@ -70,6 +70,14 @@ __device__ __forceinline__ int hpack_exponent(double wmax, double scale)
     frexpf((float)(wmax * scale) * 1.0000002f, &e);
     return e;
 }
+// the same from FP32 operands (their product rounds once more: the factor
+// covers two ulps)
+__device__ __forceinline__ int hpack_exponent_f(float wmax, float scale)
+{
+    int e = 0;
+    frexpf(wmax * scale * 1.0000004f, &e);
+    return e;
+}
 // R (complex128) = B - Z X for X complex128 and B complex64 (f32b) or complex128:
 // Zh Xh + Zh Xl + Zl Xh on the tensor cores, FP32 chunk sums reduced in FP64
 emfa_status_t hgemm_residual(Ctx* c, const HPlanes& h, const double2* X, const void* B, bool b_is_f32, double2* R,

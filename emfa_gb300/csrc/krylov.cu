@@ -625,6 +625,79 @@ __device__ void arnoldi_column(const GmresDev& s, int r, int j, double2 h, doubl
     if (lane <= j) H[lane * m + j] = h;
 }
 
+// FP32 form of arnoldi_column for the FP32-basis inner solve of the
+// refinement: the same steps in FP32 arithmetic, with H, cs, sn and g kept in
+// FP64 memory.  GB300's FP64 pipe takes about 64 cycles a warp instruction,
+// so the FP64 chain of a column (rotations, two hypot, four divisions) ran
+// for 10-20 us; the coefficients of an FP32 basis carry ~1e-7 relative error
+// already, and every restart recomputes the true residual in FP64.
+__device__ __forceinline__ float2 shfl_f2(float2 v, int src)
+{
+    return make_float2(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
+}
+
+__device__ void arnoldi_column_f32(const GmresDev& s, int r, int j, double2 hd, float beta)
+{
+    const int lane = threadIdx.x & 31, m = s.m;
+    double2* H = s.H + (size_t)r * (m + 1) * m;
+    double* cs = s.cs + (size_t)r * m;
+    double2* sn = s.sn + (size_t)r * m;
+    float2 h = make_float2((float)hd.x, (float)hd.y);
+    const float cl = lane < j ? (float)cs[lane] : 0.f;
+    const double2 sld = lane < j ? sn[lane] : make_double2(0.0, 0.0);
+    const float2 sl = make_float2((float)sld.x, (float)sld.y);
+    for (int i = 0; i < j; ++i) {
+        const float2 y = shfl_f2(h, i + 1), x = shfl_f2(h, i);
+        const float c = __shfl_sync(0xffffffffu, cl, i);
+        const float2 sv = shfl_f2(sl, i);
+        if (lane == i)
+            h = make_float2(c * x.x + sv.x * y.x - sv.y * y.y, c * x.y + sv.x * y.y + sv.y * y.x);
+        else if (lane == i + 1)
+            h = make_float2(-(sv.x * x.x + sv.y * x.y) + c * y.x, -(sv.x * x.y - sv.y * x.x) + c * y.y);
+    }
+    if (lane == j) {
+        const float2 a = h;
+        const float b = beta;
+        const float aa = hypotf(a.x, a.y);
+        const float nu = hypotf(aa, b);
+        float c;
+        float2 sv;
+        if (aa == 0.f) {
+            c = 0.f;
+            sv = make_float2(1.f, 0.f);
+            h = make_float2(b, 0.f);
+        } else {
+            c = aa / nu;
+            const float2 ph = make_float2(a.x / aa, a.y / aa);
+            sv = make_float2(ph.x * b / nu, ph.y * b / nu);
+            h = make_float2(ph.x * nu, ph.y * nu);
+        }
+        H[(j + 1) * m + j] = make_double2(0.0, 0.0);
+        cs[j] = c;
+        sn[j] = make_double2(sv.x, sv.y);
+        double2* g = s.g + (size_t)r * (m + 1);
+        const double2 gjd = g[j];
+        const float2 gj = make_float2((float)gjd.x, (float)gjd.y);
+        const float2 gn = make_float2(-(sv.x * gj.x + sv.y * gj.y), -(sv.x * gj.y - sv.y * gj.x));
+        g[j + 1] = make_double2(gn.x, gn.y);
+        g[j] = make_double2(c * gj.x, c * gj.y);
+        const double res = hypotf(gn.x, gn.y);
+        s.jlen[r] = j + 1;
+        s.est[r] = res;
+        const double thr =
+            fmax(s.inner * (s.tol_abs ? s.tol : s.tol * s.bnorm[r]), s.red * s.true_res[r] * s.bnorm[r]);
+        const bool breakdown = (double)beta <= 1e-14 * s.bnorm[r];
+        if (res < thr || breakdown || j + 1 == m) {
+            s.active[r] = 0;
+            s.scale[r] = 0.0;
+        } else {
+            s.scale[r] = 1.0 / (double)beta;
+            atomicAdd(s.counters, 1);
+        }
+    }
+    if (lane <= j) H[lane * m + j] = make_double2(h.x, h.y);
+}
+
 __global__ void k_arnoldi_finish_warp(GmresDev s, int j, const double2* __restrict__ pnorm, int nblk, int two_pass)
 {
     const int r = (int)(((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
@@ -657,46 +730,56 @@ __global__ void k_arnoldi_finish_warp(GmresDev s, int j, const double2* __restri
 }
 
 // Last kernel of the separate-pass CGS1 step (FP32 basis, restarts up to
-// 32): one CTA per right-hand side.  Warp 0 finishes the Arnoldi column (as
-// k_arnoldi_finish_warp, single pass) while the other warps write
-// V_{j+1} = W / beta and, for operators that pack their input, the FP16
-// rows of the next product (as k_hpack_scale): the column's serial FP64
-// chain and the normalisation's stream overlap.  A right-hand side that
-// this step finds converged is normalised all the same (its V_{j+1} lies
-// past its basis length); one that was already inactive writes nothing.
+// 32): CTA per (chunk of 1024 elements, right-hand side).  Every CTA forms
+// beta = ||w|| and the FP16 scale from the update's partials (the same sums
+// in the same order, so the same values) and writes its chunk of
+// V_{j+1} = W / beta and, for operators that pack their input, the FP16 rows
+// of the next product (as k_hpack_scale).  In the first chunk's CTA, warp 0
+// finishes the Arnoldi column (as k_arnoldi_finish_warp, single pass) while
+// the other warps pack: the column's serial FP64 chain overlaps the stream.
+// A right-hand side that this step finds converged is normalised all the
+// same (its V_{j+1} lies past its basis length); one that was already
+// inactive writes nothing.
+constexpr int FP_CHUNK = 1024;
+
 __global__ void __launch_bounds__(256) k_finish_pack(GmresDev s, int j, const double2* __restrict__ pnorm, int nblk,
                                                      const float2* __restrict__ W, int n, float2* __restrict__ Vout,
                                                      HPack pk)
 {
-    __shared__ double sbeta;
+    __shared__ float sbeta;
     __shared__ float nscale[2];
-    const int r = blockIdx.x, tid = threadIdx.x, lane = tid & 31;
+    const int r = blockIdx.y, chunk = blockIdx.x, tid = threadIdx.x, lane = tid & 31;
     if (!s.active[r]) {
-        if (tid == 0) s.scale[r] = 0.0;
+        if (chunk == 0 && tid == 0) s.scale[r] = 0.0;
         return;
     }
     if (tid == 0) {
-        double nr2 = 0.0, wm = 0.0;
+        // FP32 on one thread (FP64 would cost ~64 cycles an instruction here)
+        float nr2 = 0.f, wm = 0.f;
         for (int b = 0; b < nblk; ++b) {
-            nr2 += pnorm[(size_t)r * nblk + b].x;
-            wm = fmax(wm, pnorm[(size_t)r * nblk + b].y);
+            nr2 += (float)pnorm[(size_t)r * nblk + b].x;
+            wm = fmaxf(wm, (float)pnorm[(size_t)r * nblk + b].y);
         }
-        s.wmax[r] = wm;
-        const double beta = sqrt(nr2);
-        const double scale = beta > 0.0 ? 1.0 / beta : 0.0;
+        const float beta = sqrtf(nr2);
+        const float scale = beta > 0.f ? 1.f / beta : 0.f;
         sbeta = beta;
-        nscale[0] = (float)scale;
+        nscale[0] = scale;
         nscale[1] = 1.f;
+        int ex = 0;
         if (pk.bh) {
-            const int ex = hpack_exponent(wm, scale);
+            ex = hpack_exponent_f(wm, scale);
             nscale[1] = ldexpf(1.f, 14 - ex);
-            pk.inv_t[r] = ldexpf(1.f, ex - 14);
+        }
+        if (chunk == 0) {
+            s.wmax[r] = wm;
+            if (pk.bh) pk.inv_t[r] = ldexpf(1.f, ex - 14);
         }
     }
     __syncthreads();
-    if (tid < 32) {
+    const bool column = chunk == 0;
+    if (column && tid < 32) {
         const double2 h = lane <= j ? s.hcol[(size_t)lane * s.nrhs + r] : make_double2(0.0, 0.0);
-        arnoldi_column(s, r, j, h, sbeta);
+        arnoldi_column_f32(s, r, j, h, sbeta);
         return;
     }
     const float sc = nscale[0], t = nscale[1];
@@ -704,8 +787,9 @@ __global__ void __launch_bounds__(256) k_finish_pack(GmresDev s, int j, const do
     float2* v = Vout + (size_t)r * n;
     __half2* h0 = pk.bh ? reinterpret_cast<__half2*>(pk.bh + (size_t)(2 * r) * pk.ldh) : nullptr;
     __half2* h1 = pk.bh ? reinterpret_cast<__half2*>(pk.bh + (size_t)(2 * r + 1) * pk.ldh) : nullptr;
+    const int k1 = min(n, (chunk + 1) * FP_CHUNK), off = column ? 32 : 0;
 #pragma unroll 4
-    for (int k = tid - 32; k < n; k += blockDim.x - 32) {
+    for (int k = chunk * FP_CHUNK + tid - off; k < k1; k += blockDim.x - off) {
         const float2 x = w[k];
         const float2 y = make_float2(x.x * sc, x.y * sc);
         v[k] = y;
@@ -901,21 +985,21 @@ __global__ void __launch_bounds__(AS_THREADS, 2)
     cluster_arrive();
     cluster_wait();
     if (tid == 0) {
-        // one thread: FP64 square roots and divisions per thread would queue
-        // on the 1/64-rate FP64 pipe
+        // one thread, and FP32 for the root and the division (an FP64
+        // instruction costs ~64 cycles of GB300's FP64 pipe)
         double nr2 = 0.0, wm = 0.0;
         for (int c = 0; c < csize; ++c) {
             const double2 p = ld_cluster_d2(&npart, c);
             nr2 += p.x;
             wm = fmax(wm, p.y);
         }
-        const double beta = sqrt(nr2);
-        const double scale = beta > 0.0 ? 1.0 / beta : 0.0;
+        const float beta = sqrtf((float)nr2);
+        const float scale = beta > 0.f ? 1.f / beta : 0.f;
         ntot = make_double2(beta, wm);
-        nscale[0] = (float)scale;
+        nscale[0] = scale;
         nscale[1] = 1.f;
         if (pk.bh) {
-            const int ex = hpack_exponent(wm, scale);
+            const int ex = hpack_exponent_f((float)wm, scale);
             nscale[1] = ldexpf(1.f, 14 - ex);
             if (rank == 0) pk.inv_t[r] = ldexpf(1.f, ex - 14);
         }
@@ -941,7 +1025,7 @@ __global__ void __launch_bounds__(AS_THREADS, 2)
     // 5. the Arnoldi column
     if (rank == 0 && warp == 0) {
         if (lane == 0) s.wmax[r] = ntot.y;
-        arnoldi_column(s, r, j, lane <= j ? hs[lane] : make_double2(0.0, 0.0), ntot.x);
+        arnoldi_column_f32(s, r, j, lane <= j ? hs[lane] : make_double2(0.0, 0.0), (float)ntot.x);
     }
     cluster_wait();  // no CTA leaves while another may still read its shared memory
 }
@@ -1300,8 +1384,8 @@ static emfa_status_t gmres_t(Ctx* c, LinOp& A, const void* B, int nrhs, double2*
                 }
                 EMFA_CUDA(c, cudaMemsetAsync(s.counters, 0, sizeof(int), st));
                 if (finish_pack)
-                    k_finish_pack<<<nrhs, 256, 0, st>>>(s, j, pnorm, vblk, (const float2*)W, n,
-                                                        (float2*)(V + (size_t)(j + 1) * vec), pk);
+                    k_finish_pack<<<dim3((n + FP_CHUNK - 1) / FP_CHUNK, nrhs), 256, 0, st>>>(
+                        s, j, pnorm, vblk, (const float2*)W, n, (float2*)(V + (size_t)(j + 1) * vec), pk);
                 else if (m <= 32)
                     k_arnoldi_finish_warp<<<(nrhs * 32 + 127) / 128, 128, 0, st>>>(s, j, pnorm, vblk, two_pass ? 1 : 0);
                 else
