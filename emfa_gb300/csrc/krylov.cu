@@ -367,22 +367,28 @@ __global__ void __launch_bounds__(256) k_vupdate(const Cx<T>* __restrict__ V, si
     extern __shared__ unsigned char dyn_smem[];
     A* hs0 = reinterpret_cast<A*>(dyn_smem);
     A* hs1 = hs0 + nv;
-    __shared__ double red[8], redm[8];
+    __shared__ A red[8], redm[8];
     for (int i = threadIdx.x; i < nv; i += blockDim.x) {
-        double2 t;
+        // the block partials summed in the basis precision: FP32 sums for an
+        // FP32 basis (its coefficients are used in FP32; an FP64 addition
+        // costs ~64 cycles a warp instruction on GB300)
+        A tx, ty;
         if (partial) {
             const double2* p = partial + ((size_t)i * nrhs + r) * nblk;
-            t = make_double2(0.0, 0.0);
+            tx = 0;
+            ty = 0;
             for (int b = 0; b < nblk; ++b) {
-                t.x += p[b].x;
-                t.y += p[b].y;
+                tx += (A)p[b].x;
+                ty += (A)p[b].y;
             }
-            if (blk == 0) h[(size_t)i * nrhs + r] = t;
+            if (blk == 0) h[(size_t)i * nrhs + r] = make_double2((double)tx, (double)ty);
         } else {
-            t = h[(size_t)i * nrhs + r];
+            const double2 t = h[(size_t)i * nrhs + r];
+            tx = (A)t.x;
+            ty = (A)t.y;
         }
-        hs0[i] = (A)t.x;
-        hs1[i] = (A)t.y;
+        hs0[i] = tx;
+        hs1[i] = ty;
     }
     __syncthreads();
     A nr = 0, mx = 0;
@@ -426,17 +432,17 @@ __global__ void __launch_bounds__(256) k_vupdate(const Cx<T>* __restrict__ V, si
             mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
         }
         if ((threadIdx.x & 31) == 0) {
-            red[threadIdx.x >> 5] = (double)nr;
-            redm[threadIdx.x >> 5] = (double)mx;
+            red[threadIdx.x >> 5] = nr;
+            redm[threadIdx.x >> 5] = mx;
         }
         __syncthreads();
         if (threadIdx.x == 0) {
-            double t = 0, tm = 0;
+            A t = 0, tm = 0;
             for (int q = 0; q < (int)(blockDim.x >> 5); ++q) {
                 t += red[q];
                 tm = fmax(tm, redm[q]);
             }
-            pnorm[(size_t)r * nblk + blk] = make_double2(t, tm);
+            pnorm[(size_t)r * nblk + blk] = make_double2((double)t, (double)tm);
         }
     }
 }
@@ -1074,6 +1080,47 @@ __global__ void k_backsolve(GmresDev s)
     }
 }
 
+// The same for the FP32-basis inner solve (restarts up to 32): a warp per
+// right-hand side, lane q holding row q of the triangle (staged in shared
+// memory in FP32), column-oriented: y_i = b_i / H_ii on lane i, broadcast,
+// then every lane q < i takes b_q -= H_qi y_i.  FP32 like the basis; the
+// serial FP64 form spent ~60 us a launch on GB300's FP64 pipe.
+constexpr int BS_WARPS = 4;
+
+__global__ void __launch_bounds__(32 * BS_WARPS) k_backsolve_f32(GmresDev s)
+{
+    __shared__ float2 sh[BS_WARPS][32][33];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int r = blockIdx.x * BS_WARPS + w;
+    if (r >= s.nrhs) return;  // whole warps
+    const int m = s.m, jl = s.jlen[r];
+    const double2* H = s.H + (size_t)r * (m + 1) * m;
+    for (int i = 0; i < jl; ++i)
+        if (lane < jl) {
+            const double2 v = H[i * m + lane];
+            sh[w][i][lane] = make_float2((float)v.x, (float)v.y);
+        }
+    __syncwarp();
+    const double2 gl = lane < jl ? s.g[(size_t)r * (m + 1) + lane] : make_double2(0.0, 0.0);
+    float2 b = make_float2((float)gl.x, (float)gl.y), yl = make_float2(0.f, 0.f);
+    for (int i = jl - 1; i >= 0; --i) {
+        float2 yi = make_float2(0.f, 0.f);
+        if (lane == i) {
+            const float2 d = sh[w][i][i];
+            const float den = d.x * d.x + d.y * d.y;
+            if (den > 0.f) yi = make_float2((b.x * d.x + b.y * d.y) / den, (b.y * d.x - b.x * d.y) / den);
+            yl = yi;
+        }
+        yi = make_float2(__shfl_sync(0xffffffffu, yi.x, i), __shfl_sync(0xffffffffu, yi.y, i));
+        if (lane < i) {
+            const float2 h = sh[w][lane][i];
+            b.x -= h.x * yi.x - h.y * yi.y;
+            b.y -= h.x * yi.y + h.y * yi.x;
+        }
+    }
+    if (lane < m) s.y[(size_t)lane * s.nrhs + r] = make_double2((double)yl.x, (double)yl.y);
+}
+
 // X[r][k] += sum_{i < jlen[r]} y[i][r] V_i[r][k]
 template <typename T>
 __global__ void k_update_x(const Cx<T>* __restrict__ V, size_t vstride, int nvmax, const double2* __restrict__ y,
@@ -1414,7 +1461,10 @@ static emfa_status_t gmres_t(Ctx* c, LinOp& A, const void* B, int nrhs, double2*
         }
         total_iters += steps;
         EMFA_TRY(A.check(c, st));
-        k_backsolve<<<(nrhs * 32 + 127) / 128, 128, 0, st>>>(s);
+        if (std::is_same<T, float>::value && m <= 32)
+            k_backsolve_f32<<<(nrhs + BS_WARPS - 1) / BS_WARPS, 32 * BS_WARPS, 0, st>>>(s);
+        else
+            k_backsolve<<<(nrhs * 32 + 127) / 128, 128, 0, st>>>(s);
         k_update_x2<T><<<dim3((n + 255) / 256, nrhs), 256, 2 * std::max(1, steps) * sizeof(typename Acc<T>::type), st>>>(
             V, vec, steps, s.y, s.jlen, X, n, nrhs);
         c->kernel_launches += 2;
