@@ -142,6 +142,31 @@ inline emfa_status_t ensure_smem(Ctx* c, F* func, size_t bytes)
     return ensure_smem_raw(c, reinterpret_cast<const void*>(func), bytes);
 }
 
+// Programmatic dependent launch: a kernel launched with
+// cudaLaunchAttributeProgrammaticStreamSerialization may be scheduled once
+// every CTA of its predecessor has called griddep_launch (or exited), and
+// waits in griddep_wait until the predecessor has finished and its writes are
+// visible.  Both are no-ops for kernels launched without the attribute.
+__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void griddep_launch() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_dependent(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                                    Args... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 // Brackets one kernel launch with events on its stream when the context's
 // kernel timing is on; does nothing otherwise.
 class TimedLaunch {

@@ -69,6 +69,9 @@ __global__ void __launch_bounds__(THREADS, 1)
 {
     using S = Smem<BN, MS>;
     using namespace tc;
+    // one wave: every CTA is resident, so the next launch (the Gram-Schmidt
+    // coefficients) may be scheduled beside it at once and wait for its end
+    griddep_launch();
     extern __shared__ uint8_t smem_raw[];
     uint8_t* base = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint8_t* sA = base;                               // [stage][row block]

@@ -300,13 +300,18 @@ __global__ void __launch_bounds__(KB) k_norm2(const double2* __restrict__ X, int
 // ---------------------------------------------------------------------------
 constexpr int VCHUNK = 1024;
 
+// reset (optional): an int zeroed by the first CTA, after the predecessor
+// (the step's product) has finished: the step's count of active right-hand
+// sides, so that no memset sits between the step's launches.
 template <typename T>
 __global__ void __launch_bounds__(256) k_vdots(const Cx<T>* __restrict__ V, size_t vstride, int nv,
                                                const Cx<T>* __restrict__ W, int n, int nrhs, int nblk,
-                                               double2* __restrict__ partial)
+                                               double2* __restrict__ partial, int* __restrict__ reset)
 {
     using A = typename Acc<T>::type;
     const int blk = blockIdx.x, r = blockIdx.y;
+    griddep_wait();
+    if (reset && blk == 0 && r == 0 && threadIdx.x == 0) *reset = 0;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const size_t base = (size_t)r * n;
     const int k0 = blk * VCHUNK, k1 = min(n, k0 + VCHUNK);
@@ -347,6 +352,7 @@ __global__ void __launch_bounds__(256) k_vdots(const Cx<T>* __restrict__ V, size
             if (two) partial[((size_t)(i + 8) * nrhs + r) * nblk + blk] = make_double2((double)re2, (double)im2);
         }
     }
+    griddep_launch();
 }
 
 // With `partial` (the block partials of k_vdots) the coefficients are summed
@@ -362,6 +368,7 @@ __global__ void __launch_bounds__(256) k_vupdate(const Cx<T>* __restrict__ V, si
 {
     using A = typename Acc<T>::type;
     const int blk = blockIdx.x, r = nrhs - 1 - (int)blockIdx.y;
+    griddep_wait();
     const size_t base = (size_t)r * n;
     // coefficients (dynamic shared memory: 2 nv values, any restart length)
     extern __shared__ unsigned char dyn_smem[];
@@ -445,6 +452,7 @@ __global__ void __launch_bounds__(256) k_vupdate(const Cx<T>* __restrict__ V, si
             pnorm[(size_t)r * nblk + blk] = make_double2((double)t, (double)tm);
         }
     }
+    griddep_launch();
 }
 
 // X[r][k] += sum_i y_i V_i[r][k]; the sum in the basis precision, added to
@@ -755,6 +763,7 @@ __global__ void __launch_bounds__(256) k_finish_pack(GmresDev s, int j, const do
     __shared__ float sbeta;
     __shared__ float nscale[2];
     const int r = blockIdx.y, chunk = blockIdx.x, tid = threadIdx.x, lane = tid & 31;
+    griddep_wait();
     if (!s.active[r]) {
         if (chunk == 0 && tid == 0) s.scale[r] = 0.0;
         return;
@@ -1420,24 +1429,35 @@ static emfa_status_t gmres_t(Ctx* c, LinOp& A, const void* B, int nrhs, double2*
                 // the updates sum the dots' block partials themselves (block 0
                 // keeps the coefficients in s.hcol / s.y for the Arnoldi finish)
                 const size_t hsm = 2 * nv * sizeof(typename Acc<T>::type);
-                k_vdots<T><<<vg, 256, 0, st>>>(V, vec, nv, W, n, nrhs, vblk, partial);
+                if (finish_pack) {
+                    // product -> coefficients -> update -> finish: each launch may
+                    // be resident before its predecessor ends (griddep_wait); the
+                    // coefficients pass zeroes the step's active count
+                    EMFA_CUDA(c, launch_dependent(k_vdots<T>, vg, dim3(256), 0, st, (const Cx<T>*)V, vec, nv,
+                                                  (const Cx<T>*)W, n, nrhs, vblk, partial, s.counters));
+                    EMFA_CUDA(c, launch_dependent(k_vupdate<T, true>, vg, dim3(256), hsm, st, (const Cx<T>*)V, vec, nv,
+                                                  s.hcol, (const double2*)partial, W, n, nrhs, vblk, pnorm));
+                    EMFA_CUDA(c, launch_dependent(k_finish_pack, dim3((n + FP_CHUNK - 1) / FP_CHUNK, nrhs), dim3(256),
+                                                  0, st, s, j, (const double2*)pnorm, vblk, (const float2*)W, n,
+                                                  (float2*)(V + (size_t)(j + 1) * vec), pk));
+                    c->kernel_launches += 3;
+                } else {
+                k_vdots<T><<<vg, 256, 0, st>>>(V, vec, nv, W, n, nrhs, vblk, partial, nullptr);
                 if (two_pass) {
                     k_vupdate<T, false><<<vg, 256, hsm, st>>>(V, vec, nv, s.hcol, partial, W, n, nrhs, vblk, pnorm);
-                    k_vdots<T><<<vg, 256, 0, st>>>(V, vec, nv, W, n, nrhs, vblk, partial);
+                    k_vdots<T><<<vg, 256, 0, st>>>(V, vec, nv, W, n, nrhs, vblk, partial, nullptr);
                     k_vupdate<T, true><<<vg, 256, hsm, st>>>(V, vec, nv, s.y, partial, W, n, nrhs, vblk, pnorm);
                     c->kernel_launches += 2;
                 } else {
                     k_vupdate<T, true><<<vg, 256, hsm, st>>>(V, vec, nv, s.hcol, partial, W, n, nrhs, vblk, pnorm);
                 }
                 EMFA_CUDA(c, cudaMemsetAsync(s.counters, 0, sizeof(int), st));
-                if (finish_pack)
-                    k_finish_pack<<<dim3((n + FP_CHUNK - 1) / FP_CHUNK, nrhs), 256, 0, st>>>(
-                        s, j, pnorm, vblk, (const float2*)W, n, (float2*)(V + (size_t)(j + 1) * vec), pk);
-                else if (m <= 32)
+                if (m <= 32)
                     k_arnoldi_finish_warp<<<(nrhs * 32 + 127) / 128, 128, 0, st>>>(s, j, pnorm, vblk, two_pass ? 1 : 0);
                 else
                     k_arnoldi_finish<<<(nrhs * 32 + 127) / 128, 128, 0, st>>>(s, j, pnorm, vblk, two_pass ? 1 : 0);
                 c->kernel_launches += 3;
+                }
             }
             EMFA_CUDA(c, cudaMemcpyAsync((void*)(slot + (j & 1)), s.counters, sizeof(int), cudaMemcpyDeviceToHost, st));
             EMFA_CUDA(c, cudaEventRecord(sev.e[j & 1], st));
