@@ -218,6 +218,7 @@ def run_emfa(args, workload):
                                       "d2h_bytes_per_step": int(d2h), "ms": statistics.median(e2e_ms)},
         "clocks": clocks.summary(), "n": n, "n_inc": n_inc, "acc": acc, "plain": plain, "world": world,
         "rank": rank, "kernels": kernels, "n_tri": int(m.tris.shape[0]),
+        "autotune": api.autotune_query(local, n, n_inc),
     }
 
 
@@ -761,6 +762,10 @@ def main():
         "roofline": roofline(res),
         "fill_roofline": fill_roofline(res),
         "kernels": kernel_table(res),
+        # the inner product's tile shape (columns x rows) the autotuner chose in
+        # the warm-up, with each candidate's best time (ms)
+        "autotune": {"shape": res["autotune"][0],
+                     "candidates_ms": {k: round(v, 4) for k, v in res["autotune"][1].items()}},
     }
     if world == 1 and args.secondary:
         for name, fn in (("c1", run_c1), ("mlfma", run_mlfma), ("batch", run_batch), ("serve", run_serve)):

@@ -89,6 +89,8 @@ _SIGS = {
     "emfa_ctx_destroy": (ci, [vp]),
     "emfa_ctx_memory": (ci, [vp, ctypes.POINTER(sz), ctypes.POINTER(sz), ctypes.POINTER(sz)]),
     "emfa_ctx_launch_count": (ci, [vp, ctypes.POINTER(ctypes.c_int64)]),
+    "emfa_autotune_query": (ci, [ci, ci, ci, ip, ctypes.POINTER(ctypes.c_float)]),
+    "emfa_autotune_clear": (ci, []),
     "emfa_ctx_synchronize": (ci, [vp]),
     "emfa_ctx_stream": (ci, [vp, ctypes.POINTER(vp)]),
     "emfa_device_alloc": (ci, [vp, sz, ctypes.POINTER(vp)]),

@@ -185,6 +185,24 @@ def matvec(ctx: Context, Z, X, matvec="auto"):
     return Y
 
 
+TILE_SHAPES = ("64x128", "64x256", "144x128", "144x256")
+
+
+def autotune_query(device: int, n: int, n_rhs: int):
+    """The inner product's tuned tile shape for (n, n_rhs) on a device:
+    (shape name or None if not tuned yet, {shape: best ms} of the timed
+    candidates)."""
+    v = ctypes.c_int()
+    ms = (ctypes.c_float * 4)()
+    L.check(L.lib().emfa_autotune_query(device, n, n_rhs, ctypes.byref(v), ms))
+    times = {TILE_SHAPES[i]: ms[i] for i in range(4) if ms[i] >= 0}
+    return (TILE_SHAPES[v.value] if v.value >= 0 else None), times
+
+
+def autotune_clear():
+    L.check(L.lib().emfa_autotune_clear())
+
+
 def residual(ctx: Context, Z, X, B, matvec="auto"):
     """R = B - Z X (complex128) with the refinement residual of a matvec mode;
     X complex128, B in Z's precision."""

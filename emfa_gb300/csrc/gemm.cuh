@@ -83,6 +83,12 @@ __device__ __forceinline__ int hpack_exponent_f(float wmax, float scale)
 emfa_status_t hgemm_residual(Ctx* c, const HPlanes& h, const double2* X, const void* B, bool b_is_f32, double2* R,
                              int nrhs, cudaStream_t st);
 emfa_status_t hgemm_check_error(Ctx* c, cudaStream_t st);
+// the inner product's tile shapes (BN x MS) and the autotuner's record of a
+// shape bucket: variant -1 if untuned; ms[v] the best of two timed launches
+// of shape v, -1 where v was not a candidate
+enum { HV_64_1 = 0, HV_64_2, HV_144_1, HV_144_2, HV_COUNT };
+emfa_status_t hgemm_tuned_shape(int device, int n, int nrhs, int* variant, float* ms);
+void hgemm_tune_clear();
 
 // Linear operator driven by the batched Krylov solvers (krylov.cu): the
 // dense impedance matrix or the MLFMA operator.

@@ -36,6 +36,9 @@
 
 #include <algorithm>
 #include <atomic>
+#include <cstdlib>
+#include <map>
+#include <mutex>
 
 namespace emfa {
 
@@ -603,14 +606,16 @@ static emfa_status_t make_map_h(Ctx* c, CUtensorMap* m, const void* ptr, uint64_
 
 template <int BN, int MS>
 static emfa_status_t launch_h(Ctx* c, const CUtensorMap& ta, const CUtensorMap& tb, float2* Y, int n, int nrhs,
-                              const float* inv_s, const float* inv_t, int* err, cudaStream_t st)
+                              const float* inv_s, const float* inv_t, int* err, cudaStream_t st, bool timed = true)
 {
     using S = th::Smem<BN, MS>;
     EMFA_TRY(ensure_smem(c, th::k_hgemm<BN, MS>, S::TOTAL));
     dim3 grd((2 * nrhs + BN - 1) / BN, (n + th::BM * MS - 1) / (th::BM * MS));
     const int kblocks = (2 * n + th::BKH - 1) / th::BKH;
-    {
+    if (timed) {
         TimedLaunch tl(c, KT_GEMM, st, 8.0 * n * (double)n * nrhs);
+        th::k_hgemm<BN, MS><<<grd, th::THREADS, S::TOTAL, st>>>(ta, tb, Y, n, nrhs, kblocks, inv_s, inv_t, err);
+    } else {
         th::k_hgemm<BN, MS><<<grd, th::THREADS, S::TOTAL, st>>>(ta, tb, Y, n, nrhs, kblocks, inv_s, inv_t, err);
     }
     c->kernel_launches += 1;
@@ -655,24 +660,150 @@ emfa_status_t hsplit_prepare(Ctx* c, const void* Z, size_t ldz, int n, HPlanes* 
     return EMFA_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Tile-shape autotuner of the inner product.  Shapes (BN columns, MS row
+// blocks of 128): 64 x 1, 64 x 2, 144 x 1, 144 x 2.  The first product of a
+// shape bucket (device, ceil(N / 256), ceil(2 n_rhs / 16)) in the process
+// times every candidate twice with CUDA events on the caller's stream and
+// keeps the fastest; later products of the bucket launch it directly.  Every
+// shape accumulates each output over K in the same order, so the choice
+// never changes the result.  EMFA_AUTOTUNE=0 in the environment keeps the
+// fixed rule (the 256-row, 144-column tiles once they fill the SMs).
+// ---------------------------------------------------------------------------
+namespace {
+struct TuneKey {
+    int dev, rows, cols;
+    bool operator<(const TuneKey& o) const
+    {
+        return dev != o.dev ? dev < o.dev : rows != o.rows ? rows < o.rows : cols < o.cols;
+    }
+};
+struct TuneEntry {
+    int variant = -1;
+    float ms[HV_COUNT] = {-1.f, -1.f, -1.f, -1.f};
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, TuneEntry> g_tune;
+
+bool autotune_enabled()
+{
+    static const bool on = [] {
+        const char* e = getenv("EMFA_AUTOTUNE");
+        return !(e && e[0] == '0');
+    }();
+    return on;
+}
+}  // namespace
+
+static int fixed_variant(int n, int nrhs, int sms)
+{
+    if (2 * nrhs <= 64) return HV_64_1;
+    const int col_tiles = (2 * nrhs + 143) / 144;
+    return (long)col_tiles * ((n + 255) / 256) >= (long)sms * 9 / 10 ? HV_144_2 : HV_144_1;
+}
+
+static emfa_status_t launch_variant(Ctx* c, int v, const CUtensorMap& ta, const CUtensorMap* tb, float2* Y, int n,
+                                    int nrhs, const float* inv_s, const float* inv_t, int* err, cudaStream_t st,
+                                    bool timed)
+{
+    switch (v) {
+    case HV_64_1: return launch_h<64, 1>(c, ta, tb[0], Y, n, nrhs, inv_s, inv_t, err, st, timed);
+    case HV_64_2: return launch_h<64, 2>(c, ta, tb[0], Y, n, nrhs, inv_s, inv_t, err, st, timed);
+    case HV_144_1: return launch_h<144, 1>(c, ta, tb[1], Y, n, nrhs, inv_s, inv_t, err, st, timed);
+    default: return launch_h<144, 2>(c, ta, tb[1], Y, n, nrhs, inv_s, inv_t, err, st, timed);
+    }
+}
+
+// times the candidates (two launches each, the faster kept) and records the
+// choice; the last launch leaves the product in Y
+static emfa_status_t tune_variants(Ctx* c, const TuneKey& key, const CUtensorMap& ta, const CUtensorMap* tb, float2* Y,
+                                   int n, int nrhs, const float* inv_s, const float* inv_t, int* err, cudaStream_t st)
+{
+    TuneEntry e;
+    int cand[HV_COUNT], nc = 0;
+    cand[nc++] = HV_64_1;
+    if (n > 128) cand[nc++] = HV_64_2;
+    if (2 * nrhs > 64) {
+        cand[nc++] = HV_144_1;
+        if (n > 128) cand[nc++] = HV_144_2;
+    }
+    cudaEvent_t ev[2];
+    EMFA_CUDA(c, cudaEventCreate(&ev[0]));
+    EMFA_CUDA(c, cudaEventCreate(&ev[1]));
+    emfa_status_t st_ = EMFA_OK;
+    for (int i = 0; i < nc && st_ == EMFA_OK; ++i) {
+        float best = 1e30f;
+        for (int rep = 0; rep < 2 && st_ == EMFA_OK; ++rep) {
+            cudaEventRecord(ev[0], st);
+            st_ = launch_variant(c, cand[i], ta, tb, Y, n, nrhs, inv_s, inv_t, err, st, false);
+            cudaEventRecord(ev[1], st);
+            if (st_ != EMFA_OK) break;
+            if (cudaEventSynchronize(ev[1]) != cudaSuccess) {
+                st_ = EMFA_ERR_CUDA;
+                break;
+            }
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, ev[0], ev[1]);
+            best = std::min(best, ms);
+        }
+        e.ms[cand[i]] = best;
+        if (e.variant < 0 || best < e.ms[e.variant]) e.variant = cand[i];
+    }
+    cudaEventDestroy(ev[0]);
+    cudaEventDestroy(ev[1]);
+    EMFA_TRY(st_);
+    {
+        std::lock_guard<std::mutex> g(g_tune_mu);
+        g_tune[key] = e;
+    }
+    // the result of the last candidate is in Y; the chosen one gives the same bits
+    return EMFA_OK;
+}
+
 // the inner-product GEMM on an already packed B plane
 static emfa_status_t hgemm_run(Ctx* c, const HPlanes& h, const __half* bh, const float* inv_t, void* Y, int nrhs,
                                int* err, cudaStream_t st)
 {
     const int n = h.n;
     const size_t ldh = h.ldh;
-    CUtensorMap ta, tb;
-    // 256-row tiles (two M = 128 blocks sharing each B tile) once there are
-    // enough of them to fill the SMs; 144 columns = 72 right-hand sides
+    CUtensorMap ta, tb[2];  // tb[0]: 64-column boxes, tb[1]: 144-column boxes
     const int sms = c->sm_count > 0 ? c->sm_count : 148;
-    const int BN = 2 * nrhs <= 64 ? 64 : 144;
-    const int col_tiles = (2 * nrhs + BN - 1) / BN;
-    const bool tall = BN == 144 && (long)col_tiles * ((n + 255) / 256) >= (long)sms * 9 / 10;
     EMFA_TRY(make_map_h(c, &ta, h.zh, 2 * (uint64_t)n, (uint64_t)n, ldh, th::BM));
-    EMFA_TRY(make_map_h(c, &tb, bh, 2 * (uint64_t)n, 2 * (uint64_t)nrhs, ldh, BN));
-    if (BN == 64) return launch_h<64, 1>(c, ta, tb, (float2*)Y, n, nrhs, h.inv_s, inv_t, err, st);
-    if (tall) return launch_h<144, 2>(c, ta, tb, (float2*)Y, n, nrhs, h.inv_s, inv_t, err, st);
-    return launch_h<144, 1>(c, ta, tb, (float2*)Y, n, nrhs, h.inv_s, inv_t, err, st);
+    EMFA_TRY(make_map_h(c, &tb[0], bh, 2 * (uint64_t)n, 2 * (uint64_t)nrhs, ldh, 64));
+    if (2 * nrhs > 64) EMFA_TRY(make_map_h(c, &tb[1], bh, 2 * (uint64_t)n, 2 * (uint64_t)nrhs, ldh, 144));
+    int v = fixed_variant(n, nrhs, sms);
+    if (autotune_enabled()) {
+        const TuneKey key{c->device, (n + 255) / 256, (2 * nrhs + 15) / 16};
+        int known = -1;
+        {
+            std::lock_guard<std::mutex> g(g_tune_mu);
+            auto it = g_tune.find(key);
+            if (it != g_tune.end()) known = it->second.variant;
+        }
+        if (known < 0) return tune_variants(c, key, ta, tb, (float2*)Y, n, nrhs, h.inv_s, inv_t, err, st);
+        v = known;
+    }
+    return launch_variant(c, v, ta, tb, (float2*)Y, n, nrhs, h.inv_s, inv_t, err, st, true);
+}
+
+emfa_status_t hgemm_tuned_shape(int device, int n, int nrhs, int* variant, float* ms)
+{
+    std::lock_guard<std::mutex> g(g_tune_mu);
+    auto it = g_tune.find(TuneKey{device, (n + 255) / 256, (2 * nrhs + 15) / 16});
+    if (it == g_tune.end()) {
+        *variant = -1;
+        for (int i = 0; i < HV_COUNT; ++i) ms[i] = -1.f;
+        return EMFA_OK;
+    }
+    *variant = it->second.variant;
+    for (int i = 0; i < HV_COUNT; ++i) ms[i] = it->second.ms[i];
+    return EMFA_OK;
+}
+
+void hgemm_tune_clear()
+{
+    std::lock_guard<std::mutex> g(g_tune_mu);
+    g_tune.clear();
 }
 
 static emfa_status_t hgemm_bplane(Ctx* c, const HPlanes& h, int nrhs, __half** bh, float** inv_t)

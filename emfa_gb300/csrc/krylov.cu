@@ -2032,6 +2032,21 @@ using namespace emfa;
 
 extern "C" {
 
+emfa_status_t emfa_autotune_query(int device, int n, int n_rhs, int* shape, float* ms)
+{
+    if (!shape || !ms || n <= 0 || n_rhs <= 0) {
+        set_global_error("emfa_autotune_query: null output or non-positive size");
+        return EMFA_ERR_INVALID;
+    }
+    return hgemm_tuned_shape(device, n, n_rhs, shape, ms);
+}
+
+emfa_status_t emfa_autotune_clear(void)
+{
+    hgemm_tune_clear();
+    return EMFA_OK;
+}
+
 emfa_status_t emfa_matvec(emfa_ctx_t* ctx, int prec, int matvec, const void* Z_dev, int n, const void* X_dev, int n_rhs,
                           void* Y_dev, void* stream)
 {

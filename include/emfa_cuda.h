@@ -202,6 +202,20 @@ emfa_status_t emfa_fill_v(emfa_ctx_t* ctx, emfa_geom_t* geom, const emfa_fill_pa
 emfa_status_t emfa_matvec(emfa_ctx_t* ctx, int prec, int matvec, const void* Z_dev, int n, const void* X_dev,
                           int n_rhs, void* Y_dev, void* stream);
 
+/* Tile-shape autotuner of the split-FP16 inner product (EMFA_MV_F16X, the
+ * mixed dense solver's products).  The first product of a shape bucket
+ * (device, ceil(n / 256), ceil(2 n_rhs / 16)) in the process times each
+ * candidate tile shape twice with CUDA events on the caller's stream and keeps
+ * the fastest for the bucket; every shape gives the same bits.  Shapes:
+ * 0 = 64 columns x 128 rows, 1 = 64 x 256, 2 = 144 x 128, 3 = 144 x 256.
+ * emfa_autotune_query gives the bucket's choice (-1: not tuned yet) and, in
+ * ms[4], the best time of each shape (-1: not a candidate).
+ * emfa_autotune_clear forgets every choice.  EMFA_AUTOTUNE=0 in the
+ * environment keeps the fixed rule instead (256 x 144 tiles once they fill the
+ * SMs).  No counterpart in the reference. */
+emfa_status_t emfa_autotune_query(int device, int n, int n_rhs, int* shape, float* ms);
+emfa_status_t emfa_autotune_clear(void);
+
 /* Largest n * n_rhs accepted by emfa_matvec_tf32_noalloc (16 MiB of scratch). */
 #define EMFA_NOALLOC_MAX_ELEMS 1048576u
 

@@ -115,8 +115,13 @@ def test_auto_choice_by_grid_size(ctx):
     """Tens of right-hand sides take the fused step (one launch a step);
     hundreds at N = 7680 (clusters of 8: more than four CTAs an SM) take the
     separate passes (coefficients, update, column, normalisation: four)."""
+    from emfa_gb300 import api
     Z, B = _system(7680, 400, seed=11)
     few = B[:16].contiguous()
+    # the first product of a shape times the tile-shape candidates (more
+    # launches): tune both shapes before counting
+    api.matvec(ctx, Z, few, "f16x")
+    api.matvec(ctx, Z, B, "f16x")
     n_auto, i_auto = _launches(ctx, Z, few, "cgs1")
     n_split, i_split = _launches(ctx, Z, few, "cgs1_split")
     assert i_auto.iterations == i_split.iterations
