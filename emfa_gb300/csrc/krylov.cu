@@ -400,34 +400,51 @@ __global__ void __launch_bounds__(256) k_vupdate(const Cx<T>* __restrict__ V, si
     __syncthreads();
     A nr = 0, mx = 0;
     const int k0 = blk * VCHUNK, k1 = min(n, k0 + VCHUNK);
-    for (int k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
-        const Cx<T>* vk = V + base + k;
-        A sr = 0, si = 0;
-        int i = 0;
-        for (; i + 8 <= nv; i += 8) {
-            Cx<T> v[8];
+    // a thread's VCHUNK / 256 = 4 elements together, 4 basis vectors a pass:
+    // 16 independent loads in flight at clamped in-bounds addresses (a
+    // vector past the basis counts with coefficient 0), so no tail of nv
+    // loads one vector at a time
+    constexpr int EL = VCHUNK / 256, VG = 4;
+    int kc[EL];
+    Cx<T> w[EL];
 #pragma unroll
-            for (int u = 0; u < 8; ++u) v[u] = vk[(size_t)(i + u) * vstride];
+    for (int e = 0; e < EL; ++e) {
+        kc[e] = min(k0 + (int)threadIdx.x + 256 * e, k1 - 1);
+        w[e] = W[base + kc[e]];
+    }
+    A sr[EL], si[EL];
 #pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                const A hr = hs0[i + u], hi = hs1[i + u];
-                sr += hr * (A)v[u].re - hi * (A)v[u].im;
-                si += hr * (A)v[u].im + hi * (A)v[u].re;
+    for (int e = 0; e < EL; ++e) sr[e] = si[e] = 0;
+    const Cx<T>* vb = V + base;
+    for (int i = 0; i < nv; i += VG) {
+        Cx<T> v[VG][EL];
+#pragma unroll
+        for (int u = 0; u < VG; ++u) {
+            const Cx<T>* vi = vb + (size_t)min(i + u, nv - 1) * vstride;
+#pragma unroll
+            for (int e = 0; e < EL; ++e) v[u][e] = vi[kc[e]];
+        }
+#pragma unroll
+        for (int u = 0; u < VG; ++u) {
+            const bool ok = i + u < nv;
+            const A hr = ok ? hs0[i + u] : (A)0, hi = ok ? hs1[i + u] : (A)0;
+#pragma unroll
+            for (int e = 0; e < EL; ++e) {
+                sr[e] += hr * (A)v[u][e].re - hi * (A)v[u][e].im;
+                si[e] += hr * (A)v[u][e].im + hi * (A)v[u][e].re;
             }
         }
-        for (; i < nv; ++i) {
-            const Cx<T> v = vk[(size_t)i * vstride];
-            const A hr = hs0[i], hi = hs1[i];
-            sr += hr * (A)v.re - hi * (A)v.im;
-            si += hr * (A)v.im + hi * (A)v.re;
-        }
-        Cx<T> w = W[base + k];
-        w.re = (T)((A)w.re - sr);
-        w.im = (T)((A)w.im - si);
-        W[base + k] = w;
+    }
+#pragma unroll
+    for (int e = 0; e < EL; ++e) {
+        const int k = k0 + (int)threadIdx.x + 256 * e;
+        if (k >= k1) continue;
+        w[e].re = (T)((A)w[e].re - sr[e]);
+        w[e].im = (T)((A)w[e].im - si[e]);
+        W[base + k] = w[e];
         if (NORM) {
-            nr += (A)w.re * (A)w.re + (A)w.im * (A)w.im;
-            mx = fmax(mx, fmax(fabs((A)w.re), fabs((A)w.im)));
+            nr += (A)w[e].re * (A)w[e].re + (A)w[e].im * (A)w[e].im;
+            mx = fmax(mx, fmax(fabs((A)w[e].re), fabs((A)w[e].im)));
         }
     }
     if (NORM) {
