@@ -374,8 +374,10 @@ __device__ __forceinline__ float2 fsub2_rn(float2 a, float2 b)
 // B - sum / (s t) in FP64.  A drain releases the accumulator as soon as its
 // 56 columns are in registers, before the sums.
 // ---------------------------------------------------------------------------
-constexpr int RBN = 112;  // 56 columns per epilogue warp: the sums fit the 168 registers of a 10-warp block
-constexpr int RTHREADS = 320;  // producer, MMA, 8 epilogue warps
+constexpr int RBN = 112;
+constexpr int REPI = 16;                   // epilogue warps: four per SM sub-partition
+constexpr int RCOLS = RBN * 4 / REPI;      // 28 accumulator columns per epilogue warp
+constexpr int RTHREADS = 32 * (2 + REPI);  // producer, MMA, epilogue
 
 struct RSmem {
     static constexpr int A_BYTES = BM * 128;
@@ -416,7 +418,7 @@ __global__ void __launch_bounds__(RTHREADS, 1)
         }
         for (int a = 0; a < 2; ++a) {
             mbar_init(acc_full + a, 1);
-            mbar_init(acc_empty + a, 8);  // one arrival per epilogue warp
+            mbar_init(acc_empty + a, REPI);  // one arrival per epilogue warp
         }
         mbar_init(done, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -481,23 +483,24 @@ __global__ void __launch_bounds__(RTHREADS, 1)
         }
         __syncwarp();
     } else {
-        // epilogue warps 2..9: lane quadrant warp % 4, column half (warp - 2) / 4
-        const int q = warp & 3, h = (warp - 2) >> 2;
+        // epilogue warps 2..17: lane quadrant warp % 4, column quarter (warp - 2) / 4
+        constexpr int CP = RCOLS / 2;  // column pairs (right-hand sides) per thread
+        const int q = warp & 3, grp = (warp - 2) >> 2;
         const int f = f0 + 32 * q + lane;
-        const int col0 = 56 * h;
+        const int col0 = RCOLS * grp;
         // Kahan sums: sum - cmp is the running total.  cmp stays below half an
-        // ulp of sum, so bf16 holds it to 2^-32 of the total (84 registers for
-        // 56 columns instead of 112).  The accumulator's 56 columns come in
-        // one round trip (tmem_ld56: three loads, one wait), the accumulator
-        // is released as soon as they are in registers, and the sums run on
-        // column pairs (f32x2: two additions an instruction).  The drain is
-        // issue-bound: it sets the kernel's pace (0.81 ms with seven round
-        // trips and scalar sums, 0.62 ms so).  FP32 compensation (two
-        // instructions a column) spills at the 168 registers ten warps leave.
-        float2 sum[28];  // columns 2i, 2i + 1
-        __nv_bfloat162 cmp[28];
+        // ulp of sum, so bf16 holds it to 2^-32 of the total.  The drain is
+        // issue-bound and sets the kernel's pace: a k-block's 28 columns come
+        // in one tensor-memory round trip (tmem_ld28), the accumulator is
+        // released as soon as they are in registers, the sums run on column
+        // pairs (f32x2: two additions an instruction), and sixteen warps (four
+        // per SM sub-partition) share the work to hide the latencies
+        // (0.81 ms a launch with eight warps, seven round trips and scalar
+        // sums; 0.62 ms with eight warps and the rest).
+        float2 sum[CP];  // columns 2i, 2i + 1
+        __nv_bfloat162 cmp[CP];
 #pragma unroll
-        for (int i = 0; i < 28; ++i) {
+        for (int i = 0; i < CP; ++i) {
             sum[i] = make_float2(0.f, 0.f);
             cmp[i] = __floats2bfloat162_rn(0.f, 0.f);
         }
@@ -512,13 +515,13 @@ __global__ void __launch_bounds__(RTHREADS, 1)
                 break;
             }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            float v[56];
-            tmem_ld56(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(a * S::ACC + col0), v);
+            float v[RCOLS];
+            tmem_ld28(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(a * S::ACC + col0), v);
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
             __syncwarp();
             if (lane == 0) mbar_arrive(acc_empty + a);
 #pragma unroll
-            for (int i = 0; i < 28; ++i) {
+            for (int i = 0; i < CP; ++i) {
                 const float2 y = fsub2_rn(make_float2(v[2 * i], v[2 * i + 1]), __bfloat1622float2(cmp[i]));
                 const float2 t = fadd2_rn(sum[i], y);
                 const float2 cn = fsub2_rn(fsub2_rn(t, sum[i]), y);
@@ -526,36 +529,31 @@ __global__ void __launch_bounds__(RTHREADS, 1)
                 sum[i] = t;
             }
         }
-        if (ok) {
-            // the stage ring is idle once the last accumulator was drained: park
-            // the sums there and form the outputs one at a time
-            float* park = reinterpret_cast<float*>(base) + (size_t)((warp - 2) * 32 + lane) * 112;
+        if (ok && f < M) {
+            // R = B - (sum - cmp) sc.  sc = (1 / s)(1 / t_r) is a power of two,
+            // so sum sc and cmp sc are exact: for an FP32 B, R = (B - sum sc)
+            // + cmp sc is two FMAs rounded once each (FP64 would queue on
+            // GB300's 1/64-rate pipe for every output)
+            const float is = *inv_s;
+            // unrolled: static indices keep sum and cmp in registers
 #pragma unroll
-            for (int i = 0; i < 28; ++i) {
+            for (int i = 0; i < CP; ++i) {
+                const int r = (c0 + col0) / 2 + i;
+                if (r >= R) continue;
                 const float2 cf = __bfloat1622float2(cmp[i]);
-                park[4 * i] = sum[i].x;
-                park[4 * i + 1] = cf.x;
-                park[4 * i + 2] = sum[i].y;
-                park[4 * i + 3] = cf.y;
-            }
-            if (f < M) {
-                const double is = (double)*inv_s;
-#pragma unroll 1
-                for (int i = 0; i < 28; ++i) {
-                    const int r = (c0 + col0) / 2 + i;
-                    if (r >= R) break;
-                    const double sc = is * (double)inv_t[r];
-                    const double re = ((double)park[4 * i] - (double)park[4 * i + 1]) * sc;
-                    const double im = ((double)park[4 * i + 2] - (double)park[4 * i + 3]) * sc;
-                    const size_t o = (size_t)r * M + f;
-                    double2 b;
-                    if (b_f64) {
-                        b = reinterpret_cast<const double2*>(Bv)[o];
-                    } else {
-                        const float2 bf = reinterpret_cast<const float2*>(Bv)[o];
-                        b = make_double2(bf.x, bf.y);
-                    }
+                const size_t o = (size_t)r * M + f;
+                if (b_f64) {
+                    const double sc = (double)is * (double)inv_t[r];
+                    const double re = ((double)sum[i].x - (double)cf.x) * sc;
+                    const double im = ((double)sum[i].y - (double)cf.y) * sc;
+                    const double2 b = reinterpret_cast<const double2*>(Bv)[o];
                     Rout[o] = make_double2(b.x - re, b.y - im);
+                } else {
+                    const float sc = is * inv_t[r];
+                    const float2 b = reinterpret_cast<const float2*>(Bv)[o];
+                    const float rr = fmaf(cf.x, sc, fmaf(-sum[i].x, sc, b.x));
+                    const float ri = fmaf(cf.y, sc, fmaf(-sum[i].y, sc, b.y));
+                    Rout[o] = make_double2((double)rr, (double)ri);
                 }
             }
         }

@@ -188,6 +188,29 @@ __device__ __forceinline__ void tmem_ld24(uint32_t taddr, float* v)
     for (int i = 0; i < 24; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// 28 consecutive columns (32 lanes x 32 bit) of tensor memory in one round
+// trip: three loads, one wait that takes the registers as operands so no use
+// is scheduled before it.
+__device__ __forceinline__ void tmem_ld28(uint32_t taddr, float* v)
+{
+    uint32_t r[28];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+                 : "r"(taddr));
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                 : "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23])
+                 : "r"(taddr + 16));
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0, %1, %2, %3}, [%4];"
+                 : "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27])
+                 : "r"(taddr + 24));
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]), "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]), "+r"(r[15]), "+r"(r[16]), "+r"(r[17]), "+r"(r[18]), "+r"(r[19]), "+r"(r[20]), "+r"(r[21]), "+r"(r[22]), "+r"(r[23]), "+r"(r[24]), "+r"(r[25]), "+r"(r[26]), "+r"(r[27])
+                 :
+                 : "memory");
+#pragma unroll
+    for (int i = 0; i < 28; ++i) v[i] = __uint_as_float(r[i]);
+}
+
 // 48 consecutive columns (32 lanes x 32 bit) of tensor memory in one round
 // trip: two loads, one wait; the wait and an empty statement after it take
 // the registers as operands.
