@@ -303,6 +303,51 @@ __global__ void __launch_bounds__(256) k_hpack_scale(const float2* __restrict__ 
     }
 }
 
+// x = hi + lo, hi = x rounded to FP32 (to nearest, ties to even) and lo the
+// remainder rounded to FP32, from the bits of the double with integer
+// operations only: GB300's FP64 pipe takes ~64 cycles a warp instruction, and
+// the FP64 form of this packing ran at 1 TB/s.  |x| below 2^-126 gives
+// (0, 0); |x| of 2^128 and above, +-inf.  The remainder is exact to 2^-48 |x|.
+__device__ __forceinline__ float2 split_f64(double x)
+{
+    const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+    const unsigned sign = (unsigned)(u >> 63) << 31;
+    const int ex = (int)((u >> 52) & 0x7ff) - 1023;
+    if (ex < -126) return make_float2(0.f, 0.f);
+    if (ex > 127) return make_float2(__uint_as_float(sign | 0x7f800000u), 0.f);
+    const unsigned long long mant = u & 0xFFFFFFFFFFFFFull;  // 52 bits
+    unsigned m = (unsigned)(mant >> 29);                      // the 23 bits FP32 keeps
+    const int rem = (int)(mant & ((1u << 29) - 1));
+    int low = rem;  // the rest, in units of 2^(ex - 52)
+    int e2 = ex;
+    if (rem > (1 << 28) || (rem == (1 << 28) && (m & 1u))) {
+        m += 1u;
+        low -= 1 << 29;
+        if (m == (1u << 23)) {  // rounded up to the next power of two
+            m = 0u;
+            e2 += 1;
+        }
+    }
+    if (e2 > 127) return make_float2(__uint_as_float(sign | 0x7f800000u), 0.f);
+    const float hi = __uint_as_float(sign | ((unsigned)(e2 + 127) << 23) | m);
+    float lo = 0.f;
+    if (ex - 52 >= -126) {  // 2^(ex - 52) is a normal FP32: the scaling is exact
+        lo = (float)low * __uint_as_float((unsigned)(ex - 52 + 127) << 23);
+        if (sign) lo = -lo;
+    }
+    return make_float2(hi, lo);
+}
+
+// hi and lo FP16 planes of t x (t a power of two, so t hi and t lo are exact
+// in FP32): hi = fp16(t hi), lo = fp16((t hi - hi16) + t lo), the first
+// difference exact
+__device__ __forceinline__ void split_f16(float2 s, float t, __half* h, __half* l)
+{
+    const float a = t * s.x;
+    *h = __float2half_rn(a);
+    *l = __float2half_rn((a - __half2float(*h)) + t * s.y);
+}
+
 __global__ void __launch_bounds__(256) k_hpack_f64(const double2* __restrict__ X, int n, size_t ldh,
                                                    __half* __restrict__ Bh, __half* __restrict__ Bl,
                                                    float* __restrict__ inv_t)
@@ -311,24 +356,26 @@ __global__ void __launch_bounds__(256) k_hpack_f64(const double2* __restrict__ X
     const int r = blockIdx.x;
     const double2* x = X + (size_t)r * n;
     float m = 0.f;
-    for (int k = threadIdx.x; k < n; k += blockDim.x)
-        m = fmaxf(m, (float)fmax(fabs(x[k].x), fabs(x[k].y)));
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const double2 v = x[k];
+        m = fmaxf(m, fmaxf(fabsf(split_f64(v.x).x), fabsf(split_f64(v.y).x)));  // = (float) max |x|
+    }
     m = block_max(m, red);
     // the float max can round up to the next power of two: scale from it
     // keeps max |t x| < 2^14 either way
     int e = 0;
     frexpf(m, &e);
-    const double t = ldexp(1.0, 14 - e);
+    const float t = ldexpf(1.f, 14 - e);
     if (threadIdx.x == 0) inv_t[r] = ldexpf(1.f, e - 14);
     __half2* h0 = reinterpret_cast<__half2*>(Bh + (size_t)(2 * r) * ldh);
     __half2* h1 = reinterpret_cast<__half2*>(Bh + (size_t)(2 * r + 1) * ldh);
     __half2* l0 = reinterpret_cast<__half2*>(Bl + (size_t)(2 * r) * ldh);
     __half2* l1 = reinterpret_cast<__half2*>(Bl + (size_t)(2 * r + 1) * ldh);
     for (int k = threadIdx.x; k < n; k += blockDim.x) {
-        const double a = t * x[k].x, b = t * x[k].y;
-        const __half hre = __double2half(a), him = __double2half(b);
-        const __half lre = __double2half(a - (double)__half2float(hre));
-        const __half lim = __double2half(b - (double)__half2float(him));
+        const double2 v = x[k];
+        __half hre, lre, him, lim;
+        split_f16(split_f64(v.x), t, &hre, &lre);
+        split_f16(split_f64(v.y), t, &him, &lim);
         h0[k] = __halves2half2(hre, __hneg(him));
         h1[k] = __halves2half2(him, hre);
         l0[k] = __halves2half2(lre, __hneg(lim));
