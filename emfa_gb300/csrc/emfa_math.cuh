@@ -144,4 +144,39 @@ __host__ __device__ inline V3<T> centroid(V3<T> a, V3<T> b, V3<T> c)
     return divr(a + b + c, T(3));
 }
 
+// x = hi + lo, hi = x rounded to FP32 (to nearest, ties to even) and lo the
+// remainder rounded to FP32, from the bits of the double with integer
+// operations only: GB300's FP64 pipe takes ~64 cycles a warp instruction, and
+// the FP64 form of this packing ran at 1 TB/s.  |x| below 2^-126 gives
+// (0, 0); |x| of 2^128 and above, +-inf.  The remainder is exact to 2^-48 |x|.
+__device__ __forceinline__ float2 split_f64(double x)
+{
+    const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+    const unsigned sign = (unsigned)(u >> 63) << 31;
+    const int ex = (int)((u >> 52) & 0x7ff) - 1023;
+    if (ex < -126) return make_float2(0.f, 0.f);
+    if (ex > 127) return make_float2(__uint_as_float(sign | 0x7f800000u), 0.f);
+    const unsigned long long mant = u & 0xFFFFFFFFFFFFFull;  // 52 bits
+    unsigned m = (unsigned)(mant >> 29);                      // the 23 bits FP32 keeps
+    const int rem = (int)(mant & ((1u << 29) - 1));
+    int low = rem;  // the rest, in units of 2^(ex - 52)
+    int e2 = ex;
+    if (rem > (1 << 28) || (rem == (1 << 28) && (m & 1u))) {
+        m += 1u;
+        low -= 1 << 29;
+        if (m == (1u << 23)) {  // rounded up to the next power of two
+            m = 0u;
+            e2 += 1;
+        }
+    }
+    if (e2 > 127) return make_float2(__uint_as_float(sign | 0x7f800000u), 0.f);
+    const float hi = __uint_as_float(sign | ((unsigned)(e2 + 127) << 23) | m);
+    float lo = 0.f;
+    if (ex - 52 >= -126) {  // 2^(ex - 52) is a normal FP32: the scaling is exact
+        lo = (float)low * __uint_as_float((unsigned)(ex - 52 + 127) << 23);
+        if (sign) lo = -lo;
+    }
+    return make_float2(hi, lo);
+}
+
 }  // namespace emfa

@@ -273,6 +273,12 @@ __global__ void __launch_bounds__(KB) k_cgs_update(const Cx<T>* __restrict__ V, 
 }
 
 // squared norms of complex128 vectors: partial[r * nblk + blk]
+// F32: the squares of the values rounded to FP32 (split_f64's high parts,
+// integer operations) summed in FP32 within a thread: the FP32-basis
+// refinement compares the norm with its target to a few digits, and FP64
+// multiply-adds queue on GB300's 1/64-rate pipe.  The plain FP64 path keeps
+// FP64 sums.
+template <bool F32>
 __global__ void __launch_bounds__(KB) k_norm2(const double2* __restrict__ X, int n, int nblk, int chunk,
                                               double2* __restrict__ partial)
 {
@@ -282,9 +288,19 @@ __global__ void __launch_bounds__(KB) k_norm2(const double2* __restrict__ X, int
     double a1[MAXV], a2[MAXV];
     a1[0] = 0.0;
     a2[0] = 0.0;
-    for (int k = blk * chunk + threadIdx.x; k < k1; k += KB) {
-        double2 x = X[base + k];
-        a1[0] += x.x * x.x + x.y * x.y;
+    if (F32) {
+        float t = 0.f;
+        for (int k = blk * chunk + threadIdx.x; k < k1; k += KB) {
+            const double2 x = X[base + k];
+            const float xr = split_f64(x.x).x, xi = split_f64(x.y).x;
+            t += xr * xr + xi * xi;
+        }
+        a1[0] = (double)t;
+    } else {
+        for (int k = blk * chunk + threadIdx.x; k < k1; k += KB) {
+            double2 x = X[base + k];
+            a1[0] += x.x * x.x + x.y * x.y;
+        }
     }
     block_reduce_write<double>(a1, a2, 1, partial + ((size_t)r * nblk + blk), 1);
 }
@@ -1062,20 +1078,32 @@ __global__ void __launch_bounds__(AS_THREADS, 2)
     cluster_wait();  // no CTA leaves while another may still read its shared memory
 }
 
+// out[r] = scale[r] W[r]: grid over (chunks of 1024, RHS).  An FP32 basis is
+// scaled in FP32 and an FP64 source converted by split_f64 (integer
+// operations): FP64 products and conversions per element would run on
+// GB300's 1/64-rate FP64 pipe.
+template <typename T> __device__ __forceinline__ float to_f32(T v) { return (float)v; }
+template <> __device__ __forceinline__ float to_f32<double>(double v) { return split_f64(v).x; }
+__device__ __forceinline__ double cre(double2 v) { return v.x; }
+__device__ __forceinline__ double cim(double2 v) { return v.y; }
+template <typename T> __device__ __forceinline__ T cre(Cx<T> v) { return v.re; }
+template <typename T> __device__ __forceinline__ T cim(Cx<T> v) { return v.im; }
+
 template <typename TO, typename TI>
 __global__ void k_scale_store(const TI* __restrict__ W, const double* __restrict__ scale, int n, int nrhs,
                               TO* __restrict__ out)
 {
-    size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    size_t tot = (size_t)n * nrhs;
     using R = decltype(out->re);
-    for (; id < tot; id += (size_t)gridDim.x * blockDim.x) {
-        int r = (int)(id / n);
-        // an FP32 basis is scaled in FP32: FP64 products per element would
-        // run on GB300's 1/64-rate FP64 pipe
-        const R sc = (R)scale[r];
-        double2 w = ld2(W + id);
-        out[id] = TO{(R)w.x * sc, (R)w.y * sc};
+    const int r = blockIdx.y;
+    const R sc = (R)scale[r];
+    const size_t base = (size_t)r * n;
+    const int k1 = min(n, (int)(blockIdx.x + 1) * 1024);
+    for (int k = blockIdx.x * 1024 + threadIdx.x; k < k1; k += blockDim.x) {
+        const TI w = W[base + k];
+        if constexpr (sizeof(R) == 4)
+            out[base + k] = TO{to_f32(cre(w)) * sc, to_f32(cim(w)) * sc};
+        else
+            out[base + k] = TO{(R)cre(w) * sc, (R)cim(w) * sc};
     }
 }
 
@@ -1408,7 +1436,7 @@ static emfa_status_t gmres_t(Ctx* c, LinOp& A, const void* B, int nrhs, double2*
         } else {
             EMFA_TRY(A.residual(c, X, B, R, nrhs, Xt, st));
         }
-        k_norm2<<<dim3(nblk, nrhs), KB, 0, st>>>(R, n, nblk, chunk, pnorm);
+        k_norm2<std::is_same<T, float>::value><<<dim3(nblk, nrhs), KB, 0, st>>>(R, n, nblk, chunk, pnorm);
         EMFA_CUDA(c, cudaMemsetAsync(s.counters, 0, sizeof(int) * 4, st));
         k_cycle_init<<<(nrhs + 127) / 128, 128, 0, st>>>(s, pnorm, nblk, cyc == 0);
         EMFA_CUDA(c, cudaMemcpyAsync(host_cnt, s.counters, sizeof(int) * 4, cudaMemcpyDeviceToHost, st));
@@ -1418,7 +1446,7 @@ static emfa_status_t gmres_t(Ctx* c, LinOp& A, const void* B, int nrhs, double2*
         if (host_cnt[0] == 0) break;
         ++cycles;
         // V0 = R / beta
-        k_scale_store<Cx<T>, double2><<<grid1(vec), 256, 0, st>>>(R, s.scale, n, nrhs, V);
+        k_scale_store<Cx<T>, double2><<<dim3((n + 1023) / 1024, nrhs), 256, 0, st>>>(R, s.scale, n, nrhs, V);
         int steps = 0;
         for (int j = 0; j < m; ++j) {
             // W = A V_j (for j > 0 done by normalize_apply at the end of the previous step)
@@ -1846,10 +1874,10 @@ emfa_status_t LinOp::normalize_apply(Ctx* c, const void* W, const double* scale,
 {
     const size_t vec = (size_t)n * nrhs;
     if (prec == EMFA_F64)
-        k_scale_store<Cx<double>, Cx<double>><<<grid1(vec), 256, 0, st>>>((const Cx<double>*)W, scale, n, nrhs,
+        k_scale_store<Cx<double>, Cx<double>><<<dim3((n + 1023) / 1024, nrhs), 256, 0, st>>>((const Cx<double>*)W, scale, n, nrhs,
                                                                            (Cx<double>*)Vout);
     else
-        k_scale_store<Cx<float>, Cx<float>><<<grid1(vec), 256, 0, st>>>((const Cx<float>*)W, scale, n, nrhs,
+        k_scale_store<Cx<float>, Cx<float>><<<dim3((n + 1023) / 1024, nrhs), 256, 0, st>>>((const Cx<float>*)W, scale, n, nrhs,
                                                                          (Cx<float>*)Vout);
     c->kernel_launches += 1;
     return apply(c, Vout, Y, nrhs, st);
