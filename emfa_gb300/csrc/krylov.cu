@@ -319,15 +319,19 @@ constexpr int VCHUNK = 1024;
 // reset (optional): an int zeroed by the first CTA, after the predecessor
 // (the step's product) has finished: the step's count of active right-hand
 // sides, so that no memset sits between the step's launches.
+// active (optional): right-hand sides with active[r] == 0 have converged and
+// are skipped (their coefficients and norms are read by nobody).
 template <typename T>
 __global__ void __launch_bounds__(256) k_vdots(const Cx<T>* __restrict__ V, size_t vstride, int nv,
                                                const Cx<T>* __restrict__ W, int n, int nrhs, int nblk,
-                                               double2* __restrict__ partial, int* __restrict__ reset)
+                                               double2* __restrict__ partial, int* __restrict__ reset,
+                                               const int* __restrict__ active)
 {
     using A = typename Acc<T>::type;
     const int blk = blockIdx.x, r = blockIdx.y;
     griddep_wait();
     if (reset && blk == 0 && r == 0 && threadIdx.x == 0) *reset = 0;
+    if (active && !active[r]) return;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const size_t base = (size_t)r * n;
     const int k0 = blk * VCHUNK, k1 = min(n, k0 + VCHUNK);
@@ -380,11 +384,12 @@ template <typename T, bool NORM>
 __global__ void __launch_bounds__(256) k_vupdate(const Cx<T>* __restrict__ V, size_t vstride, int nv,
                                                  double2* __restrict__ h, const double2* __restrict__ partial,
                                                  Cx<T>* __restrict__ W, int n, int nrhs, int nblk,
-                                                 double2* __restrict__ pnorm)
+                                                 double2* __restrict__ pnorm, const int* __restrict__ active)
 {
     using A = typename Acc<T>::type;
     const int blk = blockIdx.x, r = nrhs - 1 - (int)blockIdx.y;
     griddep_wait();
+    if (active && !active[r]) return;  // converged: nobody reads its coefficients or norm
     const size_t base = (size_t)r * n;
     // coefficients (dynamic shared memory: 2 nv values, any restart length)
     extern __shared__ unsigned char dyn_smem[];
@@ -1479,22 +1484,27 @@ static emfa_status_t gmres_t(Ctx* c, LinOp& A, const void* B, int nrhs, double2*
                     // be resident before its predecessor ends (griddep_wait); the
                     // coefficients pass zeroes the step's active count
                     EMFA_CUDA(c, launch_dependent(k_vdots<T>, vg, dim3(256), 0, st, (const Cx<T>*)V, vec, nv,
-                                                  (const Cx<T>*)W, n, nrhs, vblk, partial, s.counters));
+                                                  (const Cx<T>*)W, n, nrhs, vblk, partial, s.counters,
+                                                  (const int*)s.active));
                     EMFA_CUDA(c, launch_dependent(k_vupdate<T, true>, vg, dim3(256), hsm, st, (const Cx<T>*)V, vec, nv,
-                                                  s.hcol, (const double2*)partial, W, n, nrhs, vblk, pnorm));
+                                                  s.hcol, (const double2*)partial, W, n, nrhs, vblk, pnorm,
+                                                  (const int*)s.active));
                     EMFA_CUDA(c, launch_dependent(k_finish_pack, dim3((n + FP_CHUNK - 1) / FP_CHUNK, nrhs), dim3(256),
                                                   0, st, s, j, (const double2*)pnorm, vblk, (const float2*)W, n,
                                                   (float2*)(V + (size_t)(j + 1) * vec), pk));
                     c->kernel_launches += 3;
                 } else {
-                k_vdots<T><<<vg, 256, 0, st>>>(V, vec, nv, W, n, nrhs, vblk, partial, nullptr);
+                k_vdots<T><<<vg, 256, 0, st>>>(V, vec, nv, W, n, nrhs, vblk, partial, nullptr, s.active);
                 if (two_pass) {
-                    k_vupdate<T, false><<<vg, 256, hsm, st>>>(V, vec, nv, s.hcol, partial, W, n, nrhs, vblk, pnorm);
-                    k_vdots<T><<<vg, 256, 0, st>>>(V, vec, nv, W, n, nrhs, vblk, partial, nullptr);
-                    k_vupdate<T, true><<<vg, 256, hsm, st>>>(V, vec, nv, s.y, partial, W, n, nrhs, vblk, pnorm);
+                    k_vupdate<T, false><<<vg, 256, hsm, st>>>(V, vec, nv, s.hcol, partial, W, n, nrhs, vblk, pnorm,
+                                                              s.active);
+                    k_vdots<T><<<vg, 256, 0, st>>>(V, vec, nv, W, n, nrhs, vblk, partial, nullptr, s.active);
+                    k_vupdate<T, true><<<vg, 256, hsm, st>>>(V, vec, nv, s.y, partial, W, n, nrhs, vblk, pnorm,
+                                                             s.active);
                     c->kernel_launches += 2;
                 } else {
-                    k_vupdate<T, true><<<vg, 256, hsm, st>>>(V, vec, nv, s.hcol, partial, W, n, nrhs, vblk, pnorm);
+                    k_vupdate<T, true><<<vg, 256, hsm, st>>>(V, vec, nv, s.hcol, partial, W, n, nrhs, vblk, pnorm,
+                                                             s.active);
                 }
                 EMFA_CUDA(c, cudaMemsetAsync(s.counters, 0, sizeof(int), st));
                 if (m <= 32)
