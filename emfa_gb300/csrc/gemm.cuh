@@ -58,6 +58,7 @@ struct HPack {
     __half* bh = nullptr;
     float* inv_t = nullptr;
     size_t ldh = 0;
+    const int* skip = nullptr;  // optional: a device int; zero when the product starts skips it
 };
 emfa_status_t hgemm_pack_target(Ctx* c, const HPlanes& h, int nrhs, HPack* out);
 emfa_status_t hgemm_apply_packed(Ctx* c, const HPlanes& h, const HPack& p, void* Y, int nrhs, cudaStream_t st);

@@ -69,13 +69,16 @@ template <int BN, int MS>
 __global__ void __launch_bounds__(THREADS, 1)
     k_hgemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
             float2* __restrict__ Y, int M, int R, int kblocks, const float* __restrict__ inv_s,
-            const float* __restrict__ inv_t, int* __restrict__ err)
+            const float* __restrict__ inv_t, int* __restrict__ err, const int* __restrict__ skip)
 {
     using S = Smem<BN, MS>;
     using namespace tc;
     // one wave: every CTA is resident, so the next launch (the Gram-Schmidt
     // coefficients) may be scheduled beside it at once and wait for its end
     griddep_launch();
+    // no right-hand side left active (the Krylov step queued after the last
+    // one): the same value in every thread, before any barrier or allocation
+    if (skip && *skip == 0) return;
     extern __shared__ uint8_t smem_raw[];
     uint8_t* base = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint8_t* sA = base;                               // [stage][row block]
@@ -615,19 +618,23 @@ static emfa_status_t make_map_h(Ctx* c, CUtensorMap* m, const void* ptr, uint64_
     return EMFA_OK;
 }
 
+// timed: bracket the launch with the context's kernel timer (launches that
+// may skip are not timed: their work is not known on the host)
 template <int BN, int MS>
 static emfa_status_t launch_h(Ctx* c, const CUtensorMap& ta, const CUtensorMap& tb, float2* Y, int n, int nrhs,
-                              const float* inv_s, const float* inv_t, int* err, cudaStream_t st, bool timed = true)
+                              const float* inv_s, const float* inv_t, int* err, cudaStream_t st, bool timed,
+                              const int* skip)
 {
     using S = th::Smem<BN, MS>;
     EMFA_TRY(ensure_smem(c, th::k_hgemm<BN, MS>, S::TOTAL));
     dim3 grd((2 * nrhs + BN - 1) / BN, (n + th::BM * MS - 1) / (th::BM * MS));
     const int kblocks = (2 * n + th::BKH - 1) / th::BKH;
-    if (timed) {
+    if (timed && !skip) {
         TimedLaunch tl(c, KT_GEMM, st, 8.0 * n * (double)n * nrhs);
-        th::k_hgemm<BN, MS><<<grd, th::THREADS, S::TOTAL, st>>>(ta, tb, Y, n, nrhs, kblocks, inv_s, inv_t, err);
+        th::k_hgemm<BN, MS><<<grd, th::THREADS, S::TOTAL, st>>>(ta, tb, Y, n, nrhs, kblocks, inv_s, inv_t, err,
+                                                                  nullptr);
     } else {
-        th::k_hgemm<BN, MS><<<grd, th::THREADS, S::TOTAL, st>>>(ta, tb, Y, n, nrhs, kblocks, inv_s, inv_t, err);
+        th::k_hgemm<BN, MS><<<grd, th::THREADS, S::TOTAL, st>>>(ta, tb, Y, n, nrhs, kblocks, inv_s, inv_t, err, skip);
     }
     c->kernel_launches += 1;
     EMFA_CUDA(c, cudaGetLastError());
@@ -715,13 +722,13 @@ static int fixed_variant(int n, int nrhs, int sms)
 
 static emfa_status_t launch_variant(Ctx* c, int v, const CUtensorMap& ta, const CUtensorMap* tb, float2* Y, int n,
                                     int nrhs, const float* inv_s, const float* inv_t, int* err, cudaStream_t st,
-                                    bool timed)
+                                    bool timed, const int* skip = nullptr)
 {
     switch (v) {
-    case HV_64_1: return launch_h<64, 1>(c, ta, tb[0], Y, n, nrhs, inv_s, inv_t, err, st, timed);
-    case HV_64_2: return launch_h<64, 2>(c, ta, tb[0], Y, n, nrhs, inv_s, inv_t, err, st, timed);
-    case HV_144_1: return launch_h<144, 1>(c, ta, tb[1], Y, n, nrhs, inv_s, inv_t, err, st, timed);
-    default: return launch_h<144, 2>(c, ta, tb[1], Y, n, nrhs, inv_s, inv_t, err, st, timed);
+    case HV_64_1: return launch_h<64, 1>(c, ta, tb[0], Y, n, nrhs, inv_s, inv_t, err, st, timed, skip);
+    case HV_64_2: return launch_h<64, 2>(c, ta, tb[0], Y, n, nrhs, inv_s, inv_t, err, st, timed, skip);
+    case HV_144_1: return launch_h<144, 1>(c, ta, tb[1], Y, n, nrhs, inv_s, inv_t, err, st, timed, skip);
+    default: return launch_h<144, 2>(c, ta, tb[1], Y, n, nrhs, inv_s, inv_t, err, st, timed, skip);
     }
 }
 
@@ -771,9 +778,10 @@ static emfa_status_t tune_variants(Ctx* c, const TuneKey& key, const CUtensorMap
     return EMFA_OK;
 }
 
-// the inner-product GEMM on an already packed B plane
+// the inner-product GEMM on an already packed B plane; skip (optional): an
+// int that, if zero when the product starts, skips it
 static emfa_status_t hgemm_run(Ctx* c, const HPlanes& h, const __half* bh, const float* inv_t, void* Y, int nrhs,
-                               int* err, cudaStream_t st)
+                               int* err, cudaStream_t st, const int* skip = nullptr)
 {
     const int n = h.n;
     const size_t ldh = h.ldh;
@@ -791,10 +799,11 @@ static emfa_status_t hgemm_run(Ctx* c, const HPlanes& h, const __half* bh, const
             auto it = g_tune.find(key);
             if (it != g_tune.end()) known = it->second.variant;
         }
-        if (known < 0) return tune_variants(c, key, ta, tb, (float2*)Y, n, nrhs, h.inv_s, inv_t, err, st);
-        v = known;
+        // a product that may be skipped is never the one that tunes
+        if (known < 0 && !skip) return tune_variants(c, key, ta, tb, (float2*)Y, n, nrhs, h.inv_s, inv_t, err, st);
+        if (known >= 0) v = known;
     }
-    return launch_variant(c, v, ta, tb, (float2*)Y, n, nrhs, h.inv_s, inv_t, err, st, true);
+    return launch_variant(c, v, ta, tb, (float2*)Y, n, nrhs, h.inv_s, inv_t, err, st, true, skip);
 }
 
 emfa_status_t hgemm_tuned_shape(int device, int n, int nrhs, int* variant, float* ms)
@@ -865,7 +874,7 @@ emfa_status_t hgemm_apply_packed(Ctx* c, const HPlanes& h, const HPack& p, void*
 {
     int* err = nullptr;
     EMFA_TRY(herr(c, &err));
-    return hgemm_run(c, h, p.bh, p.inv_t, Y, nrhs, err, st);
+    return hgemm_run(c, h, p.bh, p.inv_t, Y, nrhs, err, st, p.skip);
 }
 
 emfa_status_t hgemm_residual(Ctx* c, const HPlanes& h, const double2* X, const void* B, bool b_is_f32, double2* R,

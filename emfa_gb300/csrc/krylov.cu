@@ -1468,6 +1468,8 @@ static emfa_status_t gmres_t(Ctx* c, LinOp& A, const void* B, int nrhs, double2*
             if (normalises) {
                 packs = A.pack_target(c, nrhs, &pk);
                 if (!packs) pk = HPack{};
+                // the next product skips itself if this step leaves nothing active
+                pk.skip = s.counters;
             }
             if (fused) {
                 // V_{j+1} and the next product's operand come out of the step
