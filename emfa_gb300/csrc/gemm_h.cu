@@ -76,6 +76,9 @@ __global__ void __launch_bounds__(THREADS, 1)
     // one wave: every CTA is resident, so the next launch (the Gram-Schmidt
     // coefficients) may be scheduled beside it at once and wait for its end
     griddep_launch();
+    // launched as a dependent (the Krylov loop's products): the step that
+    // packed B and counted the active right-hand sides must have finished
+    griddep_wait();
     // no right-hand side left active (the Krylov step queued after the last
     // one): the same value in every thread, before any barrier or allocation
     if (skip && *skip == 0) return;
@@ -633,6 +636,11 @@ static emfa_status_t launch_h(Ctx* c, const CUtensorMap& ta, const CUtensorMap& 
         TimedLaunch tl(c, KT_GEMM, st, 8.0 * n * (double)n * nrhs);
         th::k_hgemm<BN, MS><<<grd, th::THREADS, S::TOTAL, st>>>(ta, tb, Y, n, nrhs, kblocks, inv_s, inv_t, err,
                                                                   nullptr);
+    } else if (skip) {
+        // the Krylov loop's product: scheduled while the step that packed its
+        // operand drains (programmatic dependent launch)
+        EMFA_CUDA(c, launch_dependent(th::k_hgemm<BN, MS>, grd, dim3(th::THREADS), (size_t)S::TOTAL, st, ta, tb, Y, n,
+                                      nrhs, kblocks, inv_s, inv_t, err, skip));
     } else {
         th::k_hgemm<BN, MS><<<grd, th::THREADS, S::TOTAL, st>>>(ta, tb, Y, n, nrhs, kblocks, inv_s, inv_t, err, skip);
     }

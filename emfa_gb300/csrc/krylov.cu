@@ -600,7 +600,7 @@ __global__ void k_arnoldi_finish(GmresDev s, int j, const double2* __restrict__ 
         s.scale[r] = 0.0;
     } else {
         s.scale[r] = 1.0 / beta;
-        atomicAdd(s.counters, 1);
+        atomicAdd(s.step_cnt, 1);
     }
 }
 
@@ -671,7 +671,7 @@ __device__ void arnoldi_column(const GmresDev& s, int r, int j, double2 h, doubl
             s.scale[r] = 0.0;
         } else {
             s.scale[r] = 1.0 / beta;
-            atomicAdd(s.counters, 1);
+            atomicAdd(s.step_cnt, 1);
         }
     }
     if (lane <= j) H[lane * m + j] = h;
@@ -744,7 +744,7 @@ __device__ void arnoldi_column_f32(const GmresDev& s, int r, int j, double2 hd, 
             s.scale[r] = 0.0;
         } else {
             s.scale[r] = 1.0 / (double)beta;
-            atomicAdd(s.counters, 1);
+            atomicAdd(s.step_cnt, 1);
         }
     }
     if (lane <= j) H[lane * m + j] = make_double2(h.x, h.y);
@@ -1422,14 +1422,24 @@ static emfa_status_t gmres_t(Ctx* c, LinOp& A, const void* B, int nrhs, double2*
     // after the last active one does nothing for converged right-hand sides
     // (k_arnoldi_finish skips them).
     struct StepEvents {
-        cudaEvent_t e[2] = {nullptr, nullptr};
+        cudaEvent_t e[2] = {nullptr, nullptr};     // the host's copy of a step's count has landed
+        cudaEvent_t done[2] = {nullptr, nullptr};  // a step's kernels have finished (main stream)
+        cudaStream_t side = nullptr;               // the copies
         ~StepEvents()
         {
+            if (side) {
+                cudaStreamSynchronize(side);
+                cudaStreamDestroy(side);
+            }
             for (auto x : e)
+                if (x) cudaEventDestroy(x);
+            for (auto x : done)
                 if (x) cudaEventDestroy(x);
         }
     } sev;
     for (auto& x : sev.e) EMFA_CUDA(c, cudaEventCreateWithFlags(&x, cudaEventDisableTiming));
+    for (auto& x : sev.done) EMFA_CUDA(c, cudaEventCreateWithFlags(&x, cudaEventDisableTiming));
+    EMFA_CUDA(c, cudaStreamCreateWithFlags(&sev.side, cudaStreamNonBlocking));
     volatile int* slot = c->pinned;
     for (int cyc = 0; cyc < max_cycles; ++cyc) {
         // true residual R = B - Z X (X = 0 on the first cycle: R = B)
@@ -1460,6 +1470,7 @@ static emfa_status_t gmres_t(Ctx* c, LinOp& A, const void* B, int nrhs, double2*
             // (h2 = V^H W; W -= V h2) and H gets h + h2.
             const dim3 vg(vblk, nrhs);
             const int nv = j + 1;
+            s.step_cnt = s.counters + 2 + (j & 1);
             HPack pk;
             bool packs = false;
             // the step normalises V_{j+1} itself (fused, or separate passes
@@ -1469,11 +1480,11 @@ static emfa_status_t gmres_t(Ctx* c, LinOp& A, const void* B, int nrhs, double2*
                 packs = A.pack_target(c, nrhs, &pk);
                 if (!packs) pk = HPack{};
                 // the next product skips itself if this step leaves nothing active
-                pk.skip = s.counters;
+                pk.skip = s.step_cnt;
             }
             if (fused) {
                 // V_{j+1} and the next product's operand come out of the step
-                EMFA_CUDA(c, cudaMemsetAsync(s.counters, 0, sizeof(int), st));
+                EMFA_CUDA(c, cudaMemsetAsync(s.step_cnt, 0, sizeof(int), st));
                 EMFA_TRY(launch_arnoldi_step(c, sh, nrhs, st, s, j, (const float2*)V, vec, (const float2*)W, n,
                                              (float2*)(V + (size_t)(j + 1) * vec), pk));
                 c->kernel_launches += 1;
@@ -1486,7 +1497,7 @@ static emfa_status_t gmres_t(Ctx* c, LinOp& A, const void* B, int nrhs, double2*
                     // be resident before its predecessor ends (griddep_wait); the
                     // coefficients pass zeroes the step's active count
                     EMFA_CUDA(c, launch_dependent(k_vdots<T>, vg, dim3(256), 0, st, (const Cx<T>*)V, vec, nv,
-                                                  (const Cx<T>*)W, n, nrhs, vblk, partial, s.counters,
+                                                  (const Cx<T>*)W, n, nrhs, vblk, partial, s.step_cnt,
                                                   (const int*)s.active));
                     EMFA_CUDA(c, launch_dependent(k_vupdate<T, true>, vg, dim3(256), hsm, st, (const Cx<T>*)V, vec, nv,
                                                   s.hcol, (const double2*)partial, W, n, nrhs, vblk, pnorm,
@@ -1508,7 +1519,7 @@ static emfa_status_t gmres_t(Ctx* c, LinOp& A, const void* B, int nrhs, double2*
                     k_vupdate<T, true><<<vg, 256, hsm, st>>>(V, vec, nv, s.hcol, partial, W, n, nrhs, vblk, pnorm,
                                                              s.active);
                 }
-                EMFA_CUDA(c, cudaMemsetAsync(s.counters, 0, sizeof(int), st));
+                EMFA_CUDA(c, cudaMemsetAsync(s.step_cnt, 0, sizeof(int), st));
                 if (m <= 32)
                     k_arnoldi_finish_warp<<<(nrhs * 32 + 127) / 128, 128, 0, st>>>(s, j, pnorm, vblk, two_pass ? 1 : 0);
                 else
@@ -1516,8 +1527,13 @@ static emfa_status_t gmres_t(Ctx* c, LinOp& A, const void* B, int nrhs, double2*
                 c->kernel_launches += 3;
                 }
             }
-            EMFA_CUDA(c, cudaMemcpyAsync((void*)(slot + (j & 1)), s.counters, sizeof(int), cudaMemcpyDeviceToHost, st));
-            EMFA_CUDA(c, cudaEventRecord(sev.e[j & 1], st));
+            // the host reads the step's count on a side stream, so no copy sits
+            // between this step's last kernel and the next product
+            EMFA_CUDA(c, cudaEventRecord(sev.done[j & 1], st));
+            EMFA_CUDA(c, cudaStreamWaitEvent(sev.side, sev.done[j & 1], 0));
+            EMFA_CUDA(c, cudaMemcpyAsync((void*)(slot + (j & 1)), s.step_cnt, sizeof(int), cudaMemcpyDeviceToHost,
+                                         sev.side));
+            EMFA_CUDA(c, cudaEventRecord(sev.e[j & 1], sev.side));
             ++steps;
             if (j > 0) {
                 EMFA_CUDA(c, cudaEventSynchronize(sev.e[(j - 1) & 1]));

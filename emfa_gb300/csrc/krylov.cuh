@@ -22,7 +22,9 @@ struct GmresDev {
     double* true_res;// nrhs  true relative residual at the last restart
     int* jlen;       // nrhs  basis vectors used in the current cycle
     int* active;     // nrhs
-    int* counters;   // [0] active RHS, [1] converged RHS
+    int* counters;   // [0] active RHS, [1] converged RHS (cycle start); [2], [3] per Arnoldi step
+    int* step_cnt;   // the step's count of RHS still active: counters + 2 + (j & 1), so that the
+                     //   host's read of step j overlaps step j + 1 (which counts into the other)
 };
 
 }  // namespace emfa
