@@ -1553,7 +1553,6 @@ static emfa_status_t gmres_t(Ctx* c, LinOp& A, const void* B, int nrhs, double2*
                 EMFA_TRY(A.normalize_apply(c, W, s.scale, s.wmax, V + (size_t)(j + 1) * vec, W, nrhs, st));
         }
         total_iters += steps;
-        EMFA_TRY(A.check(c, st));
         if (std::is_same<T, float>::value && m <= 32)
             k_backsolve_f32<<<(nrhs + BS_WARPS - 1) / BS_WARPS, 32 * BS_WARPS, 0, st>>>(s);
         else
@@ -1564,6 +1563,10 @@ static emfa_status_t gmres_t(Ctx* c, LinOp& A, const void* B, int nrhs, double2*
         EMFA_CUDA(c, cudaGetLastError());
     }
     EMFA_CUDA(c, cudaGetLastError());
+    // the operator's device-side error word (a timed-out wait) once, after the
+    // last cycle: the word is sticky, and a check per cycle cost a host
+    // synchronisation in the middle of the device's queue
+    EMFA_TRY(A.check(c, st));
     cudaEventRecord(e1, st);
     EMFA_CUDA(c, cudaStreamSynchronize(st));
     float ms = 0;
