@@ -828,7 +828,9 @@ __global__ void __launch_bounds__(256, 3) k_fill_tile_cfie_sym(const RwgPack<flo
         const RwgPack<float>& F = rw[f];
         const RwgPack<float>& S = rw[s];
         float zer = 0, zei = 0, zmr = 0, zmi = 0, ztr = 0, zti = 0;
-        double sr = 0.0, si = 0.0, sr_t = 0.0, si_t = 0.0;
+        // self terms from the FP64 table, summed in FP32 (at most two per
+        // entry; the entry is FP32): four registers, not eight
+        float sr = 0.f, si = 0.f, sr_t = 0.f, si_t = 0.f;
 #pragma unroll 1
         for (int a = 0; a < 2; ++a) {
             const int lf = loc[2 * (size_t)f + a];
@@ -849,11 +851,11 @@ __global__ void __launch_bounds__(256, 3) k_fill_tile_cfie_sym(const RwgPack<flo
                 const float sgn = (a == b) ? 1.0f : -1.0f;
                 if (F.tri[a] == S.tri[b]) {
                     const double2 v = sing[9 * F.tri[a] + 3 * F.e[a] + S.e[b]];
-                    sr += (double)sgn * v.x;
-                    si += (double)sgn * v.y;
+                    sr += sgn * (float)v.x;
+                    si += sgn * (float)v.y;
                     const double2 vt = sing[9 * S.tri[b] + 3 * S.e[b] + F.e[a]];
-                    sr_t += (double)sgn * vt.x;
-                    si_t += (double)sgn * vt.y;
+                    sr_t += sgn * (float)vt.x;
+                    si_t += sgn * (float)vt.y;
                     continue;
                 }
                 const int ls = loc[2 * (size_t)s + b];
@@ -904,8 +906,8 @@ __global__ void __launch_bounds__(256, 3) k_fill_tile_cfie_sym(const RwgPack<flo
             }
         }
         const float l = F.len * S.len;
-        out = cx((-c.ce * zei + c.cm * zmr + (float)sr) * l, (c.ce * zer + c.cm * zmi + (float)si) * l);
-        out_t = cx((-c.ce * zei + c.cm * ztr + (float)sr_t) * l, (c.ce * zer + c.cm * zti + (float)si_t) * l);
+        out = cx((-c.ce * zei + c.cm * zmr + sr) * l, (c.ce * zer + c.cm * zmi + si) * l);
+        out_t = cx((-c.ce * zei + c.cm * ztr + sr_t) * l, (c.ce * zer + c.cm * zti + si_t) * l);
         Z[(size_t)f * ldz + s] = out;
     }
     if (!mirror) return;  // uniform over the CTA
