@@ -553,7 +553,10 @@ __global__ void __launch_bounds__(256) k_fill_tile(const RwgPack<float>* __restr
         }
     }
     Cx<float> ze = cx(0.0f, 0.0f), zm = cx(0.0f, 0.0f);
-    double sr = 0.0, si = 0.0;
+    // self terms: a pair's value formed in FP64 from the table and rounded
+    // once; the sum over an entry's (at most two) self pairs in FP32, so no
+    // FP64 register or conversion in the common entry
+    float sr = 0.f, si = 0.f;
 #pragma unroll 1
     for (int a = 0; a < 2; ++a) {
         const int lf = loc[2 * (size_t)f + a];
@@ -578,13 +581,13 @@ __global__ void __launch_bounds__(256) k_fill_tile(const RwgPack<float>* __restr
                 const int id = 9 * F.tri[a] + 3 * F.e[a] + S.e[b];
                 if (CFIE) {
                     const double2 v = sing[id];
-                    sr += (double)sgn * v.x;
-                    si += (double)sgn * v.y;
+                    sr += sgn * (float)v.x;
+                    si += sgn * (float)v.y;
                 } else {
                     const double2 v = sing[3 * id + ((a == 0 && b == 0) ? 0 : 1)];
                     const double2 g = sing[3 * id + 2];
-                    sr += (double)sgn * v.x + g.x;
-                    si += (double)sgn * v.y + g.y;
+                    sr += (float)((double)sgn * v.x + g.x);
+                    si += (float)((double)sgn * v.y + g.y);
                 }
                 continue;
             }
@@ -603,12 +606,12 @@ __global__ void __launch_bounds__(256) k_fill_tile(const RwgPack<float>* __restr
     const float l = F.len * S.len;
     Cx<float> out;
     if (CFIE) {
-        const float re = -c.ce * ze.im + c.cm * zm.re + (float)sr;
-        const float im = c.ce * ze.re + c.cm * zm.im + (float)si;
+        const float re = -c.ce * ze.im + c.cm * zm.re + sr;
+        const float im = c.ce * ze.re + c.cm * zm.im + si;
         out = cx(re * l, im * l);
     } else {
         const float kz = (float)c.coef_efie * l;
-        const float re = c.ce * ze.re + (float)sr, im = c.ce * ze.im + (float)si;
+        const float re = c.ce * ze.re + sr, im = c.ce * ze.im + si;
         out = cx(-kz * im, kz * re);
     }
     Z[(size_t)f * ldz + s] = out;
@@ -688,7 +691,9 @@ __global__ void __launch_bounds__(256) k_fill_tile_sym(const RwgPack<float>* __r
         }
         if (!zeroed) {
             Cx<float> ze = cx(0.0f, 0.0f), zm = cx(0.0f, 0.0f);
-            double sr = 0.0, si = 0.0, sr_t = 0.0, si_t = 0.0;
+            // self terms: a pair's value formed in FP64 and rounded once, the
+            // sums in FP32 (no FP64 register or conversion per entry)
+            float sr = 0.f, si = 0.f, sr_t = 0.f, si_t = 0.f;
 #pragma unroll 1
             for (int a = 0; a < 2; ++a) {
                 const int lf = loc[2 * (size_t)f + a];
@@ -709,14 +714,14 @@ __global__ void __launch_bounds__(256) k_fill_tile_sym(const RwgPack<float>* __r
                         const int id = 9 * F.tri[a] + 3 * F.e[a] + S.e[b];
                         const double2 v = sing[3 * id + ((a == 0 && b == 0) ? 0 : 1)];
                         const double2 g = sing[3 * id + 2];
-                        sr += (double)sgn * v.x + g.x;
-                        si += (double)sgn * v.y + g.y;
+                        sr += (float)((double)sgn * v.x + g.x);
+                        si += (float)((double)sgn * v.y + g.y);
                         // the mirrored entry: test s (side b), source f (side a)
                         const int it = 9 * S.tri[b] + 3 * S.e[b] + F.e[a];
                         const double2 vt = sing[3 * it + ((b == 0 && a == 0) ? 0 : 1)];
                         const double2 gt = sing[3 * it + 2];
-                        sr_t += (double)sgn * vt.x + gt.x;
-                        si_t += (double)sgn * vt.y + gt.y;
+                        sr_t += (float)((double)sgn * vt.x + gt.x);
+                        si_t += (float)((double)sgn * vt.y + gt.y);
                         continue;
                     }
                     const int ls = loc[2 * (size_t)s + b];
@@ -729,10 +734,10 @@ __global__ void __launch_bounds__(256) k_fill_tile_sym(const RwgPack<float>* __r
                 }
             }
             const float kz = (float)c.coef_efie * (F.len * S.len);
-            float re = c.ce * ze.re + (float)sr, im = c.ce * ze.im + (float)si;
+            float re = c.ce * ze.re + sr, im = c.ce * ze.im + si;
             out = cx(-kz * im, kz * re);
-            re = c.ce * ze.re + (float)sr_t;
-            im = c.ce * ze.im + (float)si_t;
+            re = c.ce * ze.re + sr_t;
+            im = c.ce * ze.im + si_t;
             out_t = cx(-kz * im, kz * re);
         }
         Z[(size_t)f * ldz + s] = out;
