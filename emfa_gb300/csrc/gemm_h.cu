@@ -222,11 +222,14 @@ __global__ void k_zmax(const float2* __restrict__ Z, size_t ldz, int n, unsigned
 {
     __shared__ float red[32];
     float m = 0.f;
-    const size_t tot = (size_t)n * n;
-    for (size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x; id < tot; id += (size_t)gridDim.x * blockDim.x) {
-        const size_t i = id / n, j = id % n;
-        const float2 z = Z[i * ldz + j];
-        m = fmaxf(m, fmaxf(fabsf(z.x), fabsf(z.y)));
+    // CTAs stride the rows, threads the columns: no index division per element
+    for (int i = blockIdx.x; i < n; i += gridDim.x) {
+        const float2* zr = Z + (size_t)i * ldz;
+#pragma unroll 4
+        for (int j = threadIdx.x; j < n; j += blockDim.x) {
+            const float2 z = zr[j];
+            m = fmaxf(m, fmaxf(fabsf(z.x), fabsf(z.y)));
+        }
     }
     m = block_max(m, red);
     if (threadIdx.x == 0) atomicMax(amax, __float_as_uint(m));
@@ -241,15 +244,19 @@ __global__ void k_zsplit(const float2* __restrict__ Z, size_t ldz, int n, size_t
     frexpf(__uint_as_float(*amax), &e);
     const float s = ldexpf(1.f, 15 - e);
     if (blockIdx.x == 0 && threadIdx.x == 0) *inv_s = ldexpf(1.f, e - 15);
-    const size_t tot = (size_t)n * n;
-    for (size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x; id < tot; id += (size_t)gridDim.x * blockDim.x) {
-        const size_t i = id / n, j = id % n;
-        const float2 z = Z[i * ldz + j];
-        const float a = s * z.x, b = s * z.y;  // exact: power-of-two scaling
-        const __half ha = __float2half_rn(a), hb = __float2half_rn(b);
-        const __half la = __float2half_rn(a - __half2float(ha)), lb = __float2half_rn(b - __half2float(hb));
-        reinterpret_cast<__half2*>(Zh + i * ldh)[j] = __halves2half2(ha, hb);
-        reinterpret_cast<__half2*>(Zl + i * ldh)[j] = __halves2half2(la, lb);
+    for (int i = blockIdx.x; i < n; i += gridDim.x) {
+        const float2* zr = Z + (size_t)i * ldz;
+        __half2* hr = reinterpret_cast<__half2*>(Zh + (size_t)i * ldh);
+        __half2* lr = reinterpret_cast<__half2*>(Zl + (size_t)i * ldh);
+#pragma unroll 4
+        for (int j = threadIdx.x; j < n; j += blockDim.x) {
+            const float2 z = zr[j];
+            const float a = s * z.x, b = s * z.y;  // exact: power-of-two scaling
+            const __half ha = __float2half_rn(a), hb = __float2half_rn(b);
+            const __half la = __float2half_rn(a - __half2float(ha)), lb = __float2half_rn(b - __half2float(hb));
+            hr[j] = __halves2half2(ha, hb);
+            lr[j] = __halves2half2(la, lb);
+        }
     }
 }
 
@@ -673,7 +680,7 @@ emfa_status_t hsplit_prepare(Ctx* c, const void* Z, size_t ldz, int n, HPlanes* 
     EMFA_TRY(herr(c, &err));
     EMFA_CUDA(c, cudaMemsetAsync(err, 0, sizeof(int), st));
     EMFA_CUDA(c, cudaMemsetAsync(amax, 0, sizeof(unsigned int), st));
-    const int g = grid_stride_blocks(c, (size_t)n * n);
+    const int g = std::max(1, std::min(grid_stride_blocks(c, (size_t)n * n), n));  // CTAs stride the rows
     th::k_zmax<<<g, 256, 0, st>>>((const float2*)Z, ldz, n, amax);
     th::k_zsplit<<<g, 256, 0, st>>>((const float2*)Z, ldz, n, ldh, amax, zh, zl, inv_s);
     c->kernel_launches += 2;
