@@ -782,17 +782,17 @@ __global__ void k_arnoldi_finish_warp(GmresDev s, int j, const double2* __restri
 }
 
 // Last kernel of the separate-pass CGS1 step (FP32 basis, restarts up to
-// 32): CTA per (chunk of 1024 elements, right-hand side).  Every CTA forms
+// 32): CTA per (chunk of FP_CHUNK elements, right-hand side).  Every CTA forms
 // beta = ||w|| and the FP16 scale from the update's partials (the same sums
 // in the same order, so the same values) and writes its chunk of
 // V_{j+1} = W / beta and, for operators that pack their input, the FP16 rows
 // of the next product (as k_hpack_scale).  In the first chunk's CTA, warp 0
 // finishes the Arnoldi column (as k_arnoldi_finish_warp, single pass) while
-// the other warps pack: the column's serial FP64 chain overlaps the stream.
+// the other warps pack: the column's serial chain (FP32) overlaps the stream.
 // A right-hand side that this step finds converged is normalised all the
 // same (its V_{j+1} lies past its basis length); one that was already
 // inactive writes nothing.
-constexpr int FP_CHUNK = 1024;
+constexpr int FP_CHUNK = 4096;
 
 __global__ void __launch_bounds__(256) k_finish_pack(GmresDev s, int j, const double2* __restrict__ pnorm, int nblk,
                                                      const float2* __restrict__ W, int n, float2* __restrict__ Vout,
