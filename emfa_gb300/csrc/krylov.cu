@@ -103,50 +103,10 @@ __global__ void k_reduce_partials(const double2* __restrict__ partial, int nv, i
     out[id] = s;
 }
 
-// W[r][k] -= sum_{i < nv} h[i][r] V_i[r][k]; partial norms of the new W
-template <typename T>
-__global__ void __launch_bounds__(KB) k_axpys(const Cx<T>* __restrict__ V, size_t vstride, int nv,
-                                              const double2* __restrict__ h, Cx<T>* __restrict__ W, int n, int nrhs,
-                                              int nblk, double2* __restrict__ pnorm)
-{
-    const int blk = blockIdx.x, r = blockIdx.y;
-    const size_t base = (size_t)r * n;
-    __shared__ double2 hs[64];
-    for (int i = threadIdx.x; i < nv; i += KB) hs[i] = h[(size_t)i * nrhs + r];
-    __syncthreads();
-    double nr = 0.0;
-#pragma unroll
-    for (int e = 0; e < KE; ++e) {
-        int k = blk * KCHUNK + e * KB + threadIdx.x;
-        if (k >= n) continue;
-        double2 w = ld2(W + base + k);
-        for (int i = 0; i < nv; ++i) {
-            double2 v = ld2(V + (size_t)i * vstride + base + k);
-            w.x -= hs[i].x * v.x - hs[i].y * v.y;
-            w.y -= hs[i].x * v.y + hs[i].y * v.x;
-        }
-        Cx<T> o = cx((T)w.x, (T)w.y);
-        W[base + k] = o;
-        nr += (double)o.re * (double)o.re + (double)o.im * (double)o.im;
-    }
-    __shared__ double red[KB / 32];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) nr += __shfl_xor_sync(0xffffffffu, nr, o);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = nr;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double s = 0.0;
-        for (int q = 0; q < KB / 32; ++q) s += red[q];
-        pnorm[(size_t)r * nblk + blk] = make_double2(s, 0.0);
-    }
-}
-
 // ---------------------------------------------------------------------------
-// Gram-Schmidt passes over the whole basis.  Each thread keeps one
-// accumulator per basis vector in registers (all loads of an element
-// independent), sums its elements in the storage precision (FP32 for the
-// mixed path: GB300's FP64 pipe is ~1/64 of FP32), and the per-thread sums
-// meet in FP64 across the block and across blocks.
+// Block reductions: per-thread sums in the storage precision (FP32 for the
+// mixed path: GB300's FP64 pipe is ~1/64 of FP32), warp and block sums in
+// FP64, written as the block's partials.
 // ---------------------------------------------------------------------------
 constexpr int MAXV = 32;  // basis vectors per pass of the block-dot kernels (BiCGStab)
 constexpr int MAX_RESTART = 255;  // GMRES(m): coefficients live in dynamic shared memory
@@ -179,96 +139,6 @@ __device__ __forceinline__ void block_reduce_write(A (&ar)[MAXV], A (&ai)[MAXV],
             t.y += red[threadIdx.x][q].y;
         }
         out[(size_t)threadIdx.x * ostride] = t;
-    }
-}
-
-// partial[(i * nrhs + r) * nblk + blk] = sum over the block's chunk of conj(V_i) W
-template <typename T>
-__global__ void __launch_bounds__(KB) k_multidot(const Cx<T>* __restrict__ V, size_t vstride, int nv,
-                                                 const Cx<T>* __restrict__ W, int n, int nrhs, int nblk, int chunk,
-                                                 double2* __restrict__ partial)
-{
-    using A = typename Acc<T>::type;
-    const int blk = blockIdx.x, r = blockIdx.y;
-    const size_t base = (size_t)r * n;
-    const int k1 = min(n, (blk + 1) * chunk);
-    A ar[MAXV], ai[MAXV];
-#pragma unroll
-    for (int i = 0; i < MAXV; ++i) ar[i] = ai[i] = A(0);
-    for (int k = blk * chunk + threadIdx.x; k < k1; k += KB) {
-        const Cx<T> w = W[base + k];
-#pragma unroll
-        for (int i = 0; i < MAXV; ++i) {
-            if (i < nv) {
-                const Cx<T> v = V[(size_t)i * vstride + base + k];
-                ar[i] += (A)v.re * (A)w.re + (A)v.im * (A)w.im;
-                ai[i] += (A)v.re * (A)w.im - (A)v.im * (A)w.re;
-            }
-        }
-    }
-    block_reduce_write<A>(ar, ai, nv, partial + ((size_t)r * nblk + blk), (size_t)nrhs * nblk);
-}
-
-// W -= sum_i h_i V_i over the chunk; then either the dot products of the new
-// W with every V_i (second Gram-Schmidt pass) or the squared norm of W.
-template <typename T, bool DOTS>
-__global__ void __launch_bounds__(KB) k_cgs_update(const Cx<T>* __restrict__ V, size_t vstride, int nv,
-                                                   const double2* __restrict__ h, Cx<T>* __restrict__ W, int n,
-                                                   int nrhs, int nblk, int chunk, double2* __restrict__ partial)
-{
-    using A = typename Acc<T>::type;
-    const int blk = blockIdx.x, r = blockIdx.y;
-    const size_t base = (size_t)r * n;
-    const int k1 = min(n, (blk + 1) * chunk);
-    __shared__ double2 hs[MAXV];
-    if (threadIdx.x < nv) hs[threadIdx.x] = h[(size_t)threadIdx.x * nrhs + r];
-    __syncthreads();
-    __shared__ A hsa[2][MAXV];
-    if (threadIdx.x < MAXV) {
-        hsa[0][threadIdx.x] = threadIdx.x < nv ? (A)hs[threadIdx.x].x : A(0);
-        hsa[1][threadIdx.x] = threadIdx.x < nv ? (A)hs[threadIdx.x].y : A(0);
-    }
-    __syncthreads();
-    A ar[MAXV], ai[MAXV];
-#pragma unroll
-    for (int i = 0; i < MAXV; ++i) ar[i] = ai[i] = A(0);
-    A nr = A(0);
-    for (int k = blk * chunk + threadIdx.x; k < k1; k += KB) {
-        Cx<T> w = W[base + k];
-        A sr = A(0), si = A(0);
-#pragma unroll
-        for (int i = 0; i < MAXV; ++i) {
-            if (i < nv) {
-                const Cx<T> v = V[(size_t)i * vstride + base + k];
-                const A hr = hsa[0][i], hi = hsa[1][i];
-                sr += hr * (A)v.re - hi * (A)v.im;
-                si += hr * (A)v.im + hi * (A)v.re;
-            }
-        }
-        w.re = (T)((A)w.re - sr);
-        w.im = (T)((A)w.im - si);
-        W[base + k] = w;
-        if (DOTS) {
-            // second read of V_i[k]: the line was just fetched, served by L1
-#pragma unroll
-            for (int i = 0; i < MAXV; ++i) {
-                if (i < nv) {
-                    const Cx<T> v = V[(size_t)i * vstride + base + k];
-                    ar[i] += (A)v.re * (A)w.re + (A)v.im * (A)w.im;
-                    ai[i] += (A)v.re * (A)w.im - (A)v.im * (A)w.re;
-                }
-            }
-        } else {
-            nr += (A)w.re * (A)w.re + (A)w.im * (A)w.im;
-        }
-    }
-    if (DOTS) {
-        block_reduce_write<A>(ar, ai, nv, partial + ((size_t)r * nblk + blk), (size_t)nrhs * nblk);
-    } else {
-        A a1[MAXV], a2[MAXV];
-        a1[0] = nr;
-        a2[0] = A(0);
-        block_reduce_write<A>(a1, a2, 1, partial + ((size_t)r * nblk + blk), (size_t)nrhs * nblk);
     }
 }
 
@@ -1180,25 +1050,6 @@ __global__ void __launch_bounds__(32 * BS_WARPS) k_backsolve_f32(GmresDev s)
     if (lane < m) s.y[(size_t)lane * s.nrhs + r] = make_double2((double)yl.x, (double)yl.y);
 }
 
-// X[r][k] += sum_{i < jlen[r]} y[i][r] V_i[r][k]
-template <typename T>
-__global__ void k_update_x(const Cx<T>* __restrict__ V, size_t vstride, int nvmax, const double2* __restrict__ y,
-                           const int* __restrict__ jlen, double2* __restrict__ X, int n, int nrhs)
-{
-    const int r = blockIdx.y;
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    int jl = min(jlen[r], nvmax);
-    size_t o = (size_t)r * n + k;
-    double2 x = X[o];
-    for (int i = 0; i < jl; ++i) {
-        double2 yi = y[(size_t)i * nrhs + r];
-        double2 v = ld2(V + (size_t)i * vstride + o);
-        x.x += yi.x * v.x - yi.y * v.y;
-        x.y += yi.x * v.y + yi.y * v.x;
-    }
-    X[o] = x;
-}
 
 // R = B - Y (all complex128; B may be complex64)
 template <typename TB>
