@@ -133,7 +133,7 @@ def run_emfa(args, workload):
     dirs = api.monostatic_dirs(ang)
     fp = api.fill_params("cfie", "f32", freq, alpha)
     sp = api.solver_params("gmres", restart=30, max_iter=900, tol=1e-6, matvec=args.matvec, orth=args.orth,
-                           inner_reduction=args.inner_reduction)
+                           inner_reduction=args.inner_reduction, basis=args.basis)
     stream = torch.cuda.ExternalStream(ctx.stream_ptr())
     Z = torch.empty((n, n), dtype=torch.complex64, device="cuda")
     V = torch.empty((n_inc, n), dtype=torch.complex64, device="cuda")
@@ -700,6 +700,8 @@ def main():
     ap.add_argument("--matvec", default="auto", choices=["auto", "f32", "tf32", "f16x"])
     ap.add_argument("--check", type=int, default=1)
     ap.add_argument("--orth", default="auto", choices=["auto", "cgs1", "cgs2", "cgs1_split", "cgs1_fused"])
+    ap.add_argument("--basis", default="auto", choices=["auto", "f32", "f16"],
+                    help="GMRES basis storage of the FP32 inner solve")
     ap.add_argument("--inner-reduction", type=float, default=0.0,
                     help="GMRES refinement: per-cycle inner reduction (0 = the solver's default, <0 = none)")
     ap.add_argument("--cpu-baseline", type=int, default=1)
@@ -752,7 +754,8 @@ def main():
         "latency_ms": {"p50": round(res["p50"], 3), "p99": round(res["p99"], 3)},
         "stages_ms": {k: round(v, 3) for k, v in res["stages"].items()},
         "solver": {"iterations": res["infos"][-1][0], "cycles": res["infos"][-1][1],
-                   "converged": res["infos"][-1][2], "max_rel_residual": res["infos"][-1][3]},
+                   "converged": res["infos"][-1][2], "max_rel_residual": res["infos"][-1][3],
+                   "orth": args.orth, "basis": args.basis},
         "e2e": {k: (round(v, 3) if isinstance(v, float) else v) for k, v in res["e2e"].items()},
         "gpu_launches": res["launches"],
         "gpu_launches_per_step": res["launches"] // max(1, args.steps),

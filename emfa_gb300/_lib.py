@@ -33,7 +33,8 @@ class FillParams(ctypes.Structure):
 class SolverParams(ctypes.Structure):
     _fields_ = [("method", ctypes.c_int), ("restart", ctypes.c_int), ("max_iter", ctypes.c_int),
                 ("tol", ctypes.c_double), ("tol_absolute", ctypes.c_int), ("matvec", ctypes.c_int),
-                ("max_refine", ctypes.c_int), ("orth", ctypes.c_int), ("inner_reduction", ctypes.c_double)]
+                ("max_refine", ctypes.c_int), ("orth", ctypes.c_int), ("inner_reduction", ctypes.c_double),
+                ("basis", ctypes.c_int)]
 
 
 class MlfmaParams(ctypes.Structure):

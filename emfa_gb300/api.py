@@ -47,12 +47,13 @@ def fill_params(kind="cfie", precision="f32", freq=3e8, alpha=0.5, sigma=(0.0, 0
 
 
 def solver_params(method="gmres", restart=30, max_iter=600, tol=1e-6, tol_absolute=False, matvec="auto",
-                  max_refine=0, orth="auto", inner_reduction=0.0) -> L.SolverParams:
+                  max_refine=0, orth="auto", inner_reduction=0.0, basis="auto") -> L.SolverParams:
     mv = {"auto": 0, "f64": 1, "f32": 2, "tf32": 3, "f16x": 4}[matvec]
     og = {"auto": 0, "cgs1": 1, "cgs2": 2, "cgs1_split": 3, "cgs1_fused": 4}[orth]
+    bs = {"auto": 0, "f32": 1, "f16": 2}[basis]
     meth = {"gmres": L.EMFA_GMRES, "bicgstab": L.EMFA_BICGSTAB, "lu": L.EMFA_LU}[method]
     return L.SolverParams(meth, int(restart), int(max_iter), float(tol), int(bool(tol_absolute)), mv, int(max_refine),
-                          og, float(inner_reduction))
+                          og, float(inner_reduction), bs)
 
 
 class Context:

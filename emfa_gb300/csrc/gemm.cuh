@@ -62,6 +62,9 @@ struct HPack {
 };
 emfa_status_t hgemm_pack_target(Ctx* c, const HPlanes& h, int nrhs, HPack* out);
 emfa_status_t hgemm_apply_packed(Ctx* c, const HPlanes& h, const HPack& p, void* Y, int nrhs, cudaStream_t st);
+// packs X (complex64, RHS-major) into the rows p names, with the scale of
+// each right-hand side from its max |Re|, |Im| (the packing hgemm_apply does)
+emfa_status_t hgemm_pack(Ctx* c, const HPlanes& h, const void* X, const HPack& p, int nrhs, cudaStream_t st);
 // exponent e of the FP16 scale t = 2^(14 - e) of v = scale w, from wmax =
 // max |Re|, |Im| of w: max |t v| < 2^14 (the FP32 rounding of scale can raise
 // max |v| by an ulp, hence the factor)
@@ -122,6 +125,9 @@ struct LinOp {
     // producer has written there
     virtual bool pack_target(Ctx*, int, HPack*) { return false; }
     virtual emfa_status_t apply_packed(Ctx*, const HPack&, void*, int, cudaStream_t) { return EMFA_ERR_UNSUPPORTED; }
+    // packs X into rows of the layout pack_target gives, at p.bh / p.inv_t
+    // (with p.ldh from pack_target): the FP16 basis of GMRES
+    virtual emfa_status_t pack(Ctx*, const void*, const HPack&, int, cudaStream_t) { return EMFA_ERR_UNSUPPORTED; }
 };
 
 emfa_status_t solve_op(Ctx* c, LinOp& A, const void* B, int nrhs, void* X, const emfa_solver_params_t* sp,

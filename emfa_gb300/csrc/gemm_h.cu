@@ -892,6 +892,14 @@ emfa_status_t hgemm_apply_packed(Ctx* c, const HPlanes& h, const HPack& p, void*
     return hgemm_run(c, h, p.bh, p.inv_t, Y, nrhs, err, st, p.skip);
 }
 
+emfa_status_t hgemm_pack(Ctx* c, const HPlanes& h, const void* X, const HPack& p, int nrhs, cudaStream_t st)
+{
+    if (!p.bh || !p.inv_t || p.ldh != h.ldh) return EMFA_ERR_INVALID;
+    th::k_hpack_f32<<<nrhs, 256, 0, st>>>((const float2*)X, h.n, h.ldh, p.bh, p.inv_t);
+    c->kernel_launches += 1;
+    return EMFA_OK;
+}
+
 emfa_status_t hgemm_residual(Ctx* c, const HPlanes& h, const double2* X, const void* B, bool b_is_f32, double2* R,
                              int nrhs, cudaStream_t st)
 {

@@ -394,6 +394,325 @@ __global__ void k_update_x2(const Cx<T>* __restrict__ V, size_t vstride, int nvm
     X[o] = make_double2(x.x + (double)sr, x.y + (double)si);
 }
 
+// ---------------------------------------------------------------------------
+// The same three passes on an FP16 basis: the operand rows of the split-FP16
+// product.  Basis vector i of right-hand side r is row 2r of plane i (planes
+// `plane` halves apart, rows `ldh` halves apart): the pairs (Re, -Im) of
+// t v_i in FP16, t = 1 / inv_t[i nrhs + r] a power of two.  A stored pair c
+// is conj(t v), so h = conj(v) w is inv_t sum c w and v = inv_t conj(c).
+// The product multiplied exactly these vectors, so the Arnoldi relation
+// holds for them; each read moves 4 bytes an element instead of 8.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ const __half2* hrow(const __half* Bh, size_t plane, size_t ldh, int i, int r)
+{
+    return reinterpret_cast<const __half2*>(Bh + (size_t)i * plane + (size_t)(2 * r) * ldh);
+}
+
+// unpacks two FP16 values (one stored pair) to FP32
+__device__ __forceinline__ float2 h2f(unsigned int u)
+{
+    __half2 h;
+    memcpy(&h, &u, sizeof(h));
+    return __half22float2(h);
+}
+
+// PAIR (even N): lanes take element pairs, so that a warp's load moves 256
+// bytes of the basis (8 a lane) and 512 of W, as many bytes in flight as the
+// FP32 basis's loads; odd N takes single elements.  Measured on the dense
+// CFIE job (7680 x 360, 50 launches): single elements 3.33 ms, latency-bound
+// at 23 % of DRAM cycles; pairs 1.48 ms; the FP32 basis 1.88 ms
+template <bool PAIR>
+__global__ void __launch_bounds__(256) k_vdots_h(const __half* __restrict__ Bh, size_t plane, size_t ldh,
+                                                 const float* __restrict__ inv_t, int nv,
+                                                 const float2* __restrict__ W, int n, int nrhs, int nblk,
+                                                 double2* __restrict__ partial, int* __restrict__ reset,
+                                                 const int* __restrict__ active)
+{
+    const int blk = blockIdx.x, r = blockIdx.y;
+    griddep_wait();
+    if (reset && blk == 0 && r == 0 && threadIdx.x == 0) *reset = 0;
+    if (active && !active[r]) return;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const float2* w = W + (size_t)r * n;
+    const int k0 = blk * VCHUNK, k1 = min(n, k0 + VCHUNK);
+    for (int i = warp; i < nv; i += 16) {
+        const bool two = i + 8 < nv;
+        const __half2* va = hrow(Bh, plane, ldh, i, r);
+        const __half2* vb = hrow(Bh, plane, ldh, two ? i + 8 : i, r);
+        float re = 0.f, im = 0.f, re2 = 0.f, im2 = 0.f;
+        if (PAIR) {
+            // element pairs [p0, p1): N even, so every pair is whole, rows
+            // start 16-byte aligned and W's pairs 16-byte aligned
+            const uint2* pa = reinterpret_cast<const uint2*>(va);
+            const uint2* pb = reinterpret_cast<const uint2*>(vb);
+            const float4* w4 = reinterpret_cast<const float4*>(w);
+            const int p0 = k0 >> 1, p1 = k1 >> 1;
+            for (int p = p0 + lane; p < p1; p += 128) {
+                uint2 a[4], b[4];
+                float4 x[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int pp = p + 32 * u;
+                    const bool in = pp < p1;
+                    a[u] = in ? pa[pp] : make_uint2(0u, 0u);
+                    b[u] = in && two ? pb[pp] : make_uint2(0u, 0u);
+                    x[u] = in ? w4[pp] : make_float4(0.f, 0.f, 0.f, 0.f);
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const float2 a0 = h2f(a[u].x), a1 = h2f(a[u].y), b0 = h2f(b[u].x), b1 = h2f(b[u].y);
+                    re += a0.x * x[u].x - a0.y * x[u].y + a1.x * x[u].z - a1.y * x[u].w;
+                    im += a0.x * x[u].y + a0.y * x[u].x + a1.x * x[u].w + a1.y * x[u].z;
+                    re2 += b0.x * x[u].x - b0.y * x[u].y + b1.x * x[u].z - b1.y * x[u].w;
+                    im2 += b0.x * x[u].y + b0.y * x[u].x + b1.x * x[u].w + b1.y * x[u].z;
+                }
+            }
+        } else {
+            for (int k = k0 + lane; k < k1; k += 128) {
+                float2 a[4], b[4], x[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int kk = k + 32 * u;
+                    const bool in = kk < k1;
+                    a[u] = in ? __half22float2(va[kk]) : make_float2(0.f, 0.f);
+                    b[u] = in && two ? __half22float2(vb[kk]) : make_float2(0.f, 0.f);
+                    x[u] = in ? w[kk] : make_float2(0.f, 0.f);
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    re += a[u].x * x[u].x - a[u].y * x[u].y;
+                    im += a[u].x * x[u].y + a[u].y * x[u].x;
+                    re2 += b[u].x * x[u].x - b[u].y * x[u].y;
+                    im2 += b[u].x * x[u].y + b[u].y * x[u].x;
+                }
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            re += __shfl_xor_sync(0xffffffffu, re, o);
+            im += __shfl_xor_sync(0xffffffffu, im, o);
+            re2 += __shfl_xor_sync(0xffffffffu, re2, o);
+            im2 += __shfl_xor_sync(0xffffffffu, im2, o);
+        }
+        if (lane == 0) {
+            const float s = inv_t[(size_t)i * nrhs + r];  // a power of two: exact
+            partial[((size_t)i * nrhs + r) * nblk + blk] = make_double2((double)(re * s), (double)(im * s));
+            if (two) {
+                const float s2 = inv_t[(size_t)(i + 8) * nrhs + r];
+                partial[((size_t)(i + 8) * nrhs + r) * nblk + blk] = make_double2((double)(re2 * s2), (double)(im2 * s2));
+            }
+        }
+    }
+    griddep_launch();
+}
+
+// W -= sum_i h_i v_i with |W|^2 and max |Re|, |Im| partials (k_vupdate<float,
+// true> on the FP16 basis): the coefficients are summed from the block
+// partials, block 0 stores them in h, and each is taken times inv_t once.
+// PAIR (even N): a thread holds two element pairs (16-byte W accesses) and
+// loads 4 basis vectors a group, 8 bytes each (40 registers, six CTAs an SM).
+// Measured on the dense CFIE job (7680 x 360): 11.10 ms a solve, against
+// 11.19 with single elements and 11.32 with 8 vectors a group
+template <bool PAIR>
+__global__ void __launch_bounds__(256) k_vupdate_h(const __half* __restrict__ Bh, size_t plane, size_t ldh,
+                                                   const float* __restrict__ inv_t, int nv, double2* __restrict__ h,
+                                                   const double2* __restrict__ partial, float2* __restrict__ W, int n,
+                                                   int nrhs, int nblk, double2* __restrict__ pnorm,
+                                                   const int* __restrict__ active)
+{
+    const int blk = blockIdx.x, r = nrhs - 1 - (int)blockIdx.y;
+    griddep_wait();
+    if (active && !active[r]) return;
+    const size_t base = (size_t)r * n;
+    extern __shared__ unsigned char dyn_smem[];
+    float* hs0 = reinterpret_cast<float*>(dyn_smem);
+    float* hs1 = hs0 + nv;
+    __shared__ float red[8], redm[8];
+    for (int i = threadIdx.x; i < nv; i += blockDim.x) {
+        const double2* p = partial + ((size_t)i * nrhs + r) * nblk;
+        float tx = 0.f, ty = 0.f;
+        for (int b = 0; b < nblk; ++b) {
+            tx += (float)p[b].x;
+            ty += (float)p[b].y;
+        }
+        if (blk == 0) h[(size_t)i * nrhs + r] = make_double2((double)tx, (double)ty);
+        const float s = inv_t[(size_t)i * nrhs + r];
+        hs0[i] = tx * s;
+        hs1[i] = ty * s;
+    }
+    __syncthreads();
+    float nr = 0.f, mx = 0.f;
+    const int k0 = blk * VCHUNK, k1 = min(n, k0 + VCHUNK);
+    if (PAIR) {
+        constexpr int EP = VCHUNK / 512, VG = 4;
+        const int p0 = k0 >> 1, p1 = k1 >> 1;
+        float4* w4 = reinterpret_cast<float4*>(W + base);
+        int pc[EP];
+        float4 w[EP];
+#pragma unroll
+        for (int e = 0; e < EP; ++e) {
+            pc[e] = min(p0 + (int)threadIdx.x + 256 * e, p1 - 1);
+            w[e] = w4[pc[e]];
+        }
+        float sr[EP][2], si[EP][2];
+#pragma unroll
+        for (int e = 0; e < EP; ++e) sr[e][0] = sr[e][1] = si[e][0] = si[e][1] = 0.f;
+        for (int i = 0; i < nv; i += VG) {
+            uint2 v[VG][EP];
+#pragma unroll
+            for (int u = 0; u < VG; ++u) {
+                const uint2* vi = reinterpret_cast<const uint2*>(hrow(Bh, plane, ldh, min(i + u, nv - 1), r));
+#pragma unroll
+                for (int e = 0; e < EP; ++e) v[u][e] = vi[pc[e]];
+            }
+#pragma unroll
+            for (int u = 0; u < VG; ++u) {
+                const bool ok = i + u < nv;
+                const float hr = ok ? hs0[i + u] : 0.f, hi = ok ? hs1[i + u] : 0.f;
+#pragma unroll
+                for (int e = 0; e < EP; ++e) {
+                    const float2 c0 = h2f(v[u][e].x), c1 = h2f(v[u][e].y);
+                    sr[e][0] += hr * c0.x + hi * c0.y;
+                    si[e][0] += hi * c0.x - hr * c0.y;
+                    sr[e][1] += hr * c1.x + hi * c1.y;
+                    si[e][1] += hi * c1.x - hr * c1.y;
+                }
+            }
+        }
+#pragma unroll
+        for (int e = 0; e < EP; ++e) {
+            const int p = p0 + (int)threadIdx.x + 256 * e;
+            if (p >= p1) continue;
+            w[e].x -= sr[e][0];
+            w[e].y -= si[e][0];
+            w[e].z -= sr[e][1];
+            w[e].w -= si[e][1];
+            w4[p] = w[e];
+            nr += w[e].x * w[e].x + w[e].y * w[e].y + w[e].z * w[e].z + w[e].w * w[e].w;
+            mx = fmaxf(mx, fmaxf(fmaxf(fabsf(w[e].x), fabsf(w[e].y)), fmaxf(fabsf(w[e].z), fabsf(w[e].w))));
+        }
+    } else {
+        constexpr int EL = VCHUNK / 256, VG = 4;
+        int kc[EL];
+        float2 w[EL];
+#pragma unroll
+        for (int e = 0; e < EL; ++e) {
+            kc[e] = min(k0 + (int)threadIdx.x + 256 * e, k1 - 1);
+            w[e] = W[base + kc[e]];
+        }
+        float sr[EL], si[EL];
+#pragma unroll
+        for (int e = 0; e < EL; ++e) sr[e] = si[e] = 0.f;
+        for (int i = 0; i < nv; i += VG) {
+            float2 v[VG][EL];
+#pragma unroll
+            for (int u = 0; u < VG; ++u) {
+                const __half2* vi = hrow(Bh, plane, ldh, min(i + u, nv - 1), r);
+#pragma unroll
+                for (int e = 0; e < EL; ++e) v[u][e] = __half22float2(vi[kc[e]]);
+            }
+#pragma unroll
+            for (int u = 0; u < VG; ++u) {
+                const bool ok = i + u < nv;
+                const float hr = ok ? hs0[i + u] : 0.f, hi = ok ? hs1[i + u] : 0.f;
+#pragma unroll
+                for (int e = 0; e < EL; ++e) {
+                    // h v with v = conj(c)
+                    sr[e] += hr * v[u][e].x + hi * v[u][e].y;
+                    si[e] += hi * v[u][e].x - hr * v[u][e].y;
+                }
+            }
+        }
+#pragma unroll
+        for (int e = 0; e < EL; ++e) {
+            const int k = k0 + (int)threadIdx.x + 256 * e;
+            if (k >= k1) continue;
+            w[e].x -= sr[e];
+            w[e].y -= si[e];
+            W[base + k] = w[e];
+            nr += w[e].x * w[e].x + w[e].y * w[e].y;
+            mx = fmaxf(mx, fmaxf(fabsf(w[e].x), fabsf(w[e].y)));
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        nr += __shfl_xor_sync(0xffffffffu, nr, o);
+        mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        red[threadIdx.x >> 5] = nr;
+        redm[threadIdx.x >> 5] = mx;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float t = 0.f, tm = 0.f;
+        for (int q = 0; q < (int)(blockDim.x >> 5); ++q) {
+            t += red[q];
+            tm = fmaxf(tm, redm[q]);
+        }
+        pnorm[(size_t)r * nblk + blk] = make_double2((double)t, (double)tm);
+    }
+    griddep_launch();
+}
+
+// X[r][k] += sum_i y_i v_i on the FP16 basis, the sum in FP32.  A thread
+// takes an element pair (PAIR, even N) or one element, four basis vectors a
+// group of loads
+template <bool PAIR>
+__global__ void k_update_x2_h(const __half* __restrict__ Bh, size_t plane, size_t ldh, const float* __restrict__ inv_t,
+                              int nvmax, const double2* __restrict__ y, const int* __restrict__ jlen,
+                              double2* __restrict__ X, int n, int nrhs)
+{
+    const int r = blockIdx.y;
+    extern __shared__ unsigned char dyn_smem[];
+    float* ys0 = reinterpret_cast<float*>(dyn_smem);
+    float* ys1 = ys0 + nvmax;
+    const int jl = min(jlen[r], nvmax);
+    for (int i = threadIdx.x; i < jl; i += blockDim.x) {
+        const double2 t = y[(size_t)i * nrhs + r];
+        const float s = inv_t[(size_t)i * nrhs + r];
+        ys0[i] = (float)t.x * s;
+        ys1[i] = (float)t.y * s;
+    }
+    __syncthreads();
+    constexpr int NE = PAIR ? 2 : 1, VG = 4;
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;  // element (pair)
+    if (q * NE >= n) return;
+    float sr[NE], si[NE];
+#pragma unroll
+    for (int e = 0; e < NE; ++e) sr[e] = si[e] = 0.f;
+    for (int i = 0; i < jl; i += VG) {
+        float2 c[VG][NE];
+#pragma unroll
+        for (int u = 0; u < VG; ++u) {
+            const __half2* row = hrow(Bh, plane, ldh, min(i + u, jl - 1), r);
+            if (PAIR) {
+                const uint2 v = reinterpret_cast<const uint2*>(row)[q];
+                c[u][0] = h2f(v.x);
+                c[u][NE - 1] = h2f(v.y);
+            } else {
+                c[u][0] = __half22float2(row[q]);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < VG; ++u) {
+            const bool ok = i + u < jl;
+            const float a = ok ? ys0[i + u] : 0.f, b = ok ? ys1[i + u] : 0.f;
+#pragma unroll
+            for (int e = 0; e < NE; ++e) {
+                sr[e] += a * c[u][e].x + b * c[u][e].y;
+                si[e] += b * c[u][e].x - a * c[u][e].y;
+            }
+        }
+    }
+#pragma unroll
+    for (int e = 0; e < NE; ++e) {
+        const size_t o = (size_t)r * n + (size_t)q * NE + e;
+        const double2 x = X[o];
+        X[o] = make_double2(x.x + (double)sr[e], x.y + (double)si[e]);
+    }
+}
+
 // per-RHS: finish Arnoldi column j, rotate, test convergence.  A serial FP64
 // chain per right-hand side: one RHS per warp (lane 0) spreads the chains
 // over the SMs' FP64 units instead of packing 32 of them into one warp.
@@ -661,7 +980,8 @@ __global__ void k_arnoldi_finish_warp(GmresDev s, int j, const double2* __restri
 // the other warps pack: the column's serial chain (FP32) overlaps the stream.
 // A right-hand side that this step finds converged is normalised all the
 // same (its V_{j+1} lies past its basis length); one that was already
-// inactive writes nothing.
+// inactive writes nothing.  On the FP16 basis Vout is null: the packed rows
+// (plane j + 1 of the basis) are V_{j+1}.
 constexpr int FP_CHUNK = 4096;
 
 __global__ void __launch_bounds__(256) k_finish_pack(GmresDev s, int j, const double2* __restrict__ pnorm, int nblk,
@@ -707,7 +1027,7 @@ __global__ void __launch_bounds__(256) k_finish_pack(GmresDev s, int j, const do
     }
     const float sc = nscale[0], t = nscale[1];
     const float2* w = W + (size_t)r * n;
-    float2* v = Vout + (size_t)r * n;
+    float2* v = Vout ? Vout + (size_t)r * n : nullptr;
     __half2* h0 = pk.bh ? reinterpret_cast<__half2*>(pk.bh + (size_t)(2 * r) * pk.ldh) : nullptr;
     __half2* h1 = pk.bh ? reinterpret_cast<__half2*>(pk.bh + (size_t)(2 * r + 1) * pk.ldh) : nullptr;
     const int k1 = min(n, (chunk + 1) * FP_CHUNK), off = column ? 32 : 0;
@@ -715,7 +1035,7 @@ __global__ void __launch_bounds__(256) k_finish_pack(GmresDev s, int j, const do
     for (int k = chunk * FP_CHUNK + tid - off; k < k1; k += blockDim.x - off) {
         const float2 x = w[k];
         const float2 y = make_float2(x.x * sc, x.y * sc);
-        v[k] = y;
+        if (v) v[k] = y;
         if (h0) {
             const __half hre = __float2half_rn(t * y.x), him = __float2half_rn(t * y.y);
             h0[k] = __halves2half2(hre, __hneg(him));
@@ -1192,8 +1512,34 @@ static emfa_status_t gmres_t(Ctx* c, LinOp& A, const void* B, int nrhs, double2*
     const int nblk = std::max(1, std::min((2 * sms + nrhs - 1) / nrhs, (n + 4 * KB - 1) / (4 * KB)));
     const int chunk = (n + nblk - 1) / nblk;
     const int vblk = (n + VCHUNK - 1) / VCHUNK;  // chunks of the Gram-Schmidt passes
+    // the FP32 inner solve of the refinement only has to gain a few digits per
+    // cycle: one Gram-Schmidt pass; the plain FP64 path keeps two
+    const bool two_pass = sp->orth == 2 || (sp->orth == 0 && prec == EMFA_F64);
+    // CGS1 on an FP32 basis: one fused launch per Arnoldi step (k_arnoldi_step)
+    // where the restart and N fit it and its clusters fill at most about two
+    // waves of CTAs; orth 3 keeps the separate passes.  Measured GMRES(30)
+    // solves (split-FP16 products, 18 steps): fused 10-15 % faster for 1 to
+    // 64 right-hand sides at N = 2000, 4000 and 7680; 4-8 % slower for 360,
+    // where the separate passes' thousands of independent CTAs hide memory
+    // latency better than two staged CTAs an SM between cluster barriers.
+    const StepShape sh = step_shape(n);
+    // orth 4 takes the fused step whatever the grid size (for measurement)
+    const bool fused = std::is_same<T, float>::value && !two_pass && sp->orth != 3 && m <= AS_MAXV && sh.e > 0 &&
+                       ((long)nrhs * sh.cs <= 4L * sms || sp->orth == 4);
+    // separate passes on an FP32 basis with one Gram-Schmidt pass end in
+    // k_finish_pack (column, normalisation and packing in one launch)
+    const bool finish_pack = std::is_same<T, float>::value && !fused && !two_pass && m <= 32;
+    // ... and keep the basis as the product's FP16 operand rows where the
+    // operator packs its input (unless basis = 1): m + 1 planes of the
+    // layout pack_target gives
+    HPack pk0;
+    const bool hbasis = finish_pack && sp->basis != 1 && A.pack_target(c, nrhs, &pk0);
+    const size_t hplane = hbasis ? pk0.ldh * 2 * (size_t)nrhs : 0;  // halves
+    const size_t vslots = hbasis ? 1 : (size_t)(m + 1);
     // one workspace for the whole solve (reused across solves of a context)
-    const size_t need = Carver::round(sizeof(Cx<T>) * vec * (m + 1)) + Carver::round(sizeof(Cx<T>) * vec) +
+    const size_t need = Carver::round(sizeof(Cx<T>) * vec * vslots) + Carver::round(sizeof(Cx<T>) * vec) +
+                        Carver::round(sizeof(__half) * hplane * (m + 1)) +
+                        Carver::round(sizeof(float) * (size_t)nrhs * (m + 1)) +
                         Carver::round(sizeof(double2) * vec) + Carver::round(sizeof(float2) * vec) +
                         Carver::round(sizeof(double2) * (size_t)nrhs * (m + 1) * m) +
                         Carver::round(sizeof(double) * (size_t)nrhs * m) +
@@ -1206,8 +1552,10 @@ static emfa_status_t gmres_t(Ctx* c, LinOp& A, const void* B, int nrhs, double2*
     void* wsp = nullptr;
     EMFA_TRY(ctx_workspace(c, WS_KRYLOV, need, &wsp));
     Carver cv{(char*)wsp};
-    Cx<T>* V = cv.take<Cx<T>>(vec * (m + 1));
+    Cx<T>* V = cv.take<Cx<T>>(vec * vslots);
     Cx<T>* W = cv.take<Cx<T>>(vec);
+    __half* Bh = cv.take<__half>(hplane * (m + 1));     // FP16 basis planes (hbasis)
+    float* inv_tb = cv.take<float>((size_t)nrhs * (m + 1));  //   and their per-RHS scales
     double2* R = cv.take<double2>(vec);
     float2* Xt = cv.take<float2>(vec);
     GmresDev s;
@@ -1247,23 +1595,6 @@ static emfa_status_t gmres_t(Ctx* c, LinOp& A, const void* B, int nrhs, double2*
     EMFA_CUDA(c, cudaMemsetAsync(X, 0, sizeof(double2) * vec, st));
     int max_cycles = sp->max_iter > 0 ? (sp->max_iter + m - 1) / m : 100;
     if (prec == EMFA_F32 && sp->max_refine > 0) max_cycles = std::min(max_cycles, sp->max_refine);
-    // the FP32 inner solve of the refinement only has to gain a few digits per
-    // cycle: one Gram-Schmidt pass; the plain FP64 path keeps two
-    const bool two_pass = sp->orth == 2 || (sp->orth == 0 && prec == EMFA_F64);
-    // CGS1 on an FP32 basis: one fused launch per Arnoldi step (k_arnoldi_step)
-    // where the restart and N fit it and its clusters fill at most about two
-    // waves of CTAs; orth 3 keeps the separate passes.  Measured GMRES(30)
-    // solves (split-FP16 products, 18 steps): fused 10-15 % faster for 1 to
-    // 64 right-hand sides at N = 2000, 4000 and 7680; 4-8 % slower for 360,
-    // where the separate passes' thousands of independent CTAs hide memory
-    // latency better than two staged CTAs an SM between cluster barriers.
-    const StepShape sh = step_shape(n);
-    // orth 4 takes the fused step whatever the grid size (for measurement)
-    const bool fused = std::is_same<T, float>::value && !two_pass && sp->orth != 3 && m <= AS_MAXV && sh.e > 0 &&
-                       ((long)nrhs * sh.cs <= 4L * sms || sp->orth == 4);
-    // separate passes on an FP32 basis with one Gram-Schmidt pass end in
-    // k_finish_pack (column, normalisation and packing in one launch)
-    const bool finish_pack = std::is_same<T, float>::value && !fused && !two_pass && m <= 32;
     int total_iters = 0, cycles = 0, converged = 0;
     int host_cnt[4];
     // Arnoldi steps are checked one step late: step j and the operator
@@ -1311,12 +1642,16 @@ static emfa_status_t gmres_t(Ctx* c, LinOp& A, const void* B, int nrhs, double2*
         converged = host_cnt[1];
         if (host_cnt[0] == 0) break;
         ++cycles;
-        // V0 = R / beta
-        k_scale_store<Cx<T>, double2><<<dim3((n + 1023) / 1024, nrhs), 256, 0, st>>>(R, s.scale, n, nrhs, V);
+        // V0 = R / beta (on the FP16 basis: through W into plane 0, packed as
+        // the product packs its input)
+        const HPack p0{Bh, inv_tb, pk0.ldh, nullptr};
+        k_scale_store<Cx<T>, double2><<<dim3((n + 1023) / 1024, nrhs), 256, 0, st>>>(R, s.scale, n, nrhs,
+                                                                                     hbasis ? W : V);
+        if (hbasis) EMFA_TRY(A.pack(c, W, p0, nrhs, st));
         int steps = 0;
         for (int j = 0; j < m; ++j) {
             // W = A V_j (for j > 0 done by normalize_apply at the end of the previous step)
-            if (j == 0) EMFA_TRY(A.apply(c, V, W, nrhs, st));
+            if (j == 0) EMFA_TRY(hbasis ? A.apply_packed(c, p0, W, nrhs, st) : A.apply(c, V, W, nrhs, st));
             // CGS1: h = V^H W; W -= V h with |W|^2.  CGS2 repeats the pair
             // (h2 = V^H W; W -= V h2) and H gets h + h2.
             const dim3 vg(vblk, nrhs);
@@ -1330,6 +1665,10 @@ static emfa_status_t gmres_t(Ctx* c, LinOp& A, const void* B, int nrhs, double2*
             if (normalises) {
                 packs = A.pack_target(c, nrhs, &pk);
                 if (!packs) pk = HPack{};
+                if (hbasis) {  // V_{j+1} is plane j + 1
+                    pk.bh = Bh + (size_t)(j + 1) * hplane;
+                    pk.inv_t = inv_tb + (size_t)(j + 1) * nrhs;
+                }
                 // the next product skips itself if this step leaves nothing active
                 pk.skip = s.step_cnt;
             }
@@ -1347,6 +1686,20 @@ static emfa_status_t gmres_t(Ctx* c, LinOp& A, const void* B, int nrhs, double2*
                     // product -> coefficients -> update -> finish: each launch may
                     // be resident before its predecessor ends (griddep_wait); the
                     // coefficients pass zeroes the step's active count
+                    if (hbasis) {
+                        EMFA_CUDA(c, launch_dependent(n % 2 ? k_vdots_h<false> : k_vdots_h<true>, vg, dim3(256), 0,
+                                                      st, (const __half*)Bh, hplane,
+                                                      pk0.ldh, (const float*)inv_tb, nv, (const float2*)W, n, nrhs,
+                                                      vblk, partial, s.step_cnt, (const int*)s.active));
+                        EMFA_CUDA(c, launch_dependent(n % 2 ? k_vupdate_h<false> : k_vupdate_h<true>, vg, dim3(256),
+                                                      2 * nv * sizeof(float), st,
+                                                      (const __half*)Bh, hplane, pk0.ldh, (const float*)inv_tb, nv,
+                                                      s.hcol, (const double2*)partial, (float2*)W, n, nrhs, vblk,
+                                                      pnorm, (const int*)s.active));
+                        EMFA_CUDA(c, launch_dependent(k_finish_pack, dim3((n + FP_CHUNK - 1) / FP_CHUNK, nrhs),
+                                                      dim3(256), 0, st, s, j, (const double2*)pnorm, vblk,
+                                                      (const float2*)W, n, (float2*)nullptr, pk));
+                    } else {
                     EMFA_CUDA(c, launch_dependent(k_vdots<T>, vg, dim3(256), 0, st, (const Cx<T>*)V, vec, nv,
                                                   (const Cx<T>*)W, n, nrhs, vblk, partial, s.step_cnt,
                                                   (const int*)s.active));
@@ -1356,6 +1709,7 @@ static emfa_status_t gmres_t(Ctx* c, LinOp& A, const void* B, int nrhs, double2*
                     EMFA_CUDA(c, launch_dependent(k_finish_pack, dim3((n + FP_CHUNK - 1) / FP_CHUNK, nrhs), dim3(256),
                                                   0, st, s, j, (const double2*)pnorm, vblk, (const float2*)W, n,
                                                   (float2*)(V + (size_t)(j + 1) * vec), pk));
+                    }
                     c->kernel_launches += 3;
                 } else {
                 k_vdots<T><<<vg, 256, 0, st>>>(V, vec, nv, W, n, nrhs, vblk, partial, nullptr, s.active);
@@ -1408,8 +1762,16 @@ static emfa_status_t gmres_t(Ctx* c, LinOp& A, const void* B, int nrhs, double2*
             k_backsolve_f32<<<(nrhs + BS_WARPS - 1) / BS_WARPS, 32 * BS_WARPS, 0, st>>>(s);
         else
             k_backsolve<<<(nrhs * 32 + 127) / 128, 128, 0, st>>>(s);
-        k_update_x2<T><<<dim3((n + 255) / 256, nrhs), 256, 2 * std::max(1, steps) * sizeof(typename Acc<T>::type), st>>>(
-            V, vec, steps, s.y, s.jlen, X, n, nrhs);
+        if (hbasis && n % 2 == 0)
+            k_update_x2_h<true><<<dim3((n / 2 + 255) / 256, nrhs), 256, 2 * std::max(1, steps) * sizeof(float), st>>>(
+                Bh, hplane, pk0.ldh, inv_tb, steps, s.y, s.jlen, X, n, nrhs);
+        else if (hbasis)
+            k_update_x2_h<false><<<dim3((n + 255) / 256, nrhs), 256, 2 * std::max(1, steps) * sizeof(float), st>>>(
+                Bh, hplane, pk0.ldh, inv_tb, steps, s.y, s.jlen, X, n, nrhs);
+        else
+            k_update_x2<T><<<dim3((n + 255) / 256, nrhs), 256,
+                             2 * std::max(1, steps) * sizeof(typename Acc<T>::type), st>>>(V, vec, steps, s.y, s.jlen,
+                                                                                            X, n, nrhs);
         c->kernel_launches += 2;
         EMFA_CUDA(c, cudaGetLastError());
     }
@@ -1826,6 +2188,11 @@ struct DenseOp : LinOp {
     emfa_status_t apply_packed(Ctx* c, const HPack& p, void* Y, int nrhs, cudaStream_t st) override
     {
         return hgemm_apply_packed(c, hp, p, Y, nrhs, st);
+    }
+    emfa_status_t pack(Ctx* c, const void* X, const HPack& p, int nrhs, cudaStream_t st) override
+    {
+        if (!(prec == EMFA_F32 && mode == F16X)) return EMFA_ERR_UNSUPPORTED;
+        return hgemm_pack(c, hp, X, p, nrhs, st);
     }
     emfa_status_t check(Ctx* c, cudaStream_t st) override
     {

@@ -38,9 +38,9 @@ def _system(n, nrhs, seed):
     return Z, B
 
 
-def _solve(ctx, Z, B, orth, matvec, restart=30):
+def _solve(ctx, Z, B, orth, matvec, restart=30, basis="f32"):
     from emfa_gb300 import api
-    sp = api.solver_params("gmres", restart=restart, tol=1e-6, max_iter=2000, matvec=matvec, orth=orth)
+    sp = api.solver_params("gmres", restart=restart, tol=1e-6, max_iter=2000, matvec=matvec, orth=orth, basis=basis)
     X, info = api.solve(ctx, Z, B, sp)
     return X, info
 
@@ -105,9 +105,9 @@ def test_fused_step_reproducible(ctx):
     assert torch.equal(X1, X2)
 
 
-def _launches(ctx, Z, B, orth):
+def _launches(ctx, Z, B, orth, basis="f32"):
     before = ctx.launches()
-    X, info = _solve(ctx, Z, B, orth, "f16x")
+    X, info = _solve(ctx, Z, B, orth, "f16x", basis=basis)
     return ctx.launches() - before, info
 
 
@@ -133,3 +133,66 @@ def test_auto_choice_by_grid_size(ctx):
     # orth "cgs1_fused" takes the fused step at any grid size, same solution
     n_fused, i_fused = _launches(ctx, Z, B, "cgs1_fused")
     assert abs(i_fused.iterations - i_split.iterations) <= 1 and n_split - n_fused >= 2 * i_fused.iterations
+
+
+# ---------------------------------------------------------------------------
+# FP16 basis (basis "f16", the default where the separate passes feed the
+# split-FP16 product): the basis vectors are the product's own FP16 operand
+# rows, each scaled by a power of two.  Against the FP32 basis: the same
+# target met (true residual 1e-6), iteration counts within 10 % (at least 2),
+# solutions within 1e-5 of each other.
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("n,nrhs,restart", [
+    (300, 40, 30),     # one Gram-Schmidt chunk, one finish chunk
+    (1500, 24, 30),    # a ragged last chunk (1500 = 1024 + 476)
+    (4096, 8, 1),      # restart lengths 1, 2, 7, 32 and 33 (the longest the
+    (4096, 8, 2),      #   FP32-step path of the finish pass takes is 32;
+    (4096, 8, 7),      #   33 runs the unfused finish on the FP32 basis)
+    (4096, 8, 32),
+    (4096, 8, 33),
+    (7680, 360, 30),   # the dense CFIE job's shape
+    (16385, 3, 30),    # N past the fused step
+])
+def test_fp16_basis_matches_fp32_basis(ctx, n, nrhs, restart):
+    import torch
+    Z, B = _system(n, nrhs, seed=n + restart)
+    Xh, ih = _solve(ctx, Z, B, "cgs1_split", "f16x", restart=restart, basis="f16")
+    Xs, i_s = _solve(ctx, Z, B, "cgs1_split", "f16x", restart=restart, basis="f32")
+    assert ih.converged == nrhs and i_s.converged == nrhs
+    assert abs(ih.iterations - i_s.iterations) <= max(2, i_s.iterations // 10), (ih.iterations, i_s.iterations)
+    rh = _true_residual(Z, B, Xh)
+    assert rh.max() < 1e-6, rh.max()
+    zero = nrhs // 2
+    assert torch.count_nonzero(Xh[zero]) == 0
+    d = torch.linalg.norm(Xh - Xs, dim=1) / torch.linalg.norm(Xs, dim=1).clamp_min(1e-300)
+    d[zero] = 0
+    assert d.max().item() < 1e-5, d.max().item()
+
+
+def test_fp16_basis_reproducible_and_launches(ctx):
+    """Fixed-order sums on the FP16 basis: the same solve twice gives the same
+    bits, with as many launches as on the FP32 basis (the first basis vector
+    is packed into the basis instead of the product's own buffer)."""
+    import torch
+    Z, B = _system(7680, 200, seed=5)
+    _solve(ctx, Z, B, "cgs1_split", "f16x", basis="f16")  # tunes the product's tile shape
+    n1, i1 = _launches(ctx, Z, B, "cgs1_split", basis="f16")
+    X1, _ = _solve(ctx, Z, B, "cgs1_split", "f16x", basis="f16")
+    X2, i2 = _solve(ctx, Z, B, "cgs1_split", "f16x", basis="f16")
+    assert i1.iterations == i2.iterations and torch.equal(X1, X2)
+    n32, i32 = _launches(ctx, Z, B, "cgs1_split", basis="f32")
+    if i32.iterations == i1.iterations and i32.cycles == i1.cycles:
+        assert n1 == n32, (n1, n32)
+
+
+@pytest.mark.parametrize("matvec,orth", [("f32", "cgs1_split"), ("tf32", "cgs1_split"), ("f16x", "cgs1"),
+                                         ("f16x", "cgs2")])
+def test_fp16_basis_only_where_the_product_packs(ctx, matvec, orth):
+    """basis "f16" changes nothing where it does not apply: unpacked products,
+    the fused step (few right-hand sides) and two Gram-Schmidt passes keep the
+    FP32 basis, bit for bit."""
+    import torch
+    Z, B = _system(3000, 6, seed=9)
+    X16, i16 = _solve(ctx, Z, B, orth, matvec, basis="f16")
+    X32, i32 = _solve(ctx, Z, B, orth, matvec, basis="f32")
+    assert i16.iterations == i32.iterations and torch.equal(X16, X32)
