@@ -415,13 +415,19 @@ __device__ __forceinline__ float2 h2f(unsigned int u)
     memcpy(&h, &u, sizeof(h));
     return __half22float2(h);
 }
+// the bits of an FP16 pair
+__device__ __forceinline__ unsigned int h2u(__half2 h)
+{
+    unsigned int u;
+    memcpy(&u, &h, sizeof(u));
+    return u;
+}
 
-// PAIR (even N): lanes take element pairs, so that a warp's load moves 256
-// bytes of the basis (8 a lane) and 512 of W, as many bytes in flight as the
-// FP32 basis's loads; odd N takes single elements.  Measured on the dense
-// CFIE job (7680 x 360, 50 launches): single elements 3.33 ms, latency-bound
-// at 23 % of DRAM cycles; pairs 1.48 ms; the FP32 basis 1.88 ms
-template <bool PAIR>
+// Odd N (single elements: 4-byte loads of the basis).  Even N takes
+// k_vdots_hw.  Measured on the dense CFIE job (7680 x 360, 50 launches):
+// this form 3.33 ms, latency-bound at 23 % of DRAM cycles (half the bytes
+// of the FP32 basis's loads in flight); lanes on element pairs 1.48 ms;
+// k_vdots_hw 1.14 ms; the FP32 basis 1.88 ms
 __global__ void __launch_bounds__(256) k_vdots_h(const __half* __restrict__ Bh, size_t plane, size_t ldh,
                                                  const float* __restrict__ inv_t, int nv,
                                                  const float2* __restrict__ W, int n, int nrhs, int nblk,
@@ -440,51 +446,22 @@ __global__ void __launch_bounds__(256) k_vdots_h(const __half* __restrict__ Bh, 
         const __half2* va = hrow(Bh, plane, ldh, i, r);
         const __half2* vb = hrow(Bh, plane, ldh, two ? i + 8 : i, r);
         float re = 0.f, im = 0.f, re2 = 0.f, im2 = 0.f;
-        if (PAIR) {
-            // element pairs [p0, p1): N even, so every pair is whole, rows
-            // start 16-byte aligned and W's pairs 16-byte aligned
-            const uint2* pa = reinterpret_cast<const uint2*>(va);
-            const uint2* pb = reinterpret_cast<const uint2*>(vb);
-            const float4* w4 = reinterpret_cast<const float4*>(w);
-            const int p0 = k0 >> 1, p1 = k1 >> 1;
-            for (int p = p0 + lane; p < p1; p += 128) {
-                uint2 a[4], b[4];
-                float4 x[4];
+        for (int k = k0 + lane; k < k1; k += 128) {
+            float2 a[4], b[4], x[4];
 #pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    const int pp = p + 32 * u;
-                    const bool in = pp < p1;
-                    a[u] = in ? pa[pp] : make_uint2(0u, 0u);
-                    b[u] = in && two ? pb[pp] : make_uint2(0u, 0u);
-                    x[u] = in ? w4[pp] : make_float4(0.f, 0.f, 0.f, 0.f);
-                }
-#pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    const float2 a0 = h2f(a[u].x), a1 = h2f(a[u].y), b0 = h2f(b[u].x), b1 = h2f(b[u].y);
-                    re += a0.x * x[u].x - a0.y * x[u].y + a1.x * x[u].z - a1.y * x[u].w;
-                    im += a0.x * x[u].y + a0.y * x[u].x + a1.x * x[u].w + a1.y * x[u].z;
-                    re2 += b0.x * x[u].x - b0.y * x[u].y + b1.x * x[u].z - b1.y * x[u].w;
-                    im2 += b0.x * x[u].y + b0.y * x[u].x + b1.x * x[u].w + b1.y * x[u].z;
-                }
+            for (int u = 0; u < 4; ++u) {
+                const int kk = k + 32 * u;
+                const bool in = kk < k1;
+                a[u] = in ? __half22float2(va[kk]) : make_float2(0.f, 0.f);
+                b[u] = in && two ? __half22float2(vb[kk]) : make_float2(0.f, 0.f);
+                x[u] = in ? w[kk] : make_float2(0.f, 0.f);
             }
-        } else {
-            for (int k = k0 + lane; k < k1; k += 128) {
-                float2 a[4], b[4], x[4];
 #pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    const int kk = k + 32 * u;
-                    const bool in = kk < k1;
-                    a[u] = in ? __half22float2(va[kk]) : make_float2(0.f, 0.f);
-                    b[u] = in && two ? __half22float2(vb[kk]) : make_float2(0.f, 0.f);
-                    x[u] = in ? w[kk] : make_float2(0.f, 0.f);
-                }
-#pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    re += a[u].x * x[u].x - a[u].y * x[u].y;
-                    im += a[u].x * x[u].y + a[u].y * x[u].x;
-                    re2 += b[u].x * x[u].x - b[u].y * x[u].y;
-                    im2 += b[u].x * x[u].y + b[u].y * x[u].x;
-                }
+            for (int u = 0; u < 4; ++u) {
+                re += a[u].x * x[u].x - a[u].y * x[u].y;
+                im += a[u].x * x[u].y + a[u].y * x[u].x;
+                re2 += b[u].x * x[u].x - b[u].y * x[u].y;
+                im2 += b[u].x * x[u].y + b[u].y * x[u].x;
             }
         }
 #pragma unroll
@@ -502,6 +479,88 @@ __global__ void __launch_bounds__(256) k_vdots_h(const __half* __restrict__ Bh, 
                 partial[((size_t)(i + 8) * nrhs + r) * nblk + blk] = make_double2((double)(re2 * s2), (double)(im2 * s2));
             }
         }
+    }
+    griddep_launch();
+}
+
+// conj(v) w summed over an element pair: c the stored pairs (conj of t v)
+__device__ __forceinline__ void cmac2(uint2 c, float4 x, float& re, float& im)
+{
+    const float2 c0 = h2f(c.x), c1 = h2f(c.y);
+    re += c0.x * x.x - c0.y * x.y + c1.x * x.z - c1.y * x.w;
+    im += c0.x * x.y + c0.y * x.x + c1.x * x.w + c1.y * x.z;
+}
+
+// The coefficients on the FP16 basis for even N, a warp per 128 elements of
+// the CTA's chunk: a lane loads its two element pairs of W once (16-byte
+// loads) and then 8 basis vectors at a time (16 independent 8-byte loads, a
+// single round trip per group however short the basis).  The group's 16 sums
+// (8 vectors x Re, Im) go across the warp by a transposed butterfly: at each
+// level a lane keeps half its values and adds the partner's copy of them, 16
+// shuffles in all against 80 for 16 separate reductions.  The warps' sums
+// meet in shared memory and are added in warp order (fixed: reproducible).
+constexpr int VW_MAXV = 32;  // the separate-pass FP16 step takes restarts up to 32
+__global__ void __launch_bounds__(256) k_vdots_hw(const __half* __restrict__ Bh, size_t plane, size_t ldh,
+                                                  const float* __restrict__ inv_t, int nv,
+                                                  const float2* __restrict__ W, int n, int nrhs, int nblk,
+                                                  double2* __restrict__ partial, int* __restrict__ reset,
+                                                  const int* __restrict__ active)
+{
+    __shared__ float sp[8][2 * VW_MAXV];
+    const int blk = blockIdx.x, r = blockIdx.y;
+    griddep_wait();
+    if (reset && blk == 0 && r == 0 && threadIdx.x == 0) *reset = 0;
+    if (active && !active[r]) return;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int p1 = min(n, (blk + 1) * VCHUNK) >> 1;
+    const int q0 = ((blk * VCHUNK) >> 1) + warp * 64 + lane, q1 = q0 + 32;  // this lane's pairs
+    const bool in0 = q0 < p1, in1 = q1 < p1;
+    const float4* w4 = reinterpret_cast<const float4*>(W + (size_t)r * n);
+    const float4 x0 = in0 ? w4[q0] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 x1 = in1 ? w4[q1] : make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int g = 0; g < nv; g += 8) {
+        uint2 a[8][2];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const bool ok = g + u < nv;  // uniform across the warp
+            const uint2* row = reinterpret_cast<const uint2*>(hrow(Bh, plane, ldh, ok ? g + u : 0, r));
+            a[u][0] = ok && in0 ? row[q0] : make_uint2(0u, 0u);
+            a[u][1] = ok && in1 ? row[q1] : make_uint2(0u, 0u);
+        }
+        float v[16];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            float re = 0.f, im = 0.f;
+            cmac2(a[u][0], x0, re, im);
+            cmac2(a[u][1], x1, re, im);
+            v[2 * u] = re;
+            v[2 * u + 1] = im;
+        }
+        // after the levels 16, 8, 4, 2 lane L holds value (L >> 1) summed
+        // over the lanes that share bits 4..1 of L; level 1 adds the pair
+#pragma unroll
+        for (int h = 8, o = 16; h >= 1; h >>= 1, o >>= 1) {
+            const bool up = (lane & o) != 0;
+#pragma unroll
+            for (int t = 0; t < h; ++t) {
+                const float send = up ? v[t] : v[t + h];
+                const float keep = up ? v[t + h] : v[t];
+                v[t] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+            }
+        }
+        v[0] += __shfl_xor_sync(0xffffffffu, v[0], 1);
+        if ((lane & 1) == 0) sp[warp][2 * g + (lane >> 1)] = v[0];
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nv; i += blockDim.x) {
+        float re = 0.f, im = 0.f;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            re += sp[q][2 * i];
+            im += sp[q][2 * i + 1];
+        }
+        const float s = inv_t[(size_t)i * nrhs + r];  // a power of two: exact
+        partial[((size_t)i * nrhs + r) * nblk + blk] = make_double2((double)(re * s), (double)(im * s));
     }
     griddep_launch();
 }
@@ -981,7 +1040,9 @@ __global__ void k_arnoldi_finish_warp(GmresDev s, int j, const double2* __restri
 // A right-hand side that this step finds converged is normalised all the
 // same (its V_{j+1} lies past its basis length); one that was already
 // inactive writes nothing.  On the FP16 basis Vout is null: the packed rows
-// (plane j + 1 of the basis) are V_{j+1}.
+// (plane j + 1 of the basis) are V_{j+1}.  For even N the stream moves
+// element pairs, four 16-byte loads a thread issued before any store:
+// 0.70 -> 0.51 ms a job on the dense CFIE job (7680 x 360).
 constexpr int FP_CHUNK = 4096;
 
 __global__ void __launch_bounds__(256) k_finish_pack(GmresDev s, int j, const double2* __restrict__ pnorm, int nblk,
@@ -1026,13 +1087,45 @@ __global__ void __launch_bounds__(256) k_finish_pack(GmresDev s, int j, const do
         return;
     }
     const float sc = nscale[0], t = nscale[1];
+    const int k1 = min(n, (chunk + 1) * FP_CHUNK), off = column ? 32 : 0, nt = blockDim.x - off;
+    if (n % 2 == 0) {
+        // element pairs, PB of a thread's loads issued before any store (16
+        // bytes each): one round trip for a chunk instead of four
+        constexpr int PB = 4;
+        const float4* w4 = reinterpret_cast<const float4*>(W + (size_t)r * n);
+        float4* v4 = Vout ? reinterpret_cast<float4*>(Vout + (size_t)r * n) : nullptr;
+        uint2* g0 = pk.bh ? reinterpret_cast<uint2*>(pk.bh + (size_t)(2 * r) * pk.ldh) : nullptr;
+        uint2* g1 = pk.bh ? reinterpret_cast<uint2*>(pk.bh + (size_t)(2 * r + 1) * pk.ldh) : nullptr;
+        const int q1 = k1 >> 1;
+        for (int qb = ((chunk * FP_CHUNK) >> 1) + tid - off; qb < q1; qb += PB * nt) {
+            float4 x[PB];
+#pragma unroll
+            for (int u = 0; u < PB; ++u) {
+                const int q = qb + u * nt;
+                x[u] = q < q1 ? w4[q] : make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+#pragma unroll
+            for (int u = 0; u < PB; ++u) {
+                const int q = qb + u * nt;
+                if (q >= q1) continue;
+                const float4 y = make_float4(x[u].x * sc, x[u].y * sc, x[u].z * sc, x[u].w * sc);
+                if (v4) v4[q] = y;
+                if (g0) {
+                    const __half re0 = __float2half_rn(t * y.x), im0 = __float2half_rn(t * y.y);
+                    const __half re1 = __float2half_rn(t * y.z), im1 = __float2half_rn(t * y.w);
+                    g0[q] = make_uint2(h2u(__halves2half2(re0, __hneg(im0))), h2u(__halves2half2(re1, __hneg(im1))));
+                    g1[q] = make_uint2(h2u(__halves2half2(im0, re0)), h2u(__halves2half2(im1, re1)));
+                }
+            }
+        }
+        return;
+    }
     const float2* w = W + (size_t)r * n;
     float2* v = Vout ? Vout + (size_t)r * n : nullptr;
     __half2* h0 = pk.bh ? reinterpret_cast<__half2*>(pk.bh + (size_t)(2 * r) * pk.ldh) : nullptr;
     __half2* h1 = pk.bh ? reinterpret_cast<__half2*>(pk.bh + (size_t)(2 * r + 1) * pk.ldh) : nullptr;
-    const int k1 = min(n, (chunk + 1) * FP_CHUNK), off = column ? 32 : 0;
 #pragma unroll 4
-    for (int k = chunk * FP_CHUNK + tid - off; k < k1; k += blockDim.x - off) {
+    for (int k = chunk * FP_CHUNK + tid - off; k < k1; k += nt) {
         const float2 x = w[k];
         const float2 y = make_float2(x.x * sc, x.y * sc);
         if (v) v[k] = y;
@@ -1687,7 +1780,7 @@ static emfa_status_t gmres_t(Ctx* c, LinOp& A, const void* B, int nrhs, double2*
                     // be resident before its predecessor ends (griddep_wait); the
                     // coefficients pass zeroes the step's active count
                     if (hbasis) {
-                        EMFA_CUDA(c, launch_dependent(n % 2 ? k_vdots_h<false> : k_vdots_h<true>, vg, dim3(256), 0,
+                        EMFA_CUDA(c, launch_dependent(n % 2 ? k_vdots_h : k_vdots_hw, vg, dim3(256), 0,
                                                       st, (const __half*)Bh, hplane,
                                                       pk0.ldh, (const float*)inv_tb, nv, (const float2*)W, n, nrhs,
                                                       vblk, partial, s.step_cnt, (const int*)s.active));
