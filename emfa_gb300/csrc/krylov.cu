@@ -1623,10 +1623,14 @@ static emfa_status_t gmres_t(Ctx* c, LinOp& A, const void* B, int nrhs, double2*
     // k_finish_pack (column, normalisation and packing in one launch)
     const bool finish_pack = std::is_same<T, float>::value && !fused && !two_pass && m <= 32;
     // ... and keep the basis as the product's FP16 operand rows where the
-    // operator packs its input (unless basis = 1): m + 1 planes of the
-    // layout pack_target gives
+    // operator packs its input: m + 1 planes of the layout pack_target
+    // gives.  Auto takes it for even N, where the passes move element pairs;
+    // odd N runs them on single elements, slower than the FP32 basis (the
+    // single-element passes took 5.6 ms a job on the 7680 x 360 dense job,
+    // the FP32 basis's 4.6 ms)
     HPack pk0;
-    const bool hbasis = finish_pack && sp->basis != 1 && A.pack_target(c, nrhs, &pk0);
+    const bool hbasis = finish_pack && (sp->basis == 2 || (sp->basis == 0 && n % 2 == 0)) &&
+                        A.pack_target(c, nrhs, &pk0);
     const size_t hplane = hbasis ? pk0.ldh * 2 * (size_t)nrhs : 0;  // halves
     const size_t vslots = hbasis ? 1 : (size_t)(m + 1);
     // one workspace for the whole solve (reused across solves of a context)

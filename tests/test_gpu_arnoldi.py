@@ -196,3 +196,15 @@ def test_fp16_basis_only_where_the_product_packs(ctx, matvec, orth):
     X16, i16 = _solve(ctx, Z, B, orth, matvec, basis="f16")
     X32, i32 = _solve(ctx, Z, B, orth, matvec, basis="f32")
     assert i16.iterations == i32.iterations and torch.equal(X16, X32)
+
+
+@pytest.mark.parametrize("n,expect_f16", [(4000, True), (4001, False)])
+def test_auto_basis_by_parity_of_n(ctx, n, expect_f16):
+    """basis "auto" takes the FP16 basis for even N (element-pair passes) and
+    the FP32 basis for odd N (its passes would run on single elements):
+    bit-identical to the basis it picks."""
+    import torch
+    Z, B = _system(n, 200, seed=n)
+    Xa, ia = _solve(ctx, Z, B, "cgs1_split", "f16x", basis="auto")
+    Xp, ip = _solve(ctx, Z, B, "cgs1_split", "f16x", basis="f16" if expect_f16 else "f32")
+    assert ia.iterations == ip.iterations and torch.equal(Xa, Xp)
