@@ -423,65 +423,39 @@ __device__ __forceinline__ unsigned int h2u(__half2 h)
     return u;
 }
 
-// Odd N (single elements: 4-byte loads of the basis).  Even N takes
-// k_vdots_hw.  Measured on the dense CFIE job (7680 x 360, 50 launches):
-// this form 3.33 ms, latency-bound at 23 % of DRAM cycles (half the bytes
-// of the FP32 basis's loads in flight); lanes on element pairs 1.48 ms;
-// k_vdots_hw 1.14 ms; the FP32 basis 1.88 ms
-__global__ void __launch_bounds__(256) k_vdots_h(const __half* __restrict__ Bh, size_t plane, size_t ldh,
-                                                 const float* __restrict__ inv_t, int nv,
-                                                 const float2* __restrict__ W, int n, int nrhs, int nblk,
-                                                 double2* __restrict__ partial, int* __restrict__ reset,
-                                                 const int* __restrict__ active)
+// Element pairs of a length-n row of W (elements 2q, 2q + 1).  Rows start
+// 16-byte aligned for even n: one 16-byte access.  For odd n every other row
+// starts 8 bytes off and the last pair is half outside the row: two 8-byte
+// accesses, the second guarded (loads give 0 past the row).
+template <bool ODD>
+__device__ __forceinline__ float4 ld_wpair(const float2* w, int q, int n)
 {
-    const int blk = blockIdx.x, r = blockIdx.y;
-    griddep_wait();
-    if (reset && blk == 0 && r == 0 && threadIdx.x == 0) *reset = 0;
-    if (active && !active[r]) return;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const float2* w = W + (size_t)r * n;
-    const int k0 = blk * VCHUNK, k1 = min(n, k0 + VCHUNK);
-    for (int i = warp; i < nv; i += 16) {
-        const bool two = i + 8 < nv;
-        const __half2* va = hrow(Bh, plane, ldh, i, r);
-        const __half2* vb = hrow(Bh, plane, ldh, two ? i + 8 : i, r);
-        float re = 0.f, im = 0.f, re2 = 0.f, im2 = 0.f;
-        for (int k = k0 + lane; k < k1; k += 128) {
-            float2 a[4], b[4], x[4];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const int kk = k + 32 * u;
-                const bool in = kk < k1;
-                a[u] = in ? __half22float2(va[kk]) : make_float2(0.f, 0.f);
-                b[u] = in && two ? __half22float2(vb[kk]) : make_float2(0.f, 0.f);
-                x[u] = in ? w[kk] : make_float2(0.f, 0.f);
-            }
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                re += a[u].x * x[u].x - a[u].y * x[u].y;
-                im += a[u].x * x[u].y + a[u].y * x[u].x;
-                re2 += b[u].x * x[u].x - b[u].y * x[u].y;
-                im2 += b[u].x * x[u].y + b[u].y * x[u].x;
-            }
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            re += __shfl_xor_sync(0xffffffffu, re, o);
-            im += __shfl_xor_sync(0xffffffffu, im, o);
-            re2 += __shfl_xor_sync(0xffffffffu, re2, o);
-            im2 += __shfl_xor_sync(0xffffffffu, im2, o);
-        }
-        if (lane == 0) {
-            const float s = inv_t[(size_t)i * nrhs + r];  // a power of two: exact
-            partial[((size_t)i * nrhs + r) * nblk + blk] = make_double2((double)(re * s), (double)(im * s));
-            if (two) {
-                const float s2 = inv_t[(size_t)(i + 8) * nrhs + r];
-                partial[((size_t)(i + 8) * nrhs + r) * nblk + blk] = make_double2((double)(re2 * s2), (double)(im2 * s2));
-            }
-        }
-    }
-    griddep_launch();
+    if (!ODD) return reinterpret_cast<const float4*>(w)[q];
+    const float2 a = w[2 * q];
+    const float2 b = 2 * q + 1 < n ? w[2 * q + 1] : make_float2(0.f, 0.f);
+    return make_float4(a.x, a.y, b.x, b.y);
 }
+template <bool ODD>
+__device__ __forceinline__ void st_wpair(float2* w, int q, int n, float4 v)
+{
+    if (!ODD) {
+        reinterpret_cast<float4*>(w)[q] = v;
+        return;
+    }
+    w[2 * q] = make_float2(v.x, v.y);
+    if (2 * q + 1 < n) w[2 * q + 1] = make_float2(v.z, v.w);
+}
+// a basis row's stored pairs for elements 2q, 2q + 1 (rows are 16-byte
+// aligned and hold at least 2n + 2 halves for odd n); past the vector the
+// row's padding, which is zeroed here so that it cannot carry a NaN
+template <bool ODD>
+__device__ __forceinline__ uint2 ld_bpair(const __half2* row, int q, int n)
+{
+    uint2 v = reinterpret_cast<const uint2*>(row)[q];
+    if (ODD && 2 * q + 1 >= n) v.y = 0u;
+    return v;
+}
+
 
 // conj(v) w summed over an element pair: c the stored pairs (conj of t v)
 __device__ __forceinline__ void cmac2(uint2 c, float4 x, float& re, float& im)
@@ -491,15 +465,16 @@ __device__ __forceinline__ void cmac2(uint2 c, float4 x, float& re, float& im)
     im += c0.x * x.y + c0.y * x.x + c1.x * x.w + c1.y * x.z;
 }
 
-// The coefficients on the FP16 basis for even N, a warp per 128 elements of
-// the CTA's chunk: a lane loads its two element pairs of W once (16-byte
-// loads) and then 8 basis vectors at a time (16 independent 8-byte loads, a
+// The coefficients on the FP16 basis, a warp per 128 elements of the CTA's
+// chunk: a lane loads its two element pairs of W once (16-byte loads; for odd
+// N 8-byte ones) and then 8 basis vectors at a time (16 independent 8-byte loads, a
 // single round trip per group however short the basis).  The group's 16 sums
 // (8 vectors x Re, Im) go across the warp by a transposed butterfly: at each
 // level a lane keeps half its values and adds the partner's copy of them, 16
 // shuffles in all against 80 for 16 separate reductions.  The warps' sums
 // meet in shared memory and are added in warp order (fixed: reproducible).
 constexpr int VW_MAXV = 32;  // the separate-pass FP16 step takes restarts up to 32
+template <bool ODD>
 __global__ void __launch_bounds__(256) k_vdots_hw(const __half* __restrict__ Bh, size_t plane, size_t ldh,
                                                   const float* __restrict__ inv_t, int nv,
                                                   const float2* __restrict__ W, int n, int nrhs, int nblk,
@@ -512,20 +487,20 @@ __global__ void __launch_bounds__(256) k_vdots_hw(const __half* __restrict__ Bh,
     if (reset && blk == 0 && r == 0 && threadIdx.x == 0) *reset = 0;
     if (active && !active[r]) return;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int p1 = min(n, (blk + 1) * VCHUNK) >> 1;
+    const int p1 = (min(n, (blk + 1) * VCHUNK) + 1) >> 1;
     const int q0 = ((blk * VCHUNK) >> 1) + warp * 64 + lane, q1 = q0 + 32;  // this lane's pairs
     const bool in0 = q0 < p1, in1 = q1 < p1;
-    const float4* w4 = reinterpret_cast<const float4*>(W + (size_t)r * n);
-    const float4 x0 = in0 ? w4[q0] : make_float4(0.f, 0.f, 0.f, 0.f);
-    const float4 x1 = in1 ? w4[q1] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float2* w = W + (size_t)r * n;
+    const float4 x0 = in0 ? ld_wpair<ODD>(w, q0, n) : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 x1 = in1 ? ld_wpair<ODD>(w, q1, n) : make_float4(0.f, 0.f, 0.f, 0.f);
     for (int g = 0; g < nv; g += 8) {
         uint2 a[8][2];
 #pragma unroll
         for (int u = 0; u < 8; ++u) {
             const bool ok = g + u < nv;  // uniform across the warp
-            const uint2* row = reinterpret_cast<const uint2*>(hrow(Bh, plane, ldh, ok ? g + u : 0, r));
-            a[u][0] = ok && in0 ? row[q0] : make_uint2(0u, 0u);
-            a[u][1] = ok && in1 ? row[q1] : make_uint2(0u, 0u);
+            const __half2* row = hrow(Bh, plane, ldh, ok ? g + u : 0, r);
+            a[u][0] = ok && in0 ? ld_bpair<ODD>(row, q0, n) : make_uint2(0u, 0u);
+            a[u][1] = ok && in1 ? ld_bpair<ODD>(row, q1, n) : make_uint2(0u, 0u);
         }
         float v[16];
 #pragma unroll
@@ -568,11 +543,11 @@ __global__ void __launch_bounds__(256) k_vdots_hw(const __half* __restrict__ Bh,
 // W -= sum_i h_i v_i with |W|^2 and max |Re|, |Im| partials (k_vupdate<float,
 // true> on the FP16 basis): the coefficients are summed from the block
 // partials, block 0 stores them in h, and each is taken times inv_t once.
-// PAIR (even N): a thread holds two element pairs (16-byte W accesses) and
-// loads 4 basis vectors a group, 8 bytes each (40 registers, six CTAs an SM).
-// Measured on the dense CFIE job (7680 x 360): 11.10 ms a solve, against
-// 11.19 with single elements and 11.32 with 8 vectors a group
-template <bool PAIR>
+// A thread holds two element pairs of W (16-byte accesses; 8-byte ones for
+// odd N) and loads 4 basis vectors a group, 8 bytes each (40 registers, six
+// CTAs an SM).  Measured on the dense CFIE job (7680 x 360): 11.10 ms a
+// solve, against 11.19 with single elements and 11.32 with 8 vectors a group
+template <bool ODD>
 __global__ void __launch_bounds__(256) k_vupdate_h(const __half* __restrict__ Bh, size_t plane, size_t ldh,
                                                    const float* __restrict__ inv_t, int nv, double2* __restrict__ h,
                                                    const double2* __restrict__ partial, float2* __restrict__ W, int n,
@@ -582,7 +557,6 @@ __global__ void __launch_bounds__(256) k_vupdate_h(const __half* __restrict__ Bh
     const int blk = blockIdx.x, r = nrhs - 1 - (int)blockIdx.y;
     griddep_wait();
     if (active && !active[r]) return;
-    const size_t base = (size_t)r * n;
     extern __shared__ unsigned char dyn_smem[];
     float* hs0 = reinterpret_cast<float*>(dyn_smem);
     float* hs1 = hs0 + nv;
@@ -602,96 +576,53 @@ __global__ void __launch_bounds__(256) k_vupdate_h(const __half* __restrict__ Bh
     __syncthreads();
     float nr = 0.f, mx = 0.f;
     const int k0 = blk * VCHUNK, k1 = min(n, k0 + VCHUNK);
-    if (PAIR) {
-        constexpr int EP = VCHUNK / 512, VG = 4;
-        const int p0 = k0 >> 1, p1 = k1 >> 1;
-        float4* w4 = reinterpret_cast<float4*>(W + base);
-        int pc[EP];
-        float4 w[EP];
+    constexpr int EP = VCHUNK / 512, VG = 4;
+    const int p0 = k0 >> 1, p1 = (k1 + 1) >> 1;
+    float2* w2 = W + (size_t)r * n;
+    int pc[EP];
+    float4 w[EP];
 #pragma unroll
-        for (int e = 0; e < EP; ++e) {
-            pc[e] = min(p0 + (int)threadIdx.x + 256 * e, p1 - 1);
-            w[e] = w4[pc[e]];
-        }
-        float sr[EP][2], si[EP][2];
+    for (int e = 0; e < EP; ++e) {
+        pc[e] = min(p0 + (int)threadIdx.x + 256 * e, p1 - 1);
+        w[e] = ld_wpair<ODD>(w2, pc[e], n);
+    }
+    float sr[EP][2], si[EP][2];
 #pragma unroll
-        for (int e = 0; e < EP; ++e) sr[e][0] = sr[e][1] = si[e][0] = si[e][1] = 0.f;
-        for (int i = 0; i < nv; i += VG) {
-            uint2 v[VG][EP];
+    for (int e = 0; e < EP; ++e) sr[e][0] = sr[e][1] = si[e][0] = si[e][1] = 0.f;
+    for (int i = 0; i < nv; i += VG) {
+        uint2 v[VG][EP];
 #pragma unroll
-            for (int u = 0; u < VG; ++u) {
-                const uint2* vi = reinterpret_cast<const uint2*>(hrow(Bh, plane, ldh, min(i + u, nv - 1), r));
+        for (int u = 0; u < VG; ++u) {
+            const __half2* vi = hrow(Bh, plane, ldh, min(i + u, nv - 1), r);
 #pragma unroll
-                for (int e = 0; e < EP; ++e) v[u][e] = vi[pc[e]];
-            }
-#pragma unroll
-            for (int u = 0; u < VG; ++u) {
-                const bool ok = i + u < nv;
-                const float hr = ok ? hs0[i + u] : 0.f, hi = ok ? hs1[i + u] : 0.f;
-#pragma unroll
-                for (int e = 0; e < EP; ++e) {
-                    const float2 c0 = h2f(v[u][e].x), c1 = h2f(v[u][e].y);
-                    sr[e][0] += hr * c0.x + hi * c0.y;
-                    si[e][0] += hi * c0.x - hr * c0.y;
-                    sr[e][1] += hr * c1.x + hi * c1.y;
-                    si[e][1] += hi * c1.x - hr * c1.y;
-                }
-            }
+            for (int e = 0; e < EP; ++e) v[u][e] = ld_bpair<ODD>(vi, pc[e], n);
         }
 #pragma unroll
-        for (int e = 0; e < EP; ++e) {
-            const int p = p0 + (int)threadIdx.x + 256 * e;
-            if (p >= p1) continue;
-            w[e].x -= sr[e][0];
-            w[e].y -= si[e][0];
-            w[e].z -= sr[e][1];
-            w[e].w -= si[e][1];
-            w4[p] = w[e];
-            nr += w[e].x * w[e].x + w[e].y * w[e].y + w[e].z * w[e].z + w[e].w * w[e].w;
-            mx = fmaxf(mx, fmaxf(fmaxf(fabsf(w[e].x), fabsf(w[e].y)), fmaxf(fabsf(w[e].z), fabsf(w[e].w))));
-        }
-    } else {
-        constexpr int EL = VCHUNK / 256, VG = 4;
-        int kc[EL];
-        float2 w[EL];
+        for (int u = 0; u < VG; ++u) {
+            const bool ok = i + u < nv;
+            const float hr = ok ? hs0[i + u] : 0.f, hi = ok ? hs1[i + u] : 0.f;
 #pragma unroll
-        for (int e = 0; e < EL; ++e) {
-            kc[e] = min(k0 + (int)threadIdx.x + 256 * e, k1 - 1);
-            w[e] = W[base + kc[e]];
-        }
-        float sr[EL], si[EL];
-#pragma unroll
-        for (int e = 0; e < EL; ++e) sr[e] = si[e] = 0.f;
-        for (int i = 0; i < nv; i += VG) {
-            float2 v[VG][EL];
-#pragma unroll
-            for (int u = 0; u < VG; ++u) {
-                const __half2* vi = hrow(Bh, plane, ldh, min(i + u, nv - 1), r);
-#pragma unroll
-                for (int e = 0; e < EL; ++e) v[u][e] = __half22float2(vi[kc[e]]);
-            }
-#pragma unroll
-            for (int u = 0; u < VG; ++u) {
-                const bool ok = i + u < nv;
-                const float hr = ok ? hs0[i + u] : 0.f, hi = ok ? hs1[i + u] : 0.f;
-#pragma unroll
-                for (int e = 0; e < EL; ++e) {
-                    // h v with v = conj(c)
-                    sr[e] += hr * v[u][e].x + hi * v[u][e].y;
-                    si[e] += hi * v[u][e].x - hr * v[u][e].y;
-                }
+            for (int e = 0; e < EP; ++e) {
+                // h v with v = conj(c)
+                const float2 c0 = h2f(v[u][e].x), c1 = h2f(v[u][e].y);
+                sr[e][0] += hr * c0.x + hi * c0.y;
+                si[e][0] += hi * c0.x - hr * c0.y;
+                sr[e][1] += hr * c1.x + hi * c1.y;
+                si[e][1] += hi * c1.x - hr * c1.y;
             }
         }
+    }
 #pragma unroll
-        for (int e = 0; e < EL; ++e) {
-            const int k = k0 + (int)threadIdx.x + 256 * e;
-            if (k >= k1) continue;
-            w[e].x -= sr[e];
-            w[e].y -= si[e];
-            W[base + k] = w[e];
-            nr += w[e].x * w[e].x + w[e].y * w[e].y;
-            mx = fmaxf(mx, fmaxf(fabsf(w[e].x), fabsf(w[e].y)));
-        }
+    for (int e = 0; e < EP; ++e) {
+        const int p = p0 + (int)threadIdx.x + 256 * e;
+        if (p >= p1) continue;
+        w[e].x -= sr[e][0];
+        w[e].y -= si[e][0];
+        w[e].z -= sr[e][1];
+        w[e].w -= si[e][1];  // past the row (odd N): 0 - 0, not stored
+        st_wpair<ODD>(w2, p, n, w[e]);
+        nr += w[e].x * w[e].x + w[e].y * w[e].y + w[e].z * w[e].z + w[e].w * w[e].w;
+        mx = fmaxf(mx, fmaxf(fmaxf(fabsf(w[e].x), fabsf(w[e].y)), fmaxf(fabsf(w[e].z), fabsf(w[e].w))));
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -714,10 +645,10 @@ __global__ void __launch_bounds__(256) k_vupdate_h(const __half* __restrict__ Bh
     griddep_launch();
 }
 
-// X[r][k] += sum_i y_i v_i on the FP16 basis, the sum in FP32.  A thread
-// takes an element pair (PAIR, even N) or one element, four basis vectors a
-// group of loads
-template <bool PAIR>
+// X[r][k] += sum_i y_i v_i on the FP16 basis, the sum in FP32: a thread
+// takes an element pair (the second past the vector for odd N: computed from
+// the zeroed padding, not stored), four basis vectors a group of loads
+template <bool ODD>
 __global__ void k_update_x2_h(const __half* __restrict__ Bh, size_t plane, size_t ldh, const float* __restrict__ inv_t,
                               int nvmax, const double2* __restrict__ y, const int* __restrict__ jlen,
                               double2* __restrict__ X, int n, int nrhs)
@@ -734,39 +665,33 @@ __global__ void k_update_x2_h(const __half* __restrict__ Bh, size_t plane, size_
         ys1[i] = (float)t.y * s;
     }
     __syncthreads();
-    constexpr int NE = PAIR ? 2 : 1, VG = 4;
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;  // element (pair)
-    if (q * NE >= n) return;
-    float sr[NE], si[NE];
-#pragma unroll
-    for (int e = 0; e < NE; ++e) sr[e] = si[e] = 0.f;
+    constexpr int VG = 4;
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;  // element pair
+    if (2 * q >= n) return;
+    float sr[2] = {0.f, 0.f}, si[2] = {0.f, 0.f};
     for (int i = 0; i < jl; i += VG) {
-        float2 c[VG][NE];
+        float2 c[VG][2];
 #pragma unroll
         for (int u = 0; u < VG; ++u) {
-            const __half2* row = hrow(Bh, plane, ldh, min(i + u, jl - 1), r);
-            if (PAIR) {
-                const uint2 v = reinterpret_cast<const uint2*>(row)[q];
-                c[u][0] = h2f(v.x);
-                c[u][NE - 1] = h2f(v.y);
-            } else {
-                c[u][0] = __half22float2(row[q]);
-            }
+            const uint2 v = ld_bpair<ODD>(hrow(Bh, plane, ldh, min(i + u, jl - 1), r), q, n);
+            c[u][0] = h2f(v.x);
+            c[u][1] = h2f(v.y);
         }
 #pragma unroll
         for (int u = 0; u < VG; ++u) {
             const bool ok = i + u < jl;
             const float a = ok ? ys0[i + u] : 0.f, b = ok ? ys1[i + u] : 0.f;
 #pragma unroll
-            for (int e = 0; e < NE; ++e) {
+            for (int e = 0; e < 2; ++e) {
                 sr[e] += a * c[u][e].x + b * c[u][e].y;
                 si[e] += b * c[u][e].x - a * c[u][e].y;
             }
         }
     }
 #pragma unroll
-    for (int e = 0; e < NE; ++e) {
-        const size_t o = (size_t)r * n + (size_t)q * NE + e;
+    for (int e = 0; e < 2; ++e) {
+        if (ODD && 2 * q + e >= n) break;
+        const size_t o = (size_t)r * n + 2 * (size_t)q + e;
         const double2 x = X[o];
         X[o] = make_double2(x.x + (double)sr[e], x.y + (double)si[e]);
     }
@@ -1040,11 +965,12 @@ __global__ void k_arnoldi_finish_warp(GmresDev s, int j, const double2* __restri
 // A right-hand side that this step finds converged is normalised all the
 // same (its V_{j+1} lies past its basis length); one that was already
 // inactive writes nothing.  On the FP16 basis Vout is null: the packed rows
-// (plane j + 1 of the basis) are V_{j+1}.  For even N the stream moves
-// element pairs, four 16-byte loads a thread issued before any store:
-// 0.70 -> 0.51 ms a job on the dense CFIE job (7680 x 360).
+// (plane j + 1 of the basis) are V_{j+1}.  The stream moves element pairs,
+// four 16-byte loads a thread issued before any store: 0.70 -> 0.51 ms a
+// job on the dense CFIE job (7680 x 360).
 constexpr int FP_CHUNK = 4096;
 
+template <bool ODD>
 __global__ void __launch_bounds__(256) k_finish_pack(GmresDev s, int j, const double2* __restrict__ pnorm, int nblk,
                                                      const float2* __restrict__ W, int n, float2* __restrict__ Vout,
                                                      HPack pk)
@@ -1088,51 +1014,35 @@ __global__ void __launch_bounds__(256) k_finish_pack(GmresDev s, int j, const do
     }
     const float sc = nscale[0], t = nscale[1];
     const int k1 = min(n, (chunk + 1) * FP_CHUNK), off = column ? 32 : 0, nt = blockDim.x - off;
-    if (n % 2 == 0) {
-        // element pairs, PB of a thread's loads issued before any store (16
-        // bytes each): one round trip for a chunk instead of four
-        constexpr int PB = 4;
-        const float4* w4 = reinterpret_cast<const float4*>(W + (size_t)r * n);
-        float4* v4 = Vout ? reinterpret_cast<float4*>(Vout + (size_t)r * n) : nullptr;
-        uint2* g0 = pk.bh ? reinterpret_cast<uint2*>(pk.bh + (size_t)(2 * r) * pk.ldh) : nullptr;
-        uint2* g1 = pk.bh ? reinterpret_cast<uint2*>(pk.bh + (size_t)(2 * r + 1) * pk.ldh) : nullptr;
-        const int q1 = k1 >> 1;
-        for (int qb = ((chunk * FP_CHUNK) >> 1) + tid - off; qb < q1; qb += PB * nt) {
-            float4 x[PB];
-#pragma unroll
-            for (int u = 0; u < PB; ++u) {
-                const int q = qb + u * nt;
-                x[u] = q < q1 ? w4[q] : make_float4(0.f, 0.f, 0.f, 0.f);
-            }
-#pragma unroll
-            for (int u = 0; u < PB; ++u) {
-                const int q = qb + u * nt;
-                if (q >= q1) continue;
-                const float4 y = make_float4(x[u].x * sc, x[u].y * sc, x[u].z * sc, x[u].w * sc);
-                if (v4) v4[q] = y;
-                if (g0) {
-                    const __half re0 = __float2half_rn(t * y.x), im0 = __float2half_rn(t * y.y);
-                    const __half re1 = __float2half_rn(t * y.z), im1 = __float2half_rn(t * y.w);
-                    g0[q] = make_uint2(h2u(__halves2half2(re0, __hneg(im0))), h2u(__halves2half2(re1, __hneg(im1))));
-                    g1[q] = make_uint2(h2u(__halves2half2(im0, re0)), h2u(__halves2half2(im1, re1)));
-                }
-            }
-        }
-        return;
-    }
+    // element pairs, PB of a thread's loads issued before any store (16
+    // bytes each; two 8-byte loads for odd N): one round trip for a chunk
+    // instead of four.  Past the vector (odd N) the pair's second element is
+    // 0: V's is not stored, the rows' goes to their padding
+    constexpr int PB = 4;
     const float2* w = W + (size_t)r * n;
     float2* v = Vout ? Vout + (size_t)r * n : nullptr;
-    __half2* h0 = pk.bh ? reinterpret_cast<__half2*>(pk.bh + (size_t)(2 * r) * pk.ldh) : nullptr;
-    __half2* h1 = pk.bh ? reinterpret_cast<__half2*>(pk.bh + (size_t)(2 * r + 1) * pk.ldh) : nullptr;
-#pragma unroll 4
-    for (int k = chunk * FP_CHUNK + tid - off; k < k1; k += nt) {
-        const float2 x = w[k];
-        const float2 y = make_float2(x.x * sc, x.y * sc);
-        if (v) v[k] = y;
-        if (h0) {
-            const __half hre = __float2half_rn(t * y.x), him = __float2half_rn(t * y.y);
-            h0[k] = __halves2half2(hre, __hneg(him));
-            h1[k] = __halves2half2(him, hre);
+    uint2* g0 = pk.bh ? reinterpret_cast<uint2*>(pk.bh + (size_t)(2 * r) * pk.ldh) : nullptr;
+    uint2* g1 = pk.bh ? reinterpret_cast<uint2*>(pk.bh + (size_t)(2 * r + 1) * pk.ldh) : nullptr;
+    const int q1 = (k1 + 1) >> 1;
+    for (int qb = ((chunk * FP_CHUNK) >> 1) + tid - off; qb < q1; qb += PB * nt) {
+        float4 x[PB];
+#pragma unroll
+        for (int u = 0; u < PB; ++u) {
+            const int q = qb + u * nt;
+            x[u] = q < q1 ? ld_wpair<ODD>(w, q, n) : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+#pragma unroll
+        for (int u = 0; u < PB; ++u) {
+            const int q = qb + u * nt;
+            if (q >= q1) continue;
+            const float4 y = make_float4(x[u].x * sc, x[u].y * sc, x[u].z * sc, x[u].w * sc);
+            if (v) st_wpair<ODD>(v, q, n, y);
+            if (g0) {
+                const __half re0 = __float2half_rn(t * y.x), im0 = __float2half_rn(t * y.y);
+                const __half re1 = __float2half_rn(t * y.z), im1 = __float2half_rn(t * y.w);
+                g0[q] = make_uint2(h2u(__halves2half2(re0, __hneg(im0))), h2u(__halves2half2(re1, __hneg(im1))));
+                g1[q] = make_uint2(h2u(__halves2half2(im0, re0)), h2u(__halves2half2(im1, re1)));
+            }
         }
     }
 }
@@ -1623,14 +1533,10 @@ static emfa_status_t gmres_t(Ctx* c, LinOp& A, const void* B, int nrhs, double2*
     // k_finish_pack (column, normalisation and packing in one launch)
     const bool finish_pack = std::is_same<T, float>::value && !fused && !two_pass && m <= 32;
     // ... and keep the basis as the product's FP16 operand rows where the
-    // operator packs its input: m + 1 planes of the layout pack_target
-    // gives.  Auto takes it for even N, where the passes move element pairs;
-    // odd N runs them on single elements, slower than the FP32 basis (the
-    // single-element passes took 5.6 ms a job on the 7680 x 360 dense job,
-    // the FP32 basis's 4.6 ms)
+    // operator packs its input (unless basis = 1): m + 1 planes of the
+    // layout pack_target gives
     HPack pk0;
-    const bool hbasis = finish_pack && (sp->basis == 2 || (sp->basis == 0 && n % 2 == 0)) &&
-                        A.pack_target(c, nrhs, &pk0);
+    const bool hbasis = finish_pack && sp->basis != 1 && A.pack_target(c, nrhs, &pk0);
     const size_t hplane = hbasis ? pk0.ldh * 2 * (size_t)nrhs : 0;  // halves
     const size_t vslots = hbasis ? 1 : (size_t)(m + 1);
     // one workspace for the whole solve (reused across solves of a context)
@@ -1783,29 +1689,30 @@ static emfa_status_t gmres_t(Ctx* c, LinOp& A, const void* B, int nrhs, double2*
                     // product -> coefficients -> update -> finish: each launch may
                     // be resident before its predecessor ends (griddep_wait); the
                     // coefficients pass zeroes the step's active count
+                    // the pair kernels by the parity of N (odd N: 8-byte W accesses)
+                    const auto finish = n % 2 ? k_finish_pack<true> : k_finish_pack<false>;
+                    const dim3 fg((n + FP_CHUNK - 1) / FP_CHUNK, nrhs);
                     if (hbasis) {
-                        EMFA_CUDA(c, launch_dependent(n % 2 ? k_vdots_h : k_vdots_hw, vg, dim3(256), 0,
-                                                      st, (const __half*)Bh, hplane,
-                                                      pk0.ldh, (const float*)inv_tb, nv, (const float2*)W, n, nrhs,
-                                                      vblk, partial, s.step_cnt, (const int*)s.active));
-                        EMFA_CUDA(c, launch_dependent(n % 2 ? k_vupdate_h<false> : k_vupdate_h<true>, vg, dim3(256),
-                                                      2 * nv * sizeof(float), st,
+                        const auto dots = n % 2 ? k_vdots_hw<true> : k_vdots_hw<false>;
+                        const auto upd = n % 2 ? k_vupdate_h<true> : k_vupdate_h<false>;
+                        EMFA_CUDA(c, launch_dependent(dots, vg, dim3(256), 0, st, (const __half*)Bh, hplane, pk0.ldh,
+                                                      (const float*)inv_tb, nv, (const float2*)W, n, nrhs, vblk,
+                                                      partial, s.step_cnt, (const int*)s.active));
+                        EMFA_CUDA(c, launch_dependent(upd, vg, dim3(256), 2 * nv * sizeof(float), st,
                                                       (const __half*)Bh, hplane, pk0.ldh, (const float*)inv_tb, nv,
                                                       s.hcol, (const double2*)partial, (float2*)W, n, nrhs, vblk,
                                                       pnorm, (const int*)s.active));
-                        EMFA_CUDA(c, launch_dependent(k_finish_pack, dim3((n + FP_CHUNK - 1) / FP_CHUNK, nrhs),
-                                                      dim3(256), 0, st, s, j, (const double2*)pnorm, vblk,
+                        EMFA_CUDA(c, launch_dependent(finish, fg, dim3(256), 0, st, s, j, (const double2*)pnorm, vblk,
                                                       (const float2*)W, n, (float2*)nullptr, pk));
                     } else {
-                    EMFA_CUDA(c, launch_dependent(k_vdots<T>, vg, dim3(256), 0, st, (const Cx<T>*)V, vec, nv,
-                                                  (const Cx<T>*)W, n, nrhs, vblk, partial, s.step_cnt,
-                                                  (const int*)s.active));
-                    EMFA_CUDA(c, launch_dependent(k_vupdate<T, true>, vg, dim3(256), hsm, st, (const Cx<T>*)V, vec, nv,
-                                                  s.hcol, (const double2*)partial, W, n, nrhs, vblk, pnorm,
-                                                  (const int*)s.active));
-                    EMFA_CUDA(c, launch_dependent(k_finish_pack, dim3((n + FP_CHUNK - 1) / FP_CHUNK, nrhs), dim3(256),
-                                                  0, st, s, j, (const double2*)pnorm, vblk, (const float2*)W, n,
-                                                  (float2*)(V + (size_t)(j + 1) * vec), pk));
+                        EMFA_CUDA(c, launch_dependent(k_vdots<T>, vg, dim3(256), 0, st, (const Cx<T>*)V, vec, nv,
+                                                      (const Cx<T>*)W, n, nrhs, vblk, partial, s.step_cnt,
+                                                      (const int*)s.active));
+                        EMFA_CUDA(c, launch_dependent(k_vupdate<T, true>, vg, dim3(256), hsm, st, (const Cx<T>*)V, vec,
+                                                      nv, s.hcol, (const double2*)partial, W, n, nrhs, vblk, pnorm,
+                                                      (const int*)s.active));
+                        EMFA_CUDA(c, launch_dependent(finish, fg, dim3(256), 0, st, s, j, (const double2*)pnorm, vblk,
+                                                      (const float2*)W, n, (float2*)(V + (size_t)(j + 1) * vec), pk));
                     }
                     c->kernel_launches += 3;
                 } else {
@@ -1859,11 +1766,9 @@ static emfa_status_t gmres_t(Ctx* c, LinOp& A, const void* B, int nrhs, double2*
             k_backsolve_f32<<<(nrhs + BS_WARPS - 1) / BS_WARPS, 32 * BS_WARPS, 0, st>>>(s);
         else
             k_backsolve<<<(nrhs * 32 + 127) / 128, 128, 0, st>>>(s);
-        if (hbasis && n % 2 == 0)
-            k_update_x2_h<true><<<dim3((n / 2 + 255) / 256, nrhs), 256, 2 * std::max(1, steps) * sizeof(float), st>>>(
-                Bh, hplane, pk0.ldh, inv_tb, steps, s.y, s.jlen, X, n, nrhs);
-        else if (hbasis)
-            k_update_x2_h<false><<<dim3((n + 255) / 256, nrhs), 256, 2 * std::max(1, steps) * sizeof(float), st>>>(
+        if (hbasis)
+            (n % 2 ? k_update_x2_h<true> : k_update_x2_h<false>)<<<dim3(((n + 1) / 2 + 255) / 256, nrhs), 256,
+                                                                    2 * std::max(1, steps) * sizeof(float), st>>>(
                 Bh, hplane, pk0.ldh, inv_tb, steps, s.y, s.jlen, X, n, nrhs);
         else
             k_update_x2<T><<<dim3((n + 255) / 256, nrhs), 256,

@@ -112,9 +112,8 @@ typedef struct {
                         /* < 0 = iterate to the target                             */
     int basis;          /* GMRES basis storage of the EMFA_F32 inner solve: 0 =    */
                         /* auto (FP16 where the Gram-Schmidt passes run separately */
-                        /* and the product packs its operand to FP16, for even N;  */
-                        /* else FP32), 1 = FP32, 2 = FP16 where possible (odd N    */
-                        /* too: single-element passes).  The FP16 basis is         */
+                        /* and the product packs its operand to FP16, else FP32),  */
+                        /* 1 = FP32, 2 = FP16 where possible.  The FP16 basis is   */
                         /* the product's own operand (each vector scaled by a      */
                         /* power of two), so the orthogonalisation sees the        */
                         /* vectors the product multiplied, at half the bytes       */
