@@ -7,10 +7,26 @@
 #include "emfa_internal.cuh"
 #include "emfa_math.cuh"
 
+#include <type_traits>
+
 namespace emfa {
 
-template <typename T>
-__global__ void __launch_bounds__(256) k_rcs(const RwgPack<T>* __restrict__ rw, const T* __restrict__ q7, int n,
+// s + x with the rounding error carried in c (Kahan), FP32
+__device__ __forceinline__ void kahan_add(float& s, float& c, float x)
+{
+    const float y = x - c;
+    const float t = s + y;
+    c = (t - s) - y;
+    s = t;
+}
+
+// NT threads: 512 for FP32, three CTAs an SM at 40 registers.  The (RHS,
+// direction) grid is often one CTA an incidence (monostatic: 360 CTAs on the
+// dense CFIE job), so wider CTAs keep more warps an SM on the point loop:
+// 160 -> 146 us there (ncu).  The FP64 path keeps 256 (at three CTAs of 512
+// it would spill).
+template <typename T, int NT>
+__global__ void __launch_bounds__(NT, NT == 512 ? 3 : 1) k_rcs(const RwgPack<T>* __restrict__ rw, const T* __restrict__ q7, int n,
                                              const double2* __restrict__ I, const T* __restrict__ dirs, int n_dir,
                                              int per_rhs, T k, T kpi, double z0, double* __restrict__ out)
 {
@@ -18,6 +34,15 @@ __global__ void __launch_bounds__(256) k_rcs(const RwgPack<T>* __restrict__ rw, 
     const T* dp = dirs + 3 * ((size_t)(per_rhs ? a * n_dir : 0) + d);
     V3<T> ks = v3(dp[0], dp[1], dp[2]);
     double acc[6] = {0, 0, 0, 0, 0, 0};
+    // FP32 geometry: each RWG's term I l E_u in FP32 and a thread's terms
+    // summed with compensation, converted to FP64 once per thread (per-RWG
+    // FP64 products and conversions ran on GB300's 1/64-rate FP64 pipe:
+    // 215 -> 160 us on the dense CFIE job's 360 monostatic directions); the
+    // current's FP64 components rounded to FP32 by integer operations.  A
+    // numpy model of both sums over the 1,920-RWG sphere's 541 bistatic
+    // directions differs by at most 2.5e-7 dB
+    float ks32[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, kc32[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    constexpr bool F32 = std::is_same<T, float>::value;
     for (int u = threadIdx.x; u < n; u += blockDim.x) {
         const RwgPack<T>& R = rw[u];
         T ex[3] = {0, 0, 0}, ey[3] = {0, 0, 0};  // re / im of sum w rho e^{j..}
@@ -37,14 +62,27 @@ __global__ void __launch_bounds__(256) k_rcs(const RwgPack<T>* __restrict__ rw, 
             }
         }
         double2 iu = I[(size_t)a * n + u];
-        double ir = iu.x * (double)R.len, ii = iu.y * (double)R.len;
+        if constexpr (F32) {
+            const float ir = split_f64(iu.x).x * R.len, ii = split_f64(iu.y).x * R.len;
 #pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            acc[2 * c] += (double)ex[c] * ir - (double)ey[c] * ii;
-            acc[2 * c + 1] += (double)ex[c] * ii + (double)ey[c] * ir;
+            for (int c = 0; c < 3; ++c) {
+                kahan_add(ks32[2 * c], kc32[2 * c], fmaf(ex[c], ir, -(ey[c] * ii)));
+                kahan_add(ks32[2 * c + 1], kc32[2 * c + 1], fmaf(ex[c], ii, ey[c] * ir));
+            }
+        } else {
+            double ir = iu.x * (double)R.len, ii = iu.y * (double)R.len;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                acc[2 * c] += (double)ex[c] * ir - (double)ey[c] * ii;
+                acc[2 * c + 1] += (double)ex[c] * ii + (double)ey[c] * ir;
+            }
         }
     }
-    __shared__ double red[6][256];
+    if constexpr (F32) {
+#pragma unroll
+        for (int c = 0; c < 6; ++c) acc[c] = (double)ks32[c] - (double)kc32[c];
+    }
+    __shared__ double red[6][NT];
     for (int c = 0; c < 6; ++c) red[c][threadIdx.x] = acc[c];
     __syncthreads();
     for (int w = blockDim.x / 2; w > 0; w >>= 1) {
@@ -83,7 +121,8 @@ static emfa_status_t rcs_t(Ctx* c, Geom* g, GeomDev<T>& gd, const emfa_fill_para
     EMFA_CUDA(c, cudaMemcpyAsync(dd.ptr, dh.data(), dd.bytes, cudaMemcpyHostToDevice, st));
     T k = Phys<T>::wavenumber(p->freq);
     dim3 grd(n_dir, n_rhs);
-    k_rcs<T><<<grd, 256, 0, st>>>(dptr<RwgPack<T>>(gd.rwg), dptr<T>(gd.tri_q7), g->n, (const double2*)I,
+    constexpr int NT = std::is_same<T, float>::value ? 512 : 256;
+    k_rcs<T, NT><<<grd, NT, 0, st>>>(dptr<RwgPack<T>>(gd.rwg), dptr<T>(gd.tri_q7), g->n, (const double2*)I,
                                   dptr<T>(dd), n_dir, per_rhs, k, k / Phys<T>::pi(), (double)Phys<T>::z0(),
                                   dptr<double>(od));
     c->kernel_launches += 1;
