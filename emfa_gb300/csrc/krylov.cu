@@ -1510,9 +1510,13 @@ static emfa_status_t gmres_t(Ctx* c, LinOp& A, const void* B, int nrhs, double2*
     const int n = A.n, prec = A.prec;
     const int m = std::max(1, std::min(sp->restart > 0 ? sp->restart : 30, MAX_RESTART));
     const size_t vec = (size_t)n * nrhs;
-    // vector-pass grid: ~2 CTAs per SM over (chunks of N) x (right-hand sides)
+    // residual-norm grid: at least ~2 CTAs per SM over (chunks of N) x
+    // (right-hand sides), chunks of at most 2048 elements (with one CTA a
+    // right-hand side, 360 of them streamed 123 KB each: 23 us a launch on
+    // the dense CFIE job), and at least 4 elements a thread (1024 a CTA)
     const int sms = c->sm_count > 0 ? c->sm_count : 148;
-    const int nblk = std::max(1, std::min((2 * sms + nrhs - 1) / nrhs, (n + 4 * KB - 1) / (4 * KB)));
+    const int nblk = std::max(1, std::min(std::max((2 * sms + nrhs - 1) / nrhs, (n + 2047) / 2048),
+                                          (n + 4 * KB - 1) / (4 * KB)));
     const int chunk = (n + nblk - 1) / nblk;
     const int vblk = (n + VCHUNK - 1) / VCHUNK;  // chunks of the Gram-Schmidt passes
     // the FP32 inner solve of the refinement only has to gain a few digits per
